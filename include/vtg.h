@@ -1,0 +1,134 @@
+/* vtg.h -- the C ABI of libvtg: the sparse pyramidal Lucas-Kanade path of Lasimeri/Intel-Phi-VisionTrack on one GB300
+ * (sm_103a), for C host code.
+ *
+ * Plain C types only: pointers, sizes, ints and floats. CUDA streams are passed as `void *` (a cudaStream_t, or NULL for
+ * the library's own stream of the context). Every entry point returns an int status (VTG_OK = 0, negative on error);
+ * none traps, and no device wait is unbounded.
+ *
+ * Reference interfaces each entry point replaces are cited as path:line inside the reference tree. */
+#ifndef VTG_H
+#define VTG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VTG_MAX_LEVELS 6 /* VT_MAX_LEVELS, src/common/vt_proto.h:59 */
+#define VTG_MAX_PATCH_W 29
+#define VTG_MAX_PATCH_H 31 /* LK_MAX_H, src/kern/lk.h:19 */
+
+/* Status codes. */
+enum {
+    VTG_OK = 0,
+    VTG_EINVAL = -1,   /* an argument or configuration out of range */
+    VTG_ENOMEM = -2,   /* device or host allocation failed */
+    VTG_ECUDA = -3,    /* a CUDA call failed (vtg_last_cuda_error gives its code) */
+    VTG_ETIMEOUT = -4, /* a bounded device wait gave up */
+    VTG_EBUSY = -5,    /* the object is in use by work not yet finished */
+    VTG_ENODEV = -6,   /* no usable CUDA device */
+    VTG_EBUDGET = -7   /* the request does not fit the context's device-memory budget */
+};
+
+/* Where a buffer lives. */
+enum { VTG_HOST = 0, VTG_DEVICE = 1 };
+
+/* LK status bits: enum in src/kern/lk.h:22, bit for bit. */
+enum { VTG_LK_OK = 0, VTG_LK_OUT = 1, VTG_LK_LOWEIG = 2, VTG_LK_RESIDUAL = 4, VTG_LK_FLOWBACK = 8 };
+
+/* One tracked point: struct lk_out (src/kern/lk.h:33-40), byte for byte (32 bytes). */
+struct vtg_lk_out {
+    float x, y;         /* the estimate at level 0 */
+    float min_eig;      /* smaller eigenvalue of the structure tensor per patch pixel, at level 0 */
+    float residual;     /* mean |T - J|, 8-bit grey */
+    float cov_xx, cov_xy, cov_yy;
+    uint16_t iters;     /* summed over levels */
+    uint16_t status;    /* VTG_LK_* bits */
+};
+
+/* One cell of the per-cell flow grid: struct vt_cell (src/common/vt_proto.h:395-402), byte for byte (24 bytes). */
+struct vtg_cell {
+    float u, v;     /* flow, pixels of the cells' level */
+    float diff;     /* mean |J - I| over the cell, 8-bit grey */
+    uint32_t state; /* LK status bits in the low byte */
+    float sigma;    /* sqrt(cov_xx + cov_yy) when the status is 0 */
+    float pad;
+};
+
+/* A stream's configuration: the LK fields of struct vt_config (src/common/vt_proto.h:67-127) plus the cell grid
+ * (VT_CELL_W / VT_CELL_H, vt_proto.h:385-386) and the level it lives on (flow_level, vt_proto.h:115). */
+struct vtg_config {
+    uint32_t width, height; /* level 0, pixels; any size >= 32 x 32 */
+    uint32_t levels;        /* pyramid levels, 1 .. VTG_MAX_LEVELS */
+    uint32_t patch_w, patch_h; /* odd, 5 .. VTG_MAX_PATCH_W / VTG_MAX_PATCH_H */
+    uint32_t max_iter;
+    float eps;          /* stop when a step is below this, pixels of the level */
+    float min_eig;      /* per patch pixel, 8-bit grey per pixel */
+    float max_residual; /* mean |T - J| in 8-bit grey */
+    float fb_max;       /* forward-backward miss, pixels; 0 = no check */
+    uint32_t cell_w, cell_h; /* the cell grid, pixels of flow_level */
+    uint32_t flow_level;     /* the pyramid level the cells live on */
+};
+
+typedef struct vtg_ctx vtg_ctx;
+typedef struct vtg_tracker vtg_tracker;
+
+/* ---- library and context ---- */
+
+const char *vtg_strerror(int status);
+/* The last CUDA error code a VTG_ECUDA came from, in this thread. */
+int vtg_last_cuda_error(void);
+/* A context on CUDA device `device`, holding at most `hbm_budget` bytes of device memory for its trackers (0 = no limit
+ * beyond the device's own). */
+int vtg_ctx_create(int device, size_t hbm_budget, vtg_ctx **out);
+void vtg_ctx_destroy(vtg_ctx *ctx);
+/* Bytes of the budget in use. */
+size_t vtg_ctx_used(const vtg_ctx *ctx);
+/* Waits for all of the context's work, at most timeout_ms (VTG_ETIMEOUT after that). */
+int vtg_ctx_sync(vtg_ctx *ctx, int timeout_ms);
+
+/* ---- a tracker: one camera stream's device-resident state (tk_create, src/kern/track.h:22 / track.c:447-572) ---- */
+
+/* Device bytes one tracker of this configuration holds: two pyramid sets, a frame staging buffer, the cell results. */
+size_t vtg_tracker_bytes(const struct vtg_config *cfg);
+int vtg_tracker_create(vtg_ctx *ctx, const struct vtg_config *cfg, vtg_tracker **out);
+void vtg_tracker_destroy(vtg_tracker *t);
+/* Pyramid sets (tk_sets, src/kern/track.h:26): frame k goes to set k mod this. */
+int vtg_tracker_sets(const vtg_tracker *t);
+/* Cells of the grid: ceil(w_f / cell_w) x ceil(h_f / cell_h) at the flow level's size w_f x h_f. */
+int vtg_tracker_cells(const vtg_tracker *t, int *cols, int *rows);
+/* The tracker's stream (a cudaStream_t) -- work of one tracker is ordered on it. */
+void *vtg_tracker_stream(const vtg_tracker *t);
+
+/* ---- the hot path ---- */
+
+/* The pyramid of one 8-bit frame into set `set` (tk_build, src/kern/track.c:584-629: img_u8_to_q6 + img_reduce per
+ * level, src/kern/img_ref.c:32-40 / 98-114). Levels hold the reference's Q6 values (byte x 64, then the 5 x 5 binomial
+ * with (h + 128) >> 8) bit for bit. frame: height rows of width bytes, `stride` bytes apart, in host (pinned or
+ * pageable) or device memory as `where` says. Asynchronous on `stream` (NULL: the tracker's). */
+int vtg_build(vtg_tracker *t, int set, const uint8_t *frame, int stride, int where, void *stream);
+
+/* Per-cell flow from set `prev` to set `cur` (still_vectors, src/kern/still.c:116-141, with the tracker's LK settings):
+ * one LK vector per cell centre, the forward-backward check when fb_max > 0, and the cell record. `cells` (may be
+ * NULL) receives cols x rows struct vtg_cell, `lk` (may be NULL) the struct vtg_lk_out of each cell, both row-major, in
+ * host or device memory as `where` says. Host results are complete when the stream is. */
+int vtg_cells(vtg_tracker *t, int prev, int cur, struct vtg_cell *cells, struct vtg_lk_out *lk, int where, void *stream);
+
+/* LK for a list of points from set `prev` to set `cur` (OP_LK, src/kern/track.c:275-292: lk_track + lk_flowback,
+ * src/kern/lk.h:46-53): n points (xs, ys) in level-0 pixels, each with its own guess (gx, gy may be NULL: no guess);
+ * `top` the first level (-1: the tracker's top). Arrays in host or device memory as `where` says. */
+int vtg_points(vtg_tracker *t, int prev, int cur, int top, int n, const float *xs, const float *ys, const float *gx,
+               const float *gy, struct vtg_lk_out *out, int where, void *stream);
+
+/* Copies one level of a set out (tk_level, src/kern/track.h:61): h_L rows of w_L floats, Q6. */
+int vtg_level(vtg_tracker *t, int set, int level, float *out, int where, void *stream);
+/* A level's size. */
+int vtg_level_size(const vtg_tracker *t, int level, int *w, int *h);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

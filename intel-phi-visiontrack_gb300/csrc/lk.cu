@@ -1,0 +1,368 @@
+/* lk.cu -- sparse pyramidal Lucas-Kanade, one warp per point, and the per-cell grid driver.
+ *
+ * Reference: lk_track / lk_flowback (src/kern/lk.h:46-53): the driver of src/kern/lk_driver.inc:7-121 around three patch
+ * operations, build (src/kern/lk_vx.c:36-97), iterate (lk_vx.c:100-140) and residual (lk_vx.c:142-175); the per-cell
+ * grid of still_vectors (src/kern/still.c:116-141); the tracker's point list OP_LK (src/kern/track.c:275-292).
+ *
+ * Mapping. A warp owns one point. Lane c holds patch column c - 1 (c = 1 .. W are the patch; lane 0 and lanes past W
+ * hold the window's border columns or nothing, with zero gradients, so they add exactly nothing to any sum). A lane
+ * walks the patch's rows, carrying the previous row's horizontally interpolated value, so one J load per lane per row
+ * serves the bilinear sample (the right neighbour comes from the next lane by shuffle). The template T, Tx, Ty of the
+ * current level lives in registers (3 x H floats a lane) from its build to its last iteration. Sums are per-lane FMA
+ * chains folded across the warp by a butterfly of xor shuffles, so every lane ends with the same bits and the driver
+ * runs warp-uniform, without divergence. Arithmetic follows the reference's lane model: lerps as fma(n - l, f, l),
+ * Sobel as fma(2 dm, 2, du + dd) x 1/512, accumulation by fused multiply-add. This file is built with -fmad=false:
+ * every fused operation is written out.
+ *
+ * The driver is F32 where the reference's is long double. A position is kept as a whole pixel plus a small float
+ * offset from it (the sub-pixel phase of the level's start plus the flow so far), so the bilinear phase keeps ~1e-6 px
+ * of precision at any picture size; the determinant is formed by Kahan's fused-multiply-add product difference, and the
+ * smaller eigenvalue as det / lambda_max, so neither cancels. No FP64 anywhere. */
+#include "vtg_internal.cuh"
+
+#define LK_GRAD_SCALE (1.0f / 512.0f)
+#define LK_Q6_INV (1.0f / 64.0f)
+
+template <int MAXH>
+struct Patch {
+    float t[MAXH], tx[MAXH], ty[MAXH];
+};
+
+__device__ __forceinline__ float warp_fold(float v)
+{
+#pragma unroll
+    for (int s = 1; s < 32; s <<= 1)
+        v = v + __shfl_xor_sync(VTG_FULL, v, s);
+    return v;
+}
+
+/* The row's horizontal interpolation at this lane's column: l from this lane's load, n from the next lane's. */
+__device__ __forceinline__ float hlerp(const float *p, bool ld, float fx)
+{
+    const float l = ld ? __ldg(p) : 0.0f;
+    const float n = __shfl_down_sync(VTG_FULL, l, 1);
+    return __fmaf_rn(n - l, fx, l);
+}
+
+/* build: the window of I around pixel (ix + fx, iy + fy); T, Tx, Ty into the registers; the tensor's sums. */
+template <int MAXH>
+__device__ __forceinline__ void lk_build(const DevLevel &L, int ix, float fx, int iy, float fy, int W, int H, int lane,
+                                         Patch<MAXH> &P, float &gxx, float &gxy, float &gyy)
+{
+    const int x0 = ix - W / 2, y0 = iy - H / 2;
+    /* Lane c samples window column c - 1: loads for c <= W + 2 (lane W + 2 only feeds lane W + 1's right neighbour). */
+    const bool ld = lane <= W + 2;
+    const bool act = lane >= 1 && lane <= W;
+    const float *row = L.p + (size_t)(y0 - 1) * L.pitch + (x0 - 1 + lane);
+    float prev = hlerp(row, ld, fx);
+    float u = 0.f, ul = 0.f, ur = 0.f, m = 0.f, ml = 0.f, mr = 0.f, d = 0.f, dl = 0.f, dr = 0.f;
+    float sxx = 0.f, sxy = 0.f, syy = 0.f;
+#pragma unroll
+    for (int r = 0; r < MAXH + 2; r++) {
+        if (r < H + 2) {
+            row += L.pitch;
+            const float cur = hlerp(row, ld, fx);
+            const float S = __fmaf_rn(cur - prev, fy, prev);
+            prev = cur;
+            const float Sl = __shfl_up_sync(VTG_FULL, S, 1), Sr = __shfl_down_sync(VTG_FULL, S, 1);
+            u = m; ul = ml; ur = mr;
+            m = d; ml = dl; mr = dr;
+            d = S; dl = Sl; dr = Sr;
+            if (r >= 2) {
+                const float dxu = ur - ul, dxm = mr - ml, dxd = dr - dl;
+                float tx = __fmaf_rn(dxm, 2.0f, dxu + dxd) * LK_GRAD_SCALE;
+                const float dyl = dl - ul, dyc = d - u, dyr = dr - ur;
+                float ty = __fmaf_rn(dyc, 2.0f, dyl + dyr) * LK_GRAD_SCALE;
+                tx = act ? tx : 0.0f;
+                ty = act ? ty : 0.0f;
+                P.t[r - 2] = m;
+                P.tx[r - 2] = tx;
+                P.ty[r - 2] = ty;
+                sxx = __fmaf_rn(tx, tx, sxx);
+                sxy = __fmaf_rn(tx, ty, sxy);
+                syy = __fmaf_rn(ty, ty, syy);
+            }
+        }
+    }
+    gxx = warp_fold(sxx);
+    gxy = warp_fold(sxy);
+    gyy = warp_fold(syy);
+}
+
+/* iterate (RESID = false): J at pixel (jx + fx, jy + fy); the sums of It Tx and It Ty.
+ * residual (RESID = true): the sums of |It| and It^2, It in 8-bit grey. */
+template <int MAXH, bool RESID>
+__device__ __forceinline__ void lk_sample(const DevLevel &L, int jx, float fx, int jy, float fy, int W, int H, int lane,
+                                          const Patch<MAXH> &P, float &b0, float &b1)
+{
+    const int x0 = jx - W / 2, y0 = jy - H / 2;
+    const bool ld = lane <= W + 1;
+    const bool act = lane >= 1 && lane <= W;
+    const float *row = L.p + (size_t)y0 * L.pitch + (x0 - 1 + lane);
+    float prev = hlerp(row, ld, fx);
+    float s0 = 0.f, s1 = 0.f;
+#pragma unroll
+    for (int r = 0; r < MAXH; r++) {
+        if (r < H) {
+            row += L.pitch;
+            const float cur = hlerp(row, ld, fx);
+            const float it = P.t[r] - __fmaf_rn(cur - prev, fy, prev);
+            prev = cur;
+            if (RESID) {
+                const float g = act ? it * LK_Q6_INV : 0.0f;
+                s0 = s0 + fabsf(g);
+                s1 = __fmaf_rn(g, g, s1);
+            } else {
+                s0 = __fmaf_rn(it, P.tx[r], s0);
+                s1 = __fmaf_rn(it, P.ty[r], s1);
+            }
+        }
+    }
+    b0 = warp_fold(s0);
+    b1 = warp_fold(s1);
+}
+
+/* A position as whole pixel + offset: floor and phase of base + t, base a whole number. */
+__device__ __forceinline__ void split(int base, float t, int &i, float &f)
+{
+    const float ft = floorf(t);
+    i = base + (int)ft;
+    f = t - ft;
+}
+
+/* The pyramid walk (src/kern/lk_driver.inc:7-109), warp-uniform, F32. */
+template <int MAXH>
+__device__ void lk_track(const DevPyr &I, const DevPyr &J, int top, const LkPrm &p, float x, float y, float gx0,
+                         float gy0, int lane, Patch<MAXH> &P, vtg_lk_out &o)
+{
+    const int W = p.W, H = p.H;
+    const int mx = W / 2 + 1, my = H / 2 + 1;
+    float gx = ldexpf(gx0, -top), gy = ldexpf(gy0, -top);
+    int status = 0, iters = 0;
+    bool valid0 = false;
+    float eig0 = 0.0f, det0 = 1.0f, gxx0 = 0.0f, gxy0 = 0.0f, gyy0 = 0.0f;
+    for (int L = top; L >= 0; L--) {
+        const DevLevel IL = I.l[L], JL = J.l[L];
+        const float px = ldexpf(x, -L), py = ldexpf(y, -L); /* exact */
+        if (px < (float)mx || py < (float)my || px >= (float)(IL.w - mx - 1) || py >= (float)(IL.h - my - 1)) {
+            if (L == 0)
+                status |= VTG_LK_OUT;
+            else {
+                gx *= 2.0f;
+                gy *= 2.0f;
+            }
+            continue;
+        }
+        const float fpx = floorf(px), fpy = floorf(py);
+        const int bx = (int)fpx, by = (int)fpy;
+        const float rx = px - fpx, ry = py - fpy; /* exact */
+        float gxx, gxy, gyy;
+        lk_build<MAXH>(IL, bx, rx, by, ry, W, H, lane, P, gxx, gxy, gyy);
+        /* det = gxx gyy - gxy^2 by Kahan's product difference; the smaller eigenvalue as det / lambda_max. */
+        const float w2 = gxy * gxy;
+        const float e2 = __fmaf_rn(gxy, gxy, -w2);
+        const float det = __fmaf_rn(gxx, gyy, -w2) - e2;
+        const float tr = gxx + gyy, df = gxx - gyy;
+        const float root = sqrtf(__fmaf_rn(df, df, 4.0f * w2));
+        const float lmax = 0.5f * (tr + root);
+        const float eig = lmax > 0.0f ? (det / lmax) / p.area : 0.0f;
+        if (L == 0)
+            eig0 = eig;
+        if (eig < p.min_eig || det <= 0.0f) {
+            if (L == 0)
+                status |= VTG_LK_LOWEIG;
+            else {
+                gx *= 2.0f;
+                gy *= 2.0f;
+            }
+            continue;
+        }
+        if (L == 0) {
+            det0 = det;
+            gxx0 = gxx;
+            gxy0 = gxy;
+            gyy0 = gyy;
+            valid0 = true;
+        }
+        const float ia = gyy / det, ib = -gxy / det, ic = gxx / det;
+        const float lo_x = (float)(mx - bx), lo_y = (float)(my - by);
+        const float hi_x = (float)(JL.w - mx - 1 - bx), hi_y = (float)(JL.h - my - 1 - by);
+        float vx = 0.0f, vy = 0.0f;
+        for (int it = 0; it < p.max_iter; it++) {
+            const float qx = (rx + gx) + vx, qy = (ry + gy) + vy; /* offsets from (bx, by) */
+            if (qx < lo_x || qy < lo_y || qx >= hi_x || qy >= hi_y) {
+                if (L == 0) {
+                    status |= VTG_LK_OUT;
+                    valid0 = false;
+                }
+                break;
+            }
+            int jx, jy;
+            float fx, fy;
+            split(bx, qx, jx, fx);
+            split(by, qy, jy, fy);
+            float sx, sy;
+            lk_sample<MAXH, false>(JL, jx, fx, jy, fy, W, H, lane, P, sx, sy);
+            const float bxx = sx * LK_Q6_INV, byy = sy * LK_Q6_INV;
+            const float ex = __fmaf_rn(ia, bxx, ib * byy), ey = __fmaf_rn(ib, bxx, ic * byy);
+            vx += ex;
+            vy += ey;
+            iters++;
+            if (__fmaf_rn(ex, ex, ey * ey) < p.eps2)
+                break;
+        }
+        gx += vx;
+        gy += vy;
+        if (L > 0) {
+            gx *= 2.0f;
+            gy *= 2.0f;
+        }
+    }
+    o.x = x + gx;
+    o.y = y + gy;
+    o.min_eig = eig0;
+    o.iters = (uint16_t)iters;
+    o.residual = 0.0f;
+    o.cov_xx = o.cov_xy = o.cov_yy = 0.0f;
+    if (valid0 && !status) {
+        const DevLevel J0 = J.l[0];
+        const float fx0 = floorf(x), fy0 = floorf(y);
+        const int bx = (int)fx0, by = (int)fy0;
+        const float qx = (x - fx0) + gx, qy = (y - fy0) + gy;
+        if (qx < (float)(mx - bx) || qy < (float)(my - by) || qx >= (float)(J0.w - mx - 1 - bx) || qy >= (float)(J0.h - my - 1 - by)) {
+            status |= VTG_LK_OUT;
+        } else {
+            int jx, jy;
+            float fx, fy;
+            split(bx, qx, jx, fx);
+            split(by, qy, jy, fy);
+            float sa, ss;
+            lk_sample<MAXH, true>(J0, jx, fx, jy, fy, W, H, lane, P, sa, ss);
+            const float r0 = sa / p.area, r1 = ss / p.area;
+            o.residual = r0;
+            if (r0 > p.max_residual)
+                status |= VTG_LK_RESIDUAL;
+            const float s2 = r1 * p.area / (p.area - 2.0f);
+            o.cov_xx = s2 * gyy0 / det0;
+            o.cov_xy = -s2 * gxy0 / det0;
+            o.cov_yy = s2 * gxx0 / det0;
+        }
+    }
+    o.status = (uint16_t)status;
+}
+
+/* lk_track then, when asked and the track is good, the forward-backward check (src/kern/lk_driver.inc:111-121). */
+template <int MAXH>
+__device__ __forceinline__ void lk_point(const DevPyr &I, const DevPyr &J, int top, const LkPrm &p, float x, float y,
+                                         float gx, float gy, int lane, Patch<MAXH> &P, vtg_lk_out &o)
+{
+    lk_track<MAXH>(I, J, top, p, x, y, gx, gy, lane, P, o);
+    if (p.fb_max2 > 0.0f && o.status == 0) {
+        vtg_lk_out b;
+        lk_track<MAXH>(J, I, top, p, o.x, o.y, x - o.x, y - o.y, lane, P, b);
+        const float ex = b.x - x, ey = b.y - y;
+        if (b.status || __fmaf_rn(ex, ex, ey * ey) > p.fb_max2)
+            o.status |= VTG_LK_FLOWBACK;
+    }
+}
+
+__device__ __forceinline__ void store_out(vtg_lk_out *dst, const vtg_lk_out &o, int lane)
+{
+    /* eight 4-byte words, one per lane */
+    const uint32_t *src = reinterpret_cast<const uint32_t *>(&o);
+    uint32_t w = 0;
+#pragma unroll
+    for (int k = 0; k < 8; k++)
+        w = lane == k ? src[k] : w;
+    if (lane < 8)
+        reinterpret_cast<uint32_t *>(dst)[lane] = w;
+}
+
+/* Mean |J - I| over one cell of level 0, 8-bit grey (still.c:105-114). The differences are whole Q6 numbers, their sum
+ * below 2^24, so the F32 sum is exact and the mean is one rounding, as in the reference. */
+__device__ __forceinline__ float cell_diff(const DevLevel &A, const DevLevel &B, int col, int row, const CellGrid &g,
+                                           int lane)
+{
+    const int x = col * g.cell_w, y0 = row * g.cell_h, y1 = min(y0 + g.cell_h, A.h);
+    float s = 0.0f;
+    for (int k = lane; k < g.cell_w * (y1 - y0); k += 32) {
+        const int yy = y0 + k / g.cell_w, xx = min(x + k % g.cell_w, A.w - 1);
+        s += fabsf(__ldg(B.p + (size_t)yy * B.pitch + xx) - __ldg(A.p + (size_t)yy * A.pitch + xx));
+    }
+    s = warp_fold(s);
+    return __fdiv_rn(s, (float)((y1 - y0) * g.cell_w)) * LK_Q6_INV;
+}
+
+template <int MAXH>
+__global__ void __launch_bounds__(256) lk_cells_kernel(const DevPyr *__restrict__ Ip, const DevPyr *__restrict__ Jp,
+                                                       int top, LkPrm p, CellGrid g, int base_w, int base_h,
+                                                       vtg_lk_out *__restrict__ out, vtg_cell *__restrict__ cells)
+{
+    const int i = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (i >= g.n)
+        return;
+    const DevPyr &I = *Ip, &J = *Jp;
+    const int col = i % g.cols, row = i / g.cols;
+    /* The centre (cw c + cw / 2, ch r + ch / 2), clamped to where the patch fits (still.c:127-130). */
+    const float mx = (float)(p.W / 2 + 2), my = (float)(p.H / 2 + 2);
+    float x = (float)(col * g.cell_w + g.cell_w / 2), y = (float)(row * g.cell_h + g.cell_h / 2);
+    x = fminf(fmaxf(x, mx), (float)base_w - 1.0f - mx);
+    y = fminf(fmaxf(y, my), (float)base_h - 1.0f - my);
+    Patch<MAXH> P;
+    vtg_lk_out o;
+    lk_point<MAXH>(I, J, top, p, x, y, 0.0f, 0.0f, lane, P, o);
+    if (out)
+        store_out(out + i, o, lane);
+    if (cells) {
+        const float diff = cell_diff(I.l[0], J.l[0], col, row, g, lane);
+        if (lane == 0) {
+            vtg_cell c;
+            c.u = o.x - x;
+            c.v = o.y - y;
+            c.diff = diff;
+            c.state = o.status;
+            c.sigma = o.status ? 0.0f : sqrtf(o.cov_xx + o.cov_yy);
+            c.pad = 0.0f;
+            cells[i] = c;
+        }
+    }
+}
+
+template <int MAXH>
+__global__ void __launch_bounds__(256) lk_points_kernel(const DevPyr *__restrict__ Ip, const DevPyr *__restrict__ Jp,
+                                                        int top, LkPrm p, int n, const float *__restrict__ xs,
+                                                        const float *__restrict__ ys, const float *__restrict__ gxs,
+                                                        const float *__restrict__ gys, vtg_lk_out *__restrict__ out)
+{
+    const int i = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (i >= n)
+        return;
+    Patch<MAXH> P;
+    vtg_lk_out o;
+    lk_point<MAXH>(*Ip, *Jp, top, p, xs[i], ys[i], gxs ? gxs[i] : 0.0f, gys ? gys[i] : 0.0f, lane, P, o);
+    store_out(out + i, o, lane);
+}
+
+cudaError_t vtg_launch_cells(const DevPyr *I, const DevPyr *J, int top, const LkPrm &p, const CellGrid &g, int base_w,
+                             int base_h, vtg_lk_out *out, vtg_cell *cells, cudaStream_t s)
+{
+    const int blocks = (g.n + 7) / 8;
+    if (p.H <= 21)
+        lk_cells_kernel<21><<<blocks, 256, 0, s>>>(I, J, top, p, g, base_w, base_h, out, cells);
+    else
+        lk_cells_kernel<31><<<blocks, 256, 0, s>>>(I, J, top, p, g, base_w, base_h, out, cells);
+    return cudaGetLastError();
+}
+
+cudaError_t vtg_launch_points(const DevPyr *I, const DevPyr *J, int top, const LkPrm &p, int n, const float *xs,
+                              const float *ys, const float *gx, const float *gy, vtg_lk_out *out, cudaStream_t s)
+{
+    const int blocks = (n + 7) / 8;
+    if (n <= 0)
+        return cudaSuccess;
+    if (p.H <= 21)
+        lk_points_kernel<21><<<blocks, 256, 0, s>>>(I, J, top, p, n, xs, ys, gx, gy, out);
+    else
+        lk_points_kernel<31><<<blocks, 256, 0, s>>>(I, J, top, p, n, xs, ys, gx, gy, out);
+    return cudaGetLastError();
+}

@@ -1,0 +1,54 @@
+/* vtg_internal.cuh -- what the kernels and the C ABI share: device descriptors, LK parameters, launchers.
+ *
+ * Layout in HBM. A pyramid set is one allocation: level L is a w_L x h_L plane of F32 Q6 values (the reference's own
+ * plane values, src/kern/plane.h:1-9: byte x 64 at level 0, the binomial reduce above it), rows `pitch` floats apart,
+ * pitch a multiple of 32 floats (128-byte rows). No border is stored: every read that the reference makes into its
+ * replicated border is a clamped index here, and LK's reads never leave the plane (its bounds tests keep the window
+ * inside). Levels of one set follow each other, each starting on a 256-byte boundary. */
+#ifndef VTG_INTERNAL_CUH
+#define VTG_INTERNAL_CUH
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/vtg.h"
+
+#define VTG_FULL 0xffffffffu
+
+struct DevLevel {
+    const float *p;
+    int w, h, pitch;
+};
+
+struct DevPyr {
+    DevLevel l[VTG_MAX_LEVELS];
+    int levels;
+};
+
+/* The LK settings a kernel needs, derived once from struct vtg_config. */
+struct LkPrm {
+    int W, H, max_iter;
+    float eps2;     /* eps^2 */
+    float min_eig;
+    float max_residual;
+    float fb_max2;  /* fb_max^2; <= 0: no forward-backward check */
+    float area;     /* W H */
+};
+
+/* A cell grid on level 0 of the pyramids handed to the kernel. */
+struct CellGrid {
+    int cols, rows, n;
+    int cell_w, cell_h;
+};
+
+static inline int vtg_pitch(int w) { return (w + 31) & ~31; }
+
+/* Launchers (pyramid.cu, lk.cu). All asynchronous on `s`; each returns a cudaError_t. */
+cudaError_t vtg_launch_pyramid(const uint8_t *frame, int stride, int w, int h, float *const *levels, const int *pitches,
+                               int nlevels, cudaStream_t s);
+cudaError_t vtg_launch_cells(const DevPyr *I, const DevPyr *J, int top, const LkPrm &p, const CellGrid &g, int base_w,
+                             int base_h, vtg_lk_out *out, vtg_cell *cells, cudaStream_t s);
+cudaError_t vtg_launch_points(const DevPyr *I, const DevPyr *J, int top, const LkPrm &p, int n, const float *xs,
+                              const float *ys, const float *gx, const float *gy, vtg_lk_out *out, cudaStream_t s);
+
+#endif

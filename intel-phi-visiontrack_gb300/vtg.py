@@ -1,0 +1,197 @@
+"""vtg.py -- Python binding of libvtg's C ABI (include/vtg.h), for tests, the benchmark and Python callers.
+
+Loads the in-tree libvtg.so built by vtg_build.py and fails loudly when it is missing: there is no CPU or PyTorch
+fallback behind any function here. numpy arrays in and out for host buffers; device buffers are raw addresses (for
+example ``torch.Tensor.data_ptr()``) passed with ``where=DEVICE``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import weakref
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libvtg.so")
+
+OK, EINVAL, ENOMEM, ECUDA, ETIMEOUT, EBUSY, ENODEV, EBUDGET = 0, -1, -2, -3, -4, -5, -6, -7
+HOST, DEVICE = 0, 1
+LK_OK, LK_OUT, LK_LOWEIG, LK_RESIDUAL, LK_FLOWBACK = 0, 1, 2, 4, 8
+MAX_LEVELS = 6
+
+LK_OUT_DTYPE = np.dtype([("x", "<f4"), ("y", "<f4"), ("min_eig", "<f4"), ("residual", "<f4"), ("cov_xx", "<f4"),
+                         ("cov_xy", "<f4"), ("cov_yy", "<f4"), ("iters", "<u2"), ("status", "<u2")])
+CELL_DTYPE = np.dtype([("u", "<f4"), ("v", "<f4"), ("diff", "<f4"), ("state", "<u4"), ("sigma", "<f4"),
+                       ("pad", "<f4")])
+
+
+class Config(C.Structure):
+    """struct vtg_config."""
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("levels", C.c_uint32), ("patch_w", C.c_uint32),
+                ("patch_h", C.c_uint32), ("max_iter", C.c_uint32), ("eps", C.c_float), ("min_eig", C.c_float),
+                ("max_residual", C.c_float), ("fb_max", C.c_float), ("cell_w", C.c_uint32), ("cell_h", C.c_uint32),
+                ("flow_level", C.c_uint32)]
+
+
+def config(width, height, levels=4, patch_w=21, patch_h=21, max_iter=10, eps=0.01, min_eig=0.1, max_residual=25.0,
+           fb_max=0.5, cell_w=16, cell_h=8, flow_level=0) -> Config:
+    return Config(width, height, levels, patch_w, patch_h, max_iter, eps, min_eig, max_residual, fb_max, cell_w,
+                  cell_h, flow_level)
+
+
+class VtgError(RuntimeError):
+    def __init__(self, code: int, what: str):
+        msg = lib().vtg_strerror(code).decode()
+        if code == ECUDA:
+            msg += " (cudaError %d)" % lib().vtg_last_cuda_error()
+        super().__init__("%s: %s" % (what, msg))
+        self.code = code
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("libvtg.so is not built (run vtg_build.py / __graft_entry__.build())")
+        L = C.CDLL(LIB_PATH)
+        vp, sz, i, f = C.c_void_p, C.c_size_t, C.c_int, C.c_float
+        L.vtg_strerror.restype = C.c_char_p
+        L.vtg_strerror.argtypes = [i]
+        L.vtg_last_cuda_error.restype = i
+        L.vtg_ctx_create.argtypes = [i, sz, C.POINTER(vp)]
+        L.vtg_ctx_destroy.argtypes = [vp]
+        L.vtg_ctx_destroy.restype = None
+        L.vtg_ctx_used.argtypes = [vp]
+        L.vtg_ctx_used.restype = sz
+        L.vtg_ctx_sync.argtypes = [vp, i]
+        L.vtg_tracker_bytes.argtypes = [C.POINTER(Config)]
+        L.vtg_tracker_bytes.restype = sz
+        L.vtg_tracker_create.argtypes = [vp, C.POINTER(Config), C.POINTER(vp)]
+        L.vtg_tracker_destroy.argtypes = [vp]
+        L.vtg_tracker_destroy.restype = None
+        L.vtg_tracker_sets.argtypes = [vp]
+        L.vtg_tracker_cells.argtypes = [vp, C.POINTER(i), C.POINTER(i)]
+        L.vtg_tracker_stream.argtypes = [vp]
+        L.vtg_tracker_stream.restype = vp
+        L.vtg_build.argtypes = [vp, i, vp, i, i, vp]
+        L.vtg_cells.argtypes = [vp, i, i, vp, vp, i, vp]
+        L.vtg_points.argtypes = [vp, i, i, i, i, vp, vp, vp, vp, vp, i, vp]
+        L.vtg_level.argtypes = [vp, i, i, vp, i, vp]
+        L.vtg_level_size.argtypes = [vp, i, C.POINTER(i), C.POINTER(i)]
+        _lib = L
+    return _lib
+
+
+def check(code: int, what: str) -> int:
+    if code < 0:
+        raise VtgError(code, what)
+    return code
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+class Context:
+    def __init__(self, device: int = 0, hbm_budget: int = 0):
+        self.h = C.c_void_p()
+        self._trackers = weakref.WeakSet()
+        check(lib().vtg_ctx_create(device, hbm_budget, C.byref(self.h)), "vtg_ctx_create")
+
+    def used(self) -> int:
+        return lib().vtg_ctx_used(self.h)
+
+    def sync(self, timeout_ms: int = 10000):
+        check(lib().vtg_ctx_sync(self.h, timeout_ms), "vtg_ctx_sync")
+
+    def close(self):
+        if self.h:
+            for t in list(self._trackers):
+                t.h = C.c_void_p()  # the context frees its trackers
+            lib().vtg_ctx_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Tracker:
+    """One stream's device-resident pyramids and cell results (vtg_tracker)."""
+
+    def __init__(self, ctx: Context, cfg: Config):
+        self.ctx = ctx
+        self.cfg = cfg
+        self.h = C.c_void_p()
+        check(lib().vtg_tracker_create(ctx.h, C.byref(cfg), C.byref(self.h)), "vtg_tracker_create")
+        ctx._trackers.add(self)
+        cols, rows = C.c_int(), C.c_int()
+        lib().vtg_tracker_cells(self.h, C.byref(cols), C.byref(rows))
+        self.cols, self.rows = cols.value, rows.value
+
+    @property
+    def stream(self) -> int:
+        return lib().vtg_tracker_stream(self.h)
+
+    def sync(self, timeout_ms: int = 10000):
+        self.ctx.sync(timeout_ms)
+
+    def level_size(self, level: int):
+        w, h = C.c_int(), C.c_int()
+        check(lib().vtg_level_size(self.h, level, C.byref(w), C.byref(h)), "vtg_level_size")
+        return w.value, h.value
+
+    def build(self, set_: int, frame, stride: int | None = None, where: int = HOST, stream=None):
+        if where == HOST:
+            frame = np.ascontiguousarray(frame, np.uint8)
+            stride = frame.shape[1] if stride is None else stride
+            ptr = frame.ctypes.data
+        else:
+            ptr = frame
+        check(lib().vtg_build(self.h, set_, ptr, stride, where, stream), "vtg_build")
+
+    def level(self, set_: int, level: int) -> np.ndarray:
+        w, h = self.level_size(level)
+        out = np.empty((h, w), np.float32)
+        check(lib().vtg_level(self.h, set_, level, _p(out), HOST, None), "vtg_level")
+        self.sync()
+        return out
+
+    def cells(self, prev: int, cur: int, want_lk: bool = True):
+        n = self.cols * self.rows
+        cells = np.zeros(n, CELL_DTYPE)
+        lk = np.zeros(n, LK_OUT_DTYPE) if want_lk else None
+        check(lib().vtg_cells(self.h, prev, cur, _p(cells), _p(lk), HOST, None), "vtg_cells")
+        self.sync()
+        return cells, lk
+
+    def cells_device(self, prev: int, cur: int, cells_ptr, lk_ptr, stream=None):
+        check(lib().vtg_cells(self.h, prev, cur, cells_ptr, lk_ptr, DEVICE, stream), "vtg_cells")
+
+    def points(self, prev: int, cur: int, xs, ys, gx=None, gy=None, top: int = -1) -> np.ndarray:
+        xs = np.ascontiguousarray(xs, np.float32)
+        ys = np.ascontiguousarray(ys, np.float32)
+        gx = None if gx is None else np.ascontiguousarray(gx, np.float32)
+        gy = None if gy is None else np.ascontiguousarray(gy, np.float32)
+        out = np.zeros(len(xs), LK_OUT_DTYPE)
+        check(lib().vtg_points(self.h, prev, cur, top, len(xs), _p(xs), _p(ys), _p(gx), _p(gy), _p(out), HOST, None),
+              "vtg_points")
+        self.sync()
+        return out
+
+    def close(self):
+        if self.h:
+            lib().vtg_tracker_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

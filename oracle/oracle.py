@@ -1,0 +1,379 @@
+"""oracle.py -- TEST INFRASTRUCTURE ONLY: ctypes access to the checker's two libraries.
+
+* ``liboracle.so`` -- this project's CPU restatement of the reference's pyramid / LK / NCC path (vtg_oracle.c).
+* ``_ref/libvtref.so`` -- the reference's own kernel sources with a small harness (ref_driver.c, ref_track_tu.c), built
+  only where the reference tree is present; absent elsewhere (``ref_available()`` says which).
+
+Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg import this module, as the checker. The
+library under test never does.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LANE, F64 = 0, 1
+OK, OUT, LOWEIG, RESIDUAL, FLOWBACK = 0, 1, 2, 4, 8
+MAX_LEVELS = 8
+
+# struct lk_out (src/kern/lk.h:33-40) / struct vt_cell (src/common/vt_proto.h:395-402) as numpy records.
+LK_OUT = np.dtype([("x", "<f4"), ("y", "<f4"), ("min_eig", "<f4"), ("residual", "<f4"), ("cov_xx", "<f4"),
+                   ("cov_xy", "<f4"), ("cov_yy", "<f4"), ("iters", "<u2"), ("status", "<u2")])
+CELL = np.dtype([("u", "<f4"), ("v", "<f4"), ("diff", "<f4"), ("state", "<u4"), ("sigma", "<f4"), ("pad", "<f4")])
+assert LK_OUT.itemsize == 32 and CELL.itemsize == 24
+
+
+class Pyr(C.Structure):
+    _fields_ = [("levels", C.c_int), ("w", C.c_int * MAX_LEVELS), ("h", C.c_int * MAX_LEVELS),
+                ("stride", C.c_int * MAX_LEVELS), ("lv", C.c_void_p * MAX_LEVELS)]
+
+
+class LkCfg(C.Structure):
+    _fields_ = [("w", C.c_int), ("h", C.c_int), ("max_iter", C.c_int), ("eps", C.c_float),
+                ("min_eig", C.c_float), ("max_residual", C.c_float)]
+
+
+class Img(C.Structure):
+    _fields_ = [("p", C.c_void_p), ("w", C.c_int), ("h", C.c_int), ("stride", C.c_int)]
+
+
+class Found(C.Structure):
+    _fields_ = [("hx", C.c_int), ("hy", C.c_int), ("ncc", C.c_double), ("second", C.c_double),
+                ("ox", C.c_double), ("oy", C.c_double)]
+
+
+def _build(target: str = "all") -> None:
+    subprocess.run(["make", "-s", "-C", HERE, target], check=True)
+
+
+_lib = None
+_ref = None
+
+
+def lib() -> C.CDLL:
+    """liboracle.so, built on first use."""
+    global _lib
+    if _lib is None:
+        path = os.path.join(HERE, "liboracle.so")
+        src = os.path.join(HERE, "vtg_oracle.c")
+        if not os.path.exists(path) or os.path.getmtime(path) < os.path.getmtime(src):
+            _build("all")
+        _lib = C.CDLL(path)
+        _lib.or_fnv.restype = C.c_uint64
+        _lib.or_fnv.argtypes = [C.c_uint64, C.c_void_p, C.c_size_t]
+        for name in ("or_ncc_at", "or_ncc_half"):
+            f = getattr(_lib, name)
+            f.restype = C.c_double
+            f.argtypes = [C.POINTER(Img), C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int]
+        _lib.or_peak_offset.restype = C.c_double
+        _lib.or_peak_offset.argtypes = [C.c_double] * 3
+        _lib.or_lk_track.argtypes = [C.POINTER(Pyr), C.POINTER(Pyr), C.c_int, C.POINTER(LkCfg), C.c_float, C.c_float,
+                                     C.c_float, C.c_float, C.c_float, C.c_void_p, C.c_int]
+        _lib.or_lk_points.argtypes = [C.POINTER(Pyr), C.POINTER(Pyr), C.c_int, C.POINTER(LkCfg), C.c_int, C.c_void_p,
+                                      C.c_void_p, C.c_void_p, C.c_void_p, C.c_float, C.c_void_p, C.c_int, C.c_int]
+        _lib.or_cells.argtypes = [C.POINTER(Pyr), C.POINTER(Pyr), C.c_int, C.POINTER(LkCfg), C.c_int, C.c_int,
+                                  C.c_float, C.c_void_p, C.c_void_p, C.c_int, C.c_int]
+        _lib.or_search_slot.argtypes = [C.POINTER(Img), C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int,
+                                        C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(Found), C.c_void_p, C.c_void_p,
+                                        C.c_void_p]
+        _lib.or_ncc_map.argtypes = [C.POINTER(Img), C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int,
+                                    C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int]
+        _lib.or_cut_template.argtypes = [C.POINTER(Img), C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
+        _lib.or_u8_to_q6.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int]
+        _lib.or_reduce.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int]
+        _lib.or_m1_image.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int]
+        _lib.or_m2_render.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]
+        _lib.or_cell_centre.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(LkCfg), C.c_int, C.c_int,
+                                        C.c_void_p, C.c_void_p]
+    return _lib
+
+
+def ref_available() -> bool:
+    """True where the reference's own sources are here to build oracle/_ref (this container, not the GPU machine)."""
+    path = os.path.join(HERE, "_ref", "libvtref.so")
+    if os.path.exists(path):
+        return True
+    if os.path.isdir("/root/reference/src/kern"):
+        try:
+            _build("ref")
+        except subprocess.CalledProcessError:
+            return False
+        return os.path.exists(path)
+    return False
+
+
+def ref() -> C.CDLL:
+    """oracle/_ref/libvtref.so: the reference's own code."""
+    global _ref
+    if _ref is None:
+        if not ref_available():
+            raise RuntimeError("oracle/_ref is not built: the reference sources are not on this machine")
+        _ref = C.CDLL(os.path.join(HERE, "_ref", "libvtref.so"))
+        _ref.ref_correlate.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_double, C.c_int, C.c_void_p,
+                                       C.c_void_p, C.c_void_p]
+        _ref.ref_search_slot.restype = C.c_int
+        _ref.ref_search_slot.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_float, C.c_int,
+                                         C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                         C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_void_p, C.c_void_p,
+                                         C.c_void_p, C.c_int]
+        _ref.ref_search_half.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_float, C.c_int, C.c_void_p,
+                                         C.c_void_p, C.c_void_p]
+        _ref.ref_peak_offset.restype = C.c_double
+        _ref.ref_peak_offset.argtypes = [C.c_double] * 3
+        _ref.ref_lk_points.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                       C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int,
+                                       C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]
+        _ref.ref_pyramid.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p]
+        _ref.ref_still_vectors.restype = C.c_int
+        _ref.ref_still_vectors.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p]
+    return _ref
+
+
+def _p(a: np.ndarray | None):
+    return None if a is None else a.ctypes.data
+
+
+def fnv(data: bytes | np.ndarray, h: int = 0xcbf29ce484222325) -> int:
+    a = np.ascontiguousarray(data)
+    return lib().or_fnv(h, a.ctypes.data, a.nbytes)
+
+
+def level_dims(w: int, h: int, levels: int):
+    dims = []
+    for _ in range(levels):
+        dims.append((w, h))
+        w, h = (w + 1) // 2, (h + 1) // 2
+    return dims
+
+
+def pyramid(frame: np.ndarray, levels: int):
+    """The Q6 pyramid of a uint8 frame: a list of float32 planes (exact whole numbers), level 0 first."""
+    L = lib()
+    frame = np.ascontiguousarray(frame, dtype=np.uint8)
+    h, w = frame.shape
+    out = []
+    q = np.empty((h, w), np.float32)
+    L.or_u8_to_q6(_p(frame), C.c_int(w), C.c_int(w), C.c_int(h), _p(q), C.c_int(w))
+    out.append(q)
+    for _ in range(1, levels):
+        ph, pw = out[-1].shape
+        d = np.empty(((ph + 1) // 2, (pw + 1) // 2), np.float32)
+        L.or_reduce(_p(out[-1]), C.c_int(pw), C.c_int(ph), C.c_int(pw), _p(d), C.c_int(d.shape[1]))
+        out.append(d)
+    return out
+
+
+def make_pyr(levels_list) -> Pyr:
+    p = Pyr()
+    p.levels = len(levels_list)
+    for i, pl in enumerate(levels_list):
+        assert pl.dtype == np.float32 and pl.flags.c_contiguous
+        p.h[i], p.w[i] = pl.shape
+        p.stride[i] = pl.shape[1]
+        p.lv[i] = pl.ctypes.data
+    p._keep = levels_list  # keeps the planes alive with the struct
+    return p
+
+
+def lk_cfg(w=21, h=21, max_iter=10, eps=0.01, min_eig=0.1, max_residual=25.0) -> LkCfg:
+    return LkCfg(w, h, max_iter, eps, min_eig, max_residual)
+
+
+def lk_points(I, J, top, cfg: LkCfg, xs, ys, gxs=None, gys=None, max_fb=0.0, mode=LANE, threads=1) -> np.ndarray:
+    xs = np.ascontiguousarray(xs, np.float32)
+    ys = np.ascontiguousarray(ys, np.float32)
+    gxs = None if gxs is None else np.ascontiguousarray(gxs, np.float32)
+    gys = None if gys is None else np.ascontiguousarray(gys, np.float32)
+    out = np.zeros(len(xs), LK_OUT)
+    pi, pj = make_pyr(I), make_pyr(J)
+    lib().or_lk_points(C.byref(pi), C.byref(pj), top, C.byref(cfg), len(xs), _p(xs), _p(ys), _p(gxs), _p(gys),
+                       C.c_float(max_fb), _p(out), mode, threads)
+    return out
+
+
+def grid_shape(w: int, h: int, cell_w: int, cell_h: int):
+    return (h + cell_h - 1) // cell_h, (w + cell_w - 1) // cell_w
+
+
+def cells(I, J, top, cfg: LkCfg, cell_w, cell_h, max_fb=0.0, mode=LANE, threads=1):
+    """The per-cell grid over level 0 of I / J: (lk_out records, vt_cell records), row-major."""
+    rows, cols = grid_shape(I[0].shape[1], I[0].shape[0], cell_w, cell_h)
+    out = np.zeros(rows * cols, LK_OUT)
+    cl = np.zeros(rows * cols, CELL)
+    pi, pj = make_pyr(I), make_pyr(J)
+    lib().or_cells(C.byref(pi), C.byref(pj), top, C.byref(cfg), cell_w, cell_h, C.c_float(max_fb), _p(out), _p(cl),
+                   mode, threads)
+    return out, cl
+
+
+def cell_centres(w, h, cell_w, cell_h, pw=21, ph=21):
+    """Cell centres as the per-cell grid places them (src/kern/still.c:127-130, margin = patch / 2 + 2)."""
+    rows, cols = grid_shape(w, h, cell_w, cell_h)
+    mx, my = float(pw // 2 + 2), float(ph // 2 + 2)
+    c = np.arange(cols, dtype=np.float32) * cell_w + cell_w // 2
+    r = np.arange(rows, dtype=np.float32) * cell_h + cell_h // 2
+    c = np.clip(c, mx, np.float32(w - 1 - mx))
+    r = np.clip(r, my, np.float32(h - 1 - my))
+    xs, ys = np.meshgrid(c, r)
+    return xs.astype(np.float32).ravel(), ys.astype(np.float32).ravel()
+
+
+def img(plane: np.ndarray) -> Img:
+    plane = np.ascontiguousarray(plane, np.float32)
+    m = Img(plane.ctypes.data, plane.shape[1], plane.shape[0], plane.shape[1])
+    m._keep = plane
+    return m
+
+
+def cut_template(plane, x0, y0, tw, th):
+    app = np.empty(tw * th, np.float32)
+    norm = np.zeros(1, np.float32)
+    m = img(plane)
+    lib().or_cut_template(C.byref(m), x0, y0, tw, th, _p(app), _p(norm))
+    return app.reshape(th, tw), float(norm[0])
+
+
+def ncc_at(plane, app, norm, x, y, mode=LANE) -> float:
+    app = np.ascontiguousarray(app, np.float32)
+    m = img(plane)
+    return lib().or_ncc_at(C.byref(m), _p(app), app.shape[1], app.shape[0], norm, x, y, mode)
+
+
+def ncc_half(plane, app, norm, hx, hy, mode=LANE) -> float:
+    app = np.ascontiguousarray(app, np.float32)
+    m = img(plane)
+    return lib().or_ncc_half(C.byref(m), _p(app), app.shape[1], app.shape[0], norm, hx, hy, mode)
+
+
+def ncc_map(plane, app, norm, x0, x1, y0, y1, mode=F64) -> np.ndarray:
+    app = np.ascontiguousarray(app, np.float32)
+    out = np.empty((y1 - y0 + 1, x1 - x0 + 1), np.float32)
+    m = img(plane)
+    lib().or_ncc_map(C.byref(m), _p(app), app.shape[1], app.shape[0], norm, x0, x1, y0, y1, mode, _p(out), 1)
+    return out
+
+
+def search_slot(plane, app, norm, x0, x1, y0, y1, step, mode=LANE):
+    """search_slot: (found dict, per-cell map values, map x, map y)."""
+    app = np.ascontiguousarray(app, np.float32)
+    m = img(plane)
+    h, w = plane.shape
+    ncells = (w // 16 + 2) * (h // 16 + 2)
+    mv = np.zeros(ncells, np.float32)
+    mx = np.zeros(ncells, np.int32)
+    my = np.zeros(ncells, np.int32)
+    f = Found()
+    lib().or_search_slot(C.byref(m), _p(app), app.shape[1], app.shape[0], norm, x0, x1, y0, y1, step, mode,
+                         C.byref(f), _p(mv), _p(mx), _p(my))
+    return {"hx": f.hx, "hy": f.hy, "ncc": f.ncc, "second": f.second, "ox": f.ox, "oy": f.oy}, mv, mx, my
+
+
+def peak_offset(l, c, r) -> float:
+    return lib().or_peak_offset(l, c, r)
+
+
+def m1_image(w: int, h: int) -> np.ndarray:
+    stride = (w + 15) & ~15
+    a = np.zeros((h, stride), np.uint8)
+    lib().or_m1_image(_p(a), w, h, stride)
+    return a[:, :w].copy()
+
+
+def m2_render(w: int, h: int, ox: int, oy: int) -> np.ndarray:
+    a = np.zeros((h, w), np.uint8)
+    lib().or_m2_render(_p(a), w, h, w, ox, oy)
+    return a
+
+
+# ---------------------------------------------------------------- the reference itself (oracle/_ref)
+
+def ref_pyramid(frame: np.ndarray, levels: int, use_ref: bool = False):
+    frame = np.ascontiguousarray(frame, np.uint8)
+    h, w = frame.shape
+    stride = (w + 15) & ~15
+    buf = np.zeros((h, stride), np.uint8)
+    buf[:, :w] = frame
+    dims = level_dims(w, h, levels)
+    out = np.zeros(sum(a * b for a, b in dims), np.float32)
+    ref().ref_pyramid(_p(buf), stride, w, h, levels, int(use_ref), _p(out))
+    planes, off = [], 0
+    for (lw, lh) in dims:
+        planes.append(out[off:off + lw * lh].reshape(lh, lw))
+        off += lw * lh
+    return planes
+
+
+def ref_lk_points(f0, f1, levels, top, cfg: LkCfg, xs, ys, gxs=None, gys=None, max_fb=0.0, use_ref=False,
+                  threads=8, base=0) -> np.ndarray:
+    h, w = f0.shape
+    stride = (w + 15) & ~15
+    b0 = np.zeros((h, stride), np.uint8)
+    b1 = np.zeros((h, stride), np.uint8)
+    b0[:, :w] = f0
+    b1[:, :w] = f1
+    xs = np.ascontiguousarray(xs, np.float32)
+    ys = np.ascontiguousarray(ys, np.float32)
+    gxs = None if gxs is None else np.ascontiguousarray(gxs, np.float32)
+    gys = None if gys is None else np.ascontiguousarray(gys, np.float32)
+    out = np.zeros(len(xs), LK_OUT)
+    ref().ref_lk_points(_p(b0), _p(b1), stride, w, h, levels, base, top, cfg.w, cfg.h, cfg.max_iter, C.c_float(cfg.eps),
+                        C.c_float(cfg.min_eig), C.c_float(cfg.max_residual), C.c_float(max_fb), len(xs), _p(xs),
+                        _p(ys), _p(gxs), _p(gys), int(use_ref), threads, _p(out))
+    return out
+
+
+def ref_still_vectors(f0, f1) -> np.ndarray:
+    h, w = f0.shape
+    stride = (w + 15) & ~15
+    b0 = np.zeros((h, stride), np.uint8)
+    b1 = np.zeros((h, stride), np.uint8)
+    b0[:, :w] = f0
+    b1[:, :w] = f1
+    n = ((w + 15) // 16) * ((h + 7) // 8)
+    out = np.zeros(n, CELL)
+    got = ref().ref_still_vectors(_p(b0), _p(b1), stride, w, h, _p(out))
+    assert got == n
+    return out
+
+
+def ref_correlate(plane, app, norm, xs, ys) -> np.ndarray:
+    plane = np.ascontiguousarray(plane, np.float32)
+    app = np.ascontiguousarray(app, np.float32)
+    assert app.shape == (21, 32)
+    xs = np.ascontiguousarray(xs, np.int32)
+    ys = np.ascontiguousarray(ys, np.int32)
+    out = np.zeros(len(xs), np.float64)
+    ref().ref_correlate(_p(plane), plane.shape[1], plane.shape[0], _p(app), norm, len(xs), _p(xs), _p(ys), _p(out))
+    return out
+
+
+def ref_search_slot(plane, app, norm, x0, x1, y0, y1, step, level=0):
+    plane = np.ascontiguousarray(plane, np.float32)
+    app = np.ascontiguousarray(app, np.float32)
+    h, w = plane.shape
+    maxc = (w // 16 + 2) * (h // 16 + 2)
+    mv = np.zeros(maxc, np.float32)
+    mx = np.zeros(maxc, np.int32)
+    my = np.zeros(maxc, np.int32)
+    hx, hy = C.c_int(), C.c_int()
+    ncc, second = C.c_double(), C.c_double()
+    n = ref().ref_search_slot(_p(plane), w, h, level, _p(app), C.c_float(norm), x0, x1, y0, y1, step, C.byref(hx),
+                              C.byref(hy), C.byref(ncc), C.byref(second), _p(mv), _p(mx), _p(my), maxc)
+    if n < 0:
+        raise RuntimeError("ref_search_slot: tracker set-up failed")
+    return {"hx": hx.value, "hy": hy.value, "ncc": ncc.value, "second": second.value}, mv[:n], mx[:n], my[:n]
+
+
+def ref_search_half(plane, app, norm, hxs, hys) -> np.ndarray:
+    plane = np.ascontiguousarray(plane, np.float32)
+    app = np.ascontiguousarray(app, np.float32)
+    hxs = np.ascontiguousarray(hxs, np.int32)
+    hys = np.ascontiguousarray(hys, np.int32)
+    out = np.zeros(len(hxs), np.float64)
+    ref().ref_search_half(_p(plane), plane.shape[1], plane.shape[0], _p(app), C.c_float(norm), len(hxs), _p(hxs),
+                          _p(hys), _p(out))
+    return out

@@ -1,0 +1,186 @@
+/* ref_driver.c -- TEST INFRASTRUCTURE ONLY: this project's own harness around the reference's unmodified sources.
+ *
+ * oracle/Makefile compiles the reference's kernel sources (the C files of src/kern in Lasimeri/Intel-Phi-VisionTrack,
+ * read in place) together with this file into oracle/_ref/libvtref.so. The functions here only arrange inputs, call the
+ * reference's own public functions (and, through ref_track_tu.c, two static ones of track.c) and copy results out. They
+ * are used to pin the oracle restatement (vtg_oracle.c) and to generate the golden fixtures under tests/golden/.
+ *
+ * The reference's planes are padded F32 (src/kern/plane.h:16-35); here every plane handed in or out is its w x h
+ * interior, rows w floats apart. */
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "img.h"
+#include "lk.h"
+#include "plane.h"
+#include "still.h"
+#include "track.h"
+
+#define REF_MAX_LEVELS 8
+
+struct ref_pyr {
+    int levels;
+    struct vt_plane l[REF_MAX_LEVELS];
+};
+
+static struct vt_plane new_plane(int w, int h)
+{
+    void *m = aligned_alloc(64, (plane_bytes(w, h) + 63) & ~(size_t)63);
+    memset(m, 0, plane_bytes(w, h));
+    return plane_at(m, w, h);
+}
+
+static void free_plane(struct vt_plane *pl) { free(pl->p - (size_t)pl->stride * VT_PAD_Y - VT_PAD_X); }
+
+/* tk_build's pyramid with the vector kernels (src/kern/track.c:584-629, OP_U8 and OP_REDUCE of job_main). */
+static void build(struct ref_pyr *p, const uint8_t *img, int stride, int w, int h, int levels, int use_ref)
+{
+    p->levels = levels;
+    for (int i = 0; i < levels; i++) {
+        p->l[i] = new_plane(w, h);
+        w = (w + 1) / 2;
+        h = (h + 1) / 2;
+    }
+    if (use_ref)
+        img_u8_to_q6_ref(&p->l[0], img, stride, 0, p->l[0].h);
+    else
+        img_u8_to_q6_vx(&p->l[0], img, stride, 0, p->l[0].h);
+    img_pad_rows(&p->l[0], 0, p->l[0].h);
+    img_pad_tb(&p->l[0]);
+    for (int i = 1; i < levels; i++) {
+        if (use_ref)
+            img_reduce_ref(&p->l[i], &p->l[i - 1], 0, p->l[i].h);
+        else
+            img_reduce_vx(&p->l[i], &p->l[i - 1], 0, p->l[i].h);
+        img_pad_rows(&p->l[i], 0, p->l[i].h);
+        img_pad_tb(&p->l[i]);
+    }
+}
+
+static void release(struct ref_pyr *p)
+{
+    for (int i = 0; i < p->levels; i++)
+        free_plane(&p->l[i]);
+}
+
+/* The pyramid of one frame: every level's interior, level after level. src rows are stride bytes apart (a multiple
+ * of 16, as img.h asks). */
+void ref_pyramid(const uint8_t *src, int stride, int w, int h, int levels, int use_ref, float *out)
+{
+    struct ref_pyr p;
+    build(&p, src, stride, w, h, levels, use_ref);
+    for (int i = 0; i < levels; i++) {
+        for (int y = 0; y < p.l[i].h; y++)
+            memcpy(out + (size_t)y * p.l[i].w, plane_row(&p.l[i], y), sizeof(float) * (size_t)p.l[i].w);
+        out += (size_t)p.l[i].w * p.l[i].h;
+    }
+    release(&p);
+}
+
+struct ref_team {
+    const struct ref_pyr *I, *J;
+    const struct lk_cfg *c;
+    int top, n, use_ref, base;
+    float max_fb;
+    const float *xs, *ys, *gxs, *gys;
+    struct lk_out *out;
+    int next;
+};
+
+static void *ref_points_thread(void *arg)
+{
+    struct ref_team *j = arg;
+    void *tile = aligned_alloc(64, (lk_tile_bytes() + 63) & ~(size_t)63);
+    for (;;) {
+        const int i = __atomic_fetch_add(&j->next, 1, __ATOMIC_RELAXED);
+        if (i >= j->n)
+            break;
+        const float gx = j->gxs ? j->gxs[i] : 0.0f, gy = j->gys ? j->gys[i] : 0.0f;
+        if (j->use_ref) {
+            lk_track_ref(j->I->l + j->base, j->J->l + j->base, j->top, j->c, j->xs[i], j->ys[i], gx, gy, &j->out[i], tile);
+            if (j->max_fb > 0.0f)
+                lk_flowback_ref(j->I->l + j->base, j->J->l + j->base, j->top, j->c, j->xs[i], j->ys[i], j->max_fb, &j->out[i], tile);
+        } else {
+            lk_track_vx(j->I->l + j->base, j->J->l + j->base, j->top, j->c, j->xs[i], j->ys[i], gx, gy, &j->out[i], tile);
+            if (j->max_fb > 0.0f)
+                lk_flowback_vx(j->I->l + j->base, j->J->l + j->base, j->top, j->c, j->xs[i], j->ys[i], j->max_fb, &j->out[i], tile);
+        }
+    }
+    free(tile);
+    return NULL;
+}
+
+/* OP_LK of job_main (src/kern/track.c:275-292): every point through lk_track_{vx,ref} and, when max_fb > 0,
+ * lk_flowback_{vx,ref}, on a team of threads taking points by an atomic counter. Pyramids are built from the two frames
+ * with the vector kernels, as tk_build does; LK runs on the pyramid from level `base` up (points in that level's
+ * pixels), as the per-cell flow does at a flow level above 0. */
+void ref_lk_points(const uint8_t *f0, const uint8_t *f1, int stride, int w, int h, int levels, int base, int top, int pw, int ph, int max_iter, float eps, float min_eig, float max_residual, float max_fb, int n, const float *xs, const float *ys, const float *gxs, const float *gys, int use_ref, int threads, struct lk_out *out)
+{
+    struct ref_pyr I, J;
+    build(&I, f0, stride, w, h, levels, 0);
+    build(&J, f1, stride, w, h, levels, 0);
+    const struct lk_cfg c = {.w = pw, .h = ph, .max_iter = max_iter, .eps = eps, .min_eig = min_eig, .max_residual = max_residual, .prefetch = 0};
+    struct ref_team j = {.I = &I, .J = &J, .c = &c, .top = top, .n = n, .use_ref = use_ref, .base = base, .max_fb = max_fb, .xs = xs, .ys = ys, .gxs = gxs, .gys = gys, .out = out, .next = 0};
+    if (threads <= 1) {
+        ref_points_thread(&j);
+    } else {
+        pthread_t th[64];
+        threads = threads > 64 ? 64 : threads;
+        for (int i = 0; i < threads; i++)
+            pthread_create(&th[i], NULL, ref_points_thread, &j);
+        for (int i = 0; i < threads; i++)
+            pthread_join(th[i], NULL);
+    }
+    release(&I);
+    release(&J);
+}
+
+static void *host_alloc(void *ctx, size_t bytes)
+{
+    (void)ctx;
+    return aligned_alloc(64, (bytes + 63) & ~(size_t)63);
+}
+
+/* still_vectors itself (src/kern/still.c:116-141): one frame of the reference's per-cell flow, with the still's mean
+ * set to frame f0 (as after its first frame) and f1 the current frame, both at native resolution. cells receives
+ * ceil(w / 16) x ceil(h / 8) records. */
+int ref_still_vectors(const uint8_t *f0, const uint8_t *f1, int stride, int w, int h, struct vt_cell *cells)
+{
+    const struct still_cfg sc = {.w = w, .h = h, .avg = 8, .motion_px = 1.0f, .motion_grey = 4.0f, .threads = 1};
+    struct still *s = still_create(&sc, host_alloc, NULL);
+    if (!s)
+        return -1;
+    struct ref_pyr A, B;
+    build(&A, f0, stride, w, h, 1, 0);
+    build(&B, f1, stride, w, h, 1, 0);
+    const struct vt_plane *mean = still_mean(s);
+    for (int y = -VT_PAD_Y; y < h + VT_PAD_Y; y++)
+        memcpy(plane_row(mean, y) - VT_PAD_X, plane_row(&A.l[0], y) - VT_PAD_X, sizeof(float) * (size_t)mean->stride);
+    still_vectors(s, &B.l[0], 0, 1);
+    const int n = ((w + VT_CELL_W - 1) / VT_CELL_W) * ((h + VT_CELL_H - 1) / VT_CELL_H);
+    memcpy(cells, still_cells(s), sizeof(struct vt_cell) * (size_t)n);
+    release(&A);
+    release(&B);
+    return n;
+}
+
+/* A padded plane from an interior of whole-number values, its border replicated as img_pad_rows / img_pad_tb do. */
+static struct vt_plane plane_from(const float *interior, int w, int h)
+{
+    struct vt_plane pl = new_plane(w, h);
+    for (int y = 0; y < h; y++)
+        memcpy(plane_row(&pl, y), interior + (size_t)y * w, sizeof(float) * (size_t)w);
+    img_pad_rows(&pl, 0, h);
+    img_pad_tb(&pl);
+    return pl;
+}
+
+/* tk_correlate (src/kern/track.c:208) at each of n corners of a 32 x 21 template. */
+void ref_correlate(const float *interior, int w, int h, const float *app, double norm, int n, const int *xs, const int *ys, double *out)
+{
+    struct vt_plane pl = plane_from(interior, w, h);
+    for (int i = 0; i < n; i++)
+        out[i] = (double)tk_correlate(&pl, app, (long double)norm, xs[i], ys[i]);
+    free_plane(&pl);
+}

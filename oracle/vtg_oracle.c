@@ -1,0 +1,887 @@
+/* vtg_oracle.c -- TEST INFRASTRUCTURE ONLY. Nothing in the library links or loads this file: tests/, the smoke
+ * check and bench.py's cpu_baseline leg are its only users, and only as the checker.
+ *
+ * A CPU restatement of the reference's sparse pyramidal Lucas-Kanade path (Lasimeri/Intel-Phi-VisionTrack), in this
+ * project's own code, for checking the CUDA kernels:
+ *   - the pyramid: u8 -> Q6 (src/kern/img_ref.c:32-40) and the 5 x 5 binomial reduce with clamp-to-edge borders
+ *     (src/kern/img_ref.c:9-30, 74-114); exact integers;
+ *   - one point of pyramidal LK: the driver of src/kern/lk_driver.inc:7-109 and the three patch operations of
+ *     src/kern/lk_vx.c:36-175, and the forward-backward check (src/kern/lk_driver.inc:111-121);
+ *   - the per-cell grid of src/kern/still.c:116-141, generalised to any cell size and patch;
+ *   - the appearance correlation of src/kern/track.c:184-206, its half-pixel form (track.c:1615-1647), the parabola
+ *     (track.c:1650-1657), the per-cell map (track.c:301-329) and the top-8 search (track.c:1661-1726), generalised to
+ *     a T_w x T_h template (T_w a multiple of 16).
+ *
+ * Two arithmetics for everything that is floating point:
+ *   OR_LANE  the reference's replay arithmetic: F32 patch sums in 16 lanes, each lane a chain of fused multiply-adds in
+ *            row order, the lanes folded by the butterfly i^1, i^2, i^4, i^8 (src/common/vx.h:158-221), and the
+ *            driver in long double. With gcc on x86-64 long double is the x87 80-bit format the reference was built
+ *            with, so this mode reproduces the reference's golden LK hashes (logs/m2/host/640x480.txt) bit for bit.
+ *            On another architecture long double differs and the mode is only close.
+ *   OR_F64   every sample, sum and driver step in double: the FP64 oracle that flow tolerances are stated against.
+ *            Window sums of the correlation are exact integers (or exact quarter-integers) in this mode.
+ * Integer work (u8 -> Q6, the reduce) is exact and mode-free.
+ *
+ * Must be built with -ffp-contract=off: a * b + c stays two roundings unless fmaf/fma is written out. */
+#include <math.h>
+#include <pthread.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define OR_LANE 0
+#define OR_F64 1
+#define OR_MAX_LEVELS 8
+#define OR_MAX_W 48
+#define OR_MAX_H 31
+
+enum { OR_OK = 0, OR_OUT = 1, OR_LOWEIG = 2, OR_RESIDUAL = 4, OR_FLOWBACK = 8 };
+
+/* A pyramid: level k is w[k] x h[k] Q6 values, rows stride[k] floats apart. Level k + 1 is (w + 1) / 2 x (h + 1) / 2. */
+struct or_pyr {
+    int levels;
+    int w[OR_MAX_LEVELS], h[OR_MAX_LEVELS], stride[OR_MAX_LEVELS];
+    const float *lv[OR_MAX_LEVELS];
+};
+
+/* The LK parameters of struct lk_cfg (src/kern/lk.h:24-31). */
+struct or_lk_cfg {
+    int w, h, max_iter;
+    float eps, min_eig, max_residual;
+};
+
+/* struct lk_out (src/kern/lk.h:33-40), byte for byte: 32 bytes. */
+struct or_lk_out {
+    float x, y, min_eig, residual, cov_xx, cov_xy, cov_yy;
+    uint16_t iters, status;
+};
+
+/* struct vt_cell (src/common/vt_proto.h:395-402): 24 bytes. */
+struct or_cell {
+    float u, v, diff;
+    uint32_t state;
+    float sigma, pad;
+};
+
+/* ---------------------------------------------------------------- hashing, for the reference's golden logs */
+
+/* 64-bit FNV-1a, the hash the reference's gates print (src/common/vt_util.h:29-38). */
+uint64_t or_fnv(uint64_t h, const void *p, size_t n)
+{
+    const uint8_t *b = p;
+    for (size_t i = 0; i < n; i++) {
+        h ^= b[i];
+        h *= 0x100000001b3ull;
+    }
+    return h;
+}
+
+/* ---------------------------------------------------------------- the pyramid, exact integers */
+
+/* Q6 = byte x 64 (src/kern/img_ref.c:32-40). dst: w x h, rows dst_stride floats apart. */
+void or_u8_to_q6(const uint8_t *src, int src_stride, int w, int h, float *dst, int dst_stride)
+{
+    for (int y = 0; y < h; y++)
+        for (int x = 0; x < w; x++)
+            dst[(size_t)y * dst_stride + x] = (float)(src[(size_t)y * src_stride + x] * 64);
+}
+
+static inline int clampi(int v, int lo, int hi) { return v < lo ? lo : v > hi ? hi : v; }
+
+/* One pyramid step: (1 4 6 4 1)^2 / 256 at every second pixel of every second row, rounded as (sum + 128) >> 8
+ * (src/kern/img_ref.c:98-114). The reference reads its replicated border (img_pad_rows / img_pad_tb, img_ref.c:9-30):
+ * here that is a clamped index. Every value is a whole number below 2^24, so the integer sum is the F32 sum exactly. */
+void or_reduce(const float *src, int w, int h, int src_stride, float *dst, int dst_stride)
+{
+    static const int k[5] = {1, 4, 6, 4, 1};
+    const int dw = (w + 1) / 2, dh = (h + 1) / 2;
+    for (int y = 0; y < dh; y++)
+        for (int x = 0; x < dw; x++) {
+            int64_t s = 0;
+            for (int j = -2; j <= 2; j++) {
+                const float *row = src + (size_t)clampi(2 * y + j, 0, h - 1) * src_stride;
+                for (int i = -2; i <= 2; i++)
+                    s += (int64_t)k[j + 2] * k[i + 2] * (int64_t)row[clampi(2 * x + i, 0, w - 1)];
+            }
+            dst[(size_t)y * dst_stride + x] = (float)((s + 128) >> 8);
+        }
+}
+
+/* ---------------------------------------------------------------- lane arithmetic */
+
+static float hsum16(const float *in)
+{
+    float v[16], t[16];
+    memcpy(v, in, sizeof v);
+    for (int s = 1; s <= 8; s <<= 1) {
+        for (int i = 0; i < 16; i++)
+            t[i] = v[i] + v[i ^ s];
+        memcpy(v, t, sizeof v);
+    }
+    return v[0];
+}
+
+static inline float px_at(const struct or_pyr *p, int L, long x, long y) { return p->lv[L][(size_t)y * p->stride[L] + x]; }
+
+/* The patch state one level's build leaves for its iterations: T, Tx, Ty in lane-model F32, or in double. */
+struct or_tile {
+    float t[OR_MAX_H][OR_MAX_W], tx[OR_MAX_H][OR_MAX_W], ty[OR_MAX_H][OR_MAX_W];
+    double dt[OR_MAX_H][OR_MAX_W], dtx[OR_MAX_H][OR_MAX_W], dty[OR_MAX_H][OR_MAX_W];
+};
+
+/* build_vx (src/kern/lk_vx.c:36-97): the window of I around (px, py) at the patch's sub-pixel phase, the Sobel
+ * gradients scaled by 1/512, and the structure tensor's sums, lane by lane. */
+static void build_lane(const struct or_pyr *I, int L, long double px, long double py, const struct or_lk_cfg *c, struct or_tile *t, float g[3])
+{
+    const long ix = (long)floorl(px), iy = (long)floorl(py);
+    const float fx = (float)(px - (long double)ix), fy = (float)(py - (long double)iy);
+    const int W = c->w, H = c->h;
+    const long x0 = ix - W / 2, y0 = iy - H / 2;
+    float s[OR_MAX_H + 2][OR_MAX_W + 2], prev[OR_MAX_W + 2];
+    for (int j = -1; j <= W; j++) {
+        const float l = px_at(I, L, x0 + j, y0 - 1), n = px_at(I, L, x0 + j + 1, y0 - 1);
+        prev[j + 1] = fmaf(n - l, fx, l);
+    }
+    for (int r = 0; r < H + 2; r++)
+        for (int j = -1; j <= W; j++) {
+            const float l = px_at(I, L, x0 + j, y0 + r), n = px_at(I, L, x0 + j + 1, y0 + r);
+            const float cur = fmaf(n - l, fx, l);
+            s[r][j + 1] = fmaf(cur - prev[j + 1], fy, prev[j + 1]);
+            prev[j + 1] = cur;
+        }
+    float gxx[16] = {0}, gxy[16] = {0}, gyy[16] = {0};
+    const float gs = 1.0f / 512.0f;
+    for (int r = 0; r < H; r++) {
+        const float *u = s[r], *m = s[r + 1], *d = s[r + 2];
+        for (int j = 0; j < W; j++) {
+            const int i = j + 1, l = j & 15;
+            const float dxu = u[i + 1] - u[i - 1], dxm = m[i + 1] - m[i - 1], dxd = d[i + 1] - d[i - 1];
+            const float tx = fmaf(dxm, 2.0f, dxu + dxd) * gs;
+            const float dyl = d[i - 1] - u[i - 1], dyc = d[i] - u[i], dyr = d[i + 1] - u[i + 1];
+            const float ty = fmaf(dyc, 2.0f, dyl + dyr) * gs;
+            t->t[r][j] = m[i];
+            t->tx[r][j] = tx;
+            t->ty[r][j] = ty;
+            gxx[l] = fmaf(tx, tx, gxx[l]);
+            gxy[l] = fmaf(tx, ty, gxy[l]);
+            gyy[l] = fmaf(ty, ty, gyy[l]);
+        }
+    }
+    g[0] = hsum16(gxx);
+    g[1] = hsum16(gxy);
+    g[2] = hsum16(gyy);
+}
+
+/* iterate_vx (src/kern/lk_vx.c:100-140): J sampled at (qx, qy), It = T - J, the sums of It Tx and It Ty. */
+static void iterate_lane(const struct or_pyr *J, int L, long double qx, long double qy, const struct or_lk_cfg *c, const struct or_tile *t, float b[2])
+{
+    const long jx = (long)floorl(qx), jy = (long)floorl(qy);
+    const float fx = (float)(qx - (long double)jx), fy = (float)(qy - (long double)jy);
+    const int W = c->w, H = c->h;
+    const long x0 = jx - W / 2, y0 = jy - H / 2;
+    float prev[OR_MAX_W], bx[16] = {0}, by[16] = {0};
+    for (int j = 0; j < W; j++) {
+        const float l = px_at(J, L, x0 + j, y0), n = px_at(J, L, x0 + j + 1, y0);
+        prev[j] = fmaf(n - l, fx, l);
+    }
+    for (int r = 0; r < H; r++)
+        for (int j = 0; j < W; j++) {
+            const int l = j & 15;
+            const float a = px_at(J, L, x0 + j, y0 + r + 1), n = px_at(J, L, x0 + j + 1, y0 + r + 1);
+            const float cur = fmaf(n - a, fx, a);
+            const float it = t->t[r][j] - fmaf(cur - prev[j], fy, prev[j]);
+            bx[l] = fmaf(it, t->tx[r][j], bx[l]);
+            by[l] = fmaf(it, t->ty[r][j], by[l]);
+            prev[j] = cur;
+        }
+    b[0] = hsum16(bx);
+    b[1] = hsum16(by);
+}
+
+/* residual_vx (src/kern/lk_vx.c:142-175): mean |It| and mean It^2 in 8-bit grey. */
+static void residual_lane(const struct or_pyr *J, long double qx, long double qy, const struct or_lk_cfg *c, const struct or_tile *t, float out[2])
+{
+    const long jx = (long)floorl(qx), jy = (long)floorl(qy);
+    const float fx = (float)(qx - (long double)jx), fy = (float)(qy - (long double)jy);
+    const int W = c->w, H = c->h;
+    const long x0 = jx - W / 2, y0 = jy - H / 2;
+    float prev[OR_MAX_W], sa[16] = {0}, ss[16] = {0};
+    for (int j = 0; j < W; j++) {
+        const float l = px_at(J, 0, x0 + j, y0), n = px_at(J, 0, x0 + j + 1, y0);
+        prev[j] = fmaf(n - l, fx, l);
+    }
+    for (int r = 0; r < H; r++)
+        for (int j = 0; j < W; j++) {
+            const int l = j & 15;
+            const float a = px_at(J, 0, x0 + j, y0 + r + 1), n = px_at(J, 0, x0 + j + 1, y0 + r + 1);
+            const float cur = fmaf(n - a, fx, a);
+            const float it = (t->t[r][j] - fmaf(cur - prev[j], fy, prev[j])) * (1.0f / 64.0f);
+            sa[l] = sa[l] + fabsf(it);
+            ss[l] = fmaf(it, it, ss[l]);
+            prev[j] = cur;
+        }
+    const long double n = (long double)(W * H);
+    out[0] = (float)((long double)hsum16(sa) / n);
+    out[1] = (float)((long double)hsum16(ss) / n);
+}
+
+/* ---------------------------------------------------------------- the same three operations in double */
+
+static inline double lerp2(const struct or_pyr *p, int L, long x, long y, double fx, double fy)
+{
+    const double a = px_at(p, L, x, y), b = px_at(p, L, x + 1, y), c = px_at(p, L, x, y + 1), d = px_at(p, L, x + 1, y + 1);
+    const double top = a + fx * (b - a), bot = c + fx * (d - c);
+    return top + fy * (bot - top);
+}
+
+static void build_f64(const struct or_pyr *I, int L, double px, double py, const struct or_lk_cfg *c, struct or_tile *t, double g[3])
+{
+    const long ix = (long)floor(px), iy = (long)floor(py);
+    const double fx = px - (double)ix, fy = py - (double)iy;
+    const int W = c->w, H = c->h;
+    const long x0 = ix - W / 2, y0 = iy - H / 2;
+    double s[OR_MAX_H + 2][OR_MAX_W + 2];
+    for (int r = 0; r < H + 2; r++)
+        for (int j = -1; j <= W; j++)
+            s[r][j + 1] = lerp2(I, L, x0 + j, y0 - 1 + r, fx, fy);
+    double gxx = 0, gxy = 0, gyy = 0;
+    for (int r = 0; r < H; r++) {
+        const double *u = s[r], *m = s[r + 1], *d = s[r + 2];
+        for (int j = 0; j < W; j++) {
+            const int i = j + 1;
+            const double tx = ((u[i + 1] - u[i - 1]) + 2.0 * (m[i + 1] - m[i - 1]) + (d[i + 1] - d[i - 1])) / 512.0;
+            const double ty = ((d[i - 1] - u[i - 1]) + 2.0 * (d[i] - u[i]) + (d[i + 1] - u[i + 1])) / 512.0;
+            t->dt[r][j] = m[i];
+            t->dtx[r][j] = tx;
+            t->dty[r][j] = ty;
+            gxx += tx * tx;
+            gxy += tx * ty;
+            gyy += ty * ty;
+        }
+    }
+    g[0] = gxx;
+    g[1] = gxy;
+    g[2] = gyy;
+}
+
+static void iterate_f64(const struct or_pyr *J, int L, double qx, double qy, const struct or_lk_cfg *c, const struct or_tile *t, double b[2])
+{
+    const long jx = (long)floor(qx), jy = (long)floor(qy);
+    const double fx = qx - (double)jx, fy = qy - (double)jy;
+    const long x0 = jx - c->w / 2, y0 = jy - c->h / 2;
+    double bx = 0, by = 0;
+    for (int r = 0; r < c->h; r++)
+        for (int j = 0; j < c->w; j++) {
+            const double it = t->dt[r][j] - lerp2(J, L, x0 + j, y0 + r, fx, fy);
+            bx += it * t->dtx[r][j];
+            by += it * t->dty[r][j];
+        }
+    b[0] = bx;
+    b[1] = by;
+}
+
+static void residual_f64(const struct or_pyr *J, double qx, double qy, const struct or_lk_cfg *c, const struct or_tile *t, double out[2])
+{
+    const long jx = (long)floor(qx), jy = (long)floor(qy);
+    const double fx = qx - (double)jx, fy = qy - (double)jy;
+    const long x0 = jx - c->w / 2, y0 = jy - c->h / 2;
+    double sa = 0, ss = 0;
+    for (int r = 0; r < c->h; r++)
+        for (int j = 0; j < c->w; j++) {
+            const double it = (t->dt[r][j] - lerp2(J, 0, x0 + j, y0 + r, fx, fy)) / 64.0;
+            sa += fabs(it);
+            ss += it * it;
+        }
+    const double n = (double)(c->w * c->h);
+    out[0] = sa / n;
+    out[1] = ss / n;
+}
+
+/* ---------------------------------------------------------------- the pyramid walk (src/kern/lk_driver.inc:7-109) */
+
+/* The driver, once per arithmetic. REAL is the driver's scalar type, G the type of the patch sums. */
+#define OR_DRIVER(NAME, REAL, G, BUILD, ITERATE, RESIDUAL, FLOOR, SQRT)                                                      \
+    static void NAME(const struct or_pyr *I, const struct or_pyr *J, int top, const struct or_lk_cfg *c, float x, float y,  \
+                     float gx0, float gy0, struct or_lk_out *o, struct or_tile *tile)                                        \
+    {                                                                                                                         \
+        const REAL scale_top = (REAL)1 / (REAL)(1 << top);                                                                   \
+        REAL gx = (REAL)gx0 * scale_top, gy = (REAL)gy0 * scale_top;                                                         \
+        const REAL area = (REAL)(c->w * c->h);                                                                               \
+        const REAL eps2 = (REAL)c->eps * (REAL)c->eps;                                                                       \
+        REAL det0 = 0, gxx0 = 0, gxy0 = 0, gyy0 = 0;                                                                         \
+        int status = 0, iters = 0, valid0 = 0;                                                                               \
+        float eig0 = 0.0f;                                                                                                    \
+        const int mx = c->w / 2 + 1, my = c->h / 2 + 1;                                                                     \
+        for (int L = top; L >= 0; L--) {                                                                                      \
+            const REAL s = (REAL)1 / (REAL)(1 << L);                                                                         \
+            const REAL px = (REAL)x * s, py = (REAL)y * s;                                                                   \
+            const REAL last_x = (REAL)(I->w[L] - mx - 1), last_y = (REAL)(I->h[L] - my - 1);                                 \
+            if (px < mx || py < my || px >= last_x || py >= last_y) {                                                        \
+                if (L == 0)                                                                                                   \
+                    status |= OR_OUT;                                                                                         \
+                else {                                                                                                        \
+                    gx *= 2;                                                                                                  \
+                    gy *= 2;                                                                                                  \
+                }                                                                                                             \
+                continue;                                                                                                     \
+            }                                                                                                                 \
+            G g[3];                                                                                                           \
+            BUILD(I, L, px, py, c, tile, g);                                                                                  \
+            const REAL gxx = g[0], gxy = g[1], gyy = g[2];                                                                   \
+            const REAL det = gxx * gyy - gxy * gxy;                                                                          \
+            const REAL tr = gxx + gyy, diff = gxx - gyy;                                                                     \
+            const REAL eig = (tr - SQRT(diff * diff + 4 * gxy * gxy)) * (REAL)0.5 / area;                                    \
+            if (L == 0)                                                                                                       \
+                eig0 = (float)eig;                                                                                            \
+            if (eig < (REAL)c->min_eig || det <= 0) {                                                                        \
+                if (L == 0)                                                                                                   \
+                    status |= OR_LOWEIG;                                                                                      \
+                else {                                                                                                        \
+                    gx *= 2;                                                                                                  \
+                    gy *= 2;                                                                                                  \
+                }                                                                                                             \
+                continue;                                                                                                     \
+            }                                                                                                                 \
+            if (L == 0) {                                                                                                     \
+                det0 = det;                                                                                                   \
+                gxx0 = gxx;                                                                                                   \
+                gxy0 = gxy;                                                                                                   \
+                gyy0 = gyy;                                                                                                   \
+                valid0 = 1;                                                                                                   \
+            }                                                                                                                 \
+            const REAL ia = gyy / det, ib = -gxy / det, ic = gxx / det;                                                      \
+            REAL vx = 0, vy = 0;                                                                                              \
+            for (int it = 0; it < c->max_iter; it++) {                                                                        \
+                const REAL qxl = px + gx + vx, qyl = py + gy + vy;                                                           \
+                const REAL lx = (REAL)(J->w[L] - mx - 1), ly = (REAL)(J->h[L] - my - 1);                                     \
+                if (qxl < mx || qyl < my || qxl >= lx || qyl >= ly) {                                                        \
+                    if (L == 0) {                                                                                             \
+                        status |= OR_OUT;                                                                                     \
+                        valid0 = 0;                                                                                           \
+                    }                                                                                                         \
+                    break;                                                                                                    \
+                }                                                                                                             \
+                G b[2];                                                                                                       \
+                ITERATE(J, L, qxl, qyl, c, tile, b);                                                                          \
+                const REAL bx = (REAL)b[0] / 64, by = (REAL)b[1] / 64;                                                       \
+                const REAL ex = ia * bx + ib * by, ey = ib * bx + ic * by;                                                   \
+                vx += ex;                                                                                                     \
+                vy += ey;                                                                                                     \
+                iters++;                                                                                                      \
+                if (ex * ex + ey * ey < eps2)                                                                                 \
+                    break;                                                                                                    \
+            }                                                                                                                 \
+            gx += vx;                                                                                                         \
+            gy += vy;                                                                                                         \
+            if (L > 0) {                                                                                                      \
+                gx *= 2;                                                                                                      \
+                gy *= 2;                                                                                                      \
+            }                                                                                                                 \
+        }                                                                                                                     \
+        const REAL qx = (REAL)x + gx, qy = (REAL)y + gy;                                                                     \
+        o->x = (float)qx;                                                                                                     \
+        o->y = (float)qy;                                                                                                     \
+        o->min_eig = eig0;                                                                                                    \
+        o->iters = (uint16_t)iters;                                                                                           \
+        o->residual = 0.0f;                                                                                                   \
+        o->cov_xx = o->cov_xy = o->cov_yy = 0.0f;                                                                             \
+        if (valid0 && !status) {                                                                                              \
+            if (qx < mx || qy < my || qx >= (REAL)(J->w[0] - mx - 1) || qy >= (REAL)(J->h[0] - my - 1)) {                    \
+                status |= OR_OUT;                                                                                             \
+            } else {                                                                                                          \
+                G r[2];                                                                                                       \
+                RESIDUAL(J, qx, qy, c, tile, r);                                                                              \
+                o->residual = (float)r[0];                                                                                    \
+                if (r[0] > c->max_residual)                                                                                   \
+                    status |= OR_RESIDUAL;                                                                                    \
+                const REAL s2 = (REAL)r[1] * area / (area - 2);                                                              \
+                o->cov_xx = (float)(s2 * gyy0 / det0);                                                                        \
+                o->cov_xy = (float)(-s2 * gxy0 / det0);                                                                       \
+                o->cov_yy = (float)(s2 * gxx0 / det0);                                                                        \
+            }                                                                                                                 \
+        }                                                                                                                     \
+        o->status = (uint16_t)status;                                                                                         \
+    }
+
+OR_DRIVER(track_lane, long double, float, build_lane, iterate_lane, residual_lane, floorl, sqrtl)
+OR_DRIVER(track_f64, double, double, build_f64, iterate_f64, residual_f64, floor, sqrt)
+
+static void track_mode(const struct or_pyr *I, const struct or_pyr *J, int top, const struct or_lk_cfg *c, float x, float y, float gx, float gy, struct or_lk_out *o, struct or_tile *tile, int mode)
+{
+    if (mode == OR_F64)
+        track_f64(I, J, top, c, x, y, gx, gy, o, tile);
+    else
+        track_lane(I, J, top, c, x, y, gx, gy, o, tile);
+}
+
+/* lk_flowback (src/kern/lk_driver.inc:111-121): track the found point back from J to I, from minus the found flow; a
+ * miss beyond max_fb, or a failed return, flags the point. */
+static void flowback_mode(const struct or_pyr *I, const struct or_pyr *J, int top, const struct or_lk_cfg *c, float x, float y, float max_fb, struct or_lk_out *o, struct or_tile *tile, int mode)
+{
+    if (o->status)
+        return;
+    struct or_lk_out b;
+    if (mode == OR_F64) {
+        track_f64(J, I, top, c, o->x, o->y, (float)((double)x - (double)o->x), (float)((double)y - (double)o->y), &b, tile);
+        const double ex = (double)b.x - (double)x, ey = (double)b.y - (double)y;
+        if (b.status || ex * ex + ey * ey > (double)max_fb * (double)max_fb)
+            o->status |= OR_FLOWBACK;
+    } else {
+        track_lane(J, I, top, c, o->x, o->y, (float)((long double)x - (long double)o->x), (float)((long double)y - (long double)o->y), &b, tile);
+        const long double ex = (long double)b.x - (long double)x, ey = (long double)b.y - (long double)y;
+        if (b.status || ex * ex + ey * ey > (long double)max_fb * (long double)max_fb)
+            o->status |= OR_FLOWBACK;
+    }
+}
+
+void or_lk_track(const struct or_pyr *I, const struct or_pyr *J, int top, const struct or_lk_cfg *c, float x, float y, float gx, float gy, float max_fb, struct or_lk_out *o, int mode)
+{
+    struct or_tile *tile = malloc(sizeof *tile);
+    track_mode(I, J, top, c, x, y, gx, gy, o, tile, mode);
+    if (max_fb > 0.0f)
+        flowback_mode(I, J, top, c, x, y, max_fb, o, tile, mode);
+    free(tile);
+}
+
+/* ---------------------------------------------------------------- points and cells, on a team of threads */
+
+/* A cell's centre: (cw c + cw / 2, ch r + ch / 2), clamped to where the patch still fits (src/kern/still.c:127-130,
+ * whose margin of 9 is a 15-pixel patch's half plus 2; here it is the configured patch's). */
+void or_cell_centre(int w, int h, int cell_w, int cell_h, const struct or_lk_cfg *c, int col, int row, float *x, float *y)
+{
+    const float mx = (float)(c->w / 2 + 2), my = (float)(c->h / 2 + 2);
+    const float x_max = (float)w - 1.0f - mx, y_max = (float)h - 1.0f - my;
+    float cx = (float)(col * cell_w + cell_w / 2), cy = (float)(row * cell_h + cell_h / 2);
+    cx = cx < mx ? mx : cx > x_max ? x_max : cx;
+    cy = cy < my ? my : cy > y_max ? y_max : cy;
+    *x = cx;
+    *y = cy;
+}
+
+/* Mean |J - I| over a cell of level 0, 8-bit grey (src/kern/still.c:105-114): row sums folded as the lane model folds
+ * 16 lanes, in long double across rows. A cell past the picture's edge reads the replicated border. */
+static float cell_diff(const struct or_pyr *I, const struct or_pyr *J, int cell_w, int cell_h, int col, int row, int mode)
+{
+    const int w = I->w[0], h = I->h[0];
+    const int x = col * cell_w, y0 = row * cell_h, y1 = y0 + cell_h < h ? y0 + cell_h : h;
+    long double sum = 0.0L;
+    for (int y = y0; y < y1; y++) {
+        float lanes[16] = {0};
+        double rs = 0.0;
+        for (int k = 0; k < cell_w; k++) {
+            const int xx = clampi(x + k, 0, w - 1);
+            const float d = fabsf(px_at(J, 0, xx, y) - px_at(I, 0, xx, y));
+            lanes[k & 15] = lanes[k & 15] + d;
+            rs += d;
+        }
+        sum += mode == OR_F64 ? (long double)rs : (long double)hsum16(lanes);
+    }
+    return (float)(sum / (long double)((y1 - y0) * cell_w) / 64.0L);
+}
+
+struct team_job {
+    const struct or_pyr *I, *J;
+    const struct or_lk_cfg *c;
+    int top, mode, n;
+    float max_fb;
+    /* points */
+    const float *xs, *ys, *gxs, *gys;
+    /* cells */
+    int cell_w, cell_h, cols;
+    struct or_lk_out *out;
+    struct or_cell *cells;
+    int next;
+};
+
+static void *team_points(void *arg)
+{
+    struct team_job *j = arg;
+    struct or_tile *tile = malloc(sizeof *tile);
+    for (;;) {
+        const int i = __atomic_fetch_add(&j->next, 1, __ATOMIC_RELAXED);
+        if (i >= j->n)
+            break;
+        track_mode(j->I, j->J, j->top, j->c, j->xs[i], j->ys[i], j->gxs ? j->gxs[i] : 0.0f, j->gys ? j->gys[i] : 0.0f, &j->out[i], tile, j->mode);
+        if (j->max_fb > 0.0f)
+            flowback_mode(j->I, j->J, j->top, j->c, j->xs[i], j->ys[i], j->max_fb, &j->out[i], tile, j->mode);
+    }
+    free(tile);
+    return NULL;
+}
+
+/* The per-cell grid of still_vectors (src/kern/still.c:116-141): LK from I to J at each cell's centre, the
+ * forward-backward check when max_fb > 0, then the cell record. */
+static void *team_cells(void *arg)
+{
+    struct team_job *j = arg;
+    struct or_tile *tile = malloc(sizeof *tile);
+    for (;;) {
+        const int i = __atomic_fetch_add(&j->next, 1, __ATOMIC_RELAXED);
+        if (i >= j->n)
+            break;
+        const int col = i % j->cols, row = i / j->cols;
+        float x, y;
+        or_cell_centre(j->I->w[0], j->I->h[0], j->cell_w, j->cell_h, j->c, col, row, &x, &y);
+        struct or_lk_out o;
+        track_mode(j->I, j->J, j->top, j->c, x, y, 0.0f, 0.0f, &o, tile, j->mode);
+        if (j->max_fb > 0.0f)
+            flowback_mode(j->I, j->J, j->top, j->c, x, y, j->max_fb, &o, tile, j->mode);
+        if (j->out)
+            j->out[i] = o;
+        if (j->cells) {
+            struct or_cell *cl = &j->cells[i];
+            cl->u = (float)((long double)o.x - (long double)x);
+            cl->v = (float)((long double)o.y - (long double)y);
+            cl->diff = cell_diff(j->I, j->J, j->cell_w, j->cell_h, col, row, j->mode);
+            cl->state = o.status;
+            cl->sigma = o.status ? 0.0f : (float)sqrtl((long double)o.cov_xx + (long double)o.cov_yy);
+            cl->pad = 0.0f;
+        }
+    }
+    free(tile);
+    return NULL;
+}
+
+static void run_team(void *(*fn)(void *), struct team_job *j, int threads)
+{
+    if (threads < 1)
+        threads = 1;
+    j->next = 0;
+    if (threads == 1) {
+        fn(j);
+        return;
+    }
+    pthread_t *th = malloc(sizeof *th * (size_t)threads);
+    for (int i = 0; i < threads; i++)
+        pthread_create(&th[i], NULL, fn, j);
+    for (int i = 0; i < threads; i++)
+        pthread_join(th[i], NULL);
+    free(th);
+}
+
+/* Points with their own guesses (the tracker's OP_LK, src/kern/track.c:275-292). gxs / gys may be NULL. */
+void or_lk_points(const struct or_pyr *I, const struct or_pyr *J, int top, const struct or_lk_cfg *c, int n, const float *xs, const float *ys, const float *gxs, const float *gys, float max_fb, struct or_lk_out *out, int mode, int threads)
+{
+    struct team_job j = {.I = I, .J = J, .c = c, .top = top, .mode = mode, .n = n, .max_fb = max_fb, .xs = xs, .ys = ys, .gxs = gxs, .gys = gys, .out = out};
+    run_team(team_points, &j, threads);
+}
+
+/* The cell grid over level 0 of I and J: ceil(w / cell_w) x ceil(h / cell_h) cells, row-major. out or cells may be NULL. */
+void or_cells(const struct or_pyr *I, const struct or_pyr *J, int top, const struct or_lk_cfg *c, int cell_w, int cell_h, float max_fb, struct or_lk_out *out, struct or_cell *cells, int mode, int threads)
+{
+    const int cols = (I->w[0] + cell_w - 1) / cell_w, rows = (I->h[0] + cell_h - 1) / cell_h;
+    struct team_job j = {.I = I, .J = J, .c = c, .top = top, .mode = mode, .n = cols * rows, .max_fb = max_fb, .cell_w = cell_w, .cell_h = cell_h, .cols = cols, .out = out, .cells = cells};
+    run_team(team_cells, &j, threads);
+}
+
+/* ---------------------------------------------------------------- the appearance correlation */
+
+/* A plane for the correlation: Q6 (or 8-bit) whole-number values, w x h, rows stride floats apart. */
+struct or_img {
+    const float *p;
+    int w, h, stride;
+};
+
+static inline float im_at(const struct or_img *m, int x, int y) { return m->p[(size_t)y * m->stride + x]; }
+
+/* search_at (src/kern/track.c:184-206) for a T_w x T_h zero-mean template at corner (x, y): st = sum t v, with
+ * v = J - J(x, y); var = sum v^2 - (sum v)^2 / n; 0 when var <= norm / 16 or norm <= 0, else st / sqrt(norm var);
+ * -1 where the template does not fit inside a one-pixel margin. */
+double or_ncc_at(const struct or_img *m, const float *app, int tw, int th, double norm, int x, int y, int mode)
+{
+    if (x < 1 || y < 1 || x + tw >= m->w - 1 || y + th >= m->h - 1)
+        return -1.0;
+    const int n = tw * th;
+    if (mode == OR_F64) {
+        /* Exact window sums of whole numbers, the product sum in double (each term exact, the sum all but exact). */
+        int64_t s1 = 0, s2 = 0;
+        double st = 0.0, ts = 0.0;
+        for (int r = 0; r < th; r++)
+            for (int k = 0; k < tw; k++) {
+                const int64_t v = (int64_t)im_at(m, x + k, y + r);
+                s1 += v;
+                s2 += v * v;
+                st += (double)app[r * tw + k] * (double)v;
+                ts += (double)app[r * tw + k];
+            }
+        st -= ts * (double)im_at(m, x, y);
+        const double nvar = (double)((int64_t)n * s2 - s1 * s1); /* n var, exact */
+        if (nvar <= (double)n * norm * 0.0625 || norm <= 0.0)
+            return 0.0;
+        return st / sqrt(norm * (nvar / (double)n));
+    }
+    const float first = im_at(m, x, y);
+    float st[16] = {0}, sj[16] = {0}, sjj[16] = {0};
+    for (int r = 0; r < th; r++)
+        for (int k = 0; k < tw; k++) {
+            const int l = k & 15;
+            const float v = im_at(m, x + k, y + r) - first;
+            st[l] = fmaf(v, app[r * tw + k], st[l]);
+            sj[l] = sj[l] + v;
+            sjj[l] = fmaf(v, v, sjj[l]);
+        }
+    const long double nn = (long double)n, nt = (long double)norm;
+    const long double a = hsum16(st), b = hsum16(sj), c = hsum16(sjj);
+    const long double var = c - b * b / nn;
+    return (double)((var <= nt * 0.0625L || nt <= 0.0L) ? 0.0L : a / sqrtl(nt * var));
+}
+
+/* search_half (src/kern/track.c:1615-1647): the corner in half pixels; an odd half step averages the two neighbours. */
+double or_ncc_half(const struct or_img *m, const float *app, int tw, int th, double norm, int hx, int hy, int mode)
+{
+    const int x = hx >> 1, y = hy >> 1, ox = hx & 1, oy = hy & 1;
+    if (x < 1 || y < 1 || x + tw + 1 >= m->w - 1 || y + th + 1 >= m->h - 1)
+        return -1.0;
+    const int n = tw * th;
+    if (mode == OR_F64) {
+        /* In quarters: every sample is a whole number of quarters, so the sums are exact. */
+        int64_t s1 = 0, s2 = 0;
+        double st = 0.0, ts = 0.0;
+        for (int r = 0; r < th; r++)
+            for (int k = 0; k < tw; k++) {
+                int64_t q = 4 * (int64_t)im_at(m, x + k, y + r);
+                if (ox)
+                    q = 2 * ((int64_t)im_at(m, x + k, y + r) + (int64_t)im_at(m, x + k + 1, y + r));
+                if (oy) {
+                    int64_t b = 4 * (int64_t)im_at(m, x + k, y + r + 1);
+                    if (ox)
+                        b = 2 * ((int64_t)im_at(m, x + k, y + r + 1) + (int64_t)im_at(m, x + k + 1, y + r + 1));
+                    q = (q + b) / 2;
+                }
+                s1 += q;
+                s2 += q * q;
+                st += (double)app[r * tw + k] * (double)q * 0.25;
+                ts += (double)app[r * tw + k];
+            }
+        st -= ts * (double)im_at(m, x, y);
+        const double nvar = (double)((int64_t)n * s2 - s1 * s1) / 16.0;
+        if (nvar <= (double)n * norm * 0.0625 || norm <= 0.0)
+            return 0.0;
+        return st / sqrt(norm * (nvar / (double)n));
+    }
+    const float first = im_at(m, x, y);
+    float st[16] = {0}, sj[16] = {0}, sjj[16] = {0};
+    for (int r = 0; r < th; r++)
+        for (int k = 0; k < tw; k++) {
+            const int l = k & 15;
+            float v = im_at(m, x + k, y + r);
+            if (ox)
+                v = (v + im_at(m, x + k + 1, y + r)) * 0.5f;
+            if (oy) {
+                float w = im_at(m, x + k, y + r + 1);
+                if (ox)
+                    w = (w + im_at(m, x + k + 1, y + r + 1)) * 0.5f;
+                v = (v + w) * 0.5f;
+            }
+            v = v - first;
+            st[l] = fmaf(v, app[r * tw + k], st[l]);
+            sj[l] = sj[l] + v;
+            sjj[l] = fmaf(v, v, sjj[l]);
+        }
+    const long double nn = (long double)n, nt = (long double)norm;
+    const long double a = hsum16(st), b = hsum16(sj), c = hsum16(sjj);
+    const long double var = c - b * b / nn;
+    return (double)((var <= nt * 0.0625L || nt <= 0.0L) ? 0.0L : a / sqrtl(nt * var));
+}
+
+/* peak_offset (src/kern/track.c:1650-1657): the vertex of a parabola through three scores, within half a step. */
+double or_peak_offset(double l, double c, double r)
+{
+    const long double den = (long double)l - 2.0L * (long double)c + (long double)r;
+    if (den >= 0.0L)
+        return 0.0;
+    const long double o = 0.5L * ((long double)l - (long double)r) / den;
+    return (double)(o < -0.5L ? -0.5L : o > 0.5L ? 0.5L : o);
+}
+
+/* The zero-mean template store_appearance cuts (src/kern/track.c:935-974): T_w x T_h pixels at corner (x0, y0), their
+ * mean (lane sums, long double division) taken off, norm = the lane-folded sum of squares. */
+void or_cut_template(const struct or_img *m, int x0, int y0, int tw, int th, float *app, float *norm)
+{
+    float sum[16] = {0};
+    for (int r = 0; r < th; r++)
+        for (int k = 0; k < tw; k++) {
+            const float v = im_at(m, x0 + k, y0 + r);
+            app[r * tw + k] = v;
+            sum[k & 15] = sum[k & 15] + v;
+        }
+    const float mean = (float)((long double)hsum16(sum) / (long double)(tw * th));
+    float ss[16] = {0};
+    for (int r = 0; r < th; r++)
+        for (int k = 0; k < tw; k++) {
+            const float z = app[r * tw + k] - mean;
+            app[r * tw + k] = z;
+            ss[k & 15] = fmaf(z, z, ss[k & 15]);
+        }
+    *norm = hsum16(ss);
+}
+
+/* What one search found (struct found, src/kern/track.c:1608-1612): the best corner in half pixels, its score, the best
+ * score clear of it, and the parabola's sub-half-pixel offsets around it (take_back, track.c:1741-1742). */
+struct or_found {
+    int hx, hy;
+    double ncc, second, ox, oy;
+};
+
+#define OR_SEARCH_CELL 16
+#define OR_SEARCH_TOP 8
+
+/* search_slot (src/kern/track.c:1661-1726) with the per-cell map of OP_SEARCH (track.c:301-329): the best corner of
+ * each 16 x 16 cell of corners at the given step, the eight best cells, each looked at again in half pixels within
+ * +-(2 step - 1) (or +-1), the best of those, and the best of the rest that stands half a template away. map_v, map_x,
+ * map_y (may be NULL) receive the per-cell map. */
+void or_search_slot(const struct or_img *m, const float *app, int tw, int th, double norm, int x0, int x1, int y0, int y1, int step, int mode, struct or_found *f, float *map_v, int *map_x, int *map_y)
+{
+    const int lo_x = 1, hi_x = m->w - tw - 2, lo_y = 1, hi_y = m->h - th - 2;
+    x0 = x0 < lo_x ? lo_x : x0;
+    x1 = x1 > hi_x ? hi_x : x1;
+    y0 = y0 < lo_y ? lo_y : y0;
+    y1 = y1 > hi_y ? hi_y : y1;
+    f->ncc = -2.0;
+    f->second = -2.0;
+    f->hx = f->hy = 0;
+    f->ox = f->oy = 0.0;
+    if (x1 < x0 || y1 < y0)
+        return;
+    const int ccols = (x1 - x0) / OR_SEARCH_CELL + 1, crows = (y1 - y0) / OR_SEARCH_CELL + 1, cells = ccols * crows;
+    float *sv = malloc(sizeof(float) * (size_t)cells);
+    int *sx = malloc(sizeof(int) * (size_t)cells), *sy = malloc(sizeof(int) * (size_t)cells);
+    for (int cell = 0; cell < cells; cell++) {
+        const int cy0 = y0 + (cell / ccols) * OR_SEARCH_CELL, cx0 = x0 + (cell % ccols) * OR_SEARCH_CELL;
+        const int cy1 = cy0 + OR_SEARCH_CELL <= y1 + 1 ? cy0 + OR_SEARCH_CELL : y1 + 1, cx1 = cx0 + OR_SEARCH_CELL <= x1 + 1 ? cx0 + OR_SEARCH_CELL : x1 + 1;
+        float best = -2.0f;
+        int bx = cx0, by = cy0;
+        for (int y = cy0; y < cy1; y += step)
+            for (int x = cx0; x < cx1; x += step) {
+                const float v = (float)or_ncc_at(m, app, tw, th, norm, x, y, mode);
+                if (v > best) {
+                    best = v;
+                    bx = x;
+                    by = y;
+                }
+            }
+        sv[cell] = best;
+        sx[cell] = bx;
+        sy[cell] = by;
+    }
+    if (map_v)
+        memcpy(map_v, sv, sizeof(float) * (size_t)cells);
+    if (map_x)
+        memcpy(map_x, sx, sizeof(int) * (size_t)cells);
+    if (map_y)
+        memcpy(map_y, sy, sizeof(int) * (size_t)cells);
+    int top[OR_SEARCH_TOP], ntop = 0;
+    for (int i = 0; i < cells; i++) {
+        if (sv[i] <= -2.0f || (ntop == OR_SEARCH_TOP && sv[i] <= sv[top[ntop - 1]]))
+            continue;
+        int at = ntop < OR_SEARCH_TOP ? ntop++ : OR_SEARCH_TOP - 1;
+        for (; at > 0 && sv[top[at - 1]] < sv[i]; at--)
+            top[at] = top[at - 1];
+        top[at] = i;
+    }
+    const int around = step > 1 ? 2 * step - 1 : 1;
+    double score[OR_SEARCH_TOP];
+    int shx[OR_SEARCH_TOP], shy[OR_SEARCH_TOP];
+    for (int c = 0; c < ntop; c++) {
+        const int cx = 2 * sx[top[c]], cy = 2 * sy[top[c]];
+        score[c] = -2.0;
+        shx[c] = cx;
+        shy[c] = cy;
+        for (int hy = cy - around; hy <= cy + around; hy++)
+            for (int hx = cx - around; hx <= cx + around; hx++) {
+                const double v = or_ncc_half(m, app, tw, th, norm, hx, hy, mode);
+                if (v > score[c]) {
+                    score[c] = v;
+                    shx[c] = hx;
+                    shy[c] = hy;
+                }
+            }
+        if (score[c] > f->ncc) {
+            f->ncc = score[c];
+            f->hx = shx[c];
+            f->hy = shy[c];
+        }
+    }
+    for (int c = 0; c < ntop; c++) {
+        const int dx = shx[c] - f->hx, dy = shy[c] - f->hy;
+        if ((dx * dx > tw * tw || dy * dy > th * th) && score[c] > f->second)
+            f->second = score[c];
+    }
+    if (ntop) {
+        f->ox = or_peak_offset(or_ncc_half(m, app, tw, th, norm, f->hx - 1, f->hy, mode), f->ncc, or_ncc_half(m, app, tw, th, norm, f->hx + 1, f->hy, mode));
+        f->oy = or_peak_offset(or_ncc_half(m, app, tw, th, norm, f->hx, f->hy - 1, mode), f->ncc, or_ncc_half(m, app, tw, th, norm, f->hx, f->hy + 1, mode));
+    }
+    free(sv);
+    free(sx);
+    free(sy);
+}
+
+/* Every corner's score over a window of corners (step 1), row-major: the dense map the whole-picture search computes.
+ * out: (x1 - x0 + 1) x (y1 - y0 + 1). */
+void or_ncc_map(const struct or_img *m, const float *app, int tw, int th, double norm, int x0, int x1, int y0, int y1, int mode, float *out, int threads)
+{
+    (void)threads;
+    const int cols = x1 - x0 + 1;
+    for (int y = y0; y <= y1; y++)
+        for (int x = x0; x <= x1; x++)
+            out[(size_t)(y - y0) * cols + (x - x0)] = (float)or_ncc_at(m, app, tw, th, norm, x, y, mode);
+}
+
+/* ---------------------------------------------------------------- the reference's deterministic test images */
+
+/* xorshift64* (src/common/vt_util.h:40-49). */
+static inline uint64_t or_rand(uint64_t *s)
+{
+    uint64_t x = *s;
+    x ^= x >> 12;
+    x ^= x << 25;
+    x ^= x >> 27;
+    *s = x;
+    return x * 0x2545F4914F6CDD1Dull;
+}
+
+/* The M1 gate's frame (src/kern/m1_input.h:10-21): a ramp, 32-pixel blocks and 5 bits of noise, from integers. */
+void or_m1_image(uint8_t *img, int w, int h, int stride)
+{
+    uint64_t s = 0x9e3779b97f4a7c15ull;
+    for (int y = 0; y < h; y++)
+        for (int x = 0; x < w; x++) {
+            const int ramp = (x * 96) / w + (y * 64) / h;
+            const int block = (((x >> 5) ^ (y >> 5)) & 7) * 8;
+            const int noise = (int)(or_rand(&s) & 31);
+            img[(size_t)y * (size_t)stride + (size_t)x] = (uint8_t)(ramp + block + noise);
+        }
+}
+
+/* The M2 gate's pattern (src/kern/m2_input.h:12-50): two octaves of integer value noise on a grid four times finer
+ * than the pixels, each pixel the rounded mean of its 4 x 4 fine cells, so an offset of (ox, oy) fine cells moves the
+ * picture by exactly (ox / 4, oy / 4) pixels. */
+static inline uint32_t m2_hash(int x, int y)
+{
+    uint32_t h = (uint32_t)x * 0x9E3779B1u ^ (uint32_t)y * 0x85EBCA77u;
+    h ^= h >> 15;
+    h *= 0xC2B2AE3Du;
+    return h ^ (h >> 13);
+}
+
+static inline uint32_t m2_noise(int x, int y, int bits)
+{
+    const int xi = x >> bits, yi = y >> bits, m = (1 << bits) - 1;
+    const uint32_t fx = (uint32_t)(x & m), fy = (uint32_t)(y & m), one = 1u << bits;
+    const uint32_t a = m2_hash(xi, yi) & 255, b = m2_hash(xi + 1, yi) & 255, c = m2_hash(xi, yi + 1) & 255, d = m2_hash(xi + 1, yi + 1) & 255;
+    return (a * (one - fx) + b * fx) * (one - fy) + (c * (one - fx) + d * fx) * fy;
+}
+
+void or_m2_render(uint8_t *img, int w, int h, int stride, int ox, int oy)
+{
+    for (int y = 0; y < h; y++)
+        for (int x = 0; x < w; x++) {
+            uint32_t sum = 0;
+            for (int j = 0; j < 4; j++)
+                for (int i = 0; i < 4; i++) {
+                    const int fx = 4 * x + i + ox, fy = 4 * y + j + oy;
+                    sum += ((m2_noise(fx, fy, 5) >> 6) * 3 + (m2_noise(fx, fy, 4) >> 4)) >> 2;
+                }
+            img[(size_t)y * stride + x] = (uint8_t)((sum + 128) >> 8);
+        }
+}

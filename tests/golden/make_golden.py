@@ -1,0 +1,118 @@
+"""make_golden.py -- writes the golden fixtures of tests/golden/ from the reference itself.
+
+Run in a checkout that has the reference tree (it builds oracle/_ref from its sources):
+
+    python tests/golden/make_golden.py [/root/reference]
+
+Writes:
+  m1_m2.json        the reference's committed gate logs: per-kernel plane hashes (logs/m1/host/m1-host-*.txt) and the
+                    LK lines (logs/m2/host/640x480.txt), parsed.
+  lk_640x480.npz    the 640 x 480 frame pair of the first benchmark configuration (seeded generator) and the reference's
+                    lk_track_vx + lk_flowback_vx (and lk_track_ref + lk_flowback_ref) at its 1,200 cell centres.
+  lk_1080p.npz      the 1920 x 1080 pair: the reference pyramid's per-level FNV hashes for both frames, and
+                    lk_track_vx + lk_flowback_vx at every 8th of the 16,200 cells of the 16 x 8 grid and at every 4th
+                    of the 4,080 cells at half resolution.
+  still_vectors.npz the reference's still_vectors (15 x 15, one level, 6 iterations, flowback 0.25) on a 640 x 480 pair.
+  ncc_32x21.npz     tk_correlate at 2,000 corners and search_slot (step 1 and 2) for a 32 x 21 template on a Q6 plane.
+Frames are not stored: the generator reproduces them bit for bit, and their hashes are stored to prove it.
+"""
+from __future__ import annotations
+
+import json
+import os
+import re
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+sys.path.insert(0, os.path.join(ROOT, "intel-phi-visiontrack_gb300"))
+
+import oracle as O  # noqa: E402
+import vtg_synth as S  # noqa: E402
+
+
+def parse_logs(ref_root: str) -> dict:
+    m1 = {}
+    for size in ("640x480", "1280x720", "1920x1080"):
+        with open(os.path.join(ref_root, "logs", "m1", "host", "m1-host-%s.txt" % size)) as f:
+            for line in f:
+                m = re.match(r"kern (\S+)\s+(\d+)x(\d+) ([0-9a-f]{16})$", line.strip())
+                if m:
+                    m1["%s %s" % (m.group(1), size)] = m.group(4)
+    m2 = []
+    with open(os.path.join(ref_root, "logs", "m2", "host", "640x480.txt")) as f:
+        for line in f:
+            m2.append(line.rstrip("\n"))
+    return {"m1": m1, "m2": m2}
+
+
+def frames_1080():
+    return S.warp_pair(1920, 1080, S.seeded_shift(2, 0), 0.5, seed=2)
+
+
+def main(ref_root: str = "/root/reference") -> None:
+    assert O.ref_available(), "oracle/_ref could not be built: the reference tree is needed"
+    with open(os.path.join(HERE, "m1_m2.json"), "w") as f:
+        json.dump(parse_logs(ref_root), f, indent=1)
+
+    cfg = O.lk_cfg(21, 21, 10, 0.01, 0.1, 25.0)
+    # configuration 1: 640 x 480, 3 levels, 16 x 16 grid
+    f0, f1, _, _ = S.warp_pair(640, 480, (1.7, -0.8), 0.5, seed=1)
+    xs, ys = O.cell_centres(640, 480, 16, 16)
+    vx = O.ref_lk_points(f0, f1, 3, 2, cfg, xs, ys, max_fb=0.5)
+    rf = O.ref_lk_points(f0, f1, 3, 2, cfg, xs, ys, max_fb=0.5, use_ref=True)
+    np.savez_compressed(os.path.join(HERE, "lk_640x480.npz"), f0_fnv=np.uint64(O.fnv(f0)), f1_fnv=np.uint64(O.fnv(f1)),
+                        xs=xs, ys=ys, vx=vx.view(np.uint8), ref=rf.view(np.uint8))
+
+    # configuration 2: 1920 x 1080, 4 levels
+    f0, f1, _, _ = frames_1080()
+    p0 = O.ref_pyramid(f0, 4)
+    p1 = O.ref_pyramid(f1, 4)
+    xs, ys = O.cell_centres(1920, 1080, 16, 8)
+    sel = np.arange(0, len(xs), 8)
+    vx = O.ref_lk_points(f0, f1, 4, 3, cfg, xs[sel], ys[sel], max_fb=0.5)
+    # half resolution: cells of 16 x 8 on level 1 (960 x 540), LK on levels 1..3
+    hx, hy = O.cell_centres(960, 540, 16, 8)
+    hsel = np.arange(0, len(hx), 4)
+    hvx = O.ref_lk_points(f0, f1, 4, 2, cfg, hx[hsel], hy[hsel], max_fb=0.5, base=1)
+    np.savez_compressed(os.path.join(HERE, "lk_1080p.npz"), f0_fnv=np.uint64(O.fnv(f0)), f1_fnv=np.uint64(O.fnv(f1)),
+                        pyr0_fnv=np.array([O.fnv(p) for p in p0], np.uint64),
+                        pyr1_fnv=np.array([O.fnv(p) for p in p1], np.uint64),
+                        sel=sel.astype(np.int32), vx=vx.view(np.uint8), half_sel=hsel.astype(np.int32),
+                        half_vx=hvx.view(np.uint8))
+
+    # still_vectors, the reference's own per-cell flow (15 x 15, single level)
+    g0, g1, _, _ = S.warp_pair(640, 480, (0.6, -0.3), 0.3, seed=5)
+    sv = O.ref_still_vectors(g0, g1)
+    np.savez_compressed(os.path.join(HERE, "still_vectors.npz"), f0_fnv=np.uint64(O.fnv(g0)),
+                        f1_fnv=np.uint64(O.fnv(g1)), cells=sv.view(np.uint8))
+
+    # the appearance correlation on a Q6 plane (level 0 of a synthetic frame)
+    n0 = S.noise_frame(640, 480, seed=9)
+    plane = O.pyramid(n0, 1)[0]
+    app, norm = O.cut_template(plane, 300, 200, 32, 21)
+    u = S.uniform(9, 77, 4000)
+    cx = (1 + np.floor(u[:2000] * (640 - 32 - 3))).astype(np.int32)
+    cy = (1 + np.floor(u[2000:] * (480 - 21 - 3))).astype(np.int32)
+    cx[:9] = [300, 299, 301, 300, 300, 1, 606, 1, 606]
+    cy[:9] = [200, 200, 200, 199, 201, 1, 1, 456, 456]
+    corr = O.ref_correlate(plane, app, norm, cx, cy)
+    f1s, mv1, mx1, my1 = O.ref_search_slot(plane, app, norm, 250, 360, 150, 260, 1)
+    f2s, mv2, mx2, my2 = O.ref_search_slot(plane, app, norm, 1, 640, 1, 480, 2)
+    hxs = np.array([2 * 300 + d for d in (-1, 0, 1, 0, 0, 1, -1)], np.int32)
+    hys = np.array([2 * 200 + d for d in (0, 0, 0, -1, 1, 1, -1)], np.int32)
+    half = O.ref_search_half(plane, app, norm, hxs, hys)
+    np.savez_compressed(os.path.join(HERE, "ncc_32x21.npz"), frame_fnv=np.uint64(O.fnv(n0)), app=app,
+                        norm=np.float32(norm), cx=cx, cy=cy, corr=corr,
+                        s1=np.array([f1s["hx"], f1s["hy"]], np.int32), s1_ncc=f1s["ncc"], s1_second=f1s["second"],
+                        s1_map_v=mv1, s1_map_x=mx1, s1_map_y=my1,
+                        s2=np.array([f2s["hx"], f2s["hy"]], np.int32), s2_ncc=f2s["ncc"], s2_second=f2s["second"],
+                        s2_map_v=mv2, s2_map_x=mx2, s2_map_y=my2, half_hx=hxs, half_hy=hys, half=half)
+    print("golden fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

@@ -1,0 +1,71 @@
+"""The C ABI without a GPU: libvtg.so builds for sm_103a, loads, exports every function include/*.h declares, and its
+host-only entry points answer. No kernel runs here."""
+import ctypes as C
+import glob
+import os
+import re
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        text = open(h).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"\b(vtg_[a-z0-9_]+)\s*\(", text):
+            names.add(m.group(1))
+    return sorted(names)
+
+
+def test_headers_declare_entry_points():
+    names = declared_functions()
+    assert "vtg_build" in names and "vtg_cells" in names and "vtg_points" in names
+
+
+def test_library_exports_every_declared_symbol(vtg_lib):
+    out = subprocess.run(["nm", "-D", "--defined-only", vtg_lib.LIB_PATH], capture_output=True, text=True, check=True)
+    exported = {line.split()[-1] for line in out.stdout.splitlines() if " T " in line}
+    missing = [n for n in declared_functions() if n not in exported]
+    assert not missing, "declared but not exported: %s" % missing
+    lib = vtg_lib.lib()
+    for n in declared_functions():
+        assert hasattr(lib, n)
+
+
+def test_host_only_entry_points(vtg_lib):
+    lib = vtg_lib.lib()
+    assert lib.vtg_strerror(vtg_lib.EBUDGET).decode().startswith("over")
+    cfg = vtg_lib.config(1920, 1080, levels=4, cell_w=16, cell_h=8)
+    b = lib.vtg_tracker_bytes(C.byref(cfg))
+    # two sets of F32 planes (pitch 1920, 960, 480, 256) plus staging and 16,200 cells
+    assert b > 2 * 4 * (1920 * 1080 + 960 * 540 + 480 * 270 + 256 * 135) and b < 40_000_000
+    for bad in (dict(levels=0), dict(levels=7), dict(patch_w=31), dict(patch_h=33), dict(flow_level=4),
+                dict(cell_w=0), dict(max_iter=0)):
+        kw = dict(width=1920, height=1080, levels=4, cell_w=16, cell_h=8)
+        kw.update(bad)
+        assert lib.vtg_tracker_bytes(C.byref(vtg_lib.config(**kw))) == 0, bad
+
+
+def test_context_without_gpu_is_refused(vtg_lib):
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    h = C.c_void_p()
+    assert vtg_lib.lib().vtg_ctx_create(0, 0, C.byref(h)) == vtg_lib.ENODEV
+
+
+def test_no_fallback_without_library(tmp_path, monkeypatch, vtg_lib):
+    """The binding refuses to run without the compiled library: no CPU fallback exists."""
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location("vtg_copy", os.path.join(os.path.dirname(vtg_lib.__file__), "vtg.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    monkeypatch.setattr(mod, "LIB_PATH", str(tmp_path / "missing.so"))
+    with pytest.raises(RuntimeError):
+        mod.lib()

@@ -1,0 +1,186 @@
+"""GPU parity for the pyramid and LK, through the C ABI.
+
+Bar: the pyramid is bit-exact (the reference's F32 planes are exact integers); the cell record's `diff` is bit-exact;
+flow agrees with the FP64 oracle within 0.01 px max-abs on every cell both call good, and status agrees on at least 99 %
+of cells (a cell whose minimum eigenvalue or bounds test sits on a threshold may flip between arithmetics)."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+import vtg_synth as S
+
+pytestmark = pytest.mark.gpu
+
+TOL_PX = 0.01
+
+
+def _flow_err(a, b):
+    ok = (a["status"] == 0) & (b["status"] == 0)
+    err = np.maximum(np.abs(a["x"] - b["x"]), np.abs(a["y"] - b["y"]))[ok]
+    return ok, (float(err.max()) if err.size else 0.0)
+
+
+def _tracker(vtg_lib, ctx, w, h, **kw):
+    return vtg_lib.Tracker(ctx, vtg_lib.config(w, h, **kw))
+
+
+@pytest.mark.parametrize("w,h,levels", [(32, 32, 1), (33, 47, 3), (97, 61, 4), (640, 480, 3), (1281, 719, 5),
+                                        (1920, 1080, 4)])
+def test_pyramid_bit_exact(vtg_lib, ctx, w, h, levels):
+    frame = S.noise_frame(w, h, seed=w + 3 * h)
+    t = _tracker(vtg_lib, ctx, w, h, levels=levels)
+    t.build(1, frame)
+    ref = O.pyramid(frame, levels)
+    for L in range(levels):
+        assert np.array_equal(t.level(1, L), ref[L]), "level %d" % L
+    t.close()
+
+
+def test_pyramid_strided_and_device_input(vtg_lib, ctx):
+    import torch
+
+    w, h = 650, 301
+    frame = S.noise_frame(w, h, seed=4)
+    padded = np.zeros((h, 704), np.uint8)
+    padded[:, :w] = frame
+    t = _tracker(vtg_lib, ctx, w, h, levels=3)
+    t.build(0, padded, stride=704)
+    dev = torch.from_numpy(padded).cuda()
+    torch.cuda.synchronize()
+    t.build(1, dev.data_ptr(), stride=704, where=vtg_lib.DEVICE)
+    ref = O.pyramid(frame, 3)
+    for L in range(3):
+        assert np.array_equal(t.level(0, L), ref[L]) and np.array_equal(t.level(1, L), ref[L])
+    t.close()
+
+
+def test_pyramid_1080p_matches_reference_hashes(vtg_lib, ctx, golden):
+    g = np.load(os.path.join(golden, "lk_1080p.npz"))
+    f0, f1, _, _ = S.warp_pair(1920, 1080, S.seeded_shift(2, 0), 0.5, seed=2)
+    t = _tracker(vtg_lib, ctx, 1920, 1080, levels=4)
+    t.build(0, f0)
+    t.build(1, f1)
+    assert [O.fnv(t.level(0, L)) for L in range(4)] == [int(v) for v in g["pyr0_fnv"]]
+    assert [O.fnv(t.level(1, L)) for L in range(4)] == [int(v) for v in g["pyr1_fnv"]]
+    t.close()
+
+
+def test_cells_config1(vtg_lib, ctx, golden):
+    """640 x 480, 1,200 cells on a 16 px grid, 21 x 21, 3 levels, <= 10 iterations, eps 0.01, flowback 0.5."""
+    g = np.load(os.path.join(golden, "lk_640x480.npz"))
+    f0, f1, _, _ = S.warp_pair(640, 480, (1.7, -0.8), 0.5, seed=1)
+    t = _tracker(vtg_lib, ctx, 640, 480, levels=3, cell_w=16, cell_h=16)
+    t.build(0, f0)
+    t.build(1, f1)
+    cells, lk = t.cells(0, 1)
+    assert len(cells) == 1200
+    P0, P1 = O.pyramid(f0, 3), O.pyramid(f1, 3)
+    olk, ocells = O.cells(P0, P1, 2, O.lk_cfg(), 16, 16, max_fb=0.5, mode=O.F64, threads=8)
+    ok, err = _flow_err(lk, olk)
+    assert (lk["status"] == olk["status"]).mean() >= 0.99
+    assert err <= TOL_PX, err
+    ref = g["vx"].view(O.LK_OUT)  # the reference's own lk_track_vx + lk_flowback_vx
+    ok2, err2 = _flow_err(lk, ref)
+    assert (lk["status"] == ref["status"]).mean() >= 0.99 and err2 <= TOL_PX
+    assert np.array_equal(cells["diff"], ocells["diff"])
+    good = cells["state"] == 0
+    assert np.allclose(cells["u"][good], lk["x"][good] - g["xs"][good], atol=0)
+    assert np.abs(cells["sigma"] - ocells["sigma"])[good & (ocells["state"] == 0)].max() < 1e-4
+
+
+def test_cells_config2_full_and_half(vtg_lib, ctx, golden):
+    """1920 x 1080, 4 levels: 16,200 cells (16 x 8) at level 0 and 4,080 at level 1."""
+    g = np.load(os.path.join(golden, "lk_1080p.npz"))
+    f0, f1, _, _ = S.warp_pair(1920, 1080, S.seeded_shift(2, 0), 0.5, seed=2)
+    P0, P1 = O.pyramid(f0, 4), O.pyramid(f1, 4)
+    for flow_level, n, top, sel, ref in ((0, 16200, 3, g["sel"], g["vx"]), (1, 4080, 2, g["half_sel"], g["half_vx"])):
+        t = _tracker(vtg_lib, ctx, 1920, 1080, levels=4, cell_w=16, cell_h=8, flow_level=flow_level)
+        t.build(0, f0)
+        t.build(1, f1)
+        cells, lk = t.cells(0, 1)
+        assert len(cells) == n
+        olk, ocells = O.cells(P0[flow_level:], P1[flow_level:], top, O.lk_cfg(), 16, 8, max_fb=0.5, mode=O.F64,
+                              threads=8)
+        ok, err = _flow_err(lk, olk)
+        assert (lk["status"] == olk["status"]).mean() >= 0.99
+        assert err <= TOL_PX, (flow_level, err)
+        assert np.array_equal(cells["diff"], ocells["diff"])
+        r = ref.view(O.LK_OUT)
+        _, err2 = _flow_err(lk[sel], r)
+        assert err2 <= TOL_PX
+        t.close()
+
+
+def test_points_with_guesses_and_borders(vtg_lib, ctx):
+    """The point list (OP_LK) with per-point guesses, points past every border, a flat band and two patch sizes."""
+    w, h = 200, 150
+    f0, f1, _, _ = S.warp_pair(w, h, (2.5, -1.5), 0.5, seed=11)
+    f0[:, :40] = 128
+    f1[:, :40] = 128
+    xs = np.array([5, 11, 12, 13, 100, 187, 188, 189, 195, 30, 60, 150, 100.25, 99.75], np.float32)
+    ys = np.array([75, 75, 75, 75, 5, 75, 75, 75, 75, 75, 140, 12, 70.5, 71.125], np.float32)
+    gx = np.linspace(-3, 3, len(xs)).astype(np.float32)
+    gy = np.linspace(2, -2, len(xs)).astype(np.float32)
+    for (pw, ph, levels, fb) in ((21, 21, 3, 0.5), (15, 15, 1, 0.25), (9, 13, 2, 0.0), (29, 31, 2, 0.5)):
+        t = _tracker(vtg_lib, ctx, w, h, levels=levels, patch_w=pw, patch_h=ph, fb_max=fb)
+        t.build(0, f0)
+        t.build(1, f1)
+        out = t.points(0, 1, xs, ys, gx, gy)
+        P0, P1 = O.pyramid(f0, levels), O.pyramid(f1, levels)
+        ref = O.lk_points(P0, P1, levels - 1, O.lk_cfg(pw, ph), xs, ys, gx, gy, max_fb=fb, mode=O.F64)
+        assert np.array_equal(out["status"], ref["status"]), (pw, ph)
+        ok, err = _flow_err(out, ref)
+        assert err <= TOL_PX
+        assert np.array_equal(out["iters"][ok], ref["iters"][ok]) or np.abs(
+            out["iters"].astype(int) - ref["iters"].astype(int)).max() <= 1
+        t.close()
+
+
+def test_still_vectors_config(vtg_lib, ctx, golden):
+    """The reference's own per-cell flow settings (15 x 15, one level, 6 iterations, flowback 0.25, 16 x 8 cells)
+    against its still_vectors output."""
+    g = np.load(os.path.join(golden, "still_vectors.npz"))
+    f0, f1, _, _ = S.warp_pair(640, 480, (0.6, -0.3), 0.3, seed=5)
+    t = _tracker(vtg_lib, ctx, 640, 480, levels=1, patch_w=15, patch_h=15, max_iter=6, max_residual=16.0,
+                 fb_max=0.25, cell_w=16, cell_h=8)
+    t.build(0, f0)
+    t.build(1, f1)
+    cells, lk = t.cells(0, 1)
+    ref = g["cells"].view(O.CELL)
+    assert np.array_equal(cells["diff"], ref["diff"])
+    assert (cells["state"] == ref["state"]).mean() >= 0.99
+    ok = (cells["state"] == 0) & (ref["state"] == 0)
+    assert np.maximum(np.abs(cells["u"] - ref["u"]), np.abs(cells["v"] - ref["v"]))[ok].max() <= TOL_PX
+    t.close()
+
+
+def test_repeatable_and_set_order(vtg_lib, ctx):
+    """Same inputs, same bits, run after run; and the sets are symmetric (build order does not matter)."""
+    f0, f1, _, _ = S.warp_pair(320, 240, (1.0, 0.5), 0.5, seed=3)
+    t = _tracker(vtg_lib, ctx, 320, 240, levels=3, cell_w=16, cell_h=16)
+    t.build(0, f0)
+    t.build(1, f1)
+    a = t.cells(0, 1)
+    b = t.cells(0, 1)
+    t.build(1, f0)
+    t.build(0, f1)
+    c = t.cells(1, 0)
+    for x, y in ((a, b), (a, c)):
+        assert x[0].tobytes() == y[0].tobytes() and x[1].tobytes() == y[1].tobytes()
+    t.close()
+
+
+def test_errors_are_status_codes(vtg_lib, ctx):
+    lib = vtg_lib.lib()
+    t = _tracker(vtg_lib, ctx, 64, 64, levels=2)
+    assert lib.vtg_build(t.h, 2, None, 64, 0, None) == vtg_lib.EINVAL
+    assert lib.vtg_cells(t.h, 0, 3, None, None, 0, None) == vtg_lib.EINVAL
+    assert lib.vtg_points(t.h, 0, 1, 5, 1, None, None, None, None, None, 0, None) == vtg_lib.EINVAL
+    t.close()
+    small = vtg_lib.Context(0, hbm_budget=1 << 20)
+    with pytest.raises(vtg_lib.VtgError) as e:
+        vtg_lib.Tracker(small, vtg_lib.config(1920, 1080))
+    assert e.value.code == vtg_lib.EBUDGET
+    small.close()

@@ -1,0 +1,219 @@
+"""The oracle, pinned: this project's CPU restatement against the reference's own golden logs, against fixtures the
+reference produced (tests/golden/make_golden.py), and, where the reference tree is here, against the reference's code
+itself (oracle/_ref). No GPU."""
+import json
+import os
+import platform
+
+import numpy as np
+import pytest
+
+import oracle as O
+import vtg_synth as S
+
+X86 = platform.machine() in ("x86_64", "AMD64")
+x86_only = pytest.mark.skipif(not X86, reason="the lane model's long double is the x87 format only on x86-64")
+
+
+def _golden(golden, name):
+    return np.load(os.path.join(golden, name))
+
+
+@pytest.mark.parametrize("size", ["640x480", "1280x720", "1920x1080"])
+def test_pyramid_matches_m1_logs(golden, size):
+    """u8 -> Q6 and one reduce reproduce the reference's M1 gate hashes (logs/m1/host/m1-host-*.txt)."""
+    with open(os.path.join(golden, "m1_m2.json")) as f:
+        m1 = json.load(f)["m1"]
+    w, h = map(int, size.split("x"))
+    p = O.pyramid(O.m1_image(w, h), 2)
+    assert "%016x" % O.fnv(p[0]) == m1["u8_to_q6 " + size]
+    assert "%016x" % O.fnv(p[1]) == m1["reduce " + size]
+
+
+@x86_only
+def test_lk_lane_matches_m2_logs(golden):
+    """The lane-model LK reproduces the reference's M2 gate lines (logs/m2/host/640x480.txt) bit for bit: 10 exact
+    displacements, 330 points each, raw bits of point 0 and a hash of all 330 lk_out records."""
+    with open(os.path.join(golden, "m1_m2.json")) as f:
+        m2 = json.load(f)["m2"]
+    w, h = 640, 480
+    cfg = O.lk_cfg(21, 21, 10, 0.005, 0.1, 40.0)
+    margin = 40 + 21
+    pts = [(x, y) for y in range(margin, h - margin, 24) for x in range(margin, w - margin, 24)]
+    xs = np.array([p[0] for p in pts], np.float32)
+    ys = np.array([p[1] for p in pts], np.float32)
+    p0 = O.pyramid(O.m2_render(w, h, 2048, 2048), 4)
+    cases = [(0, 0), (1, 0), (0, 1), (2, 2), (-3, 1), (5, -6), (13, 7), (-22, 17), (49, -30), (-101, 66)]
+    lines = []
+    bits = lambda f: int(np.float32(f).view(np.uint32))
+    for dx, dy in cases:
+        p1 = O.pyramid(O.m2_render(w, h, 2048 - dx, 2048 - dy), 4)
+        out = O.lk_points(p0, p1, 3, cfg, xs, ys, mode=O.LANE)
+        o = out[0]
+        lines.append("lk_first %d,%d x %08x y %08x eig %08x res %08x cxx %08x cxy %08x cyy %08x it %u st %u" % (
+            dx, dy, bits(o["x"]), bits(o["y"]), bits(o["min_eig"]), bits(o["residual"]), bits(o["cov_xx"]),
+            bits(o["cov_xy"]), bits(o["cov_yy"]), o["iters"], o["status"]))
+        lines.append("lk_hash %d,%d %016x" % (dx, dy, O.fnv(out)))
+    assert lines == m2
+
+
+def test_m2_f64_accuracy_against_exact_truth():
+    """The FP64 oracle recovers the M2 pattern's exact quarter-pixel displacements to within 0.05 px (the reference's
+    own accuracy table, docs/measurements.md:93-104, reads EPE medians of 0.007-0.012 px)."""
+    w, h = 640, 480
+    cfg = O.lk_cfg(21, 21, 10, 0.005, 0.1, 40.0)
+    xs, ys = np.meshgrid(np.arange(61, w - 61, 24, dtype=np.float32), np.arange(61, h - 61, 24, dtype=np.float32))
+    xs, ys = xs.ravel(), ys.ravel()
+    p0 = O.pyramid(O.m2_render(w, h, 2048, 2048), 4)
+    for dx, dy in [(5, -6), (13, 7), (-22, 17)]:
+        p1 = O.pyramid(O.m2_render(w, h, 2048 - dx, 2048 - dy), 4)
+        out = O.lk_points(p0, p1, 3, cfg, xs, ys, mode=O.F64)
+        ok = out["status"] == 0
+        epe = np.hypot(out["x"] - xs - dx / 4.0, out["y"] - ys - dy / 4.0)[ok]
+        assert ok.mean() > 0.95 and np.median(epe) < 0.05
+
+
+def test_config1_fixture(golden):
+    """640 x 480, 1,200 cells, 3 levels, flowback: the oracle against the reference's lk_track_vx / lk_track_ref."""
+    g = _golden(golden, "lk_640x480.npz")
+    f0, f1, _, _ = S.warp_pair(640, 480, (1.7, -0.8), 0.5, seed=1)
+    assert O.fnv(f0) == int(g["f0_fnv"]) and O.fnv(f1) == int(g["f1_fnv"]), "the generator no longer reproduces"
+    P0, P1 = O.pyramid(f0, 3), O.pyramid(f1, 3)
+    cfg = O.lk_cfg()
+    vx = g["vx"].view(O.LK_OUT)
+    lane = O.lk_points(P0, P1, 2, cfg, g["xs"], g["ys"], max_fb=0.5, mode=O.LANE, threads=4)
+    if X86:
+        assert lane.tobytes() == vx.tobytes()
+    f64 = O.lk_points(P0, P1, 2, cfg, g["xs"], g["ys"], max_fb=0.5, mode=O.F64, threads=4)
+    ok = (f64["status"] == 0) & (vx["status"] == 0)
+    assert (f64["status"] == vx["status"]).mean() >= 0.99
+    err = np.maximum(np.abs(f64["x"] - vx["x"]), np.abs(f64["y"] - vx["y"]))[ok]
+    assert err.max() < 1e-3
+    ref = g["ref"].view(O.LK_OUT)  # the scalar reference differs from the lane model by rounding only
+    ok2 = (ref["status"] == 0) & ok
+    assert np.abs(ref["x"] - vx["x"])[ok2].max() < 1e-3
+
+
+def test_config2_fixture(golden):
+    """1920 x 1080, 4 levels: the oracle's pyramid against the reference's per-level hashes (bit-exact), and its LK at
+    every 8th cell of the 16,200-cell grid and every 4th of the 4,080 half-resolution cells."""
+    g = _golden(golden, "lk_1080p.npz")
+    f0, f1, _, _ = S.warp_pair(1920, 1080, S.seeded_shift(2, 0), 0.5, seed=2)
+    assert O.fnv(f0) == int(g["f0_fnv"]) and O.fnv(f1) == int(g["f1_fnv"])
+    P0, P1 = O.pyramid(f0, 4), O.pyramid(f1, 4)
+    assert [O.fnv(p) for p in P0] == [int(v) for v in g["pyr0_fnv"]]
+    assert [O.fnv(p) for p in P1] == [int(v) for v in g["pyr1_fnv"]]
+    cfg = O.lk_cfg()
+    xs, ys = O.cell_centres(1920, 1080, 16, 8)
+    sel = g["sel"]
+    vx = g["vx"].view(O.LK_OUT)
+    lane = O.lk_points(P0, P1, 3, cfg, xs[sel], ys[sel], max_fb=0.5, mode=O.LANE, threads=8)
+    if X86:
+        assert lane.tobytes() == vx.tobytes()
+    hx, hy = O.cell_centres(960, 540, 16, 8)
+    hsel = g["half_sel"]
+    hvx = g["half_vx"].view(O.LK_OUT)
+    hl = O.lk_points(P0[1:], P1[1:], 2, cfg, hx[hsel], hy[hsel], max_fb=0.5, mode=O.LANE, threads=8)
+    if X86:
+        assert hl.tobytes() == hvx.tobytes()
+    f64 = O.lk_points(P0[1:], P1[1:], 2, cfg, hx[hsel], hy[hsel], max_fb=0.5, mode=O.F64, threads=8)
+    ok = (f64["status"] == 0) & (hvx["status"] == 0)
+    assert np.maximum(np.abs(f64["x"] - hvx["x"]), np.abs(f64["y"] - hvx["y"]))[ok].max() < 1e-3
+
+
+def test_still_vectors_fixture(golden):
+    """The per-cell grid restated (centre, clamp, LK, flowback, cell record) against the reference's still_vectors."""
+    g = _golden(golden, "still_vectors.npz")
+    f0, f1, _, _ = S.warp_pair(640, 480, (0.6, -0.3), 0.3, seed=5)
+    assert O.fnv(f0) == int(g["f0_fnv"]) and O.fnv(f1) == int(g["f1_fnv"])
+    ref = g["cells"].view(O.CELL)
+    cfg = O.lk_cfg(15, 15, 6, 0.01, 0.1, 16.0)
+    _, cl = O.cells(O.pyramid(f0, 1), O.pyramid(f1, 1), 0, cfg, 16, 8, max_fb=0.25, mode=O.LANE, threads=4)
+    if X86:
+        assert cl.tobytes() == ref.tobytes()
+    assert np.array_equal(cl["diff"], ref["diff"])
+    assert np.array_equal(cl["state"], ref["state"])
+
+
+def test_ncc_fixture(golden):
+    """search_at, search_half, the per-cell map and search_slot on a 32 x 21 template: the lane restatement against the
+    reference (bit for bit on x86), the exact-sum FP64 form within 1e-5."""
+    g = _golden(golden, "ncc_32x21.npz")
+    n0 = S.noise_frame(640, 480, seed=9)
+    assert O.fnv(n0) == int(g["frame_fnv"])
+    plane = O.pyramid(n0, 1)[0]
+    app, norm = O.cut_template(plane, 300, 200, 32, 21)
+    assert np.array_equal(app, g["app"]) and np.float32(norm) == g["norm"]
+    lane = np.array([O.ncc_at(plane, app, norm, int(x), int(y), O.LANE) for x, y in zip(g["cx"], g["cy"])])
+    f64 = np.array([O.ncc_at(plane, app, norm, int(x), int(y), O.F64) for x, y in zip(g["cx"], g["cy"])])
+    if X86:
+        assert np.array_equal(lane, g["corr"])
+    assert np.abs(f64 - g["corr"]).max() < 1e-5
+    assert g["corr"][0] > 0.999999
+    half = np.array([O.ncc_half(plane, app, norm, int(a), int(b), O.LANE) for a, b in zip(g["half_hx"], g["half_hy"])])
+    if X86:
+        assert np.array_equal(half, g["half"])
+    for key, args in (("s1", (250, 360, 150, 260, 1)), ("s2", (1, 640, 1, 480, 2))):
+        f, mv, mx, my = O.search_slot(plane, app, norm, *args, mode=O.LANE)
+        assert [f["hx"], f["hy"]] == list(g[key])
+        n = len(g[key + "_map_v"])
+        assert np.array_equal(mx[:n], g[key + "_map_x"]) and np.array_equal(my[:n], g[key + "_map_y"])
+        if X86:
+            assert f["ncc"] == float(g[key + "_ncc"]) and f["second"] == float(g[key + "_second"])
+            assert np.array_equal(mv[:n], g[key + "_map_v"])
+
+
+def test_near_blank_never_matches():
+    """vt_ncc_check's property (src/host/vt_ncc_check.c:17-63), restated: windows with under a few grey levels of noise
+    never read 0.5 or more, nothing reads over 1, and the template itself reads 1."""
+    rng = np.random.default_rng(7)
+    app = rng.integers(6000, 10000, size=(21, 32)).astype(np.float32)
+    app -= np.float32(app.sum(dtype=np.float64) / app.size)
+    norm = float((app.astype(np.float64) ** 2).sum())
+    worst = -2.0
+    for level in (16320, 12800, 640):
+        for step in (0, 1, 2, 4, 8, 16, 32, 64):
+            for _ in range(40):
+                pl = (level - (rng.integers(0, step + 1, size=(42, 64)) if step else np.zeros((42, 64), int))).astype(np.float32)
+                for mode in (O.LANE, O.F64):
+                    v = O.ncc_at(np.ascontiguousarray(pl), app, norm, 4, 4, mode)
+                    worst = max(worst, v)
+                    assert v <= 1.0 + 1e-9
+    assert worst < 0.5
+    pl = np.full((42, 64), 8000.0, np.float32)
+    pl[4:25, 4:36] += app
+    assert O.ncc_at(pl, app, norm, 4, 4, O.LANE) > 0.999 and O.ncc_at(pl, app, norm, 4, 4, O.F64) > 0.999
+
+
+@pytest.mark.skipif(not O.ref_available(), reason="the reference tree is not on this machine")
+@pytest.mark.parametrize("w,h", [(33, 47), (64, 64), (97, 61), (640, 480), (1281, 719)])
+def test_pyramid_against_reference_code(w, h):
+    """Odd and small sizes: the oracle's pyramid equals the reference's img_u8_to_q6 + img_reduce, both variants."""
+    frame = S.noise_frame(w, h, seed=w * 7 + h)
+    levels = 4 if min(w, h) >= 64 else 3
+    mine = O.pyramid(frame, levels)
+    for use_ref in (False, True):
+        ref = O.ref_pyramid(frame, levels, use_ref=use_ref)
+        for a, b in zip(mine, ref):
+            assert np.array_equal(a, b)
+
+
+@pytest.mark.skipif(not (O.ref_available() and X86), reason="needs the reference tree and x86-64")
+def test_lk_edge_cases_against_reference_code():
+    """Points at and past the borders (LK_OUT), a flat picture (LK_LOWEIG), guesses, and a larger patch: the lane
+    restatement equals lk_track_vx + lk_flowback_vx bit for bit."""
+    w, h = 200, 150
+    f0, f1, _, _ = S.warp_pair(w, h, (2.5, -1.5), 0.5, seed=11)
+    f1[:, :40] = 128  # a flat band
+    f0[:, :40] = 128
+    xs = np.array([5, 11, 12, 13, 100, 187, 188, 189, 195, 30, 60, 150, 100.25, 99.75], np.float32)
+    ys = np.array([75, 75, 75, 75, 5, 75, 75, 75, 75, 75, 140, 12, 70.5, 71.125], np.float32)
+    gx = np.linspace(-3, 3, len(xs)).astype(np.float32)
+    gy = np.linspace(2, -2, len(xs)).astype(np.float32)
+    for (pw, ph, levels) in ((21, 21, 3), (15, 15, 1), (9, 13, 2), (29, 31, 2)):
+        cfg = O.lk_cfg(pw, ph, 10, 0.01, 0.1, 25.0)
+        P0, P1 = O.pyramid(f0, levels), O.pyramid(f1, levels)
+        for fb in (0.0, 0.5):
+            mine = O.lk_points(P0, P1, levels - 1, cfg, xs, ys, gx, gy, max_fb=fb, mode=O.LANE)
+            ref = O.ref_lk_points(f0, f1, levels, levels - 1, cfg, xs, ys, gx, gy, max_fb=fb, threads=1)
+            assert mine.tobytes() == ref.tobytes(), (pw, ph, levels, fb)
