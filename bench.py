@@ -169,6 +169,11 @@ def run_ours(args) -> dict:
     value = world * n * args.steps / (total_ms / 1e3)
 
     # end to end through the C ABI: pinned host frame in, cell records out, every step
+    if args.skip_e2e:
+        t.close()
+        ctx.close()
+        return {"metric": METRIC, "value": value, "unit": "cells/s", "ms_per_step": total_ms / args.steps,
+                "lk_ms": float(lk_ms.mean()), "note": "profiling run: e2e and baselines skipped"} if rank == 0 else None
     pinned = [torch.from_numpy(f).pin_memory() for f in frames]
     host_cells = torch.empty(n * 24, dtype=torch.uint8).pin_memory()
     import ctypes as C
@@ -295,6 +300,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--form", default="plain", choices=["plain"])
+    ap.add_argument("--skip-e2e", action="store_true", help="time the kernels only (for profiling)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     line = run_reference(args) if args.impl == "reference" else run_ours(args)

@@ -36,90 +36,104 @@ __device__ __forceinline__ float warp_fold(float v)
     return v;
 }
 
-/* The row's horizontal interpolation at this lane's column: l from this lane's load, n from the next lane's. */
-__device__ __forceinline__ float hlerp(const float *p, bool ld, float fx)
+/* The row's horizontal interpolation at this lane's column: l from this lane's load, n from the next lane's. Every lane
+ * loads (a clamped column for lanes past the window), so the load needs no predicate. */
+__device__ __forceinline__ float hlerp(const float *p, float fx)
 {
-    const float l = ld ? __ldg(p) : 0.0f;
+    const float l = __ldg(p);
     const float n = __shfl_down_sync(VTG_FULL, l, 1);
     return __fmaf_rn(n - l, fx, l);
 }
 
-/* build: the window of I around pixel (ix + fx, iy + fy); T, Tx, Ty into the registers; the tensor's sums. */
-template <int MAXH>
-__device__ __forceinline__ void lk_build(const DevLevel &L, int ix, float fx, int iy, float fy, int W, int H, int lane,
+/* build: the window of I around pixel (ix + fx, iy + fy); T, Tx, Ty into the registers; the tensor's sums.
+ * EXACT: the patch height is MAXH at compile time (no row guards). */
+template <int MAXH, bool EXACT>
+__device__ __forceinline__ void lk_build(const DevLevel &L, int ix, float fx, int iy, float fy, int W, int Hr, int lane,
                                          Patch<MAXH> &P, float &gxx, float &gxy, float &gyy)
 {
+    const int H = EXACT ? MAXH : Hr;
     const int x0 = ix - W / 2, y0 = iy - H / 2;
-    /* Lane c samples window column c - 1: loads for c <= W + 2 (lane W + 2 only feeds lane W + 1's right neighbour). */
-    const bool ld = lane <= W + 2;
-    const bool act = lane >= 1 && lane <= W;
-    const float *row = L.p + (size_t)(y0 - 1) * L.pitch + (x0 - 1 + lane);
-    float prev = hlerp(row, ld, fx);
-    float u = 0.f, ul = 0.f, ur = 0.f, m = 0.f, ml = 0.f, mr = 0.f, d = 0.f, dl = 0.f, dr = 0.f;
-    float sxx = 0.f, sxy = 0.f, syy = 0.f;
+    /* Lane c samples window column c - 1 (c = 0 .. W + 1; lane W + 2 feeds lane W + 1's right neighbour; the lanes past
+     * it read a clamped column and feed nothing). Patch columns are lanes 1 .. W: the gradient scale is 0 elsewhere. */
+    const float gs = (lane >= 1 && lane <= W) ? LK_GRAD_SCALE : 0.0f;
+    const float *row = L.p + (size_t)(y0 - 1) * L.pitch + (x0 - 1 + min(lane, W + 2));
+    float prev = hlerp(row, fx);
+    /* S rows r - 2, r - 1, r: values, and their x + 1 minus x - 1 differences (shared by three patch rows) */
+    float u = 0.f, ul = 0.f, ur = 0.f, m = 0.f, ml = 0.f, mr = 0.f, mdx = 0.f, udx = 0.f;
+    float sxx0 = 0.f, sxy0 = 0.f, syy0 = 0.f, sxx1 = 0.f, sxy1 = 0.f, syy1 = 0.f;
 #pragma unroll
     for (int r = 0; r < MAXH + 2; r++) {
-        if (r < H + 2) {
+        if (EXACT || r < H + 2) {
             row += L.pitch;
-            const float cur = hlerp(row, ld, fx);
-            const float S = __fmaf_rn(cur - prev, fy, prev);
+            const float cur = hlerp(row, fx);
+            const float d = __fmaf_rn(cur - prev, fy, prev);
             prev = cur;
-            const float Sl = __shfl_up_sync(VTG_FULL, S, 1), Sr = __shfl_down_sync(VTG_FULL, S, 1);
-            u = m; ul = ml; ur = mr;
-            m = d; ml = dl; mr = dr;
-            d = S; dl = Sl; dr = Sr;
+            const float dl = __shfl_up_sync(VTG_FULL, d, 1), dr = __shfl_down_sync(VTG_FULL, d, 1);
+            const float ddx = dr - dl;
             if (r >= 2) {
-                const float dxu = ur - ul, dxm = mr - ml, dxd = dr - dl;
-                float tx = __fmaf_rn(dxm, 2.0f, dxu + dxd) * LK_GRAD_SCALE;
-                const float dyl = dl - ul, dyc = d - u, dyr = dr - ur;
-                float ty = __fmaf_rn(dyc, 2.0f, dyl + dyr) * LK_GRAD_SCALE;
-                tx = act ? tx : 0.0f;
-                ty = act ? ty : 0.0f;
+                const float tx = __fmaf_rn(mdx, 2.0f, udx + ddx) * gs;
+                const float ty = __fmaf_rn(d - u, 2.0f, (dl - ul) + (dr - ur)) * gs;
                 P.t[r - 2] = m;
                 P.tx[r - 2] = tx;
                 P.ty[r - 2] = ty;
-                sxx = __fmaf_rn(tx, tx, sxx);
-                sxy = __fmaf_rn(tx, ty, sxy);
-                syy = __fmaf_rn(ty, ty, syy);
+                if (r & 1) {
+                    sxx1 = __fmaf_rn(tx, tx, sxx1);
+                    sxy1 = __fmaf_rn(tx, ty, sxy1);
+                    syy1 = __fmaf_rn(ty, ty, syy1);
+                } else {
+                    sxx0 = __fmaf_rn(tx, tx, sxx0);
+                    sxy0 = __fmaf_rn(tx, ty, sxy0);
+                    syy0 = __fmaf_rn(ty, ty, syy0);
+                }
             }
+            u = m; ul = ml; ur = mr; udx = mdx;
+            m = d; ml = dl; mr = dr; mdx = ddx;
         }
     }
-    gxx = warp_fold(sxx);
-    gxy = warp_fold(sxy);
-    gyy = warp_fold(syy);
+    gxx = warp_fold(sxx0 + sxx1);
+    gxy = warp_fold(sxy0 + sxy1);
+    gyy = warp_fold(syy0 + syy1);
 }
 
 /* iterate (RESID = false): J at pixel (jx + fx, jy + fy); the sums of It Tx and It Ty.
  * residual (RESID = true): the sums of |It| and It^2, It in 8-bit grey. */
-template <int MAXH, bool RESID>
-__device__ __forceinline__ void lk_sample(const DevLevel &L, int jx, float fx, int jy, float fy, int W, int H, int lane,
+template <int MAXH, bool EXACT, bool RESID>
+__device__ __forceinline__ void lk_sample(const DevLevel &L, int jx, float fx, int jy, float fy, int W, int Hr, int lane,
                                           const Patch<MAXH> &P, float &b0, float &b1)
 {
+    const int H = EXACT ? MAXH : Hr;
     const int x0 = jx - W / 2, y0 = jy - H / 2;
-    const bool ld = lane <= W + 1;
-    const bool act = lane >= 1 && lane <= W;
-    const float *row = L.p + (size_t)y0 * L.pitch + (x0 - 1 + lane);
-    float prev = hlerp(row, ld, fx);
-    float s0 = 0.f, s1 = 0.f;
+    const float q6 = (lane >= 1 && lane <= W) ? LK_Q6_INV : 0.0f;
+    const float *row = L.p + (size_t)y0 * L.pitch + (x0 - 1 + min(lane, W + 1));
+    float prev = hlerp(row, fx);
+    float s00 = 0.f, s01 = 0.f, s10 = 0.f, s11 = 0.f;
 #pragma unroll
     for (int r = 0; r < MAXH; r++) {
-        if (r < H) {
+        if (EXACT || r < H) {
             row += L.pitch;
-            const float cur = hlerp(row, ld, fx);
+            const float cur = hlerp(row, fx);
             const float it = P.t[r] - __fmaf_rn(cur - prev, fy, prev);
             prev = cur;
             if (RESID) {
-                const float g = act ? it * LK_Q6_INV : 0.0f;
-                s0 = s0 + fabsf(g);
-                s1 = __fmaf_rn(g, g, s1);
+                const float g = it * q6;
+                if (r & 1) {
+                    s01 = s01 + fabsf(g);
+                    s11 = __fmaf_rn(g, g, s11);
+                } else {
+                    s00 = s00 + fabsf(g);
+                    s10 = __fmaf_rn(g, g, s10);
+                }
+            } else if (r & 1) {
+                s01 = __fmaf_rn(it, P.tx[r], s01);
+                s11 = __fmaf_rn(it, P.ty[r], s11);
             } else {
-                s0 = __fmaf_rn(it, P.tx[r], s0);
-                s1 = __fmaf_rn(it, P.ty[r], s1);
+                s00 = __fmaf_rn(it, P.tx[r], s00);
+                s10 = __fmaf_rn(it, P.ty[r], s10);
             }
         }
     }
-    b0 = warp_fold(s0);
-    b1 = warp_fold(s1);
+    b0 = warp_fold(s00 + s01);
+    b1 = warp_fold(s10 + s11);
 }
 
 /* A position as whole pixel + offset: floor and phase of base + t, base a whole number. */
@@ -131,16 +145,16 @@ __device__ __forceinline__ void split(int base, float t, int &i, float &f)
 }
 
 /* The pyramid walk (src/kern/lk_driver.inc:7-109), warp-uniform, F32. */
-template <int MAXH>
-__device__ void lk_track(const DevPyr &I, const DevPyr &J, int top, const LkPrm &p, float x, float y, float gx0,
-                         float gy0, int lane, Patch<MAXH> &P, vtg_lk_out &o)
+template <int MAXH, bool EXACT>
+__device__ __forceinline__ void lk_track(const DevPyr &I, const DevPyr &J, int top, const LkPrm &p, float x, float y,
+                                         float gx0, float gy0, int lane, Patch<MAXH> &P, vtg_lk_out &o)
 {
-    const int W = p.W, H = p.H;
+    const int W = p.W, H = EXACT ? MAXH : p.H;
     const int mx = W / 2 + 1, my = H / 2 + 1;
     float gx = ldexpf(gx0, -top), gy = ldexpf(gy0, -top);
     int status = 0, iters = 0;
     bool valid0 = false;
-    float eig0 = 0.0f, det0 = 1.0f, gxx0 = 0.0f, gxy0 = 0.0f, gyy0 = 0.0f;
+    float eig0 = 0.0f, idet0 = 0.0f, gxx0 = 0.0f, gxy0 = 0.0f, gyy0 = 0.0f;
     for (int L = top; L >= 0; L--) {
         const DevLevel IL = I.l[L], JL = J.l[L];
         const float px = ldexpf(x, -L), py = ldexpf(y, -L); /* exact */
@@ -157,7 +171,7 @@ __device__ void lk_track(const DevPyr &I, const DevPyr &J, int top, const LkPrm 
         const int bx = (int)fpx, by = (int)fpy;
         const float rx = px - fpx, ry = py - fpy; /* exact */
         float gxx, gxy, gyy;
-        lk_build<MAXH>(IL, bx, rx, by, ry, W, H, lane, P, gxx, gxy, gyy);
+        lk_build<MAXH, EXACT>(IL, bx, rx, by, ry, W, H, lane, P, gxx, gxy, gyy);
         /* det = gxx gyy - gxy^2 by Kahan's product difference; the smaller eigenvalue as det / lambda_max. */
         const float w2 = gxy * gxy;
         const float e2 = __fmaf_rn(gxy, gxy, -w2);
@@ -177,14 +191,16 @@ __device__ void lk_track(const DevPyr &I, const DevPyr &J, int top, const LkPrm 
             }
             continue;
         }
+        const float idet = 1.0f / det;
         if (L == 0) {
-            det0 = det;
+            idet0 = idet;
             gxx0 = gxx;
             gxy0 = gxy;
             gyy0 = gyy;
             valid0 = true;
         }
-        const float ia = gyy / det, ib = -gxy / det, ic = gxx / det;
+        /* G^-1 / 64: b arrives in Q6 grey x 8-bit grey per pixel */
+        const float ia = gyy * idet * LK_Q6_INV, ib = -gxy * idet * LK_Q6_INV, ic = gxx * idet * LK_Q6_INV;
         const float lo_x = (float)(mx - bx), lo_y = (float)(my - by);
         const float hi_x = (float)(JL.w - mx - 1 - bx), hi_y = (float)(JL.h - my - 1 - by);
         float vx = 0.0f, vy = 0.0f;
@@ -202,9 +218,8 @@ __device__ void lk_track(const DevPyr &I, const DevPyr &J, int top, const LkPrm 
             split(bx, qx, jx, fx);
             split(by, qy, jy, fy);
             float sx, sy;
-            lk_sample<MAXH, false>(JL, jx, fx, jy, fy, W, H, lane, P, sx, sy);
-            const float bxx = sx * LK_Q6_INV, byy = sy * LK_Q6_INV;
-            const float ex = __fmaf_rn(ia, bxx, ib * byy), ey = __fmaf_rn(ib, bxx, ic * byy);
+            lk_sample<MAXH, EXACT, false>(JL, jx, fx, jy, fy, W, H, lane, P, sx, sy);
+            const float ex = __fmaf_rn(ia, sx, ib * sy), ey = __fmaf_rn(ib, sx, ic * sy);
             vx += ex;
             vy += ey;
             iters++;
@@ -237,32 +252,44 @@ __device__ void lk_track(const DevPyr &I, const DevPyr &J, int top, const LkPrm 
             split(bx, qx, jx, fx);
             split(by, qy, jy, fy);
             float sa, ss;
-            lk_sample<MAXH, true>(J0, jx, fx, jy, fy, W, H, lane, P, sa, ss);
+            lk_sample<MAXH, EXACT, true>(J0, jx, fx, jy, fy, W, H, lane, P, sa, ss);
             const float r0 = sa / p.area, r1 = ss / p.area;
             o.residual = r0;
             if (r0 > p.max_residual)
                 status |= VTG_LK_RESIDUAL;
             const float s2 = r1 * p.area / (p.area - 2.0f);
-            o.cov_xx = s2 * gyy0 / det0;
-            o.cov_xy = -s2 * gxy0 / det0;
-            o.cov_yy = s2 * gxx0 / det0;
+            o.cov_xx = s2 * gyy0 * idet0;
+            o.cov_xy = -s2 * gxy0 * idet0;
+            o.cov_yy = s2 * gxx0 * idet0;
         }
     }
     o.status = (uint16_t)status;
 }
 
-/* lk_track then, when asked and the track is good, the forward-backward check (src/kern/lk_driver.inc:111-121). */
-template <int MAXH>
+/* lk_track then, when asked and the track is good, the forward-backward check (src/kern/lk_driver.inc:111-121): the
+ * found point tracked back from J to I from minus the found flow. One copy of the walk serves both passes. */
+template <int MAXH, bool EXACT>
 __device__ __forceinline__ void lk_point(const DevPyr &I, const DevPyr &J, int top, const LkPrm &p, float x, float y,
                                          float gx, float gy, int lane, Patch<MAXH> &P, vtg_lk_out &o)
 {
-    lk_track<MAXH>(I, J, top, p, x, y, gx, gy, lane, P, o);
-    if (p.fb_max2 > 0.0f && o.status == 0) {
-        vtg_lk_out b;
-        lk_track<MAXH>(J, I, top, p, o.x, o.y, x - o.x, y - o.y, lane, P, b);
-        const float ex = b.x - x, ey = b.y - y;
-        if (b.status || __fmaf_rn(ex, ex, ey * ey) > p.fb_max2)
-            o.status |= VTG_LK_FLOWBACK;
+    const int passes = p.fb_max2 > 0.0f ? 2 : 1;
+    float sx = x, sy = y;
+    for (int pass = 0; pass < passes; pass++) {
+        vtg_lk_out r;
+        lk_track<MAXH, EXACT>(pass ? J : I, pass ? I : J, top, p, sx, sy, gx, gy, lane, P, r);
+        if (pass == 0) {
+            o = r;
+            if (o.status)
+                break;
+            sx = o.x;
+            sy = o.y;
+            gx = x - o.x;
+            gy = y - o.y;
+        } else {
+            const float ex = r.x - x, ey = r.y - y;
+            if (r.status || __fmaf_rn(ex, ex, ey * ey) > p.fb_max2)
+                o.status |= VTG_LK_FLOWBACK;
+        }
     }
 }
 
@@ -293,8 +320,8 @@ __device__ __forceinline__ float cell_diff(const DevLevel &A, const DevLevel &B,
     return __fdiv_rn(s, (float)((y1 - y0) * g.cell_w)) * LK_Q6_INV;
 }
 
-template <int MAXH>
-__global__ void __launch_bounds__(256) lk_cells_kernel(const DevPyr *__restrict__ Ip, const DevPyr *__restrict__ Jp,
+template <int MAXH, bool EXACT>
+__global__ void __launch_bounds__(256, 2) lk_cells_kernel(const DevPyr *__restrict__ Ip, const DevPyr *__restrict__ Jp,
                                                        int top, LkPrm p, CellGrid g, int base_w, int base_h,
                                                        vtg_lk_out *__restrict__ out, vtg_cell *__restrict__ cells)
 {
@@ -310,7 +337,7 @@ __global__ void __launch_bounds__(256) lk_cells_kernel(const DevPyr *__restrict_
     y = fminf(fmaxf(y, my), (float)base_h - 1.0f - my);
     Patch<MAXH> P;
     vtg_lk_out o;
-    lk_point<MAXH>(I, J, top, p, x, y, 0.0f, 0.0f, lane, P, o);
+    lk_point<MAXH, EXACT>(I, J, top, p, x, y, 0.0f, 0.0f, lane, P, o);
     if (out)
         store_out(out + i, o, lane);
     if (cells) {
@@ -328,8 +355,8 @@ __global__ void __launch_bounds__(256) lk_cells_kernel(const DevPyr *__restrict_
     }
 }
 
-template <int MAXH>
-__global__ void __launch_bounds__(256) lk_points_kernel(const DevPyr *__restrict__ Ip, const DevPyr *__restrict__ Jp,
+template <int MAXH, bool EXACT>
+__global__ void __launch_bounds__(256, 2) lk_points_kernel(const DevPyr *__restrict__ Ip, const DevPyr *__restrict__ Jp,
                                                         int top, LkPrm p, int n, const float *__restrict__ xs,
                                                         const float *__restrict__ ys, const float *__restrict__ gxs,
                                                         const float *__restrict__ gys, vtg_lk_out *__restrict__ out)
@@ -339,7 +366,7 @@ __global__ void __launch_bounds__(256) lk_points_kernel(const DevPyr *__restrict
         return;
     Patch<MAXH> P;
     vtg_lk_out o;
-    lk_point<MAXH>(*Ip, *Jp, top, p, xs[i], ys[i], gxs ? gxs[i] : 0.0f, gys ? gys[i] : 0.0f, lane, P, o);
+    lk_point<MAXH, EXACT>(*Ip, *Jp, top, p, xs[i], ys[i], gxs ? gxs[i] : 0.0f, gys ? gys[i] : 0.0f, lane, P, o);
     store_out(out + i, o, lane);
 }
 
@@ -347,10 +374,12 @@ cudaError_t vtg_launch_cells(const DevPyr *I, const DevPyr *J, int top, const Lk
                              int base_h, vtg_lk_out *out, vtg_cell *cells, cudaStream_t s)
 {
     const int blocks = (g.n + 7) / 8;
-    if (p.H <= 21)
-        lk_cells_kernel<21><<<blocks, 256, 0, s>>>(I, J, top, p, g, base_w, base_h, out, cells);
+    if (p.H == 21)
+        lk_cells_kernel<21, true><<<blocks, 256, 0, s>>>(I, J, top, p, g, base_w, base_h, out, cells);
+    else if (p.H == 15)
+        lk_cells_kernel<15, true><<<blocks, 256, 0, s>>>(I, J, top, p, g, base_w, base_h, out, cells);
     else
-        lk_cells_kernel<31><<<blocks, 256, 0, s>>>(I, J, top, p, g, base_w, base_h, out, cells);
+        lk_cells_kernel<31, false><<<blocks, 256, 0, s>>>(I, J, top, p, g, base_w, base_h, out, cells);
     return cudaGetLastError();
 }
 
@@ -360,9 +389,11 @@ cudaError_t vtg_launch_points(const DevPyr *I, const DevPyr *J, int top, const L
     const int blocks = (n + 7) / 8;
     if (n <= 0)
         return cudaSuccess;
-    if (p.H <= 21)
-        lk_points_kernel<21><<<blocks, 256, 0, s>>>(I, J, top, p, n, xs, ys, gx, gy, out);
+    if (p.H == 21)
+        lk_points_kernel<21, true><<<blocks, 256, 0, s>>>(I, J, top, p, n, xs, ys, gx, gy, out);
+    else if (p.H == 15)
+        lk_points_kernel<15, true><<<blocks, 256, 0, s>>>(I, J, top, p, n, xs, ys, gx, gy, out);
     else
-        lk_points_kernel<31><<<blocks, 256, 0, s>>>(I, J, top, p, n, xs, ys, gx, gy, out);
+        lk_points_kernel<31, false><<<blocks, 256, 0, s>>>(I, J, top, p, n, xs, ys, gx, gy, out);
     return cudaGetLastError();
 }
