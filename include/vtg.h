@@ -126,6 +126,52 @@ int vtg_points(vtg_tracker *t, int prev, int cur, int top, int n, const float *x
 int vtg_level(vtg_tracker *t, int set, int level, float *out, int where, void *stream);
 /* A level's size. */
 int vtg_level_size(const vtg_tracker *t, int level, int *w, int *h);
+/* The device address of a level of a set (F32 Q6, rows `pitch` floats apart), for searching it in place. Valid until
+ * the tracker is destroyed; its contents change with every vtg_build of that set. */
+int vtg_level_device(const vtg_tracker *t, int set, int level, const float **plane, int *w, int *h, int *pitch);
+
+/* ---- the appearance search (reacquisition) ---- */
+
+/* Plane element types. */
+enum { VTG_PLANE_U8 = 0, VTG_PLANE_F32 = 1 };
+/* Arithmetic of the correlation map: F32 products (CUDA cores), or BF16 / FP16 products with F32 accumulation on the
+ * tensor cores (U8 planes). Window sums are exact in every case; the final scores of the eight candidates are always
+ * F32. */
+enum { VTG_NCC_F32 = 0, VTG_NCC_BF16 = 1, VTG_NCC_FP16 = 2 };
+#define VTG_NCC_MAX_T 128
+
+/* What a search found: struct found (src/kern/track.c:1608-1612) plus take_back's parabola offsets
+ * (track.c:1741-1742). hx, hy: the template's corner in half pixels of the plane; ncc: its score; second: the best
+ * score clear of it by half a template (-2 if none); ox, oy: sub-half-pixel offsets in [-0.5, 0.5]; ntop: candidates
+ * looked at; cells: cells of the map. */
+struct vtg_found {
+    int hx, hy;
+    float ncc, second, ox, oy;
+    int ntop, cells;
+};
+
+typedef struct vtg_search vtg_search;
+
+/* Device bytes of a search context for planes up to max_w x max_h and templates up to max_tw x max_th. */
+size_t vtg_search_bytes(int max_w, int max_h, int max_tw, int max_th);
+/* A search context: its template, the integral images, the per-cell map and the candidates, in one allocation charged
+ * to the context's budget. */
+int vtg_search_create(vtg_ctx *ctx, int max_w, int max_h, int max_tw, int max_th, vtg_search **out);
+void vtg_search_destroy(vtg_search *s);
+void *vtg_search_stream(const vtg_search *s);
+/* The template (store_appearance, src/kern/track.c:935-974): th rows of tw zero-mean floats (tw a multiple of 8) and
+ * norm, the sum of their squares. Host or device memory as `where` says. */
+int vtg_search_template(vtg_search *s, const float *app, int tw, int th, float norm, int where, void *stream);
+/* search_slot (src/kern/track.c:1661-1726) over corners [x0, x1] x [y0, y1] of a plane (w x h, rows `pitch` elements
+ * apart, device memory, type VTG_PLANE_*), at `step`; the window is clamped to where the template fits as the
+ * reference clamps it. `precision` VTG_NCC_*. *found (and, if not NULL, the per-cell map of `cells` entries) in host
+ * or device memory as `where` says. */
+int vtg_search_run(vtg_search *s, const void *plane, int w, int h, int pitch, int plane_type, int x0, int x1, int y0,
+                   int y1, int step, int precision, struct vtg_found *found, float *map_v, int *map_x, int *map_y,
+                   int where, void *stream);
+/* tk_correlate (src/kern/track.c:208, track.h:59) at n corners: the score of each, -1 where the template does not fit. */
+int vtg_correlate(vtg_search *s, const void *plane, int w, int h, int pitch, int plane_type, int n, const int *xs,
+                  const int *ys, float *out, int where, void *stream);
 
 #ifdef __cplusplus
 }

@@ -10,9 +10,12 @@
 #include <thread>
 #include <vector>
 
+#include "vtg_ctx.h"
 #include "vtg_internal.cuh"
 
 static thread_local int g_last_cuda = 0;
+
+void vtg_set_cuda_error(cudaError_t e) { g_last_cuda = (int)e; }
 
 #define CU(call)                                                                                                       \
     do {                                                                                                               \
@@ -28,7 +31,39 @@ struct vtg_ctx {
     size_t budget, used;
     std::mutex mu;
     std::vector<vtg_tracker *> trackers;
+    std::vector<cudaStream_t> streams; /* of the other objects (search contexts, batches) */
 };
+
+int vtg_ctx_charge(vtg_ctx *ctx, size_t bytes)
+{
+    std::lock_guard<std::mutex> g(ctx->mu);
+    if (ctx->budget && ctx->used + bytes > ctx->budget)
+        return VTG_EBUDGET;
+    ctx->used += bytes;
+    return VTG_OK;
+}
+
+void vtg_ctx_release(vtg_ctx *ctx, size_t bytes)
+{
+    std::lock_guard<std::mutex> g(ctx->mu);
+    ctx->used -= bytes;
+}
+
+int vtg_ctx_device(const vtg_ctx *ctx) { return ctx->device; }
+
+void vtg_ctx_track(vtg_ctx *ctx, cudaStream_t s, bool add)
+{
+    std::lock_guard<std::mutex> g(ctx->mu);
+    if (add) {
+        ctx->streams.push_back(s);
+        return;
+    }
+    for (size_t i = 0; i < ctx->streams.size(); i++)
+        if (ctx->streams[i] == s) {
+            ctx->streams.erase(ctx->streams.begin() + (long)i);
+            return;
+        }
+}
 
 struct vtg_tracker {
     vtg_ctx *ctx;
@@ -113,6 +148,8 @@ extern "C" int vtg_ctx_sync(vtg_ctx *ctx, int timeout_ms)
         std::lock_guard<std::mutex> g(ctx->mu);
         for (vtg_tracker *t : ctx->trackers)
             streams.push_back(t->stream);
+        for (cudaStream_t s : ctx->streams)
+            streams.push_back(s);
     }
     const auto deadline = std::chrono::steady_clock::now() + std::chrono::milliseconds(timeout_ms < 0 ? 0 : timeout_ms);
     for (cudaStream_t s : streams) {
@@ -428,6 +465,20 @@ extern "C" int vtg_points(vtg_tracker *t, int prev, int cur, int top, int n, con
     CU(vtg_launch_points(t->desc + 2 * prev, t->desc + 2 * cur, top, t->prm, n, dx, dy, dgx, dgy, dout, s));
     CU(cudaMemcpyAsync(out, dout, (size_t)n * sizeof(vtg_lk_out), cudaMemcpyDeviceToHost, s));
     CU(cudaFreeAsync(d, s));
+    return VTG_OK;
+}
+
+extern "C" int vtg_level_device(const vtg_tracker *t, int set, int level, const float **plane, int *w, int *h, int *pitch)
+{
+    if (!t || !plane || set < 0 || set > 1 || level < 0 || level >= t->levels)
+        return VTG_EINVAL;
+    *plane = t->sets[set] + t->loff[level];
+    if (w)
+        *w = t->lw[level];
+    if (h)
+        *h = t->lh[level];
+    if (pitch)
+        *pitch = t->lpitch[level];
     return VTG_OK;
 }
 

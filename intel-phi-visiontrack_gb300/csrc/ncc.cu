@@ -1,0 +1,455 @@
+/* ncc.cu -- the appearance search: zero-mean normalised cross-correlation of a T_w x T_h template over a window of
+ * corners, the best corner of every 16 x 16 cell of corners, the eight best cells looked at again in half pixels, the
+ * best and the second peak, and the parabola's sub-half-pixel offsets.
+ *
+ * Reference: search_at / tk_correlate (src/kern/track.c:184-208), OP_SEARCH (track.c:301-329), search_slot
+ * (track.c:1661-1726), search_half (track.c:1615-1647), peak_offset (track.c:1650-1657), take_back (track.c:1737-1775).
+ * The reference's template is 32 x 21 on a Q6 plane; here T_w (a multiple of 8, <= 128) x T_h (<= 128) on an 8-bit or
+ * Q6 plane.
+ *
+ * Score at corner (x, y): st = sum t (J - J(x, y)); var = sum J^2 - (sum J)^2 / n; 0 when var <= norm / 16 or
+ * norm <= 0, else st / sqrt(norm var). The window sums come from exact int64 integral images (sum J and sum J^2), so the
+ * near-blank rule compares an exact integer n var with n norm / 16 and never lets a flat window through.
+ *
+ * Pipeline (all on one stream, no host round trip):
+ *   integral_rows / integral_cols  int64 tables of J and J^2 ((h + 1) x (w + 1)), exact
+ *   ncc_map_f32 (or the tensor-core map in ncc_tc.cu)  per cell: best score and its corner
+ *   ncc_top                       the eight best cells, value descending then cell index ascending (the reference's
+ *                                 insertion order)
+ *   ncc_refine                    each candidate in half pixels within +-(2 step - 1) (or +-1), the best, the second
+ *                                 peak clear of it by half a template, and the parabola offsets; F32 products with exact
+ *                                 integer (quarter-pixel) window sums. */
+#include <float.h>
+
+#include "vtg_internal.cuh"
+#include "vtg_ncc.cuh"
+
+/* ---- integral images ---- */
+
+template <typename T>
+__device__ __forceinline__ long long pix(const T *p, size_t i)
+{
+    return (long long)__ldg(p + i);
+}
+
+/* Row pass: table row y + 1, columns 1 .. w, holds the prefix of row y (and of its squares). One warp per row. */
+template <typename T>
+__global__ void integral_rows(const T *__restrict__ plane, int pitch, int w, int h, long long *__restrict__ S1,
+                              long long *__restrict__ S2, int tp)
+{
+    const int lane = threadIdx.x & 31;
+    const int y = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (y > h)
+        return;
+    long long *r1 = S1 + (size_t)y * tp, *r2 = S2 + (size_t)y * tp;
+    if (y == 0) {
+        for (int x = lane; x <= w; x += 32)
+            r1[x] = r2[x] = 0;
+        return;
+    }
+    if (lane == 0)
+        r1[0] = r2[0] = 0;
+    long long c1 = 0, c2 = 0;
+    const T *src = plane + (size_t)(y - 1) * pitch;
+    for (int x0 = 0; x0 < w; x0 += 32) {
+        const int x = x0 + lane;
+        long long v1 = x < w ? pix(src, x) : 0;
+        long long v2 = v1 * v1;
+#pragma unroll
+        for (int s = 1; s < 32; s <<= 1) {
+            const long long a = __shfl_up_sync(VTG_FULL, v1, s), b = __shfl_up_sync(VTG_FULL, v2, s);
+            if (lane >= s) {
+                v1 += a;
+                v2 += b;
+            }
+        }
+        if (x < w) {
+            r1[x + 1] = c1 + v1;
+            r2[x + 1] = c2 + v2;
+        }
+        c1 += __shfl_sync(VTG_FULL, v1, 31);
+        c2 += __shfl_sync(VTG_FULL, v2, 31);
+    }
+}
+
+/* Column pass: running sums down the rows, one thread per column. */
+__global__ void integral_cols(int w, int h, long long *__restrict__ S1, long long *__restrict__ S2, int tp)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x > w)
+        return;
+    long long a = 0, b = 0;
+    for (int y = 1; y <= h; y++) {
+        const size_t i = (size_t)y * tp + x;
+        a += S1[i];
+        b += S2[i];
+        S1[i] = a;
+        S2[i] = b;
+    }
+}
+
+/* ---- the score, shared by every map kernel ---- */
+
+__device__ __forceinline__ long long box(const long long *S, int tp, int x, int y, int tw, int th)
+{
+    const long long *a = S + (size_t)y * tp + x, *b = S + (size_t)(y + th) * tp + x;
+    return b[tw] - b[0] - a[tw] + a[0];
+}
+
+/* score from st and the exact window sums; -1 where the corner is outside the reference's bounds. */
+__device__ __forceinline__ float ncc_score(float st, long long s1, long long s2, const NccPrm &p)
+{
+    const long long nvar = (long long)p.n * s2 - s1 * s1; /* n var, exact */
+    if ((double)nvar <= (double)p.n * (double)p.norm * 0.0625 || p.norm <= 0.0f)
+        return 0.0f;
+    const float var = (float)nvar / (float)p.n;
+    return st / sqrtf(p.norm * var);
+}
+
+/* ---- the map, F32 products: one CTA per cell ---- */
+
+/* A cell's best: value descending, then row-major scan order (the first maximum wins, as OP_SEARCH's strict > does). */
+__device__ __forceinline__ bool better(float v, int k, float bv, int bk) { return v > bv || (v == bv && k < bk); }
+
+template <typename T>
+__global__ void __launch_bounds__(256) ncc_map_f32(const T *__restrict__ plane, int pitch, const float *__restrict__ app,
+                                                   NccPrm p, const long long *__restrict__ S1,
+                                                   const long long *__restrict__ S2, int tp, float *__restrict__ map_v,
+                                                   int *__restrict__ map_x, int *__restrict__ map_y)
+{
+    extern __shared__ float sm[];
+    const int cell = blockIdx.x;
+    const int cx0 = p.x0 + (cell % p.ccols) * NCC_CELL, cy0 = p.y0 + (cell / p.ccols) * NCC_CELL;
+    const int cx1 = min(cx0 + NCC_CELL, p.x1 + 1), cy1 = min(cy0 + NCC_CELL, p.y1 + 1);
+    const int iw = NCC_CELL + p.tw, ih = NCC_CELL + p.th;
+    float *s_app = sm, *s_img = sm + p.tw * p.th;
+    for (int i = threadIdx.x; i < p.tw * p.th; i += blockDim.x)
+        s_app[i] = app[i];
+    for (int i = threadIdx.x; i < iw * ih; i += blockDim.x) {
+        const int r = i / iw, c = i - r * iw;
+        const int yy = min(cy0 + r, p.h - 1), xx = min(cx0 + c, p.w - 1);
+        s_img[i] = (float)__ldg(plane + (size_t)yy * pitch + xx);
+    }
+    __syncthreads();
+    const int per = NCC_CELL / p.step;
+    const int a = threadIdx.x % NCC_CELL, b = threadIdx.x / NCC_CELL;
+    float v = -2.0f;
+    int key = 1 << 30;
+    if (a < per && b < per) {
+        const int x = cx0 + a * p.step, y = cy0 + b * p.step;
+        if (x < cx1 && y < cy1) {
+            key = b * per + a;
+            const float *im = s_img + (y - cy0) * iw + (x - cx0);
+            const float first = im[0];
+            float s0 = 0.f, s1 = 0.f;
+            for (int i = 0; i < p.th; i++) {
+                const float *row = im + i * iw, *t = s_app + i * p.tw;
+                for (int j = 0; j < p.tw; j += 2) {
+                    s0 = __fmaf_rn(row[j] - first, t[j], s0);
+                    s1 = __fmaf_rn(row[j + 1] - first, t[j + 1], s1);
+                }
+            }
+            v = ncc_score(s0 + s1, box(S1, tp, x, y, p.tw, p.th), box(S2, tp, x, y, p.tw, p.th), p);
+        }
+    }
+    /* block argmax */
+    __shared__ float rv[8];
+    __shared__ int rk[8];
+#pragma unroll
+    for (int s = 16; s >= 1; s >>= 1) {
+        const float ov = __shfl_xor_sync(VTG_FULL, v, s);
+        const int ok = __shfl_xor_sync(VTG_FULL, key, s);
+        if (better(ov, ok, v, key)) {
+            v = ov;
+            key = ok;
+        }
+    }
+    const int warp = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        rv[warp] = v;
+        rk[warp] = key;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float bv = rv[0];
+        int bk = rk[0];
+        for (int k = 1; k < 8; k++)
+            if (better(rv[k], rk[k], bv, bk)) {
+                bv = rv[k];
+                bk = rk[k];
+            }
+        if (bk >= (1 << 30)) { /* no corner: the reference leaves top at -2 and the cell origin */
+            map_v[cell] = -2.0f;
+            map_x[cell] = cx0;
+            map_y[cell] = cy0;
+        } else {
+            /* a cell whose every corner reads -1 (out of bounds) keeps -2 and its origin, as `v > top` never fires */
+            const bool fired = bv > -2.0f;
+            map_v[cell] = fired ? bv : -2.0f;
+            map_x[cell] = fired ? cx0 + (bk % per) * p.step : cx0;
+            map_y[cell] = fired ? cy0 + (bk / per) * p.step : cy0;
+        }
+    }
+}
+
+/* ---- the eight best cells ---- */
+
+__device__ __forceinline__ unsigned long long top_key(float v, int i)
+{
+    if (!(v > -2.0f))
+        return 0ull;
+    unsigned u = __float_as_uint(v);
+    u = (u & 0x80000000u) ? ~u : (u | 0x80000000u); /* ascending float order as unsigned */
+    return ((unsigned long long)u << 32) | (unsigned long long)(0xFFFFFFFFu - (unsigned)i);
+}
+
+__device__ __forceinline__ void top_insert(unsigned long long *t, unsigned long long k)
+{
+    if (k <= t[NCC_TOP - 1])
+        return;
+    int at = NCC_TOP - 1;
+    while (at > 0 && t[at - 1] < k) {
+        t[at] = t[at - 1];
+        at--;
+    }
+    t[at] = k;
+}
+
+__global__ void __launch_bounds__(256) ncc_top(const float *__restrict__ map_v, int cells, int *__restrict__ top,
+                                               int *__restrict__ ntop)
+{
+    __shared__ unsigned long long s[256][NCC_TOP];
+    unsigned long long t[NCC_TOP];
+#pragma unroll
+    for (int k = 0; k < NCC_TOP; k++)
+        t[k] = 0ull;
+    for (int i = threadIdx.x; i < cells; i += blockDim.x)
+        top_insert(t, top_key(map_v[i], i));
+#pragma unroll
+    for (int k = 0; k < NCC_TOP; k++)
+        s[threadIdx.x][k] = t[k];
+    __syncthreads();
+    for (int half = 128; half >= 1; half >>= 1) {
+        if (threadIdx.x < half) {
+            for (int k = 0; k < NCC_TOP; k++)
+                top_insert(t, s[threadIdx.x + half][k]);
+            for (int k = 0; k < NCC_TOP; k++)
+                s[threadIdx.x][k] = t[k];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        int n = 0;
+        for (int k = 0; k < NCC_TOP; k++) {
+            if (t[k] == 0ull)
+                break;
+            top[n++] = (int)(0xFFFFFFFFu - (unsigned)(t[k] & 0xFFFFFFFFull));
+        }
+        *ntop = n;
+    }
+}
+
+/* ---- half-pixel refinement (search_half, search_slot's second half, take_back's parabola) ---- */
+
+/* One warp scores one corner in half pixels: F32 products, exact quarter-pixel sums for the variance. */
+template <typename T>
+__device__ float half_score(const T *__restrict__ plane, int pitch, const float *__restrict__ app, const NccPrm &p,
+                            int hx, int hy, int lane)
+{
+    const int x = hx >> 1, y = hy >> 1, ox = hx & 1, oy = hy & 1;
+    if (x < 1 || y < 1 || x + p.tw + 1 >= p.w - 1 || y + p.th + 1 >= p.h - 1)
+        return -1.0f;
+    const float first = (float)__ldg(plane + (size_t)y * pitch + x);
+    float st = 0.0f;
+    long long q1 = 0, q2 = 0; /* in quarters */
+    for (int k = lane; k < p.tw * p.th; k += 32) {
+        const int i = k / p.tw, j = k - i * p.tw;
+        const T *r0 = plane + (size_t)(y + i) * pitch + x + j, *r1 = r0 + pitch;
+        long long a = (long long)__ldg(r0), b = ox ? (long long)__ldg(r0 + 1) : a;
+        long long q = 2 * (a + b);
+        if (oy) {
+            const long long c = (long long)__ldg(r1), d = ox ? (long long)__ldg(r1 + 1) : c;
+            q = (q + 2 * (c + d)) / 2;
+        }
+        q1 += q;
+        q2 += q * q;
+        st = __fmaf_rn((float)q * 0.25f - first, app[k], st);
+    }
+#pragma unroll
+    for (int s = 16; s >= 1; s >>= 1) {
+        st += __shfl_xor_sync(VTG_FULL, st, s);
+        q1 += __shfl_xor_sync(VTG_FULL, q1, s);
+        q2 += __shfl_xor_sync(VTG_FULL, q2, s);
+    }
+    const long long nvar16 = (long long)p.n * q2 - q1 * q1; /* 16 n var, exact */
+    if ((double)nvar16 <= 16.0 * (double)p.n * (double)p.norm * 0.0625 || p.norm <= 0.0f)
+        return 0.0f;
+    const float var = (float)nvar16 / (16.0f * (float)p.n);
+    return st / sqrtf(p.norm * var);
+}
+
+__device__ __forceinline__ float parabola(float l, float c, float r)
+{
+    const float den = l - 2.0f * c + r;
+    if (den >= 0.0f)
+        return 0.0f;
+    const float o = 0.5f * (l - r) / den;
+    return fminf(fmaxf(o, -0.5f), 0.5f);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(NCC_TOP * 32) ncc_refine(const T *__restrict__ plane, int pitch,
+                                                           const float *__restrict__ app, NccPrm p,
+                                                           const float *__restrict__ map_v, const int *__restrict__ map_x,
+                                                           const int *__restrict__ map_y, const int *__restrict__ top,
+                                                           const int *__restrict__ ntop, vtg_found *__restrict__ out)
+{
+    __shared__ float s_score[NCC_TOP];
+    __shared__ int s_hx[NCC_TOP], s_hy[NCC_TOP];
+    __shared__ float s_side[4];
+    const int c = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int n = *ntop;
+    const int around = p.step > 1 ? 2 * p.step - 1 : 1;
+    if (c < n) {
+        const int cell = top[c];
+        const int cx = 2 * map_x[cell], cy = 2 * map_y[cell];
+        float best = -2.0f;
+        int bx = cx, by = cy;
+        for (int hy = cy - around; hy <= cy + around; hy++)
+            for (int hx = cx - around; hx <= cx + around; hx++) {
+                const float v = half_score(plane, pitch, app, p, hx, hy, lane);
+                if (v > best) {
+                    best = v;
+                    bx = hx;
+                    by = hy;
+                }
+            }
+        if (lane == 0) {
+            s_score[c] = best;
+            s_hx[c] = bx;
+            s_hy[c] = by;
+        }
+    }
+    __syncthreads();
+    if (c == 0) {
+        float ncc = -2.0f, second = -2.0f;
+        int hx = 0, hy = 0;
+        for (int k = 0; k < n; k++)
+            if (s_score[k] > ncc) {
+                ncc = s_score[k];
+                hx = s_hx[k];
+                hy = s_hy[k];
+            }
+        for (int k = 0; k < n; k++) {
+            const int dx = s_hx[k] - hx, dy = s_hy[k] - hy;
+            if ((dx * dx > p.tw * p.tw || dy * dy > p.th * p.th) && s_score[k] > second)
+                second = s_score[k];
+        }
+        float ox = 0.0f, oy = 0.0f;
+        if (n > 0) {
+            const float l = half_score(plane, pitch, app, p, hx - 1, hy, lane);
+            const float r = half_score(plane, pitch, app, p, hx + 1, hy, lane);
+            const float u = half_score(plane, pitch, app, p, hx, hy - 1, lane);
+            const float d = half_score(plane, pitch, app, p, hx, hy + 1, lane);
+            ox = parabola(l, ncc, r);
+            oy = parabola(u, ncc, d);
+        }
+        if (lane == 0) {
+            vtg_found f;
+            f.hx = hx;
+            f.hy = hy;
+            f.ncc = ncc;
+            f.second = second;
+            f.ox = ox;
+            f.oy = oy;
+            f.ntop = n;
+            f.cells = p.ccols * p.crows;
+            *out = f;
+        }
+    }
+    (void)s_side;
+}
+
+/* ---- corners one by one (tk_correlate): one warp per corner ---- */
+
+template <typename T>
+__global__ void ncc_corners(const T *__restrict__ plane, int pitch, const float *__restrict__ app, NccPrm p, int count,
+                            const int *__restrict__ xs, const int *__restrict__ ys, float *__restrict__ out)
+{
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (i >= count)
+        return;
+    /* a whole-pixel corner is the half-pixel corner (2x, 2y) with the bounds of search_at */
+    const int x = xs[i], y = ys[i];
+    float v;
+    if (x < 1 || y < 1 || x + p.tw >= p.w - 1 || y + p.th >= p.h - 1) {
+        v = -1.0f;
+    } else {
+        const float first = (float)__ldg(plane + (size_t)y * pitch + x);
+        float st = 0.0f;
+        long long q1 = 0, q2 = 0;
+        for (int k = lane; k < p.tw * p.th; k += 32) {
+            const int r = k / p.tw, j = k - r * p.tw;
+            const long long q = (long long)__ldg(plane + (size_t)(y + r) * pitch + x + j);
+            q1 += q;
+            q2 += q * q;
+            st = __fmaf_rn((float)q - first, app[k], st);
+        }
+#pragma unroll
+        for (int s = 16; s >= 1; s >>= 1) {
+            st += __shfl_xor_sync(VTG_FULL, st, s);
+            q1 += __shfl_xor_sync(VTG_FULL, q1, s);
+            q2 += __shfl_xor_sync(VTG_FULL, q2, s);
+        }
+        v = ncc_score(st, q1, q2, p);
+    }
+    if (lane == 0)
+        out[i] = v;
+}
+
+/* ---- launchers ---- */
+
+template <typename T>
+static cudaError_t launch_all(const T *plane, int pitch, const float *app, const NccPrm &p, const NccScratch &s,
+                              int map_kind, vtg_found *out, cudaStream_t st)
+{
+    integral_rows<T><<<(p.h + 1 + 7) / 8, 256, 0, st>>>(plane, pitch, p.w, p.h, s.S1, s.S2, s.tp);
+    integral_cols<<<(p.w + 1 + 255) / 256, 256, 0, st>>>(p.w, p.h, s.S1, s.S2, s.tp);
+    const int cells = p.ccols * p.crows;
+    cudaError_t e = cudaSuccess;
+    if (map_kind == VTG_NCC_F32) {
+        const size_t smem = sizeof(float) * ((size_t)p.tw * p.th + (size_t)(NCC_CELL + p.tw) * (NCC_CELL + p.th));
+        e = cudaFuncSetAttribute(ncc_map_f32<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess)
+            return e;
+        ncc_map_f32<T><<<cells, 256, smem, st>>>(plane, pitch, app, p, s.S1, s.S2, s.tp, s.map_v, s.map_x, s.map_y);
+    } else {
+        e = vtg_launch_ncc_map_tc(plane, pitch, sizeof(T), p, s, map_kind, st);
+        if (e != cudaSuccess)
+            return e;
+    }
+    ncc_top<<<1, 256, 0, st>>>(s.map_v, cells, s.top, s.ntop);
+    ncc_refine<T><<<1, NCC_TOP * 32, 0, st>>>(plane, pitch, app, p, s.map_v, s.map_x, s.map_y, s.top, s.ntop, out);
+    return cudaGetLastError();
+}
+
+cudaError_t vtg_launch_ncc(const void *plane, int pitch, int plane_type, const float *app, const NccPrm &p,
+                           const NccScratch &s, int map_kind, vtg_found *out, cudaStream_t st)
+{
+    if (plane_type == VTG_PLANE_U8)
+        return launch_all((const uint8_t *)plane, pitch, app, p, s, map_kind, out, st);
+    return launch_all((const float *)plane, pitch, app, p, s, map_kind, out, st);
+}
+
+cudaError_t vtg_launch_ncc_corners(const void *plane, int pitch, int plane_type, const float *app, const NccPrm &p,
+                                   int count, const int *xs, const int *ys, float *out, cudaStream_t st)
+{
+    const int blocks = (count + 7) / 8;
+    if (count <= 0)
+        return cudaSuccess;
+    if (plane_type == VTG_PLANE_U8)
+        ncc_corners<uint8_t><<<blocks, 256, 0, st>>>((const uint8_t *)plane, pitch, app, p, count, xs, ys, out);
+    else
+        ncc_corners<float><<<blocks, 256, 0, st>>>((const float *)plane, pitch, app, p, count, xs, ys, out);
+    return cudaGetLastError();
+}

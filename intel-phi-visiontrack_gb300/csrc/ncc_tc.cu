@@ -1,0 +1,366 @@
+/* ncc_tc.cu -- the correlation map on the 5th-generation tensor cores: tcgen05.mma (kind::f16, BF16 or FP16 products,
+ * F32 accumulation in tensor memory), operands from shared memory through matrix descriptors, the accumulator read back
+ * with tcgen05.ld, scored against exact int64 window sums and reduced to the per-cell map in the epilogue.
+ *
+ * The correlation as a GEMM. A CTA owns a tile of corners: 1024 consecutive x (X0 + 8 m + s, m < 128, s < 8) by 16
+ * consecutive y (Y0 + q). Then
+ *     st(X0 + 8 m + s, Y0 + q) = sum over image rows r, columns c of  A_r[m][c] * B_r[(q, s)][c]
+ * with A_r[m][c] = J[r][X0 + 8 m + c] and B_r[(q, s)][c] = t[r - Y0 - q][c - s] (zero outside the template). So D =
+ * sum_r A_r B_r^T: M = 128, N = 8 x 16 = 128, K = the image rows of the tile's band times K_row = T_w + 8 rounded up
+ * to 16.
+ *   A needs no im2col. Consecutive rows of A_r start 8 elements (16 bytes) apart in the image row, so a K-major,
+ *   no-swizzle descriptor with 16-byte rows in a core matrix, a 16-byte leading (K) offset and a 128-byte stride (M)
+ *   offset reads A_r straight from the row staged once in shared memory: address(m, k) = row + 2 (8 m + k).
+ *   B_r depends only on r - Y0, so the band (16 + T_h - 1 blocks of 128 x K_row) is built once per template, already in
+ *   the canonical core-matrix layout, and streamed from L2 into shared memory per image row.
+ * The epilogue: each of the 128 threads owns one accumulator row (8 x-corners, 16 y-corners): it subtracts
+ * J(x, y) sum t (the reference's st is relative to the corner's first pixel), forms the score with the exact int64
+ * window sums, keeps its best per cell, and pairs with its neighbour lane (two rows = one 16 x 16 cell).
+ *
+ * The pipeline has three shared-memory stages: all threads stage row r (bytes to BF16/FP16) and its band block, fence
+ * them to the async proxy, and one thread issues the MMAs and commits them to the stage's mbarrier, which the stage's
+ * next filling waits for. Every wait is bounded: past the limit the kernel records an error word and stops issuing. */
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include "vtg_ncc.cuh"
+
+#define TC_M 128
+#define TC_Q 16
+#define TC_N (8 * TC_Q)
+#define TC_XS (8 * TC_M) /* x-corners of a tile */
+#define TC_STAGES 3
+#define TC_TMEM_COLS 128
+#define TC_WAIT_NS 2000000000ull /* a wait gives up after 2 s of the global timer */
+
+static inline int tc_krow(int tw) { return ((tw + 8 + 15) / 16) * 16; }
+
+size_t vtg_ncc_band_bytes(int tw, int th) { return (size_t)(TC_Q + th - 1) * TC_N * tc_krow(tw) * sizeof(uint16_t); }
+
+/* ---- the band ---- */
+
+__device__ __forceinline__ uint16_t to16(float v, int kind)
+{
+    return kind == VTG_NCC_BF16 ? __bfloat16_as_ushort(__float2bfloat16_rn(v)) : __half_as_ushort(__float2half_rn(v));
+}
+
+__device__ __forceinline__ float from16(uint16_t v, int kind)
+{
+    return kind == VTG_NCC_BF16 ? __bfloat162float(__ushort_as_bfloat16(v)) : __half2float(__ushort_as_half(v));
+}
+
+/* Band block k (image row Y0 + k of a tile), element (n = 8 q + s, c) at core matrix (c / 8, n / 8), row n % 8, column
+ * c % 8: core matrices of 8 x 8 elements (128 bytes), K-chunks of 8 columns N / 8 matrices apart. */
+__global__ void ncc_band_kernel(const float *__restrict__ app, int tw, int th, int kind, int krow, int rows,
+                                uint16_t *__restrict__ band)
+{
+    const size_t per = (size_t)TC_N * krow;
+    const size_t total = per * rows;
+    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total; idx += (size_t)gridDim.x * blockDim.x) {
+        const int k = (int)(idx / per);
+        const int rem = (int)(idx - (size_t)k * per);
+        const int n = rem / krow, c = rem - n * krow;
+        const int q = n >> 3, s = n & 7;
+        const int i = k - q, j = c - s;
+        const float v = (i >= 0 && i < th && j >= 0 && j < tw) ? app[i * tw + j] : 0.0f;
+        const size_t off = (size_t)k * per + ((size_t)(c >> 3) * (TC_N / 8) + (n >> 3)) * 64 + (n & 7) * 8 + (c & 7);
+        band[off] = to16(v, kind);
+    }
+}
+
+/* The sum of the template as the tensor cores see it (its rounded values), in double. */
+__global__ void ncc_band_sum(const float *__restrict__ app, int count, int kind, float *__restrict__ out)
+{
+    __shared__ double s[256];
+    double a = 0.0;
+    for (int i = threadIdx.x; i < count; i += blockDim.x)
+        a += (double)from16(to16(app[i], kind), kind);
+    s[threadIdx.x] = a;
+    __syncthreads();
+    for (int h = 128; h >= 1; h >>= 1) {
+        if (threadIdx.x < h)
+            s[threadIdx.x] += s[threadIdx.x + h];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        *out = (float)s[0];
+}
+
+cudaError_t vtg_launch_ncc_band(const float *app, int tw, int th, int kind, uint16_t *band, float *sum_t, cudaStream_t st)
+{
+    const int krow = tc_krow(tw), rows = TC_Q + th - 1;
+    const size_t total = (size_t)TC_N * krow * rows;
+    const int blocks = (int)((total + 255) / 256 < 4096 ? (total + 255) / 256 : 4096);
+    ncc_band_kernel<<<blocks, 256, 0, st>>>(app, tw, th, kind, krow, rows, band);
+    ncc_band_sum<<<1, 256, 0, st>>>(app, tw * th, kind, sum_t);
+    return cudaGetLastError();
+}
+
+/* ---- PTX helpers ---- */
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+/* A tcgen05 shared-memory matrix descriptor, no swizzle: start, leading (K) and stride (M/N) byte offsets, all in
+ * 16-byte units, and the fixed version bits 46-48 = 0b001. */
+__device__ __forceinline__ uint64_t mdesc(uint32_t addr, uint32_t lbo, uint32_t sbo)
+{
+    return (uint64_t)((addr >> 4) & 0x3FFF) | ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | (1ull << 46);
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t a, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ uint64_t globaltimer()
+{
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+/* Bounded wait on an mbarrier phase: true when the phase with this parity completed, false after TC_WAIT_NS. */
+__device__ __forceinline__ bool mbar_wait(uint32_t a, uint32_t parity)
+{
+    const uint64_t t0 = globaltimer();
+    for (;;) {
+        uint32_t done;
+        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+                     : "=r"(done)
+                     : "r"(a), "r"(parity), "r"(100000u)
+                     : "memory");
+        if (done)
+            return true;
+        if (globaltimer() - t0 > TC_WAIT_NS)
+            return false;
+    }
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accumulate)
+{
+    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %4, 0;\n\ttcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(
+                     tmem_d),
+                 "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+                 : "memory");
+}
+
+__device__ __forceinline__ void tc_commit(uint32_t mbar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar) : "memory");
+}
+
+__device__ __forceinline__ void tc_ld32(uint32_t taddr, float (&v)[32])
+{
+    uint32_t r[32];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+                 "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+                   "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]),
+                   "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]),
+                   "=r"(r[30]), "=r"(r[31])
+                 : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; i++)
+        v[i] = __uint_as_float(r[i]);
+}
+
+/* ---- the map ---- */
+
+__device__ __forceinline__ long long tbox(const long long *S, int tp, int x, int y, int tw, int th)
+{
+    const long long *a = S + (size_t)y * tp + x, *b = S + (size_t)(y + th) * tp + x;
+    return b[tw] - b[0] - a[tw] + a[0];
+}
+
+__device__ __forceinline__ bool tbetter(float v, int k, float bv, int bk) { return v > bv || (v == bv && k < bk); }
+
+struct TcSmem {
+    uint32_t a_bytes, b_bytes, stage_bytes, total;
+};
+
+static TcSmem tc_smem(int krow)
+{
+    TcSmem s;
+    s.a_bytes = (uint32_t)((((TC_XS + krow) * 2) + 127) & ~127);
+    s.b_bytes = (uint32_t)(TC_N * krow * 2);
+    s.stage_bytes = s.a_bytes + s.b_bytes;
+    s.total = TC_STAGES * s.stage_bytes + 128; /* + mbarriers and the tensor-memory address */
+    if (s.total < 64 * 1024)
+        s.total = 64 * 1024; /* at most three CTAs an SM: 3 x 128 tensor-memory columns fit its 512 */
+    return s;
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(128, 1) ncc_map_tc(const uint8_t *__restrict__ plane, int pitch, NccPrm p,
+                                                     const uint16_t *__restrict__ band, int krow, int tiles_x,
+                                                     uint32_t a_bytes, uint32_t stage_bytes,
+                                                     const long long *__restrict__ S1, const long long *__restrict__ S2,
+                                                     int tp, float *__restrict__ map_v, int *__restrict__ map_x,
+                                                     int *__restrict__ map_y, int *__restrict__ err)
+{
+    extern __shared__ __align__(1024) uint8_t smem[];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
+    const int X0 = p.x0 + tx * TC_XS, Y0 = p.y0 + ty * TC_Q;
+    const int nk = TC_Q + p.th - 1;
+    const int kchunks = krow / 16;
+    uint8_t *ctl = smem + TC_STAGES * stage_bytes;
+    const uint32_t mbar0 = smem_u32(ctl);
+    uint32_t *tmem_slot = (uint32_t *)(ctl + 64);
+
+    if (tid == 0) {
+        for (int s = 0; s < TC_STAGES; s++)
+            mbar_init(mbar0 + 8 * s, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(TC_TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+
+    const int fmt = KIND == VTG_NCC_BF16 ? 1 : 0;
+    const uint32_t idesc = (1u << 4) | ((uint32_t)fmt << 7) | ((uint32_t)fmt << 10) | ((uint32_t)(TC_N >> 3) << 17) |
+                           ((uint32_t)(TC_M >> 4) << 24);
+    const int row_elems = TC_XS + krow;
+    bool ok = true;
+
+    for (int k = 0; k < nk; k++) {
+        const int s = k % TC_STAGES;
+        uint8_t *sa = smem + s * stage_bytes, *sb = sa + a_bytes;
+        /* the stage's previous MMAs must be done before it is refilled: thread 0 waits, the block agrees */
+        int good = 1;
+        if (k >= TC_STAGES && tid == 0)
+            good = mbar_wait(mbar0 + 8 * s, (uint32_t)((k / TC_STAGES - 1) & 1)) ? 1 : 0;
+        if (!__syncthreads_and(good)) {
+            ok = false;
+            break;
+        }
+        /* row Y0 + k of the picture, X0 .. X0 + row_elems - 1, to 16-bit (zero past the picture) */
+        const int r = Y0 + k;
+        uint16_t *a16 = (uint16_t *)sa;
+        for (int e = tid; e < row_elems; e += 128) {
+            const int x = X0 + e;
+            const float v = (r < p.h && x < p.w) ? (float)__ldg(plane + (size_t)r * pitch + x) : 0.0f;
+            a16[e] = to16(v, KIND);
+        }
+        /* the band block for this row */
+        const uint4 *src = (const uint4 *)(band + (size_t)k * TC_N * krow);
+        uint4 *dst = (uint4 *)sb;
+        const int vec = TC_N * krow * 2 / 16;
+        for (int i = tid; i < vec; i += 128)
+            dst[i] = __ldg(src + i);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t a0 = smem_u32(sa), b0 = smem_u32(sb);
+            for (int kc = 0; kc < kchunks; kc++) {
+                const uint64_t ad = mdesc(a0 + 32 * kc, 16, 128);
+                const uint64_t bd = mdesc(b0 + kc * 2 * (TC_N / 8) * 128, (TC_N / 8) * 128, 128);
+                tc_mma(tmem, ad, bd, idesc, (k | kc) != 0);
+            }
+            tc_commit(mbar0 + 8 * s);
+        }
+    }
+    /* the last commit covers every MMA thread 0 issued */
+    int good = ok ? 1 : 0;
+    if (ok && tid == 0) {
+        const int last = nk - 1;
+        good = mbar_wait(mbar0 + 8 * (last % TC_STAGES), (uint32_t)((last / TC_STAGES) & 1)) ? 1 : 0;
+    }
+    const int ok_all = __syncthreads_and(good);
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (!ok_all) {
+        if (tid == 0)
+            atomicExch(err, 1);
+    } else {
+        /* epilogue: thread m owns accumulator row m */
+        const int m = warp * 32 + lane;
+        const int per = NCC_CELL / p.step;
+        float best = -2.0f;
+        int bkey = 1 << 30;
+#pragma unroll 1
+        for (int c = 0; c < TC_N / 32; c++) {
+            float v[32];
+            tc_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(32 * c), v);
+#pragma unroll
+            for (int j = 0; j < 32; j++) {
+                const int q = 4 * c + (j >> 3), s = j & 7;
+                const int x = X0 + 8 * m + s, y = Y0 + q;
+                if (x > p.x1 || y > p.y1 || ((x - p.x0) % p.step) || ((y - p.y0) % p.step))
+                    continue;
+                const float j0 = (float)__ldg(plane + (size_t)y * pitch + x);
+                const float st = v[j] - j0 * p.sum_t;
+                const long long s1 = tbox(S1, tp, x, y, p.tw, p.th), s2 = tbox(S2, tp, x, y, p.tw, p.th);
+                const long long nvar = (long long)p.n * s2 - s1 * s1;
+                float score;
+                if ((double)nvar <= (double)p.n * (double)p.norm * 0.0625 || p.norm <= 0.0f)
+                    score = 0.0f;
+                else
+                    score = st / sqrtf(p.norm * ((float)nvar / (float)p.n));
+                const int key = (q / p.step) * per + ((8 * (m & 1) + s) / p.step);
+                if (tbetter(score, key, best, bkey)) {
+                    best = score;
+                    bkey = key;
+                }
+            }
+        }
+        const float ob = __shfl_xor_sync(VTG_FULL, best, 1);
+        const int ok2 = __shfl_xor_sync(VTG_FULL, bkey, 1);
+        if (tbetter(ob, ok2, best, bkey)) {
+            best = ob;
+            bkey = ok2;
+        }
+        const int ccol = tx * (TC_XS / NCC_CELL) + (m >> 1);
+        if ((m & 1) == 0 && ccol < p.ccols && ty < p.crows) {
+            const int cell = ty * p.ccols + ccol;
+            const int cx0 = p.x0 + ccol * NCC_CELL, cy0 = p.y0 + ty * NCC_CELL;
+            const bool fired = bkey < (1 << 30) && best > -2.0f;
+            map_v[cell] = fired ? best : -2.0f;
+            map_x[cell] = fired ? cx0 + (bkey % per) * p.step : cx0;
+            map_y[cell] = fired ? cy0 + (bkey / per) * p.step : cy0;
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS) : "memory");
+    }
+}
+
+cudaError_t vtg_launch_ncc_map_tc(const void *plane, int pitch, int elem_bytes, const NccPrm &p, const NccScratch &s,
+                                  int kind, cudaStream_t st)
+{
+    if (elem_bytes != 1 || !s.band || (kind != VTG_NCC_BF16 && kind != VTG_NCC_FP16))
+        return cudaErrorInvalidValue;
+    const int krow = tc_krow(p.tw);
+    const TcSmem sm = tc_smem(krow);
+    const int tiles_x = (p.x1 - p.x0 + 1 + TC_XS - 1) / TC_XS, tiles_y = (p.y1 - p.y0 + 1 + TC_Q - 1) / TC_Q;
+    cudaError_t e;
+    if (kind == VTG_NCC_BF16) {
+        e = cudaFuncSetAttribute(ncc_map_tc<VTG_NCC_BF16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm.total);
+        if (e != cudaSuccess)
+            return e;
+        ncc_map_tc<VTG_NCC_BF16><<<tiles_x * tiles_y, 128, sm.total, st>>>(
+            (const uint8_t *)plane, pitch, p, s.band, krow, tiles_x, sm.a_bytes, sm.stage_bytes, s.S1, s.S2, s.tp,
+            s.map_v, s.map_x, s.map_y, s.err);
+    } else {
+        e = cudaFuncSetAttribute(ncc_map_tc<VTG_NCC_FP16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm.total);
+        if (e != cudaSuccess)
+            return e;
+        ncc_map_tc<VTG_NCC_FP16><<<tiles_x * tiles_y, 128, sm.total, st>>>(
+            (const uint8_t *)plane, pitch, p, s.band, krow, tiles_x, sm.a_bytes, sm.stage_bytes, s.S1, s.S2, s.tp,
+            s.map_v, s.map_x, s.map_y, s.err);
+    }
+    return cudaGetLastError();
+}

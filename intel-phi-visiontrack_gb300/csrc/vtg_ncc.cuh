@@ -1,0 +1,43 @@
+/* vtg_ncc.cuh -- what the appearance search's kernels share (ncc.cu, ncc_tc.cu) and the C ABI (api_ncc.cu). */
+#ifndef VTG_NCC_CUH
+#define VTG_NCC_CUH
+
+#include "vtg_internal.cuh"
+
+#define NCC_CELL 16 /* SEARCH_CELL, src/kern/track.c:61: corners to a cell of the map */
+#define NCC_TOP 8   /* SEARCH_TOP, src/kern/track.c:62: cells looked at again in half pixels */
+
+/* One search: the plane, the template and the clamped window of corners. */
+struct NccPrm {
+    int w, h;        /* the plane */
+    int tw, th, n;   /* template, n = tw th */
+    float norm;      /* sum of the template's squares */
+    float sum_t;     /* sum of the template as the tensor-core map multiplies it (its rounded values) */
+    int x0, x1, y0, y1, step;
+    int ccols, crows; /* the map's cells */
+};
+
+/* Scratch of a search context, in device memory. */
+struct NccScratch {
+    long long *S1, *S2; /* integral images of J and J^2, (h + 1) rows of tp */
+    int tp;
+    float *map_v;
+    int *map_x, *map_y;
+    int *top, *ntop;
+    const uint16_t *band; /* the template band for the tensor-core map (ncc_tc.cu), NULL if unset */
+    int band_rows, krow;  /* image rows of a tile's band (NCC_TC_Q + th - 1), K per image row */
+    int *err;             /* device status word: nonzero when a bounded wait gave up */
+};
+
+cudaError_t vtg_launch_ncc(const void *plane, int pitch, int plane_type, const float *app, const NccPrm &p,
+                           const NccScratch &s, int map_kind, vtg_found *out, cudaStream_t st);
+cudaError_t vtg_launch_ncc_corners(const void *plane, int pitch, int plane_type, const float *app, const NccPrm &p,
+                                   int count, const int *xs, const int *ys, float *out, cudaStream_t st);
+/* The tensor-core map (ncc_tc.cu): the same map_v / map_x / map_y as ncc_map_f32, products in BF16 or FP16. */
+cudaError_t vtg_launch_ncc_map_tc(const void *plane, int pitch, int elem_bytes, const NccPrm &p, const NccScratch &s,
+                                  int kind, cudaStream_t st);
+/* Builds the template band for the tensor-core map from a zero-mean template. */
+cudaError_t vtg_launch_ncc_band(const float *app, int tw, int th, int kind, uint16_t *band, float *sum_t, cudaStream_t st);
+size_t vtg_ncc_band_bytes(int tw, int th);
+
+#endif

@@ -111,7 +111,10 @@ class Context:
     def close(self):
         if self.h:
             for t in list(self._trackers):
-                t.h = C.c_void_p()  # the context frees its trackers
+                if isinstance(t, Tracker):
+                    t.h = C.c_void_p()  # the context frees its trackers
+                else:
+                    t.close()
             lib().vtg_ctx_destroy(self.h)
             self.h = C.c_void_p()
 
@@ -195,3 +198,92 @@ class Tracker:
             self.close()
         except Exception:
             pass
+
+
+# ---------------------------------------------------------------- the appearance search
+
+PLANE_U8, PLANE_F32 = 0, 1
+NCC_F32, NCC_BF16, NCC_FP16 = 0, 1, 2
+
+
+class Found(C.Structure):
+    """struct vtg_found."""
+    _fields_ = [("hx", C.c_int), ("hy", C.c_int), ("ncc", C.c_float), ("second", C.c_float), ("ox", C.c_float),
+                ("oy", C.c_float), ("ntop", C.c_int), ("cells", C.c_int)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+def _search_sigs(L):
+    vp, i, f, sz = C.c_void_p, C.c_int, C.c_float, C.c_size_t
+    L.vtg_search_bytes.argtypes = [i, i, i, i]
+    L.vtg_search_bytes.restype = sz
+    L.vtg_search_create.argtypes = [vp, i, i, i, i, C.POINTER(vp)]
+    L.vtg_search_destroy.argtypes = [vp]
+    L.vtg_search_destroy.restype = None
+    L.vtg_search_stream.argtypes = [vp]
+    L.vtg_search_stream.restype = vp
+    L.vtg_search_template.argtypes = [vp, vp, i, i, f, i, vp]
+    L.vtg_search_run.argtypes = [vp, vp, i, i, i, i, i, i, i, i, i, i, C.POINTER(Found), vp, vp, vp, i, vp]
+    L.vtg_correlate.argtypes = [vp, vp, i, i, i, i, i, vp, vp, vp, i, vp]
+    L.vtg_level_device.argtypes = [vp, i, i, C.POINTER(vp), C.POINTER(i), C.POINTER(i), C.POINTER(i)]
+
+
+class Search:
+    """A search context (vtg_search): a template and the scratch of its searches."""
+
+    def __init__(self, ctx: Context, max_w: int, max_h: int, max_tw: int = 128, max_th: int = 128):
+        _search_sigs(lib())
+        self.ctx = ctx
+        self.h = C.c_void_p()
+        check(lib().vtg_search_create(ctx.h, max_w, max_h, max_tw, max_th, C.byref(self.h)), "vtg_search_create")
+        ctx._trackers.add(self)
+
+    def template(self, app, norm: float):
+        app = np.ascontiguousarray(app, np.float32)
+        check(lib().vtg_search_template(self.h, _p(app), app.shape[1], app.shape[0], C.c_float(norm), HOST, None),
+              "vtg_search_template")
+
+    def run(self, plane_ptr: int, w: int, h: int, pitch: int, plane_type: int, x0: int, x1: int, y0: int, y1: int,
+            step: int = 1, precision: int = NCC_F32, want_map: bool = False):
+        f = Found()
+        ncell = (w // 16 + 2) * (h // 16 + 2)
+        mv = np.zeros(ncell, np.float32) if want_map else None
+        mx = np.zeros(ncell, np.int32) if want_map else None
+        my = np.zeros(ncell, np.int32) if want_map else None
+        check(lib().vtg_search_run(self.h, plane_ptr, w, h, pitch, plane_type, x0, x1, y0, y1, step, precision,
+                                   C.byref(f), _p(mv), _p(mx), _p(my), HOST, None), "vtg_search_run")
+        d = f.as_dict()
+        if want_map:
+            n = d["cells"]
+            return d, mv[:n], mx[:n], my[:n]
+        return d
+
+    def correlate(self, plane_ptr: int, w: int, h: int, pitch: int, plane_type: int, xs, ys) -> np.ndarray:
+        xs = np.ascontiguousarray(xs, np.int32)
+        ys = np.ascontiguousarray(ys, np.int32)
+        out = np.zeros(len(xs), np.float32)
+        check(lib().vtg_correlate(self.h, plane_ptr, w, h, pitch, plane_type, len(xs), _p(xs), _p(ys), _p(out), HOST,
+                                  None), "vtg_correlate")
+        return out
+
+    def close(self):
+        if self.h:
+            lib().vtg_search_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def level_device(tracker: Tracker, set_: int, level: int):
+    """(device address, w, h, pitch) of a tracker's pyramid level (F32 Q6)."""
+    _search_sigs(lib())
+    p, w, h, pitch = C.c_void_p(), C.c_int(), C.c_int(), C.c_int()
+    check(lib().vtg_level_device(tracker.h, set_, level, C.byref(p), C.byref(w), C.byref(h), C.byref(pitch)),
+          "vtg_level_device")
+    return p.value, w.value, h.value, pitch.value

@@ -1,0 +1,61 @@
+"""The tensor-core correlation map (tcgen05, BF16 / FP16 products, F32 accumulation) against the F32 map and the FP64
+oracle. The map's values carry the products' rounding; the found corner and its score come from the F32 re-score of
+the eight candidates, so they must agree with the F32 path's whenever the candidates do."""
+import numpy as np
+import pytest
+
+import oracle as O
+import vtg_synth as S
+
+pytestmark = pytest.mark.gpu
+
+TOL_MAP = {1: 0.02, 2: 0.005}  # BF16, FP16: max |map value - F32 map value|
+
+
+def _dev(a):
+    import torch
+
+    t = torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    torch.cuda.synchronize()
+    return t
+
+
+@pytest.mark.parametrize("precision", [1, 2])
+@pytest.mark.parametrize("tw,th,w,h", [(32, 21, 200, 100), (32, 32, 640, 480), (64, 64, 640, 480), (96, 96, 1100, 300)])
+def test_tc_map_matches_f32_map(vtg_lib, ctx, precision, tw, th, w, h):
+    frame = S.noise_frame(w, h, seed=tw + th + w)
+    tpl, xs, ys, blank = S.ncc_templates(frame, max(tw, th), 2, seed=3, blank_share=0.0)
+    patch = tpl[0][:th, :tw].astype(np.float32)
+    app = (patch - np.float32(patch.mean(dtype=np.float64))).astype(np.float32)
+    norm = float(np.sum(app.astype(np.float64) ** 2))
+    dp = _dev(frame)
+    s = vtg_lib.Search(ctx, w, h)
+    s.template(app, norm)
+    f32, v32, x32, y32 = s.run(dp.data_ptr(), w, h, w, vtg_lib.PLANE_U8, 1, w, 1, h, 1, vtg_lib.NCC_F32, want_map=True)
+    ftc, vtc, xtc, ytc = s.run(dp.data_ptr(), w, h, w, vtg_lib.PLANE_U8, 1, w, 1, h, 1, precision, want_map=True)
+    assert ftc["cells"] == f32["cells"]
+    assert np.abs(vtc - v32).max() < TOL_MAP[precision]
+    assert (ftc["hx"], ftc["hy"]) == (f32["hx"], f32["hy"]) == (2 * xs[0], 2 * ys[0])
+    assert abs(ftc["ncc"] - f32["ncc"]) < 1e-6
+    s.close()
+
+
+@pytest.mark.parametrize("precision", [1, 2])
+def test_tc_step2_and_window(vtg_lib, ctx, precision):
+    """A window that starts off the cell grid, at step 2, as the whole-picture band search runs at levels 0 and 1."""
+    w, h = 500, 260
+    frame = S.noise_frame(w, h, seed=77)
+    tpl, xs, ys, _ = S.ncc_templates(frame, 32, 1, seed=9, blank_share=0.0)
+    app = (tpl[0].astype(np.float32) - np.float32(tpl[0].mean(dtype=np.float64))).astype(np.float32)
+    norm = float(np.sum(app.astype(np.float64) ** 2))
+    dp = _dev(frame)
+    s = vtg_lib.Search(ctx, w, h)
+    s.template(app, norm)
+    for (x0, x1, y0, y1, step) in ((37, 433, 5, 201, 2), (3, 499, 1, 259, 1), (40, 41, 40, 41, 1)):
+        a, av, ax, ay = s.run(dp.data_ptr(), w, h, w, vtg_lib.PLANE_U8, x0, x1, y0, y1, step, vtg_lib.NCC_F32, True)
+        b, bv, bx, by = s.run(dp.data_ptr(), w, h, w, vtg_lib.PLANE_U8, x0, x1, y0, y1, step, precision, True)
+        assert a["cells"] == b["cells"] and np.abs(av - bv).max() < TOL_MAP[precision]
+        clear = np.abs(av - bv) < 1e-7
+        assert np.array_equal(ax[clear], bx[clear]) and np.array_equal(ay[clear], by[clear])
+        assert (a["hx"], a["hy"]) == (b["hx"], b["hy"])
+    s.close()
