@@ -173,6 +173,24 @@ int vtg_search_run(vtg_search *s, const void *plane, int w, int h, int pitch, in
 int vtg_correlate(vtg_search *s, const void *plane, int w, int h, int pitch, int plane_type, int n, const int *xs,
                   const int *ys, float *out, int where, void *stream);
 
+/* ---- the appearance search without any allocation ---- */
+
+#define VTG_NOALLOC_SCRATCH_BYTES (5u << 20) /* held on every GPU that loads the library, until exit */
+#define VTG_NOALLOC_MAX_PIXELS 320000        /* (w + 1) (h + 1) at most: a 640 x 480 plane fits */
+#define VTG_NOALLOC_MAX_T 64                 /* template sides at most */
+
+/* No counterpart in the reference: an extra entry point for callers that cannot allocate device memory when they search
+ * (a real-time loop that cannot absorb a cudaMalloc, a host runtime that owns every byte of device memory). The same
+ * search as vtg_search_run with an F32 map, but nothing is allocated: no context, no search context; the caller
+ * passes the plane, the template (th rows of tw zero-mean floats, tw a multiple of 8) and its norm, and *found (and the
+ * optional per-cell map) in device memory; the scratch lives in one fixed device array of VTG_NOALLOC_SCRATCH_BYTES.
+ * Larger planes or templates than the limits above return VTG_EINVAL. All calls share that array: calls whose work
+ * overlaps on the GPU race, so order them on one stream. The first call on a device looks the array's address up;
+ * make it before any stream capture. Asynchronous on `stream` (a cudaStream_t, NULL for the legacy default). */
+int vtg_search_run_noalloc(const void *plane, int w, int h, int pitch, int plane_type, const float *app, int tw, int th,
+                           float norm, int x0, int x1, int y0, int y1, int step, struct vtg_found *found, float *map_v,
+                           int *map_x, int *map_y, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
