@@ -130,6 +130,44 @@ int vtg_level_size(const vtg_tracker *t, int level, int *w, int *h);
  * the tracker is destroyed; its contents change with every vtg_build of that set. */
 int vtg_level_device(const vtg_tracker *t, int set, int level, const float **plane, int *w, int *h, int *pitch);
 
+/* The cell results of a tracker's last vtg_cells or batch step: cols x rows records each (either may be NULL). */
+int vtg_tracker_results(vtg_tracker *t, struct vtg_cell *cells, struct vtg_lk_out *lk, int where, void *stream);
+
+/* ---- many streams in one step: the batched form of tk_build + still_vectors ---- */
+
+/* How the batched LK launch runs (its autotuner's choices): warps per CTA (4, 8 or 16), cells per work item, a
+ * persistent grid of ctas_per_sm CTAs per SM pulling items from a device counter (persistent = 1) or one warp per item
+ * (persistent = 0). */
+struct vtg_tune {
+    int block_warps, chunk, persistent, ctas_per_sm;
+};
+
+typedef struct vtg_batch vtg_batch;
+
+/* A batch of up to max_jobs streams (all of one context, one LK setting). Two slots hold two prepared steps. */
+int vtg_batch_create(vtg_ctx *ctx, int max_jobs, vtg_batch **out);
+void vtg_batch_destroy(vtg_batch *b);
+void *vtg_batch_stream(const vtg_batch *b);
+/* Prepares one step into `slot`: for each of n trackers, frames[j] (height rows of width bytes, strides[j] apart, or
+ * NULL strides: width) becomes the pyramid of set cur_sets[j], and the cells flow from set 1 - cur_sets[j] to it
+ * (tk_build + still_vectors, src/kern/track.c:584-629, src/kern/still.c:116-141). Host frames must stay valid (and
+ * pinned, to be captured in a graph) for every launch of the slot. */
+int vtg_batch_prepare(vtg_batch *b, int slot, int n, vtg_tracker *const *trackers, const uint8_t *const *frames,
+                      const int *strides, int where, const int *cur_sets);
+/* Runs a prepared step: the batched pyramid launches, then one LK launch over every stream's cells. Results stay in
+ * each tracker (vtg_tracker_results). */
+int vtg_batch_launch(vtg_batch *b, int slot, void *stream);
+/* Captures a prepared step into a CUDA graph, and replays it. */
+int vtg_batch_capture(vtg_batch *b, int slot);
+int vtg_batch_replay(vtg_batch *b, int slot, void *stream);
+/* Cells of a prepared step. */
+int vtg_batch_cells(const vtg_batch *b, int slot);
+int vtg_batch_set_tune(vtg_batch *b, const struct vtg_tune *t);
+int vtg_batch_get_tune(const vtg_batch *b, struct vtg_tune *t);
+/* Times every candidate launch shape on the prepared step (median of reps) and keeps the fastest for this mix of
+ * stream sizes; reports it, its time and the default shape's time. */
+int vtg_batch_autotune(vtg_batch *b, int slot, int reps, struct vtg_tune *best, float *best_ms, float *default_ms);
+
 /* ---- the appearance search (reacquisition) ---- */
 
 /* Plane element types. */

@@ -12,6 +12,7 @@
 
 #include "vtg_ctx.h"
 #include "vtg_internal.cuh"
+#include "vtg_tracker.h"
 
 static thread_local int g_last_cuda = 0;
 
@@ -65,23 +66,7 @@ void vtg_ctx_track(vtg_ctx *ctx, cudaStream_t s, bool add)
         }
 }
 
-struct vtg_tracker {
-    vtg_ctx *ctx;
-    vtg_config cfg;
-    cudaStream_t stream;
-    int levels, cols, rows;
-    int lw[VTG_MAX_LEVELS], lh[VTG_MAX_LEVELS], lpitch[VTG_MAX_LEVELS];
-    size_t loff[VTG_MAX_LEVELS]; /* float offset of each level inside a set */
-    size_t set_floats;
-    size_t bytes;
-    char *mem;            /* the one allocation */
-    float *sets[2];       /* pyramid sets */
-    uint8_t *staging;     /* a frame uploaded from the host */
-    DevPyr *desc;         /* [set][0: from level 0, 1: from flow_level] */
-    vtg_lk_out *d_lk;     /* cells x lk_out */
-    vtg_cell *d_cells;    /* cells x vt_cell */
-    LkPrm prm;
-};
+
 
 extern "C" const char *vtg_strerror(int status)
 {

@@ -320,17 +320,14 @@ __device__ __forceinline__ float cell_diff(const DevLevel &A, const DevLevel &B,
     return __fdiv_rn(s, (float)((y1 - y0) * g.cell_w)) * LK_Q6_INV;
 }
 
+/* One cell of a grid: its centre (cw c + cw / 2, ch r + ch / 2), clamped to where the patch fits (still.c:127-130),
+ * LK with the forward-backward check, and the cell record (still.c:132-140). The whole warp calls it. */
 template <int MAXH, bool EXACT>
-__global__ void __launch_bounds__(256, 2) lk_cells_kernel(const DevPyr *__restrict__ Ip, const DevPyr *__restrict__ Jp,
-                                                       int top, LkPrm p, CellGrid g, int base_w, int base_h,
-                                                       vtg_lk_out *__restrict__ out, vtg_cell *__restrict__ cells)
+__device__ __forceinline__ void lk_cell(const DevPyr &I, const DevPyr &J, int top, const LkPrm &p, const CellGrid &g,
+                                        int base_w, int base_h, int i, int lane, vtg_lk_out *__restrict__ out,
+                                        vtg_cell *__restrict__ cells)
 {
-    const int i = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
-    if (i >= g.n)
-        return;
-    const DevPyr &I = *Ip, &J = *Jp;
     const int col = i % g.cols, row = i / g.cols;
-    /* The centre (cw c + cw / 2, ch r + ch / 2), clamped to where the patch fits (still.c:127-130). */
     const float mx = (float)(p.W / 2 + 2), my = (float)(p.H / 2 + 2);
     float x = (float)(col * g.cell_w + g.cell_w / 2), y = (float)(row * g.cell_h + g.cell_h / 2);
     x = fminf(fmaxf(x, mx), (float)base_w - 1.0f - mx);
@@ -353,6 +350,102 @@ __global__ void __launch_bounds__(256, 2) lk_cells_kernel(const DevPyr *__restri
             cells[i] = c;
         }
     }
+}
+
+template <int MAXH, bool EXACT>
+__global__ void __launch_bounds__(256, 2) lk_cells_kernel(const DevPyr *__restrict__ Ip, const DevPyr *__restrict__ Jp,
+                                                          int top, LkPrm p, CellGrid g, int base_w, int base_h,
+                                                          vtg_lk_out *__restrict__ out, vtg_cell *__restrict__ cells)
+{
+    const int i = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (i >= g.n)
+        return;
+    lk_cell<MAXH, EXACT>(*Ip, *Jp, top, p, g, base_w, base_h, i, lane, out, cells);
+}
+
+/* Many streams' cells in one launch. Work items are runs of `chunk` cells of one job; job j's items start at
+ * item_start[j]. PERSISTENT: a fixed grid whose warps take items from `counter` until none is left, so uneven streams
+ * balance themselves; otherwise one warp per item. The cell code is the single-stream kernel's: a cell's result does
+ * not depend on what else is in the batch. */
+#define LK_BATCH_MAX_JOBS 512
+
+template <int MAXH, bool EXACT, bool PERSISTENT, int WARPS, int MINB>
+__global__ void __launch_bounds__(WARPS * 32, MINB) lk_batch_kernel(const LkJob *__restrict__ jobs,
+                                                                    const int *__restrict__ item_start, int njobs,
+                                                                    int items, int chunk, LkPrm p,
+                                                                    int *__restrict__ counter)
+{
+    __shared__ int s_start[LK_BATCH_MAX_JOBS + 1];
+    for (int k = threadIdx.x; k <= njobs; k += blockDim.x)
+        s_start[k] = item_start[k];
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    int item = PERSISTENT ? 0 : (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    for (;;) {
+        if (PERSISTENT) {
+            int t = 0;
+            if (lane == 0)
+                t = atomicAdd(counter, 1);
+            item = __shfl_sync(VTG_FULL, t, 0);
+        }
+        if (item >= items)
+            break;
+        int lo = 0, hi = njobs;
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (s_start[mid] <= item)
+                lo = mid;
+            else
+                hi = mid;
+        }
+        const LkJob &jb = jobs[lo];
+        const int c0 = (item - s_start[lo]) * chunk, c1 = min(c0 + chunk, jb.g.n);
+        for (int c = c0; c < c1; c++)
+            lk_cell<MAXH, EXACT>(*jb.I, *jb.J, jb.top, p, jb.g, jb.base_w, jb.base_h, c, lane, jb.out, jb.cells);
+        if (!PERSISTENT)
+            break;
+    }
+}
+
+template <int MAXH, bool EXACT>
+static cudaError_t lk_batch_launch(const LkJob *jobs, const int *item_start, int njobs, int items, const LkPrm &p,
+                                   const LkTune &t, int sms, int *counter, cudaStream_t s)
+{
+#define LKB(P, WARPS, MINB)                                                                                            \
+    do {                                                                                                               \
+        const int blocks = P ? sms * t.ctas_per_sm : (items + WARPS - 1) / WARPS;                                      \
+        lk_batch_kernel<MAXH, EXACT, P, WARPS, MINB><<<blocks, WARPS * 32, 0, s>>>(jobs, item_start, njobs, items,    \
+                                                                                   t.chunk, p, counter);               \
+    } while (0)
+    if (t.persistent) {
+        if (t.block_warps == 4)
+            LKB(true, 4, 4);
+        else if (t.block_warps == 16)
+            LKB(true, 16, 1);
+        else
+            LKB(true, 8, 2);
+    } else {
+        if (t.block_warps == 4)
+            LKB(false, 4, 4);
+        else if (t.block_warps == 16)
+            LKB(false, 16, 1);
+        else
+            LKB(false, 8, 2);
+    }
+#undef LKB
+    return cudaGetLastError();
+}
+
+cudaError_t vtg_launch_lk_batch(const LkJob *jobs, const int *item_start, int njobs, int items, const LkPrm &p,
+                                const LkTune &tune, int sms, int *counter, cudaStream_t s)
+{
+    if (njobs < 1 || njobs > LK_BATCH_MAX_JOBS || items <= 0)
+        return items <= 0 ? cudaSuccess : cudaErrorInvalidValue;
+    if (p.H == 21)
+        return lk_batch_launch<21, true>(jobs, item_start, njobs, items, p, tune, sms, counter, s);
+    if (p.H == 15)
+        return lk_batch_launch<15, true>(jobs, item_start, njobs, items, p, tune, sms, counter, s);
+    return lk_batch_launch<31, false>(jobs, item_start, njobs, items, p, tune, sms, counter, s);
 }
 
 template <int MAXH, bool EXACT>

@@ -17,15 +17,14 @@
 #define RS_X (2 * RT_X + 4) /* source tile: two output pixels per step, two each side */
 #define RS_Y (2 * RT_Y + 4)
 
+/* One 64 x 16 tile of the output level at (ox, oy), from a 132 x 36 source tile in shared memory; with FROM_U8 the
+ * source is the frame's bytes and level 0 (byte x 64) is written from the same tile. dst may be NULL (level 0 only). */
 template <bool FROM_U8>
-__global__ void __launch_bounds__(256) pyr_reduce_kernel(const void *__restrict__ src_, int sw, int sh, int spitch,
-                                                         float *__restrict__ l0, int l0pitch, float *__restrict__ dst,
-                                                         int dw, int dh, int dpitch)
+__device__ __forceinline__ void reduce_tile(const void *__restrict__ src_, int sw, int sh, int spitch,
+                                            float *__restrict__ l0, int l0pitch, float *__restrict__ dst, int dw, int dh,
+                                            int dpitch, int ox, int oy, int (*s_src)[RS_X + 1], int (*s_v)[RS_X + 1])
 {
-    __shared__ int s_src[RS_Y][RS_X + 1];
-    __shared__ int s_v[RT_Y][RS_X + 1];
     const int tid = threadIdx.x;
-    const int ox = blockIdx.x * RT_X, oy = blockIdx.y * RT_Y;
     const int sx0 = 2 * ox - 2, sy0 = 2 * oy - 2;
     for (int i = tid; i < RS_Y * RS_X; i += blockDim.x) {
         const int r = i / RS_X, c = i - r * RS_X;
@@ -56,6 +55,75 @@ __global__ void __launch_bounds__(256) pyr_reduce_kernel(const void *__restrict_
         if (gy < dh && gx < dw)
             dst[(size_t)gy * dpitch + gx] = (float)((h + 128) >> 8);
     }
+}
+
+template <bool FROM_U8>
+__global__ void __launch_bounds__(256) pyr_reduce_kernel(const void *__restrict__ src_, int sw, int sh, int spitch,
+                                                         float *__restrict__ l0, int l0pitch, float *__restrict__ dst,
+                                                         int dw, int dh, int dpitch)
+{
+    __shared__ int s_src[RS_Y][RS_X + 1];
+    __shared__ int s_v[RT_Y][RS_X + 1];
+    reduce_tile<FROM_U8>(src_, sw, sh, spitch, l0, l0pitch, dst, dw, dh, dpitch, blockIdx.x * RT_X, blockIdx.y * RT_Y,
+                         s_src, s_v);
+}
+
+/* Many frames at once: the launch's tiles are every job's tiles of this level, back to back; a block finds its job by
+ * binary search over the tile offsets. Level 1 (with level 0) from each job's bytes, or level L from level L - 1. */
+template <bool FROM_U8>
+__global__ void __launch_bounds__(256) pyr_batch_kernel(const PyrJob *__restrict__ jobs, const int *__restrict__ start,
+                                                        int njobs, int level)
+{
+    __shared__ int s_src[RS_Y][RS_X + 1];
+    __shared__ int s_v[RT_Y][RS_X + 1];
+    const int b = blockIdx.x;
+    int lo = 0, hi = njobs; /* start[lo] <= b < start[hi] */
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(start + mid) <= b)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    const PyrJob &j = jobs[lo];
+    const int t = b - __ldg(start + lo);
+    const int sw = FROM_U8 ? j.w : j.lw[level - 1], sh = FROM_U8 ? j.h : j.lh[level - 1];
+    const int dw = (sw + 1) / 2, dh = (sh + 1) / 2;
+    const int tiles_x = (dw + RT_X - 1) / RT_X;
+    const int ox = (t % tiles_x) * RT_X, oy = (t / tiles_x) * RT_Y;
+    if (FROM_U8)
+        reduce_tile<true>(j.src, j.w, j.h, j.stride, j.lv[0], j.pitch[0], j.levels > 1 ? j.lv[1] : nullptr, dw, dh,
+                          j.pitch[1], ox, oy, s_src, s_v);
+    else
+        reduce_tile<false>(j.lv[level - 1], sw, sh, j.pitch[level - 1], nullptr, 0, j.lv[level], dw, dh, j.pitch[level],
+                           ox, oy, s_src, s_v);
+}
+
+int vtg_pyr_tiles(int w, int h, int level)
+{
+    /* tiles of the launch that makes `level` (1: levels 0 and 1) from a w x h frame */
+    int sw = w, sh = h;
+    for (int L = 1; L < level; L++) {
+        sw = (sw + 1) / 2;
+        sh = (sh + 1) / 2;
+    }
+    const int dw = (sw + 1) / 2, dh = (sh + 1) / 2;
+    return ((dw + RT_X - 1) / RT_X) * ((dh + RT_Y - 1) / RT_Y);
+}
+
+cudaError_t vtg_launch_pyramid_batch(const PyrJob *jobs, const int *starts, const int *tiles_total, int njobs,
+                                     int max_levels, cudaStream_t s)
+{
+    for (int L = 1; L < (max_levels > 1 ? max_levels : 2); L++) {
+        const int tiles = tiles_total[L - 1];
+        if (tiles <= 0)
+            continue;
+        if (L == 1)
+            pyr_batch_kernel<true><<<tiles, 256, 0, s>>>(jobs, starts + (size_t)(L - 1) * (njobs + 1), njobs, L);
+        else
+            pyr_batch_kernel<false><<<tiles, 256, 0, s>>>(jobs, starts + (size_t)(L - 1) * (njobs + 1), njobs, L);
+    }
+    return cudaGetLastError();
 }
 
 cudaError_t vtg_launch_pyramid(const uint8_t *frame, int stride, int w, int h, float *const *levels, const int *pitches,

@@ -43,11 +43,43 @@ struct CellGrid {
 
 static inline int vtg_pitch(int w) { return (w + 31) & ~31; }
 
+/* One frame's pyramid in a batched build: its bytes and its set's level planes. lw / lh: level sizes. */
+struct PyrJob {
+    const uint8_t *src;
+    int stride, w, h, levels;
+    float *lv[VTG_MAX_LEVELS];
+    int pitch[VTG_MAX_LEVELS], lw[VTG_MAX_LEVELS], lh[VTG_MAX_LEVELS];
+};
+
+/* One stream's per-cell flow in a batched step (the LK settings are the batch's, shared by every job). */
+struct LkJob {
+    const DevPyr *I, *J;
+    int top;
+    CellGrid g;
+    int base_w, base_h;
+    vtg_lk_out *out;
+    vtg_cell *cells;
+};
+
+/* How a batched step runs its LK (the autotuner's choices). */
+struct LkTune {
+    int block_warps;   /* warps per CTA: 4, 8 or 16 */
+    int chunk;         /* cells per work item */
+    int persistent;    /* 1: a grid of ctas_per_sm x SMs pulling items from a counter; 0: one warp per item */
+    int ctas_per_sm;   /* for the persistent form */
+};
+
 /* Launchers (pyramid.cu, lk.cu). All asynchronous on `s`; each returns a cudaError_t. */
 cudaError_t vtg_launch_pyramid(const uint8_t *frame, int stride, int w, int h, float *const *levels, const int *pitches,
                                int nlevels, cudaStream_t s);
 cudaError_t vtg_launch_cells(const DevPyr *I, const DevPyr *J, int top, const LkPrm &p, const CellGrid &g, int base_w,
                              int base_h, vtg_lk_out *out, vtg_cell *cells, cudaStream_t s);
+int vtg_pyr_tiles(int w, int h, int level);
+cudaError_t vtg_launch_pyramid_batch(const PyrJob *jobs, const int *starts, const int *tiles_total, int njobs,
+                                     int max_levels, cudaStream_t s);
+/* Batched LK over jobs: items of `chunk` cells, job j's items from item_start[j]; `counter` must be 0 at launch. */
+cudaError_t vtg_launch_lk_batch(const LkJob *jobs, const int *item_start, int njobs, int items, const LkPrm &p,
+                                const LkTune &tune, int sms, int *counter, cudaStream_t s);
 cudaError_t vtg_launch_points(const DevPyr *I, const DevPyr *J, int top, const LkPrm &p, int n, const float *xs,
                               const float *ys, const float *gx, const float *gy, vtg_lk_out *out, cudaStream_t s);
 

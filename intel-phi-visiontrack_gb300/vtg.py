@@ -157,6 +157,7 @@ class Tracker:
             ptr = frame.ctypes.data
         else:
             ptr = frame
+            stride = self.cfg.width if stride is None else stride
         check(lib().vtg_build(self.h, set_, ptr, stride, where, stream), "vtg_build")
 
     def level(self, set_: int, level: int) -> np.ndarray:
@@ -287,3 +288,114 @@ def level_device(tracker: Tracker, set_: int, level: int):
     check(lib().vtg_level_device(tracker.h, set_, level, C.byref(p), C.byref(w), C.byref(h), C.byref(pitch)),
           "vtg_level_device")
     return p.value, w.value, h.value, pitch.value
+
+
+# ---------------------------------------------------------------- many streams in one step
+
+class Tune(C.Structure):
+    """struct vtg_tune."""
+    _fields_ = [("block_warps", C.c_int), ("chunk", C.c_int), ("persistent", C.c_int), ("ctas_per_sm", C.c_int)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+def _batch_sigs(L):
+    vp, i = C.c_void_p, C.c_int
+    L.vtg_batch_create.argtypes = [vp, i, C.POINTER(vp)]
+    L.vtg_batch_destroy.argtypes = [vp]
+    L.vtg_batch_destroy.restype = None
+    L.vtg_batch_stream.argtypes = [vp]
+    L.vtg_batch_stream.restype = vp
+    L.vtg_batch_prepare.argtypes = [vp, i, i, C.POINTER(vp), C.POINTER(vp), C.POINTER(i), i, C.POINTER(i)]
+    L.vtg_batch_launch.argtypes = [vp, i, vp]
+    L.vtg_batch_capture.argtypes = [vp, i]
+    L.vtg_batch_replay.argtypes = [vp, i, vp]
+    L.vtg_batch_cells.argtypes = [vp, i]
+    L.vtg_batch_set_tune.argtypes = [vp, C.POINTER(Tune)]
+    L.vtg_batch_get_tune.argtypes = [vp, C.POINTER(Tune)]
+    L.vtg_batch_autotune.argtypes = [vp, i, i, C.POINTER(Tune), C.POINTER(C.c_float), C.POINTER(C.c_float)]
+    L.vtg_tracker_results.argtypes = [vp, vp, vp, i, vp]
+
+
+class Batch:
+    """A batch (vtg_batch): many trackers' frame pairs in one step, graph-capturable, autotuned."""
+
+    def __init__(self, ctx: Context, max_jobs: int):
+        _batch_sigs(lib())
+        self.ctx = ctx
+        self.h = C.c_void_p()
+        check(lib().vtg_batch_create(ctx.h, max_jobs, C.byref(self.h)), "vtg_batch_create")
+        ctx._trackers.add(self)
+        self._keep = {}
+
+    @property
+    def stream(self) -> int:
+        return lib().vtg_batch_stream(self.h)
+
+    def prepare(self, slot: int, trackers, frames, cur_sets, where: int = DEVICE, strides=None):
+        """frames: device addresses (where=DEVICE) or uint8 numpy arrays (where=HOST; kept alive here)."""
+        n = len(trackers)
+        th = (C.c_void_p * n)(*[t.h.value for t in trackers])
+        if where == HOST:
+            arrs = [np.ascontiguousarray(f, np.uint8) for f in frames]
+            self._keep[slot] = arrs
+            ptrs = [a.ctypes.data for a in arrs]
+            strides = strides or [a.shape[1] for a in arrs]
+        else:
+            ptrs = list(frames)
+        fp = (C.c_void_p * n)(*ptrs)
+        sp = (C.c_int * n)(*strides) if strides is not None else None
+        cs = (C.c_int * n)(*cur_sets)
+        check(lib().vtg_batch_prepare(self.h, slot, n, th, fp, sp, where, cs), "vtg_batch_prepare")
+
+    def launch(self, slot: int, stream=None):
+        check(lib().vtg_batch_launch(self.h, slot, stream), "vtg_batch_launch")
+
+    def capture(self, slot: int):
+        check(lib().vtg_batch_capture(self.h, slot), "vtg_batch_capture")
+
+    def replay(self, slot: int, stream=None):
+        check(lib().vtg_batch_replay(self.h, slot, stream), "vtg_batch_replay")
+
+    def cells(self, slot: int) -> int:
+        return check(lib().vtg_batch_cells(self.h, slot), "vtg_batch_cells")
+
+    def set_tune(self, **kw):
+        t = Tune()
+        check(lib().vtg_batch_get_tune(self.h, C.byref(t)), "vtg_batch_get_tune")
+        for k, v in kw.items():
+            setattr(t, k, v)
+        check(lib().vtg_batch_set_tune(self.h, C.byref(t)), "vtg_batch_set_tune")
+
+    def get_tune(self) -> dict:
+        t = Tune()
+        check(lib().vtg_batch_get_tune(self.h, C.byref(t)), "vtg_batch_get_tune")
+        return t.as_dict()
+
+    def autotune(self, slot: int, reps: int = 5):
+        t = Tune()
+        b, d = C.c_float(), C.c_float()
+        check(lib().vtg_batch_autotune(self.h, slot, reps, C.byref(t), C.byref(b), C.byref(d)), "vtg_batch_autotune")
+        return t.as_dict(), b.value, d.value
+
+    def close(self):
+        if self.h:
+            lib().vtg_batch_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def tracker_results(t: Tracker, want_lk: bool = True):
+    _batch_sigs(lib())
+    n = t.cols * t.rows
+    cells = np.zeros(n, CELL_DTYPE)
+    lk = np.zeros(n, LK_OUT_DTYPE) if want_lk else None
+    check(lib().vtg_tracker_results(t.h, _p(cells), _p(lk), HOST, None), "vtg_tracker_results")
+    t.ctx.sync()
+    return cells, lk
