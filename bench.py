@@ -1,14 +1,18 @@
-"""bench.py -- LK cells/s on one GB300 for the 1920 x 1080 configuration (4 levels, 16,200 cells of 16 x 8, 21 x 21
-patch, <= 10 iterations, eps 0.01, forward-backward check 0.5), seeded synthetic frames.
+"""bench.py -- LK cells/s and frame-pair latency on one GB300, served-batched against the plain GPU form, for the
+1920 x 1080 configuration: 4 levels, 16,200 cells of 16 x 8, 21 x 21 patch, <= 10 iterations, eps 0.01, forward-
+backward check 0.5. Seeded synthetic frames (noise blurred at sigma 1.5, warped by a shift of up to 12 px plus a
+smooth field of at most 0.5 px).
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--form plain]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--streams B]
 
-A step is one frame pair of one stream: the pyramid of the new frame and the per-cell flow from the previous frame's
-pyramid to it. `value` times K steps with the frames already in HBM (CUDA events on the tracker's stream, L2 flushed
-before every step by writing a 256 MiB buffer, outside the timed spans). `e2e` times the same steps through the public
-C ABI with host buffers: the pinned frame's upload and the cell records' download inside the timed region.
-`--impl reference` times the CPU restatement of the reference's path (oracle/, FP64 form) on all host cores over the
-same workload.
+A step is one frame pair of each of B streams (default 8): the pyramids of their new frames and their per-cell flow,
+as one batched step replayed from a CUDA graph (the batched form). `value` is cells/s over K steps with the frames in
+HBM; the B streams' frames and pyramid sets (about 26 MB a stream) exceed the 129 MB L2, so no flush is needed. The
+plain form beside it runs one stream, one vtg_build + vtg_cells per frame pair, with the L2 flushed before each.
+`e2e` is the served request loop (vtg_serve_run) through the C ABI: pinned host frames in, cell records out, Poisson
+arrivals from B 1080p streams at a saturating rate, continuous batching, 2 % of pairs followed by an appearance
+search; beside it the same loop in its plain form, and a mixed-size served run at nominal frame rates for latency.
+`--impl reference` times the CPU restatement of the reference's path (oracle/, FP64 form) on all host cores.
 """
 from __future__ import annotations
 
@@ -28,19 +32,21 @@ ORACLE = os.path.join(ROOT, "oracle")
 sys.path.insert(0, PKG)
 
 METRIC = "LK cells/s + p99 ms/frame-pair, served-batched vs plain GPU; ≤0.01px vs FP64"
-W, H, LEVELS, CELL_W, CELL_H = 1920, 1080, 4, 16, 8
-PATCH = 21
+W, H, LEVELS, CELL_W, CELL_H, PATCH = 1920, 1080, 4, 16, 8, 21
+CELLS = 16200
 
 
-def workload(form: str) -> dict:
+def workload(form: str, streams: int) -> dict:
     return {"workload": "per-cell LK flow, 1920x1080 frame pairs, 4 levels, 16,200 cells (16x8), 21x21 patch, "
-                        "<=10 iters, eps 0.01, fb 0.5; form=" + form,
-            "width": W, "height": H, "levels": LEVELS, "cells_per_pair": 16200, "patch": PATCH,
-            "l2": "flushed before every timed step (256 MiB write)"}
+                        "<=10 iters, eps 0.01, fb 0.5",
+            "form": form, "streams_per_step": streams, "width": W, "height": H, "levels": LEVELS,
+            "cells_per_pair": CELLS, "patch": PATCH,
+            "l2": "batched: inputs larger than L2 (%d streams x ~26 MB of frames and pyramid sets); plain: L2 flushed "
+                  "before every timed step (256 MiB write)" % streams}
 
 
 class Clocks:
-    """nvidia-smi sampled every 200 ms while the timed region runs."""
+    """nvidia-smi sampled every 200 ms while the GPU work runs."""
 
     def __init__(self, device: int):
         self.device = device
@@ -49,13 +55,12 @@ class Clocks:
 
     def __enter__(self):
         q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap,power.draw")
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + q,
                                           "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
                                          stderr=subprocess.DEVNULL, text=True)
-            self.reader = threading.Thread(target=self._read, daemon=True)
-            self.reader.start()
+            threading.Thread(target=self._read, daemon=True).start()
         except OSError:
             self.proc = None
         return self
@@ -73,19 +78,19 @@ class Clocks:
                 self.proc.kill()
 
     def summary(self) -> dict:
-        sm = [float(r[0]) for r in self.rows if len(r) >= 6 and r[0].replace(".", "").isdigit()]
-        mx = [float(r[1]) for r in self.rows if len(r) >= 6 and r[1].replace(".", "").isdigit()]
+        ok = [r for r in self.rows if len(r) >= 6 and r[0].replace(".", "").isdigit()]
+        sm = [float(r[0]) for r in ok]
+        mx = [float(r[1]) for r in ok if r[1].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for r in self.rows if len(r) >= 6 for i in range(4) if r[2 + i] == "Active"})
+        reasons = sorted({names[i] for r in ok for i in range(4) if r[2 + i] == "Active"})
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": reasons, "samples": len(sm)}
 
 
-def lk_flops(lk: np.ndarray, levels: int, w: int = PATCH, h: int = PATCH) -> float:
-    """Algorithmic FLOPs of the cells just computed, counting the reference's patch operations (src/kern/lk_ref.c) with
-    FMA = 2: build 9 (W+2)(H+2) + 20 W H per level built, iterate 14 W H per iteration, residual 12 W H; the
-    forward-backward track costs the same again for the cells that ran it (its iteration count taken equal to the
-    forward track's)."""
+def lk_flops(lk: np.ndarray, levels: int = LEVELS, w: int = PATCH, h: int = PATCH) -> float:
+    """Algorithmic FLOPs of computed cells, counting the reference's patch operations (src/kern/lk_ref.c) with FMA = 2:
+    build 9 (W+2)(H+2) + 20 W H per level, iterate 14 W H per iteration, residual 12 W H; the forward-backward track
+    costs the same again for the cells that ran it (its iteration count taken equal to the forward track's)."""
     build = 9 * (w + 2) * (h + 2) + 20 * w * h
     fwd = levels * build + 14 * w * h * lk["iters"].astype(np.float64) + 12 * w * h
     back = np.where((lk["status"] == 0) | (lk["status"] == 8), fwd, 0.0)
@@ -100,12 +105,49 @@ def peaks() -> dict:
         return {}
 
 
-def run_ours(args) -> dict:
+def frames_1080(n: int):
+    import vtg_synth as S
+
+    return [S.warp_pair(W, H, S.seeded_shift(2 + k, 0), 0.5, seed=2 + k)[:2] for k in range(n)]
+
+
+def time_plain(vtg, torch, ctx, dframes, steps: int, warmup: int, device: str):
+    """One stream, one vtg_build + vtg_cells per frame pair; L2 flushed before each timed step."""
+    t = vtg.Tracker(ctx, vtg.config(W, H, levels=LEVELS, cell_w=CELL_W, cell_h=CELL_H))
+    stream = torch.cuda.ExternalStream(t.stream)
+    dcells = torch.empty(CELLS * 24, dtype=torch.uint8, device=device)
+    dlk = torch.empty(CELLS * 32, dtype=torch.uint8, device=device)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=device)
+    f0, f1 = dframes
+    t.build(0, f0.data_ptr(), where=vtg.DEVICE)
+    for k in range(1, warmup + 1):
+        cur = k & 1
+        t.build(cur, (f1 if cur else f0).data_ptr(), where=vtg.DEVICE)
+        t.cells_device(cur ^ 1, cur, dcells.data_ptr(), dlk.data_ptr())
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for k in range(steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(k & 255)
+            ev[k][0].record(stream)
+        cur = (warmup + 1 + k) & 1
+        t.build(cur, (f1 if cur else f0).data_ptr(), where=vtg.DEVICE)
+        t.cells_device(cur ^ 1, cur, dcells.data_ptr(), dlk.data_ptr())
+        with torch.cuda.stream(stream):
+            ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    ms = np.array([a.elapsed_time(b) for a, b in ev])
+    t.close()
+    return {"value": CELLS * steps / (ms.sum() / 1e3), "unit": "cells/s", "ms_per_pair": float(ms.mean()),
+            "p50_ms_per_pair": float(np.percentile(ms, 50)), "p99_ms_per_pair": float(np.percentile(ms, 99)),
+            "gpu_launches_per_pair": LEVELS}
+
+
+def run_ours(args) -> dict | None:
     import torch
 
     import vtg
     import vtg_build
-    import vtg_synth as S
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -115,155 +157,167 @@ def run_ours(args) -> dict:
 
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
+    device = f"cuda:{local}"
     vtg_build.build()
-    f0, f1, _, _ = S.warp_pair(W, H, S.seeded_shift(2, 0), 0.5, seed=2)
-    frames = [f0, f1]
+    B = args.streams
+    pairs = frames_1080(B)
+    dev = [(torch.from_numpy(f0).to(device), torch.from_numpy(f1).to(device)) for f0, f1 in pairs]
+    torch.cuda.synchronize()
     ctx = vtg.Context(local)
-    t = vtg.Tracker(ctx, vtg.config(W, H, levels=LEVELS, cell_w=CELL_W, cell_h=CELL_H))
-    n = t.cols * t.rows
-    stream = torch.cuda.ExternalStream(t.stream)
-    dframes = [torch.from_numpy(f).to(f"cuda:{local}") for f in frames]
-    dcells = torch.empty(n * 24, dtype=torch.uint8, device=f"cuda:{local}")
-    dlk = torch.empty(n * 32, dtype=torch.uint8, device=f"cuda:{local}")
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
-    torch.cuda.synchronize()
+    clk = Clocks(local).__enter__()
 
-    def step(k: int):
-        cur = k & 1
-        t.build(cur, dframes[cur].data_ptr(), W, where=vtg.DEVICE, stream=None)
-        t.cells_device(cur ^ 1, cur, dcells.data_ptr(), dlk.data_ptr())
+    # ---- the plain GPU form
+    plain = time_plain(vtg, torch, ctx, dev[0], max(args.steps, 20), args.warmup, device)
 
-    t.build(0, dframes[0].data_ptr(), W, where=vtg.DEVICE)
-    for k in range(1, args.warmup + 1):
-        step(k)
-    torch.cuda.synchronize()
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    lk_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    # ---- the batched form: B streams a step, autotuned, replayed from CUDA graphs
+    trackers = [vtg.Tracker(ctx, vtg.config(W, H, levels=LEVELS, cell_w=CELL_W, cell_h=CELL_H)) for _ in range(B)]
+    batch = vtg.Batch(ctx, B)
+    batch.prepare(0, trackers, [d0.data_ptr() for d0, _ in dev], [0] * B)
+    batch.prepare(1, trackers, [d1.data_ptr() for _, d1 in dev], [1] * B)
+    batch.launch(0)
+    batch.launch(1)
+    ctx.sync()
+    tuned, tuned_ms, default_ms = batch.autotune(1, reps=5)
+    batch.capture(0)
+    batch.capture(1)
+    bstream = torch.cuda.ExternalStream(batch.stream)
+    for k in range(args.warmup):
+        batch.replay(k & 1)
+    ctx.sync()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
-    with Clocks(local) as clk:
-        wall0 = time.perf_counter()
-        for k in range(args.steps):
-            with torch.cuda.stream(stream):
-                flush.fill_(k & 255)
-                starts[k].record(stream)
-            cur = (args.warmup + 1 + k) & 1
-            t.build(cur, dframes[cur].data_ptr(), W, where=vtg.DEVICE)
-            with torch.cuda.stream(stream):
-                lk_ev[k][0].record(stream)
-            t.cells_device(cur ^ 1, cur, dcells.data_ptr(), dlk.data_ptr())
-            with torch.cuda.stream(stream):
-                lk_ev[k][1].record(stream)
-                ends[k].record(stream)
-        torch.cuda.synchronize()
-        wall = time.perf_counter() - wall0
-    step_ms = np.array([s.elapsed_time(e) for s, e in zip(starts, ends)])
-    lk_ms = np.array([a.elapsed_time(b) for a, b in lk_ev])
+    for k in range(args.steps):
+        ev[k][0].record(bstream)
+        batch.replay((args.warmup + k) & 1)
+        ev[k][1].record(bstream)
+    torch.cuda.synchronize()
+    step_ms = np.array([a.elapsed_time(b) for a, b in ev])
     total_ms = float(step_ms.sum())
     if world > 1:
-        tt = torch.tensor([total_ms], device=f"cuda:{local}")
+        tt = torch.tensor([total_ms], device=device)
         torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
         total_ms = float(tt.item())
-    value = world * n * args.steps / (total_ms / 1e3)
+    value = world * B * CELLS * args.steps / (total_ms / 1e3)
 
-    # end to end through the C ABI: pinned host frame in, cell records out, every step
-    if args.skip_e2e:
-        t.close()
-        ctx.close()
-        return {"metric": METRIC, "value": value, "unit": "cells/s", "ms_per_step": total_ms / args.steps,
-                "lk_ms": float(lk_ms.mean()), "note": "profiling run: e2e and baselines skipped"} if rank == 0 else None
-    pinned = [torch.from_numpy(f).pin_memory() for f in frames]
-    host_cells = torch.empty(n * 24, dtype=torch.uint8).pin_memory()
-    import ctypes as C
-
-    L = vtg.lib()
-    torch.cuda.synchronize()
-    e2e_steps = max(args.steps, 10)
-    t0 = time.perf_counter()
-    for k in range(e2e_steps):
-        cur = k & 1
-        vtg.check(L.vtg_build(t.h, cur, C.c_void_p(pinned[cur].data_ptr()), W, vtg.HOST, None), "vtg_build")
-        vtg.check(L.vtg_cells(t.h, cur ^ 1, cur, C.c_void_p(host_cells.data_ptr()), None, vtg.HOST, None), "vtg_cells")
-        ctx.sync(10000)
-    e2e_s = time.perf_counter() - t0
-    e2e = {"value": n * e2e_steps / e2e_s, "unit": "cells/s", "h2d_bytes_per_step": W * H,
-           "d2h_bytes_per_step": n * 24, "ms_per_step": 1e3 * e2e_s / e2e_steps}
-
-    # the cells of one step, for the algorithmic FLOP count
-    t.build(0, dframes[0].data_ptr(), W, where=vtg.DEVICE)
-    t.build(1, dframes[1].data_ptr(), W, where=vtg.DEVICE)
-    cells, lk = t.cells(0, 1)
-    flops = lk_flops(lk, LEVELS)
+    # ---- rooflines: the LK launch and the pyramid launches of a batched step, timed apart
+    pyr_ms, lk_ms = batch.profile(1, reps=7)
+    flops = sum(lk_flops(vtg.tracker_results(t)[1]) for t in trackers)
     pk = peaks()
     sm_max = pk.get("sm_max_mhz", 2070.0)
     fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12
-    lk_avg_s = float(lk_ms.mean()) / 1e3
-    achieved = flops / lk_avg_s / 1e12
-    roofline = {"kernel": "lk_cells_kernel", "bound": "fp32", "achieved": achieved, "peak": fp32_peak,
+    achieved = flops / (lk_ms / 1e3) / 1e12
+    roofline = {"kernel": "lk_batch_kernel", "bound": "fp32", "achieved": achieved, "peak": fp32_peak,
                 "unit": "TFLOP/s", "frac": achieved / fp32_peak,
-                "peak_source": "nominal FP32 CUDA-core rate (152 SMs x 128 lanes x 2) at the measured max SM clock; "
-                               "MEASURED_PEAKS.json holds no FP32 figure",
-                "algorithmic_flop_per_launch": flops, "launch_ms": float(lk_ms.mean()), "traffic": None}
-    pyr_ms = float((step_ms - lk_ms).mean())
-    pyr_bytes = W * H + 4 * sum(a * b for a, b in [(1920, 1080), (960, 540), (480, 270), (240, 135)])
-    roof_pyr = {"kernel": "pyr_reduce_kernel (3 launches)", "bound": "hbm", "achieved": pyr_bytes / (pyr_ms / 1e3) / 1e9,
-                "peak": pk.get("hbm_gbs", 6800.0), "unit": "GB/s",
+                "peak_source": "nominal FP32 CUDA-core rate (152 SMs x 128 lanes x 2) at the measured max SM clock "
+                               "(MEASURED_PEAKS.json sm_max_mhz); MEASURED_PEAKS.json holds no FP32 rate",
+                "algorithmic_flop_per_launch": flops, "launch_ms": lk_ms, "traffic": None,
+                "traffic_note": "see profiles/lk_batch_kernel_1080p.md (ncu dram bytes per launch)"}
+    pyr_bytes = B * (W * H + 4 * sum(a * b for a, b in [(1920, 1080), (960, 540), (480, 270), (240, 135)]))
+    roof_pyr = {"kernel": "pyr_batch_kernel (3 launches a step)", "bound": "hbm",
+                "achieved": pyr_bytes / (pyr_ms / 1e3) / 1e9, "peak": pk.get("hbm_gbs", 6800.0), "unit": "GB/s",
                 "frac": pyr_bytes / (pyr_ms / 1e3) / 1e9 / pk.get("hbm_gbs", 6800.0),
                 "algorithmic_bytes_per_step": pyr_bytes, "ms_per_step": pyr_ms,
-                "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in pk else "fallback"}
-    t.close()
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in pk else "fallback 6.8 TB/s"}
+    batch.close()
+    for t in trackers:
+        t.close()
+
+    # ---- end to end: the served loop through the C ABI, pinned host frames in, cell records out
+    pinned = []
+    for f0, f1 in pairs:
+        pinned += [torch.from_numpy(f0).pin_memory(), torch.from_numpy(f1).pin_memory()]
+    lkcfg = vtg.config(64, 64, levels=LEVELS, cell_w=CELL_W, cell_h=CELL_H)
+    frames_per_stream = max(60, args.steps * 4)
+    sat = [dict(width=W, height=H, fps=1000.0, start_s=0.0, frames=frames_per_stream) for _ in range(B)]
+    served = vtg.serve(ctx, sat, [p.data_ptr() for p in pinned], lkcfg, duration_s=10.0, max_batch=B, inflight=2,
+                       ncc_share=0.02, seed=11)
+    served_plain = vtg.serve(ctx, sat, [p.data_ptr() for p in pinned], lkcfg, duration_s=30.0, max_batch=B,
+                             inflight=1, ncc_share=0.02, plain=True, seed=11)
+    e2e = {"value": served["cells_per_s"], "unit": "cells/s", "h2d_bytes_per_step": W * H,
+           "d2h_bytes_per_step": CELLS * 24, "step": "one frame pair (new frame in, its 16,200 cell records out)",
+           "p50_ms_per_pair": served["p50_ms"], "p99_ms_per_pair": served["p99_ms"], "mean_batch": served["mean_batch"],
+           "ncc_searches": served["ncc"], "arrivals": "Poisson, %d streams x 1000 fps (saturating)" % B}
+    e2e_plain = {"value": served_plain["cells_per_s"], "unit": "cells/s", "p50_ms_per_pair": served_plain["p50_ms"],
+                 "p99_ms_per_pair": served_plain["p99_ms"]}
+    # nominal rates, mixed sizes: two 1080p at 60 fps (4,080 cells at level 1), one 720p at 15 fps, 13 more
+    mix = [dict(width=1920, height=1080, flow_level=1, fps=60.0, start_s=0.0, frames=90),
+           dict(width=1920, height=1080, flow_level=1, fps=60.0, start_s=0.0, frames=90),
+           dict(width=1280, height=720, fps=15.0, start_s=0.0, frames=25)]
+    sizes = [(640, 480), (1280, 720), (1920, 1080)]
+    for k in range(13):
+        w, h = sizes[k % 3]
+        mix.append(dict(width=w, height=h, fps=30.0, start_s=0.05 * k, frames=45))
+    mix_frames = []
+    for k, s in enumerate(mix):
+        src = pairs[k % B]
+        for f in src:
+            mix_frames.append(torch.from_numpy(np.ascontiguousarray(f[:s["height"], :s["width"]])).pin_memory())
+    mixed = vtg.serve(ctx, mix, [p.data_ptr() for p in mix_frames], lkcfg, duration_s=3.0, max_batch=32, inflight=2,
+                      ncc_share=0.02, seed=12)
+    mixed_plain = vtg.serve(ctx, mix, [p.data_ptr() for p in mix_frames], lkcfg, duration_s=3.0, max_batch=32,
+                            inflight=1, ncc_share=0.02, plain=True, seed=12)
+    clk.__exit__(None, None, None)
     ctx.close()
+    if rank != 0:
+        return None
     line = {"metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded noise, blur 1.5, warp)",
-            "config": workload("plain"), "p50_ms_per_pair": float(np.percentile(step_ms, 50)),
-            "p99_ms_per_pair": float(np.percentile(step_ms, 99)), "e2e": e2e, "roofline": roofline,
-            "roofline_pyramid": roof_pyr, "gpu_launches": args.steps * LEVELS, "clocks": clk.summary(),
-            "wall_s": wall}
-    if rank == 0:
-        line["cpu_baseline"] = cpu_baseline(cells_sample=4050, frames=(f0, f1))
-    return line if rank == 0 else None
+            "config": workload("batched, graph-replayed", B),
+            "p50_ms_per_step": float(np.percentile(step_ms, 50)), "p99_ms_per_step": float(np.percentile(step_ms, 99)),
+            "plain": plain, "batched_vs_plain": value / plain["value"],
+            "autotune": {"chosen": tuned, "chosen_ms": tuned_ms, "default_ms": default_ms,
+                         "default": {"block_warps": 8, "chunk": 1, "persistent": 1, "ctas_per_sm": 2}},
+            "e2e": e2e, "e2e_plain": e2e_plain, "e2e_vs_plain": e2e["value"] / max(e2e_plain["value"], 1e-9),
+            "served_mix": {"served": {k: mixed[k] for k in ("cells_per_s", "p50_ms", "p99_ms", "mean_batch", "ncc",
+                                                            "served")},
+                           "plain": {k: mixed_plain[k] for k in ("cells_per_s", "p50_ms", "p99_ms", "served")},
+                           "streams": "2x1080p@60 (4,080 cells), 1x720p@15, 13 more 640x480..1080p@30"},
+            "roofline": roofline, "roofline_pyramid": roof_pyr, "gpu_launches": args.steps * LEVELS,
+            "clocks": clk.summary()}
+    line["cpu_baseline"] = cpu_baseline(pairs[0])
+    return line
 
 
-def cpu_baseline(cells_sample: int, frames, threads: int | None = None) -> dict:
-    """The oracle's FP64 restatement of the reference's path on the host cores: the pyramid of one frame and LK with
-    forward-backward at the first `cells_sample` cells of the 16,200, repeated to at least 10 s."""
+def cpu_baseline(frames, seconds: float = 10.0) -> dict:
+    """The oracle's FP64 restatement of the reference's path on all host cores: the new frame's pyramid and LK with
+    the forward-backward check at every 4th cell of the 16,200, repeated for `seconds`."""
     sys.path.insert(0, ORACLE)
+    import platform
+
     import oracle as O
 
-    threads = threads or os.cpu_count() or 1
+    threads = os.cpu_count() or 1
     f0, f1 = frames
     xs, ys = O.cell_centres(W, H, CELL_W, CELL_H)
-    xs, ys = xs[:cells_sample], ys[:cells_sample]
+    xs, ys = xs[::4], ys[::4]
     cfg = O.lk_cfg()
     P0 = O.pyramid(f0, LEVELS)
     done, t0 = 0, time.perf_counter()
-    while time.perf_counter() - t0 < 10.0:
+    while time.perf_counter() - t0 < seconds:
         P1 = O.pyramid(f1, LEVELS)
         O.lk_points(P0, P1, LEVELS - 1, cfg, xs, ys, max_fb=0.5, mode=O.F64, threads=threads)
         done += len(xs)
     dt = time.perf_counter() - t0
-    import platform
-
     return {"value": done / dt, "unit": "cells/s", "cores": threads, "kind": "port",
-            "sample": "pyramid + %d of 16,200 cells per repetition, FP64 oracle form, %d reps in %.1f s on %s" % (
-                cells_sample, done // cells_sample, dt, platform.machine())}
+            "sample": "the new frame's pyramid + every 4th of the 16,200 cells (4,050) per repetition, FP64 oracle form, "
+                      "%d repetitions in %.1f s on %s" % (done // len(xs), dt, platform.machine())}
 
 
 def run_reference(args) -> dict | None:
-    rank = int(os.environ.get("RANK", "0"))
-    if rank != 0:
+    if int(os.environ.get("RANK", "0")) != 0:
         return None
     sys.path.insert(0, ORACLE)
+    import platform
+
     import oracle as O
     import vtg_synth as S
 
     threads = os.cpu_count() or 1
     f0, f1, _, _ = S.warp_pair(W, H, S.seeded_shift(2, 0), 0.5, seed=2)
     xs, ys = O.cell_centres(W, H, CELL_W, CELL_H)
-    sample = 2025  # one eighth of the grid, every 8th cell
     xs, ys = xs[::8], ys[::8]
     cfg = O.lk_cfg()
     P0 = O.pyramid(f0, LEVELS)
@@ -280,17 +334,55 @@ def run_reference(args) -> dict | None:
         step()
         times.append(time.perf_counter() - t0)
     total = sum(times)
-    value = sample * args.steps / total
-    import platform
-
+    value = len(xs) * args.steps / total
     cb = {"value": value, "unit": "cells/s", "cores": threads, "kind": "port",
           "sample": "per step: the new frame's pyramid and every 8th cell (2,025 of 16,200), FP64 oracle form, %s" %
                     platform.machine()}
     return {"impl": "reference", "metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": 0,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded noise, blur 1.5, warp)", "config": workload("cpu"), "cpu_baseline": cb,
+            "data": "synthetic (seeded noise, blur 1.5, warp)", "config": workload("cpu", 1), "cpu_baseline": cb,
             "e2e": {"value": value, "unit": "cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def run_profile(args) -> None:
+    """Launches for an ncu capture, nothing timed: `batch` primes B 1080p streams (2 batched steps) and runs 2 more
+    (capture lk_batch_kernel with -s 2); `ncc` runs one 1080p whole-picture search per precision (32 x 32 template)."""
+    import torch
+
+    import vtg
+    import vtg_build
+    import vtg_synth as S
+
+    vtg_build.build()
+    ctx = vtg.Context(0)
+    if args.profile == "batch":
+        B = args.streams
+        pairs = frames_1080(B)
+        dev = [(torch.from_numpy(f0).cuda(), torch.from_numpy(f1).cuda()) for f0, f1 in pairs]
+        torch.cuda.synchronize()
+        trackers = [vtg.Tracker(ctx, vtg.config(W, H, levels=LEVELS, cell_w=CELL_W, cell_h=CELL_H)) for _ in range(B)]
+        batch = vtg.Batch(ctx, B)
+        batch.prepare(0, trackers, [d0.data_ptr() for d0, _ in dev], [0] * B)
+        batch.prepare(1, trackers, [d1.data_ptr() for _, d1 in dev], [1] * B)
+        for k in range(4):
+            batch.launch(k & 1)
+        ctx.sync()
+        print("profile batch: %d streams, %d cells a step" % (B, batch.cells(0)))
+    else:
+        frame = S.noise_frame(W, H, seed=3)
+        tpl, xs, ys, _ = S.ncc_templates(frame, 32, 1, seed=1, blank_share=0.0)
+        app = (tpl[0].astype(np.float32) - np.float32(tpl[0].mean(dtype=np.float64))).astype(np.float32)
+        norm = float(np.sum(app.astype(np.float64) ** 2))
+        d = torch.from_numpy(frame).cuda()
+        torch.cuda.synchronize()
+        s = vtg.Search(ctx, W, H)
+        s.template(app, norm)
+        for prec in (vtg.NCC_BF16, vtg.NCC_FP16, vtg.NCC_F32):
+            f = s.run(d.data_ptr(), W, H, W, vtg.PLANE_U8, 1, W, 1, H, 1, prec)
+            print("profile ncc precision %d: found (%d, %d) ncc %.4f" % (prec, f["hx"], f["hy"], f["ncc"]))
+        s.close()
+    ctx.close()
 
 
 def main():
@@ -299,10 +391,14 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--form", default="plain", choices=["plain"])
-    ap.add_argument("--skip-e2e", action="store_true", help="time the kernels only (for profiling)")
+    ap.add_argument("--streams", type=int, default=8, help="1080p streams a batched step")
+    ap.add_argument("--profile", default=None, choices=["batch", "ncc"],
+                    help="a short run for an ncu capture: the batched step (prime, then 2 steps) or one NCC search")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.profile:
+        run_profile(args)
+        return
     line = run_reference(args) if args.impl == "reference" else run_ours(args)
     if line is not None:
         print(json.dumps(line))

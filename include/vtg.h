@@ -167,6 +167,9 @@ int vtg_batch_get_tune(const vtg_batch *b, struct vtg_tune *t);
 /* Times every candidate launch shape on the prepared step (median of reps) and keeps the fastest for this mix of
  * stream sizes; reports it, its time and the default shape's time. */
 int vtg_batch_autotune(vtg_batch *b, int slot, int reps, struct vtg_tune *best, float *best_ms, float *default_ms);
+/* Runs a prepared step reps times with events between its phases: the median time of the pyramids (with any host
+ * frames' upload) and of the LK launch. For rooflines. */
+int vtg_batch_profile(vtg_batch *b, int slot, int reps, float *pyr_ms, float *lk_ms);
 
 /* ---- the appearance search (reacquisition) ---- */
 

@@ -474,3 +474,42 @@ extern "C" int vtg_tracker_results(vtg_tracker *t, struct vtg_cell *cells, struc
         CU(cudaMemcpyAsync(lk, t->d_lk, n * sizeof(vtg_lk_out), k, s));
     return VTG_OK;
 }
+
+extern "C" int vtg_batch_profile(vtg_batch *b, int slot, int reps, float *pyr_ms, float *lk_ms)
+{
+    if (!b || slot < 0 || slot >= BATCH_SLOTS || !b->slot[slot].ready || reps < 1)
+        return VTG_EINVAL;
+    BatchSlot &sl = b->slot[slot];
+    cudaEvent_t e[3];
+    for (int i = 0; i < 3; i++)
+        CU(cudaEventCreate(&e[i]));
+    std::vector<float> tp, tl;
+    LkTune t = b->tune;
+    t.chunk = sl.chunk;
+    for (int r = 0; r < reps; r++) {
+        CU(cudaEventRecord(e[0], b->stream));
+        for (size_t k = 0; k < sl.h_src.size(); k++)
+            CU(cudaMemcpy2DAsync(sl.h_dst[k], (size_t)sl.h_w[k], sl.h_src[k], (size_t)sl.h_stride[k], (size_t)sl.h_w[k],
+                                 (size_t)sl.h_h[k], cudaMemcpyHostToDevice, b->stream));
+        CU(vtg_launch_pyramid_batch(sl.d_pyr, sl.d_tiles, sl.tiles, sl.njobs, sl.max_levels, b->stream));
+        CU(cudaMemsetAsync(sl.d_counter, 0, sizeof(int), b->stream));
+        CU(cudaEventRecord(e[1], b->stream));
+        CU(vtg_launch_lk_batch(sl.d_lk, sl.d_items, sl.njobs, sl.items, sl.prm, t, b->sms, sl.d_counter, b->stream));
+        CU(cudaEventRecord(e[2], b->stream));
+        CU(cudaEventSynchronize(e[2]));
+        float a = 0.0f, c = 0.0f;
+        CU(cudaEventElapsedTime(&a, e[0], e[1]));
+        CU(cudaEventElapsedTime(&c, e[1], e[2]));
+        tp.push_back(a);
+        tl.push_back(c);
+    }
+    for (int i = 0; i < 3; i++)
+        cudaEventDestroy(e[i]);
+    std::sort(tp.begin(), tp.end());
+    std::sort(tl.begin(), tl.end());
+    if (pyr_ms)
+        *pyr_ms = tp[tp.size() / 2];
+    if (lk_ms)
+        *lk_ms = tl[tl.size() / 2];
+    return VTG_OK;
+}

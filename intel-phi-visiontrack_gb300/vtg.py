@@ -316,6 +316,7 @@ def _batch_sigs(L):
     L.vtg_batch_get_tune.argtypes = [vp, C.POINTER(Tune)]
     L.vtg_batch_autotune.argtypes = [vp, i, i, C.POINTER(Tune), C.POINTER(C.c_float), C.POINTER(C.c_float)]
     L.vtg_tracker_results.argtypes = [vp, vp, vp, i, vp]
+    L.vtg_batch_profile.argtypes = [vp, i, i, C.POINTER(C.c_float), C.POINTER(C.c_float)]
 
 
 class Batch:
@@ -379,6 +380,12 @@ class Batch:
         check(lib().vtg_batch_autotune(self.h, slot, reps, C.byref(t), C.byref(b), C.byref(d)), "vtg_batch_autotune")
         return t.as_dict(), b.value, d.value
 
+    def profile(self, slot: int, reps: int = 5):
+        """(pyramid ms, LK ms): medians over reps runs of the prepared step."""
+        a, b = C.c_float(), C.c_float()
+        check(lib().vtg_batch_profile(self.h, slot, reps, C.byref(a), C.byref(b)), "vtg_batch_profile")
+        return a.value, b.value
+
     def close(self):
         if self.h:
             lib().vtg_batch_destroy(self.h)
@@ -399,3 +406,41 @@ def tracker_results(t: Tracker, want_lk: bool = True):
     check(lib().vtg_tracker_results(t.h, _p(cells), _p(lk), HOST, None), "vtg_tracker_results")
     t.ctx.sync()
     return cells, lk
+
+
+# ---------------------------------------------------------------- the served request loop
+
+class ServeStream(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("flow_level", C.c_uint32), ("fps", C.c_float),
+                ("start_s", C.c_float), ("frames", C.c_int)]
+
+
+class ServeCfg(C.Structure):
+    _fields_ = [("nstreams", C.c_int), ("streams", C.POINTER(ServeStream)), ("frames", C.POINTER(C.c_void_p)),
+                ("lk", Config), ("duration_s", C.c_double), ("max_batch", C.c_int), ("inflight", C.c_int),
+                ("hbm_budget", C.c_size_t), ("ncc_share", C.c_float), ("plain", C.c_int), ("seed", C.c_uint64)]
+
+
+class ServeStats(C.Structure):
+    _fields_ = [("streams_admitted", C.c_int), ("streams_waited", C.c_int), ("streams_rejected", C.c_int),
+                ("requests", C.c_long), ("served", C.c_long), ("cells", C.c_long), ("ncc", C.c_long),
+                ("wall_s", C.c_double), ("cells_per_s", C.c_double), ("p50_ms", C.c_double), ("p99_ms", C.c_double),
+                ("max_ms", C.c_double), ("mean_batch", C.c_double)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+def serve(ctx: Context, streams, frames, lk: Config, duration_s: float, max_batch: int = 64, inflight: int = 2,
+          hbm_budget: int = 0, ncc_share: float = 0.0, plain: bool = False, seed: int = 1) -> dict:
+    """Runs vtg_serve_run. streams: dicts (width, height, flow_level, fps, start_s, frames); frames: two host
+    addresses per stream (pinned uint8 buffers, width bytes a row)."""
+    L = lib()
+    L.vtg_serve_run.argtypes = [C.c_void_p, C.POINTER(ServeCfg), C.POINTER(ServeStats)]
+    ss = (ServeStream * len(streams))(*[ServeStream(s["width"], s["height"], s.get("flow_level", 0), s["fps"],
+                                                     s.get("start_s", 0.0), s["frames"]) for s in streams])
+    fp = (C.c_void_p * len(frames))(*frames)
+    cfg = ServeCfg(len(streams), ss, fp, lk, duration_s, max_batch, inflight, hbm_budget, ncc_share, int(plain), seed)
+    st = ServeStats()
+    check(L.vtg_serve_run(ctx.h, C.byref(cfg), C.byref(st)), "vtg_serve_run")
+    return st.as_dict()
