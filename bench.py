@@ -345,6 +345,65 @@ def run_reference(args) -> dict | None:
             "e2e": {"value": value, "unit": "cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def run_ncc(args) -> dict:
+    """The whole-picture appearance search over a 1920 x 1080 8-bit frame, templates of 32, 64 and 96 (5 each, one in
+    ten near-blank at 10 %, here one of each size), per map precision: CUDA-event time of the whole search (integral
+    images, map, eight candidates, half-pixel re-score), the map's tensor FLOP rate, and agreement: the found corner
+    against the true one and against the F32 map's, the score against the FP64 oracle at the found corner."""
+    import torch
+
+    import vtg
+    import vtg_build
+    import vtg_synth as S
+
+    sys.path.insert(0, ORACLE)
+    import oracle as O
+
+    vtg_build.build()
+    frame = S.noise_frame(W, H, seed=3)
+    d = torch.from_numpy(frame).cuda()
+    torch.cuda.synchronize()
+    ctx = vtg.Context(0)
+    s = vtg.Search(ctx, W, H)
+    stream = torch.cuda.ExternalStream(vtg.lib().vtg_search_stream(s.h))
+    out = {"metric": "appearance search ms per template (whole 1920x1080 picture, step 1)", "unit": "ms",
+           "higher_is_better": False, "results": []}
+    pk = peaks()
+    for size in (32, 64, 96):
+        tpl, xs, ys, blank = S.ncc_templates(frame, size, 5, seed=size, blank_share=0.2)
+        for k in range(5):
+            app = (tpl[k].astype(np.float32) - np.float32(tpl[k].mean(dtype=np.float64))).astype(np.float32)
+            norm = float(np.sum(app.astype(np.float64) ** 2))
+            s.template(app, norm)
+            row = {"size": size, "blank": bool(blank[k]), "true": [int(xs[k]), int(ys[k])]}
+            for prec, name in ((vtg.NCC_F32, "f32"), (vtg.NCC_BF16, "bf16"), (vtg.NCC_FP16, "fp16")):
+                reps = 3 if prec == vtg.NCC_F32 else 10
+                s.run(d.data_ptr(), W, H, W, vtg.PLANE_U8, 1, W, 1, H, 1, prec)
+                ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+                for a, b in ev:
+                    a.record(stream)
+                    f = s.run(d.data_ptr(), W, H, W, vtg.PLANE_U8, 1, W, 1, H, 1, prec)
+                    b.record(stream)
+                torch.cuda.synchronize()
+                ms = float(np.median([a.elapsed_time(b) for a, b in ev]))
+                corners = (W - size - 2) * (H - size - 2)
+                row[name] = {"ms": ms, "found": [f["hx"] / 2, f["hy"] / 2], "ncc": f["ncc"], "second": f["second"]}
+                if prec != vtg.NCC_F32:
+                    row[name]["map_tflops_useful"] = 2.0 * size * size * corners / (ms / 1e3) / 1e12
+            o = O.ncc_half(frame.astype(np.float32), app, norm, int(row["f32"]["found"][0] * 2),
+                           int(row["f32"]["found"][1] * 2), O.F64)
+            row["fp64_score_at_found"] = o
+            row["score_err_f32"] = abs(row["f32"]["ncc"] - o)
+            row["agree_bf16_f32"] = row["bf16"]["found"] == row["f32"]["found"]
+            row["agree_fp16_f32"] = row["fp16"]["found"] == row["f32"]["found"]
+            row["found_true"] = row["f32"]["found"] == row["true"]
+            out["results"].append(row)
+    s.close()
+    ctx.close()
+    out["peak_bf16_tflops"] = pk.get("bf16_tflops")
+    return out
+
+
 def run_profile(args) -> None:
     """Launches for an ncu capture, nothing timed: `batch` primes B 1080p streams (2 batched steps) and runs 2 more
     (capture lk_batch_kernel with -s 2); `ncc` runs one 1080p whole-picture search per precision (32 x 32 template)."""
@@ -392,12 +451,17 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--streams", type=int, default=8, help="1080p streams a batched step")
+    ap.add_argument("--ncc", action="store_true",
+                    help="the whole-picture appearance search on a 1080p frame (32, 64, 96 templates), per precision")
     ap.add_argument("--profile", default=None, choices=["batch", "ncc"],
                     help="a short run for an ncu capture: the batched step (prime, then 2 steps) or one NCC search")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.profile:
         run_profile(args)
+        return
+    if args.ncc:
+        print(json.dumps(run_ncc(args)))
         return
     line = run_reference(args) if args.impl == "reference" else run_ours(args)
     if line is not None:

@@ -225,7 +225,7 @@ int vtg_correlate(vtg_search *s, const void *plane, int w, int h, int pitch, int
  * search as vtg_search_run with an F32 map, but nothing is allocated: no context, no search context; the caller
  * passes the plane, the template (th rows of tw zero-mean floats, tw a multiple of 8) and its norm, and *found (and the
  * optional per-cell map) in device memory; the scratch lives in one fixed device array of VTG_NOALLOC_SCRATCH_BYTES.
- * Larger planes or templates than the limits above return VTG_EINVAL. All calls share that array: calls whose work
+ * Larger planes or templates than the limits above, or a step above 4, return VTG_EINVAL. All calls share that array: calls whose work
  * overlaps on the GPU race, so order them on one stream. The first call on a device looks the array's address up;
  * make it before any stream capture. Asynchronous on `stream` (a cudaStream_t, NULL for the legacy default). */
 int vtg_search_run_noalloc(const void *plane, int w, int h, int pitch, int plane_type, const float *app, int tw, int th,

@@ -28,7 +28,8 @@ struct vtg_search {
 static size_t up256(size_t n) { return (n + 255) & ~(size_t)255; }
 
 struct SearchLayout {
-    size_t app, sum, S1, S2, map_v, map_x, map_y, top, ntop, err, band0, band1, found, bytes;
+    size_t app, sum, S1, S2, map_v, map_x, map_y, top, ntop, err, half, band0, band1, found, conv, fac, cellw, bytes;
+    size_t conv_elems, fac_elems;
     int tp, cells;
 };
 
@@ -64,12 +65,22 @@ static SearchLayout search_layout(int max_w, int max_h, int max_tw, int max_th)
     b += 256;
     L.err = b;
     b += 256;
+    L.half = b;
+    b += up256(sizeof(float) * NCC_HALF_MAX);
     L.band0 = b;
     b += up256(vtg_ncc_band_bytes(max_tw, max_th));
     L.band1 = b;
     b += up256(vtg_ncc_band_bytes(max_tw, max_th));
     L.found = b;
     b += 256;
+    L.conv_elems = vtg_ncc_conv_elems(max_w, max_h, max_th);
+    L.conv = b;
+    b += up256(sizeof(uint16_t) * L.conv_elems);
+    L.fac_elems = (size_t)max_w * max_h;
+    L.fac = b;
+    b += up256(sizeof(float) * L.fac_elems);
+    L.cellw = b;
+    b += up256(sizeof(unsigned long long) * (size_t)L.cells);
     L.bytes = b;
     return L;
 }
@@ -134,9 +145,16 @@ extern "C" int vtg_search_create(vtg_ctx *ctx, int max_w, int max_h, int max_tw,
     s->sc.top = (int *)(s->mem + L.top);
     s->sc.ntop = (int *)(s->mem + L.ntop);
     s->sc.err = (int *)(s->mem + L.err);
+    s->sc.half = (float *)(s->mem + L.half);
     s->band[0] = (uint16_t *)(s->mem + L.band0);
     s->band[1] = (uint16_t *)(s->mem + L.band1);
     s->sc.band = nullptr;
+    s->sc.band_rows = s->sc.krow = 0;
+    s->sc.conv = (uint16_t *)(s->mem + L.conv);
+    s->sc.conv_elems = L.conv_elems;
+    s->sc.fac = (float *)(s->mem + L.fac);
+    s->sc.fac_elems = L.fac_elems;
+    s->sc.cellw = (unsigned long long *)(s->mem + L.cellw);
     s->found = (vtg_found *)(s->mem + L.found);
     s->xy = nullptr;
     s->vals = nullptr;

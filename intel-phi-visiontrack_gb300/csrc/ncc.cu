@@ -16,9 +16,9 @@
  *   ncc_map_f32 (or the tensor-core map in ncc_tc.cu)  per cell: best score and its corner
  *   ncc_top                       the eight best cells, value descending then cell index ascending (the reference's
  *                                 insertion order)
- *   ncc_refine                    each candidate in half pixels within +-(2 step - 1) (or +-1), the best, the second
- *                                 peak clear of it by half a template, and the parabola offsets; F32 products with exact
- *                                 integer (quarter-pixel) window sums. */
+ *   ncc_half_all / ncc_pick       each candidate in half pixels within +-(2 step - 1) (or +-1), one warp per corner;
+ *                                 then the best, the second peak clear of it by half a template, and the parabola
+ *                                 offsets; F32 products with exact integer (quarter-pixel) window sums. */
 #include <float.h>
 
 #include "vtg_internal.cuh"
@@ -32,7 +32,8 @@ __device__ __forceinline__ long long pix(const T *p, size_t i)
     return (long long)__ldg(p + i);
 }
 
-/* Row pass: table row y + 1, columns 1 .. w, holds the prefix of row y (and of its squares). One warp per row. */
+/* Row pass: table row y + 1, columns 1 .. w, holds the prefix of row y (and of its squares); row 0 and column 0 are
+ * zero. One warp per row, 4 pixels a lane per round, sums in 64 bits. */
 template <typename T>
 __global__ void integral_rows(const T *__restrict__ plane, int pitch, int w, int h, long long *__restrict__ S1,
                               long long *__restrict__ S2, int tp)
@@ -51,41 +52,83 @@ __global__ void integral_rows(const T *__restrict__ plane, int pitch, int w, int
         r1[0] = r2[0] = 0;
     long long c1 = 0, c2 = 0;
     const T *src = plane + (size_t)(y - 1) * pitch;
-    for (int x0 = 0; x0 < w; x0 += 32) {
-        const int x = x0 + lane;
-        long long v1 = x < w ? pix(src, x) : 0;
-        long long v2 = v1 * v1;
+    for (int x0 = 0; x0 < w; x0 += 128) {
+        long long v[4], q[4];
+        long long a1 = 0, a2 = 0;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const int x = x0 + 4 * lane + k;
+            const long long p = x < w ? pix(src, x) : 0;
+            a1 += p;
+            a2 += p * p;
+            v[k] = a1;
+            q[k] = a2;
+        }
+        long long s1 = a1, s2 = a2;
 #pragma unroll
         for (int s = 1; s < 32; s <<= 1) {
-            const long long a = __shfl_up_sync(VTG_FULL, v1, s), b = __shfl_up_sync(VTG_FULL, v2, s);
+            const long long b1 = __shfl_up_sync(VTG_FULL, s1, s), b2 = __shfl_up_sync(VTG_FULL, s2, s);
             if (lane >= s) {
-                v1 += a;
-                v2 += b;
+                s1 += b1;
+                s2 += b2;
             }
         }
-        if (x < w) {
-            r1[x + 1] = c1 + v1;
-            r2[x + 1] = c2 + v2;
+        const long long e1 = c1 + s1 - a1, e2 = c2 + s2 - a2; /* exclusive prefix of this lane's four */
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const int x = x0 + 4 * lane + k;
+            if (x < w) {
+                r1[x + 1] = e1 + v[k];
+                r2[x + 1] = e2 + q[k];
+            }
         }
-        c1 += __shfl_sync(VTG_FULL, v1, 31);
-        c2 += __shfl_sync(VTG_FULL, v2, 31);
+        c1 += __shfl_sync(VTG_FULL, s1, 31);
+        c2 += __shfl_sync(VTG_FULL, s2, 31);
     }
 }
 
-/* Column pass: running sums down the rows, one thread per column. */
-__global__ void integral_cols(int w, int h, long long *__restrict__ S1, long long *__restrict__ S2, int tp)
+/* Column pass: running sums down the rows. A CTA takes 32 columns and splits the rows into 32 segments: each thread
+ * sums its segment, the segments' totals are scanned in shared memory, and each thread adds its offset. */
+#define IC_COLS 32
+#define IC_SEGS 32
+__global__ void __launch_bounds__(IC_COLS *IC_SEGS) integral_cols(int w, int h, long long *__restrict__ S1,
+                                                                  long long *__restrict__ S2, int tp)
 {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    if (x > w)
-        return;
+    __shared__ long long t1[IC_SEGS][IC_COLS + 1], t2[IC_SEGS][IC_COLS + 1];
+    const int c = threadIdx.x % IC_COLS, g = threadIdx.x / IC_COLS;
+    const int x = blockIdx.x * IC_COLS + c;
+    const int rows = h + 1, seg = (rows + IC_SEGS - 1) / IC_SEGS;
+    const int r0 = g * seg, r1 = min(r0 + seg, rows);
     long long a = 0, b = 0;
-    for (int y = 1; y <= h; y++) {
-        const size_t i = (size_t)y * tp + x;
-        a += S1[i];
-        b += S2[i];
-        S1[i] = a;
-        S2[i] = b;
+    if (x <= w)
+        for (int y = r0; y < r1; y++) {
+            const size_t i = (size_t)y * tp + x;
+            a += S1[i];
+            b += S2[i];
+            S1[i] = a;
+            S2[i] = b;
+        }
+    t1[g][c] = a;
+    t2[g][c] = b;
+    __syncthreads();
+    if (g == 0) {
+        long long o1 = 0, o2 = 0;
+        for (int k = 0; k < IC_SEGS; k++) {
+            const long long u1 = t1[k][c], u2 = t2[k][c];
+            t1[k][c] = o1;
+            t2[k][c] = o2;
+            o1 += u1;
+            o2 += u2;
+        }
     }
+    __syncthreads();
+    const long long o1 = t1[g][c], o2 = t2[g][c];
+    if (x <= w && (o1 | o2))
+        for (int y = r0; y < r1; y++) {
+            const size_t i = (size_t)y * tp + x;
+            S1[i] += o1;
+            S2[i] += o2;
+        }
 }
 
 /* ---- the score, shared by every map kernel ---- */
@@ -297,42 +340,58 @@ __device__ __forceinline__ float parabola(float l, float c, float r)
     return fminf(fmaxf(o, -0.5f), 0.5f);
 }
 
+/* Every half-pixel corner around every candidate, one warp each: scores into hs[candidate][offset]. */
 template <typename T>
-__global__ void __launch_bounds__(NCC_TOP * 32) ncc_refine(const T *__restrict__ plane, int pitch,
-                                                           const float *__restrict__ app, NccPrm p,
-                                                           const float *__restrict__ map_v, const int *__restrict__ map_x,
-                                                           const int *__restrict__ map_y, const int *__restrict__ top,
-                                                           const int *__restrict__ ntop, vtg_found *__restrict__ out)
+__global__ void __launch_bounds__(256) ncc_half_all(const T *__restrict__ plane, int pitch, const float *__restrict__ app,
+                                                    NccPrm p, const int *__restrict__ map_x, const int *__restrict__ map_y,
+                                                    const int *__restrict__ top, const int *__restrict__ ntop,
+                                                    float *__restrict__ hs)
 {
-    __shared__ float s_score[NCC_TOP];
-    __shared__ int s_hx[NCC_TOP], s_hy[NCC_TOP];
-    __shared__ float s_side[4];
-    const int c = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int around = p.step > 1 ? 2 * p.step - 1 : 1, side = 2 * around + 1;
+    const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    const int c = wid / (side * side), o = wid - c * side * side;
+    if (c >= *ntop)
+        return;
+    const int cell = top[c];
+    const int hx = 2 * map_x[cell] + (o % side) - around, hy = 2 * map_y[cell] + (o / side) - around;
+    const float v = half_score(plane, pitch, app, p, hx, hy, lane);
+    if (lane == 0)
+        hs[c * side * side + o] = v;
+}
+
+/* The best of each candidate's corners (row-major first maximum, as search_slot's strict > over hy then hx), the
+ * best over candidates in rank order, the second peak half a template away, and the parabola through the four
+ * neighbours of the best (take_back's peak_offset), one warp each for the four. */
+template <typename T>
+__global__ void __launch_bounds__(128) ncc_pick(const T *__restrict__ plane, int pitch, const float *__restrict__ app,
+                                                NccPrm p, const int *__restrict__ map_x, const int *__restrict__ map_y,
+                                                const int *__restrict__ top, const int *__restrict__ ntop,
+                                                const float *__restrict__ hs, vtg_found *__restrict__ out)
+{
+    __shared__ float s_score[NCC_TOP], s_side[4];
+    __shared__ int s_hx[NCC_TOP], s_hy[NCC_TOP], s_best[3];
     const int n = *ntop;
-    const int around = p.step > 1 ? 2 * p.step - 1 : 1;
-    if (c < n) {
-        const int cell = top[c];
+    const int around = p.step > 1 ? 2 * p.step - 1 : 1, side = 2 * around + 1;
+    if (threadIdx.x < n) {
+        const int c = threadIdx.x, cell = top[c];
         const int cx = 2 * map_x[cell], cy = 2 * map_y[cell];
         float best = -2.0f;
         int bx = cx, by = cy;
-        for (int hy = cy - around; hy <= cy + around; hy++)
-            for (int hx = cx - around; hx <= cx + around; hx++) {
-                const float v = half_score(plane, pitch, app, p, hx, hy, lane);
-                if (v > best) {
-                    best = v;
-                    bx = hx;
-                    by = hy;
-                }
+        for (int o = 0; o < side * side; o++) {
+            const float v = hs[c * side * side + o];
+            if (v > best) {
+                best = v;
+                bx = cx + (o % side) - around;
+                by = cy + (o / side) - around;
             }
-        if (lane == 0) {
-            s_score[c] = best;
-            s_hx[c] = bx;
-            s_hy[c] = by;
         }
+        s_score[c] = best;
+        s_hx[c] = bx;
+        s_hy[c] = by;
     }
     __syncthreads();
-    if (c == 0) {
-        float ncc = -2.0f, second = -2.0f;
+    if (threadIdx.x == 0) {
+        float ncc = -2.0f;
         int hx = 0, hy = 0;
         for (int k = 0; k < n; k++)
             if (s_score[k] > ncc) {
@@ -340,34 +399,39 @@ __global__ void __launch_bounds__(NCC_TOP * 32) ncc_refine(const T *__restrict__
                 hx = s_hx[k];
                 hy = s_hy[k];
             }
+        s_best[0] = hx;
+        s_best[1] = hy;
+        s_best[2] = __float_as_int(ncc);
+    }
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int hx = s_best[0], hy = s_best[1];
+    if (n > 0) {
+        const int dx = warp == 0 ? -1 : warp == 1 ? 1 : 0, dy = warp == 2 ? -1 : warp == 3 ? 1 : 0;
+        const float v = half_score(plane, pitch, app, p, hx + dx, hy + dy, lane);
+        if (lane == 0)
+            s_side[warp] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const float ncc = __int_as_float(s_best[2]);
+        float second = -2.0f;
         for (int k = 0; k < n; k++) {
             const int dx = s_hx[k] - hx, dy = s_hy[k] - hy;
             if ((dx * dx > p.tw * p.tw || dy * dy > p.th * p.th) && s_score[k] > second)
                 second = s_score[k];
         }
-        float ox = 0.0f, oy = 0.0f;
-        if (n > 0) {
-            const float l = half_score(plane, pitch, app, p, hx - 1, hy, lane);
-            const float r = half_score(plane, pitch, app, p, hx + 1, hy, lane);
-            const float u = half_score(plane, pitch, app, p, hx, hy - 1, lane);
-            const float d = half_score(plane, pitch, app, p, hx, hy + 1, lane);
-            ox = parabola(l, ncc, r);
-            oy = parabola(u, ncc, d);
-        }
-        if (lane == 0) {
-            vtg_found f;
-            f.hx = hx;
-            f.hy = hy;
-            f.ncc = ncc;
-            f.second = second;
-            f.ox = ox;
-            f.oy = oy;
-            f.ntop = n;
-            f.cells = p.ccols * p.crows;
-            *out = f;
-        }
+        vtg_found f;
+        f.hx = hx;
+        f.hy = hy;
+        f.ncc = ncc;
+        f.second = second;
+        f.ox = n > 0 ? parabola(s_side[0], ncc, s_side[1]) : 0.0f;
+        f.oy = n > 0 ? parabola(s_side[2], ncc, s_side[3]) : 0.0f;
+        f.ntop = n;
+        f.cells = p.ccols * p.crows;
+        *out = f;
     }
-    (void)s_side;
 }
 
 /* ---- corners one by one (tk_correlate): one warp per corner ---- */
@@ -414,7 +478,7 @@ static cudaError_t launch_all(const T *plane, int pitch, const float *app, const
                               int map_kind, vtg_found *out, cudaStream_t st)
 {
     integral_rows<T><<<(p.h + 1 + 7) / 8, 256, 0, st>>>(plane, pitch, p.w, p.h, s.S1, s.S2, s.tp);
-    integral_cols<<<(p.w + 1 + 255) / 256, 256, 0, st>>>(p.w, p.h, s.S1, s.S2, s.tp);
+    integral_cols<<<(p.w + 1 + IC_COLS - 1) / IC_COLS, IC_COLS * IC_SEGS, 0, st>>>(p.w, p.h, s.S1, s.S2, s.tp);
     const int cells = p.ccols * p.crows;
     cudaError_t e = cudaSuccess;
     if (map_kind == VTG_NCC_F32) {
@@ -429,7 +493,10 @@ static cudaError_t launch_all(const T *plane, int pitch, const float *app, const
             return e;
     }
     ncc_top<<<1, 256, 0, st>>>(s.map_v, cells, s.top, s.ntop);
-    ncc_refine<T><<<1, NCC_TOP * 32, 0, st>>>(plane, pitch, app, p, s.map_v, s.map_x, s.map_y, s.top, s.ntop, out);
+    const int around = p.step > 1 ? 2 * p.step - 1 : 1, side = 2 * around + 1;
+    const int warps = NCC_TOP * side * side;
+    ncc_half_all<T><<<(warps + 7) / 8, 256, 0, st>>>(plane, pitch, app, p, s.map_x, s.map_y, s.top, s.ntop, s.half);
+    ncc_pick<T><<<1, 128, 0, st>>>(plane, pitch, app, p, s.map_x, s.map_y, s.top, s.ntop, s.half, out);
     return cudaGetLastError();
 }
 

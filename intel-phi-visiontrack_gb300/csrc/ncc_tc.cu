@@ -1,41 +1,50 @@
 /* ncc_tc.cu -- the correlation map on the 5th-generation tensor cores: tcgen05.mma (kind::f16, BF16 or FP16 products,
- * F32 accumulation in tensor memory), operands from shared memory through matrix descriptors, the accumulator read back
- * with tcgen05.ld, scored against exact int64 window sums and reduced to the per-cell map in the epilogue.
+ * F32 accumulation in tensor memory), operands brought into shared memory by asynchronous bulk copies and read through
+ * matrix descriptors, the accumulator read back with tcgen05.ld, scored with exact int64 window sums and reduced to the
+ * per-cell map in the epilogue.
  *
- * The correlation as a GEMM. A CTA owns a tile of corners: 1024 consecutive x (X0 + 8 m + s, m < 128, s < 8) by 16
- * consecutive y (Y0 + q). Then
+ * The correlation as a GEMM. A CTA owns a tile of corners: 1024 consecutive x (X0 + 8 m + s, m < 128, s < 8) by 8
+ * consecutive y (Y0 + q, q < 8). Then
  *     st(X0 + 8 m + s, Y0 + q) = sum over image rows r, columns c of  A_r[m][c] * B_r[(q, s)][c]
- * with A_r[m][c] = J[r][X0 + 8 m + c] and B_r[(q, s)][c] = t[r - Y0 - q][c - s] (zero outside the template). So D =
- * sum_r A_r B_r^T: M = 128, N = 8 x 16 = 128, K = the image rows of the tile's band times K_row = T_w + 8 rounded up
- * to 16.
+ * with A_r[m][c] = J[r][X0 + 8 m + c] and B_r[(q, s)][c] = t[r - Y0 - q][c - s] (zero outside the template): D =
+ * sum_r A_r B_r^T with M = 128, N = 8 x 8 = 64, and K = the tile's 8 + T_h - 1 image rows times K_row = T_w + 8
+ * rounded up to 16.
  *   A needs no im2col. Consecutive rows of A_r start 8 elements (16 bytes) apart in the image row, so a K-major,
- *   no-swizzle descriptor with 16-byte rows in a core matrix, a 16-byte leading (K) offset and a 128-byte stride (M)
- *   offset reads A_r straight from the row staged once in shared memory: address(m, k) = row + 2 (8 m + k).
- *   B_r depends only on r - Y0, so the band (16 + T_h - 1 blocks of 128 x K_row) is built once per template, already in
- *   the canonical core-matrix layout, and streamed from L2 into shared memory per image row.
- * The epilogue: each of the 128 threads owns one accumulator row (8 x-corners, 16 y-corners): it subtracts
- * J(x, y) sum t (the reference's st is relative to the corner's first pixel), forms the score with the exact int64
- * window sums, keeps its best per cell, and pairs with its neighbour lane (two rows = one 16 x 16 cell).
- *
- * The pipeline has three shared-memory stages: all threads stage row r (bytes to BF16/FP16) and its band block, fence
- * them to the async proxy, and one thread issues the MMAs and commits them to the stage's mbarrier, which the stage's
- * next filling waits for. Every wait is bounded: past the limit the kernel records an error word and stops issuing. */
+ *   no-swizzle descriptor with 16-byte core-matrix rows, a 16-byte leading (K) offset and a 128-byte stride (M) offset
+ *   reads A_r straight from the row: address(m, k) = row + 2 (8 m + k). The picture is converted to 16 bits once per
+ *   search (ncc_conv), shifted so that every tile's row segment starts on a 16-byte boundary.
+ *   B_r depends only on r - Y0: the band (8 + T_h - 1 blocks of 64 x K_row) is built once per template in the canonical
+ *   core-matrix layout.
+ * Pipeline: one thread drives it. Six shared-memory stages, each an image-row segment and a band block, arrive by
+ * cp.async.bulk on a "full" mbarrier (expected bytes); the MMAs of a stage commit to its "empty" mbarrier, which its
+ * next filling waits for, so copies run several stages ahead of the tensor core. Every wait is bounded by the global
+ * timer; past it the kernel records an error word.
+ * Epilogue: each of the 128 threads owns one accumulator row (8 x-corners by 8 y-corners). Per corner: st = acc -
+ * J(x, y) sum t' (the reference's st is relative to the corner's first pixel), times the corner's factor 1 / sqrt(norm
+ * var) from ncc_prep (0 for a near-blank window: the exact int64 rule), the best per 16 x 16 cell by value then scan
+ * order, merged across tiles by a 64-bit atomicMax on (ordered score, inverted scan index). */
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
 #include "vtg_ncc.cuh"
 
 #define TC_M 128
-#define TC_Q 16
+#define TC_Q 8
 #define TC_N (8 * TC_Q)
 #define TC_XS (8 * TC_M) /* x-corners of a tile */
-#define TC_STAGES 3
-#define TC_TMEM_COLS 128
+#define TC_STAGES 6
+#define TC_TMEM_COLS 64
 #define TC_WAIT_NS 2000000000ull /* a wait gives up after 2 s of the global timer */
+#define TC_MAX_KROW 144          /* T_w <= 128 */
 
 static inline int tc_krow(int tw) { return ((tw + 8 + 15) / 16) * 16; }
 
 size_t vtg_ncc_band_bytes(int tw, int th) { return (size_t)(TC_Q + th - 1) * TC_N * tc_krow(tw) * sizeof(uint16_t); }
+
+/* The 16-bit picture: rows up to h + TC_Q + T_h (zeros past the picture), TC_XS-aligned tiles plus the last K row. */
+static inline int conv_pitch(int w) { return ((w + TC_XS - 1) / TC_XS) * TC_XS + TC_MAX_KROW; }
+
+size_t vtg_ncc_conv_elems(int max_w, int max_h, int max_th) { return (size_t)conv_pitch(max_w) * (size_t)(max_h + TC_Q + max_th); }
 
 /* ---- the band ---- */
 
@@ -96,6 +105,43 @@ cudaError_t vtg_launch_ncc_band(const float *app, int tw, int th, int kind, uint
     return cudaGetLastError();
 }
 
+/* ---- per-search preparation ---- */
+
+/* conv[r][i] = 16-bit J[r][x0 + i] (zero past the picture), for rows 0 .. rows - 1 and columns 0 .. cpitch - 1. */
+template <int KIND>
+__global__ void ncc_conv(const uint8_t *__restrict__ plane, int pitch, int w, int h, int x0, int rows, int cpitch,
+                         uint16_t *__restrict__ conv)
+{
+    const size_t total = (size_t)rows * cpitch;
+    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total; idx += (size_t)gridDim.x * blockDim.x) {
+        const int r = (int)(idx / cpitch), i = (int)(idx - (size_t)r * cpitch);
+        const int x = x0 + i;
+        const float v = (r < h && x < w) ? (float)__ldg(plane + (size_t)r * pitch + x) : 0.0f;
+        conv[idx] = to16(v, KIND);
+    }
+}
+
+/* fac[(y - y0) fw + (x - x0)] = 1 / sqrt(norm var) from the exact int64 window sums; 0 for a near-blank window
+ * (n var <= n norm / 16) or norm <= 0 -- the reference's rule (src/kern/track.c:203-205) on exact integers. */
+__global__ void ncc_prep(NccPrm p, const long long *__restrict__ S1, const long long *__restrict__ S2, int tp, int fw,
+                         float *__restrict__ fac)
+{
+    const int fh = p.y1 - p.y0 + 1;
+    const size_t total = (size_t)fw * fh;
+    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total; idx += (size_t)gridDim.x * blockDim.x) {
+        const int y = p.y0 + (int)(idx / fw), x = p.x0 + (int)(idx % fw);
+        const long long *a = S1 + (size_t)y * tp + x, *b = S1 + (size_t)(y + p.th) * tp + x;
+        const long long s1 = b[p.tw] - b[0] - a[p.tw] + a[0];
+        const long long *c = S2 + (size_t)y * tp + x, *d = S2 + (size_t)(y + p.th) * tp + x;
+        const long long s2 = d[p.tw] - d[0] - c[p.tw] + c[0];
+        const long long nvar = (long long)p.n * s2 - s1 * s1;
+        float f = 0.0f;
+        if (!((double)nvar <= (double)p.n * (double)p.norm * 0.0625 || p.norm <= 0.0f))
+            f = 1.0f / sqrtf(p.norm * ((float)nvar / (float)p.n));
+        fac[idx] = f;
+    }
+}
+
 /* ---- PTX helpers ---- */
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -137,6 +183,19 @@ __device__ __forceinline__ bool mbar_wait(uint32_t a, uint32_t parity)
     }
 }
 
+/* Arms a stage's full barrier for `bytes` and brings its two operands in by bulk copy. */
+__device__ __forceinline__ void tc_fill(uint32_t mbar, uint32_t dst_a, const void *src_a, uint32_t bytes_a, uint32_t dst_b,
+                                        const void *src_b, uint32_t bytes_b)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes_a + bytes_b) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst_a),
+                 "l"(src_a), "r"(bytes_a), "r"(mbar)
+                 : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst_b),
+                 "l"(src_b), "r"(bytes_b), "r"(mbar)
+                 : "memory");
+}
+
 __device__ __forceinline__ void tc_mma(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accumulate)
 {
     asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %4, 0;\n\ttcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(
@@ -167,15 +226,15 @@ __device__ __forceinline__ void tc_ld32(uint32_t taddr, float (&v)[32])
         v[i] = __uint_as_float(r[i]);
 }
 
-/* ---- the map ---- */
-
-__device__ __forceinline__ long long tbox(const long long *S, int tp, int x, int y, int tw, int th)
+/* A cell's candidate as one orderable word: higher score first, then the earlier corner in scan order. 0: none. */
+__device__ __forceinline__ unsigned long long cell_word(float v, int key)
 {
-    const long long *a = S + (size_t)y * tp + x, *b = S + (size_t)(y + th) * tp + x;
-    return b[tw] - b[0] - a[tw] + a[0];
+    unsigned u = __float_as_uint(v);
+    u = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+    return ((unsigned long long)u << 32) | (unsigned long long)(0xFFFFFFFFu - (unsigned)key);
 }
 
-__device__ __forceinline__ bool tbetter(float v, int k, float bv, int bk) { return v > bv || (v == bv && k < bk); }
+/* ---- the map ---- */
 
 struct TcSmem {
     uint32_t a_bytes, b_bytes, stage_bytes, total;
@@ -184,12 +243,10 @@ struct TcSmem {
 static TcSmem tc_smem(int krow)
 {
     TcSmem s;
-    s.a_bytes = (uint32_t)((((TC_XS + krow) * 2) + 127) & ~127);
+    s.a_bytes = (uint32_t)(((TC_XS + krow) * 2 + 127) & ~127);
     s.b_bytes = (uint32_t)(TC_N * krow * 2);
     s.stage_bytes = s.a_bytes + s.b_bytes;
-    s.total = TC_STAGES * s.stage_bytes + 128; /* + mbarriers and the tensor-memory address */
-    if (s.total < 64 * 1024)
-        s.total = 64 * 1024; /* at most three CTAs an SM: 3 x 128 tensor-memory columns fit its 512 */
+    s.total = TC_STAGES * s.stage_bytes + 256; /* + mbarriers and the tensor-memory address */
     return s;
 }
 
@@ -197,9 +254,9 @@ template <int KIND>
 __global__ void __launch_bounds__(128, 1) ncc_map_tc(const uint8_t *__restrict__ plane, int pitch, NccPrm p,
                                                      const uint16_t *__restrict__ band, int krow, int tiles_x,
                                                      uint32_t a_bytes, uint32_t stage_bytes,
-                                                     const long long *__restrict__ S1, const long long *__restrict__ S2,
-                                                     int tp, float *__restrict__ map_v, int *__restrict__ map_x,
-                                                     int *__restrict__ map_y, int *__restrict__ err)
+                                                     const uint16_t *__restrict__ conv, int cpitch,
+                                                     const float *__restrict__ fac, int fw,
+                                                     unsigned long long *__restrict__ cellw, int *__restrict__ err)
 {
     extern __shared__ __align__(1024) uint8_t smem[];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -208,12 +265,15 @@ __global__ void __launch_bounds__(128, 1) ncc_map_tc(const uint8_t *__restrict__
     const int nk = TC_Q + p.th - 1;
     const int kchunks = krow / 16;
     uint8_t *ctl = smem + TC_STAGES * stage_bytes;
-    const uint32_t mbar0 = smem_u32(ctl);
-    uint32_t *tmem_slot = (uint32_t *)(ctl + 64);
+    const uint32_t full0 = smem_u32(ctl), empty0 = full0 + 8 * TC_STAGES;
+    uint32_t *tmem_slot = (uint32_t *)(ctl + 16 * TC_STAGES);
+    const uint32_t a_copy = (uint32_t)((TC_XS + krow) * 2), b_copy = (uint32_t)(TC_N * krow * 2);
 
     if (tid == 0) {
-        for (int s = 0; s < TC_STAGES; s++)
-            mbar_init(mbar0 + 8 * s, 1);
+        for (int s = 0; s < TC_STAGES; s++) {
+            mbar_init(full0 + 8 * s, 1);
+            mbar_init(empty0 + 8 * s, 1);
+        }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
@@ -230,52 +290,48 @@ __global__ void __launch_bounds__(128, 1) ncc_map_tc(const uint8_t *__restrict__
     const int fmt = KIND == VTG_NCC_BF16 ? 1 : 0;
     const uint32_t idesc = (1u << 4) | ((uint32_t)fmt << 7) | ((uint32_t)fmt << 10) | ((uint32_t)(TC_N >> 3) << 17) |
                            ((uint32_t)(TC_M >> 4) << 24);
-    const int row_elems = TC_XS + krow;
-    bool ok = true;
-
-    for (int k = 0; k < nk; k++) {
-        const int s = k % TC_STAGES;
-        uint8_t *sa = smem + s * stage_bytes, *sb = sa + a_bytes;
-        /* the stage's previous MMAs must be done before it is refilled: thread 0 waits, the block agrees */
-        int good = 1;
-        if (k >= TC_STAGES && tid == 0)
-            good = mbar_wait(mbar0 + 8 * s, (uint32_t)((k / TC_STAGES - 1) & 1)) ? 1 : 0;
-        if (!__syncthreads_and(good)) {
-            ok = false;
-            break;
+    int good = 1;
+    if (tid == 0) {
+        /* conv row r holds picture row r from column p.x0 on: this tile's segment starts at column tx * TC_XS */
+        const uint16_t *arow = conv + (size_t)Y0 * cpitch + (size_t)tx * TC_XS;
+        const int pre = nk < TC_STAGES ? nk : TC_STAGES;
+        for (int k = 0; k < pre; k++) {
+            uint8_t *sa = smem + k * stage_bytes;
+            tc_fill(full0 + 8 * k, smem_u32(sa), arow + (size_t)k * cpitch, a_copy, smem_u32(sa + a_bytes),
+                    band + (size_t)k * TC_N * krow, b_copy);
         }
-        /* row Y0 + k of the picture, X0 .. X0 + row_elems - 1, to 16-bit (zero past the picture) */
-        const int r = Y0 + k;
-        uint16_t *a16 = (uint16_t *)sa;
-        for (int e = tid; e < row_elems; e += 128) {
-            const int x = X0 + e;
-            const float v = (r < p.h && x < p.w) ? (float)__ldg(plane + (size_t)r * pitch + x) : 0.0f;
-            a16[e] = to16(v, KIND);
-        }
-        /* the band block for this row */
-        const uint4 *src = (const uint4 *)(band + (size_t)k * TC_N * krow);
-        uint4 *dst = (uint4 *)sb;
-        const int vec = TC_N * krow * 2 / 16;
-        for (int i = tid; i < vec; i += 128)
-            dst[i] = __ldg(src + i);
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncthreads();
-        if (tid == 0) {
+        for (int k = 0; k < nk && good; k++) {
+            const int s = k % TC_STAGES;
+            if (!mbar_wait(full0 + 8 * s, (uint32_t)((k / TC_STAGES) & 1))) {
+                good = 0;
+                break;
+            }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t a0 = smem_u32(sa), b0 = smem_u32(sb);
+            const uint32_t a0 = smem_u32(smem + s * stage_bytes), b0 = a0 + a_bytes;
             for (int kc = 0; kc < kchunks; kc++) {
                 const uint64_t ad = mdesc(a0 + 32 * kc, 16, 128);
                 const uint64_t bd = mdesc(b0 + kc * 2 * (TC_N / 8) * 128, (TC_N / 8) * 128, 128);
                 tc_mma(tmem, ad, bd, idesc, (k | kc) != 0);
             }
-            tc_commit(mbar0 + 8 * s);
+            tc_commit(empty0 + 8 * s);
+            /* refill the stage whose MMAs were issued last round with the stage TC_STAGES - 1 ahead of this one */
+            const int kr = k - 1 + TC_STAGES;
+            if (k >= 1 && kr < nk) {
+                const int sp = (k - 1) % TC_STAGES;
+                if (!mbar_wait(empty0 + 8 * sp, (uint32_t)(((k - 1) / TC_STAGES) & 1))) {
+                    good = 0;
+                    break;
+                }
+                uint8_t *sa = smem + sp * stage_bytes;
+                tc_fill(full0 + 8 * sp, smem_u32(sa), arow + (size_t)kr * cpitch, a_copy, smem_u32(sa + a_bytes),
+                        band + (size_t)kr * TC_N * krow, b_copy);
+            }
         }
-    }
-    /* the last commit covers every MMA thread 0 issued */
-    int good = ok ? 1 : 0;
-    if (ok && tid == 0) {
-        const int last = nk - 1;
-        good = mbar_wait(mbar0 + 8 * (last % TC_STAGES), (uint32_t)((last / TC_STAGES) & 1)) ? 1 : 0;
+        /* the last commit covers every MMA */
+        if (good) {
+            const int last = nk - 1;
+            good = mbar_wait(empty0 + 8 * (last % TC_STAGES), (uint32_t)((last / TC_STAGES) & 1)) ? 1 : 0;
+        }
     }
     const int ok_all = __syncthreads_and(good);
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -283,9 +339,10 @@ __global__ void __launch_bounds__(128, 1) ncc_map_tc(const uint8_t *__restrict__
         if (tid == 0)
             atomicExch(err, 1);
     } else {
-        /* epilogue: thread m owns accumulator row m */
+        /* epilogue: thread m owns accumulator row m: corners X0 + 8 m + s, Y0 + q */
         const int m = warp * 32 + lane;
         const int per = NCC_CELL / p.step;
+        const int ly0 = (ty & 1) * TC_Q; /* this tile's first row inside its cell row */
         float best = -2.0f;
         int bkey = 1 << 30;
 #pragma unroll 1
@@ -299,36 +356,24 @@ __global__ void __launch_bounds__(128, 1) ncc_map_tc(const uint8_t *__restrict__
                 if (x > p.x1 || y > p.y1 || ((x - p.x0) % p.step) || ((y - p.y0) % p.step))
                     continue;
                 const float j0 = (float)__ldg(plane + (size_t)y * pitch + x);
-                const float st = v[j] - j0 * p.sum_t;
-                const long long s1 = tbox(S1, tp, x, y, p.tw, p.th), s2 = tbox(S2, tp, x, y, p.tw, p.th);
-                const long long nvar = (long long)p.n * s2 - s1 * s1;
-                float score;
-                if ((double)nvar <= (double)p.n * (double)p.norm * 0.0625 || p.norm <= 0.0f)
-                    score = 0.0f;
-                else
-                    score = st / sqrtf(p.norm * ((float)nvar / (float)p.n));
-                const int key = (q / p.step) * per + ((8 * (m & 1) + s) / p.step);
-                if (tbetter(score, key, best, bkey)) {
+                const float f = __ldg(fac + (size_t)(y - p.y0) * fw + (x - p.x0));
+                const float score = (v[j] - j0 * p.sum_t) * f;
+                const int key = ((ly0 + q) / p.step) * per + ((8 * (m & 1) + s) / p.step);
+                if (score > best || (score == best && key < bkey)) {
                     best = score;
                     bkey = key;
                 }
             }
         }
         const float ob = __shfl_xor_sync(VTG_FULL, best, 1);
-        const int ok2 = __shfl_xor_sync(VTG_FULL, bkey, 1);
-        if (tbetter(ob, ok2, best, bkey)) {
+        const int okey = __shfl_xor_sync(VTG_FULL, bkey, 1);
+        if (ob > best || (ob == best && okey < bkey)) {
             best = ob;
-            bkey = ok2;
+            bkey = okey;
         }
-        const int ccol = tx * (TC_XS / NCC_CELL) + (m >> 1);
-        if ((m & 1) == 0 && ccol < p.ccols && ty < p.crows) {
-            const int cell = ty * p.ccols + ccol;
-            const int cx0 = p.x0 + ccol * NCC_CELL, cy0 = p.y0 + ty * NCC_CELL;
-            const bool fired = bkey < (1 << 30) && best > -2.0f;
-            map_v[cell] = fired ? best : -2.0f;
-            map_x[cell] = fired ? cx0 + (bkey % per) * p.step : cx0;
-            map_y[cell] = fired ? cy0 + (bkey / per) * p.step : cy0;
-        }
+        const int ccol = tx * (TC_XS / NCC_CELL) + (m >> 1), crow = (Y0 - p.y0) / NCC_CELL;
+        if ((m & 1) == 0 && ccol < p.ccols && crow < p.crows && bkey < (1 << 30))
+            atomicMax(cellw + (size_t)crow * p.ccols + ccol, cell_word(best, bkey));
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
@@ -338,29 +383,71 @@ __global__ void __launch_bounds__(128, 1) ncc_map_tc(const uint8_t *__restrict__
     }
 }
 
+/* The map from the cells' words: value and corner, or -2 and the cell's origin where no corner was scored. */
+__global__ void ncc_cells_out(NccPrm p, const unsigned long long *__restrict__ cellw, float *__restrict__ map_v,
+                              int *__restrict__ map_x, int *__restrict__ map_y)
+{
+    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+    if (cell >= p.ccols * p.crows)
+        return;
+    const int cx0 = p.x0 + (cell % p.ccols) * NCC_CELL, cy0 = p.y0 + (cell / p.ccols) * NCC_CELL;
+    const unsigned long long w = cellw[cell];
+    const int per = NCC_CELL / p.step;
+    if (w == 0ull) {
+        map_v[cell] = -2.0f;
+        map_x[cell] = cx0;
+        map_y[cell] = cy0;
+        return;
+    }
+    unsigned u = (unsigned)(w >> 32);
+    u = (u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u;
+    const int key = (int)(0xFFFFFFFFu - (unsigned)(w & 0xFFFFFFFFull));
+    map_v[cell] = __uint_as_float(u);
+    map_x[cell] = cx0 + (key % per) * p.step;
+    map_y[cell] = cy0 + (key / per) * p.step;
+}
+
 cudaError_t vtg_launch_ncc_map_tc(const void *plane, int pitch, int elem_bytes, const NccPrm &p, const NccScratch &s,
                                   int kind, cudaStream_t st)
 {
-    if (elem_bytes != 1 || !s.band || (kind != VTG_NCC_BF16 && kind != VTG_NCC_FP16))
+    if (elem_bytes != 1 || !s.band || !s.conv || !s.fac || !s.cellw || (kind != VTG_NCC_BF16 && kind != VTG_NCC_FP16) ||
+        p.tw > 128)
         return cudaErrorInvalidValue;
     const int krow = tc_krow(p.tw);
     const TcSmem sm = tc_smem(krow);
-    const int tiles_x = (p.x1 - p.x0 + 1 + TC_XS - 1) / TC_XS, tiles_y = (p.y1 - p.y0 + 1 + TC_Q - 1) / TC_Q;
-    cudaError_t e;
+    const int fw = p.x1 - p.x0 + 1, fh = p.y1 - p.y0 + 1;
+    const int tiles_x = (fw + TC_XS - 1) / TC_XS, tiles_y = (fh + TC_Q - 1) / TC_Q;
+    const int cpitch = tiles_x * TC_XS + TC_MAX_KROW;
+    const int rows = p.y0 + tiles_y * TC_Q + p.th; /* every row a tile's band reads */
+    if ((size_t)cpitch * rows > s.conv_elems || (size_t)fw * fh > s.fac_elems)
+        return cudaErrorInvalidValue;
+    const int cells = p.ccols * p.crows;
+    cudaError_t e = cudaMemsetAsync(s.cellw, 0, sizeof(unsigned long long) * (size_t)cells, st);
+    if (e != cudaSuccess)
+        return e;
+    const size_t conv_total = (size_t)cpitch * rows;
+    const int cblocks = (int)((conv_total + 255) / 256 < 8192 ? (conv_total + 255) / 256 : 8192);
+    if (kind == VTG_NCC_BF16)
+        ncc_conv<VTG_NCC_BF16><<<cblocks, 256, 0, st>>>((const uint8_t *)plane, pitch, p.w, p.h, p.x0, rows, cpitch, s.conv);
+    else
+        ncc_conv<VTG_NCC_FP16><<<cblocks, 256, 0, st>>>((const uint8_t *)plane, pitch, p.w, p.h, p.x0, rows, cpitch, s.conv);
+    const size_t ftotal = (size_t)fw * fh;
+    ncc_prep<<<(int)((ftotal + 255) / 256 < 8192 ? (ftotal + 255) / 256 : 8192), 256, 0, st>>>(p, s.S1, s.S2, s.tp, fw, s.fac);
     if (kind == VTG_NCC_BF16) {
         e = cudaFuncSetAttribute(ncc_map_tc<VTG_NCC_BF16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm.total);
         if (e != cudaSuccess)
             return e;
         ncc_map_tc<VTG_NCC_BF16><<<tiles_x * tiles_y, 128, sm.total, st>>>(
-            (const uint8_t *)plane, pitch, p, s.band, krow, tiles_x, sm.a_bytes, sm.stage_bytes, s.S1, s.S2, s.tp,
-            s.map_v, s.map_x, s.map_y, s.err);
+            (const uint8_t *)plane, pitch, p, s.band, krow, tiles_x, sm.a_bytes, sm.stage_bytes, s.conv, cpitch, s.fac, fw,
+            s.cellw, s.err);
     } else {
         e = cudaFuncSetAttribute(ncc_map_tc<VTG_NCC_FP16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm.total);
         if (e != cudaSuccess)
             return e;
         ncc_map_tc<VTG_NCC_FP16><<<tiles_x * tiles_y, 128, sm.total, st>>>(
-            (const uint8_t *)plane, pitch, p, s.band, krow, tiles_x, sm.a_bytes, sm.stage_bytes, s.S1, s.S2, s.tp,
-            s.map_v, s.map_x, s.map_y, s.err);
+            (const uint8_t *)plane, pitch, p, s.band, krow, tiles_x, sm.a_bytes, sm.stage_bytes, s.conv, cpitch, s.fac, fw,
+            s.cellw, s.err);
     }
+    ncc_cells_out<<<(cells + 255) / 256, 256, 0, st>>>(p, s.cellw, s.map_v, s.map_x, s.map_y);
     return cudaGetLastError();
 }

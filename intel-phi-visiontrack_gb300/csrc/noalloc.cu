@@ -11,8 +11,9 @@
  * What that costs and what it limits:
  *   - VTG_NOALLOC_SCRATCH_BYTES (5 MiB) of device memory on every GPU that loads this library, held until the process
  *     exits, whether or not the entry point is ever called;
- *   - planes with (w + 1) (h + 1) <= VTG_NOALLOC_MAX_PIXELS (320,000: 640 x 480 fits) and templates up to 64 x 64, F32 map
- *     only; larger requests are refused with VTG_EINVAL, before anything runs;
+ *   - planes with (w + 1) (h + 1) <= VTG_NOALLOC_MAX_PIXELS (320,000: 640 x 480 fits), templates up to 64 x 64, steps up
+ *     to 4 (the reference searches at 1 and 2), F32 map only; larger requests are refused with VTG_EINVAL, before
+ *     anything runs;
  *   - every call shares the one array, so calls whose work overlaps on the GPU (different streams, or different host
  *     threads) race and corrupt each other's results: order them on one stream, or serialize them;
  *   - the first call on a device looks the array's device address up (cudaGetSymbolAddress, once per device, with that
@@ -29,8 +30,12 @@
 /* The scratch: two integral images of VTG_NOALLOC_MAX_PIXELS int64 each, then the map and the candidates. */
 static __device__ __align__(256) unsigned char g_noalloc_scratch[VTG_NOALLOC_SCRATCH_BYTES];
 
+#define VTG_NOALLOC_MAX_STEP 4
+#define VTG_NOALLOC_HALF (NCC_TOP * (4 * VTG_NOALLOC_MAX_STEP - 1) * (4 * VTG_NOALLOC_MAX_STEP - 1))
+
 static_assert(2 * sizeof(long long) * (size_t)VTG_NOALLOC_MAX_PIXELS +
-                      (size_t)VTG_NOALLOC_MAX_CELLS * (sizeof(float) + 2 * sizeof(int)) + 256 <=
+                      (size_t)VTG_NOALLOC_MAX_CELLS * (sizeof(float) + 2 * sizeof(int)) + 256 +
+                      sizeof(float) * VTG_NOALLOC_HALF <=
                   VTG_NOALLOC_SCRATCH_BYTES,
               "the scratch array holds the largest search it accepts");
 
@@ -68,7 +73,8 @@ extern "C" int vtg_search_run_noalloc(const void *plane, int w, int h, int pitch
         return VTG_EINVAL;
     if (tw < 8 || th < 1 || (tw % 8) || tw > VTG_NOALLOC_MAX_T || th > VTG_NOALLOC_MAX_T || !(norm >= 0.0f))
         return VTG_EINVAL;
-    if ((long long)(w + 1) * (long long)(h + 1) > VTG_NOALLOC_MAX_PIXELS || step < 1 || step > 16 || (NCC_CELL % step))
+    if ((long long)(w + 1) * (long long)(h + 1) > VTG_NOALLOC_MAX_PIXELS || step < 1 || step > VTG_NOALLOC_MAX_STEP ||
+        (NCC_CELL % step))
         return VTG_EINVAL;
     NccPrm p;
     p.w = w;
@@ -119,6 +125,12 @@ extern "C" int vtg_search_run_noalloc(const void *plane, int w, int h, int pitch
     s.band = nullptr;
     s.band_rows = s.krow = 0;
     s.err = s.ntop + 1;
+    s.half = (float *)(rest + sizeof(float) * VTG_NOALLOC_MAX_CELLS + 2 * sizeof(int) * VTG_NOALLOC_MAX_CELLS + 256);
+    s.conv = nullptr; /* the F32 map needs none of the tensor-core map's scratch */
+    s.conv_elems = 0;
+    s.fac = nullptr;
+    s.fac_elems = 0;
+    s.cellw = nullptr;
     e = vtg_launch_ncc(plane, pitch, plane_type, app, p, s, VTG_NCC_F32, found, st);
     const size_t cells = (size_t)p.ccols * p.crows;
     if (e == cudaSuccess && map_v)

@@ -6,6 +6,7 @@
 
 #define NCC_CELL 16 /* SEARCH_CELL, src/kern/track.c:61: corners to a cell of the map */
 #define NCC_TOP 8   /* SEARCH_TOP, src/kern/track.c:62: cells looked at again in half pixels */
+#define NCC_HALF_MAX (NCC_TOP * 63 * 63) /* half-pixel scores of the candidates at the largest step (16) */
 
 /* One search: the plane, the template and the clamped window of corners. */
 struct NccPrm {
@@ -24,10 +25,21 @@ struct NccScratch {
     float *map_v;
     int *map_x, *map_y;
     int *top, *ntop;
+    float *half;          /* the candidates' half-pixel scores: NCC_TOP x (2 around + 1)^2, around <= 2 x 16 - 1 */
     const uint16_t *band; /* the template band for the tensor-core map (ncc_tc.cu), NULL if unset */
     int band_rows, krow;  /* image rows of a tile's band (NCC_TC_Q + th - 1), K per image row */
     int *err;             /* device status word: nonzero when a bounded wait gave up */
+    /* the tensor-core map's own scratch: the 16-bit picture (shifted so a tile's row starts 16-byte aligned), each
+     * corner's normalisation factor, and one 64-bit (score, corner) word per cell */
+    uint16_t *conv;
+    size_t conv_elems;
+    float *fac;
+    size_t fac_elems;
+    unsigned long long *cellw;
 };
+
+/* Elements of the tensor-core map's scratch for planes up to max_w x max_h and templates up to max_tw x max_th. */
+size_t vtg_ncc_conv_elems(int max_w, int max_h, int max_th);
 
 cudaError_t vtg_launch_ncc(const void *plane, int pitch, int plane_type, const float *app, const NccPrm &p,
                            const NccScratch &s, int map_kind, vtg_found *out, cudaStream_t st);
