@@ -341,11 +341,14 @@ extern "C" int vtg_batch_set_tune(vtg_batch *b, const struct vtg_tune *t)
     if (!b || !t || (t->block_warps != 4 && t->block_warps != 8 && t->block_warps != 16) || t->chunk < 1 ||
         t->chunk > 64 || t->ctas_per_sm < 1 || t->ctas_per_sm > 8)
         return VTG_EINVAL;
+    if (t->tsmem && (!t->persistent || t->block_warps == 16 || t->ctas_per_sm > (t->block_warps == 4 ? 5 : 3)))
+        return VTG_EINVAL;
     std::lock_guard<std::mutex> g(b->mu);
     b->tune.block_warps = t->block_warps;
     b->tune.chunk = t->chunk;
     b->tune.persistent = t->persistent ? 1 : 0;
     b->tune.ctas_per_sm = t->ctas_per_sm;
+    b->tune.tsmem = t->tsmem ? 1 : 0;
     return VTG_OK;
 }
 
@@ -357,6 +360,7 @@ extern "C" int vtg_batch_get_tune(const vtg_batch *b, struct vtg_tune *t)
     t->chunk = b->tune.chunk;
     t->persistent = b->tune.persistent;
     t->ctas_per_sm = b->tune.ctas_per_sm;
+    t->tsmem = b->tune.tsmem;
     return VTG_OK;
 }
 
@@ -400,6 +404,11 @@ extern "C" int vtg_batch_autotune(vtg_batch *b, int slot, int reps, struct vtg_t
                     cands.push_back({warps, chunk, 0, 1});
                 }
             }
+    /* the template's intensities in shared memory: 20 or 24 warps an SM */
+    for (int chunk : {1, 2, 4}) {
+        cands.push_back({4, chunk, 1, 5, 1});
+        cands.push_back({8, chunk, 1, 3, 1});
+    }
     cudaEvent_t e0, e1;
     CU(cudaEventCreate(&e0));
     CU(cudaEventCreate(&e1));
@@ -452,6 +461,7 @@ extern "C" int vtg_batch_autotune(vtg_batch *b, int slot, int reps, struct vtg_t
         best->chunk = best_c.chunk;
         best->persistent = best_c.persistent;
         best->ctas_per_sm = best_c.ctas_per_sm;
+        best->tsmem = best_c.tsmem;
     }
     if (best_ms)
         *best_ms = best_t;

@@ -23,10 +23,89 @@
 #define LK_GRAD_SCALE (1.0f / 512.0f)
 #define LK_Q6_INV (1.0f / 64.0f)
 
-template <int MAXH>
+/* Two floats in one 64-bit register (lo, hi), for the packed FP32 pair instructions (add/sub/mul/fma .f32x2): one
+ * instruction moves two independent row chains of a patch. Each half rounds like its scalar instruction. */
+typedef unsigned long long f2_t;
+
+__device__ __forceinline__ f2_t f2_pack(float lo, float hi)
+{
+    f2_t r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ void f2_split(f2_t v, float &lo, float &hi)
+{
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ float f2_hi(f2_t v)
+{
+    float lo, hi;
+    f2_split(v, lo, hi);
+    return hi;
+}
+__device__ __forceinline__ float f2_sum(f2_t v)
+{
+    float lo, hi;
+    f2_split(v, lo, hi);
+    return lo + hi;
+}
+__device__ __forceinline__ f2_t f2_add(f2_t a, f2_t b)
+{
+    f2_t d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2_t f2_sub(f2_t a, f2_t b)
+{
+    f2_t d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2_t f2_mul(f2_t a, f2_t b)
+{
+    f2_t d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2_t f2_fma(f2_t a, f2_t b, f2_t c)
+{
+    f2_t d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+/* |lo|, |hi|: both sign bits cleared */
+__device__ __forceinline__ f2_t f2_abs(f2_t v) { return v & 0x7fffffff7fffffffull; }
+
+/* The template of the current level, patch rows paired as (r, HH + r), HH = MAXH / 2, so the sample walks the top and
+ * bottom halves of the patch together; an odd MAXH's last row (2 HH) is kept apart. Tx, Ty are the unscaled Sobel sums
+ * (the 1/512 is applied to the folded sums, an exact power of two). T is in registers or, with TS, in this warp's
+ * rows of shared memory ([HH][32] pairs: a lane reads only what it wrote). */
+template <int MAXH, bool TS>
 struct Patch {
-    float t[MAXH], tx[MAXH], ty[MAXH];
+    static constexpr int HH = MAXH / 2;
+    f2_t tx[HH], ty[HH];
+    f2_t t[TS ? 1 : HH];
+    float txl, tyl, tl;
+    f2_t *ts;
 };
+
+template <int MAXH, bool TS>
+__device__ __forceinline__ void put_t(Patch<MAXH, TS> &P, int r, int lane, f2_t v)
+{
+    if constexpr (TS)
+        P.ts[r * 32 + lane] = v;
+    else
+        P.t[r] = v;
+}
+
+template <int MAXH, bool TS>
+__device__ __forceinline__ f2_t get_t(const Patch<MAXH, TS> &P, int r, int lane)
+{
+    if constexpr (TS)
+        return P.ts[r * 32 + lane];
+    else
+        return P.t[r];
+}
 
 __device__ __forceinline__ float warp_fold(float v)
 {
@@ -34,6 +113,19 @@ __device__ __forceinline__ float warp_fold(float v)
     for (int s = 1; s < 32; s <<= 1)
         v = v + __shfl_xor_sync(VTG_FULL, v, s);
     return v;
+}
+
+/* Two butterfly folds at once (the same partners, the same order of additions as warp_fold on each half). */
+__device__ __forceinline__ void warp_fold2(float &a, float &b)
+{
+    f2_t v = f2_pack(a, b);
+#pragma unroll
+    for (int s = 1; s < 32; s <<= 1) {
+        float lo, hi;
+        f2_split(v, lo, hi);
+        v = f2_add(v, f2_pack(__shfl_xor_sync(VTG_FULL, lo, s), __shfl_xor_sync(VTG_FULL, hi, s)));
+    }
+    f2_split(v, a, b);
 }
 
 /* The row's horizontal interpolation at this lane's column: l from this lane's load, n from the next lane's. Every lane
@@ -45,22 +137,38 @@ __device__ __forceinline__ float hlerp(const float *p, float fx)
     return __fmaf_rn(n - l, fx, l);
 }
 
-/* build: the window of I around pixel (ix + fx, iy + fy); T, Tx, Ty into the registers; the tensor's sums.
- * EXACT: the patch height is MAXH at compile time (no row guards). */
-template <int MAXH, bool EXACT>
-__device__ __forceinline__ void lk_build(const DevLevel &L, int ix, float fx, int iy, float fy, int W, int Hr, int lane,
-                                         Patch<MAXH> &P, float &gxx, float &gxy, float &gyy)
+/* hlerp of two rows at once, (row a, row b); FX = (fx, fx) */
+__device__ __forceinline__ f2_t hlerp2(const float *pa, const float *pb, f2_t FX)
 {
+    const float la = __ldg(pa), lb = __ldg(pb);
+    const f2_t l = f2_pack(la, lb);
+    const f2_t n = f2_pack(__shfl_down_sync(VTG_FULL, la, 1), __shfl_down_sync(VTG_FULL, lb, 1));
+    return f2_fma(f2_sub(n, l), FX, l);
+}
+
+/* build: the window of I around pixel (ix + fx, iy + fy); T, Tx, Ty into the patch; the tensor's sums.
+ * EXACT: the patch height is MAXH at compile time (no row guards); otherwise rows past H are zero in the patch. */
+template <int MAXH, bool EXACT, bool TS>
+__device__ __forceinline__ void lk_build(const DevLevel &L, int ix, float fx, int iy, float fy, int W, int Hr, int lane,
+                                         Patch<MAXH, TS> &P, float &gxx, float &gxy, float &gyy)
+{
+    constexpr int HH = MAXH / 2;
     const int H = EXACT ? MAXH : Hr;
     const int x0 = ix - W / 2, y0 = iy - H / 2;
     /* Lane c samples window column c - 1 (c = 0 .. W + 1; lane W + 2 feeds lane W + 1's right neighbour; the lanes past
-     * it read a clamped column and feed nothing). Patch columns are lanes 1 .. W: the gradient scale is 0 elsewhere. */
-    const float gs = (lane >= 1 && lane <= W) ? LK_GRAD_SCALE : 0.0f;
+     * it read a clamped column and feed nothing). Patch columns are lanes 1 .. W; the others' sums are dropped before
+     * the fold. */
+    const bool act = lane >= 1 && lane <= W;
     const float *row = L.p + (size_t)(y0 - 1) * L.pitch + (x0 - 1 + min(lane, W + 2));
     float prev = hlerp(row, fx);
     /* S rows r - 2, r - 1, r: values, and their x + 1 minus x - 1 differences (shared by three patch rows) */
     float u = 0.f, ul = 0.f, ur = 0.f, m = 0.f, ml = 0.f, mr = 0.f, mdx = 0.f, udx = 0.f;
     float sxx0 = 0.f, sxy0 = 0.f, syy0 = 0.f, sxx1 = 0.f, sxy1 = 0.f, syy1 = 0.f;
+    /* the top half's rows, held until their bottom-half partner is made */
+    float ht[HH], htx[HH], hty[HH];
+#pragma unroll
+    for (int k = 0; k < HH; k++)
+        ht[k] = htx[k] = hty[k] = 0.0f;
 #pragma unroll
     for (int r = 0; r < MAXH + 2; r++) {
         if (EXACT || r < H + 2) {
@@ -71,11 +179,22 @@ __device__ __forceinline__ void lk_build(const DevLevel &L, int ix, float fx, in
             const float dl = __shfl_up_sync(VTG_FULL, d, 1), dr = __shfl_down_sync(VTG_FULL, d, 1);
             const float ddx = dr - dl;
             if (r >= 2) {
-                const float tx = __fmaf_rn(mdx, 2.0f, udx + ddx) * gs;
-                const float ty = __fmaf_rn(d - u, 2.0f, (dl - ul) + (dr - ur)) * gs;
-                P.t[r - 2] = m;
-                P.tx[r - 2] = tx;
-                P.ty[r - 2] = ty;
+                const int k = r - 2;
+                const float tx = __fmaf_rn(mdx, 2.0f, udx + ddx);
+                const float ty = __fmaf_rn(d - u, 2.0f, (dl - ul) + (dr - ur));
+                if (k < HH) {
+                    ht[k] = m;
+                    htx[k] = tx;
+                    hty[k] = ty;
+                } else if (k < 2 * HH) {
+                    put_t(P, k - HH, lane, f2_pack(ht[k - HH], m));
+                    P.tx[k - HH] = f2_pack(htx[k - HH], tx);
+                    P.ty[k - HH] = f2_pack(hty[k - HH], ty);
+                } else {
+                    P.tl = m;
+                    P.txl = tx;
+                    P.tyl = ty;
+                }
                 if (r & 1) {
                     sxx1 = __fmaf_rn(tx, tx, sxx1);
                     sxy1 = __fmaf_rn(tx, ty, sxy1);
@@ -90,50 +209,93 @@ __device__ __forceinline__ void lk_build(const DevLevel &L, int ix, float fx, in
             m = d; ml = dl; mr = dr; mdx = ddx;
         }
     }
-    gxx = warp_fold(sxx0 + sxx1);
-    gxy = warp_fold(sxy0 + sxy1);
-    gyy = warp_fold(syy0 + syy1);
+    if constexpr (!EXACT) {
+        /* rows H .. MAXH - 1 were not built: pair the top half's rows whose partner is missing with zeros */
+#pragma unroll
+        for (int k = 0; k < HH; k++) {
+            if (HH + k >= H) {
+                put_t(P, k, lane, f2_pack(ht[k], 0.0f));
+                P.tx[k] = f2_pack(htx[k], 0.0f);
+                P.ty[k] = f2_pack(hty[k], 0.0f);
+            }
+        }
+        if (H < MAXH)
+            P.tl = P.txl = P.tyl = 0.0f;
+    }
+    /* (Sobel / 512)^2 = Sobel^2 x 2^-18, exact */
+    float fxx = act ? sxx0 + sxx1 : 0.0f, fxy = act ? sxy0 + sxy1 : 0.0f, fyy = act ? syy0 + syy1 : 0.0f;
+    warp_fold2(fxx, fxy);
+    fyy = warp_fold(fyy);
+    gxx = fxx * (LK_GRAD_SCALE * LK_GRAD_SCALE);
+    gxy = fxy * (LK_GRAD_SCALE * LK_GRAD_SCALE);
+    gyy = fyy * (LK_GRAD_SCALE * LK_GRAD_SCALE);
 }
 
 /* iterate (RESID = false): J at pixel (jx + fx, jy + fy); the sums of It Tx and It Ty.
- * residual (RESID = true): the sums of |It| and It^2, It in 8-bit grey. */
-template <int MAXH, bool EXACT, bool RESID>
+ * residual (RESID = true): the sums of |It| and It^2, It in 8-bit grey.
+ * The top half's rows (image rows y0 .. y0 + HH) and the bottom half's (y0 + HH .. y0 + 2 HH) run as the two halves
+ * of packed pairs, each carrying its own previous row; an odd height's last row follows the bottom half. With a height
+ * below MAXH (not EXACT), bottom-half rows past H read row H again and count for nothing (zero Tx, Ty; masked It). */
+template <int MAXH, bool EXACT, bool RESID, bool TS>
 __device__ __forceinline__ void lk_sample(const DevLevel &L, int jx, float fx, int jy, float fy, int W, int Hr, int lane,
-                                          const Patch<MAXH> &P, float &b0, float &b1)
+                                          const Patch<MAXH, TS> &P, float &b0, float &b1)
 {
+    constexpr int HH = MAXH / 2;
     const int H = EXACT ? MAXH : Hr;
     const int x0 = jx - W / 2, y0 = jy - H / 2;
-    const float q6 = (lane >= 1 && lane <= W) ? LK_Q6_INV : 0.0f;
-    const float *row = L.p + (size_t)y0 * L.pitch + (x0 - 1 + min(lane, W + 1));
-    float prev = hlerp(row, fx);
-    float s00 = 0.f, s01 = 0.f, s10 = 0.f, s11 = 0.f;
+    const bool act = lane >= 1 && lane <= W;
+    const float q6 = act ? LK_Q6_INV : 0.0f;
+    const float *col = L.p + (size_t)y0 * L.pitch + (x0 - 1 + min(lane, W + 1));
+    const float *ra = col;
+    const float *rb = col + (size_t)(EXACT ? HH : min(HH, H)) * L.pitch;
+    const f2_t FX = f2_pack(fx, fx), FY = f2_pack(fy, fy);
+    f2_t prev = hlerp2(ra, rb, FX);
+    f2_t s0 = 0ull, s1 = 0ull; /* (+0, +0) */
 #pragma unroll
-    for (int r = 0; r < MAXH; r++) {
+    for (int r = 0; r < HH; r++) {
         if (EXACT || r < H) {
-            row += L.pitch;
-            const float cur = hlerp(row, fx);
-            const float it = P.t[r] - __fmaf_rn(cur - prev, fy, prev);
+            ra += L.pitch;
+            if (EXACT)
+                rb += L.pitch;
+            else
+                rb = col + (size_t)min(HH + 1 + r, H) * L.pitch;
+            const f2_t cur = hlerp2(ra, rb, FX);
+            const f2_t it = f2_sub(get_t(P, r, lane), f2_fma(f2_sub(cur, prev), FY, prev));
             prev = cur;
             if (RESID) {
-                const float g = it * q6;
-                if (r & 1) {
-                    s01 = s01 + fabsf(g);
-                    s11 = __fmaf_rn(g, g, s11);
-                } else {
-                    s00 = s00 + fabsf(g);
-                    s10 = __fmaf_rn(g, g, s10);
-                }
-            } else if (r & 1) {
-                s01 = __fmaf_rn(it, P.tx[r], s01);
-                s11 = __fmaf_rn(it, P.ty[r], s11);
+                const f2_t g = f2_mul(it, f2_pack(q6, (EXACT || HH + r < H) ? q6 : 0.0f));
+                s0 = f2_add(s0, f2_abs(g));
+                s1 = f2_fma(g, g, s1);
             } else {
-                s00 = __fmaf_rn(it, P.tx[r], s00);
-                s10 = __fmaf_rn(it, P.ty[r], s10);
+                s0 = f2_fma(it, P.tx[r], s0);
+                s1 = f2_fma(it, P.ty[r], s1);
             }
         }
     }
-    b0 = warp_fold(s00 + s01);
-    b1 = warp_fold(s10 + s11);
+    float t0 = f2_sum(s0), t1 = f2_sum(s1);
+    if constexpr ((MAXH & 1) != 0) {
+        if (EXACT || H == MAXH) {
+            const float cur = hlerp(EXACT ? rb + L.pitch : col + (size_t)H * L.pitch, fx);
+            const float pb = f2_hi(prev);
+            const float it = P.tl - __fmaf_rn(cur - pb, fy, pb);
+            if (RESID) {
+                const float g = it * q6;
+                t0 = t0 + fabsf(g);
+                t1 = __fmaf_rn(g, g, t1);
+            } else {
+                t0 = __fmaf_rn(it, P.txl, t0);
+                t1 = __fmaf_rn(it, P.tyl, t1);
+            }
+        }
+    }
+    if (!RESID) {
+        t0 = act ? t0 : 0.0f;
+        t1 = act ? t1 : 0.0f;
+    }
+    warp_fold2(t0, t1);
+    /* iterate: It Tx / 512, the gradient scale applied to the folded sums (exact) */
+    b0 = RESID ? t0 : t0 * LK_GRAD_SCALE;
+    b1 = RESID ? t1 : t1 * LK_GRAD_SCALE;
 }
 
 /* A position as whole pixel + offset: floor and phase of base + t, base a whole number. */
@@ -145,9 +307,9 @@ __device__ __forceinline__ void split(int base, float t, int &i, float &f)
 }
 
 /* The pyramid walk (src/kern/lk_driver.inc:7-109), warp-uniform, F32. */
-template <int MAXH, bool EXACT>
+template <int MAXH, bool EXACT, bool TS>
 __device__ __forceinline__ void lk_track(const DevPyr &I, const DevPyr &J, int top, const LkPrm &p, float x, float y,
-                                         float gx0, float gy0, int lane, Patch<MAXH> &P, vtg_lk_out &o)
+                                         float gx0, float gy0, int lane, Patch<MAXH, TS> &P, vtg_lk_out &o)
 {
     const int W = p.W, H = EXACT ? MAXH : p.H;
     const int mx = W / 2 + 1, my = H / 2 + 1;
@@ -171,7 +333,7 @@ __device__ __forceinline__ void lk_track(const DevPyr &I, const DevPyr &J, int t
         const int bx = (int)fpx, by = (int)fpy;
         const float rx = px - fpx, ry = py - fpy; /* exact */
         float gxx, gxy, gyy;
-        lk_build<MAXH, EXACT>(IL, bx, rx, by, ry, W, H, lane, P, gxx, gxy, gyy);
+        lk_build<MAXH, EXACT, TS>(IL, bx, rx, by, ry, W, H, lane, P, gxx, gxy, gyy);
         /* det = gxx gyy - gxy^2 by Kahan's product difference; the smaller eigenvalue as det / lambda_max. */
         const float w2 = gxy * gxy;
         const float e2 = __fmaf_rn(gxy, gxy, -w2);
@@ -218,7 +380,7 @@ __device__ __forceinline__ void lk_track(const DevPyr &I, const DevPyr &J, int t
             split(bx, qx, jx, fx);
             split(by, qy, jy, fy);
             float sx, sy;
-            lk_sample<MAXH, EXACT, false>(JL, jx, fx, jy, fy, W, H, lane, P, sx, sy);
+            lk_sample<MAXH, EXACT, false, TS>(JL, jx, fx, jy, fy, W, H, lane, P, sx, sy);
             const float ex = __fmaf_rn(ia, sx, ib * sy), ey = __fmaf_rn(ib, sx, ic * sy);
             vx += ex;
             vy += ey;
@@ -252,7 +414,7 @@ __device__ __forceinline__ void lk_track(const DevPyr &I, const DevPyr &J, int t
             split(bx, qx, jx, fx);
             split(by, qy, jy, fy);
             float sa, ss;
-            lk_sample<MAXH, EXACT, true>(J0, jx, fx, jy, fy, W, H, lane, P, sa, ss);
+            lk_sample<MAXH, EXACT, true, TS>(J0, jx, fx, jy, fy, W, H, lane, P, sa, ss);
             const float r0 = sa / p.area, r1 = ss / p.area;
             o.residual = r0;
             if (r0 > p.max_residual)
@@ -268,15 +430,15 @@ __device__ __forceinline__ void lk_track(const DevPyr &I, const DevPyr &J, int t
 
 /* lk_track then, when asked and the track is good, the forward-backward check (src/kern/lk_driver.inc:111-121): the
  * found point tracked back from J to I from minus the found flow. One copy of the walk serves both passes. */
-template <int MAXH, bool EXACT>
+template <int MAXH, bool EXACT, bool TS>
 __device__ __forceinline__ void lk_point(const DevPyr &I, const DevPyr &J, int top, const LkPrm &p, float x, float y,
-                                         float gx, float gy, int lane, Patch<MAXH> &P, vtg_lk_out &o)
+                                         float gx, float gy, int lane, Patch<MAXH, TS> &P, vtg_lk_out &o)
 {
     const int passes = p.fb_max2 > 0.0f ? 2 : 1;
     float sx = x, sy = y;
     for (int pass = 0; pass < passes; pass++) {
         vtg_lk_out r;
-        lk_track<MAXH, EXACT>(pass ? J : I, pass ? I : J, top, p, sx, sy, gx, gy, lane, P, r);
+        lk_track<MAXH, EXACT, TS>(pass ? J : I, pass ? I : J, top, p, sx, sy, gx, gy, lane, P, r);
         if (pass == 0) {
             o = r;
             if (o.status)
@@ -322,19 +484,20 @@ __device__ __forceinline__ float cell_diff(const DevLevel &A, const DevLevel &B,
 
 /* One cell of a grid: its centre (cw c + cw / 2, ch r + ch / 2), clamped to where the patch fits (still.c:127-130),
  * LK with the forward-backward check, and the cell record (still.c:132-140). The whole warp calls it. */
-template <int MAXH, bool EXACT>
+template <int MAXH, bool EXACT, bool TS>
 __device__ __forceinline__ void lk_cell(const DevPyr &I, const DevPyr &J, int top, const LkPrm &p, const CellGrid &g,
                                         int base_w, int base_h, int i, int lane, vtg_lk_out *__restrict__ out,
-                                        vtg_cell *__restrict__ cells)
+                                        vtg_cell *__restrict__ cells, f2_t *ts)
 {
     const int col = i % g.cols, row = i / g.cols;
     const float mx = (float)(p.W / 2 + 2), my = (float)(p.H / 2 + 2);
     float x = (float)(col * g.cell_w + g.cell_w / 2), y = (float)(row * g.cell_h + g.cell_h / 2);
     x = fminf(fmaxf(x, mx), (float)base_w - 1.0f - mx);
     y = fminf(fmaxf(y, my), (float)base_h - 1.0f - my);
-    Patch<MAXH> P;
+    Patch<MAXH, TS> P;
+    P.ts = ts;
     vtg_lk_out o;
-    lk_point<MAXH, EXACT>(I, J, top, p, x, y, 0.0f, 0.0f, lane, P, o);
+    lk_point<MAXH, EXACT, TS>(I, J, top, p, x, y, 0.0f, 0.0f, lane, P, o);
     if (out)
         store_out(out + i, o, lane);
     if (cells) {
@@ -360,7 +523,7 @@ __global__ void __launch_bounds__(256, 2) lk_cells_kernel(const DevPyr *__restri
     const int i = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
     if (i >= g.n)
         return;
-    lk_cell<MAXH, EXACT>(*Ip, *Jp, top, p, g, base_w, base_h, i, lane, out, cells);
+    lk_cell<MAXH, EXACT, false>(*Ip, *Jp, top, p, g, base_w, base_h, i, lane, out, cells, nullptr);
 }
 
 /* Many streams' cells in one launch. Work items are runs of `chunk` cells of one job; job j's items start at
@@ -369,13 +532,15 @@ __global__ void __launch_bounds__(256, 2) lk_cells_kernel(const DevPyr *__restri
  * not depend on what else is in the batch. */
 #define LK_BATCH_MAX_JOBS 512
 
-template <int MAXH, bool EXACT, bool PERSISTENT, int WARPS, int MINB>
+template <int MAXH, bool EXACT, bool PERSISTENT, int WARPS, int MINB, bool TS>
 __global__ void __launch_bounds__(WARPS * 32, MINB) lk_batch_kernel(const LkJob *__restrict__ jobs,
                                                                     const int *__restrict__ item_start, int njobs,
                                                                     int items, int chunk, LkPrm p,
                                                                     int *__restrict__ counter)
 {
     __shared__ int s_start[LK_BATCH_MAX_JOBS + 1];
+    extern __shared__ f2_t s_t[]; /* TS: WARPS x (MAXH / 2) x 32 pairs */
+    f2_t *ts = TS ? s_t + (size_t)(threadIdx.x >> 5) * (MAXH / 2) * 32 : nullptr;
     for (int k = threadIdx.x; k <= njobs; k += blockDim.x)
         s_start[k] = item_start[k];
     __syncthreads();
@@ -401,7 +566,7 @@ __global__ void __launch_bounds__(WARPS * 32, MINB) lk_batch_kernel(const LkJob 
         const LkJob &jb = jobs[lo];
         const int c0 = (item - s_start[lo]) * chunk, c1 = min(c0 + chunk, jb.g.n);
         for (int c = c0; c < c1; c++)
-            lk_cell<MAXH, EXACT>(*jb.I, *jb.J, jb.top, p, jb.g, jb.base_w, jb.base_h, c, lane, jb.out, jb.cells);
+            lk_cell<MAXH, EXACT, TS>(*jb.I, *jb.J, jb.top, p, jb.g, jb.base_w, jb.base_h, c, lane, jb.out, jb.cells, ts);
         if (!PERSISTENT)
             break;
     }
@@ -414,10 +579,23 @@ static cudaError_t lk_batch_launch(const LkJob *jobs, const int *item_start, int
 #define LKB(P, WARPS, MINB)                                                                                            \
     do {                                                                                                               \
         const int blocks = P ? sms * t.ctas_per_sm : (items + WARPS - 1) / WARPS;                                      \
-        lk_batch_kernel<MAXH, EXACT, P, WARPS, MINB><<<blocks, WARPS * 32, 0, s>>>(jobs, item_start, njobs, items,    \
-                                                                                   t.chunk, p, counter);               \
+        lk_batch_kernel<MAXH, EXACT, P, WARPS, MINB, false><<<blocks, WARPS * 32, 0, s>>>(jobs, item_start, njobs,    \
+                                                                                          items, t.chunk, p, counter); \
     } while (0)
-    if (t.persistent) {
+#define LKT(WARPS, MINB)                                                                                               \
+    do {                                                                                                               \
+        /* WARPS x (MAXH / 2) x 32 pairs: at most 30 KB, under the 48 KB that needs no opt-in */                      \
+        const size_t smem = sizeof(f2_t) * WARPS * (MAXH / 2) * 32;                                                  \
+        lk_batch_kernel<MAXH, EXACT, true, WARPS, MINB, true><<<sms * t.ctas_per_sm, WARPS * 32, smem, s>>>(          \
+            jobs, item_start, njobs, items, t.chunk, p, counter);                                                      \
+    } while (0)
+    if (t.tsmem) {
+        /* the template's T in shared memory: fewer registers, more warps an SM */
+        if (t.block_warps == 4)
+            LKT(4, 5);
+        else
+            LKT(8, 3);
+    } else if (t.persistent) {
         if (t.block_warps == 4)
             LKB(true, 4, 4);
         else if (t.block_warps == 16)
@@ -433,6 +611,7 @@ static cudaError_t lk_batch_launch(const LkJob *jobs, const int *item_start, int
             LKB(false, 8, 2);
     }
 #undef LKB
+#undef LKT
     return cudaGetLastError();
 }
 
@@ -457,9 +636,10 @@ __global__ void __launch_bounds__(256, 2) lk_points_kernel(const DevPyr *__restr
     const int i = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
     if (i >= n)
         return;
-    Patch<MAXH> P;
+    Patch<MAXH, false> P;
+    P.ts = nullptr;
     vtg_lk_out o;
-    lk_point<MAXH, EXACT>(*Ip, *Jp, top, p, xs[i], ys[i], gxs ? gxs[i] : 0.0f, gys ? gys[i] : 0.0f, lane, P, o);
+    lk_point<MAXH, EXACT, false>(*Ip, *Jp, top, p, xs[i], ys[i], gxs ? gxs[i] : 0.0f, gys ? gys[i] : 0.0f, lane, P, o);
     store_out(out + i, o, lane);
 }
 
