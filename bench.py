@@ -33,6 +33,8 @@ sys.path.insert(0, PKG)
 
 METRIC = "LK cells/s + p99 ms/frame-pair, served-batched vs plain GPU; ≤0.01px vs FP64"
 W, H, LEVELS, CELL_W, CELL_H, PATCH = 1920, 1080, 4, 16, 8, 21
+# DRAM bytes (read + write) of one batched LK launch of 8 streams, from ncu (profiles/lk_batch_kernel_1080p_x8.md)
+LK_TRAFFIC_BYTES = 176_629_504 + 8_708_352
 CELLS = 16200
 
 
@@ -111,36 +113,101 @@ def frames_1080(n: int):
     return [S.warp_pair(W, H, S.seeded_shift(2 + k, 0), 0.5, seed=2 + k)[:2] for k in range(n)]
 
 
-def time_plain(vtg, torch, ctx, dframes, steps: int, warmup: int, device: str):
-    """One stream, one vtg_build + vtg_cells per frame pair; L2 flushed before each timed step."""
-    t = vtg.Tracker(ctx, vtg.config(W, H, levels=LEVELS, cell_w=CELL_W, cell_h=CELL_H))
-    stream = torch.cuda.ExternalStream(t.stream)
+def time_plain(vtg, torch, ctx, dev, steps: int, warmup: int, device: str):
+    """The plain form: one vtg_build + vtg_cells call per frame pair, one pair at a time on one stream, taking the
+    streams in turn (tracker j for stream j), so it does the batched step's work; L2 flushed before each timed pair."""
+    B = len(dev)
+    trackers = [vtg.Tracker(ctx, vtg.config(W, H, levels=LEVELS, cell_w=CELL_W, cell_h=CELL_H)) for _ in range(B)]
+    stream = torch.cuda.Stream(device=device)
+    sp = stream.cuda_stream
     dcells = torch.empty(CELLS * 24, dtype=torch.uint8, device=device)
     dlk = torch.empty(CELLS * 32, dtype=torch.uint8, device=device)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=device)
-    f0, f1 = dframes
-    t.build(0, f0.data_ptr(), where=vtg.DEVICE)
-    for k in range(1, warmup + 1):
-        cur = k & 1
-        t.build(cur, (f1 if cur else f0).data_ptr(), where=vtg.DEVICE)
-        t.cells_device(cur ^ 1, cur, dcells.data_ptr(), dlk.data_ptr())
+    torch.cuda.synchronize()
+    for t, (f0, _) in zip(trackers, dev):
+        t.build(0, f0.data_ptr(), where=vtg.DEVICE, stream=sp)
+
+    def pair(k):
+        j, cur = k % B, (k // B + 1) & 1
+        f0, f1 = dev[j]
+        trackers[j].build(cur, (f1 if cur else f0).data_ptr(), where=vtg.DEVICE, stream=sp)
+        trackers[j].cells_device(cur ^ 1, cur, dcells.data_ptr(), dlk.data_ptr(), stream=sp)
+
+    w = warmup * B
+    for k in range(w):
+        pair(k)
+    steps = -(-steps // B) * B
     torch.cuda.synchronize()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
     for k in range(steps):
         with torch.cuda.stream(stream):
             flush.fill_(k & 255)
             ev[k][0].record(stream)
-        cur = (warmup + 1 + k) & 1
-        t.build(cur, (f1 if cur else f0).data_ptr(), where=vtg.DEVICE)
-        t.cells_device(cur ^ 1, cur, dcells.data_ptr(), dlk.data_ptr())
+        pair(w + k)
         with torch.cuda.stream(stream):
             ev[k][1].record(stream)
     torch.cuda.synchronize()
     ms = np.array([a.elapsed_time(b) for a, b in ev])
-    t.close()
+    for t in trackers:
+        t.close()
     return {"value": CELLS * steps / (ms.sum() / 1e3), "unit": "cells/s", "ms_per_pair": float(ms.mean()),
             "p50_ms_per_pair": float(np.percentile(ms, 50)), "p99_ms_per_pair": float(np.percentile(ms, 99)),
-            "gpu_launches_per_pair": LEVELS}
+            "pairs": steps, "streams": B,
+            # one pyramid launch for each level above 0, then the LK launch
+            "gpu_launches_per_pair": (LEVELS - 1) + 1}
+
+
+def time_batched_mix(vtg, torch, ctx, device: str, nstreams: int = 64, steps: int = 300, warmup: int = 3) -> dict:
+    """Many uneven streams in one step: nstreams streams with sizes drawn uniformly (seeded) from 640x480, 1280x720 and
+    1920x1080 (1,200 cells on a 16-px grid at 640x480 with 3 levels; 7,200 and 16,200 cells on 16x8 with 4 levels),
+    each with its own seeded shift of up to 12 px. Every stream's pyramid sets and cell state stay on the device for
+    `steps` frames, replayed from the two captured graphs; the autotuned launch shape against the default one."""
+    import concurrent.futures as cf
+
+    import vtg_synth as S
+
+    sizes = [(640, 480), (1280, 720), (1920, 1080)]
+    pick = np.random.default_rng(4).integers(0, 3, nstreams)
+    with cf.ThreadPoolExecutor(min(16, os.cpu_count() or 4)) as ex:
+        pairs = list(ex.map(lambda k: S.warp_pair(*sizes[pick[k]], S.seeded_shift(100 + k, 0), 0.5,
+                                                  seed=100 + k)[:2], range(nstreams)))
+    dev = [(torch.from_numpy(f0).to(device), torch.from_numpy(f1).to(device)) for f0, f1 in pairs]
+    torch.cuda.synchronize()
+    trackers = []
+    for k in range(nstreams):
+        w, h = sizes[pick[k]]
+        small = w == 640
+        trackers.append(vtg.Tracker(ctx, vtg.config(w, h, levels=3 if small else 4, cell_w=16,
+                                                    cell_h=16 if small else 8)))
+    batch = vtg.Batch(ctx, nstreams)
+    batch.prepare(0, trackers, [d0.data_ptr() for d0, _ in dev], [0] * nstreams)
+    batch.prepare(1, trackers, [d1.data_ptr() for _, d1 in dev], [1] * nstreams)
+    batch.launch(0)
+    batch.launch(1)
+    ctx.sync()
+    cells = batch.cells(1)
+    tuned, tuned_ms, default_ms = batch.autotune(1, reps=5)
+    batch.capture(0)
+    batch.capture(1)
+    bstream = torch.cuda.ExternalStream(batch.stream)
+    for k in range(warmup):
+        batch.replay(k & 1)
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for k in range(steps):
+        ev[k][0].record(bstream)
+        batch.replay((warmup + k) & 1)
+        ev[k][1].record(bstream)
+    torch.cuda.synchronize()
+    ms = np.array([a.elapsed_time(b) for a, b in ev])
+    batch.close()
+    for t in trackers:
+        t.close()
+    return {"streams": nstreams, "sizes": {"%dx%d" % sizes[i]: int((pick == i).sum()) for i in range(3)},
+            "cells_per_step": cells, "frames": steps, "cells_per_s": cells * steps / (ms.sum() / 1e3),
+            "ms_per_step": float(ms.mean()), "p50_ms_per_step": float(np.percentile(ms, 50)),
+            "p99_ms_per_step": float(np.percentile(ms, 99)),
+            "autotune": {"chosen": tuned, "chosen_ms": tuned_ms, "default_ms": default_ms}}
 
 
 def run_ours(args) -> dict | None:
@@ -167,7 +234,7 @@ def run_ours(args) -> dict | None:
     clk = Clocks(local).__enter__()
 
     # ---- the plain GPU form
-    plain = time_plain(vtg, torch, ctx, dev[0], max(args.steps, 20), args.warmup, device)
+    plain = time_plain(vtg, torch, ctx, dev, max(args.steps, 24), args.warmup, device)
 
     # ---- the batched form: B streams a step, autotuned, replayed from CUDA graphs
     trackers = [vtg.Tracker(ctx, vtg.config(W, H, levels=LEVELS, cell_w=CELL_W, cell_h=CELL_H)) for _ in range(B)]
@@ -212,8 +279,10 @@ def run_ours(args) -> dict | None:
                 "unit": "TFLOP/s", "frac": achieved / fp32_peak,
                 "peak_source": "nominal FP32 CUDA-core rate (152 SMs x 128 lanes x 2) at the measured max SM clock "
                                "(MEASURED_PEAKS.json sm_max_mhz); MEASURED_PEAKS.json holds no FP32 rate",
-                "algorithmic_flop_per_launch": flops, "launch_ms": lk_ms, "traffic": None,
-                "traffic_note": "see profiles/lk_batch_kernel_1080p.md (ncu dram bytes per launch)"}
+                "algorithmic_flop_per_launch": flops, "launch_ms": lk_ms, "traffic": LK_TRAFFIC_BYTES * B / 8,
+                "traffic_note": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch of this step "
+                                "(profiles/lk_batch_kernel_1080p_x8.md); the algorithmic bytes are the 8 streams' "
+                                "two pyramid sets read once plus the cell records written"}
     pyr_bytes = B * (W * H + 4 * sum(a * b for a, b in [(1920, 1080), (960, 540), (480, 270), (240, 135)]))
     roof_pyr = {"kernel": "pyr_batch_kernel (3 launches a step)", "bound": "hbm",
                 "achieved": pyr_bytes / (pyr_ms / 1e3) / 1e9, "peak": pk.get("hbm_gbs", 6800.0), "unit": "GB/s",
@@ -223,6 +292,7 @@ def run_ours(args) -> dict | None:
     batch.close()
     for t in trackers:
         t.close()
+    mix64 = time_batched_mix(vtg, torch, ctx, device)
 
     # ---- end to end: the served loop through the C ABI, pinned host frames in, cell records out
     pinned = []
@@ -241,6 +311,15 @@ def run_ours(args) -> dict | None:
            "ncc_searches": served["ncc"], "arrivals": "Poisson, %d streams x 1000 fps (saturating)" % B}
     e2e_plain = {"value": served_plain["cells_per_s"], "unit": "cells/s", "p50_ms_per_pair": served_plain["p50_ms"],
                  "p99_ms_per_pair": served_plain["p99_ms"]}
+    # latency below saturation: the same streams at a camera's 30 fps (240 frame pairs/s offered)
+    live = [dict(width=W, height=H, fps=30.0, start_s=0.0, frames=150) for _ in range(B)]
+    lat = vtg.serve(ctx, live, [p.data_ptr() for p in pinned], lkcfg, duration_s=5.0, max_batch=B, inflight=2,
+                    ncc_share=0.02, seed=13)
+    lat_plain = vtg.serve(ctx, live, [p.data_ptr() for p in pinned], lkcfg, duration_s=5.0, max_batch=B,
+                          inflight=1, ncc_share=0.02, plain=True, seed=13)
+    e2e_latency = {"arrivals": "Poisson, %d streams x 30 fps of 1920x1080" % B,
+                   "served": {k: lat[k] for k in ("cells_per_s", "p50_ms", "p99_ms", "mean_batch", "served")},
+                   "plain": {k: lat_plain[k] for k in ("cells_per_s", "p50_ms", "p99_ms", "served")}}
     # nominal rates, mixed sizes: two 1080p at 60 fps (4,080 cells at level 1), one 720p at 15 fps, 13 more
     mix = [dict(width=1920, height=1080, flow_level=1, fps=60.0, start_s=0.0, frames=90),
            dict(width=1920, height=1080, flow_level=1, fps=60.0, start_s=0.0, frames=90),
@@ -269,13 +348,15 @@ def run_ours(args) -> dict | None:
             "p50_ms_per_step": float(np.percentile(step_ms, 50)), "p99_ms_per_step": float(np.percentile(step_ms, 99)),
             "plain": plain, "batched_vs_plain": value / plain["value"],
             "autotune": {"chosen": tuned, "chosen_ms": tuned_ms, "default_ms": default_ms,
-                         "default": {"block_warps": 8, "chunk": 1, "persistent": 1, "ctas_per_sm": 2}},
+                         "default": {"block_warps": 8, "chunk": 1, "persistent": 1, "ctas_per_sm": 2, "tsmem": 0}},
             "e2e": e2e, "e2e_plain": e2e_plain, "e2e_vs_plain": e2e["value"] / max(e2e_plain["value"], 1e-9),
+            "e2e_latency": e2e_latency, "batched_mix64": mix64,
             "served_mix": {"served": {k: mixed[k] for k in ("cells_per_s", "p50_ms", "p99_ms", "mean_batch", "ncc",
                                                             "served")},
                            "plain": {k: mixed_plain[k] for k in ("cells_per_s", "p50_ms", "p99_ms", "served")},
                            "streams": "2x1080p@60 (4,080 cells), 1x720p@15, 13 more 640x480..1080p@30"},
-            "roofline": roofline, "roofline_pyramid": roof_pyr, "gpu_launches": args.steps * LEVELS,
+            # a batched step: one pyramid launch for each level above 0, then one LK launch
+            "roofline": roofline, "roofline_pyramid": roof_pyr, "gpu_launches": args.steps * ((LEVELS - 1) + 1),
             "clocks": clk.summary()}
     line["cpu_baseline"] = cpu_baseline(pairs[0])
     return line

@@ -250,7 +250,8 @@ __device__ __forceinline__ void lk_sample(const DevLevel &L, int jx, float fx, i
     const float *rb = col + (size_t)(EXACT ? HH : min(HH, H)) * L.pitch;
     const f2_t FX = f2_pack(fx, fx), FY = f2_pack(fy, fy);
     f2_t prev = hlerp2(ra, rb, FX);
-    f2_t s0 = 0ull, s1 = 0ull; /* (+0, +0) */
+    /* It Tx, It Ty: pairs of even and of odd r in separate chains */
+    f2_t s0 = 0ull, s1 = 0ull, s2 = 0ull, s3 = 0ull; /* (+0, +0) */
 #pragma unroll
     for (int r = 0; r < HH; r++) {
         if (EXACT || r < H) {
@@ -266,11 +267,18 @@ __device__ __forceinline__ void lk_sample(const DevLevel &L, int jx, float fx, i
                 const f2_t g = f2_mul(it, f2_pack(q6, (EXACT || HH + r < H) ? q6 : 0.0f));
                 s0 = f2_add(s0, f2_abs(g));
                 s1 = f2_fma(g, g, s1);
+            } else if (r & 1) {
+                s2 = f2_fma(it, P.tx[r], s2);
+                s3 = f2_fma(it, P.ty[r], s3);
             } else {
                 s0 = f2_fma(it, P.tx[r], s0);
                 s1 = f2_fma(it, P.ty[r], s1);
             }
         }
+    }
+    if (!RESID) {
+        s0 = f2_add(s0, s2);
+        s1 = f2_add(s1, s3);
     }
     float t0 = f2_sum(s0), t1 = f2_sum(s1);
     if constexpr ((MAXH & 1) != 0) {
