@@ -14,47 +14,159 @@
 
 #define RT_X 64 /* output tile */
 #define RT_Y 16
-#define RS_X (2 * RT_X + 4) /* source tile: two output pixels per step, two each side */
-#define RS_Y (2 * RT_Y + 4)
+#define RS_Y (2 * RT_Y + 4) /* source rows of a tile: two each side */
+/* Staged columns. A tile's source columns are 2 ox - 2 .. 2 ox + 129; staging starts 16-byte aligned before them:
+ * bytes from 2 ox - 16 (160 of them), F32 values from 2 ox - 4 (136). Column k of the vertical sums is source column
+ * 2 ox - 4 + k in both. */
+#define SB_X 160
+#define SF_X 136
+#define SF_P 140 /* int row pitch of staged F32 values and of the vertical sums: 16-byte aligned rows */
 
-/* One 64 x 16 tile of the output level at (ox, oy), from a 132 x 36 source tile in shared memory; with FROM_U8 the
- * source is the frame's bytes and level 0 (byte x 64) is written from the same tile. dst may be NULL (level 0 only). */
+/* One 64 x 16 tile of the output level at (ox, oy). With FROM_U8 the source is the frame's bytes (rows `spitch`
+ * bytes apart), level 0 (byte x 64) is written from the same staged bytes, and the sums run on the bytes:
+ * (64 h + 128) >> 8 = (h + 2) >> 2 exactly. Otherwise the source is level L - 1 (F32 Q6, whole numbers) and the result
+ * is (h + 128) >> 8. vec: the source rows may be read 16 bytes at a time (base and pitch 16-byte aligned). dst may be
+ * NULL (level 0 only). Staging reads whole 16-byte chunks inside the row and clamps the chunks that reach past an
+ * edge element by element, so every read is inside the plane and the border is the reference's replicated edge. */
 template <bool FROM_U8>
-__device__ __forceinline__ void reduce_tile(const void *__restrict__ src_, int sw, int sh, int spitch,
+__device__ __forceinline__ void reduce_tile(const void *__restrict__ src_, int sw, int sh, int spitch, bool vec,
                                             float *__restrict__ l0, int l0pitch, float *__restrict__ dst, int dw, int dh,
-                                            int dpitch, int ox, int oy, int (*s_src)[RS_X + 1], int (*s_v)[RS_X + 1])
+                                            int dpitch, int ox, int oy, uint8_t (*s_b)[SB_X], int (*s_f)[SF_P],
+                                            int (*s_v)[SF_P])
 {
     const int tid = threadIdx.x;
-    const int sx0 = 2 * ox - 2, sy0 = 2 * oy - 2;
-    for (int i = tid; i < RS_Y * RS_X; i += blockDim.x) {
-        const int r = i / RS_X, c = i - r * RS_X;
-        const int sy = min(max(sy0 + r, 0), sh - 1), sx = min(max(sx0 + c, 0), sw - 1);
-        int v;
-        if (FROM_U8)
-            v = 64 * (int)__ldg((const uint8_t *)src_ + (size_t)sy * spitch + sx);
-        else
-            v = (int)__ldg((const float *)src_ + (size_t)sy * spitch + sx);
-        s_src[r][c] = v;
-        /* Level 0 itself, from the same bytes: this tile's own 2 RT_X x 2 RT_Y pixels. */
-        if (FROM_U8 && r >= 2 && r < RS_Y - 2 && c >= 2 && c < RS_X - 2 && sy0 + r < sh && sx0 + c < sw)
-            l0[(size_t)(sy0 + r) * l0pitch + (sx0 + c)] = (float)v;
+    const int sy0 = 2 * oy - 2;
+    if (FROM_U8) {
+        const uint8_t *src = (const uint8_t *)src_;
+        const int gx0 = 2 * ox - 16;
+        for (int i = tid; i < RS_Y * (SB_X / 16); i += blockDim.x) {
+            const int r = i / (SB_X / 16), k = i - r * (SB_X / 16);
+            const int gy = min(max(sy0 + r, 0), sh - 1), gx = gx0 + 16 * k;
+            const uint8_t *row = src + (size_t)gy * spitch;
+            uint4 v;
+            if (vec && gx >= 0 && gx + 16 <= sw) {
+                v = __ldg(reinterpret_cast<const uint4 *>(row + gx));
+            } else {
+                uint32_t w[4];
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    uint32_t x = 0;
+#pragma unroll
+                    for (int e = 0; e < 4; e++)
+                        x |= (uint32_t)__ldg(row + min(max(gx + 4 * q + e, 0), sw - 1)) << (8 * e);
+                    w[q] = x;
+                }
+                v = make_uint4(w[0], w[1], w[2], w[3]);
+            }
+            *reinterpret_cast<uint4 *>(&s_b[r][16 * k]) = v;
+        }
+        __syncthreads();
+        /* level 0: rows 2 oy .. 2 oy + 31, columns 2 ox .. 2 ox + 127 (staged columns 16 .. 143), four a thread */
+        for (int i = tid; i < 2 * RT_Y * (2 * RT_X / 4); i += blockDim.x) {
+            const int r = i / (2 * RT_X / 4), g = i - r * (2 * RT_X / 4);
+            const int gy = 2 * oy + r, gx = 2 * ox + 4 * g;
+            if (gy >= sh || gx >= sw)
+                continue;
+            const uint32_t w = *reinterpret_cast<const uint32_t *>(&s_b[r + 2][16 + 4 * g]);
+            const float4 f = make_float4((float)(64u * (w & 255u)), (float)(64u * ((w >> 8) & 255u)),
+                                         (float)(64u * ((w >> 16) & 255u)), (float)(64u * (w >> 24)));
+            float *d = l0 + (size_t)gy * l0pitch + gx;
+            if (gx + 4 <= sw) {
+                *reinterpret_cast<float4 *>(d) = f;
+            } else {
+                d[0] = f.x;
+                if (gx + 1 < sw)
+                    d[1] = f.y;
+                if (gx + 2 < sw)
+                    d[2] = f.z;
+            }
+        }
+        if (!dst)
+            return;
+        /* vertical sums of staged byte columns 12 .. 147 (source 2 ox - 4 ..), four columns a thread */
+        for (int i = tid; i < RT_Y * (SF_X / 4); i += blockDim.x) {
+            const int r = i / (SF_X / 4), g = i - r * (SF_X / 4);
+            uint32_t w[5];
+#pragma unroll
+            for (int t = 0; t < 5; t++)
+                w[t] = *reinterpret_cast<const uint32_t *>(&s_b[2 * r + t][12 + 4 * g]);
+            int4 o;
+            int *op = &o.x;
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                const int a = (w[0] >> (8 * e)) & 255, b = (w[1] >> (8 * e)) & 255, c = (w[2] >> (8 * e)) & 255,
+                          d = (w[3] >> (8 * e)) & 255, f = (w[4] >> (8 * e)) & 255;
+                op[e] = a + f + 4 * (b + d) + 6 * c;
+            }
+            *reinterpret_cast<int4 *>(&s_v[r][4 * g]) = o;
+        }
+    } else {
+        const float *src = (const float *)src_;
+        const int gx0 = 2 * ox - 4;
+        for (int i = tid; i < RS_Y * (SF_X / 4); i += blockDim.x) {
+            const int r = i / (SF_X / 4), k = i - r * (SF_X / 4);
+            const int gy = min(max(sy0 + r, 0), sh - 1), gx = gx0 + 4 * k;
+            const float *row = src + (size_t)gy * spitch;
+            float4 v;
+            if (gx >= 0 && gx + 4 <= sw)
+                v = __ldg(reinterpret_cast<const float4 *>(row + gx));
+            else
+                v = make_float4(__ldg(row + min(max(gx, 0), sw - 1)), __ldg(row + min(max(gx + 1, 0), sw - 1)),
+                                __ldg(row + min(max(gx + 2, 0), sw - 1)), __ldg(row + min(max(gx + 3, 0), sw - 1)));
+            *reinterpret_cast<int4 *>(&s_f[r][4 * k]) = make_int4((int)v.x, (int)v.y, (int)v.z, (int)v.w);
+        }
+        __syncthreads();
+        for (int i = tid; i < RT_Y * (SF_X / 4); i += blockDim.x) {
+            const int r = i / (SF_X / 4), g = i - r * (SF_X / 4);
+            int4 t[5];
+#pragma unroll
+            for (int q = 0; q < 5; q++)
+                t[q] = *reinterpret_cast<const int4 *>(&s_f[2 * r + q][4 * g]);
+            int4 o;
+            o.x = t[0].x + t[4].x + 4 * (t[1].x + t[3].x) + 6 * t[2].x;
+            o.y = t[0].y + t[4].y + 4 * (t[1].y + t[3].y) + 6 * t[2].y;
+            o.z = t[0].z + t[4].z + 4 * (t[1].z + t[3].z) + 6 * t[2].z;
+            o.w = t[0].w + t[4].w + 4 * (t[1].w + t[3].w) + 6 * t[2].w;
+            *reinterpret_cast<int4 *>(&s_v[r][4 * g]) = o;
+        }
     }
-    if (!dst)
-        return;
     __syncthreads();
-    for (int i = tid; i < RT_Y * RS_X; i += blockDim.x) {
-        const int r = i / RS_X, c = i - r * RS_X;
-        s_v[r][c] = s_src[2 * r][c] + s_src[2 * r + 4][c] + 4 * (s_src[2 * r + 1][c] + s_src[2 * r + 3][c]) + 6 * s_src[2 * r + 2][c];
+    /* horizontal: output x takes vertical sums 2 x + 2 .. 2 x + 6; four outputs a thread (sums 8 g .. 8 g + 15) */
+    for (int i = tid; i < RT_Y * (RT_X / 4); i += blockDim.x) {
+        const int r = i / (RT_X / 4), g = i - r * (RT_X / 4);
+        const int gy = oy + r, gx = ox + 4 * g;
+        if (gy >= dh || gx >= dw)
+            continue;
+        int v[16];
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+            *reinterpret_cast<int4 *>(&v[4 * q]) = *reinterpret_cast<const int4 *>(&s_v[r][8 * g + 4 * q]);
+        float o[4];
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            const int c = 2 * e + 4;
+            const int h = v[c - 2] + v[c + 2] + 4 * (v[c - 1] + v[c + 1]) + 6 * v[c];
+            o[e] = (float)(FROM_U8 ? (h + 2) >> 2 : (h + 128) >> 8);
+        }
+        float *d = dst + (size_t)gy * dpitch + gx;
+        if (gx + 4 <= dw) {
+            *reinterpret_cast<float4 *>(d) = make_float4(o[0], o[1], o[2], o[3]);
+        } else {
+            for (int e = 0; e < 4 && gx + e < dw; e++)
+                d[e] = o[e];
+        }
     }
-    __syncthreads();
-    for (int i = tid; i < RT_Y * RT_X; i += blockDim.x) {
-        const int r = i / RT_X, x = i - r * RT_X;
-        const int c = 2 * x + 2;
-        const int h = s_v[r][c - 2] + s_v[r][c + 2] + 4 * (s_v[r][c - 1] + s_v[r][c + 1]) + 6 * s_v[r][c];
-        const int gy = oy + r, gx = ox + x;
-        if (gy < dh && gx < dw)
-            dst[(size_t)gy * dpitch + gx] = (float)((h + 128) >> 8);
-    }
+}
+
+/* The staged source: bytes for the first launch, ints (F32 values) for the others. */
+union TileSmem {
+    __align__(16) uint8_t b[RS_Y][SB_X];
+    __align__(16) int f[RS_Y][SF_P];
+};
+
+static __device__ __forceinline__ bool aligned16(const void *p, int pitch_bytes)
+{
+    return (((uintptr_t)p | (uintptr_t)pitch_bytes) & 15) == 0;
 }
 
 template <bool FROM_U8>
@@ -62,10 +174,10 @@ __global__ void __launch_bounds__(256) pyr_reduce_kernel(const void *__restrict_
                                                          float *__restrict__ l0, int l0pitch, float *__restrict__ dst,
                                                          int dw, int dh, int dpitch)
 {
-    __shared__ int s_src[RS_Y][RS_X + 1];
-    __shared__ int s_v[RT_Y][RS_X + 1];
-    reduce_tile<FROM_U8>(src_, sw, sh, spitch, l0, l0pitch, dst, dw, dh, dpitch, blockIdx.x * RT_X, blockIdx.y * RT_Y,
-                         s_src, s_v);
+    __shared__ TileSmem s_t;
+    __shared__ __align__(16) int s_v[RT_Y][SF_P];
+    reduce_tile<FROM_U8>(src_, sw, sh, spitch, aligned16(src_, spitch), l0, l0pitch, dst, dw, dh, dpitch,
+                         blockIdx.x * RT_X, blockIdx.y * RT_Y, s_t.b, s_t.f, s_v);
 }
 
 /* Many frames at once: the launch's tiles are every job's tiles of this level, back to back; a block finds its job by
@@ -74,8 +186,8 @@ template <bool FROM_U8>
 __global__ void __launch_bounds__(256) pyr_batch_kernel(const PyrJob *__restrict__ jobs, const int *__restrict__ start,
                                                         int njobs, int level)
 {
-    __shared__ int s_src[RS_Y][RS_X + 1];
-    __shared__ int s_v[RT_Y][RS_X + 1];
+    __shared__ TileSmem s_t;
+    __shared__ __align__(16) int s_v[RT_Y][SF_P];
     const int b = blockIdx.x;
     int lo = 0, hi = njobs; /* start[lo] <= b < start[hi] */
     while (hi - lo > 1) {
@@ -92,11 +204,11 @@ __global__ void __launch_bounds__(256) pyr_batch_kernel(const PyrJob *__restrict
     const int tiles_x = (dw + RT_X - 1) / RT_X;
     const int ox = (t % tiles_x) * RT_X, oy = (t / tiles_x) * RT_Y;
     if (FROM_U8)
-        reduce_tile<true>(j.src, j.w, j.h, j.stride, j.lv[0], j.pitch[0], j.levels > 1 ? j.lv[1] : nullptr, dw, dh,
-                          j.pitch[1], ox, oy, s_src, s_v);
+        reduce_tile<true>(j.src, j.w, j.h, j.stride, aligned16(j.src, j.stride), j.lv[0], j.pitch[0],
+                          j.levels > 1 ? j.lv[1] : nullptr, dw, dh, j.pitch[1], ox, oy, s_t.b, s_t.f, s_v);
     else
-        reduce_tile<false>(j.lv[level - 1], sw, sh, j.pitch[level - 1], nullptr, 0, j.lv[level], dw, dh, j.pitch[level],
-                           ox, oy, s_src, s_v);
+        reduce_tile<false>(j.lv[level - 1], sw, sh, j.pitch[level - 1], true, nullptr, 0, j.lv[level], dw, dh,
+                           j.pitch[level], ox, oy, s_t.b, s_t.f, s_v);
 }
 
 int vtg_pyr_tiles(int w, int h, int level)
