@@ -1,0 +1,440 @@
+/* compat.cu -- the reference-signature entry points of include/vtg_compat.h.
+ *
+ * Each call takes the reference's arguments (planes in its padded layout, host or device memory), moves what is in
+ * host memory to device scratch, runs the same kernels as the native API (lk.cu's point and cell kernels, the
+ * search's corner kernel) or a small kernel of its own for the image rows, and brings the outputs back before it
+ * returns. One lock serialises the calls; the scratch and the stream belong to the device of the first call. */
+#include <math.h>
+
+#include <mutex>
+
+#include "vtg_ctx.h"
+#include "vtg_internal.cuh"
+
+#include "../../include/vtg_compat.h"
+
+namespace {
+
+thread_local int t_status = VTG_OK;
+
+struct Compat {
+    std::mutex mu;
+    int device = -1;
+    cudaStream_t stream = nullptr;
+    char *scratch = nullptr;
+    size_t scratch_bytes = 0;
+    vtg_ctx *ctx = nullptr;       /* for the correlation's search context */
+    vtg_search *search = nullptr; /* sized sw x sh, 32 x 21 templates */
+    int sw = 0, sh = 0;
+};
+Compat g_c;
+
+#define TRY(x)                                                                                                         \
+    do {                                                                                                               \
+        const cudaError_t e_ = (x);                                                                                    \
+        if (e_ != cudaSuccess) {                                                                                       \
+            vtg_set_cuda_error(e_);                                                                                    \
+            return VTG_ECUDA;                                                                                          \
+        }                                                                                                              \
+    } while (0)
+
+/* The stream and scratch of the current device, made on first use. */
+int ready()
+{
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return VTG_ENODEV;
+    }
+    if (g_c.device == dev && g_c.stream)
+        return VTG_OK;
+    if (g_c.device >= 0)
+        return VTG_EINVAL; /* one device per process for these entry points */
+    TRY(cudaStreamCreateWithFlags(&g_c.stream, cudaStreamNonBlocking));
+    g_c.device = dev;
+    return VTG_OK;
+}
+
+/* At least `bytes` of device scratch, 256-byte aligned. */
+int scratch(size_t bytes, char **out)
+{
+    if (bytes > g_c.scratch_bytes) {
+        if (g_c.scratch) {
+            TRY(cudaStreamSynchronize(g_c.stream));
+            TRY(cudaFree(g_c.scratch));
+            g_c.scratch = nullptr;
+            g_c.scratch_bytes = 0;
+        }
+        const size_t want = bytes + (bytes >> 2);
+        if (cudaMalloc((void **)&g_c.scratch, want) != cudaSuccess) {
+            cudaGetLastError();
+            return VTG_ENOMEM;
+        }
+        g_c.scratch_bytes = want;
+    }
+    *out = g_c.scratch;
+    return VTG_OK;
+}
+
+size_t up256(size_t n) { return (n + 255) & ~(size_t)255; }
+
+/* Device or managed memory: the kernels read it in place. Anything else is staged. */
+bool on_device(const void *p)
+{
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+bool plane_ok(const vtg_ref_plane *pl)
+{
+    return pl && pl->p && pl->w >= 1 && pl->h >= 1 && pl->stride >= pl->w;
+}
+
+__global__ void q6_rows_kernel(float *__restrict__ dst, int dpitch, const uint8_t *__restrict__ src, int spitch, int w,
+                               int rows)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, r = blockIdx.y;
+    if (x < w && r < rows)
+        dst[(size_t)r * dpitch + x] = (float)(64 * (int)src[(size_t)r * spitch + x]);
+}
+
+/* Rows [y0, y1) of the reduce of src (rows srow0 .. of the full plane are at src), edges clamped to the plane's
+ * sh rows and sw columns; out row y - y0. Whole-number sums, as img_reduce. */
+__global__ void reduce_rows_kernel(float *__restrict__ dst, int dpitch, const float *__restrict__ src, int spitch,
+                                   int sw, int sh, int srow0, int dw, int y0, int y1)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = y0 + (int)blockIdx.y;
+    if (x >= dw || y >= y1)
+        return;
+    const int k[5] = {1, 4, 6, 4, 1};
+    int h = 0;
+    for (int i = 0; i < 5; i++) {
+        const int sy = min(max(2 * y + i - 2, 0), sh - 1) - srow0;
+        int v = 0;
+        for (int j = 0; j < 5; j++)
+            v += k[j] * (int)src[(size_t)sy * spitch + min(max(2 * x + j - 2, 0), sw - 1)];
+        h += k[i] * v;
+    }
+    dst[(size_t)(y - y0) * dpitch + x] = (float)((h + 128) >> 8);
+}
+
+LkPrm lk_prm(const vtg_ref_lk_cfg *c, float fb_max)
+{
+    LkPrm p;
+    p.W = c->w;
+    p.H = c->h;
+    p.max_iter = c->max_iter;
+    p.eps2 = c->eps * c->eps;
+    p.min_eig = c->min_eig;
+    p.max_residual = c->max_residual;
+    p.fb_max2 = fb_max > 0.0f ? fb_max * fb_max : 0.0f;
+    p.area = (float)(c->w * c->h);
+    return p;
+}
+
+bool cfg_ok(const vtg_ref_lk_cfg *c)
+{
+    return c && c->w >= 5 && c->w <= VTG_MAX_PATCH_W && c->h >= 5 && c->h <= VTG_MAX_PATCH_H && c->max_iter >= 1 &&
+           c->max_iter <= 1000 && c->eps >= 0.0f;
+}
+
+/* The device view of planes pl[0 .. n - 1]: in place, or their rows copied into scratch starting at *off. */
+int stage_levels(const vtg_ref_plane *pl, int n, DevPyr *d, char *base, size_t *off)
+{
+    d->levels = n;
+    for (int L = 0; L < n; L++) {
+        const vtg_ref_plane &q = pl[L];
+        if (!plane_ok(&q))
+            return VTG_EINVAL;
+        d->l[L].w = q.w;
+        d->l[L].h = q.h;
+        if (on_device(q.p)) {
+            d->l[L].p = q.p;
+            d->l[L].pitch = q.stride;
+        } else {
+            const int pitch = (q.w + 31) & ~31;
+            float *dst = (float *)(base + *off);
+            *off += up256((size_t)pitch * (size_t)q.h * sizeof(float));
+            TRY(cudaMemcpy2DAsync(dst, (size_t)pitch * sizeof(float), q.p, (size_t)q.stride * sizeof(float),
+                                  (size_t)q.w * sizeof(float), (size_t)q.h, cudaMemcpyHostToDevice, g_c.stream));
+            d->l[L].p = dst;
+            d->l[L].pitch = pitch;
+        }
+    }
+    return VTG_OK;
+}
+
+size_t levels_bytes(const vtg_ref_plane *pl, int n)
+{
+    size_t b = 0;
+    for (int L = 0; L < n; L++)
+        if (plane_ok(&pl[L]))
+            b += up256((size_t)((pl[L].w + 31) & ~31) * (size_t)pl[L].h * sizeof(float));
+    return b;
+}
+
+/* One point from pyramid I to pyramid J (levels 0 .. top), as lk_track: the result in *o. */
+int track_one(const vtg_ref_plane *I, const vtg_ref_plane *J, int top, const vtg_ref_lk_cfg *c, float x, float y,
+              float gx, float gy, vtg_lk_out *o)
+{
+    if (!I || !J || !o || !cfg_ok(c) || top < 0 || top >= VTG_MAX_LEVELS)
+        return VTG_EINVAL;
+    int rc = ready();
+    if (rc != VTG_OK)
+        return rc;
+    const size_t fixed = up256(2 * sizeof(DevPyr)) + up256(4 * sizeof(float)) + up256(sizeof(vtg_lk_out));
+    char *base = nullptr;
+    rc = scratch(fixed + levels_bytes(I, top + 1) + levels_bytes(J, top + 1), &base);
+    if (rc != VTG_OK)
+        return rc;
+    DevPyr h[2];
+    size_t off = fixed;
+    if ((rc = stage_levels(I, top + 1, &h[0], base, &off)) != VTG_OK ||
+        (rc = stage_levels(J, top + 1, &h[1], base, &off)) != VTG_OK)
+        return rc;
+    DevPyr *dp = (DevPyr *)base;
+    float *pt = (float *)(base + up256(2 * sizeof(DevPyr)));
+    vtg_lk_out *dout = (vtg_lk_out *)(base + up256(2 * sizeof(DevPyr)) + up256(4 * sizeof(float)));
+    const float hp[4] = {x, y, gx, gy};
+    TRY(cudaMemcpyAsync(dp, h, sizeof(h), cudaMemcpyHostToDevice, g_c.stream));
+    TRY(cudaMemcpyAsync(pt, hp, sizeof(hp), cudaMemcpyHostToDevice, g_c.stream));
+    TRY(vtg_launch_points(dp, dp + 1, top, lk_prm(c, 0.0f), 1, pt, pt + 1, pt + 2, pt + 3, dout, g_c.stream));
+    TRY(cudaMemcpyAsync(o, dout, sizeof(vtg_lk_out), cudaMemcpyDeviceToHost, g_c.stream));
+    TRY(cudaStreamSynchronize(g_c.stream));
+    return VTG_OK;
+}
+
+void lost(vtg_lk_out *o, float x, float y)
+{
+    if (!o)
+        return;
+    o->x = x;
+    o->y = y;
+    o->min_eig = o->residual = o->cov_xx = o->cov_xy = o->cov_yy = 0.0f;
+    o->iters = 0;
+    o->status = VTG_LK_OUT;
+}
+
+} // namespace
+
+extern "C" size_t lk_tile_bytes_cuda(void) { return 64; }
+
+extern "C" int vtg_compat_error(void) { return t_status; }
+
+extern "C" void img_u8_to_q6_cuda(const struct vtg_ref_plane *dst, const uint8_t *src, int src_stride, int y0, int y1)
+{
+    std::lock_guard<std::mutex> g(g_c.mu);
+    t_status = [&]() -> int {
+        if (!plane_ok(dst) || !src || src_stride < dst->w || y0 < 0 || y1 > dst->h)
+            return VTG_EINVAL;
+        if (y0 >= y1)
+            return VTG_OK;
+        int rc = ready();
+        if (rc != VTG_OK)
+            return rc;
+        const int w = dst->w, rows = y1 - y0;
+        const bool sdev = on_device(src), ddev = on_device(dst->p);
+        const size_t sbytes = sdev ? 0 : up256((size_t)w * rows), dbytes = ddev ? 0 : (size_t)w * rows * sizeof(float);
+        char *base = nullptr;
+        if (sbytes + dbytes > 0 && (rc = scratch(sbytes + dbytes + 256, &base)) != VTG_OK)
+            return rc;
+        const uint8_t *s = src + (size_t)y0 * src_stride;
+        int spitch = src_stride;
+        if (!sdev) {
+            TRY(cudaMemcpy2DAsync(base, (size_t)w, s, (size_t)src_stride, (size_t)w, (size_t)rows,
+                                  cudaMemcpyHostToDevice, g_c.stream));
+            s = (const uint8_t *)base;
+            spitch = w;
+        }
+        float *d = ddev ? dst->p + (size_t)y0 * dst->stride : (float *)(base + sbytes);
+        const int dpitch = ddev ? dst->stride : w;
+        q6_rows_kernel<<<dim3((w + 127) / 128, rows), 128, 0, g_c.stream>>>(d, dpitch, s, spitch, w, rows);
+        TRY(cudaGetLastError());
+        if (!ddev)
+            TRY(cudaMemcpy2DAsync(dst->p + (size_t)y0 * dst->stride, (size_t)dst->stride * sizeof(float), d,
+                                  (size_t)w * sizeof(float), (size_t)w * sizeof(float), (size_t)rows,
+                                  cudaMemcpyDeviceToHost, g_c.stream));
+        TRY(cudaStreamSynchronize(g_c.stream));
+        return VTG_OK;
+    }();
+}
+
+extern "C" void img_reduce_cuda(const struct vtg_ref_plane *dst, const struct vtg_ref_plane *src, int y0, int y1)
+{
+    std::lock_guard<std::mutex> g(g_c.mu);
+    t_status = [&]() -> int {
+        if (!plane_ok(dst) || !plane_ok(src) || dst->w != (src->w + 1) / 2 || dst->h != (src->h + 1) / 2 || y0 < 0 ||
+            y1 > dst->h)
+            return VTG_EINVAL;
+        if (y0 >= y1)
+            return VTG_OK;
+        int rc = ready();
+        if (rc != VTG_OK)
+            return rc;
+        const int dw = dst->w, rows = y1 - y0;
+        /* the source rows these output rows read */
+        const int s0 = max(2 * y0 - 2, 0), s1 = min(2 * (y1 - 1) + 2, src->h - 1);
+        const bool sdev = on_device(src->p), ddev = on_device(dst->p);
+        const size_t sbytes = sdev ? 0 : up256((size_t)src->w * (size_t)(s1 - s0 + 1) * sizeof(float));
+        const size_t dbytes = ddev ? 0 : (size_t)dw * rows * sizeof(float);
+        char *base = nullptr;
+        if (sbytes + dbytes > 0 && (rc = scratch(sbytes + dbytes + 256, &base)) != VTG_OK)
+            return rc;
+        const float *s = src->p + (size_t)s0 * src->stride;
+        int spitch = src->stride;
+        if (!sdev) {
+            TRY(cudaMemcpy2DAsync(base, (size_t)src->w * sizeof(float), s, (size_t)src->stride * sizeof(float),
+                                  (size_t)src->w * sizeof(float), (size_t)(s1 - s0 + 1), cudaMemcpyHostToDevice,
+                                  g_c.stream));
+            s = (const float *)base;
+            spitch = src->w;
+        }
+        float *d = ddev ? dst->p + (size_t)y0 * dst->stride : (float *)(base + sbytes);
+        const int dpitch = ddev ? dst->stride : dw;
+        reduce_rows_kernel<<<dim3((dw + 127) / 128, rows), 128, 0, g_c.stream>>>(d, dpitch, s, spitch, src->w, src->h,
+                                                                                  s0, dw, y0, y1);
+        TRY(cudaGetLastError());
+        if (!ddev)
+            TRY(cudaMemcpy2DAsync(dst->p + (size_t)y0 * dst->stride, (size_t)dst->stride * sizeof(float), d,
+                                  (size_t)dw * sizeof(float), (size_t)dw * sizeof(float), (size_t)rows,
+                                  cudaMemcpyDeviceToHost, g_c.stream));
+        TRY(cudaStreamSynchronize(g_c.stream));
+        return VTG_OK;
+    }();
+}
+
+extern "C" void lk_track_cuda(const struct vtg_ref_plane *I, const struct vtg_ref_plane *J, int top,
+                              const struct vtg_ref_lk_cfg *c, float x, float y, float gx, float gy,
+                              struct vtg_lk_out *o, void *tile)
+{
+    (void)tile;
+    std::lock_guard<std::mutex> g(g_c.mu);
+    t_status = track_one(I, J, top, c, x, y, gx, gy, o);
+    if (t_status != VTG_OK)
+        lost(o, x, y);
+}
+
+extern "C" void lk_flowback_cuda(const struct vtg_ref_plane *I, const struct vtg_ref_plane *J, int top,
+                                 const struct vtg_ref_lk_cfg *c, float x, float y, float max_fb, struct vtg_lk_out *o,
+                                 void *tile)
+{
+    (void)tile;
+    if (!o)
+        return;
+    if (o->status) {
+        t_status = VTG_OK;
+        return;
+    }
+    std::lock_guard<std::mutex> g(g_c.mu);
+    /* back from J to I, from the estimate, with minus the found flow as the guess */
+    vtg_lk_out b;
+    t_status = track_one(J, I, top, c, o->x, o->y, (float)((double)x - (double)o->x), (float)((double)y - (double)o->y),
+                         &b);
+    if (t_status != VTG_OK) {
+        o->status |= VTG_LK_FLOWBACK;
+        return;
+    }
+    const double ex = (double)b.x - (double)x, ey = (double)b.y - (double)y;
+    if (b.status || ex * ex + ey * ey > (double)max_fb * (double)max_fb)
+        o->status |= VTG_LK_FLOWBACK;
+}
+
+extern "C" void still_vectors_cuda(const struct vtg_ref_plane *mean, const struct vtg_ref_plane *cur,
+                                   const struct vtg_ref_lk_cfg *lk, float max_fb, struct vtg_cell *cells, int tid, int n)
+{
+    (void)n;
+    if (tid != 0)
+        return;
+    std::lock_guard<std::mutex> g(g_c.mu);
+    t_status = [&]() -> int {
+        if (!plane_ok(mean) || !plane_ok(cur) || mean->w != cur->w || mean->h != cur->h || !cells || !cfg_ok(lk) ||
+            !(max_fb >= 0.0f))
+            return VTG_EINVAL;
+        int rc = ready();
+        if (rc != VTG_OK)
+            return rc;
+        CellGrid gr;
+        gr.cell_w = 16; /* VT_CELL_W x VT_CELL_H, src/common/vt_proto.h */
+        gr.cell_h = 8;
+        gr.cols = (cur->w + gr.cell_w - 1) / gr.cell_w;
+        gr.rows = (cur->h + gr.cell_h - 1) / gr.cell_h;
+        gr.n = gr.cols * gr.rows;
+        const bool cdev = on_device(cells);
+        const size_t fixed = up256(2 * sizeof(DevPyr)) + (cdev ? 0 : up256((size_t)gr.n * sizeof(vtg_cell)));
+        char *base = nullptr;
+        if ((rc = scratch(fixed + levels_bytes(mean, 1) + levels_bytes(cur, 1), &base)) != VTG_OK)
+            return rc;
+        DevPyr h[2];
+        size_t off = fixed;
+        if ((rc = stage_levels(mean, 1, &h[0], base, &off)) != VTG_OK ||
+            (rc = stage_levels(cur, 1, &h[1], base, &off)) != VTG_OK)
+            return rc;
+        DevPyr *dp = (DevPyr *)base;
+        vtg_cell *dc = cdev ? cells : (vtg_cell *)(base + up256(2 * sizeof(DevPyr)));
+        TRY(cudaMemcpyAsync(dp, h, sizeof(h), cudaMemcpyHostToDevice, g_c.stream));
+        TRY(vtg_launch_cells(dp, dp + 1, 0, lk_prm(lk, max_fb), gr, cur->w, cur->h, nullptr, dc, g_c.stream));
+        if (!cdev)
+            TRY(cudaMemcpyAsync(cells, dc, (size_t)gr.n * sizeof(vtg_cell), cudaMemcpyDeviceToHost, g_c.stream));
+        TRY(cudaStreamSynchronize(g_c.stream));
+        return VTG_OK;
+    }();
+}
+
+extern "C" long double tk_correlate_cuda(const struct vtg_ref_plane *pl, const float *app, long double norm, int x,
+                                         int y)
+{
+    enum { APP_W = 32, APP_H = 21 }; /* src/kern/track.c:21-22 */
+    std::lock_guard<std::mutex> g(g_c.mu);
+    float v = -1.0f;
+    t_status = [&]() -> int {
+        if (!plane_ok(pl) || !app)
+            return VTG_EINVAL;
+        /* search_at's bounds (track.c:187-188): no GPU work outside them */
+        if (x < 1 || y < 1 || x + APP_W >= pl->w - 1 || y + APP_H >= pl->h - 1)
+            return VTG_OK;
+        int rc = ready();
+        if (rc != VTG_OK)
+            return rc;
+        if (!g_c.ctx && (rc = vtg_ctx_create(g_c.device, 0, &g_c.ctx)) != VTG_OK)
+            return rc;
+        /* a plane in host memory: only the corner's window moves, one pixel around it and two past its far edges, so
+         * the corner is (1, 1) of a window where search_at's bounds hold as they do in the whole plane */
+        const bool pdev = on_device(pl->p);
+        const int ww = pdev ? pl->w : APP_W + 3, wh = pdev ? pl->h : APP_H + 3;
+        if (!g_c.search || g_c.sw < ww || g_c.sh < wh) {
+            if (g_c.search)
+                vtg_search_destroy(g_c.search);
+            g_c.search = nullptr;
+            if ((rc = vtg_search_create(g_c.ctx, max(ww, 64), max(wh, 64), APP_W, APP_H, &g_c.search)) != VTG_OK)
+                return rc;
+            g_c.sw = max(ww, 64);
+            g_c.sh = max(wh, 64);
+        }
+        if ((rc = vtg_search_template(g_c.search, app, APP_W, APP_H, (float)norm,
+                                      on_device(app) ? VTG_DEVICE : VTG_HOST, g_c.stream)) != VTG_OK)
+            return rc;
+        const float *plane = pl->p;
+        int pitch = pl->stride, cx = x, cy = y;
+        if (!pdev) {
+            char *base = nullptr;
+            if ((rc = scratch(up256((size_t)ww * wh * sizeof(float)), &base)) != VTG_OK)
+                return rc;
+            TRY(cudaMemcpy2DAsync(base, (size_t)ww * sizeof(float), pl->p + (size_t)(y - 1) * pl->stride + (x - 1),
+                                  (size_t)pl->stride * sizeof(float), (size_t)ww * sizeof(float), (size_t)wh,
+                                  cudaMemcpyHostToDevice, g_c.stream));
+            plane = (const float *)base;
+            pitch = ww;
+            cx = cy = 1;
+        }
+        if ((rc = vtg_correlate(g_c.search, plane, ww, wh, pitch, VTG_PLANE_F32, 1, &cx, &cy, &v, VTG_HOST,
+                                g_c.stream)) != VTG_OK)
+            return rc;
+        TRY(cudaStreamSynchronize(g_c.stream));
+        return VTG_OK;
+    }();
+    return t_status == VTG_OK ? (long double)v : -1.0L;
+}

@@ -445,3 +445,39 @@ def serve(ctx: Context, streams, frames, lk: Config, duration_s: float, max_batc
     st = ServeStats()
     check(L.vtg_serve_run(ctx.h, C.byref(cfg), C.byref(st)), "vtg_serve_run")
     return st.as_dict()
+
+
+# ---------------------------------------------------------------- the reference's kernel signatures (vtg_compat.h)
+
+class RefPlane(C.Structure):
+    """struct vtg_ref_plane: the reference's struct vt_plane (pixel (0, 0), w, h, stride in floats)."""
+    _fields_ = [("p", C.c_void_p), ("w", C.c_int), ("h", C.c_int), ("stride", C.c_int)]
+
+
+class RefLkCfg(C.Structure):
+    """struct vtg_ref_lk_cfg: the reference's struct lk_cfg."""
+    _fields_ = [("w", C.c_int), ("h", C.c_int), ("max_iter", C.c_int), ("eps", C.c_float), ("min_eig", C.c_float),
+                ("max_residual", C.c_float), ("prefetch", C.c_int)]
+
+
+def compat() -> C.CDLL:
+    """The library with the vtg_compat.h signatures set."""
+    L = lib()
+    if not getattr(L, "_compat_sigs", False):
+        P, PL, i, f, vp = C.POINTER(RefPlane), C.POINTER(RefPlane), C.c_int, C.c_float, C.c_void_p
+        L.lk_tile_bytes_cuda.restype = C.c_size_t
+        L.img_u8_to_q6_cuda.argtypes = [P, vp, i, i, i]
+        L.img_u8_to_q6_cuda.restype = None
+        L.img_reduce_cuda.argtypes = [P, P, i, i]
+        L.img_reduce_cuda.restype = None
+        L.lk_track_cuda.argtypes = [PL, PL, i, C.POINTER(RefLkCfg), f, f, f, f, vp, vp]
+        L.lk_track_cuda.restype = None
+        L.lk_flowback_cuda.argtypes = [PL, PL, i, C.POINTER(RefLkCfg), f, f, f, vp, vp]
+        L.lk_flowback_cuda.restype = None
+        L.still_vectors_cuda.argtypes = [P, P, C.POINTER(RefLkCfg), f, vp, i, i]
+        L.still_vectors_cuda.restype = None
+        L.tk_correlate_cuda.argtypes = [P, vp, C.c_longdouble, i, i]
+        L.tk_correlate_cuda.restype = C.c_longdouble
+        L.vtg_compat_error.restype = C.c_int
+        L._compat_sigs = True
+    return L

@@ -16,7 +16,8 @@ def declared_functions():
     for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
         text = open(h).read()
         text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-        for m in re.finditer(r"\b(vtg_[a-z0-9_]+)\s*\(", text):
+        # the native entry points (vtg_*) and the reference-signature ones (*_cuda, vtg_compat.h)
+        for m in re.finditer(r"\b(vtg_[a-z0-9_]+|[a-z0-9_]+_cuda)\s*\(", text):
             names.add(m.group(1))
     return sorted(names)
 
@@ -24,6 +25,8 @@ def declared_functions():
 def test_headers_declare_entry_points():
     names = declared_functions()
     assert "vtg_build" in names and "vtg_cells" in names and "vtg_points" in names
+    assert {"img_u8_to_q6_cuda", "img_reduce_cuda", "lk_track_cuda", "lk_flowback_cuda", "lk_tile_bytes_cuda",
+            "still_vectors_cuda", "tk_correlate_cuda"} <= set(names)
 
 
 def test_library_exports_every_declared_symbol(vtg_lib):
