@@ -158,6 +158,10 @@ int vtg_batch_prepare(vtg_batch *b, int slot, int n, vtg_tracker *const *tracker
 /* Runs a prepared step: the batched pyramid launches, then one LK launch over every stream's cells. Results stay in
  * each tracker (vtg_tracker_results). */
 int vtg_batch_launch(vtg_batch *b, int slot, void *stream);
+/* The same, with the steps that wrote these trackers' pyramid sets and results before still in flight on other
+ * streams: host frames are uploaded at once (each set has its own staging buffer), then the kernels wait for the
+ * `nwait` CUDA events (cudaEvent_t) recorded after those steps. */
+int vtg_batch_launch_after(vtg_batch *b, int slot, void *stream, int nwait, void *const *events);
 /* Captures a prepared step into a CUDA graph, and replays it. */
 int vtg_batch_capture(vtg_batch *b, int slot);
 int vtg_batch_replay(vtg_batch *b, int slot, void *stream);

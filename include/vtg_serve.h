@@ -36,6 +36,9 @@ struct vtg_serve_cfg {
     float ncc_share;       /* share of frame pairs followed by an appearance search on their level 1 */
     int plain;             /* 1: the plain form, one frame pair at a time in arrival order, no batching */
     uint64_t seed;
+    /* optional (NULL, or NULL entries): per stream, host memory for its cols x rows cell records, which receives the
+     * results of each of its frame pairs as it completes, so it ends with its last one's */
+    struct vtg_cell *const *last_cells;
 };
 
 struct vtg_serve_stats {

@@ -197,8 +197,9 @@ static void layout(const vtg_config *c, Layout *L)
     L->cols = (fw + (int)c->cell_w - 1) / (int)c->cell_w;
     L->rows = (fh + (int)c->cell_h - 1) / (int)c->cell_h;
     size_t b = 2 * off * sizeof(float);
+    /* one staging buffer a set: a frame's upload never waits for the previous frame's pyramid to finish reading */
     L->staging_off = b;
-    b += up256((size_t)c->width * c->height);
+    b += 2 * up256((size_t)c->width * c->height);
     L->desc_off = b;
     b += up256(4 * sizeof(DevPyr));
     L->lk_off = b;
@@ -291,6 +292,7 @@ extern "C" int vtg_tracker_create(vtg_ctx *ctx, const vtg_config *cfg, vtg_track
     t->sets[0] = (float *)t->mem;
     t->sets[1] = (float *)t->mem + L.set_floats;
     t->staging = (uint8_t *)(t->mem + L.staging_off);
+    t->staging_set = up256((size_t)cfg->width * cfg->height);
     t->desc = (DevPyr *)(t->mem + L.desc_off);
     t->d_lk = (vtg_lk_out *)(t->mem + L.lk_off);
     t->d_cells = (vtg_cell *)(t->mem + L.cells_off);
@@ -384,8 +386,9 @@ extern "C" int vtg_build(vtg_tracker *t, int set, const uint8_t *frame, int stri
     const uint8_t *src = frame;
     int sstride = stride;
     if (where == VTG_HOST) {
-        CU(cudaMemcpy2DAsync(t->staging, (size_t)w, frame, (size_t)stride, (size_t)w, (size_t)h, cudaMemcpyHostToDevice, s));
-        src = t->staging;
+        uint8_t *stage = t->staging + (size_t)set * t->staging_set;
+        CU(cudaMemcpy2DAsync(stage, (size_t)w, frame, (size_t)stride, (size_t)w, (size_t)h, cudaMemcpyHostToDevice, s));
+        src = stage;
         sstride = w;
     }
     float *lv[VTG_MAX_LEVELS];

@@ -195,11 +195,12 @@ extern "C" int vtg_batch_prepare(vtg_batch *b, int slot, int n, vtg_tracker *con
         PyrJob &p = pj[(size_t)j];
         if (where == VTG_HOST) {
             sl.h_src.push_back(frames[j]);
-            sl.h_dst.push_back(t->staging);
+            uint8_t *stage = t->staging + (size_t)cur * t->staging_set;
+            sl.h_dst.push_back(stage);
             sl.h_stride.push_back(stride);
             sl.h_w.push_back(w);
             sl.h_h.push_back(h);
-            p.src = t->staging;
+            p.src = stage;
             p.stride = w;
         } else {
             p.src = frames[j];
@@ -281,11 +282,14 @@ extern "C" int vtg_batch_prepare(vtg_batch *b, int slot, int n, vtg_tracker *con
 }
 
 /* The tiles table is laid out with the prepared n; the batched pyramid launcher wants one row per level. */
-static int launch_slot(vtg_batch *b, BatchSlot &sl, cudaStream_t s)
+static int launch_slot(vtg_batch *b, BatchSlot &sl, cudaStream_t s, int nwait = 0, void *const *wait = nullptr)
 {
     for (size_t k = 0; k < sl.h_src.size(); k++)
         CU(cudaMemcpy2DAsync(sl.h_dst[k], (size_t)sl.h_w[k], sl.h_src[k], (size_t)sl.h_stride[k], (size_t)sl.h_w[k],
                              (size_t)sl.h_h[k], cudaMemcpyHostToDevice, s));
+    /* the uploads went to each frame's own set's staging buffer; the kernels reuse pyramid sets and result buffers */
+    for (int k = 0; k < nwait; k++)
+        CU(cudaStreamWaitEvent(s, (cudaEvent_t)wait[k], 0));
     CU(vtg_launch_pyramid_batch(sl.d_pyr, sl.d_tiles, sl.tiles, sl.njobs, sl.max_levels, s));
     CU(cudaMemsetAsync(sl.d_counter, 0, sizeof(int), s));
     LkTune t = b->tune;
@@ -299,6 +303,14 @@ extern "C" int vtg_batch_launch(vtg_batch *b, int slot, void *stream)
     if (!b || slot < 0 || slot >= BATCH_SLOTS || !b->slot[slot].ready)
         return VTG_EINVAL;
     return launch_slot(b, b->slot[slot], stream ? (cudaStream_t)stream : b->stream);
+}
+
+extern "C" int vtg_batch_launch_after(vtg_batch *b, int slot, void *stream, int nwait, void *const *events)
+{
+    if (!b || slot < 0 || slot >= BATCH_SLOTS || !b->slot[slot].ready || nwait < 0 || (nwait > 0 && !events))
+        return VTG_EINVAL;
+    CU(cudaSetDevice(vtg_ctx_device(b->ctx)));
+    return launch_slot(b, b->slot[slot], stream ? (cudaStream_t)stream : b->stream, nwait, events);
 }
 
 extern "C" int vtg_batch_capture(vtg_batch *b, int slot)

@@ -20,7 +20,8 @@ struct vtg_tracker {
     size_t bytes;
     char *mem;            /* the one allocation */
     float *sets[2];       /* pyramid sets */
-    uint8_t *staging;     /* a frame uploaded from the host */
+    uint8_t *staging;     /* frames uploaded from the host: one buffer per set, staging_set bytes apart */
+    size_t staging_set;
     DevPyr *desc;         /* [set][0: from level 0, 1: from flow_level] */
     vtg_lk_out *d_lk;     /* cells x lk_out */
     vtg_cell *d_cells;    /* cells x vt_cell */

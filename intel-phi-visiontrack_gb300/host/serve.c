@@ -51,10 +51,12 @@ struct req {
 
 struct sstate {
     vtg_tracker *t;
-    int admitted, waiting, finished, in_flight, cells, cols, rows;
+    int admitted, waiting, finished, cells, cols, rows;
+    int in_flight;              /* frame pairs on the GPU, at most one a slot */
+    int last_slot;              /* the slot that holds its latest one */
     int first, count, next;     /* this stream's requests in the sorted list: pending from `next` */
     int done;                   /* served */
-    struct vtg_cell *host_cells;
+    struct vtg_cell *host_cells[SERVE_SLOTS]; /* results, one buffer a slot */
     size_t bytes;
 };
 
@@ -97,11 +99,17 @@ static int admit(vtg_ctx *ctx, const struct vtg_serve_cfg *c, struct sstate *st,
         return rc;
     vtg_tracker_cells(st[s].t, &st[s].cols, &st[s].rows);
     st[s].cells = st[s].cols * st[s].rows;
-    if (cudaHostAlloc((void **)&st[s].host_cells, sizeof(struct vtg_cell) * (size_t)st[s].cells, cudaHostAllocDefault) != cudaSuccess) {
-        vtg_tracker_destroy(st[s].t);
-        st[s].t = NULL;
-        return VTG_ENOMEM;
-    }
+    for (int k = 0; k < c->inflight; k++)
+        if (cudaHostAlloc((void **)&st[s].host_cells[k], sizeof(struct vtg_cell) * (size_t)st[s].cells,
+                          cudaHostAllocDefault) != cudaSuccess) {
+            for (int j = 0; j < k; j++) {
+                cudaFreeHost(st[s].host_cells[j]);
+                st[s].host_cells[j] = NULL;
+            }
+            vtg_tracker_destroy(st[s].t);
+            st[s].t = NULL;
+            return VTG_ENOMEM;
+        }
     rc = vtg_build(st[s].t, 0, c->frames[2 * s], (int)g.width, VTG_HOST, NULL);
     if (rc == VTG_OK)
         rc = vtg_ctx_sync(ctx, 10000);
@@ -116,10 +124,11 @@ static void retire(struct sstate *st, int s)
         vtg_tracker_destroy(st[s].t);
         st[s].t = NULL;
     }
-    if (st[s].host_cells) {
-        cudaFreeHost(st[s].host_cells);
-        st[s].host_cells = NULL;
-    }
+    for (int k = 0; k < SERVE_SLOTS; k++)
+        if (st[s].host_cells[k]) {
+            cudaFreeHost(st[s].host_cells[k]);
+            st[s].host_cells[k] = NULL;
+        }
     st[s].finished = 1;
 }
 
@@ -249,7 +258,9 @@ int vtg_serve_run(vtg_ctx *ctx, const struct vtg_serve_cfg *c, struct vtg_serve_
                 r->t_done = td;
                 lat[served++] = 1e3 * (td - r->t_arrive);
                 struct sstate *ss = &st[r->stream];
-                ss->in_flight = 0;
+                if (c->last_cells && c->last_cells[r->stream])
+                    memcpy(c->last_cells[r->stream], ss->host_cells[k], sizeof(struct vtg_cell) * (size_t)ss->cells);
+                ss->in_flight--;
                 ss->done++;
                 cells += ss->cells;
                 if (ss->done == ss->count)
@@ -266,14 +277,17 @@ int vtg_serve_run(vtg_ctx *ctx, const struct vtg_serve_cfg *c, struct vtg_serve_
             if (sl[k].busy)
                 continue;
             int m = 0;
-            /* the oldest arrived frame of each stream with nothing in flight, oldest first */
+            unsigned wait_slots = 0; /* slots holding the previous frame of a stream in this batch */
+            /* the oldest arrived frame of each stream with a slot to spare, oldest first. A stream's next frame may
+             * go to one slot while its previous one is on the GPU in another: the new step then waits on the GPU
+             * for that slot's work (its pyramid set and result buffers are reused), with no host round trip. */
             for (int pass = 0; pass < 1; pass++) {
                 for (;;) {
                     int best = -1;
                     double bt = 1e300;
                     for (int s = 0; s < ns; s++) {
                         struct sstate *ss = &st[s];
-                        if (!ss->admitted || ss->finished || ss->in_flight || ss->next >= ss->count)
+                        if (!ss->admitted || ss->finished || ss->in_flight >= c->inflight || ss->next >= ss->count)
                             continue;
                         const struct req *r = &rq[order[ss->first + ss->next]];
                         if (r->t_arrive > now || r->t_arrive >= bt)
@@ -291,6 +305,8 @@ int vtg_serve_run(vtg_ctx *ctx, const struct vtg_serve_cfg *c, struct vtg_serve_
                     struct sstate *ss = &st[best];
                     const int ri = order[ss->first + ss->next];
                     const int kk = rq[ri].k;
+                    if (ss->in_flight)
+                        wait_slots |= 1u << ss->last_slot;
                     stream_of[m] = best;
                     sl[k].reqs[m] = ri;
                     tr[m] = ss->t;
@@ -304,18 +320,28 @@ int vtg_serve_run(vtg_ctx *ctx, const struct vtg_serve_cfg *c, struct vtg_serve_
             if (m == 0)
                 break;
             cudaStream_t bs = (cudaStream_t)vtg_batch_stream(sl[k].b);
+            void *waits[SERVE_SLOTS];
+            int nw = 0;
+            for (int j = 0; j < c->inflight; j++)
+                if (wait_slots >> j & 1u)
+                    waits[nw++] = (void *)sl[j].ev;
             if (c->plain) {
                 /* one launch set per frame pair, no batching: vtg_build + vtg_cells on the batch's stream */
                 const int s = stream_of[0];
-                rc = vtg_build(tr[0], cur[0], fr[0], (int)c->streams[s].width, VTG_HOST, bs);
+                for (int j = 0; j < nw && rc == VTG_OK; j++)
+                    if (cudaStreamWaitEvent(bs, (cudaEvent_t)waits[j], 0) != cudaSuccess)
+                        rc = VTG_ECUDA;
                 if (rc == VTG_OK)
-                    rc = vtg_cells(tr[0], cur[0] ^ 1, cur[0], st[s].host_cells, NULL, VTG_HOST, bs);
+                    rc = vtg_build(tr[0], cur[0], fr[0], (int)c->streams[s].width, VTG_HOST, bs);
+                if (rc == VTG_OK)
+                    rc = vtg_cells(tr[0], cur[0] ^ 1, cur[0], st[s].host_cells[k], NULL, VTG_HOST, bs);
             } else {
                 rc = vtg_batch_prepare(sl[k].b, 0, m, tr, fr, NULL, VTG_HOST, cur);
+                /* the uploads overlap the other slot's step; the kernels wait for it on the GPU */
                 if (rc == VTG_OK)
-                    rc = vtg_batch_launch(sl[k].b, 0, NULL);
+                    rc = vtg_batch_launch_after(sl[k].b, 0, NULL, nw, waits);
                 for (int i = 0; i < m && rc == VTG_OK; i++)
-                    rc = vtg_tracker_results(tr[i], st[stream_of[i]].host_cells, NULL, VTG_HOST, bs);
+                    rc = vtg_tracker_results(tr[i], st[stream_of[i]].host_cells[k], NULL, VTG_HOST, bs);
             }
             for (int i = 0; i < m && rc == VTG_OK; i++) {
                 if (sl[k].s && urand(&seed) < (double)c->ncc_share) {
@@ -330,7 +356,8 @@ int vtg_serve_run(vtg_ctx *ctx, const struct vtg_serve_cfg *c, struct vtg_serve_
                     ncc++;
                     (void)s;
                 }
-                st[stream_of[i]].in_flight = 1;
+                st[stream_of[i]].in_flight++;
+                st[stream_of[i]].last_slot = k;
                 st[stream_of[i]].next++;
             }
             if (rc == VTG_OK && cudaEventRecord(sl[k].ev, bs) != cudaSuccess)

@@ -419,7 +419,8 @@ class ServeStream(C.Structure):
 class ServeCfg(C.Structure):
     _fields_ = [("nstreams", C.c_int), ("streams", C.POINTER(ServeStream)), ("frames", C.POINTER(C.c_void_p)),
                 ("lk", Config), ("duration_s", C.c_double), ("max_batch", C.c_int), ("inflight", C.c_int),
-                ("hbm_budget", C.c_size_t), ("ncc_share", C.c_float), ("plain", C.c_int), ("seed", C.c_uint64)]
+                ("hbm_budget", C.c_size_t), ("ncc_share", C.c_float), ("plain", C.c_int), ("seed", C.c_uint64),
+                ("last_cells", C.POINTER(C.c_void_p))]
 
 
 class ServeStats(C.Structure):
@@ -433,15 +434,20 @@ class ServeStats(C.Structure):
 
 
 def serve(ctx: Context, streams, frames, lk: Config, duration_s: float, max_batch: int = 64, inflight: int = 2,
-          hbm_budget: int = 0, ncc_share: float = 0.0, plain: bool = False, seed: int = 1) -> dict:
+          hbm_budget: int = 0, ncc_share: float = 0.0, plain: bool = False, seed: int = 1, last_cells=None) -> dict:
     """Runs vtg_serve_run. streams: dicts (width, height, flow_level, fps, start_s, frames); frames: two host
-    addresses per stream (pinned uint8 buffers, width bytes a row)."""
+    addresses per stream (pinned uint8 buffers, width bytes a row); last_cells: optional list of CELL_DTYPE arrays
+    (cols x rows each, or None) that end with each stream's last frame pair's cells."""
     L = lib()
     L.vtg_serve_run.argtypes = [C.c_void_p, C.POINTER(ServeCfg), C.POINTER(ServeStats)]
     ss = (ServeStream * len(streams))(*[ServeStream(s["width"], s["height"], s.get("flow_level", 0), s["fps"],
                                                      s.get("start_s", 0.0), s["frames"]) for s in streams])
     fp = (C.c_void_p * len(frames))(*frames)
-    cfg = ServeCfg(len(streams), ss, fp, lk, duration_s, max_batch, inflight, hbm_budget, ncc_share, int(plain), seed)
+    lc = None
+    if last_cells is not None:
+        lc = (C.c_void_p * len(streams))(*[None if a is None else a.ctypes.data for a in last_cells])
+    cfg = ServeCfg(len(streams), ss, fp, lk, duration_s, max_batch, inflight, hbm_budget, ncc_share, int(plain), seed,
+                   lc)
     st = ServeStats()
     check(L.vtg_serve_run(ctx.h, C.byref(cfg), C.byref(st)), "vtg_serve_run")
     return st.as_dict()

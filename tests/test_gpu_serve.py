@@ -46,3 +46,35 @@ def test_serve_admission_waits_for_memory(vtg_lib, ctx):
     streams = [dict(width=1920, height=1080, fps=200.0, start_s=0.0, frames=10) for _ in sizes]
     st = vtg_lib.serve(ctx, streams, [b.data_ptr() for b in bufs], lk, duration_s=1.0, hbm_budget=2 * one + 1024)
     assert st["served"] == 40 and st["streams_admitted"] == 4 and st["streams_waited"] >= 2
+
+
+@pytest.mark.parametrize("plain", [False, True])
+def test_serve_results_same_alone_and_in_mix(vtg_lib, ctx, plain):
+    """Each stream's results from the served loop are the bits its own tracker gives alone. The loop batches the
+    streams together and pipelines each stream's consecutive frame pairs across the two slots (the later one waits
+    on the GPU for the earlier one), so this holds the batching and that ordering to the single-stream result."""
+    import numpy as np
+
+    sizes = [(640, 480), (1280, 720), (1920, 1080), (960, 544)]
+    flow = [1 if w == 1920 else 0 for w, _ in sizes]
+    bufs = _frames(sizes)
+    streams = [dict(width=w, height=h, flow_level=fl, fps=2000.0, start_s=0.0, frames=12)
+               for (w, h), fl in zip(sizes, flow)]
+    last = []
+    for (w, h), fl in zip(sizes, flow):
+        t = vtg_lib.Tracker(ctx, vtg_lib.config(w, h, levels=4, flow_level=fl))
+        last.append(np.zeros(t.cols * t.rows, vtg_lib.CELL_DTYPE))
+        t.close()
+    lk = vtg_lib.config(64, 64, levels=4)
+    st = vtg_lib.serve(ctx, streams, [b.data_ptr() for b in bufs], lk, duration_s=1.0, plain=plain, last_cells=last)
+    assert st["served"] == 48
+    if not plain:
+        assert st["mean_batch"] > 1.0
+    for k, ((w, h), fl) in enumerate(zip(sizes, flow)):
+        # the 12th pair: frame 1 in set 1 (from the 11th pair), frame 0 rebuilt into set 0, cells from set 1 to set 0
+        t = vtg_lib.Tracker(ctx, vtg_lib.config(w, h, levels=4, flow_level=fl))
+        t.build(1, bufs[2 * k + 1].numpy())
+        t.build(0, bufs[2 * k].numpy())
+        cells, _ = t.cells(1, 0)
+        t.close()
+        assert np.array_equal(cells.view(np.uint8), last[k].view(np.uint8)), (w, h)
