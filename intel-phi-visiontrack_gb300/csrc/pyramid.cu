@@ -22,6 +22,19 @@
 #define SF_X 136
 #define SF_P 140 /* int row pitch of staged F32 values and of the vertical sums: 16-byte aligned rows */
 
+/* A whole number 0 <= v < 2^23 as a float without a conversion instruction: the bits of 2^23 + v, less 2^23. */
+__device__ __forceinline__ float small_int_to_float(int v)
+{
+    return __int_as_float(0x4B000000 | v) - 8388608.0f;
+}
+
+/* Byte e of w times 64 (a Q6 value) as a float: the byte placed in the mantissa of 2^23 by one byte permute, then
+ * (2^23 + b) x 64 - 2^29 = 64 b in one fused multiply-add, exact (2^29 + 64 b is a multiple of 64 below 2^30). */
+__device__ __forceinline__ float q6_of(uint32_t w, int e)
+{
+    return __fmaf_rn(__int_as_float((int)__byte_perm(w, 0x4Bu, 0x4550u + (unsigned)e)), 64.0f, -536870912.0f);
+}
+
 /* One 64 x 16 tile of the output level at (ox, oy). With FROM_U8 the source is the frame's bytes (rows `spitch`
  * bytes apart), level 0 (byte x 64) is written from the same staged bytes, and the sums run on the bytes:
  * (64 h + 128) >> 8 = (h + 2) >> 2 exactly. Otherwise the source is level L - 1 (F32 Q6, whole numbers) and the result
@@ -68,8 +81,7 @@ __device__ __forceinline__ void reduce_tile(const void *__restrict__ src_, int s
             if (gy >= sh || gx >= sw)
                 continue;
             const uint32_t w = *reinterpret_cast<const uint32_t *>(&s_b[r + 2][16 + 4 * g]);
-            const float4 f = make_float4((float)(64u * (w & 255u)), (float)(64u * ((w >> 8) & 255u)),
-                                         (float)(64u * ((w >> 16) & 255u)), (float)(64u * (w >> 24)));
+            const float4 f = make_float4(q6_of(w, 0), q6_of(w, 1), q6_of(w, 2), q6_of(w, 3));
             float *d = l0 + (size_t)gy * l0pitch + gx;
             if (gx + 4 <= sw) {
                 *reinterpret_cast<float4 *>(d) = f;
@@ -113,21 +125,22 @@ __device__ __forceinline__ void reduce_tile(const void *__restrict__ src_, int s
             else
                 v = make_float4(__ldg(row + min(max(gx, 0), sw - 1)), __ldg(row + min(max(gx + 1, 0), sw - 1)),
                                 __ldg(row + min(max(gx + 2, 0), sw - 1)), __ldg(row + min(max(gx + 3, 0), sw - 1)));
-            *reinterpret_cast<int4 *>(&s_f[r][4 * k]) = make_int4((int)v.x, (int)v.y, (int)v.z, (int)v.w);
+            *reinterpret_cast<float4 *>(&s_f[r][4 * k]) = v;
         }
         __syncthreads();
         for (int i = tid; i < RT_Y * (SF_X / 4); i += blockDim.x) {
             const int r = i / (SF_X / 4), g = i - r * (SF_X / 4);
-            int4 t[5];
+            /* F32 as the reference sums: whole numbers below 2^24, so every sum is exact */
+            float4 t[5];
 #pragma unroll
             for (int q = 0; q < 5; q++)
-                t[q] = *reinterpret_cast<const int4 *>(&s_f[2 * r + q][4 * g]);
-            int4 o;
-            o.x = t[0].x + t[4].x + 4 * (t[1].x + t[3].x) + 6 * t[2].x;
-            o.y = t[0].y + t[4].y + 4 * (t[1].y + t[3].y) + 6 * t[2].y;
-            o.z = t[0].z + t[4].z + 4 * (t[1].z + t[3].z) + 6 * t[2].z;
-            o.w = t[0].w + t[4].w + 4 * (t[1].w + t[3].w) + 6 * t[2].w;
-            *reinterpret_cast<int4 *>(&s_v[r][4 * g]) = o;
+                t[q] = *reinterpret_cast<const float4 *>(&s_f[2 * r + q][4 * g]);
+            float4 o;
+            o.x = t[0].x + t[4].x + 4.0f * (t[1].x + t[3].x) + 6.0f * t[2].x;
+            o.y = t[0].y + t[4].y + 4.0f * (t[1].y + t[3].y) + 6.0f * t[2].y;
+            o.z = t[0].z + t[4].z + 4.0f * (t[1].z + t[3].z) + 6.0f * t[2].z;
+            o.w = t[0].w + t[4].w + 4.0f * (t[1].w + t[3].w) + 6.0f * t[2].w;
+            *reinterpret_cast<float4 *>(&s_v[r][4 * g]) = o;
         }
     }
     __syncthreads();
@@ -145,8 +158,14 @@ __device__ __forceinline__ void reduce_tile(const void *__restrict__ src_, int s
 #pragma unroll
         for (int e = 0; e < 4; e++) {
             const int c = 2 * e + 4;
-            const int h = v[c - 2] + v[c + 2] + 4 * (v[c - 1] + v[c + 1]) + 6 * v[c];
-            o[e] = (float)(FROM_U8 ? (h + 2) >> 2 : (h + 128) >> 8);
+            if (FROM_U8) {
+                const int h = v[c - 2] + v[c + 2] + 4 * (v[c - 1] + v[c + 1]) + 6 * v[c];
+                o[e] = small_int_to_float((h + 2) >> 2);
+            } else {
+                const float *f = reinterpret_cast<const float *>(v);
+                const float h = f[c - 2] + f[c + 2] + 4.0f * (f[c - 1] + f[c + 1]) + 6.0f * f[c];
+                o[e] = floorf((h + 128.0f) * (1.0f / 256.0f)); /* (h + 128) >> 8, exact */
+            }
         }
         float *d = dst + (size_t)gy * dpitch + gx;
         if (gx + 4 <= dw) {
