@@ -186,6 +186,7 @@ def time_batched_mix(vtg, torch, ctx, device: str, nstreams: int = 64, steps: in
     batch.launch(1)
     ctx.sync()
     cells = batch.cells(1)
+    default_tune = batch.get_tune()
     tuned, tuned_ms, default_ms = batch.autotune(1, reps=5)
     batch.capture(0)
     batch.capture(1)
@@ -207,7 +208,7 @@ def time_batched_mix(vtg, torch, ctx, device: str, nstreams: int = 64, steps: in
             "cells_per_step": cells, "frames": steps, "cells_per_s": cells * steps / (ms.sum() / 1e3),
             "ms_per_step": float(ms.mean()), "p50_ms_per_step": float(np.percentile(ms, 50)),
             "p99_ms_per_step": float(np.percentile(ms, 99)),
-            "autotune": {"chosen": tuned, "chosen_ms": tuned_ms, "default_ms": default_ms}}
+            "autotune": {"chosen": tuned, "chosen_ms": tuned_ms, "default": default_tune, "default_ms": default_ms}}
 
 
 def run_ours(args) -> dict | None:
@@ -244,6 +245,7 @@ def run_ours(args) -> dict | None:
     batch.launch(0)
     batch.launch(1)
     ctx.sync()
+    default_tune = batch.get_tune()
     tuned, tuned_ms, default_ms = batch.autotune(1, reps=5)
     batch.capture(0)
     batch.capture(1)
@@ -348,7 +350,7 @@ def run_ours(args) -> dict | None:
             "p50_ms_per_step": float(np.percentile(step_ms, 50)), "p99_ms_per_step": float(np.percentile(step_ms, 99)),
             "plain": plain, "batched_vs_plain": value / plain["value"],
             "autotune": {"chosen": tuned, "chosen_ms": tuned_ms, "default_ms": default_ms,
-                         "default": {"block_warps": 8, "chunk": 1, "persistent": 1, "ctas_per_sm": 2, "tsmem": 0}},
+                         "default": default_tune},
             "e2e": e2e, "e2e_plain": e2e_plain, "e2e_vs_plain": e2e["value"] / max(e2e_plain["value"], 1e-9),
             "e2e_latency": e2e_latency, "batched_mix64": mix64,
             "served_mix": {"served": {k: mixed[k] for k in ("cells_per_s", "p50_ms", "p99_ms", "mean_batch", "ncc",

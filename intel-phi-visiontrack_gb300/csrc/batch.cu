@@ -66,7 +66,7 @@ static size_t slot_bytes(int max_jobs)
            up256(sizeof(LkJob) * (size_t)max_jobs) + up256(sizeof(int) * (size_t)(max_jobs + 1)) + 256;
 }
 
-static const LkTune k_default_tune = {8, 1, 1, 2};
+static const LkTune k_default_tune = {16, 2, 1, 1, 1};
 
 #define CU(call)                                                                                                       \
     do {                                                                                                               \
@@ -353,7 +353,7 @@ extern "C" int vtg_batch_set_tune(vtg_batch *b, const struct vtg_tune *t)
     if (!b || !t || (t->block_warps != 4 && t->block_warps != 8 && t->block_warps != 16) || t->chunk < 1 ||
         t->chunk > 64 || t->ctas_per_sm < 1 || t->ctas_per_sm > 8)
         return VTG_EINVAL;
-    if (t->tsmem && (!t->persistent || t->block_warps == 16 || t->ctas_per_sm > (t->block_warps == 4 ? 5 : 3)))
+    if (t->tsmem && (!t->persistent || t->ctas_per_sm > (t->block_warps == 4 ? 5 : t->block_warps == 8 ? 3 : 1)))
         return VTG_EINVAL;
     std::lock_guard<std::mutex> g(b->mu);
     b->tune.block_warps = t->block_warps;
@@ -420,6 +420,7 @@ extern "C" int vtg_batch_autotune(vtg_batch *b, int slot, int reps, struct vtg_t
     for (int chunk : {1, 2, 4}) {
         cands.push_back({4, chunk, 1, 5, 1});
         cands.push_back({8, chunk, 1, 3, 1});
+        cands.push_back({16, chunk, 1, 1, 1});
     }
     cudaEvent_t e0, e1;
     CU(cudaEventCreate(&e0));

@@ -18,6 +18,8 @@
  * offset from it (the sub-pixel phase of the level's start plus the flow so far), so the bilinear phase keeps ~1e-6 px
  * of precision at any picture size; the determinant is formed by Kahan's fused-multiply-add product difference, and the
  * smaller eigenvalue as det / lambda_max, so neither cancels. No FP64 anywhere. */
+#include <limits.h>
+
 #include "vtg_internal.cuh"
 
 #define LK_GRAD_SCALE (1.0f / 512.0f)
@@ -146,11 +148,17 @@ __device__ __forceinline__ f2_t hlerp2(const float *pa, const float *pb, f2_t FX
     return f2_fma(f2_sub(n, l), FX, l);
 }
 
-/* build: the window of I around pixel (ix + fx, iy + fy); T, Tx, Ty into the patch; the tensor's sums.
- * EXACT: the patch height is MAXH at compile time (no row guards); otherwise rows past H are zero in the patch. */
+/* build: the window of I around pixel (ix + fx, iy + fy); T, Tx, Ty into the patch; the tensor's sums; tc (the
+ * patch's centre value on its first row) and C = sum (T - tc) Tx, sum (T - tc) Ty for the correlation below.
+ * S row s is the bilinear row between image rows y0 + s and y0 + s + 1; patch row k takes its Sobel from S rows k - 1,
+ * k, k + 1. The top half (rows 0 .. HH - 1, S rows -1 .. HH) and the bottom half (rows HH .. 2 HH - 1, S rows HH - 1
+ * .. 2 HH) run as the two halves of packed pairs, each with its own three-row window, so each pair of rows lands in
+ * the patch's pair register directly; an odd height's last row continues the bottom half. Not EXACT: rows from H on
+ * read the last image row again and are zero in Tx, Ty. */
 template <int MAXH, bool EXACT, bool TS>
 __device__ __forceinline__ void lk_build(const DevLevel &L, int ix, float fx, int iy, float fy, int W, int Hr, int lane,
-                                         Patch<MAXH, TS> &P, float &gxx, float &gxy, float &gyy)
+                                         Patch<MAXH, TS> &P, float &gxx, float &gxy, float &gyy, float &tco,
+                                         float &cxo, float &cyo)
 {
     constexpr int HH = MAXH / 2;
     const int H = EXACT ? MAXH : Hr;
@@ -159,76 +167,202 @@ __device__ __forceinline__ void lk_build(const DevLevel &L, int ix, float fx, in
      * it read a clamped column and feed nothing). Patch columns are lanes 1 .. W; the others' sums are dropped before
      * the fold. */
     const bool act = lane >= 1 && lane <= W;
-    const float *row = L.p + (size_t)(y0 - 1) * L.pitch + (x0 - 1 + min(lane, W + 2));
-    float prev = hlerp(row, fx);
-    /* S rows r - 2, r - 1, r: values, and their x + 1 minus x - 1 differences (shared by three patch rows) */
-    float u = 0.f, ul = 0.f, ur = 0.f, m = 0.f, ml = 0.f, mr = 0.f, mdx = 0.f, udx = 0.f;
-    float sxx0 = 0.f, sxy0 = 0.f, syy0 = 0.f, sxx1 = 0.f, sxy1 = 0.f, syy1 = 0.f;
-    /* the top half's rows, held until their bottom-half partner is made */
-    float ht[HH], htx[HH], hty[HH];
+    const float *col = L.p + (x0 - 1 + min(lane, W + 2));
+    /* image row y0 + r, r in -1 .. H + 1 (rows past that are read as row H + 1) */
+    auto img = [&](int r) { return col + (size_t)(y0 + (EXACT ? r : min(r, H + 1))) * L.pitch; };
+    const f2_t FX = f2_pack(fx, fx), FY = f2_pack(fy, fy), TWO = f2_pack(2.0f, 2.0f);
+    const float *pa = img(-1), *pb = img(HH - 1);
+    f2_t prev = hlerp2(pa, pb, FX);
+    /* S rows k - 1, k, k + 1 of each half: values, and their x + 1 minus x - 1 differences */
+    f2_t u = 0ull, ul = 0ull, ur = 0ull, m = 0ull, ml = 0ull, mr = 0ull, mdx = 0ull, udx = 0ull;
+    f2_t sxx = 0ull, sxy = 0ull, syy = 0ull, scx = 0ull, scy = 0ull, TC = 0ull;
+    float tc = 0.0f;
 #pragma unroll
-    for (int k = 0; k < HH; k++)
-        ht[k] = htx[k] = hty[k] = 0.0f;
-#pragma unroll
-    for (int r = 0; r < MAXH + 2; r++) {
-        if (EXACT || r < H + 2) {
-            row += L.pitch;
-            const float cur = hlerp(row, fx);
-            const float d = __fmaf_rn(cur - prev, fy, prev);
+    for (int t = 0; t < HH + 2; t++) {
+        if (EXACT || t < H + 2) {
+            if (EXACT) {
+                pa += L.pitch;
+                pb += L.pitch;
+            } else {
+                pa = img(t);
+                pb = img(HH + t);
+            }
+            const f2_t cur = hlerp2(pa, pb, FX);
+            const f2_t d = f2_fma(f2_sub(cur, prev), FY, prev);
             prev = cur;
-            const float dl = __shfl_up_sync(VTG_FULL, d, 1), dr = __shfl_down_sync(VTG_FULL, d, 1);
-            const float ddx = dr - dl;
-            if (r >= 2) {
-                const int k = r - 2;
-                const float tx = __fmaf_rn(mdx, 2.0f, udx + ddx);
-                const float ty = __fmaf_rn(d - u, 2.0f, (dl - ul) + (dr - ur));
-                if (k < HH) {
-                    ht[k] = m;
-                    htx[k] = tx;
-                    hty[k] = ty;
-                } else if (k < 2 * HH) {
-                    put_t(P, k - HH, lane, f2_pack(ht[k - HH], m));
-                    P.tx[k - HH] = f2_pack(htx[k - HH], tx);
-                    P.ty[k - HH] = f2_pack(hty[k - HH], ty);
-                } else {
-                    P.tl = m;
-                    P.txl = tx;
-                    P.tyl = ty;
+            float dlo, dhi;
+            f2_split(d, dlo, dhi);
+            const f2_t dl = f2_pack(__shfl_up_sync(VTG_FULL, dlo, 1), __shfl_up_sync(VTG_FULL, dhi, 1));
+            const f2_t dr = f2_pack(__shfl_down_sync(VTG_FULL, dlo, 1), __shfl_down_sync(VTG_FULL, dhi, 1));
+            const f2_t ddx = f2_sub(dr, dl);
+            if (t >= 2) {
+                const int k = t - 2; /* rows k and HH + k */
+                f2_t tx = f2_fma(mdx, TWO, f2_add(udx, ddx));
+                f2_t ty = f2_fma(f2_sub(d, u), TWO, f2_add(f2_sub(dl, ul), f2_sub(dr, ur)));
+                if (!EXACT) {
+                    const f2_t keep = f2_pack(k < H ? 1.0f : 0.0f, HH + k < H ? 1.0f : 0.0f);
+                    tx = f2_mul(tx, keep);
+                    ty = f2_mul(ty, keep);
                 }
-                if (r & 1) {
-                    sxx1 = __fmaf_rn(tx, tx, sxx1);
-                    sxy1 = __fmaf_rn(tx, ty, sxy1);
-                    syy1 = __fmaf_rn(ty, ty, syy1);
-                } else {
-                    sxx0 = __fmaf_rn(tx, tx, sxx0);
-                    sxy0 = __fmaf_rn(tx, ty, sxy0);
-                    syy0 = __fmaf_rn(ty, ty, syy0);
+                if (k == 0) {
+                    float mlo, mhi;
+                    f2_split(m, mlo, mhi);
+                    tc = __shfl_sync(VTG_FULL, mlo, W / 2 + 1);
+                    TC = f2_pack(tc, tc);
                 }
+                put_t(P, k, lane, m);
+                P.tx[k] = tx;
+                P.ty[k] = ty;
+                sxx = f2_fma(tx, tx, sxx);
+                sxy = f2_fma(tx, ty, sxy);
+                syy = f2_fma(ty, ty, syy);
+                const f2_t tt = f2_sub(m, TC);
+                scx = f2_fma(tt, tx, scx);
+                scy = f2_fma(tt, ty, scy);
             }
             u = m; ul = ml; ur = mr; udx = mdx;
             m = d; ml = dl; mr = dr; mdx = ddx;
         }
     }
-    if constexpr (!EXACT) {
-        /* rows H .. MAXH - 1 were not built: pair the top half's rows whose partner is missing with zeros */
-#pragma unroll
-        for (int k = 0; k < HH; k++) {
-            if (HH + k >= H) {
-                put_t(P, k, lane, f2_pack(ht[k], 0.0f));
-                P.tx[k] = f2_pack(htx[k], 0.0f);
-                P.ty[k] = f2_pack(hty[k], 0.0f);
-            }
-        }
-        if (H < MAXH)
+    float fxx = f2_sum(sxx), fxy = f2_sum(sxy), fyy = f2_sum(syy), fcx = f2_sum(scx), fcy = f2_sum(scy);
+    if constexpr ((MAXH & 1) != 0) {
+        /* the last row, 2 HH: one more step of the bottom half (S row 2 HH + 1, image rows H, H + 1) */
+        if (EXACT || H == MAXH) {
+            const float c1 = hlerp(EXACT ? pb + L.pitch : img(H + 1), fx);
+            const float p1 = f2_hi(prev);
+            const float d = __fmaf_rn(c1 - p1, fy, p1);
+            const float dl = __shfl_up_sync(VTG_FULL, d, 1), dr = __shfl_down_sync(VTG_FULL, d, 1);
+            const float tx = __fmaf_rn(f2_hi(mdx), 2.0f, f2_hi(udx) + (dr - dl));
+            const float ty = __fmaf_rn(d - f2_hi(u), 2.0f, (dl - f2_hi(ul)) + (dr - f2_hi(ur)));
+            const float mt = f2_hi(m);
+            P.tl = mt;
+            P.txl = tx;
+            P.tyl = ty;
+            fxx = __fmaf_rn(tx, tx, fxx);
+            fxy = __fmaf_rn(tx, ty, fxy);
+            fyy = __fmaf_rn(ty, ty, fyy);
+            fcx = __fmaf_rn(mt - tc, tx, fcx);
+            fcy = __fmaf_rn(mt - tc, ty, fcy);
+        } else {
             P.tl = P.txl = P.tyl = 0.0f;
+        }
+    }
+    if constexpr (!EXACT) {
+        /* rows the loop did not reach (t >= H + 2): zero */
+#pragma unroll
+        for (int k = 0; k < HH; k++)
+            if (k + 2 >= H + 2) {
+                P.tx[k] = 0ull;
+                P.ty[k] = 0ull;
+                put_t(P, k, lane, 0ull);
+            }
     }
     /* (Sobel / 512)^2 = Sobel^2 x 2^-18, exact */
-    float fxx = act ? sxx0 + sxx1 : 0.0f, fxy = act ? sxy0 + sxy1 : 0.0f, fyy = act ? syy0 + syy1 : 0.0f;
+    fxx = act ? fxx : 0.0f;
+    fxy = act ? fxy : 0.0f;
+    fyy = act ? fyy : 0.0f;
+    fcx = act ? fcx : 0.0f;
+    fcy = act ? fcy : 0.0f;
     warp_fold2(fxx, fxy);
-    fyy = warp_fold(fyy);
+    warp_fold2(fyy, fcx);
+    fcy = warp_fold(fcy);
     gxx = fxx * (LK_GRAD_SCALE * LK_GRAD_SCALE);
     gxy = fxy * (LK_GRAD_SCALE * LK_GRAD_SCALE);
     gyy = fyy * (LK_GRAD_SCALE * LK_GRAD_SCALE);
+    tco = tc;
+    cxo = fcx;
+    cyo = fcy;
+}
+
+/* iterate's sums for every sub-pixel phase at one whole-pixel position. Bilinear sampling is linear in J's four
+ * whole-pixel shifts, so with J' = J - tc,
+ *     sum (T - J(p + q)) Tx = C - [lerp_y(lerp_x(X00, X10, fx), lerp_x(X01, X11, fx), fy)],
+ *     X_ab = sum over the patch of J'(x0 + col + a, y0 + row + b) Tx,   C = sum (T - tc) Tx
+ * (the tc terms cancel, since the weights sum to 1). One pass over the window gives X for Tx (X[0..3]) and Ty
+ * (X[4..7]); every iteration that stays at the same whole pixel then needs only these eight numbers. Subtracting tc
+ * keeps the sums near the patch's contrast, not its brightness, so F32 rounding stays far below 1e-4 px. Rows as in
+ * lk_sample: the top and bottom halves of the patch as the two halves of packed pairs. */
+template <int MAXH, bool EXACT, bool TS>
+__device__ __forceinline__ void lk_correlate(const DevLevel &L, int jx, int jy, int W, int Hr, int lane,
+                                             const Patch<MAXH, TS> &P, float tc, float (&X)[8])
+{
+    constexpr int HH = MAXH / 2;
+    const int H = EXACT ? MAXH : Hr;
+    const int x0 = jx - W / 2, y0 = jy - H / 2;
+    const bool act = lane >= 1 && lane <= W;
+    const float *col = L.p + (size_t)y0 * L.pitch + (x0 - 1 + min(lane, W + 1));
+    const float *ra = col;
+    const float *rb = col + (size_t)(EXACT ? HH : min(HH, H)) * L.pitch;
+    const f2_t M = f2_pack(-tc, -tc);
+    /* a row pair: l = J' at this lane's column, n = J' at the next column (the next lane's l) */
+    auto load = [&](const float *pa, const float *pb, f2_t &l, f2_t &n) {
+        l = f2_add(f2_pack(__ldg(pa), __ldg(pb)), M);
+        float a, b;
+        f2_split(l, a, b);
+        n = f2_pack(__shfl_down_sync(VTG_FULL, a, 1), __shfl_down_sync(VTG_FULL, b, 1));
+    };
+    f2_t pl, pn;
+    load(ra, rb, pl, pn);
+    f2_t a00 = 0ull, a10 = 0ull, a01 = 0ull, a11 = 0ull, b00 = 0ull, b10 = 0ull, b01 = 0ull, b11 = 0ull;
+#pragma unroll
+    for (int r = 0; r < HH; r++) {
+        if (EXACT || r < H) {
+            ra += L.pitch;
+            if (EXACT)
+                rb += L.pitch;
+            else
+                rb = col + (size_t)min(HH + 1 + r, H) * L.pitch;
+            f2_t cl, cn;
+            load(ra, rb, cl, cn);
+            a00 = f2_fma(pl, P.tx[r], a00);
+            a10 = f2_fma(pn, P.tx[r], a10);
+            a01 = f2_fma(cl, P.tx[r], a01);
+            a11 = f2_fma(cn, P.tx[r], a11);
+            b00 = f2_fma(pl, P.ty[r], b00);
+            b10 = f2_fma(pn, P.ty[r], b10);
+            b01 = f2_fma(cl, P.ty[r], b01);
+            b11 = f2_fma(cn, P.ty[r], b11);
+            pl = cl;
+            pn = cn;
+        }
+    }
+    X[0] = f2_sum(a00);
+    X[1] = f2_sum(a10);
+    X[2] = f2_sum(a01);
+    X[3] = f2_sum(a11);
+    X[4] = f2_sum(b00);
+    X[5] = f2_sum(b10);
+    X[6] = f2_sum(b01);
+    X[7] = f2_sum(b11);
+    if constexpr ((MAXH & 1) != 0) {
+        if (EXACT || H == MAXH) {
+            /* the last row follows the bottom half: its previous row is the pairs' high halves */
+            const float l = __ldg(EXACT ? rb + L.pitch : col + (size_t)H * L.pitch) - tc;
+            const float n = __shfl_down_sync(VTG_FULL, l, 1);
+            const float ol = f2_hi(pl), on = f2_hi(pn);
+            X[0] = __fmaf_rn(ol, P.txl, X[0]);
+            X[1] = __fmaf_rn(on, P.txl, X[1]);
+            X[2] = __fmaf_rn(l, P.txl, X[2]);
+            X[3] = __fmaf_rn(n, P.txl, X[3]);
+            X[4] = __fmaf_rn(ol, P.tyl, X[4]);
+            X[5] = __fmaf_rn(on, P.tyl, X[5]);
+            X[6] = __fmaf_rn(l, P.tyl, X[6]);
+            X[7] = __fmaf_rn(n, P.tyl, X[7]);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 8; k++)
+        X[k] = act ? X[k] : 0.0f;
+#pragma unroll
+    for (int k = 0; k < 8; k += 2)
+        warp_fold2(X[k], X[k + 1]);
+}
+
+/* sum (T - J) T_grad at phase (fx, fy) from the correlation's four shifts and C, times the Sobel scale */
+__device__ __forceinline__ float lk_at_phase(const float *X, float C, float fx, float fy)
+{
+    const float r0 = __fmaf_rn(X[1] - X[0], fx, X[0]), r1 = __fmaf_rn(X[3] - X[2], fx, X[2]);
+    return (C - __fmaf_rn(r1 - r0, fy, r0)) * LK_GRAD_SCALE;
 }
 
 /* iterate (RESID = false): J at pixel (jx + fx, jy + fy); the sums of It Tx and It Ty.
@@ -340,8 +474,8 @@ __device__ __forceinline__ void lk_track(const DevPyr &I, const DevPyr &J, int t
         const float fpx = floorf(px), fpy = floorf(py);
         const int bx = (int)fpx, by = (int)fpy;
         const float rx = px - fpx, ry = py - fpy; /* exact */
-        float gxx, gxy, gyy;
-        lk_build<MAXH, EXACT, TS>(IL, bx, rx, by, ry, W, H, lane, P, gxx, gxy, gyy);
+        float gxx, gxy, gyy, tc, cx, cy;
+        lk_build<MAXH, EXACT, TS>(IL, bx, rx, by, ry, W, H, lane, P, gxx, gxy, gyy, tc, cx, cy);
         /* det = gxx gyy - gxy^2 by Kahan's product difference; the smaller eigenvalue as det / lambda_max. */
         const float w2 = gxy * gxy;
         const float e2 = __fmaf_rn(gxy, gxy, -w2);
@@ -374,6 +508,9 @@ __device__ __forceinline__ void lk_track(const DevPyr &I, const DevPyr &J, int t
         const float lo_x = (float)(mx - bx), lo_y = (float)(my - by);
         const float hi_x = (float)(JL.w - mx - 1 - bx), hi_y = (float)(JL.h - my - 1 - by);
         float vx = 0.0f, vy = 0.0f;
+        /* the correlation at the last whole pixel sampled (none yet on this level) */
+        float X[8];
+        int cjx = INT_MIN, cjy = INT_MIN;
         for (int it = 0; it < p.max_iter; it++) {
             const float qx = (rx + gx) + vx, qy = (ry + gy) + vy; /* offsets from (bx, by) */
             if (qx < lo_x || qy < lo_y || qx >= hi_x || qy >= hi_y) {
@@ -387,8 +524,12 @@ __device__ __forceinline__ void lk_track(const DevPyr &I, const DevPyr &J, int t
             float fx, fy;
             split(bx, qx, jx, fx);
             split(by, qy, jy, fy);
-            float sx, sy;
-            lk_sample<MAXH, EXACT, false, TS>(JL, jx, fx, jy, fy, W, H, lane, P, sx, sy);
+            if (jx != cjx || jy != cjy) {
+                lk_correlate<MAXH, EXACT, TS>(JL, jx, jy, W, H, lane, P, tc, X);
+                cjx = jx;
+                cjy = jy;
+            }
+            const float sx = lk_at_phase(X, cx, fx, fy), sy = lk_at_phase(X + 4, cy, fx, fy);
             const float ex = __fmaf_rn(ia, sx, ib * sy), ey = __fmaf_rn(ib, sx, ic * sy);
             vx += ex;
             vy += ey;
@@ -592,15 +733,23 @@ static cudaError_t lk_batch_launch(const LkJob *jobs, const int *item_start, int
     } while (0)
 #define LKT(WARPS, MINB)                                                                                               \
     do {                                                                                                               \
-        /* WARPS x (MAXH / 2) x 32 pairs: at most 30 KB, under the 48 KB that needs no opt-in */                      \
+        /* WARPS x (MAXH / 2) x 32 pairs: at most 60 KB (16 warps, MAXH 31) */                                       \
         const size_t smem = sizeof(f2_t) * WARPS * (MAXH / 2) * 32;                                                  \
+        if (smem > 48 * 1024) {                                                                                        \
+            const cudaError_t e = cudaFuncSetAttribute(lk_batch_kernel<MAXH, EXACT, true, WARPS, MINB, true>,          \
+                                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);        \
+            if (e != cudaSuccess)                                                                                      \
+                return e;                                                                                              \
+        }                                                                                                              \
         lk_batch_kernel<MAXH, EXACT, true, WARPS, MINB, true><<<sms * t.ctas_per_sm, WARPS * 32, smem, s>>>(          \
             jobs, item_start, njobs, items, t.chunk, p, counter);                                                      \
     } while (0)
     if (t.tsmem) {
-        /* the template's T in shared memory: fewer registers, more warps an SM */
+        /* the template's T in shared memory: fewer registers, or more warps an SM */
         if (t.block_warps == 4)
             LKT(4, 5);
+        else if (t.block_warps == 16)
+            LKT(16, 1);
         else
             LKT(8, 3);
     } else if (t.persistent) {

@@ -67,7 +67,7 @@ struct LkTune {
     int chunk;         /* cells per work item */
     int persistent;    /* 1: a grid of ctas_per_sm x SMs pulling items from a counter; 0: one warp per item */
     int ctas_per_sm;   /* for the persistent form */
-    int tsmem;         /* 1: the template's T in shared memory (persistent, 4 warps x <= 5 or 8 x <= 3 CTAs an SM) */
+    int tsmem;         /* 1: the template's T in shared memory (persistent; 4 warps x <= 5, 8 x <= 3 or 16 x 1 CTAs an SM) */
 };
 
 /* Launchers (pyramid.cu, lk.cu). All asynchronous on `s`; each returns a cudaError_t. */

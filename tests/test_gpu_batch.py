@@ -75,7 +75,8 @@ def test_batch_equals_single_streams(vtg_lib, ctx, batch_setup):
                                   dict(persistent=0, block_warps=16, chunk=2, ctas_per_sm=1, tsmem=0),
                                   dict(persistent=1, block_warps=16, chunk=8, ctas_per_sm=1, tsmem=0),
                                   dict(persistent=1, block_warps=4, chunk=2, ctas_per_sm=5, tsmem=1),
-                                  dict(persistent=1, block_warps=8, chunk=1, ctas_per_sm=3, tsmem=1)])
+                                  dict(persistent=1, block_warps=8, chunk=1, ctas_per_sm=3, tsmem=1),
+                                  dict(persistent=1, block_warps=16, chunk=2, ctas_per_sm=1, tsmem=1)])
 def test_batch_launch_shapes_do_not_change_results(vtg_lib, ctx, batch_setup, tune):
     """Every launch shape, the template in registers or in shared memory, gives the single-stream bits."""
     pairs, trackers, dev, singles, b = batch_setup
@@ -91,7 +92,7 @@ def test_batch_launch_shapes_do_not_change_results(vtg_lib, ctx, batch_setup, tu
 def test_batch_refuses_bad_tunes(vtg_lib, ctx, batch_setup):
     b = batch_setup[4]
     before = b.get_tune()
-    for bad in (dict(persistent=1, block_warps=16, chunk=1, ctas_per_sm=1, tsmem=1),
+    for bad in (dict(persistent=1, block_warps=16, chunk=1, ctas_per_sm=2, tsmem=1),
                 dict(persistent=0, block_warps=4, chunk=1, ctas_per_sm=1, tsmem=1),
                 dict(persistent=1, block_warps=8, chunk=1, ctas_per_sm=4, tsmem=1),
                 dict(persistent=1, block_warps=6, chunk=1, ctas_per_sm=1, tsmem=0),
