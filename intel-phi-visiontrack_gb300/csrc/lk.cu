@@ -669,10 +669,12 @@ __global__ void __launch_bounds__(256, 2) lk_cells_kernel(const DevPyr *__restri
                                                           int top, LkPrm p, CellGrid g, int base_w, int base_h,
                                                           vtg_lk_out *__restrict__ out, vtg_cell *__restrict__ cells)
 {
+    extern __shared__ f2_t s_tc[]; /* the template's T: 8 warps x (MAXH / 2) x 32 pairs */
     const int i = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
     if (i >= g.n)
         return;
-    lk_cell<MAXH, EXACT, false>(*Ip, *Jp, top, p, g, base_w, base_h, i, lane, out, cells, nullptr);
+    lk_cell<MAXH, EXACT, true>(*Ip, *Jp, top, p, g, base_w, base_h, i, lane, out, cells,
+                               s_tc + (size_t)(threadIdx.x >> 5) * (MAXH / 2) * 32);
 }
 
 /* Many streams' cells in one launch. Work items are runs of `chunk` cells of one job; job j's items start at
@@ -790,26 +792,30 @@ __global__ void __launch_bounds__(256, 2) lk_points_kernel(const DevPyr *__restr
                                                         const float *__restrict__ ys, const float *__restrict__ gxs,
                                                         const float *__restrict__ gys, vtg_lk_out *__restrict__ out)
 {
+    extern __shared__ f2_t s_tp[]; /* the template's T: 8 warps x (MAXH / 2) x 32 pairs */
     const int i = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
     if (i >= n)
         return;
-    Patch<MAXH, false> P;
-    P.ts = nullptr;
+    Patch<MAXH, true> P;
+    P.ts = s_tp + (size_t)(threadIdx.x >> 5) * (MAXH / 2) * 32;
     vtg_lk_out o;
-    lk_point<MAXH, EXACT, false>(*Ip, *Jp, top, p, xs[i], ys[i], gxs ? gxs[i] : 0.0f, gys ? gys[i] : 0.0f, lane, P, o);
+    lk_point<MAXH, EXACT, true>(*Ip, *Jp, top, p, xs[i], ys[i], gxs ? gxs[i] : 0.0f, gys ? gys[i] : 0.0f, lane, P, o);
     store_out(out + i, o, lane);
 }
+
+/* shared memory of a 256-thread single-stream CTA: its 8 warps' template intensities (at most 30 KB) */
+static constexpr size_t lk_t_bytes(int maxh) { return sizeof(f2_t) * 8 * (size_t)(maxh / 2) * 32; }
 
 cudaError_t vtg_launch_cells(const DevPyr *I, const DevPyr *J, int top, const LkPrm &p, const CellGrid &g, int base_w,
                              int base_h, vtg_lk_out *out, vtg_cell *cells, cudaStream_t s)
 {
     const int blocks = (g.n + 7) / 8;
     if (p.H == 21)
-        lk_cells_kernel<21, true><<<blocks, 256, 0, s>>>(I, J, top, p, g, base_w, base_h, out, cells);
+        lk_cells_kernel<21, true><<<blocks, 256, lk_t_bytes(21), s>>>(I, J, top, p, g, base_w, base_h, out, cells);
     else if (p.H == 15)
-        lk_cells_kernel<15, true><<<blocks, 256, 0, s>>>(I, J, top, p, g, base_w, base_h, out, cells);
+        lk_cells_kernel<15, true><<<blocks, 256, lk_t_bytes(15), s>>>(I, J, top, p, g, base_w, base_h, out, cells);
     else
-        lk_cells_kernel<31, false><<<blocks, 256, 0, s>>>(I, J, top, p, g, base_w, base_h, out, cells);
+        lk_cells_kernel<31, false><<<blocks, 256, lk_t_bytes(31), s>>>(I, J, top, p, g, base_w, base_h, out, cells);
     return cudaGetLastError();
 }
 
@@ -820,10 +826,10 @@ cudaError_t vtg_launch_points(const DevPyr *I, const DevPyr *J, int top, const L
     if (n <= 0)
         return cudaSuccess;
     if (p.H == 21)
-        lk_points_kernel<21, true><<<blocks, 256, 0, s>>>(I, J, top, p, n, xs, ys, gx, gy, out);
+        lk_points_kernel<21, true><<<blocks, 256, lk_t_bytes(21), s>>>(I, J, top, p, n, xs, ys, gx, gy, out);
     else if (p.H == 15)
-        lk_points_kernel<15, true><<<blocks, 256, 0, s>>>(I, J, top, p, n, xs, ys, gx, gy, out);
+        lk_points_kernel<15, true><<<blocks, 256, lk_t_bytes(15), s>>>(I, J, top, p, n, xs, ys, gx, gy, out);
     else
-        lk_points_kernel<31, false><<<blocks, 256, 0, s>>>(I, J, top, p, n, xs, ys, gx, gy, out);
+        lk_points_kernel<31, false><<<blocks, 256, lk_t_bytes(31), s>>>(I, J, top, p, n, xs, ys, gx, gy, out);
     return cudaGetLastError();
 }
