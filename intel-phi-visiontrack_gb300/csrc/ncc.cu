@@ -16,10 +16,13 @@
  *   ncc_map_f32 (or the tensor-core map in ncc_tc.cu)  per cell: best score and its corner
  *   ncc_top                       the eight best cells, value descending then cell index ascending (the reference's
  *                                 insertion order)
- *   ncc_half_all / ncc_pick       each candidate in half pixels within +-(2 step - 1) (or +-1), one warp per corner;
- *                                 then the best, the second peak clear of it by half a template, and the parabola
- *                                 offsets; F32 products with exact integer (quarter-pixel) window sums. */
+ *   ncc_half_all / ncc_pick       each candidate in half pixels within +-(2 step - 1) (or +-1) and one ring past it,
+ *                                 one CTA per corner; then the best, the second peak clear of it by half a template,
+ *                                 and the parabola offsets from the ring; F32 products with exact integer
+ *                                 (quarter-pixel) window sums. */
 #include <float.h>
+
+#include <type_traits>
 
 #include "vtg_internal.cuh"
 #include "vtg_ncc.cuh"
@@ -246,83 +249,124 @@ __device__ __forceinline__ unsigned long long top_key(float v, int i)
     return ((unsigned long long)u << 32) | (unsigned long long)(0xFFFFFFFFu - (unsigned)i);
 }
 
-__device__ __forceinline__ void top_insert(unsigned long long *t, unsigned long long k)
+/* k into the descending list t, keeping its NCC_TOP largest: one compare-exchange a place, unrolled, so t stays in
+ * registers. Keys are distinct (the cell index is in their low bits). */
+__device__ __forceinline__ void top_insert(unsigned long long (&t)[NCC_TOP], unsigned long long k)
 {
     if (k <= t[NCC_TOP - 1])
         return;
-    int at = NCC_TOP - 1;
-    while (at > 0 && t[at - 1] < k) {
-        t[at] = t[at - 1];
-        at--;
+#pragma unroll
+    for (int j = 0; j < NCC_TOP; j++) {
+        const unsigned long long hi = t[j] > k ? t[j] : k;
+        k = t[j] > k ? k : t[j];
+        t[j] = hi;
     }
-    t[at] = k;
 }
 
+/* The eight best cells: each thread its strided share, then the lists merge across the warp by xor partners (both
+ * partners end with the best eight of the pair) and across the eight warps in the first warp. */
 __global__ void __launch_bounds__(256) ncc_top(const float *__restrict__ map_v, int cells, int *__restrict__ top,
                                                int *__restrict__ ntop)
 {
-    __shared__ unsigned long long s[256][NCC_TOP];
+    __shared__ unsigned long long s[8][NCC_TOP];
     unsigned long long t[NCC_TOP];
 #pragma unroll
     for (int k = 0; k < NCC_TOP; k++)
         t[k] = 0ull;
     for (int i = threadIdx.x; i < cells; i += blockDim.x)
-        top_insert(t, top_key(map_v[i], i));
+        top_insert(t, top_key(__ldg(map_v + i), i));
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    auto merge = [&](int width) {
+        for (int sh = 1; sh < width; sh <<= 1) {
+            unsigned long long o[NCC_TOP];
 #pragma unroll
-    for (int k = 0; k < NCC_TOP; k++)
-        s[threadIdx.x][k] = t[k];
+            for (int k = 0; k < NCC_TOP; k++)
+                o[k] = __shfl_xor_sync(VTG_FULL, t[k], sh);
+#pragma unroll
+            for (int k = 0; k < NCC_TOP; k++)
+                top_insert(t, o[k]);
+        }
+    };
+    merge(32);
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < NCC_TOP; k++)
+            s[warp][k] = t[k];
     __syncthreads();
-    for (int half = 128; half >= 1; half >>= 1) {
-        if (threadIdx.x < half) {
-            for (int k = 0; k < NCC_TOP; k++)
-                top_insert(t, s[threadIdx.x + half][k]);
-            for (int k = 0; k < NCC_TOP; k++)
-                s[threadIdx.x][k] = t[k];
+    if (warp == 0) {
+#pragma unroll
+        for (int k = 0; k < NCC_TOP; k++)
+            t[k] = lane < 8 ? s[lane][k] : 0ull;
+        merge(8);
+        if (lane == 0) {
+            int n = 0;
+            for (int k = 0; k < NCC_TOP; k++) {
+                if (t[k] == 0ull)
+                    break;
+                top[n++] = (int)(0xFFFFFFFFu - (unsigned)(t[k] & 0xFFFFFFFFull));
+            }
+            *ntop = n;
         }
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-        int n = 0;
-        for (int k = 0; k < NCC_TOP; k++) {
-            if (t[k] == 0ull)
-                break;
-            top[n++] = (int)(0xFFFFFFFFu - (unsigned)(t[k] & 0xFFFFFFFFull));
-        }
-        *ntop = n;
     }
 }
 
 /* ---- half-pixel refinement (search_half, search_slot's second half, take_back's parabola) ---- */
 
-/* One warp scores one corner in half pixels: F32 products, exact quarter-pixel sums for the variance. */
+/* A corner's score in half pixels (search_half), by a whole CTA of 256 threads: its 8 warps take template rows i = warp, warp + 8, .., its lanes the
+ * columns, so one corner's latency is a few rows, not the whole template. The quarter-pixel sums are exact integers:
+ * 32-bit a thread for byte planes (at most 64 terms of at most 1,020^2 each, for a 128 x 128 template), 64-bit for F32
+ * planes and for every sum across threads. The F32 product sum is added in a fixed order (each thread's rows, the
+ * warp's butterfly, then warps 0 .. 7), so a corner's score is the same every run. The result is thread 0's. */
 template <typename T>
-__device__ float half_score(const T *__restrict__ plane, int pitch, const float *__restrict__ app, const NccPrm &p,
-                            int hx, int hy, int lane)
+__device__ float half_score_cta(const T *__restrict__ plane, int pitch, const float *__restrict__ app, const NccPrm &p,
+                                int hx, int hy)
 {
+    using Q = typename std::conditional<sizeof(T) == 1, int, long long>::type;
+    __shared__ float s_st[8];
+    __shared__ long long s_q1[8], s_q2[8];
     const int x = hx >> 1, y = hy >> 1, ox = hx & 1, oy = hy & 1;
     if (x < 1 || y < 1 || x + p.tw + 1 >= p.w - 1 || y + p.th + 1 >= p.h - 1)
         return -1.0f;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const float first = (float)__ldg(plane + (size_t)y * pitch + x);
     float st = 0.0f;
-    long long q1 = 0, q2 = 0; /* in quarters */
-    for (int k = lane; k < p.tw * p.th; k += 32) {
-        const int i = k / p.tw, j = k - i * p.tw;
-        const T *r0 = plane + (size_t)(y + i) * pitch + x + j, *r1 = r0 + pitch;
-        long long a = (long long)__ldg(r0), b = ox ? (long long)__ldg(r0 + 1) : a;
-        long long q = 2 * (a + b);
-        if (oy) {
-            const long long c = (long long)__ldg(r1), d = ox ? (long long)__ldg(r1 + 1) : c;
-            q = (q + 2 * (c + d)) / 2;
+    Q a1 = 0, a2 = 0; /* in quarters */
+    for (int i = warp; i < p.th; i += 8) {
+        const T *r0 = plane + (size_t)(y + i) * pitch + x, *r1 = r0 + pitch;
+        const float *ar = app + (size_t)i * p.tw;
+        for (int j = lane; j < p.tw; j += 32) {
+            const Q a = (Q)__ldg(r0 + j), b = ox ? (Q)__ldg(r0 + j + 1) : a;
+            Q q = 2 * (a + b);
+            if (oy) {
+                const Q c = (Q)__ldg(r1 + j), d = ox ? (Q)__ldg(r1 + j + 1) : c;
+                q = (q + 2 * (c + d)) / 2;
+            }
+            a1 += q;
+            a2 += q * q;
+            st = __fmaf_rn((float)q * 0.25f - first, __ldg(ar + j), st);
         }
-        q1 += q;
-        q2 += q * q;
-        st = __fmaf_rn((float)q * 0.25f - first, app[k], st);
     }
+    long long q1 = a1, q2 = a2;
 #pragma unroll
     for (int s = 16; s >= 1; s >>= 1) {
         st += __shfl_xor_sync(VTG_FULL, st, s);
         q1 += __shfl_xor_sync(VTG_FULL, q1, s);
         q2 += __shfl_xor_sync(VTG_FULL, q2, s);
+    }
+    if (lane == 0) {
+        s_st[warp] = st;
+        s_q1[warp] = q1;
+        s_q2[warp] = q2;
+    }
+    __syncthreads();
+    if (threadIdx.x != 0)
+        return 0.0f;
+    st = 0.0f;
+    q1 = q2 = 0;
+    for (int k = 0; k < 8; k++) {
+        st += s_st[k];
+        q1 += s_q1[k];
+        q2 += s_q2[k];
     }
     const long long nvar16 = (long long)p.n * q2 - q1 * q1; /* 16 n var, exact */
     if ((double)nvar16 <= 16.0 * (double)p.n * (double)p.norm * 0.0625 || p.norm <= 0.0f)
@@ -340,98 +384,90 @@ __device__ __forceinline__ float parabola(float l, float c, float r)
     return fminf(fmaxf(o, -0.5f), 0.5f);
 }
 
-/* Every half-pixel corner around every candidate, one warp each: scores into hs[candidate][offset]. */
+/* The half-pixel corners around every candidate, one CTA each: the window of +-around half pixels that
+ * search_slot compares, and one ring past it, so the parabola's neighbours of any best are already scored. Scores go
+ * to hs[candidate][(around + 1 + dy) ring + around + 1 + dx], ring = 2 around + 3. */
 template <typename T>
 __global__ void __launch_bounds__(256) ncc_half_all(const T *__restrict__ plane, int pitch, const float *__restrict__ app,
                                                     NccPrm p, const int *__restrict__ map_x, const int *__restrict__ map_y,
                                                     const int *__restrict__ top, const int *__restrict__ ntop,
                                                     float *__restrict__ hs)
 {
-    const int around = p.step > 1 ? 2 * p.step - 1 : 1, side = 2 * around + 1;
-    const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    const int c = wid / (side * side), o = wid - c * side * side;
+    const int around = p.step > 1 ? 2 * p.step - 1 : 1, ring = 2 * around + 3, r = around + 1;
+    const int c = blockIdx.x / (ring * ring), o = blockIdx.x - c * ring * ring;
     if (c >= *ntop)
         return;
     const int cell = top[c];
-    const int hx = 2 * map_x[cell] + (o % side) - around, hy = 2 * map_y[cell] + (o / side) - around;
-    const float v = half_score(plane, pitch, app, p, hx, hy, lane);
-    if (lane == 0)
-        hs[c * side * side + o] = v;
+    const int hx = 2 * map_x[cell] + (o % ring) - r, hy = 2 * map_y[cell] + (o / ring) - r;
+    const float v = half_score_cta(plane, pitch, app, p, hx, hy);
+    if (threadIdx.x == 0)
+        hs[c * ring * ring + o] = v;
 }
 
-/* The best of each candidate's corners (row-major first maximum, as search_slot's strict > over hy then hx), the
- * best over candidates in rank order, the second peak half a template away, and the parabola through the four
- * neighbours of the best (take_back's peak_offset), one warp each for the four. */
-template <typename T>
-__global__ void __launch_bounds__(128) ncc_pick(const T *__restrict__ plane, int pitch, const float *__restrict__ app,
-                                                NccPrm p, const int *__restrict__ map_x, const int *__restrict__ map_y,
-                                                const int *__restrict__ top, const int *__restrict__ ntop,
-                                                const float *__restrict__ hs, vtg_found *__restrict__ out)
+/* The best of each candidate's window (row-major first maximum, as search_slot's strict > over hy then hx), the best
+ * over candidates in rank order, the second peak half a template away, and the parabola through the four neighbours
+ * of the best (take_back's peak_offset), all from hs: one thread. */
+__global__ void ncc_pick(NccPrm p, const int *__restrict__ map_x, const int *__restrict__ map_y,
+                         const int *__restrict__ top, const int *__restrict__ ntop, const float *__restrict__ hs,
+                         vtg_found *__restrict__ out)
 {
-    __shared__ float s_score[NCC_TOP], s_side[4];
-    __shared__ int s_hx[NCC_TOP], s_hy[NCC_TOP], s_best[3];
+    if (threadIdx.x != 0)
+        return;
     const int n = *ntop;
-    const int around = p.step > 1 ? 2 * p.step - 1 : 1, side = 2 * around + 1;
-    if (threadIdx.x < n) {
-        const int c = threadIdx.x, cell = top[c];
+    const int around = p.step > 1 ? 2 * p.step - 1 : 1, side = 2 * around + 1, ring = side + 2;
+    float score[NCC_TOP];
+    int bhx[NCC_TOP], bhy[NCC_TOP], bo[NCC_TOP];
+    for (int c = 0; c < n; c++) {
+        const int cell = top[c];
         const int cx = 2 * map_x[cell], cy = 2 * map_y[cell];
+        const float *h = hs + (size_t)c * ring * ring;
         float best = -2.0f;
-        int bx = cx, by = cy;
-        for (int o = 0; o < side * side; o++) {
-            const float v = hs[c * side * side + o];
-            if (v > best) {
-                best = v;
-                bx = cx + (o % side) - around;
-                by = cy + (o / side) - around;
+        int bx = cx, by = cy, at = (around + 1) * ring + around + 1;
+        for (int dy = -around; dy <= around; dy++)
+            for (int dx = -around; dx <= around; dx++) {
+                const int k = (around + 1 + dy) * ring + around + 1 + dx;
+                if (h[k] > best) {
+                    best = h[k];
+                    bx = cx + dx;
+                    by = cy + dy;
+                    at = k;
+                }
             }
+        score[c] = best;
+        bhx[c] = bx;
+        bhy[c] = by;
+        bo[c] = at;
+    }
+    float ncc = -2.0f;
+    int win = -1, hx = 0, hy = 0;
+    for (int c = 0; c < n; c++)
+        if (score[c] > ncc) {
+            ncc = score[c];
+            win = c;
+            hx = bhx[c];
+            hy = bhy[c];
         }
-        s_score[c] = best;
-        s_hx[c] = bx;
-        s_hy[c] = by;
+    float second = -2.0f;
+    for (int c = 0; c < n; c++) {
+        const int dx = bhx[c] - hx, dy = bhy[c] - hy;
+        if ((dx * dx > p.tw * p.tw || dy * dy > p.th * p.th) && score[c] > second)
+            second = score[c];
     }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        float ncc = -2.0f;
-        int hx = 0, hy = 0;
-        for (int k = 0; k < n; k++)
-            if (s_score[k] > ncc) {
-                ncc = s_score[k];
-                hx = s_hx[k];
-                hy = s_hy[k];
-            }
-        s_best[0] = hx;
-        s_best[1] = hy;
-        s_best[2] = __float_as_int(ncc);
+    vtg_found f;
+    f.hx = hx;
+    f.hy = hy;
+    f.ncc = ncc;
+    f.second = second;
+    f.ox = f.oy = 0.0f;
+    if (win >= 0) {
+        const float *h = hs + (size_t)win * ring * ring;
+        const int k = bo[win];
+        f.ox = parabola(h[k - 1], ncc, h[k + 1]);
+        f.oy = parabola(h[k - ring], ncc, h[k + ring]);
     }
-    __syncthreads();
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int hx = s_best[0], hy = s_best[1];
-    if (n > 0) {
-        const int dx = warp == 0 ? -1 : warp == 1 ? 1 : 0, dy = warp == 2 ? -1 : warp == 3 ? 1 : 0;
-        const float v = half_score(plane, pitch, app, p, hx + dx, hy + dy, lane);
-        if (lane == 0)
-            s_side[warp] = v;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        const float ncc = __int_as_float(s_best[2]);
-        float second = -2.0f;
-        for (int k = 0; k < n; k++) {
-            const int dx = s_hx[k] - hx, dy = s_hy[k] - hy;
-            if ((dx * dx > p.tw * p.tw || dy * dy > p.th * p.th) && s_score[k] > second)
-                second = s_score[k];
-        }
-        vtg_found f;
-        f.hx = hx;
-        f.hy = hy;
-        f.ncc = ncc;
-        f.second = second;
-        f.ox = n > 0 ? parabola(s_side[0], ncc, s_side[1]) : 0.0f;
-        f.oy = n > 0 ? parabola(s_side[2], ncc, s_side[3]) : 0.0f;
-        f.ntop = n;
-        f.cells = p.ccols * p.crows;
-        *out = f;
-    }
+    f.ntop = n;
+    f.cells = p.ccols * p.crows;
+    *out = f;
 }
 
 /* ---- corners one by one (tk_correlate): one warp per corner ---- */
@@ -493,10 +529,10 @@ static cudaError_t launch_all(const T *plane, int pitch, const float *app, const
             return e;
     }
     ncc_top<<<1, 256, 0, st>>>(s.map_v, cells, s.top, s.ntop);
-    const int around = p.step > 1 ? 2 * p.step - 1 : 1, side = 2 * around + 1;
-    const int warps = NCC_TOP * side * side;
-    ncc_half_all<T><<<(warps + 7) / 8, 256, 0, st>>>(plane, pitch, app, p, s.map_x, s.map_y, s.top, s.ntop, s.half);
-    ncc_pick<T><<<1, 128, 0, st>>>(plane, pitch, app, p, s.map_x, s.map_y, s.top, s.ntop, s.half, out);
+    const int around = p.step > 1 ? 2 * p.step - 1 : 1, ring = 2 * around + 3;
+    ncc_half_all<T><<<NCC_TOP * ring * ring, 256, 0, st>>>(plane, pitch, app, p, s.map_x, s.map_y, s.top, s.ntop,
+                                                            s.half);
+    ncc_pick<<<1, 32, 0, st>>>(p, s.map_x, s.map_y, s.top, s.ntop, s.half, out);
     return cudaGetLastError();
 }
 

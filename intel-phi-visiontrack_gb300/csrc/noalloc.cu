@@ -31,7 +31,7 @@
 static __device__ __align__(256) unsigned char g_noalloc_scratch[VTG_NOALLOC_SCRATCH_BYTES];
 
 #define VTG_NOALLOC_MAX_STEP 4
-#define VTG_NOALLOC_HALF (NCC_TOP * (4 * VTG_NOALLOC_MAX_STEP - 1) * (4 * VTG_NOALLOC_MAX_STEP - 1))
+#define VTG_NOALLOC_HALF (NCC_TOP * (4 * VTG_NOALLOC_MAX_STEP + 1) * (4 * VTG_NOALLOC_MAX_STEP + 1))
 
 static_assert(2 * sizeof(long long) * (size_t)VTG_NOALLOC_MAX_PIXELS +
                       (size_t)VTG_NOALLOC_MAX_CELLS * (sizeof(float) + 2 * sizeof(int)) + 256 +

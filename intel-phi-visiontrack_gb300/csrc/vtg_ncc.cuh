@@ -6,7 +6,8 @@
 
 #define NCC_CELL 16 /* SEARCH_CELL, src/kern/track.c:61: corners to a cell of the map */
 #define NCC_TOP 8   /* SEARCH_TOP, src/kern/track.c:62: cells looked at again in half pixels */
-#define NCC_HALF_MAX (NCC_TOP * 63 * 63) /* half-pixel scores of the candidates at the largest step (16) */
+#define NCC_HALF_MAX (NCC_TOP * 65 * 65) /* half-pixel scores of the candidates at the largest step (16), with
+                                          * the ring around each window */
 
 /* One search: the plane, the template and the clamped window of corners. */
 struct NccPrm {
@@ -25,7 +26,7 @@ struct NccScratch {
     float *map_v;
     int *map_x, *map_y;
     int *top, *ntop;
-    float *half;          /* the candidates' half-pixel scores: NCC_TOP x (2 around + 1)^2, around <= 2 x 16 - 1 */
+    float *half;          /* the candidates' half-pixel scores: NCC_TOP x (2 around + 3)^2, around <= 2 x 16 - 1 */
     const uint16_t *band; /* the template band for the tensor-core map (ncc_tc.cu), NULL if unset */
     int band_rows, krow;  /* image rows of a tile's band (NCC_TC_Q + th - 1), K per image row */
     int *err;             /* device status word: nonzero when a bounded wait gave up */
