@@ -218,6 +218,7 @@ static int make_prm(const vtg_search *s, int w, int h, int x0, int x1, int y0, i
     p->th = s->th;
     p->n = s->tw * s->th;
     p->norm = s->norm;
+    ncc_thresholds(*p);
     p->sum_t = precision == VTG_NCC_BF16 ? s->host_sum[0] : precision == VTG_NCC_FP16 ? s->host_sum[1] : 0.0f;
     /* the reference's clamp of the window (search_slot, track.c:1665-1670) */
     const int lo_x = 1, hi_x = w - s->tw - 2, lo_y = 1, hi_y = h - s->th - 2;

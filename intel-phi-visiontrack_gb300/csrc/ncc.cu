@@ -12,7 +12,8 @@
  * near-blank rule compares an exact integer n var with n norm / 16 and never lets a flat window through.
  *
  * Pipeline (all on one stream, no host round trip):
- *   integral_rows / integral_cols  int64 tables of J and J^2 ((h + 1) x (w + 1)), exact
+ *   integral_rows / integral_cols  int64 tables of J and J^2 ((h + 1) x (w + 1)), exact (for the F32 map; the
+ *                                 tensor-core map's ncc_box_prep sums the window bytes directly)
  *   ncc_map_f32 (or the tensor-core map in ncc_tc.cu)  per cell: best score and its corner
  *   ncc_top                       the eight best cells, value descending then cell index ascending (the reference's
  *                                 insertion order)
@@ -146,7 +147,7 @@ __device__ __forceinline__ long long box(const long long *S, int tp, int x, int 
 __device__ __forceinline__ float ncc_score(float st, long long s1, long long s2, const NccPrm &p)
 {
     const long long nvar = (long long)p.n * s2 - s1 * s1; /* n var, exact */
-    if ((double)nvar <= (double)p.n * (double)p.norm * 0.0625 || p.norm <= 0.0f)
+    if (nvar <= p.nthr || p.norm <= 0.0f)
         return 0.0f;
     const float var = (float)nvar / (float)p.n;
     return st / sqrtf(p.norm * var);
@@ -273,18 +274,42 @@ __global__ void __launch_bounds__(256) ncc_top(const float *__restrict__ map_v, 
 #pragma unroll
     for (int k = 0; k < NCC_TOP; k++)
         t[k] = 0ull;
-    for (int i = threadIdx.x; i < cells; i += blockDim.x)
-        top_insert(t, top_key(__ldg(map_v + i), i));
+    /* eight loads in flight a thread, then their inserts */
+    for (int i0 = threadIdx.x; i0 < cells; i0 += 8 * blockDim.x) {
+        float v[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            const int i = i0 + u * blockDim.x;
+            v[u] = i < cells ? __ldg(map_v + i) : -3.0f;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+            top_insert(t, top_key(v[u], i0 + u * blockDim.x));
+    }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    /* two descending lists' best eight: max(a_k, b_(7 - k)) is their top eight as a bitonic sequence, which three
+     * compare-exchange layers sort; both xor partners compute the same list */
     auto merge = [&](int width) {
         for (int sh = 1; sh < width; sh <<= 1) {
-            unsigned long long o[NCC_TOP];
+            unsigned long long c[NCC_TOP];
+#pragma unroll
+            for (int k = 0; k < NCC_TOP; k++) {
+                const unsigned long long o = __shfl_xor_sync(VTG_FULL, t[NCC_TOP - 1 - k], sh);
+                c[k] = t[k] > o ? t[k] : o;
+            }
+#pragma unroll
+            for (int d = NCC_TOP / 2; d >= 1; d >>= 1)
+#pragma unroll
+                for (int k = 0; k < NCC_TOP; k++)
+                    if ((k & d) == 0) {
+                        const unsigned long long hi = c[k] > c[k + d] ? c[k] : c[k + d];
+                        const unsigned long long lo = c[k] > c[k + d] ? c[k + d] : c[k];
+                        c[k] = hi;
+                        c[k + d] = lo;
+                    }
 #pragma unroll
             for (int k = 0; k < NCC_TOP; k++)
-                o[k] = __shfl_xor_sync(VTG_FULL, t[k], sh);
-#pragma unroll
-            for (int k = 0; k < NCC_TOP; k++)
-                top_insert(t, o[k]);
+                t[k] = c[k];
         }
     };
     merge(32);
@@ -369,7 +394,7 @@ __device__ float half_score_cta(const T *__restrict__ plane, int pitch, const fl
         q2 += s_q2[k];
     }
     const long long nvar16 = (long long)p.n * q2 - q1 * q1; /* 16 n var, exact */
-    if ((double)nvar16 <= 16.0 * (double)p.n * (double)p.norm * 0.0625 || p.norm <= 0.0f)
+    if (nvar16 <= p.nthr16 || p.norm <= 0.0f)
         return 0.0f;
     const float var = (float)nvar16 / (16.0f * (float)p.n);
     return st / sqrtf(p.norm * var);
@@ -404,54 +429,67 @@ __global__ void __launch_bounds__(256) ncc_half_all(const T *__restrict__ plane,
         hs[c * ring * ring + o] = v;
 }
 
-/* The best of each candidate's window (row-major first maximum, as search_slot's strict > over hy then hx), the best
- * over candidates in rank order, the second peak half a template away, and the parabola through the four neighbours
- * of the best (take_back's peak_offset), all from hs: one thread. */
-__global__ void ncc_pick(NccPrm p, const int *__restrict__ map_x, const int *__restrict__ map_y,
-                         const int *__restrict__ top, const int *__restrict__ ntop, const float *__restrict__ hs,
-                         vtg_found *__restrict__ out)
+/* The best of each candidate's window (row-major first maximum, as search_slot's strict > over hy then hx: the
+ * smallest index among equal scores), one warp a candidate; then, on one thread, the best over candidates in rank
+ * order, the second peak half a template away, and the parabola through the four neighbours of the best (take_back's
+ * peak_offset), all from hs. */
+__global__ void __launch_bounds__(NCC_TOP * 32) ncc_pick(NccPrm p, const int *__restrict__ map_x,
+                                                         const int *__restrict__ map_y, const int *__restrict__ top,
+                                                         const int *__restrict__ ntop, const float *__restrict__ hs,
+                                                         vtg_found *__restrict__ out)
 {
-    if (threadIdx.x != 0)
-        return;
+    __shared__ float s_score[NCC_TOP];
+    __shared__ int s_hx[NCC_TOP], s_hy[NCC_TOP], s_at[NCC_TOP];
     const int n = *ntop;
     const int around = p.step > 1 ? 2 * p.step - 1 : 1, side = 2 * around + 1, ring = side + 2;
-    float score[NCC_TOP];
-    int bhx[NCC_TOP], bhy[NCC_TOP], bo[NCC_TOP];
-    for (int c = 0; c < n; c++) {
-        const int cell = top[c];
-        const int cx = 2 * map_x[cell], cy = 2 * map_y[cell];
+    const int c = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (c < n) {
         const float *h = hs + (size_t)c * ring * ring;
         float best = -2.0f;
-        int bx = cx, by = cy, at = (around + 1) * ring + around + 1;
-        for (int dy = -around; dy <= around; dy++)
-            for (int dx = -around; dx <= around; dx++) {
-                const int k = (around + 1 + dy) * ring + around + 1 + dx;
-                if (h[k] > best) {
-                    best = h[k];
-                    bx = cx + dx;
-                    by = cy + dy;
-                    at = k;
-                }
+        int bo = side * side; /* scan index of the best; side^2: none */
+        for (int o = lane; o < side * side; o += 32) {
+            const float v = h[(o / side + 1) * ring + o % side + 1];
+            if (v > best) {
+                best = v;
+                bo = o;
             }
-        score[c] = best;
-        bhx[c] = bx;
-        bhy[c] = by;
-        bo[c] = at;
+        }
+#pragma unroll
+        for (int sh = 16; sh >= 1; sh >>= 1) {
+            const float ov = __shfl_xor_sync(VTG_FULL, best, sh);
+            const int oo = __shfl_xor_sync(VTG_FULL, bo, sh);
+            if (ov > best || (ov == best && oo < bo)) {
+                best = ov;
+                bo = oo;
+            }
+        }
+        if (lane == 0) {
+            const int cell = top[c];
+            if (bo == side * side)
+                bo = (side * side) / 2; /* no score above -2: the centre */
+            s_score[c] = best;
+            s_hx[c] = 2 * map_x[cell] + bo % side - around;
+            s_hy[c] = 2 * map_y[cell] + bo / side - around;
+            s_at[c] = (bo / side + 1) * ring + bo % side + 1;
+        }
     }
+    __syncthreads();
+    if (threadIdx.x != 0)
+        return;
     float ncc = -2.0f;
     int win = -1, hx = 0, hy = 0;
-    for (int c = 0; c < n; c++)
-        if (score[c] > ncc) {
-            ncc = score[c];
-            win = c;
-            hx = bhx[c];
-            hy = bhy[c];
+    for (int k = 0; k < n; k++)
+        if (s_score[k] > ncc) {
+            ncc = s_score[k];
+            win = k;
+            hx = s_hx[k];
+            hy = s_hy[k];
         }
     float second = -2.0f;
-    for (int c = 0; c < n; c++) {
-        const int dx = bhx[c] - hx, dy = bhy[c] - hy;
-        if ((dx * dx > p.tw * p.tw || dy * dy > p.th * p.th) && score[c] > second)
-            second = score[c];
+    for (int k = 0; k < n; k++) {
+        const int dx = s_hx[k] - hx, dy = s_hy[k] - hy;
+        if ((dx * dx > p.tw * p.tw || dy * dy > p.th * p.th) && s_score[k] > second)
+            second = s_score[k];
     }
     vtg_found f;
     f.hx = hx;
@@ -461,7 +499,7 @@ __global__ void ncc_pick(NccPrm p, const int *__restrict__ map_x, const int *__r
     f.ox = f.oy = 0.0f;
     if (win >= 0) {
         const float *h = hs + (size_t)win * ring * ring;
-        const int k = bo[win];
+        const int k = s_at[win];
         f.ox = parabola(h[k - 1], ncc, h[k + 1]);
         f.oy = parabola(h[k - ring], ncc, h[k + ring]);
     }
@@ -513,11 +551,12 @@ template <typename T>
 static cudaError_t launch_all(const T *plane, int pitch, const float *app, const NccPrm &p, const NccScratch &s,
                               int map_kind, vtg_found *out, cudaStream_t st)
 {
-    integral_rows<T><<<(p.h + 1 + 7) / 8, 256, 0, st>>>(plane, pitch, p.w, p.h, s.S1, s.S2, s.tp);
-    integral_cols<<<(p.w + 1 + IC_COLS - 1) / IC_COLS, IC_COLS * IC_SEGS, 0, st>>>(p.w, p.h, s.S1, s.S2, s.tp);
     const int cells = p.ccols * p.crows;
     cudaError_t e = cudaSuccess;
     if (map_kind == VTG_NCC_F32) {
+        /* the F32 map takes its window sums from the integral images; the tensor-core map's prep sums the bytes */
+        integral_rows<T><<<(p.h + 1 + 7) / 8, 256, 0, st>>>(plane, pitch, p.w, p.h, s.S1, s.S2, s.tp);
+        integral_cols<<<(p.w + 1 + IC_COLS - 1) / IC_COLS, IC_COLS * IC_SEGS, 0, st>>>(p.w, p.h, s.S1, s.S2, s.tp);
         const size_t smem = sizeof(float) * ((size_t)p.tw * p.th + (size_t)(NCC_CELL + p.tw) * (NCC_CELL + p.th));
         e = cudaFuncSetAttribute(ncc_map_f32<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess)
@@ -532,7 +571,7 @@ static cudaError_t launch_all(const T *plane, int pitch, const float *app, const
     const int around = p.step > 1 ? 2 * p.step - 1 : 1, ring = 2 * around + 3;
     ncc_half_all<T><<<NCC_TOP * ring * ring, 256, 0, st>>>(plane, pitch, app, p, s.map_x, s.map_y, s.top, s.ntop,
                                                             s.half);
-    ncc_pick<<<1, 32, 0, st>>>(p, s.map_x, s.map_y, s.top, s.ntop, s.half, out);
+    ncc_pick<<<1, NCC_TOP * 32, 0, st>>>(p, s.map_x, s.map_y, s.top, s.ntop, s.half, out);
     return cudaGetLastError();
 }
 

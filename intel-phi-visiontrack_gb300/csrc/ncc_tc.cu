@@ -21,7 +21,7 @@
  * timer; past it the kernel records an error word.
  * Epilogue: each of the 128 threads owns one accumulator row (8 x-corners by 8 y-corners). Per corner: st = acc -
  * J(x, y) sum t' (the reference's st is relative to the corner's first pixel), times the corner's factor 1 / sqrt(norm
- * var) from ncc_prep (0 for a near-blank window: the exact int64 rule), the best per 16 x 16 cell by value then scan
+ * var) from ncc_box_prep (0 for a near-blank window: the exact integer rule), the best per 16 x 16 cell by value then scan
  * order, merged across tiles by a 64-bit atomicMax on (ordered score, inverted scan index). */
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
@@ -121,24 +121,97 @@ __global__ void ncc_conv(const uint8_t *__restrict__ plane, int pitch, int w, in
     }
 }
 
-/* fac[(y - y0) fw + (x - x0)] = 1 / sqrt(norm var) from the exact int64 window sums; 0 for a near-blank window
- * (n var <= n norm / 16) or norm <= 0 -- the reference's rule (src/kern/track.c:203-205) on exact integers. */
-__global__ void ncc_prep(NccPrm p, const long long *__restrict__ S1, const long long *__restrict__ S2, int tp, int fw,
-                         float *__restrict__ fac)
+/* fac[(y - y0) fw + (x - x0)] = 1 / sqrt(norm var) from the corner's exact window sums; 0 for a near-blank window
+ * (n var <= n norm / 16) or norm <= 0 -- the reference's rule (src/kern/track.c:203-205) on exact integers.
+ * The sums come straight from the bytes, a tile of BP_TX x BP_TY corners a CTA, one thread a column of the tile:
+ *   - down its column, running sums over the template's T_h rows for the tile's BP_TY corner rows (registers);
+ *   - across the columns, each row's prefix sums: a shuffle scan in the warp, the earlier warps' totals added from
+ *     shared memory;
+ *   - a corner's window sums are then P(x + T_w) - P(x), consecutive lanes on consecutive corners.
+ * Bytes keep every window sum in 32 bits (sum J^2 <= 255^2 x 128^2 < 2^31). A row's prefix of J^2 may pass 2^32, so
+ * the prefixes are unsigned and wrap: their differences are still exact. n var is formed in 64 bits. */
+#define BP_TX 128
+#define BP_TY 8
+__global__ void __launch_bounds__(256) ncc_box_prep(const uint8_t *__restrict__ plane, int pitch, NccPrm p, int fw,
+                                                    float *__restrict__ fac)
 {
+    __shared__ unsigned P1[BP_TY][257], P2[BP_TY][257]; /* P[r][c]: columns 0 .. c - 1 of row r */
+    __shared__ unsigned t1[8][BP_TY], t2[8][BP_TY];     /* each warp's column totals */
     const int fh = p.y1 - p.y0 + 1;
-    const size_t total = (size_t)fw * fh;
-    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total; idx += (size_t)gridDim.x * blockDim.x) {
-        const int y = p.y0 + (int)(idx / fw), x = p.x0 + (int)(idx % fw);
-        const long long *a = S1 + (size_t)y * tp + x, *b = S1 + (size_t)(y + p.th) * tp + x;
-        const long long s1 = b[p.tw] - b[0] - a[p.tw] + a[0];
-        const long long *c = S2 + (size_t)y * tp + x, *d = S2 + (size_t)(y + p.th) * tp + x;
-        const long long s2 = d[p.tw] - d[0] - c[p.tw] + c[0];
+    const int tx0 = blockIdx.x * BP_TX, ty0 = blockIdx.y * BP_TY;
+    const int nx = min(BP_TX, fw - tx0), ny = min(BP_TY, fh - ty0);
+    const int c = threadIdx.x, lane = c & 31, warp = c >> 5;
+    const int ncol = nx + p.tw - 1; /* <= 255 */
+    unsigned a[BP_TY], b[BP_TY];
+    if (c < ncol) {
+        const uint8_t *col = plane + (size_t)(p.y0 + ty0) * pitch + (p.x0 + tx0 + c);
+        unsigned sa = 0, sb = 0;
+#pragma unroll 8
+        for (int i = 0; i < p.th; i++) {
+            const unsigned v = __ldg(col + (size_t)i * pitch);
+            sa += v;
+            sb += v * v;
+        }
+        a[0] = sa;
+        b[0] = sb;
+#pragma unroll
+        for (int r = 1; r < BP_TY; r++) {
+            if (r < ny) {
+                const unsigned o = __ldg(col + (size_t)(r - 1) * pitch), n = __ldg(col + (size_t)(r - 1 + p.th) * pitch);
+                sa += n - o;
+                sb += n * n - o * o;
+            }
+            a[r] = sa;
+            b[r] = sb;
+        }
+    } else {
+#pragma unroll
+        for (int r = 0; r < BP_TY; r++)
+            a[r] = b[r] = 0u;
+    }
+    /* inclusive scans across the warp's 32 columns */
+#pragma unroll
+    for (int sh = 1; sh < 32; sh <<= 1)
+#pragma unroll
+        for (int r = 0; r < BP_TY; r++) {
+            const unsigned ua = __shfl_up_sync(VTG_FULL, a[r], sh), ub = __shfl_up_sync(VTG_FULL, b[r], sh);
+            if (lane >= sh) {
+                a[r] += ua;
+                b[r] += ub;
+            }
+        }
+    if (lane == 31)
+#pragma unroll
+        for (int r = 0; r < BP_TY; r++) {
+            t1[warp][r] = a[r];
+            t2[warp][r] = b[r];
+        }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < BP_TY; r++) {
+        unsigned ca = 0, cb = 0;
+        for (int w = 0; w < warp; w++) {
+            ca += t1[w][r];
+            cb += t2[w][r];
+        }
+        P1[r][c + 1] = ca + a[r];
+        P2[r][c + 1] = cb + b[r];
+        if (c == 0) {
+            P1[r][0] = 0u;
+            P2[r][0] = 0u;
+        }
+    }
+    __syncthreads();
+    for (int q = c; q < BP_TY * BP_TX; q += blockDim.x) {
+        const int r = q / BP_TX, x = q - r * BP_TX;
+        if (r >= ny || x >= nx)
+            continue;
+        const long long s1 = (long long)(P1[r][x + p.tw] - P1[r][x]), s2 = (long long)(P2[r][x + p.tw] - P2[r][x]);
         const long long nvar = (long long)p.n * s2 - s1 * s1;
         float f = 0.0f;
-        if (!((double)nvar <= (double)p.n * (double)p.norm * 0.0625 || p.norm <= 0.0f))
+        if (!(nvar <= p.nthr || p.norm <= 0.0f))
             f = 1.0f / sqrtf(p.norm * ((float)nvar / (float)p.n));
-        fac[idx] = f;
+        fac[(size_t)(ty0 + r) * fw + (tx0 + x)] = f;
     }
 }
 
@@ -431,8 +504,8 @@ cudaError_t vtg_launch_ncc_map_tc(const void *plane, int pitch, int elem_bytes, 
         ncc_conv<VTG_NCC_BF16><<<cblocks, 256, 0, st>>>((const uint8_t *)plane, pitch, p.w, p.h, p.x0, rows, cpitch, s.conv);
     else
         ncc_conv<VTG_NCC_FP16><<<cblocks, 256, 0, st>>>((const uint8_t *)plane, pitch, p.w, p.h, p.x0, rows, cpitch, s.conv);
-    const size_t ftotal = (size_t)fw * fh;
-    ncc_prep<<<(int)((ftotal + 255) / 256 < 8192 ? (ftotal + 255) / 256 : 8192), 256, 0, st>>>(p, s.S1, s.S2, s.tp, fw, s.fac);
+    ncc_box_prep<<<dim3((fw + BP_TX - 1) / BP_TX, (fh + BP_TY - 1) / BP_TY), 256, 0, st>>>((const uint8_t *)plane, pitch,
+                                                                                          p, fw, s.fac);
     if (kind == VTG_NCC_BF16) {
         e = cudaFuncSetAttribute(ncc_map_tc<VTG_NCC_BF16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm.total);
         if (e != cudaSuccess)

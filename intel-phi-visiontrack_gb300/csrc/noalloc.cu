@@ -83,6 +83,7 @@ extern "C" int vtg_search_run_noalloc(const void *plane, int w, int h, int pitch
     p.th = th;
     p.n = tw * th;
     p.norm = norm;
+    ncc_thresholds(p);
     p.sum_t = 0.0f;
     /* the reference's clamp of the window (search_slot, src/kern/track.c:1665-1670) */
     const int lo_x = 1, hi_x = w - tw - 2, lo_y = 1, hi_y = h - th - 2;

@@ -2,6 +2,8 @@
 #ifndef VTG_NCC_CUH
 #define VTG_NCC_CUH
 
+#include <math.h>
+
 #include "vtg_internal.cuh"
 
 #define NCC_CELL 16 /* SEARCH_CELL, src/kern/track.c:61: corners to a cell of the map */
@@ -17,7 +19,18 @@ struct NccPrm {
     float sum_t;     /* sum of the template as the tensor-core map multiplies it (its rounded values) */
     int x0, x1, y0, y1, step;
     int ccols, crows; /* the map's cells */
+    /* the near-blank rule on exact integers: n var <= nthr, 16 n var <= nthr16 (half pixels) */
+    long long nthr, nthr16;
 };
+
+/* nthr = floor(n norm / 16) and nthr16 = floor(n norm): n norm is exact in double (n <= 2^14, norm an F32), so an
+ * integer n var compares with them exactly as with n norm / 16 itself, and no kernel needs FP64 for the rule. */
+static inline void ncc_thresholds(NccPrm &p)
+{
+    const double nn = (double)p.n * (double)p.norm;
+    p.nthr = (long long)floor(nn * 0.0625);
+    p.nthr16 = (long long)floor(nn);
+}
 
 /* Scratch of a search context, in device memory. */
 struct NccScratch {
