@@ -136,7 +136,7 @@ __global__ void __launch_bounds__(256) ncc_box_prep(const uint8_t *__restrict__ 
                                                     float *__restrict__ fac)
 {
     __shared__ unsigned P1[BP_TY][257], P2[BP_TY][257]; /* P[r][c]: columns 0 .. c - 1 of row r */
-    __shared__ unsigned t1[8][BP_TY], t2[8][BP_TY];     /* each warp's column totals */
+    __shared__ unsigned t1[8][BP_TY], t2[8][BP_TY];     /* each warp's column totals, then the earlier warps' */
     const int fh = p.y1 - p.y0 + 1;
     const int tx0 = blockIdx.x * BP_TX, ty0 = blockIdx.y * BP_TY;
     const int nx = min(BP_TX, fw - tx0), ny = min(BP_TY, fh - ty0);
@@ -187,15 +187,21 @@ __global__ void __launch_bounds__(256) ncc_box_prep(const uint8_t *__restrict__ 
             t2[warp][r] = b[r];
         }
     __syncthreads();
+    if (c < 2 * BP_TY) { /* each (row, table): the totals of the warps before, in place */
+        unsigned(*t)[BP_TY] = c < BP_TY ? t1 : t2;
+        const int r = c % BP_TY;
+        unsigned run = 0;
+        for (int w = 0; w < 8; w++) {
+            const unsigned v = t[w][r];
+            t[w][r] = run;
+            run += v;
+        }
+    }
+    __syncthreads();
 #pragma unroll
     for (int r = 0; r < BP_TY; r++) {
-        unsigned ca = 0, cb = 0;
-        for (int w = 0; w < warp; w++) {
-            ca += t1[w][r];
-            cb += t2[w][r];
-        }
-        P1[r][c + 1] = ca + a[r];
-        P2[r][c + 1] = cb + b[r];
+        P1[r][c + 1] = t1[warp][r] + a[r];
+        P2[r][c + 1] = t2[warp][r] + b[r];
         if (c == 0) {
             P1[r][0] = 0u;
             P2[r][0] = 0u;
@@ -208,10 +214,8 @@ __global__ void __launch_bounds__(256) ncc_box_prep(const uint8_t *__restrict__ 
             continue;
         const long long s1 = (long long)(P1[r][x + p.tw] - P1[r][x]), s2 = (long long)(P2[r][x + p.tw] - P2[r][x]);
         const long long nvar = (long long)p.n * s2 - s1 * s1;
-        float f = 0.0f;
-        if (!(nvar <= p.nthr || p.norm <= 0.0f))
-            f = 1.0f / sqrtf(p.norm * ((float)nvar / (float)p.n));
-        fac[(size_t)(ty0 + r) * fw + (tx0 + x)] = f;
+        /* 1 / sqrt(norm var) = sqrt(n / norm) / sqrt(n var) */
+        fac[(size_t)(ty0 + r) * fw + (tx0 + x)] = (nvar <= p.nthr || p.norm <= 0.0f) ? 0.0f : p.rnorm * rsqrtf((float)nvar);
     }
 }
 

@@ -21,6 +21,7 @@ struct NccPrm {
     int ccols, crows; /* the map's cells */
     /* the near-blank rule on exact integers: n var <= nthr, 16 n var <= nthr16 (half pixels) */
     long long nthr, nthr16;
+    float rnorm; /* sqrt(n / norm): the tensor-core map's factor is rnorm / sqrt(n var) */
 };
 
 /* nthr = floor(n norm / 16) and nthr16 = floor(n norm): n norm is exact in double (n <= 2^14, norm an F32), so an
@@ -30,6 +31,7 @@ static inline void ncc_thresholds(NccPrm &p)
     const double nn = (double)p.n * (double)p.norm;
     p.nthr = (long long)floor(nn * 0.0625);
     p.nthr16 = (long long)floor(nn);
+    p.rnorm = p.norm > 0.0f ? (float)sqrt((double)p.n / (double)p.norm) : 0.0f;
 }
 
 /* Scratch of a search context, in device memory. */
