@@ -172,6 +172,16 @@ def test_repeatable_and_set_order(vtg_lib, ctx):
     t.close()
 
 
+def test_empty_point_list(vtg_lib, ctx):
+    f0, f1, _, _ = S.warp_pair(64, 64, (1.0, 0.5), 0.5, seed=4)
+    t = _tracker(vtg_lib, ctx, 64, 64, levels=2)
+    t.build(0, f0)
+    t.build(1, f1)
+    out = t.points(0, 1, np.zeros(0, np.float32), np.zeros(0, np.float32))
+    assert len(out) == 0
+    t.close()
+
+
 def test_errors_are_status_codes(vtg_lib, ctx):
     lib = vtg_lib.lib()
     t = _tracker(vtg_lib, ctx, 64, 64, levels=2)

@@ -21,7 +21,8 @@ def _dev(a):
 
 
 @pytest.mark.parametrize("precision", [1, 2])
-@pytest.mark.parametrize("tw,th,w,h", [(32, 21, 200, 100), (32, 32, 640, 480), (64, 64, 640, 480), (96, 96, 1100, 300)])
+@pytest.mark.parametrize("tw,th,w,h", [(32, 21, 200, 100), (32, 32, 640, 480), (64, 64, 640, 480), (96, 96, 1100, 300),
+                                      (128, 128, 640, 480), (128, 40, 700, 300)])
 def test_tc_map_matches_f32_map(vtg_lib, ctx, precision, tw, th, w, h):
     frame = S.noise_frame(w, h, seed=tw + th + w)
     tpl, xs, ys, blank = S.ncc_templates(frame, max(tw, th), 2, seed=3, blank_share=0.0)
@@ -58,4 +59,43 @@ def test_tc_step2_and_window(vtg_lib, ctx, precision):
         clear = np.abs(av - bv) < 1e-7
         assert np.array_equal(ax[clear], bx[clear]) and np.array_equal(ay[clear], by[clear])
         assert (a["hx"], a["hy"]) == (b["hx"], b["hy"])
+    s.close()
+
+
+@pytest.mark.parametrize("step", [2, 4, 8, 16])
+def test_steps_against_fp64_oracle(vtg_lib, ctx, step):
+    """search_slot at every step the reference's band search uses: each candidate's half-pixel window of
+    +-(2 step - 1), the second peak and the parabola, with the F32 and the tensor-core maps, against the FP64 oracle."""
+    w, h, tw, th = 320, 240, 32, 24
+    frame = S.noise_frame(w, h, seed=40 + step)
+    tpl, xs, ys, _ = S.ncc_templates(frame, 32, 1, seed=step, blank_share=0.0)
+    patch = tpl[0][:th, :tw].astype(np.float32)
+    app = (patch - np.float32(patch.mean(dtype=np.float64))).astype(np.float32)
+    norm = float(np.sum(app.astype(np.float64) ** 2))
+    ref, _, _, _ = O.search_slot(frame.astype(np.float32), app, norm, 1, w, 1, h, step, mode=O.F64)
+    dp = _dev(frame)
+    s = vtg_lib.Search(ctx, w, h)
+    s.template(app, norm)
+    for prec in (vtg_lib.NCC_F32, vtg_lib.NCC_BF16, vtg_lib.NCC_FP16):
+        f = s.run(dp.data_ptr(), w, h, w, vtg_lib.PLANE_U8, 1, w, 1, h, step, prec)
+        assert (f["hx"], f["hy"]) == (ref["hx"], ref["hy"]), (prec, f, ref)
+        assert abs(f["ncc"] - ref["ncc"]) < 1e-4 and abs(f["second"] - ref["second"]) < 1e-4
+        assert abs(f["ox"] - ref["ox"]) < 2e-3 and abs(f["oy"] - ref["oy"]) < 2e-3
+    s.close()
+
+
+def test_window_without_corners(vtg_lib, ctx):
+    """A window that the template cannot fit anywhere in: no candidates, nothing found, no kernel runs past the
+    clamp."""
+    w, h = 200, 100
+    frame = S.noise_frame(w, h, seed=5)
+    app = np.zeros((21, 32), np.float32)
+    app[::2] = 1.0
+    app -= app.mean()
+    dp = _dev(frame)
+    s = vtg_lib.Search(ctx, w, h)
+    s.template(app, float(np.sum(app.astype(np.float64) ** 2)))
+    for prec in (vtg_lib.NCC_F32, vtg_lib.NCC_BF16):
+        f = s.run(dp.data_ptr(), w, h, w, vtg_lib.PLANE_U8, w - 20, w, 1, h, 1, prec)
+        assert f["ntop"] == 0 and f["ncc"] == -2.0
     s.close()
