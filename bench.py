@@ -202,12 +202,32 @@ def time_batched_mix(vtg, torch, ctx, device: str, nstreams: int = 64, steps: in
     torch.cuda.synchronize()
     ms = np.array([a.elapsed_time(b) for a, b in ev])
     batch.close()
+    # the plain form on the same streams: one vtg_build + vtg_cells per frame pair, the streams in turn, one stream
+    pstream = torch.cuda.Stream(device=device)
+    sp = pstream.cuda_stream
+    dc = torch.empty(16200 * 24, dtype=torch.uint8, device=device)
+    rounds = 6
+    for r in range(rounds + 1):
+        if r == 1:
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(pstream)
+        for k, t in enumerate(trackers):
+            cur = (r + 1) & 1
+            t.build(cur, dev[k][cur].data_ptr(), where=vtg.DEVICE, stream=sp)
+            t.cells_device(cur ^ 1, cur, dc.data_ptr(), 0, stream=sp)
+    e1.record(pstream)
+    torch.cuda.synchronize()
+    plain_ms = e0.elapsed_time(e1) / rounds
     for t in trackers:
         t.close()
     return {"streams": nstreams, "sizes": {"%dx%d" % sizes[i]: int((pick == i).sum()) for i in range(3)},
             "cells_per_step": cells, "frames": steps, "cells_per_s": cells * steps / (ms.sum() / 1e3),
             "ms_per_step": float(ms.mean()), "p50_ms_per_step": float(np.percentile(ms, 50)),
             "p99_ms_per_step": float(np.percentile(ms, 99)),
+            "plain": {"cells_per_s": cells / (plain_ms / 1e3), "ms_per_round": plain_ms,
+                      "form": "one vtg_build + vtg_cells per frame pair, the 64 streams in turn on one stream"},
+            "batched_vs_plain": (cells * steps / (ms.sum() / 1e3)) / (cells / (plain_ms / 1e3)),
             "autotune": {"chosen": tuned, "chosen_ms": tuned_ms, "default": default_tune, "default_ms": default_ms}}
 
 
