@@ -89,7 +89,67 @@ def lib() -> C.CDLL:
         _lib.or_m2_render.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]
         _lib.or_cell_centre.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(LkCfg), C.c_int, C.c_int,
                                         C.c_void_p, C.c_void_p]
+        _lib.or_detect_geometry.argtypes = [C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int,
+                                            C.POINTER(DetGeo)]
+        _lib.or_detect_maps.argtypes = [C.POINTER(Img), C.POINTER(DetGeo), C.c_void_p, C.c_void_p]
+        _lib.or_detect_finish.argtypes = [C.POINTER(DetGeo), C.c_void_p, C.c_void_p, C.c_int, C.c_float, C.c_float,
+                                          C.c_void_p, C.c_void_p]
     return _lib
+
+
+class DetGeo(C.Structure):
+    """struct or_det_geo: a detection region as detect_begin lays it out."""
+    _fields_ = [(k, C.c_int) for k in ("x0", "y0", "x1", "y1", "ax", "cols", "rows", "nv", "cell_rows")]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+def detect_geometry(w, h, rx, ry, rw, rh, margin):
+    """detect_begin's layout (src/kern/detect.c:28-66), or None when the rectangle is empty."""
+    g = DetGeo()
+    return g if lib().or_detect_geometry(w, h, rx, ry, rw, rh, margin, C.byref(g)) else None
+
+
+def detect_maps(plane, g: DetGeo):
+    """(resp rows x cols, cells cell_rows x nv): the Harris response and each cell's strongest (detect.c:68-141)."""
+    plane = np.ascontiguousarray(plane, np.float32)
+    m = img(plane)
+    resp = np.zeros((g.rows, g.cols), np.float32)
+    cell = np.zeros((g.cell_rows, g.nv), np.float32)
+    lib().or_detect_maps(C.byref(m), C.byref(g), _p(resp), _p(cell))
+    return resp, cell
+
+
+def detect(plane, rx, ry, rw, rh, margin, max_n, min_dist, quality):
+    """Corner detection as the tracker seeds features (track.c:988-992): (xs, ys), best first."""
+    h, w = plane.shape
+    g = detect_geometry(w, h, rx, ry, rw, rh, margin)
+    if g is None:
+        return np.zeros(0, np.float32), np.zeros(0, np.float32)
+    resp, cell = detect_maps(plane, g)
+    xs = np.zeros(max(max_n, 1), np.float32)
+    ys = np.zeros(max(max_n, 1), np.float32)
+    n = lib().or_detect_finish(C.byref(g), _p(resp), _p(cell), max_n, min_dist, quality, _p(xs), _p(ys))
+    return xs[:n].copy(), ys[:n].copy()
+
+
+def ref_detect(plane, rx, ry, rw, rh, margin, max_n, min_dist, quality):
+    """The reference's own detection: (geometry dict, resp, cells, xs, ys), or None when the rectangle is empty."""
+    plane = np.ascontiguousarray(plane, np.float32)
+    h, w = plane.shape
+    geo = np.zeros(9, np.int32)
+    resp = np.zeros(w * h + 16 * w, np.float32)
+    cell = np.zeros(w * h // 16 + 1024, np.float32)
+    xs = np.zeros(max(max_n, 1), np.float32)
+    ys = np.zeros(max(max_n, 1), np.float32)
+    n = ref().ref_detect(_p(plane), w, h, rx, ry, rw, rh, margin, max_n, min_dist, quality, _p(geo), _p(resp),
+                         _p(cell), _p(xs), _p(ys))
+    if n < 0:
+        return None
+    g = dict(zip(("x0", "y0", "x1", "y1", "ax", "cols", "rows", "nv", "cell_rows"), [int(v) for v in geo]))
+    return (g, resp[:g["rows"] * g["cols"]].reshape(g["rows"], g["cols"]).copy(),
+            cell[:g["cell_rows"] * g["nv"]].reshape(g["cell_rows"], g["nv"]).copy(), xs[:n].copy(), ys[:n].copy())
 
 
 def ref_available() -> bool:
@@ -123,6 +183,10 @@ def ref() -> C.CDLL:
         _ref.ref_search_half.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_float, C.c_int, C.c_void_p,
                                          C.c_void_p, C.c_void_p]
         _ref.ref_peak_offset.restype = C.c_double
+        _ref.ref_detect.restype = C.c_int
+        _ref.ref_detect.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int,
+                                    C.c_int, C.c_float, C.c_float, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                    C.c_void_p]
         _ref.ref_peak_offset.argtypes = [C.c_double] * 3
         _ref.ref_lk_points.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                        C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int,

@@ -11,6 +11,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include "detect.h"
 #include "img.h"
 #include "lk.h"
 #include "plane.h"
@@ -183,4 +184,32 @@ void ref_correlate(const float *interior, int w, int h, const float *app, double
     for (int i = 0; i < n; i++)
         out[i] = (double)tk_correlate(&pl, app, (long double)norm, xs[i], ys[i]);
     free_plane(&pl);
+}
+
+/* Corner detection as the tracker's seed_at runs it (src/kern/track.c:988-992): detect_begin, the three stages over
+ * their whole ranges on one thread, detect_finish. geo gets x0, y0, x1, y1, ax, cols, rows, nv, cell_rows; resp
+ * (rows x cols) and cell (cell_rows x nv) get the stages' planes when not NULL. Returns the corners found (-1: the
+ * rectangle is empty). */
+int ref_detect(const float *interior, int w, int h, float rx, float ry, float rw, float rh, int margin, int max, float min_dist, float quality,
+               int *geo, float *resp, float *cell, float *xs, float *ys)
+{
+    struct vt_plane pl = plane_from(interior, w, h);
+    void *scratch = aligned_alloc(64, (detect_scratch_bytes(w, h) + 63) & ~(size_t)63);
+    struct detect_job j;
+    int n = -1;
+    if (detect_begin(&j, &pl, rx, ry, rw, rh, margin, max, min_dist, quality, scratch)) {
+        detect_tensor(&j, 0, j.rows + 4);
+        detect_response(&j, 0, j.rows);
+        detect_cells(&j, 0, j.cell_rows);
+        const int g[9] = {j.x0, j.y0, j.x1, j.y1, j.ax, j.cols, j.rows, j.nv, j.cell_rows};
+        memcpy(geo, g, sizeof g);
+        if (resp)
+            memcpy(resp, j.resp, sizeof(float) * (size_t)j.rows * (size_t)j.cols);
+        if (cell)
+            memcpy(cell, j.cell, sizeof(float) * (size_t)j.nv * (size_t)j.cell_rows);
+        n = detect_finish(&j, xs, ys);
+    }
+    free(scratch);
+    free_plane(&pl);
+    return n;
 }

@@ -10,7 +10,10 @@
  *   - the per-cell grid of src/kern/still.c:116-141, generalised to any cell size and patch;
  *   - the appearance correlation of src/kern/track.c:184-206, its half-pixel form (track.c:1615-1647), the parabola
  *     (track.c:1650-1657), the per-cell map (track.c:301-329) and the top-8 search (track.c:1661-1726), generalised to
- *     a T_w x T_h template (T_w a multiple of 16).
+ *     a T_w x T_h template (T_w a multiple of 16);
+ *   - corner detection: the Harris response over Sobel gradients on a 5 x 5 box and the cells' strongest responses
+ *     in the reference's F32 operation order (src/kern/detect.c:68-141), exact in any IEEE arithmetic, and the
+ *     selection of detect_finish (detect.c:175-258), long double as the reference.
  *
  * Two arithmetics for everything that is floating point:
  *   OR_LANE  the reference's replay arithmetic: F32 patch sums in 16 lanes, each lane a chain of fused multiply-adds in
@@ -884,4 +887,198 @@ void or_m2_render(uint8_t *img, int w, int h, int stride, int ox, int oy)
                 }
             img[(size_t)y * stride + x] = (uint8_t)((sum + 128) >> 8);
         }
+}
+
+/* ---------------------------------------------------------------- corner detection */
+
+/* A region laid out as detect_begin does (src/kern/detect.c:28-66): the rectangle in whole pixels, clamped to the
+ * margin; columns from ax = x0 rounded down to 16, a whole number of 16-column groups; 16 x 16 cells. */
+struct or_det_geo {
+    int x0, y0, x1, y1, ax, cols, rows, nv, cell_rows;
+};
+
+/* 0 when nothing of the rectangle lies inside the margin (detect_begin's false). */
+int or_detect_geometry(int w, int h, float rx, float ry, float rw, float rh, int margin, struct or_det_geo *g)
+{
+    int x0 = (int)rx, y0 = (int)ry, x1 = (int)(rx + rw), y1 = (int)(ry + rh);
+    x0 = x0 < margin ? margin : x0;
+    y0 = y0 < margin ? margin : y0;
+    x1 = x1 > w - margin ? w - margin : x1;
+    y1 = y1 > h - margin ? h - margin : y1;
+    if (x1 <= x0 || y1 <= y0)
+        return 0;
+    g->x0 = x0;
+    g->y0 = y0;
+    g->x1 = x1;
+    g->y1 = y1;
+    g->ax = x0 & ~15;
+    g->cols = (x1 - g->ax + 15) & ~15;
+    g->rows = y1 - y0;
+    g->nv = g->cols / 16;
+    g->cell_rows = g->rows / 16 + 1;
+    return 1;
+}
+
+/* The plane at (x, y), edges replicated (the reference reads its padding). */
+static inline float det_px(const struct or_img *m, int x, int y)
+{
+    return m->p[(size_t)clampi(y, 0, m->h - 1) * m->stride + clampi(x, 0, m->w - 1)];
+}
+
+/* The Harris response of detect_tensor / detect_response (src/kern/detect.c:68-125) at resp[r * cols + c] (image row
+ * y0 + r, column ax + c) and each 16 x 16 cell's strongest response, floored at 0 (detect_cells, detect.c:127-141),
+ * at cell[cr * nv + k], in the reference's F32 operation order:
+ *   gx = (2 (M(x+1) - M(x-1)) + ((U(x+1) - U(x-1)) + (D(x+1) - D(x-1)))) / 512 as one fused multiply-add, gy alike,
+ *   the three products rounded; the 5-row sum added top to bottom; the 5-column box as (v + (v_-1 + v_+1)) +
+ *   (v_-2 + v_+2), columns outside the region's 16-column groups reading 0; det - k trace^2 as two fused
+ *   multiply-subtracts with k = 0.04. */
+void or_detect_maps(const struct or_img *m, const struct or_det_geo *g, float *resp, float *cell)
+{
+    const int cols = g->cols, rows = g->rows, trows = rows + 4;
+    const float two = 2.0f, gs = 1.0f / 512.0f, kh = 0.04f;
+    float *t = malloc(sizeof(float) * 3 * (size_t)cols * (size_t)trows);
+    float *xx = t, *xy = t + (size_t)cols * trows, *yy = t + 2 * (size_t)cols * trows;
+    for (int r = 0; r < trows; r++) {
+        const int sy = g->y0 - 2 + r;
+        for (int c = 0; c < cols; c++) {
+            const int x = g->ax + c;
+            const float dxu = det_px(m, x + 1, sy - 1) - det_px(m, x - 1, sy - 1);
+            const float dxm = det_px(m, x + 1, sy) - det_px(m, x - 1, sy);
+            const float dxd = det_px(m, x + 1, sy + 1) - det_px(m, x - 1, sy + 1);
+            const float gx = fmaf(dxm, two, dxu + dxd) * gs;
+            const float dyl = det_px(m, x - 1, sy + 1) - det_px(m, x - 1, sy - 1);
+            const float dyc = det_px(m, x, sy + 1) - det_px(m, x, sy - 1);
+            const float dyr = det_px(m, x + 1, sy + 1) - det_px(m, x + 1, sy - 1);
+            const float gy = fmaf(dyc, two, dyl + dyr) * gs;
+            const size_t i = (size_t)r * cols + c;
+            xx[i] = gx * gx;
+            xy[i] = gx * gy;
+            yy[i] = gy * gy;
+        }
+    }
+    float *v = malloc(sizeof(float) * 3 * (size_t)(cols + 4));
+    for (int r = 0; r < rows; r++) {
+        for (int q = 0; q < 3; q++) {
+            const float *p = q == 0 ? xx : q == 1 ? xy : yy;
+            float *vq = v + (size_t)q * (cols + 4) + 2;
+            vq[-2] = vq[-1] = vq[cols] = vq[cols + 1] = 0.0f;
+            for (int c = 0; c < cols; c++) {
+                const float *a = p + (size_t)r * cols + c;
+                vq[c] = (((a[0] + a[cols]) + a[2 * (size_t)cols]) + a[3 * (size_t)cols]) + a[4 * (size_t)cols];
+            }
+        }
+        const float *va = v + 2, *vb = v + (cols + 4) + 2, *vc = v + 2 * (cols + 4) + 2;
+        for (int c = 0; c < cols; c++) {
+            const float a = (va[c] + (va[c - 1] + va[c + 1])) + (va[c - 2] + va[c + 2]);
+            const float b = (vb[c] + (vb[c - 1] + vb[c + 1])) + (vb[c - 2] + vb[c + 2]);
+            const float cc = (vc[c] + (vc[c - 1] + vc[c + 1])) + (vc[c - 2] + vc[c + 2]);
+            const float tr = a + cc;
+            resp[(size_t)r * cols + c] = fmaf(-kh, tr * tr, fmaf(-b, b, a * cc));
+        }
+    }
+    for (int cr = 0; cr < g->cell_rows; cr++)
+        for (int k = 0; k < g->nv; k++) {
+            float mx = 0.0f;
+            const int r1 = (cr + 1) * 16 < rows ? (cr + 1) * 16 : rows;
+            for (int r = cr * 16; r < r1; r++)
+                for (int c = 16 * k; c < 16 * k + 16; c++)
+                    mx = fmaxf(mx, resp[(size_t)r * cols + c]);
+            cell[cr * g->nv + k] = mx;
+        }
+    free(v);
+    free(t);
+}
+
+struct or_det_cand {
+    float score;
+    int order, x, y;
+};
+
+static int det_cand_cmp(const void *a, const void *b)
+{
+    const struct or_det_cand *p = a, *q = b;
+    if (p->score != q->score)
+        return p->score > q->score ? -1 : 1;
+    return p->order - q->order;
+}
+
+/* detect_finish (src/kern/detect.c:175-258): the best cell, each cell's 3 x 3 neighbourhood strongest, the local
+ * maxima of the response inside the rectangle above max(quality x their neighbourhood's strongest, 2500), at most
+ * 8,192 in row-major scan order, scored v / local + 0.001 v / best in long double and rounded to F32; best first
+ * (equal scores in scan order), then greedily those at least min_dist from every one taken, up to max. */
+int or_detect_finish(const struct or_det_geo *g, const float *resp, const float *cell, int max, float min_dist,
+                     float quality, float *xs, float *ys)
+{
+    const int nv = g->nv, ch = g->cell_rows, cols = g->cols;
+    float best = 0.0f;
+    for (int i = 0; i < nv * ch; i++)
+        if (cell[i] > best)
+            best = cell[i];
+    if (best <= 0.0f)
+        return 0;
+    float *near = malloc(sizeof(float) * (size_t)nv * ch);
+    for (int cr = 0; cr < ch; cr++)
+        for (int k = 0; k < nv; k++) {
+            float mx = 0.0f;
+            for (int a = cr > 0 ? cr - 1 : 0; a <= cr + 1 && a < ch; a++)
+                for (int b = k > 0 ? k - 1 : 0; b <= k + 1 && b < nv; b++)
+                    if (cell[a * nv + b] > mx)
+                        mx = cell[a * nv + b];
+            near[cr * nv + k] = mx;
+        }
+    const int lane_lo = g->x0 - g->ax > 1 ? g->x0 - g->ax : 1, lane_hi = g->x1 - g->ax < cols - 1 ? g->x1 - g->ax : cols - 1;
+    struct or_det_cand *cand = malloc(sizeof *cand * 8192);
+    int nc = 0;
+    for (int r = 1; r < g->rows - 1 && nc < 8192; r++) {
+        const int cr = r / 16;
+        for (int c = lane_lo; c < lane_hi && nc < 8192; c++) {
+            const float v = resp[(size_t)r * cols + c];
+            const long double local = (long double)near[cr * nv + c / 16], rel = local * (long double)quality;
+            const float thresh = (float)(rel > 2500.0L ? rel : 2500.0L);
+            if (!(thresh < v))
+                continue;
+            int keep = 1;
+            for (int dr = -1; dr <= 1 && keep; dr++)
+                for (int dc = -1; dc <= 1 && keep; dc++) {
+                    if (!dr && !dc)
+                        continue;
+                    const int cc = c + dc;
+                    const float nb = cc < 0 || cc >= cols ? 0.0f : resp[(size_t)(r + dr) * cols + cc];
+                    keep = nb <= v;
+                }
+            if (!keep)
+                continue;
+            cand[nc].score = (float)((long double)v / local + 0.001L * (long double)v / (long double)best);
+            cand[nc].order = nc;
+            cand[nc].x = g->ax + c;
+            cand[nc].y = g->y0 + r;
+            nc++;
+        }
+    }
+    qsort(cand, (size_t)nc, sizeof *cand, det_cand_cmp);
+    const long double min2 = (long double)min_dist * (long double)min_dist;
+    int need = (int)min2;
+    if ((long double)need < min2)
+        need++;
+    int taken = 0;
+    int *tx = malloc(sizeof(int) * (size_t)(max > 0 ? max : 1)), *ty = malloc(sizeof(int) * (size_t)(max > 0 ? max : 1));
+    for (int i = 0; i < nc && taken < max; i++) {
+        int far = 1;
+        for (int k = 0; k < taken && far; k++) {
+            const int dx = tx[k] - cand[i].x, dy = ty[k] - cand[i].y;
+            far = dx * dx + dy * dy >= need;
+        }
+        if (far) {
+            tx[taken] = cand[i].x;
+            ty[taken] = cand[i].y;
+            xs[taken] = (float)cand[i].x;
+            ys[taken] = (float)cand[i].y;
+            taken++;
+        }
+    }
+    free(ty);
+    free(tx);
+    free(cand);
+    free(near);
+    return taken;
 }

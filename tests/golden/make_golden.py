@@ -14,6 +14,9 @@ Writes:
                     of the 4,080 cells at half resolution.
   still_vectors.npz the reference's still_vectors (15 x 15, one level, 6 iterations, flowback 0.25) on a 640 x 480 pair.
   ncc_32x21.npz     tk_correlate at 2,000 corners and search_slot (step 1 and 2) for a 32 x 21 template on a Q6 plane.
+  detect.npz        corner detection (detect_begin, the three stages, detect_finish) over seven regions of two Q6
+                    planes: each region's layout, a hash of its response map, its cells' strongest responses and the
+                    corners found.
 Frames are not stored: the generator reproduces them bit for bit, and their hashes are stored to prove it.
 """
 from __future__ import annotations
@@ -111,6 +114,33 @@ def main(ref_root: str = "/root/reference") -> None:
                         s1_map_v=mv1, s1_map_x=mx1, s1_map_y=my1,
                         s2=np.array([f2s["hx"], f2s["hy"]], np.int32), s2_ncc=f2s["ncc"], s2_second=f2s["second"],
                         s2_map_v=mv2, s2_map_x=mx2, s2_map_y=my2, half_hx=hxs, half_hy=hys, half=half)
+    # corner detection (detect.c) on Q6 planes: a textured 640 x 480 frame with a flat block, and a 1080p frame
+    d0, _, _, _ = S.warp_pair(640, 480, (1.7, -0.8), 0.5, seed=1)
+    d0 = d0.copy()
+    d0[300:420, 40:200] = 128
+    dplane = O.pyramid(d0, 1)[0]
+    hplane = O.pyramid(f0, 1)[0]
+    cases = [(0, 100.3, 80.7, 384, 307, 12, 128, 8.0, 0.05), (0, 0, 0, 640, 480, 12, 512, 6.0, 0.01),
+             (0, 600, 400, 100, 100, 12, 64, 5.5, 0.1), (0, 17, 33, 50, 40, 4, 32, 3.0, 0.02),
+             (0, 200.5, 150.25, 15, 10, 12, 16, 4.0, 0.05), (0, 50, 310, 140, 100, 12, 64, 5.0, 0.05),
+             (1, 0, 0, 1920, 1080, 12, 512, 10.0, 0.01)]
+    geo, resp_fnv, cells, cell_n, xs_all, ys_all, counts = [], [], [], [], [], [], []
+    for (which, rx, ry, rw, rh, margin, mx, md, q) in cases:
+        r = O.ref_detect(hplane if which else dplane, rx, ry, rw, rh, margin, mx, md, q)
+        g, resp, cell, xs, ys = r
+        geo.append([g[k] for k in ("x0", "y0", "x1", "y1", "ax", "cols", "rows", "nv", "cell_rows")])
+        resp_fnv.append(O.fnv(resp))
+        cells.append(cell.ravel())
+        cell_n.append(cell.size)
+        xs_all.append(xs)
+        ys_all.append(ys)
+        counts.append(len(xs))
+    np.savez_compressed(os.path.join(HERE, "detect.npz"), frame_fnv=np.uint64(O.fnv(d0)),
+                        frame1080_fnv=np.uint64(O.fnv(f0)), cases=np.array(cases, np.float64),
+                        geo=np.array(geo, np.int32), resp_fnv=np.array(resp_fnv, np.uint64),
+                        cells=np.concatenate(cells).astype(np.float32), cell_n=np.array(cell_n, np.int32),
+                        xs=np.concatenate(xs_all).astype(np.float32), ys=np.concatenate(ys_all).astype(np.float32),
+                        counts=np.array(counts, np.int32))
     print("golden fixtures written to", HERE)
 
 

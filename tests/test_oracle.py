@@ -217,3 +217,66 @@ def test_lk_edge_cases_against_reference_code():
             mine = O.lk_points(P0, P1, levels - 1, cfg, xs, ys, gx, gy, max_fb=fb, mode=O.LANE)
             ref = O.ref_lk_points(f0, f1, levels, levels - 1, cfg, xs, ys, gx, gy, max_fb=fb, threads=1)
             assert mine.tobytes() == ref.tobytes(), (pw, ph, levels, fb)
+
+
+def _detect_planes():
+    """The detection fixture's two Q6 planes: a textured 640 x 480 frame with a flat block, and 1080p level 0."""
+    d0, _, _, _ = S.warp_pair(640, 480, (1.7, -0.8), 0.5, seed=1)
+    d0 = d0.copy()
+    d0[300:420, 40:200] = 128
+    f0, _, _, _ = S.warp_pair(1920, 1080, S.seeded_shift(2, 0), 0.5, seed=2)
+    return d0, f0
+
+
+def test_detect_fixture(golden):
+    """The oracle's corner detection against the reference's (tests/golden/detect.npz): the region's layout, the
+    response map and the cells bit for bit everywhere (F32 in the reference's operation order); the corners found bit
+    for bit on x86-64, where long double is the reference's x87 format."""
+    g = np.load(os.path.join(golden, "detect.npz"))
+    d0, f0 = _detect_planes()
+    assert O.fnv(d0) == int(g["frame_fnv"]) and O.fnv(f0) == int(g["frame1080_fnv"])
+    planes = [O.pyramid(d0, 1)[0], O.pyramid(f0, 1)[0]]
+    c0 = p0 = 0
+    for k, (which, rx, ry, rw, rh, margin, mx, md, q) in enumerate(g["cases"]):
+        plane = planes[int(which)]
+        geo = O.detect_geometry(plane.shape[1], plane.shape[0], rx, ry, rw, rh, int(margin))
+        gd = geo.as_dict()
+        assert [gd[n] for n in ("x0", "y0", "x1", "y1", "ax", "cols", "rows", "nv", "cell_rows")] == list(g["geo"][k])
+        resp, cell = O.detect_maps(plane, geo)
+        assert O.fnv(resp) == int(g["resp_fnv"][k])
+        n = int(g["cell_n"][k])
+        assert np.array_equal(cell.ravel(), g["cells"][c0:c0 + n])
+        c0 += n
+        xs, ys = O.detect(plane, rx, ry, rw, rh, int(margin), int(mx), float(md), float(q))
+        m = int(g["counts"][k])
+        if X86:
+            assert np.array_equal(xs, g["xs"][p0:p0 + m]) and np.array_equal(ys, g["ys"][p0:p0 + m]), k
+        else:
+            assert abs(len(xs) - m) <= max(1, m // 50)
+        p0 += m
+
+
+@pytest.mark.skipif(not (O.ref_available() and X86), reason="needs the reference tree and x86-64")
+def test_detect_against_reference_code():
+    """Random regions, margins, spacings and qualities over three planes: the oracle equals detect_begin, the three
+    stages and detect_finish of the reference bit for bit."""
+    rng = np.random.default_rng(12)
+    planes = [O.pyramid(S.noise_frame(320, 240, seed=s), 1)[0] for s in (3, 4)]
+    planes.append(O.pyramid(O.m1_image(512, 384), 1)[0])
+    for _ in range(40):
+        plane = planes[int(rng.integers(0, len(planes)))]
+        h, w = plane.shape
+        rx, ry = float(rng.uniform(-20, w - 10)), float(rng.uniform(-20, h - 10))
+        rw, rh = float(rng.uniform(5, w)), float(rng.uniform(5, h))
+        margin, mx = int(rng.integers(3, 20)), int(rng.integers(1, 513))
+        md, q = float(rng.uniform(1.0, 15.0)), float(rng.uniform(0.0, 0.2))
+        ref = O.ref_detect(plane, rx, ry, rw, rh, margin, mx, md, q)
+        geo = O.detect_geometry(w, h, rx, ry, rw, rh, margin)
+        if ref is None:
+            assert geo is None
+            continue
+        rg, rresp, rcell, rxs, rys = ref
+        resp, cell = O.detect_maps(plane, geo)
+        assert np.array_equal(resp, rresp) and np.array_equal(cell, rcell)
+        xs, ys = O.detect(plane, rx, ry, rw, rh, margin, mx, md, q)
+        assert np.array_equal(xs, rxs) and np.array_equal(ys, rys)
