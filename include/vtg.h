@@ -237,6 +237,30 @@ int vtg_search_run_noalloc(const void *plane, int w, int h, int pitch, int plane
                            float norm, int x0, int x1, int y0, int y1, int step, struct vtg_found *found, float *map_v,
                            int *map_x, int *map_y, void *stream);
 
+/* ---- corner detection: seed_at's detect_begin, detect_tensor / detect_response / detect_cells, detect_finish
+ *      (src/kern/track.c:988-992; src/kern/detect.h:21-37, src/kern/detect.c:28-258) ---- */
+
+typedef struct vtg_detector vtg_detector;
+
+/* Device bytes of a detector for regions up to max_w x max_h: the response map, the cells, 8,192 candidates. */
+size_t vtg_detector_bytes(int max_w, int max_h);
+int vtg_detector_create(vtg_ctx *ctx, int max_w, int max_h, vtg_detector **out);
+void vtg_detector_destroy(vtg_detector *d);
+void *vtg_detector_stream(const vtg_detector *d);
+/* Corners inside the rectangle (rx, ry, rw, rh) of a Q6 plane (w x h, rows `pitch` floats apart, device memory), kept
+ * `margin` pixels from its edges: the Harris response on a 5 x 5 box over Sobel gradients, the local maxima above
+ * max(quality x the strongest of their 3 x 3 cells of 16 x 16, 2500), best first, and greedily those at least min_dist
+ * from every one taken, up to max (<= 512). xs, ys get the corners, *count their number. where: VTG_HOST (xs, ys,
+ * count in host memory; the call waits) or VTG_DEVICE (asynchronous on `stream`, or the detector's). */
+int vtg_detect(vtg_detector *d, const float *plane, int w, int h, int pitch, float rx, float ry, float rw, float rh,
+               int margin, int max, float min_dist, float quality, float *xs, float *ys, int *count, int where,
+               void *stream);
+/* For checking, after vtg_detect: its region's layout (geo: x0, y0, x1, y1, ax, cols, rows, nv, cell_rows), its
+ * response map (rows x cols) and its cells' strongest responses (cell_rows x nv), as detect_begin, detect_response
+ * and detect_cells leave them; resp and cells may be NULL. Waits for the detector's stream. */
+int vtg_detect_maps(vtg_detector *d, float rx, float ry, float rw, float rh, int w, int h, int margin, int *geo,
+                    float *resp, float *cells);
+
 #ifdef __cplusplus
 }
 #endif

@@ -487,3 +487,56 @@ def compat() -> C.CDLL:
         L.vtg_compat_error.restype = C.c_int
         L._compat_sigs = True
     return L
+
+
+# ---------------------------------------------------------------- corner detection
+
+class Detector:
+    """A corner detector (vtg_detector): detect_begin .. detect_finish of the reference on the GPU."""
+
+    def __init__(self, ctx: Context, max_w: int, max_h: int):
+        L = lib()
+        vp, i, f = C.c_void_p, C.c_int, C.c_float
+        L.vtg_detector_create.argtypes = [vp, i, i, C.POINTER(vp)]
+        L.vtg_detector_destroy.argtypes = [vp]
+        L.vtg_detector_destroy.restype = None
+        L.vtg_detector_stream.argtypes = [vp]
+        L.vtg_detector_stream.restype = vp
+        L.vtg_detect.argtypes = [vp, vp, i, i, i, f, f, f, f, i, i, f, f, vp, vp, vp, i, vp]
+        L.vtg_detect_maps.argtypes = [vp, f, f, f, f, i, i, i, vp, vp, vp]
+        self.ctx = ctx
+        self.h = C.c_void_p()
+        check(L.vtg_detector_create(ctx.h, max_w, max_h, C.byref(self.h)), "vtg_detector_create")
+        ctx._trackers.add(self)
+
+    def detect(self, plane_ptr: int, w: int, h: int, pitch: int, rx, ry, rw, rh, margin: int, max_n: int,
+               min_dist: float, quality: float):
+        """(xs, ys), best first: the corners of a device Q6 plane."""
+        xs = np.zeros(max(max_n, 1), np.float32)
+        ys = np.zeros(max(max_n, 1), np.float32)
+        n = C.c_int()
+        check(lib().vtg_detect(self.h, plane_ptr, w, h, pitch, rx, ry, rw, rh, margin, max_n, min_dist, quality,
+                               _p(xs), _p(ys), C.byref(n), HOST, None), "vtg_detect")
+        return xs[:n.value].copy(), ys[:n.value].copy()
+
+    def maps(self, rx, ry, rw, rh, w: int, h: int, margin: int):
+        """(geometry dict, resp, cells) of the last detect."""
+        geo = np.zeros(9, np.int32)
+        check(lib().vtg_detect_maps(self.h, rx, ry, rw, rh, w, h, margin, _p(geo), None, None), "vtg_detect_maps")
+        g = dict(zip(("x0", "y0", "x1", "y1", "ax", "cols", "rows", "nv", "cell_rows"), [int(v) for v in geo]))
+        resp = np.zeros((g["rows"], g["cols"]), np.float32)
+        cell = np.zeros((g["cell_rows"], g["nv"]), np.float32)
+        check(lib().vtg_detect_maps(self.h, rx, ry, rw, rh, w, h, margin, _p(geo), _p(resp), _p(cell)),
+              "vtg_detect_maps")
+        return g, resp, cell
+
+    def close(self):
+        if self.h:
+            lib().vtg_detector_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
