@@ -507,6 +507,61 @@ def run_ncc(args) -> dict:
     return out
 
 
+def run_detect(args) -> dict:
+    """Corner detection (seed_at's detect_begin .. detect_finish) on level 0 of a 1080p frame: a 384 x 307 box (the size
+    the reference times on the card: 3.78 ms on its thread team) and the whole frame. CUDA-event time of the whole
+    detection, the response kernel's share, and the FP64-free selection; the oracle's CPU time beside it; the corners
+    against the oracle's."""
+    import torch
+
+    import vtg
+    import vtg_build
+
+    sys.path.insert(0, ORACLE)
+    import oracle as O
+
+    vtg_build.build()
+    f0, _, _, _ = __import__("vtg_synth").warp_pair(W, H, __import__("vtg_synth").seeded_shift(2, 0), 0.5, seed=2)
+    plane = O.pyramid(f0, 1)[0]
+    d = torch.from_numpy(plane).cuda()
+    torch.cuda.synchronize()
+    ctx = vtg.Context(0)
+    det = vtg.Detector(ctx, W, H)
+    stream = torch.cuda.ExternalStream(vtg.lib().vtg_detector_stream(det.h))
+    out = {"metric": "corner detection ms per region (Harris response, cells, selection) on a 1920x1080 Q6 plane",
+           "unit": "ms", "higher_is_better": False, "results": []}
+    pk = peaks()
+    for name, (rx, ry, rw, rh, mx, md, q) in (("box 384x307", (700.5, 400.25, 384, 307, 128, 8.0, 0.05)),
+                                              ("whole frame", (0, 0, W, H, 512, 10.0, 0.01))):
+        args_ = (d.data_ptr(), W, H, W, rx, ry, rw, rh, 12, mx, md, q)
+        xs, ys = det.detect(*args_)
+        reps = 20
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+        xd = torch.empty(512, device="cuda")
+        yd = torch.empty(512, device="cuda")
+        cd = torch.empty(1, dtype=torch.int32, device="cuda")
+        for a, b in ev:
+            a.record(stream)
+            vtg.check(vtg.lib().vtg_detect(det.h, d.data_ptr(), W, H, W, rx, ry, rw, rh, 12, mx, md, q, xd.data_ptr(),
+                                           yd.data_ptr(), cd.data_ptr(), vtg.DEVICE, None), "vtg_detect")
+            b.record(stream)
+        torch.cuda.synchronize()
+        ms = float(np.median([a.elapsed_time(b) for a, b in ev]))
+        g = O.detect_geometry(W, H, rx, ry, rw, rh, 12)
+        t0 = time.perf_counter()
+        oxs, oys = O.detect(plane, rx, ry, rw, rh, 12, mx, md, q)
+        cpu_ms = 1e3 * (time.perf_counter() - t0)
+        # the response pass reads the plane tile once and writes the response: its algorithmic bytes
+        resp_bytes = 4 * (g.rows + 4) * (g.cols + 4) + 4 * g.rows * g.cols
+        out["results"].append({"region": name, "rows": g.rows, "cols": g.cols, "corners": int(len(xs)), "ms": ms,
+                               "same_as_oracle": bool(np.array_equal(xs, oxs) and np.array_equal(ys, oys)),
+                               "cpu_oracle_ms_1_thread": cpu_ms, "response_algorithmic_bytes": resp_bytes})
+    det.close()
+    ctx.close()
+    out["hbm_gbs"] = pk.get("hbm_gbs")
+    return out
+
+
 def run_profile(args) -> None:
     """Launches for an ncu capture, nothing timed: `batch` primes B 1080p streams (2 batched steps) and runs 2 more
     (capture lk_batch_kernel with -s 2); `ncc` runs one 1080p whole-picture search per precision (32 x 32 template)."""
@@ -531,6 +586,18 @@ def run_profile(args) -> None:
             batch.launch(k & 1)
         ctx.sync()
         print("profile batch: %d streams, %d cells a step" % (B, batch.cells(0)))
+    elif args.profile == "detect":
+        sys.path.insert(0, ORACLE)
+        import oracle as O
+
+        f0, _, _, _ = S.warp_pair(W, H, S.seeded_shift(2, 0), 0.5, seed=2)
+        d = torch.from_numpy(O.pyramid(f0, 1)[0]).cuda()
+        torch.cuda.synchronize()
+        det = vtg.Detector(ctx, W, H)
+        for reg in ((700.5, 400.25, 384, 307, 128, 8.0, 0.05), (0, 0, W, H, 512, 10.0, 0.01)):
+            xs, ys = det.detect(d.data_ptr(), W, H, W, *reg[:4], 12, *reg[4:])
+            print("profile detect: %d corners" % len(xs))
+        det.close()
     else:
         frame = S.noise_frame(W, H, seed=3)
         tpl, xs, ys, _ = S.ncc_templates(frame, 32, 1, seed=1, blank_share=0.0)
@@ -556,7 +623,8 @@ def main():
     ap.add_argument("--streams", type=int, default=8, help="1080p streams a batched step")
     ap.add_argument("--ncc", action="store_true",
                     help="the whole-picture appearance search on a 1080p frame (32, 64, 96 templates), per precision")
-    ap.add_argument("--profile", default=None, choices=["batch", "ncc"],
+    ap.add_argument("--detect", action="store_true", help="corner detection on a 1080p plane: a 384 x 307 box, the frame")
+    ap.add_argument("--profile", default=None, choices=["batch", "ncc", "detect"],
                     help="a short run for an ncu capture: the batched step (prime, then 2 steps) or one NCC search")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -565,6 +633,9 @@ def main():
         return
     if args.ncc:
         print(json.dumps(run_ncc(args)))
+        return
+    if args.detect:
+        print(json.dumps(run_detect(args)))
         return
     line = run_reference(args) if args.impl == "reference" else run_ours(args)
     if line is not None:

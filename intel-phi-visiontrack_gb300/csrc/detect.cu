@@ -14,13 +14,14 @@
  *   det_response  a CTA a tile of 16 rows x 64 columns: the plane tile, the tensor, the row sums and the box in
  *                 shared memory; the response out, and the four cells' strongest (floored at 0)
  *   det_near      the best cell, and each cell's 3 x 3 neighbourhood strongest
- *   det_count     a warp a row: the local maxima above max(quality x neighbourhood, 2500), counted
- *   det_scan      the rows' counts scanned: each row's first place in scan order
- *   det_collect   a warp a row: the candidates in scan order, the first 8,192 kept (DETECT_MAX_CANDIDATES), each
+ *   det_count     a warp an eighth of a row: the local maxima above max(quality x neighbourhood, 2500), counted
+ *   det_scan      the segments' counts scanned: each segment's first place in scan order
+ *   det_collect   a warp a segment: the candidates in scan order, the first 8,192 kept (DETECT_MAX_CANDIDATES), each
  *                 scored v / local + 0.001 v / best in FP64 and rounded to F32 (the reference's long double rounds to
  *                 the same F32 but where the sum lies within 2^-53 of a rounding boundary)
  *   det_select    one CTA: the candidates sorted by (score descending, scan order) -- a bitonic sort of 64-bit keys in
- *                 shared memory -- then the greedy spacing in one warp, up to max corners.
+ *                 shared memory -- their places gathered into shared memory, then the greedy spacing 32 candidates
+ *                 a round (the distance tests across the CTA, the order within the 32 in one warp), up to max corners.
  * The threshold needs no long double: local x quality is an exact product of two F32s, so its F32 rounding is the
  * reference's (float)(rel) and max(fl(rel), 2500) equals its (float)(rel > 2500 ? rel : 2500). */
 #include <math.h>
@@ -35,6 +36,7 @@
 #define DET_TX 64           /* a response tile: four cells wide ... */
 #define DET_TY 16           /* ... and one cell row high */
 #define DET_SELECT_THREADS 1024
+#define DET_SEGS 8          /* a row's candidate columns in this many segments, a warp each */
 
 struct DetGeo {
     int x0, y0, x1, y1, ax, cols, rows, nv, cell_rows;
@@ -199,24 +201,35 @@ __device__ __forceinline__ void det_lanes(const DetGeo &g, int &lo, int &hi)
     hi = g.x1 - g.ax < g.cols - 1 ? g.x1 - g.ax : g.cols - 1;
 }
 
+/* Segment s of a row's candidate columns [lo, hi): [a, b), consecutive segments in column order. */
+__device__ __forceinline__ void det_segment(const DetGeo &g, int s, int &a, int &b)
+{
+    int lo, hi;
+    det_lanes(g, lo, hi);
+    const int len = hi > lo ? hi - lo : 0, per = (len + DET_SEGS - 1) / DET_SEGS;
+    a = lo + s * per;
+    b = min(a + per, lo + len);
+}
+
 __global__ void __launch_bounds__(256) det_count(DetPrm q, const float *__restrict__ resp,
                                                  const float *__restrict__ near, const float *__restrict__ best,
                                                  int *__restrict__ rowcount)
 {
-    const int r = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    const int w = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    const int r = w / DET_SEGS, sg = w - r * DET_SEGS;
     if (r >= q.g.rows)
         return;
     int cnt = 0;
     if (*best > 0.0f && r >= 1 && r < q.g.rows - 1) {
-        int lo, hi;
-        det_lanes(q.g, lo, hi);
-        for (int c0 = lo; c0 < hi; c0 += 32) {
+        int a, b;
+        det_segment(q.g, sg, a, b);
+        for (int c0 = a; c0 < b; c0 += 32) {
             const int c = c0 + lane;
-            cnt += __popc(__ballot_sync(VTG_FULL, c < hi && det_candidate(q, resp, near, r, c)));
+            cnt += __popc(__ballot_sync(VTG_FULL, c < b && det_candidate(q, resp, near, r, c)));
         }
     }
     if (lane == 0)
-        rowcount[r] = cnt;
+        rowcount[w] = cnt;
 }
 
 /* Each row's first place in scan order (exclusive scan over rows), and the candidates kept: at most 8,192. */
@@ -250,18 +263,19 @@ __global__ void __launch_bounds__(256) det_collect(DetPrm q, const float *__rest
                                                    const int *__restrict__ rowbase, unsigned long long *__restrict__ keys,
                                                    int *__restrict__ cx, int *__restrict__ cy)
 {
-    const int r = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    const int w = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    const int r = w / DET_SEGS, sg = w - r * DET_SEGS;
     if (r < 1 || r >= q.g.rows - 1 || !(*best > 0.0f))
         return;
-    int pos = rowbase[r];
+    int pos = rowbase[w];
     if (pos >= DET_MAX_CAND)
         return;
     const double bst = (double)*best;
-    int lo, hi;
-    det_lanes(q.g, lo, hi);
-    for (int c0 = lo; c0 < hi && pos < DET_MAX_CAND; c0 += 32) {
+    int a, b;
+    det_segment(q.g, sg, a, b);
+    for (int c0 = a; c0 < b && pos < DET_MAX_CAND; c0 += 32) {
         const int c = c0 + lane;
-        const bool f = c < hi && det_candidate(q, resp, near, r, c);
+        const bool f = c < b && det_candidate(q, resp, near, r, c);
         const unsigned m = __ballot_sync(VTG_FULL, f);
         const int p = pos + __popc(m & ((1u << lane) - 1u));
         if (f && p < DET_MAX_CAND) {
@@ -283,8 +297,9 @@ __global__ void __launch_bounds__(DET_SELECT_THREADS) det_select(DetPrm q, const
                                                                  float *__restrict__ xs, float *__restrict__ ys,
                                                                  int *__restrict__ count)
 {
-    extern __shared__ unsigned long long s_key[]; /* DET_MAX_CAND */
-    __shared__ int s_tx[512], s_ty[512];
+    extern __shared__ unsigned long long s_key[]; /* DET_MAX_CAND keys, then their places as (x, y) pairs */
+    __shared__ int s_tx[512], s_ty[512], s_far[32], s_taken;
+    int2 *s_xy = reinterpret_cast<int2 *>(s_key + DET_MAX_CAND);
     const int tid = threadIdx.x;
     const int n = *best > 0.0f ? *ncand : 0;
     int P = 1;
@@ -307,30 +322,58 @@ __global__ void __launch_bounds__(DET_SELECT_THREADS) det_select(DetPrm q, const
             }
             __syncthreads();
         }
-    if (tid >= 32)
-        return;
-    const int lane = tid;
-    int taken = 0;
-    for (int i = 0; i < n && taken < q.max; i++) {
+    for (int i = tid; i < n; i += blockDim.x) {
         const int p = (int)(s_key[i] & 0xFFFFFFFFull);
-        const int x = cx[p], y = cy[p];
-        bool far = true;
-        for (int t = lane; t < taken; t += 32) {
-            const int dx = s_tx[t] - x, dy = s_ty[t] - y;
-            far = far && dx * dx + dy * dy >= q.need;
-        }
-        if (__all_sync(VTG_FULL, far)) {
-            if (lane == 0) {
-                s_tx[taken] = x;
-                s_ty[taken] = y;
-                xs[taken] = (float)x;
-                ys[taken] = (float)y;
-            }
-            taken++;
-            __syncwarp();
-        }
+        s_xy[i] = make_int2(cx[p], cy[p]);
     }
-    if (lane == 0)
+    if (tid == 0)
+        s_taken = 0;
+    __syncthreads();
+    /* The greedy spacing, 32 candidates at a time and exactly the one-by-one order: warp w tests candidate base + w
+     * against every corner taken so far (a lane per 32 of them); then warp 0 settles the 32 in order, candidate k
+     * rejecting every later one of the 32 too close to it once it is taken. */
+    const int lane = tid & 31, warp = tid >> 5;
+    int taken = 0;
+    for (int base = 0; base < n && taken < q.max; base += 32) {
+        const int i = base + warp;
+        bool far = i < n;
+        if (far) {
+            const int2 c = s_xy[i];
+            for (int t = lane; t < taken; t += 32) {
+                const int dx = s_tx[t] - c.x, dy = s_ty[t] - c.y;
+                far = far && dx * dx + dy * dy >= q.need;
+            }
+        }
+        far = __all_sync(VTG_FULL, far);
+        if (lane == 0)
+            s_far[warp] = far;
+        __syncthreads();
+        if (warp == 0) {
+            bool ok = s_far[lane] != 0;
+            const int2 c = ok ? s_xy[base + lane] : make_int2(0, 0);
+            int cnt = taken;
+            for (int k = 0; k < 32 && cnt < q.max; k++) {
+                if (!__shfl_sync(VTG_FULL, (int)ok, k))
+                    continue;
+                const int kx = __shfl_sync(VTG_FULL, c.x, k), ky = __shfl_sync(VTG_FULL, c.y, k);
+                if (lane == k) {
+                    s_tx[cnt] = kx;
+                    s_ty[cnt] = ky;
+                    xs[cnt] = (float)kx;
+                    ys[cnt] = (float)ky;
+                } else if (lane > k) {
+                    const int dx = kx - c.x, dy = ky - c.y;
+                    ok = ok && dx * dx + dy * dy >= q.need;
+                }
+                cnt++;
+            }
+            if (lane == 0)
+                s_taken = cnt;
+        }
+        __syncthreads();
+        taken = s_taken;
+    }
+    if (tid == 0)
         *count = taken;
 }
 
@@ -388,9 +431,9 @@ static DetLayout det_layout(int max_w, int max_h, int &max_cols, int &max_cells)
     L.best = b;
     b += 256;
     L.rowcount = b;
-    b += up256(sizeof(int) * (size_t)max_h);
+    b += up256(sizeof(int) * (size_t)max_h * DET_SEGS);
     L.rowbase = b;
-    b += up256(sizeof(int) * (size_t)max_h);
+    b += up256(sizeof(int) * (size_t)max_h * DET_SEGS);
     L.ncand = b;
     b += 256;
     L.keys = b;
@@ -523,11 +566,11 @@ extern "C" int vtg_detect(vtg_detector *d, const float *plane, int w, int h, int
     det_response<<<dim3((g.cols + DET_TX - 1) / DET_TX, (g.rows + DET_TY - 1) / DET_TY), 256, 0, st>>>(q, d->resp,
                                                                                                    d->cell);
     det_near<<<1, 1024, 0, st>>>(g, d->cell, d->near, d->best);
-    const int rblocks = (g.rows * 32 + 255) / 256;
+    const int rblocks = (g.rows * DET_SEGS * 32 + 255) / 256;
     det_count<<<rblocks, 256, 0, st>>>(q, d->resp, d->near, d->best, d->rowcount);
-    det_scan<<<1, 1024, 0, st>>>(g.rows, d->rowcount, d->rowbase, d->ncand);
+    det_scan<<<1, 1024, 0, st>>>(g.rows * DET_SEGS, d->rowcount, d->rowbase, d->ncand);
     det_collect<<<rblocks, 256, 0, st>>>(q, d->resp, d->near, d->best, d->rowbase, d->keys, d->cx, d->cy);
-    const int smem = (int)(sizeof(unsigned long long) * DET_MAX_CAND);
+    const int smem = (int)((sizeof(unsigned long long) + sizeof(int2)) * DET_MAX_CAND);
     CU(cudaFuncSetAttribute(det_select, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     float *oxs = where == VTG_DEVICE ? xs : d->xs, *oys = where == VTG_DEVICE ? ys : d->ys;
     int *ocount = where == VTG_DEVICE ? count : d->count;
