@@ -13,15 +13,17 @@
  * Pipeline, one stream, no host round trip:
  *   det_response  a CTA a tile of 16 rows x 64 columns: the plane tile, the tensor, the row sums and the box in
  *                 shared memory; the response out, and the four cells' strongest (floored at 0)
- *   det_near      the best cell, and each cell's 3 x 3 neighbourhood strongest
+ *   det_near      each cell's 3 x 3 neighbourhood strongest, a thread a cell, and the best cell
  *   det_count     a warp an eighth of a row: the local maxima above max(quality x neighbourhood, 2500), counted
  *   det_scan      the segments' counts scanned: each segment's first place in scan order
  *   det_collect   a warp a segment: the candidates in scan order, the first 8,192 kept (DETECT_MAX_CANDIDATES), each
  *                 scored v / local + 0.001 v / best in FP64 and rounded to F32 (the reference's long double rounds to
  *                 the same F32 but where the sum lies within 2^-53 of a rounding boundary)
- *   det_select    one CTA: the candidates sorted by (score descending, scan order) -- a bitonic sort of 64-bit keys in
- *                 shared memory -- their places gathered into shared memory, then the greedy spacing 32 candidates
- *                 a round (the distance tests across the CTA, the order within the 32 in one warp), up to max corners.
+ *   det_select    one CTA: the candidates sorted by (score descending, scan order) -- a stable radix sort of the 32-bit
+ *                 score keys in shared memory, four 8-bit passes -- their places gathered, then the greedy spacing
+ *                 in blocks of 1,024 candidates, a thread each, settled in parallel passes with the in-order result,
+ *                 up to max corners. The corners taken and the block's candidates sit in grids of linked lists (cells
+ *                 at least the spacing wide), so a candidate looks at its 3 x 3 grid cells only.
  * The threshold needs no long double: local x quality is an exact product of two F32s, so its F32 rounding is the
  * reference's (float)(rel) and max(fl(rel), 2500) equals its (float)(rel > 2500 ? rel : 2500). */
 #include <math.h>
@@ -37,6 +39,13 @@
 #define DET_TY 16           /* ... and one cell row high */
 #define DET_SELECT_THREADS 1024
 #define DET_SEGS 8          /* a row's candidate columns in this many segments, a warp each */
+#define DET_GRID_MAX 16384  /* the taken corners' grid: at most this many cells (their list heads fill the keys' space) */
+#define DET_RADIX 256       /* the sort's digit: 8 bits, four passes over the 32-bit score key */
+#define DET_HIST_PITCH 257  /* a warp's digit counts: one word of padding against bank conflicts */
+static_assert(DET_SELECT_THREADS / 32 * 256 == DET_MAX_CAND, "the sort: a warp 256 candidates, 8 a lane");
+static_assert(DET_GRID_MAX <= 2 * DET_MAX_CAND, "grid heads in the spare keys' and places' space");
+static_assert(DET_SELECT_THREADS * 2 <= DET_MAX_CAND, "a block's places in the keys' space");
+static_assert(DET_GRID_MAX <= 2 * DET_HIST_PITCH * 32, "block grid heads in the counts' space");
 
 struct DetGeo {
     int x0, y0, x1, y1, ax, cols, rows, nv, cell_rows;
@@ -49,6 +58,7 @@ struct DetPrm {
     float quality;
     int need; /* ceil(min_dist^2): the spacing test on whole-pixel places */
     int max;
+    int gs, gw, gh; /* the grid of corners taken: cells gs pixels square (gs^2 >= need), gw x gh of them */
 };
 
 struct vtg_detector {
@@ -59,15 +69,16 @@ struct vtg_detector {
     int max_w, max_h, max_cols, max_cells;
     float *resp, *cell, *near, *best;
     int *rowcount, *rowbase, *ncand;
-    unsigned long long *keys;
-    int *cx, *cy;
+    unsigned *keys;
+    int2 *cxy;
     float *xs, *ys;
     int *count;
 };
 
 /* ---- the response and the cells ---- */
 
-__global__ void __launch_bounds__(256) det_response(DetPrm q, float *__restrict__ resp, float *__restrict__ cell)
+__global__ void __launch_bounds__(256) det_response(DetPrm q, float *__restrict__ resp, float *__restrict__ cell,
+                                                    float *__restrict__ best)
 {
     __shared__ float s_p[DET_TY + 6][DET_TX + 6];   /* image rows y0 - 3 + r0 + i, columns ax + c0 - 3 + j */
     __shared__ float s_t[3][DET_TY + 4][DET_TX + 4]; /* tensor rows r0 + i, region columns c0 - 2 + j */
@@ -76,6 +87,8 @@ __global__ void __launch_bounds__(256) det_response(DetPrm q, float *__restrict_
     const DetGeo &g = q.g;
     const int tid = threadIdx.x;
     const int r0 = blockIdx.y * DET_TY, c0 = blockIdx.x * DET_TX;
+    if (tid == 0 && blockIdx.x == 0 && blockIdx.y == 0)
+        *best = 0.0f; /* det_near's maximum starts here */
     for (int i = tid; i < (DET_TY + 6) * (DET_TX + 6); i += blockDim.x) {
         const int a = i / (DET_TX + 6), b = i - a * (DET_TX + 6);
         const int y = min(max(g.y0 - 3 + r0 + a, 0), q.h - 1), x = min(max(g.ax + c0 - 3 + b, 0), q.w - 1);
@@ -148,33 +161,33 @@ __global__ void __launch_bounds__(256) det_response(DetPrm q, float *__restrict_
 
 /* ---- the selection ---- */
 
-__global__ void __launch_bounds__(1024) det_near(DetGeo g, const float *__restrict__ cell, float *__restrict__ near,
-                                                 float *__restrict__ best)
+/* Each cell's 3 x 3 neighbourhood strongest, a thread a cell, and the best cell over the CTAs: an integer atomicMax
+ * on the F32 bits orders them as the floats, all being >= 0 (det_response zeroes the best first). */
+__global__ void __launch_bounds__(256) det_near(DetGeo g, const float *__restrict__ cell, float *__restrict__ near,
+                                                float *__restrict__ best)
 {
-    __shared__ float s_w[32];
-    const int n = g.nv * g.cell_rows, tid = threadIdx.x;
+    __shared__ float s_w[8];
+    const int n = g.nv * g.cell_rows, i = (int)(blockIdx.x * blockDim.x + threadIdx.x), tid = threadIdx.x;
     float m = 0.0f;
-    for (int i = tid; i < n; i += blockDim.x)
-        m = fmaxf(m, cell[i]);
+    if (i < n) {
+        const int cr = i / g.nv, k = i - cr * g.nv;
+        for (int a = cr > 0 ? cr - 1 : 0; a <= cr + 1 && a < g.cell_rows; a++)
+            for (int b = k > 0 ? k - 1 : 0; b <= k + 1 && b < g.nv; b++)
+                m = fmaxf(m, cell[a * g.nv + b]);
+        near[i] = m;
+    }
 #pragma unroll
     for (int s = 16; s >= 1; s >>= 1)
         m = fmaxf(m, __shfl_xor_sync(VTG_FULL, m, s));
     if ((tid & 31) == 0)
         s_w[tid >> 5] = m;
-    for (int i = tid; i < n; i += blockDim.x) {
-        const int cr = i / g.nv, k = i - cr * g.nv;
-        float mx = 0.0f;
-        for (int a = cr > 0 ? cr - 1 : 0; a <= cr + 1 && a < g.cell_rows; a++)
-            for (int b = k > 0 ? k - 1 : 0; b <= k + 1 && b < g.nv; b++)
-                mx = fmaxf(mx, cell[a * g.nv + b]);
-        near[i] = mx;
-    }
     __syncthreads();
     if (tid == 0) {
         float b = 0.0f;
         for (int w = 0; w < (int)(blockDim.x >> 5); w++)
             b = fmaxf(b, s_w[w]);
-        *best = b;
+        if (b > 0.0f)
+            atomicMax(reinterpret_cast<int *>(best), __float_as_int(b));
     }
 }
 
@@ -260,8 +273,8 @@ __global__ void __launch_bounds__(1024) det_scan(int rows, const int *__restrict
 
 __global__ void __launch_bounds__(256) det_collect(DetPrm q, const float *__restrict__ resp,
                                                    const float *__restrict__ near, const float *__restrict__ best,
-                                                   const int *__restrict__ rowbase, unsigned long long *__restrict__ keys,
-                                                   int *__restrict__ cx, int *__restrict__ cy)
+                                                   const int *__restrict__ rowbase, unsigned *__restrict__ keys,
+                                                   int2 *__restrict__ cxy)
 {
     const int w = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
     const int r = w / DET_SEGS, sg = w - r * DET_SEGS;
@@ -282,96 +295,249 @@ __global__ void __launch_bounds__(256) det_collect(DetPrm q, const float *__rest
             const double v = (double)resp[(size_t)r * q.g.cols + c];
             const double local = (double)near[(r >> 4) * q.g.nv + (c >> 4)];
             const float score = (float)(v / local + 0.001 * v / bst);
-            keys[p] = ((unsigned long long)(~__float_as_uint(score)) << 32) | (unsigned)p;
-            cx[p] = q.g.ax + c;
-            cy[p] = q.g.y0 + r;
+            keys[p] = ~__float_as_uint(score); /* ascending: the best first; the place is the index */
+            cxy[p] = make_int2(q.g.ax + c, q.g.y0 + r);
         }
         pos += __popc(m);
     }
 }
 
-__global__ void __launch_bounds__(DET_SELECT_THREADS) det_select(DetPrm q, const int *__restrict__ ncand,
+/* Whether the corner at (x, y) keeps the spacing from every corner in the grid: the 3 x 3 grid cells around its own
+ * (a cell's side is at least the spacing, so no corner farther out can be too close). */
+__device__ __forceinline__ bool det_far(const DetPrm &q, const int *s_head, const int *s_next, const int *s_tx,
+                                        const int *s_ty, int x, int y)
+{
+    const int gx = (x - q.g.ax) / q.gs, gy = (y - q.g.y0) / q.gs;
+    int h[9];
+#pragma unroll
+    for (int j = 0; j < 9; j++) {
+        const int a = gx + j % 3 - 1, b = gy + j / 3 - 1;
+        h[j] = a >= 0 && a < q.gw && b >= 0 && b < q.gh ? s_head[b * q.gw + a] : -1;
+    }
+#pragma unroll
+    for (int j = 0; j < 9; j++)
+        for (int t = h[j]; t >= 0; t = s_next[t]) {
+            const int dx = s_tx[t] - x, dy = s_ty[t] - y;
+            if (dx * dx + dy * dy < q.need)
+                return false;
+        }
+    return true;
+}
+
+#define DET_OPEN 0
+#define DET_TAKEN 1
+#define DET_OUT 2
+
+/* A block candidate's earlier neighbours within the spacing (the block grid's 3 x 3 cells around it): DET_OUT when
+ * one of them is taken, DET_OPEN when none is but one is still open, else DET_TAKEN. The states are read while other
+ * threads set theirs: a state once set never changes, so a stale read only defers the answer to the next pass. */
+__device__ __forceinline__ int det_earlier(const DetPrm &q, const int *s_bhead, const int *s_bnext, const int2 *xy,
+                                           const unsigned char *s_st, int me, int x, int y)
+{
+    const volatile unsigned char *st = s_st;
+    const int gx = (x - q.g.ax) / q.gs, gy = (y - q.g.y0) / q.gs;
+    bool pending = false;
+    for (int j = 0; j < 9; j++) {
+        const int a = gx + j % 3 - 1, b = gy + j / 3 - 1;
+        if (a < 0 || a >= q.gw || b < 0 || b >= q.gh)
+            continue;
+        for (int u = s_bhead[b * q.gw + a]; u >= 0; u = s_bnext[u]) {
+            if (u >= me)
+                continue;
+            const int dx = xy[u].x - x, dy = xy[u].y - y;
+            if (dx * dx + dy * dy >= q.need)
+                continue;
+            const int su = st[u];
+            if (su == DET_TAKEN)
+                return DET_OUT;
+            pending = pending || su == DET_OPEN;
+        }
+    }
+    return pending ? DET_OPEN : DET_TAKEN;
+}
+
+/* One pass of the stable LSD radix sort over the candidates' score keys in shared memory: the 8-bit digit at shift,
+ * from (ka, va) to (kb, vb). Warp w holds elements 256 w + 32 k + lane (k = 0..7), ranked in that order within the
+ * warp (the lanes with the same digit found by eight ballots); the per-(digit, warp) counts, scanned in digit-major
+ * order, place them. The counts sit at warp * DET_HIST_PITCH + digit: a warp's lanes and a scan step's lanes fall in
+ * different banks. Two count buffers alternate: this pass counts in hist (zeroed by the pass before) and zeroes
+ * next. Warps past the candidates (256 w >= n) count nothing. */
+__device__ __forceinline__ void det_radix_pass(const unsigned *ka, const unsigned *va, unsigned *kb, unsigned *vb,
+                                               int *hist, int *next, int *s_wsum, int n, int shift, bool first)
+{
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int i = tid; i < DET_HIST_PITCH * 32; i += blockDim.x)
+        next[i] = 0;
+    const bool active = 256 * warp < n;
+    unsigned key[8], val[8];
+    int rank[8];
+    if (active) {
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            const int i = 256 * warp + 32 * k + lane;
+            key[k] = ka[i];
+            val[k] = first ? (unsigned)i : va[i];
+            const unsigned dig = (key[k] >> shift) & (DET_RADIX - 1);
+            unsigned peers = VTG_FULL;
+#pragma unroll
+            for (int b = 0; b < 8; b++) {
+                const unsigned m = __ballot_sync(VTG_FULL, (dig >> b) & 1u);
+                peers &= ((dig >> b) & 1u) ? m : ~m;
+            }
+            const int lt = __popc(peers & ((1u << lane) - 1u));
+            int *h = hist + warp * DET_HIST_PITCH + dig;
+            const int base = *h;
+            rank[k] = base + lt;
+            __syncwarp();
+            if (lt == 0)
+                *h = base + __popc(peers);
+            __syncwarp();
+        }
+    }
+    __syncthreads();
+    /* exclusive scan of the 8,192 counts: 8 a thread, across a warp, then across the warps (each warp scans the 32
+     * warp totals itself) */
+    int c[8], sum = 0;
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+        const int e = 8 * tid + j; /* digit e / 32, warp e % 32 */
+        c[j] = hist[(e & 31) * DET_HIST_PITCH + (e >> 5)];
+        sum += c[j];
+    }
+    int inc = sum;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int v = __shfl_up_sync(VTG_FULL, inc, d);
+        if (lane >= d)
+            inc += v;
+    }
+    if (lane == 31)
+        s_wsum[warp] = inc;
+    __syncthreads();
+    const int t = s_wsum[lane];
+    int ti = t;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int v = __shfl_up_sync(VTG_FULL, ti, d);
+        if (lane >= d)
+            ti += v;
+    }
+    int run = __shfl_sync(VTG_FULL, ti - t, warp) + inc - sum;
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+        const int e = 8 * tid + j;
+        hist[(e & 31) * DET_HIST_PITCH + (e >> 5)] = run;
+        run += c[j];
+    }
+    __syncthreads();
+    if (active) {
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            const unsigned dig = (key[k] >> shift) & (DET_RADIX - 1);
+            const int dst = hist[warp * DET_HIST_PITCH + dig] + rank[k];
+            kb[dst] = key[k];
+            vb[dst] = val[k];
+        }
+    }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(DET_SELECT_THREADS, 1) det_select(DetPrm q, const int *__restrict__ ncand,
                                                                  const float *__restrict__ best,
-                                                                 const unsigned long long *__restrict__ keys,
-                                                                 const int *__restrict__ cx, const int *__restrict__ cy,
+                                                                 const unsigned *__restrict__ keys,
+                                                                 const int2 *__restrict__ cxy,
                                                                  float *__restrict__ xs, float *__restrict__ ys,
                                                                  int *__restrict__ count)
 {
-    extern __shared__ unsigned long long s_key[]; /* DET_MAX_CAND keys, then their places as (x, y) pairs */
-    __shared__ int s_tx[512], s_ty[512], s_far[32], s_taken;
-    int2 *s_xy = reinterpret_cast<int2 *>(s_key + DET_MAX_CAND);
+    /* two buffers of keys and places (DET_MAX_CAND each), then two of radix counts. Once sorted (places in v0),
+     * k1 and v1 hold the taken corners' grid heads, the counts the block grid's, and k0 a block's (x, y). */
+    extern __shared__ unsigned s_buf[];
+    __shared__ int s_tx[512], s_ty[512], s_next[512], s_wsum[32];
+    __shared__ int s_bnext[DET_SELECT_THREADS];
+    __shared__ unsigned char s_st[DET_SELECT_THREADS];
+    unsigned *k0 = s_buf, *v0 = s_buf + DET_MAX_CAND, *k1 = s_buf + 2 * DET_MAX_CAND, *v1 = s_buf + 3 * DET_MAX_CAND;
+    int *h0 = reinterpret_cast<int *>(s_buf + 4 * DET_MAX_CAND), *h1 = h0 + DET_HIST_PITCH * 32;
+    int2 *s_xy = reinterpret_cast<int2 *>(k0);
+    int *s_head = reinterpret_cast<int *>(k1);
+    int *s_bhead = h0;
     const int tid = threadIdx.x;
     const int n = *best > 0.0f ? *ncand : 0;
-    int P = 1;
-    while (P < n)
-        P <<= 1;
-    for (int i = tid; i < P; i += blockDim.x)
-        s_key[i] = i < n ? keys[i] : ~0ull;
+    const int n256 = (n + 255) & ~255;
+    for (int i = tid; i < n256; i += blockDim.x)
+        k0[i] = i < n ? keys[i] : ~0u; /* past the candidates: after every score, and stable behind them */
+    for (int i = tid; i < DET_HIST_PITCH * 32; i += blockDim.x)
+        h0[i] = 0;
     __syncthreads();
-    /* ascending: ~score bits first (the best first), then the place in scan order */
-    for (int size = 2; size <= P; size <<= 1)
-        for (int stride = size >> 1; stride > 0; stride >>= 1) {
-            for (int i = tid; i < P / 2; i += blockDim.x) {
-                const int lo = 2 * i - (i & (stride - 1)), hi = lo + stride;
-                const bool up = (lo & size) == 0;
-                const unsigned long long a = s_key[lo], b = s_key[hi];
-                if ((a > b) == up) {
-                    s_key[lo] = b;
-                    s_key[hi] = a;
-                }
-            }
-            __syncthreads();
-        }
-    for (int i = tid; i < n; i += blockDim.x) {
-        const int p = (int)(s_key[i] & 0xFFFFFFFFull);
-        s_xy[i] = make_int2(cx[p], cy[p]);
+    /* ascending ~score bits, ties in scan order: the order detect_finish's qsort gives (score descending, then order) */
+    det_radix_pass(k0, v0, k1, v1, h0, h1, s_wsum, n, 0, true);
+    det_radix_pass(k1, v1, k0, v0, h1, h0, s_wsum, n, 8, false);
+    det_radix_pass(k0, v0, k1, v1, h0, h1, s_wsum, n, 16, false);
+    det_radix_pass(k1, v1, k0, v0, h1, h0, s_wsum, n, 24, false);
+    for (int i = tid; i < q.gw * q.gh; i += blockDim.x) {
+        s_head[i] = -1;
+        s_bhead[i] = -1;
     }
-    if (tid == 0)
-        s_taken = 0;
     __syncthreads();
-    /* The greedy spacing, 32 candidates at a time and exactly the one-by-one order: warp w tests candidate base + w
-     * against every corner taken so far (a lane per 32 of them); then warp 0 settles the 32 in order, candidate k
-     * rejecting every later one of the 32 too close to it once it is taken. */
+    /* The greedy spacing in blocks of up to 1,024 candidates, a thread a candidate; the result is the one-by-one
+     * order's. A candidate too close to a corner taken in an earlier block is out. Within the block the candidates
+     * sit in a grid of their own, and each open one looks at its earlier neighbours within the spacing: out once one
+     * of them is taken, taken once all of them are out. Every pass settles at least the earliest open one, so a block ends
+     * within as many passes as it has candidates. The taken ones past max are dropped in order. */
     const int lane = tid & 31, warp = tid >> 5;
     int taken = 0;
-    for (int base = 0; base < n && taken < q.max; base += 32) {
-        const int i = base + warp;
-        bool far = i < n;
-        if (far) {
-            const int2 c = s_xy[i];
-            for (int t = lane; t < taken; t += 32) {
-                const int dx = s_tx[t] - c.x, dy = s_ty[t] - c.y;
-                far = far && dx * dx + dy * dy >= q.need;
-            }
+    for (int base = 0, B = 0; base < n && taken < q.max; base += B) {
+        /* twice the corners still wanted, 64 to 1,024: the greedy rarely looks further, and a shorter block settles
+         * in fewer passes */
+        B = min(n - base, min(DET_SELECT_THREADS, max(64, 2 * (q.max - taken))));
+        int2 me = make_int2(0, 0);
+        int cell = 0;
+        if (tid < B) {
+            me = cxy[v0[base + tid]]; /* the block's places, gathered as it starts */
+            s_xy[tid] = me;
+            cell = ((me.y - q.g.y0) / q.gs) * q.gw + (me.x - q.g.ax) / q.gs;
+            s_st[tid] = det_far(q, s_head, s_next, s_tx, s_ty, me.x, me.y) ? DET_OPEN : DET_OUT;
+            s_bnext[tid] = atomicExch(&s_bhead[cell], tid);
         }
-        far = __all_sync(VTG_FULL, far);
-        if (lane == 0)
-            s_far[warp] = far;
         __syncthreads();
-        if (warp == 0) {
-            bool ok = s_far[lane] != 0;
-            const int2 c = ok ? s_xy[base + lane] : make_int2(0, 0);
-            int cnt = taken;
-            for (int k = 0; k < 32 && cnt < q.max; k++) {
-                if (!__shfl_sync(VTG_FULL, (int)ok, k))
-                    continue;
-                const int kx = __shfl_sync(VTG_FULL, c.x, k), ky = __shfl_sync(VTG_FULL, c.y, k);
-                if (lane == k) {
-                    s_tx[cnt] = kx;
-                    s_ty[cnt] = ky;
-                    xs[cnt] = (float)kx;
-                    ys[cnt] = (float)ky;
-                } else if (lane > k) {
-                    const int dx = kx - c.x, dy = ky - c.y;
-                    ok = ok && dx * dx + dy * dy >= q.need;
+        bool open = tid < B && s_st[tid] == DET_OPEN;
+        while (__syncthreads_or(open)) {
+            if (open) {
+                const int r = det_earlier(q, s_bhead, s_bnext, s_xy, s_st, tid, me.x, me.y);
+                if (r != DET_OPEN) {
+                    s_st[tid] = (unsigned char)r;
+                    open = false;
                 }
-                cnt++;
             }
-            if (lane == 0)
-                s_taken = cnt;
         }
+        /* the taken ones in order: their places in the list of corners */
+        const bool yes = tid < B && s_st[tid] == DET_TAKEN;
+        const unsigned bal = __ballot_sync(VTG_FULL, yes);
+        if (lane == 0)
+            s_wsum[warp] = __popc(bal);
         __syncthreads();
-        taken = s_taken;
+        const int wt = s_wsum[lane];
+        int wi = wt;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const int v = __shfl_up_sync(VTG_FULL, wi, d);
+            if (lane >= d)
+                wi += v;
+        }
+        const int rank = __shfl_sync(VTG_FULL, wi - wt, warp) + __popc(bal & ((1u << lane) - 1u));
+        const int total = __shfl_sync(VTG_FULL, wi, 31);
+        if (yes && taken + rank < q.max) {
+            const int at = taken + rank;
+            s_tx[at] = me.x;
+            s_ty[at] = me.y;
+            xs[at] = (float)me.x;
+            ys[at] = (float)me.y;
+            s_next[at] = atomicExch(&s_head[cell], at);
+        }
+        taken = min(taken + total, q.max);
+        __syncthreads();
+        if (tid < B)
+            s_bhead[cell] = -1;
+        __syncthreads();
     }
     if (tid == 0)
         *count = taken;
@@ -413,7 +579,7 @@ static bool det_geometry(int w, int h, float rx, float ry, float rw, float rh, i
 static size_t up256(size_t n) { return (n + 255) & ~(size_t)255; }
 
 struct DetLayout {
-    size_t resp, cell, near, best, rowcount, rowbase, ncand, keys, cx, cy, xs, ys, count, bytes;
+    size_t resp, cell, near, best, rowcount, rowbase, ncand, keys, cxy, xs, ys, count, bytes;
 };
 
 static DetLayout det_layout(int max_w, int max_h, int &max_cols, int &max_cells)
@@ -437,11 +603,9 @@ static DetLayout det_layout(int max_w, int max_h, int &max_cols, int &max_cells)
     L.ncand = b;
     b += 256;
     L.keys = b;
-    b += up256(sizeof(unsigned long long) * DET_MAX_CAND);
-    L.cx = b;
-    b += up256(sizeof(int) * DET_MAX_CAND);
-    L.cy = b;
-    b += up256(sizeof(int) * DET_MAX_CAND);
+    b += up256(sizeof(unsigned) * DET_MAX_CAND);
+    L.cxy = b;
+    b += up256(sizeof(int2) * DET_MAX_CAND);
     L.xs = b;
     b += up256(sizeof(float) * 512);
     L.ys = b;
@@ -505,9 +669,8 @@ extern "C" int vtg_detector_create(vtg_ctx *ctx, int max_w, int max_h, vtg_detec
     d->rowcount = (int *)(d->mem + L.rowcount);
     d->rowbase = (int *)(d->mem + L.rowbase);
     d->ncand = (int *)(d->mem + L.ncand);
-    d->keys = (unsigned long long *)(d->mem + L.keys);
-    d->cx = (int *)(d->mem + L.cx);
-    d->cy = (int *)(d->mem + L.cy);
+    d->keys = (unsigned *)(d->mem + L.keys);
+    d->cxy = (int2 *)(d->mem + L.cxy);
     d->xs = (float *)(d->mem + L.xs);
     d->ys = (float *)(d->mem + L.ys);
     d->count = (int *)(d->mem + L.count);
@@ -548,11 +711,24 @@ extern "C" int vtg_detect(vtg_detector *d, const float *plane, int w, int h, int
     q.pitch = pitch;
     q.quality = quality;
     q.max = max;
-    const double min2 = (double)min_dist * (double)min_dist; /* exact: a product of two F32s */
-    q.need = (int)ceil(min2);
+    /* exact: a product of two F32s; past 2^30 no two places in a 16384 x 16384 region are that far apart */
+    const double min2 = (double)min_dist * (double)min_dist;
+    q.need = min2 < (double)(1 << 30) ? (int)ceil(min2) : 1 << 30;
     const bool any = det_geometry(w, h, rx, ry, rw, rh, margin, q.g);
     if (any && (q.g.rows > d->max_h || q.g.cols > d->max_cols || q.g.nv * q.g.cell_rows > d->max_cells))
         return VTG_EINVAL;
+    if (any) {
+        /* the smallest side whose square reaches need, grown until the region's grid fits DET_GRID_MAX cells */
+        long long gs = (long long)sqrt((double)q.need);
+        while (gs * gs < q.need)
+            gs++;
+        gs = gs < 1 ? 1 : gs;
+        while (((q.g.cols + gs - 1) / gs) * ((q.g.rows + gs - 1) / gs) > DET_GRID_MAX)
+            gs++;
+        q.gs = (int)gs;
+        q.gw = (int)((q.g.cols + gs - 1) / gs);
+        q.gh = (int)((q.g.rows + gs - 1) / gs);
+    }
     if (!any || max == 0) {
         if (where == VTG_HOST) {
             *count = 0;
@@ -564,17 +740,17 @@ extern "C" int vtg_detect(vtg_detector *d, const float *plane, int w, int h, int
     const DetGeo &g = q.g;
     CU(cudaMemsetAsync(d->cell, 0, sizeof(float) * (size_t)g.nv * g.cell_rows, st));
     det_response<<<dim3((g.cols + DET_TX - 1) / DET_TX, (g.rows + DET_TY - 1) / DET_TY), 256, 0, st>>>(q, d->resp,
-                                                                                                   d->cell);
-    det_near<<<1, 1024, 0, st>>>(g, d->cell, d->near, d->best);
+                                                                                                   d->cell, d->best);
+    det_near<<<(g.nv * g.cell_rows + 255) / 256, 256, 0, st>>>(g, d->cell, d->near, d->best);
     const int rblocks = (g.rows * DET_SEGS * 32 + 255) / 256;
     det_count<<<rblocks, 256, 0, st>>>(q, d->resp, d->near, d->best, d->rowcount);
     det_scan<<<1, 1024, 0, st>>>(g.rows * DET_SEGS, d->rowcount, d->rowbase, d->ncand);
-    det_collect<<<rblocks, 256, 0, st>>>(q, d->resp, d->near, d->best, d->rowbase, d->keys, d->cx, d->cy);
-    const int smem = (int)((sizeof(unsigned long long) + sizeof(int2)) * DET_MAX_CAND);
+    det_collect<<<rblocks, 256, 0, st>>>(q, d->resp, d->near, d->best, d->rowbase, d->keys, d->cxy);
+    const int smem = (int)(4 * sizeof(unsigned) * DET_MAX_CAND + 2 * sizeof(int) * DET_HIST_PITCH * 32);
     CU(cudaFuncSetAttribute(det_select, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     float *oxs = where == VTG_DEVICE ? xs : d->xs, *oys = where == VTG_DEVICE ? ys : d->ys;
     int *ocount = where == VTG_DEVICE ? count : d->count;
-    det_select<<<1, DET_SELECT_THREADS, smem, st>>>(q, d->ncand, d->best, d->keys, d->cx, d->cy, oxs, oys, ocount);
+    det_select<<<1, DET_SELECT_THREADS, smem, st>>>(q, d->ncand, d->best, d->keys, d->cxy, oxs, oys, ocount);
     CU(cudaGetLastError());
     if (where == VTG_HOST) {
         CU(cudaMemcpyAsync(count, d->count, sizeof(int), cudaMemcpyDeviceToHost, st));
