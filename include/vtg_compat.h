@@ -19,7 +19,7 @@
  *
  * A call that cannot run (no GPU, a CUDA error, an argument out of range such as a patch wider than VTG_MAX_PATCH_W)
  * leaves image outputs untouched, marks an LK result VTG_LK_OUT (no measurement is invented, as lk.h says), returns
- * -1 from tk_correlate_cuda, and records its status for vtg_compat_error. */
+ * -1 from tk_correlate_cuda and 0 corners from detect_run_cuda, and records its status for vtg_compat_error. */
 #ifndef VTG_COMPAT_H
 #define VTG_COMPAT_H
 
@@ -82,6 +82,14 @@ void still_vectors_cuda(const struct vtg_ref_plane *mean, const struct vtg_ref_p
 /* tk_correlate (src/kern/track.h:59, track.c:184-208): the NCC of a zero-mean 32 x 21 template `app` (sum of squares
  * `norm`) against the plane at corner (x, y); -1 outside the valid corners, 0 for a near-blank window. */
 long double tk_correlate_cuda(const struct vtg_ref_plane *pl, const float *app, long double norm, int x, int y);
+
+/* Corner detection as seed_at runs it (src/kern/track.c:988-992): detect_begin (src/kern/detect.h:27), the three
+ * stages detect_tensor / detect_response / detect_cells (detect.h:30-32) and detect_finish (detect.h:35) in one call.
+ * The same arguments as detect_begin without the job and its scratch, and detect_finish's outputs: up to max (at most
+ * 512) corners in x and y (host memory), best first, at least min_dist apart; returns how many, 0 when nothing of the
+ * rectangle lies inside the plane's margin. The plane may be in host or device memory. */
+int detect_run_cuda(const struct vtg_ref_plane *pl, float rx, float ry, float rw, float rh, int margin, int max,
+                    float min_dist, float quality, float *x, float *y);
 
 /* The status of this thread's last call above: VTG_OK or a VTG_E* code. */
 int vtg_compat_error(void);

@@ -3,7 +3,8 @@
  * Each call takes the reference's arguments (planes in its padded layout, host or device memory), moves what is in
  * host memory to device scratch, runs the same kernels as the native API (lk.cu's point and cell kernels, the
  * search's corner kernel) or a small kernel of its own for the image rows, and brings the outputs back before it
- * returns. One lock serialises the calls; the scratch and the stream belong to the device of the first call. */
+ * returns. One lock serialises the calls; the scratch and the stream belong to the device of the first call. Corner
+ * detection runs detect.cu's pipeline through a detector kept for the largest plane seen. */
 #include <math.h>
 
 #include <mutex>
@@ -26,6 +27,8 @@ struct Compat {
     vtg_ctx *ctx = nullptr;       /* for the correlation's search context */
     vtg_search *search = nullptr; /* sized sw x sh, 32 x 21 templates */
     int sw = 0, sh = 0;
+    vtg_detector *det = nullptr; /* sized dw x dh */
+    int dw = 0, dh = 0;
 };
 Compat g_c;
 
@@ -437,4 +440,45 @@ extern "C" long double tk_correlate_cuda(const struct vtg_ref_plane *pl, const f
         return VTG_OK;
     }();
     return t_status == VTG_OK ? (long double)v : -1.0L;
+}
+
+extern "C" int detect_run_cuda(const struct vtg_ref_plane *pl, float rx, float ry, float rw, float rh, int margin,
+                               int want, float min_dist, float quality, float *x, float *y)
+{
+    std::lock_guard<std::mutex> g(g_c.mu);
+    int found = 0;
+    t_status = [&]() -> int {
+        if (!plane_ok(pl) || want < 0 || want > 512 || (want > 0 && (!x || !y)))
+            return VTG_EINVAL;
+        int rc = ready();
+        if (rc != VTG_OK)
+            return rc;
+        if (!g_c.ctx && (rc = vtg_ctx_create(g_c.device, 0, &g_c.ctx)) != VTG_OK)
+            return rc;
+        if (!g_c.det || g_c.dw < pl->w || g_c.dh < pl->h) {
+            const int dw = max(pl->w, g_c.dw), dh = max(pl->h, g_c.dh);
+            if (g_c.det)
+                vtg_detector_destroy(g_c.det);
+            g_c.det = nullptr;
+            if ((rc = vtg_detector_create(g_c.ctx, dw, dh, &g_c.det)) != VTG_OK)
+                return rc;
+            g_c.dw = dw;
+            g_c.dh = dh;
+        }
+        const float *plane = pl->p;
+        int pitch = pl->stride;
+        if (!on_device(pl->p)) {
+            /* the whole plane: detect_begin's margins and the clamped reads are the plane's own */
+            pitch = (pl->w + 31) & ~31;
+            char *base = nullptr;
+            if ((rc = scratch(up256((size_t)pitch * (size_t)pl->h * sizeof(float)), &base)) != VTG_OK)
+                return rc;
+            TRY(cudaMemcpy2DAsync(base, (size_t)pitch * sizeof(float), pl->p, (size_t)pl->stride * sizeof(float),
+                                  (size_t)pl->w * sizeof(float), (size_t)pl->h, cudaMemcpyHostToDevice, g_c.stream));
+            plane = (const float *)base;
+        }
+        return vtg_detect(g_c.det, plane, pl->w, pl->h, pitch, rx, ry, rw, rh, margin, want, min_dist, quality, x, y,
+                          &found, VTG_HOST, g_c.stream);
+    }();
+    return t_status == VTG_OK ? found : 0;
 }

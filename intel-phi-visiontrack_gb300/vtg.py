@@ -484,6 +484,8 @@ def compat() -> C.CDLL:
         L.still_vectors_cuda.restype = None
         L.tk_correlate_cuda.argtypes = [P, vp, C.c_longdouble, i, i]
         L.tk_correlate_cuda.restype = C.c_longdouble
+        L.detect_run_cuda.argtypes = [P, f, f, f, f, i, i, f, f, vp, vp]
+        L.detect_run_cuda.restype = i
         L.vtg_compat_error.restype = C.c_int
         L._compat_sigs = True
     return L

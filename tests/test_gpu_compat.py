@@ -167,6 +167,42 @@ def test_compat_tk_correlate(vtg_lib, torch_cuda, golden):
         assert float(L.tk_correlate_cuda(p.ref, app.ctypes.data, float(norm), 640 - 33, 5)) == -1.0
 
 
+def test_compat_detect_run(vtg_lib, torch_cuda, golden):
+    """detect_run_cuda as seed_at calls the detection (detect_begin, the three stages, detect_finish), on padded planes in
+    host and device memory, against the reference's own detect.c outputs (tests/golden/detect.npz) and the oracle."""
+    L = vtg_lib.compat()
+    g = np.load(os.path.join(golden, "detect.npz"))
+    d0, _, _, _ = S.warp_pair(640, 480, (1.7, -0.8), 0.5, seed=1)
+    d0 = d0.copy()
+    d0[300:420, 40:200] = 128
+    plane = O.pyramid(d0, 1)[0]
+    xs = np.zeros(512, np.float32)
+    ys = np.zeros(512, np.float32)
+    for where in ("host", "device"):
+        p = Plane(vtg_lib, 640, 480, torch_cuda if where == "device" else None)
+        p.set(plane)
+        p0 = 0
+        for k, (which, rx, ry, rw, rh, margin, mx, md, q) in enumerate(g["cases"]):
+            m = int(g["counts"][k])
+            if int(which) == 0:
+                n = L.detect_run_cuda(p.ref, rx, ry, rw, rh, int(margin), int(mx), md, q, xs.ctypes.data,
+                                      ys.ctypes.data)
+                assert L.vtg_compat_error() == 0
+                assert n == m and np.array_equal(xs[:n], g["xs"][p0:p0 + m]), (where, k)
+                assert np.array_equal(ys[:n], g["ys"][p0:p0 + m]), (where, k)
+            p0 += m
+        # a seed_at box against the oracle, and a rectangle wholly inside the margin
+        n = L.detect_run_cuda(p.ref, 120.5, 90.25, 384.0, 307.0, 12, 128, 8.0, 0.05, xs.ctypes.data, ys.ctypes.data)
+        oxs, oys = O.detect(plane, 120.5, 90.25, 384, 307, 12, 128, 8.0, 0.05)
+        assert n == len(oxs) and np.array_equal(xs[:n], oxs) and np.array_equal(ys[:n], oys)
+        assert L.detect_run_cuda(p.ref, 630.0, 470.0, 50.0, 50.0, 12, 64, 4.0, 0.05, xs.ctypes.data,
+                                 ys.ctypes.data) == 0
+        assert L.vtg_compat_error() == 0
+    # more corners than detect_finish keeps: refused, nothing found
+    assert L.detect_run_cuda(p.ref, 0.0, 0.0, 640.0, 480.0, 12, 513, 4.0, 0.05, xs.ctypes.data, ys.ctypes.data) == 0
+    assert L.vtg_compat_error() == vtg_lib.EINVAL
+
+
 def test_compat_refusals(vtg_lib):
     """Arguments out of range: a status, the LK point marked lost, the image untouched; no kernel runs."""
     import ctypes as C
