@@ -562,6 +562,72 @@ def run_detect(args) -> dict:
     return out
 
 
+def run_still(args) -> dict:
+    """The still picture (still_vectors, still_decide, still_update, still_finish) a frame, on a 12-frame sequence at
+    level 1 of a 1080p camera (960 x 540, 4,080 cells) and at native 1080p (16,200 cells): CUDA-event time of a whole
+    frame and of the decision and update alone (the frame's cells fed from device memory), the oracle's CPU time a
+    frame beside it. The reference's card times these at 1,448 + 1,648 us (level 1) and 4,515 + 5,825 us (native):
+    vectors + "mean" (docs/measurements.md:446-448)."""
+    import torch
+
+    import vtg
+    import vtg_build
+
+    sys.path.insert(0, ORACLE)
+    import oracle as O
+
+    S = __import__("vtg_synth")
+    vtg_build.build()
+    ctx = vtg.Context(0)
+    out = {"metric": "still picture ms a frame (per-cell LK from the mean, decision, running mean)", "unit": "ms",
+           "higher_is_better": False, "results": []}
+    cores = os.cpu_count() or 1
+    for name, (w, h), ref_us in (("level 1 of 1080p", (960, 540), (1448, 1648)),
+                                 ("native 1080p", (1920, 1080), (4515, 5825))):
+        seq = S.still_sequence(w, h, 12, seed=4)
+        planes = [torch.from_numpy(O.pyramid(f, 1)[0]).cuda() for f in seq]
+        torch.cuda.synchronize()
+        st = vtg.Still(ctx, w, h, 8, 1.0, 4.0)
+        stream = torch.cuda.ExternalStream(st.stream())
+        for k in range(3):
+            st.frame(planes[k].data_ptr(), w)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(9)]
+        for k, (a, b) in enumerate(ev):
+            a.record(stream)
+            st.frame(planes[3 + k].data_ptr(), w)
+            b.record(stream)
+        torch.cuda.synchronize()
+        frame_ms = float(np.median([a.elapsed_time(b) for a, b in ev]))
+        cells, m, _ = st.read()
+        dcells = torch.from_numpy(cells.view(np.uint8).copy()).cuda()
+        torch.cuda.synchronize()
+        L = vtg.lib()
+        for a, b in ev:
+            a.record(stream)
+            vtg.check(L.vtg_still_frame(st.h, planes[11].data_ptr(), w, dcells.data_ptr(), vtg.DEVICE, None),
+                      "vtg_still_frame")
+            b.record(stream)
+        torch.cuda.synchronize()
+        mean_ms = float(np.median([a.elapsed_time(b) for a, b in ev]))
+        st.close()
+        # the oracle: two frames after the first, all host cores (FP64 vectors)
+        ref = O.Still(w, h, 8, 1.0, 4.0)
+        qs = [O.pyramid(f, 1)[0] for f in seq[:3]]
+        ref.frame(qs[0])
+        t0 = time.perf_counter()
+        for q in qs[1:]:
+            ref.frame(q, mode=O.F64, threads=cores)
+        cpu_ms = 1e3 * (time.perf_counter() - t0) / 2
+        ref.close()
+        out["results"].append({"plane": name, "w": w, "h": h, "cells": int(len(cells)), "frame_ms": frame_ms,
+                               "decide_update_ms": mean_ms, "vectors_ms": frame_ms - mean_ms,
+                               "moving": int(m["moving"]), "tracked": int(m["tracked"]),
+                               "cpu_oracle_ms": cpu_ms, "cpu_cores": cores,
+                               "reference_card_ms": {"vectors": ref_us[0] / 1e3, "mean": ref_us[1] / 1e3}})
+    ctx.close()
+    return out
+
+
 def run_profile(args) -> None:
     """Launches for an ncu capture, nothing timed: `batch` primes B 1080p streams (2 batched steps) and runs 2 more
     (capture lk_batch_kernel with -s 2); `ncc` runs one 1080p whole-picture search per precision (32 x 32 template)."""
@@ -586,6 +652,19 @@ def run_profile(args) -> None:
             batch.launch(k & 1)
         ctx.sync()
         print("profile batch: %d streams, %d cells a step" % (B, batch.cells(0)))
+    elif args.profile == "still":
+        sys.path.insert(0, ORACLE)
+        import oracle as O
+
+        seq = S.still_sequence(W, H, 4, seed=4)
+        planes = [torch.from_numpy(O.pyramid(f, 1)[0]).cuda() for f in seq]
+        torch.cuda.synchronize()
+        st = vtg.Still(ctx, W, H, 8, 1.0, 4.0)
+        for p_ in planes:
+            st.frame(p_.data_ptr(), W)
+        _, m, _ = st.read()
+        print("profile still: %d frames, %d moving" % (int(m["frames"]), int(m["moving"])))
+        st.close()
     elif args.profile == "detect":
         sys.path.insert(0, ORACLE)
         import oracle as O
@@ -624,7 +703,9 @@ def main():
     ap.add_argument("--ncc", action="store_true",
                     help="the whole-picture appearance search on a 1080p frame (32, 64, 96 templates), per precision")
     ap.add_argument("--detect", action="store_true", help="corner detection on a 1080p plane: a 384 x 307 box, the frame")
-    ap.add_argument("--profile", default=None, choices=["batch", "ncc", "detect"],
+    ap.add_argument("--still", action="store_true",
+                    help="the still picture a frame at 960 x 540 and 1920 x 1080 (vectors, decision, running mean)")
+    ap.add_argument("--profile", default=None, choices=["batch", "ncc", "detect", "still"],
                     help="a short run for an ncu capture: the batched step (prime, then 2 steps) or one NCC search")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -636,6 +717,9 @@ def main():
         return
     if args.detect:
         print(json.dumps(run_detect(args)))
+        return
+    if args.still:
+        print(json.dumps(run_still(args)))
         return
     line = run_reference(args) if args.impl == "reference" else run_ours(args)
     if line is not None:

@@ -261,6 +261,49 @@ int vtg_detect(vtg_detector *d, const float *plane, int w, int h, int pitch, flo
 int vtg_detect_maps(vtg_detector *d, float rx, float ry, float rw, float rh, int w, int h, int margin, int *geo,
                     float *resp, float *cells);
 
+/* ---- the still picture: one camera's mean over the frames each cell held still (src/kern/still.h:1-53,
+ *      src/kern/still.c) ---- */
+
+typedef struct vtg_still vtg_still;
+
+/* struct still_cfg (src/kern/still.h:21-27) without its thread count: the plane size (32 to 4096 a side), frames at
+ * most in a cell's mean (avg, 1 to 65,535: weight 1 / min(count, avg)), the good-vector length past which a cell
+ * moved (motion_px, pixels) and the mean |frame - mean| over a cell past which it changed (motion_grey, 8-bit grey). */
+struct vtg_still_config {
+    int w, h, avg;
+    float motion_px, motion_grey;
+};
+
+/* What still_motion fills (src/kern/still.c:262-275) of struct vt_motion (src/common/vt_proto.h:403-415), for the
+ * newest frame: 48 bytes. */
+struct vtg_still_motion {
+    uint32_t cols, rows, tracked, moving;
+    float count_mean, drift_u, drift_v, drift_rms, diff_median, diff_limit;
+    uint64_t frames;
+};
+
+/* still_bytes / still_create (still.h:31-32, still.c:55-99): the mean, the 16 x 8 cells, their counts, all zero. */
+size_t vtg_still_bytes(const struct vtg_still_config *c);
+int vtg_still_create(vtg_ctx *ctx, const struct vtg_still_config *c, vtg_still **out);
+void vtg_still_destroy(vtg_still *s);
+void *vtg_still_stream(const vtg_still *s);
+
+/* One frame, as the reference runs it (still.h:11): still_vectors unless it is the first frame (LK from the mean to
+ * the frame at every cell, 15 x 15, 6 iterations, forward-backward 0.25 px), still_decide, still_update, still_finish.
+ * cur: the frame's Q6 plane (w x h, rows `pitch` floats apart) in device memory, e.g. a tracker's resident level
+ * (vtg_level_device). cells_in (host or device memory as `where` says) replaces the vectors with the caller's own
+ * cells; NULL runs them. Asynchronous on `stream` (NULL: the still's own). */
+int vtg_still_frame(vtg_still *s, const float *cur, int pitch, const struct vtg_cell *cells_in, int where,
+                    void *stream);
+
+/* still_cells / still_motion / still_mean (still.h:45-51) of the newest frame: any of cells (cols x rows), motion and
+ * mean (w x h, rows mean_pitch floats apart) may be NULL. VTG_HOST waits for the copies; VTG_DEVICE does not. */
+int vtg_still_read(vtg_still *s, struct vtg_cell *cells, struct vtg_still_motion *motion, float *mean, int mean_pitch,
+                   int where, void *stream);
+
+/* The mean plane in device memory (still_mean, still.h:45), valid until the next frame. */
+int vtg_still_mean(const vtg_still *s, const float **plane, int *pitch);
+
 #ifdef __cplusplus
 }
 #endif

@@ -542,3 +542,67 @@ class Detector:
             self.close()
         except Exception:
             pass
+
+
+class StillConfig(C.Structure):
+    """struct vtg_still_config: still_cfg (src/kern/still.h:21-27) without its thread count."""
+    _fields_ = [("w", C.c_int), ("h", C.c_int), ("avg", C.c_int), ("motion_px", C.c_float),
+                ("motion_grey", C.c_float)]
+
+
+# struct vtg_still_motion: what still_motion fills (src/kern/still.c:262-275), 48 bytes.
+STILL_MOTION = np.dtype([("cols", "<u4"), ("rows", "<u4"), ("tracked", "<u4"), ("moving", "<u4"),
+                         ("count_mean", "<f4"), ("drift_u", "<f4"), ("drift_v", "<f4"), ("drift_rms", "<f4"),
+                         ("diff_median", "<f4"), ("diff_limit", "<f4"), ("frames", "<u8")])
+
+
+class Still:
+    """One camera's still picture (vtg_still): still_vectors, still_decide, still_update, still_finish a frame."""
+
+    def __init__(self, ctx: Context, w: int, h: int, avg: int = 8, motion_px: float = 1.0, motion_grey: float = 4.0):
+        L = lib()
+        vp, i = C.c_void_p, C.c_int
+        L.vtg_still_bytes.argtypes = [C.POINTER(StillConfig)]
+        L.vtg_still_bytes.restype = C.c_size_t
+        L.vtg_still_create.argtypes = [vp, C.POINTER(StillConfig), C.POINTER(vp)]
+        L.vtg_still_destroy.argtypes = [vp]
+        L.vtg_still_destroy.restype = None
+        L.vtg_still_stream.argtypes = [vp]
+        L.vtg_still_stream.restype = vp
+        L.vtg_still_frame.argtypes = [vp, vp, i, vp, i, vp]
+        L.vtg_still_read.argtypes = [vp, vp, vp, vp, i, i, vp]
+        L.vtg_still_mean.argtypes = [vp, C.POINTER(vp), C.POINTER(i)]
+        self.ctx, self.w, self.h_ = ctx, w, h
+        self.cols, self.rows = (w + 15) // 16, (h + 7) // 8
+        self.cfg = StillConfig(w, h, avg, motion_px, motion_grey)
+        self.h = C.c_void_p()
+        check(L.vtg_still_create(ctx.h, C.byref(self.cfg), C.byref(self.h)), "vtg_still_create")
+        ctx._trackers.add(self)
+
+    def frame(self, cur_ptr: int, pitch: int, cells=None, stream=None):
+        """One frame on a device Q6 plane; cells (a host CELL array) replaces the GPU's own vectors."""
+        c = None if cells is None else np.ascontiguousarray(cells, CELL_DTYPE)
+        check(lib().vtg_still_frame(self.h, cur_ptr, pitch, None if c is None else _p(c), HOST, stream),
+              "vtg_still_frame")
+
+    def read(self):
+        """(cells, motion record, mean plane) of the newest frame."""
+        cells = np.zeros(self.cols * self.rows, CELL_DTYPE)
+        m = np.zeros(1, STILL_MOTION)
+        mean = np.zeros((self.h_, self.w), np.float32)
+        check(lib().vtg_still_read(self.h, _p(cells), _p(m), _p(mean), self.w, HOST, None), "vtg_still_read")
+        return cells, m[0], mean
+
+    def stream(self):
+        return lib().vtg_still_stream(self.h)
+
+    def close(self):
+        if self.h:
+            lib().vtg_still_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

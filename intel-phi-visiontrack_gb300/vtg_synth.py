@@ -126,6 +126,27 @@ def warp_pair(w: int, h: int, shift=(1.7, -0.8), amp: float = 0.5, seed: int = 1
     return to_u8(base), to_u8(moved), dx, dy
 
 
+def still_sequence(w: int, h: int, frames: int, seed: int, jump_at: int | None = None, mover: int = 24):
+    """A still camera's frames over a room: the blurred-noise scene drifting 0.03 px right and 0.02 px down a frame
+    (the camera against its own past), sensor noise uniform in [-3, 3) grey each frame, a textured square of `mover`
+    px entering at frame 2 and moving 3 px right a frame, and from frame `jump_at` on the whole picture 40 grey
+    brighter (a light turned on: everything changed)."""
+    base = blurred_noise(w, h, seed)
+    tex = blurred_noise(mover, mover, seed + 7) * 0.5 + 100.0
+    ys, xs = np.mgrid[0:h, 0:w].astype(np.float64)
+    out = []
+    for i in range(frames):
+        img = bilinear(base, xs - 0.03 * i, ys - 0.02 * i)
+        if i >= 2:
+            x0, y0 = min(w // 5 + 3 * (i - 2), w - mover), h // 3
+            img[y0:y0 + mover, x0:x0 + mover] = tex
+        img = img + (uniform(seed, 300 + i, w * h) * 6.0 - 3.0).reshape(h, w)
+        if jump_at is not None and i >= jump_at:
+            img = img + 40.0
+        out.append(to_u8(img))
+    return out
+
+
 def seeded_shift(seed: int, stream: int, reach: float = 12.0):
     u = uniform(seed, 100 + stream, 2)
     return (float(-reach + 2 * reach * u[0]), float(-reach + 2 * reach * u[1]))

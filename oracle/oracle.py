@@ -24,6 +24,10 @@ MAX_LEVELS = 8
 LK_OUT = np.dtype([("x", "<f4"), ("y", "<f4"), ("min_eig", "<f4"), ("residual", "<f4"), ("cov_xx", "<f4"),
                    ("cov_xy", "<f4"), ("cov_yy", "<f4"), ("iters", "<u2"), ("status", "<u2")])
 CELL = np.dtype([("u", "<f4"), ("v", "<f4"), ("diff", "<f4"), ("state", "<u4"), ("sigma", "<f4"), ("pad", "<f4")])
+# What still_motion fills (src/kern/still.c:262-275), as the library's struct vtg_still_motion: 48 bytes.
+STILL_MOTION = np.dtype([("cols", "<u4"), ("rows", "<u4"), ("tracked", "<u4"), ("moving", "<u4"),
+                         ("count_mean", "<f4"), ("drift_u", "<f4"), ("drift_v", "<f4"), ("drift_rms", "<f4"),
+                         ("diff_median", "<f4"), ("diff_limit", "<f4"), ("frames", "<u8")])
 assert LK_OUT.itemsize == 32 and CELL.itemsize == 24
 
 
@@ -94,6 +98,14 @@ def lib() -> C.CDLL:
         _lib.or_detect_maps.argtypes = [C.POINTER(Img), C.POINTER(DetGeo), C.c_void_p, C.c_void_p]
         _lib.or_detect_finish.argtypes = [C.POINTER(DetGeo), C.c_void_p, C.c_void_p, C.c_int, C.c_float, C.c_float,
                                           C.c_void_p, C.c_void_p]
+        _lib.or_still_create.restype = C.c_void_p
+        _lib.or_still_create.argtypes = [C.c_int, C.c_int, C.c_int, C.c_float, C.c_float]
+        _lib.or_still_destroy.argtypes = [C.c_void_p]
+        _lib.or_still_first.argtypes = [C.c_void_p]
+        _lib.or_still_decide.argtypes = [C.c_void_p, C.c_void_p]
+        _lib.or_still_update.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int]
+        _lib.or_still_finish.argtypes = [C.c_void_p]
+        _lib.or_still_motion.argtypes = [C.c_void_p, C.c_void_p]
     return _lib
 
 
@@ -194,6 +206,9 @@ def ref() -> C.CDLL:
         _ref.ref_pyramid.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p]
         _ref.ref_still_vectors.restype = C.c_int
         _ref.ref_still_vectors.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p]
+        _ref.ref_still_run.restype = C.c_int
+        _ref.ref_still_run.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float,
+                                       C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
     return _ref
 
 
@@ -441,3 +456,76 @@ def ref_search_half(plane, app, norm, hxs, hys) -> np.ndarray:
     ref().ref_search_half(_p(plane), plane.shape[1], plane.shape[0], _p(app), C.c_float(norm), len(hxs), _p(hxs),
                           _p(hys), _p(out))
     return out
+
+
+# ---------------------------------------------------------------- the still picture (src/kern/still.c)
+
+def still_cfg() -> LkCfg:
+    """still.c's LK: a 15 x 15 patch, 6 iterations, eps 0.01, min_eig 0.1, residual 16 (src/kern/still.c:14-19)."""
+    return lk_cfg(15, 15, 6, 0.01, 0.1, 16.0)
+
+
+STILL_FB = 0.25  # FB_MAX, src/kern/still.c:19
+
+
+class Still:
+    """One camera's still picture, as the reference runs a frame: still_vectors unless it is the first frame (the
+    per-cell grid from the mean to the frame, one level, OR_LANE by default), still_decide, still_update, still_finish.
+    ``frame(cur, cells=...)`` takes the frame's vectors from the caller instead (their LK byte of state is what the
+    decision reads)."""
+
+    def __init__(self, w, h, avg=8, motion_px=1.0, motion_grey=4.0):
+        self.w, self.h = w, h
+        self.cols, self.rows = (w + 15) // 16, (h + 7) // 8
+        self.s = lib().or_still_create(w, h, avg, C.c_float(motion_px), C.c_float(motion_grey))
+        self.mean = np.zeros((h, w), np.float32)
+        self.cells = np.zeros(self.cols * self.rows, CELL)
+
+    def frame(self, cur, cells=None, mode=LANE, threads=1):
+        """One frame on the Q6 plane cur (h x w): the cells after the decision and the motion record."""
+        cur = np.ascontiguousarray(cur, np.float32)
+        if cells is not None:
+            self.cells = np.ascontiguousarray(cells, CELL).copy()
+        elif not lib().or_still_first(self.s):
+            _, self.cells = globals()["cells"]([self.mean], [cur], 0, still_cfg(), 16, 8, max_fb=STILL_FB, mode=mode,
+                                               threads=threads)
+        lib().or_still_decide(self.s, _p(self.cells))
+        lib().or_still_update(self.s, _p(self.mean), self.w, _p(cur), self.w)
+        lib().or_still_finish(self.s)
+        m = np.zeros(1, STILL_MOTION)
+        lib().or_still_motion(self.s, _p(m))
+        return self.cells.copy(), m[0]
+
+    def close(self):
+        if self.s:
+            lib().or_still_destroy(self.s)
+            self.s = None
+
+    def __del__(self):
+        self.close()
+
+
+def still_hash(cells: np.ndarray, mean: np.ndarray, h: int = 0xcbf29ce484222325) -> int:
+    """still_hash (src/kern/still.c:253-259): the cells' bytes, then the mean's rows."""
+    h = fnv(np.ascontiguousarray(cells, CELL), h)
+    return fnv(np.ascontiguousarray(mean, np.float32), h)
+
+
+def ref_still_run(frames, avg=8, motion_px=1.0, motion_grey=4.0):
+    """The reference's still picture over 8-bit frames (src/host/m3_ref.c:272-283): per frame (cells, motion, hash),
+    and the mean after the last frame."""
+    f0 = np.ascontiguousarray(frames[0])
+    h, w = f0.shape
+    stride = (w + 15) & ~15
+    buf = np.zeros((len(frames), h, stride), np.uint8)
+    for k, f in enumerate(frames):
+        buf[k, :, :w] = f
+    n = ((w + 15) // 16) * ((h + 7) // 8)
+    cells = np.zeros((len(frames), n), CELL)
+    motion = np.zeros(len(frames), STILL_MOTION)
+    hashes = np.zeros(len(frames), np.uint64)
+    mean = np.zeros((h, w), np.float32)
+    got = ref().ref_still_run(_p(buf), len(frames), stride, w, h, avg, C.c_float(motion_px), C.c_float(motion_grey),
+                              _p(cells), _p(motion), _p(hashes), _p(mean))
+    assert got == n
+    return cells, motion, hashes, mean

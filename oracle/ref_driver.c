@@ -213,3 +213,46 @@ int ref_detect(const float *interior, int w, int h, float rx, float ry, float rw
     free_plane(&pl);
     return n;
 }
+
+/* What still_motion fills (src/kern/still.c:262-275), in the layout of the library's struct vtg_still_motion. */
+struct ref_still_motion {
+    uint32_t cols, rows, tracked, moving;
+    float count_mean, drift_u, drift_v, drift_rms, diff_median, diff_limit;
+    uint64_t frames;
+};
+
+/* The reference's still picture over a sequence of 8-bit frames, in the order m3_ref runs it (src/host/m3_ref.c:
+ * 272-283): each frame's Q6 plane, still_vectors unless it is the first frame, still_decide, still_update,
+ * still_finish. Per frame: the cells after the decision, still_motion, and still_hash from the FNV basis
+ * 0xcbf29ce484222325; after the last frame, the mean's w x h interior. Returns the cells a frame. */
+int ref_still_run(const uint8_t *frames, int nframes, int stride, int w, int h, int avg, float motion_px,
+                  float motion_grey, struct vt_cell *cells, struct ref_still_motion *motion, uint64_t *hash,
+                  float *mean_out)
+{
+    const struct still_cfg sc = {.w = w, .h = h, .avg = avg, .motion_px = motion_px, .motion_grey = motion_grey, .threads = 1};
+    struct still *s = still_create(&sc, host_alloc, NULL);
+    if (!s)
+        return -1;
+    const int n = ((w + VT_CELL_W - 1) / VT_CELL_W) * ((h + VT_CELL_H - 1) / VT_CELL_H);
+    for (int f = 0; f < nframes; f++) {
+        struct ref_pyr P;
+        build(&P, frames + (size_t)f * (size_t)stride * (size_t)h, stride, w, h, 1, 0);
+        if (!still_first(s))
+            still_vectors(s, &P.l[0], 0, 1);
+        still_decide(s);
+        still_update(s, &P.l[0], 0, 1);
+        still_finish(s);
+        memcpy(cells + (size_t)f * (size_t)n, still_cells(s), sizeof(struct vt_cell) * (size_t)n);
+        struct vt_motion m;
+        memset(&m, 0, sizeof m);
+        still_motion(s, &m);
+        motion[f] = (struct ref_still_motion){m.cols, m.rows, m.tracked, m.moving, m.count_mean, m.drift_u, m.drift_v,
+                                              m.drift_rms, m.diff_median, m.diff_limit, m.frames};
+        hash[f] = still_hash(s, 0xcbf29ce484222325ull);
+        release(&P);
+    }
+    const struct vt_plane *mp = still_mean(s);
+    for (int y = 0; y < h; y++)
+        memcpy(mean_out + (size_t)y * (size_t)w, plane_row(mp, y), sizeof(float) * (size_t)w);
+    return n;
+}

@@ -13,7 +13,9 @@
  *     a T_w x T_h template (T_w a multiple of 16);
  *   - corner detection: the Harris response over Sobel gradients on a 5 x 5 box and the cells' strongest responses
  *     in the reference's F32 operation order (src/kern/detect.c:68-141), exact in any IEEE arithmetic, and the
- *     selection of detect_finish (detect.c:175-258), long double as the reference.
+ *     selection of detect_finish (detect.c:175-258), long double as the reference;
+ *   - the still picture's decision and update (src/kern/still.c:143-246): the noise median, each cell's evidence, the
+ *     3 x 3 vote, the counts and weights, the drift statistics, and the running mean; long double as the reference.
  *
  * Two arithmetics for everything that is floating point:
  *   OR_LANE  the reference's replay arithmetic: F32 patch sums in 16 lanes, each lane a chain of fused multiply-adds in
@@ -1081,4 +1083,163 @@ int or_detect_finish(const struct or_det_geo *g, const float *resp, const float 
     free(cand);
     free(near);
     return taken;
+}
+
+/* ---------------------------------------------------------------- the still picture (src/kern/still.c:143-242) */
+
+/* One camera's still-picture state (struct still, src/kern/still.c:36-52, the fields the decision and the update use):
+ * the frames in each cell's mean, this frame's weights, the usual noise, and the newest frame's statistics. */
+struct or_still {
+    int w, h, cols, rows, n, avg;
+    float motion_px, motion_grey;
+    uint64_t frames;
+    long double noise_usual;
+    uint16_t *count;
+    float *weight;
+    uint8_t *raw; /* (cols + 2) x (rows + 2), a zero border */
+    uint32_t tracked, moving;
+    float count_mean, drift_u, drift_v, drift_rms, diff_median, diff_limit;
+};
+
+/* What still_motion fills (src/kern/still.c:262-275), in the layout of the library's struct vtg_still_motion. */
+struct or_still_motion {
+    uint32_t cols, rows, tracked, moving;
+    float count_mean, drift_u, drift_v, drift_rms, diff_median, diff_limit;
+    uint64_t frames;
+};
+
+struct or_still *or_still_create(int w, int h, int avg, float motion_px, float motion_grey)
+{
+    struct or_still *s = calloc(1, sizeof *s);
+    if (!s)
+        return NULL;
+    s->w = w;
+    s->h = h;
+    s->cols = (w + 15) / 16; /* VT_CELL_W x VT_CELL_H */
+    s->rows = (h + 7) / 8;
+    s->n = s->cols * s->rows;
+    s->avg = avg;
+    s->motion_px = motion_px;
+    s->motion_grey = motion_grey;
+    s->count = calloc((size_t)s->n, sizeof *s->count);
+    s->weight = calloc((size_t)s->n, sizeof *s->weight);
+    s->raw = calloc((size_t)(s->cols + 2) * (size_t)(s->rows + 2), 1);
+    return s;
+}
+
+void or_still_destroy(struct or_still *s)
+{
+    if (!s)
+        return;
+    free(s->count);
+    free(s->weight);
+    free(s->raw);
+    free(s);
+}
+
+int or_still_first(const struct or_still *s) { return s->frames == 0; }
+
+/* still_decide (src/kern/still.c:143-222), long double as the reference: the median cell difference (a histogram of
+ * 1/16 grey bins) is this camera's noise; a cell's own evidence is a good vector longer than max(12 sigma, motion_px),
+ * a lost patch (LK_RESIDUAL) or a difference above max(3 noise, motion_grey); a cell moves when two cells of its 3 x 3
+ * have evidence, or when the median leapt past 3x its usual value (everything moved). A moving cell's mean restarts
+ * (count 1); a still one's count grows to avg. cells[].state gets the LK byte, CHANGED, MOVING and the count. */
+void or_still_decide(struct or_still *s, struct or_cell *cells)
+{
+    const int cols = s->cols, rows = s->rows, wide = cols + 2, n = s->n;
+    uint32_t hist[256] = {0};
+    for (int i = 0; i < n; i++) {
+        const long b = (long)((long double)cells[i].diff * 16.0L);
+        hist[b < 255 ? b : 255]++;
+    }
+    uint32_t below = 0;
+    int med = 0;
+    while (med < 255 && below + hist[med] < (uint32_t)n / 2u)
+        below += hist[med++];
+    const long double noise = (long double)med / 16.0L, three = noise * 3.0L;
+    const long double limit = three > (long double)s->motion_grey ? three : (long double)s->motion_grey;
+    s->diff_median = (float)noise;
+    s->diff_limit = (float)limit;
+    const long double usual3 = s->noise_usual * 3.0L;
+    const long double usual = usual3 > (long double)s->motion_grey ? usual3 : (long double)s->motion_grey;
+    const int everything = s->frames >= 2 && noise > usual;
+    if (!everything && s->frames >= 1)
+        s->noise_usual = s->frames == 1 ? noise : s->noise_usual + (noise - s->noise_usual) / 32.0L;
+    const long double px2 = (long double)s->motion_px * (long double)s->motion_px;
+    for (int i = 0; i < n; i++) {
+        const struct or_cell *c = &cells[i];
+        const uint32_t lk = c->state & 0xffu;
+        const long double u = c->u, v = c->v, sg = (long double)c->sigma * 12.0L;
+        const long double need = sg * sg > px2 ? sg * sg : px2;
+        const int moved = lk == 0 && u * u + v * v > need;
+        const int failed = (lk & OR_RESIDUAL) != 0;
+        const int changed = (long double)c->diff > limit;
+        s->raw[(size_t)(i / cols + 1) * (size_t)wide + (size_t)(i % cols + 1)] = (uint8_t)(moved || failed || changed);
+    }
+    uint32_t tracked = 0, moving = 0, good = 0;
+    long double su = 0.0L, sv = 0.0L, suu = 0.0L, counts = 0.0L;
+    for (int r = 0; r < rows; r++)
+        for (int c = 0; c < cols; c++) {
+            const int i = r * cols + c;
+            uint32_t votes = 0;
+            for (int dy = 0; dy < 3; dy++)
+                for (int dx = 0; dx < 3; dx++)
+                    votes += s->raw[(size_t)(r + dy) * (size_t)wide + (size_t)(c + dx)];
+            const int any = votes >= 2 || everything;
+            const int own = s->raw[(size_t)(r + 1) * (size_t)wide + (size_t)(c + 1)] != 0;
+            const uint32_t grown = (uint32_t)s->count[i] + 1u, cnt = any ? 1u : grown < (uint32_t)s->avg ? grown : (uint32_t)s->avg;
+            s->count[i] = (uint16_t)cnt;
+            s->weight[i] = (float)(1.0L / (long double)cnt);
+            struct or_cell *cl = &cells[i];
+            const uint32_t lk = cl->state & 0xffu;
+            cl->state = lk | (own ? 0x100u : 0u) | (any ? 0x200u : 0u) | (cnt << 16);
+            tracked += lk == 0;
+            moving += any != 0;
+            counts += (long double)cnt;
+            if (lk == 0 && !any) {
+                su += cl->u;
+                sv += cl->v;
+                suu += (long double)cl->u * cl->u + (long double)cl->v * cl->v;
+                good++;
+            }
+        }
+    s->tracked = tracked;
+    s->moving = moving;
+    s->count_mean = (float)(counts / (long double)n);
+    const long double mu = good ? su / (long double)good : 0.0L, mv = good ? sv / (long double)good : 0.0L;
+    s->drift_u = (float)mu;
+    s->drift_v = (float)mv;
+    const long double var = good ? suu / (long double)good - mu * mu - mv * mv : 0.0L;
+    s->drift_rms = var > 0.0L ? (float)sqrtl(var) : 0.0f;
+}
+
+/* still_update (src/kern/still.c:224-246): each pixel of the mean moves toward the frame by its cell's weight,
+ * m + w (f - m) as one fused multiply-add; a cell of weight 1 takes the frame exactly. Planes w x h, rows `pitch`
+ * floats apart. */
+void or_still_update(const struct or_still *s, float *mean, int mean_pitch, const float *cur, int cur_pitch)
+{
+    for (int y = 0; y < s->h; y++)
+        for (int x = 0; x < s->w; x++) {
+            const float wt = s->weight[(y / 8) * s->cols + x / 16];
+            const float f = cur[(size_t)y * cur_pitch + x];
+            float *m = &mean[(size_t)y * mean_pitch + x];
+            *m = wt == 1.0f ? f : fmaf(f - *m, wt, *m);
+        }
+}
+
+void or_still_finish(struct or_still *s) { s->frames++; }
+
+void or_still_motion(const struct or_still *s, struct or_still_motion *m)
+{
+    m->cols = (uint32_t)s->cols;
+    m->rows = (uint32_t)s->rows;
+    m->tracked = s->tracked;
+    m->moving = s->moving;
+    m->count_mean = s->count_mean;
+    m->drift_u = s->drift_u;
+    m->drift_v = s->drift_v;
+    m->drift_rms = s->drift_rms;
+    m->diff_median = s->diff_median;
+    m->diff_limit = s->diff_limit;
+    m->frames = s->frames;
 }

@@ -17,6 +17,8 @@ Writes:
   detect.npz        corner detection (detect_begin, the three stages, detect_finish) over seven regions of two Q6
                     planes: each region's layout, a hash of its response map, its cells' strongest responses and the
                     corners found.
+  still.npz         the still picture (still_vectors, still_decide, still_update, still_finish) over a 12-frame
+                    320 x 240 sequence: per frame the cells after the decision, still_motion and still_hash.
 Frames are not stored: the generator reproduces them bit for bit, and their hashes are stored to prove it.
 """
 from __future__ import annotations
@@ -141,7 +143,25 @@ def main(ref_root: str = "/root/reference") -> None:
                         cells=np.concatenate(cells).astype(np.float32), cell_n=np.array(cell_n, np.int32),
                         xs=np.concatenate(xs_all).astype(np.float32), ys=np.concatenate(ys_all).astype(np.float32),
                         counts=np.array(counts, np.int32))
+    write_still()
     print("golden fixtures written to", HERE)
+
+
+STILL_SEQ = dict(w=320, h=240, frames=12, seed=5, jump_at=9)
+STILL_CFG = dict(avg=8, motion_px=1.0, motion_grey=4.0)
+
+
+def write_still() -> None:
+    """still.npz: the reference's still picture (still_vectors, still_decide, still_update, still_finish) over a
+    12-frame 320 x 240 sequence: a drifting scene, sensor noise, a square moving in at frame 2, everything 40 grey
+    brighter from frame 9. Per frame the cells after the decision, still_motion and still_hash."""
+    frames = S.still_sequence(STILL_SEQ["w"], STILL_SEQ["h"], STILL_SEQ["frames"], STILL_SEQ["seed"],
+                              jump_at=STILL_SEQ["jump_at"])
+    cells, motion, hashes, mean = O.ref_still_run(frames, **STILL_CFG)
+    np.savez_compressed(os.path.join(HERE, "still.npz"), frames_fnv=np.array([O.fnv(f) for f in frames], np.uint64),
+                        seq=np.array([STILL_SEQ[k] for k in ("w", "h", "frames", "seed", "jump_at")], np.int64),
+                        cfg=np.array([STILL_CFG["avg"], STILL_CFG["motion_px"], STILL_CFG["motion_grey"]], np.float64),
+                        cells=cells, motion=motion, hashes=hashes, mean_fnv=np.uint64(O.fnv(mean)))
 
 
 if __name__ == "__main__":

@@ -280,3 +280,57 @@ def test_detect_against_reference_code():
         assert np.array_equal(resp, rresp) and np.array_equal(cell, rcell)
         xs, ys = O.detect(plane, rx, ry, rw, rh, margin, mx, md, q)
         assert np.array_equal(xs, rxs) and np.array_equal(ys, rys)
+
+
+def _still_frames(g):
+    w, h, n, seed, jump = (int(v) for v in g["seq"])
+    frames = S.still_sequence(w, h, n, seed, jump_at=jump)
+    assert [O.fnv(f) for f in frames] == [int(v) for v in g["frames_fnv"]]
+    return frames
+
+
+@x86_only
+def test_still_fixture(golden):
+    """The oracle's still picture (its per-cell grid in the lane model, then still_decide, still_update, still_finish)
+    reproduces the reference's still_hash on every frame of the fixture: a drifting scene, a square moving in, the
+    counts reaching avg, and a frame where everything changed."""
+    g = _golden(golden, "still.npz")
+    avg, px, grey = g["cfg"]
+    frames = _still_frames(g)
+    st = O.Still(frames[0].shape[1], frames[0].shape[0], int(avg), float(px), float(grey))
+    for k, f in enumerate(frames):
+        cells, m = st.frame(O.pyramid(f, 1)[0])
+        assert O.still_hash(cells, st.mean) == int(g["hashes"][k]), k
+        assert m.tobytes() == g["motion"][k].tobytes(), k
+    assert O.fnv(st.mean) == int(g["mean_fnv"])
+    assert int(g["motion"]["moving"][int(g["seq"][4])]) == len(cells)  # the frame where everything changed
+    st.close()
+
+
+def test_still_decision_on_reference_cells(golden):
+    """still_decide and still_update alone, fed the reference's own vectors of each frame: the reference's hash on
+    every frame, on any host (the decision's long double steps are exact or far from a rounding boundary here)."""
+    g = _golden(golden, "still.npz")
+    avg, px, grey = g["cfg"]
+    frames = _still_frames(g)
+    st = O.Still(frames[0].shape[1], frames[0].shape[0], int(avg), float(px), float(grey))
+    for k, f in enumerate(frames):
+        cells, m = st.frame(O.pyramid(f, 1)[0], cells=g["cells"][k])
+        assert O.still_hash(cells, st.mean) == int(g["hashes"][k]), k
+        assert np.array_equal(cells["state"], g["cells"][k]["state"])
+    st.close()
+
+
+@pytest.mark.skipif(not (O.ref_available() and X86), reason="needs the reference tree and x86-64")
+@pytest.mark.parametrize("w,h,frames,avg,px,grey", [(200, 120, 7, 3, 0.5, 2.0), (129, 77, 5, 16, 2.0, 6.0)])
+def test_still_against_reference_code(w, h, frames, avg, px, grey):
+    """Other sizes (a ragged last cell row and column), averaging depths and gates, against still.c itself."""
+    seq = S.still_sequence(w, h, frames, seed=11, jump_at=frames - 1, mover=16)
+    _, rm, rh, rmean = O.ref_still_run(seq, avg, px, grey)
+    st = O.Still(w, h, avg, px, grey)
+    for k, f in enumerate(seq):
+        cells, m = st.frame(O.pyramid(f, 1)[0])
+        assert O.still_hash(cells, st.mean) == int(rh[k]), k
+        assert m.tobytes() == rm[k].tobytes(), k
+    assert np.array_equal(st.mean, rmean)
+    st.close()
