@@ -628,6 +628,59 @@ def run_still(args) -> dict:
     return out
 
 
+def run_framegen(args) -> dict:
+    """Frame generation (framegen.c as tk_generate_make runs it): one generated frame between two frames of a warped
+    pair, CUDA-event time of the whole call (the field's pyramid, the scene test, search, filter and upscale at every
+    level, the middle vectors, the blended frame and its bytes), at 640 x 480, 1280 x 720 and 1920 x 1080. The fields
+    and frame are checked against the oracle, whose time (one CPU thread) is beside it. The reference's card: 5.98 ms a
+    1080p frame, 2.79 ms of it the search (docs/measurements.md:534-536); 1.68 to 1.93 ms at 640 x 480 (:532)."""
+    import torch
+
+    import vtg
+    import vtg_build
+
+    sys.path.insert(0, ORACLE)
+    import oracle as O
+
+    S = __import__("vtg_synth")
+    vtg_build.build()
+    ctx = vtg.Context(0)
+    out = {"metric": "generated frame ms (motion field, middle vectors, blend)", "unit": "ms",
+           "higher_is_better": False, "results": []}
+    card = {(640, 480): 1.93, (1920, 1080): 5.977}
+    for w, h in ((640, 480), (1280, 720), (1920, 1080)):
+        f0, f1, _, _ = S.warp_pair(w, h, (-17.0, 12.0), 3.0, seed=8)
+        a = torch.from_numpy(O.pyramid(f0, 1)[0]).cuda()
+        b = torch.from_numpy(O.pyramid(f1, 1)[0]).cuda()
+        dpic = torch.zeros((h, w), dtype=torch.uint8, device="cuda")
+        torch.cuda.synchronize()
+        fg = vtg.Framegen(ctx, w, h)
+        stream = torch.cuda.ExternalStream(fg.stream())
+        L = vtg.lib()
+        for _ in range(3):
+            vtg.check(L.vtg_framegen_run(fg.h, a.data_ptr(), w, b.data_ptr(), w, None, 0, dpic.data_ptr(), vtg.DEVICE,
+                                         None), "vtg_framegen_run")
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(20)]
+        for e0, e1 in ev:
+            e0.record(stream)
+            L.vtg_framegen_run(fg.h, a.data_ptr(), w, b.data_ptr(), w, None, 0, dpic.data_ptr(), vtg.DEVICE, None)
+            e1.record(stream)
+        torch.cuda.synchronize()
+        ms = float(np.median([e0.elapsed_time(e1) for e0, e1 in ev]))
+        r = fg.fields()
+        pic = dpic.cpu().numpy()
+        fg.close()
+        t0 = time.perf_counter()
+        o = O.framegen(O.pyramid(f0, 1)[0], O.pyramid(f1, 1)[0])
+        cpu_ms = 1e3 * (time.perf_counter() - t0)
+        same = np.array_equal(pic, o["pic"]) and all(x.tobytes() == y.tobytes() for x, y in zip(r["fil"], o["fil"]))
+        out["results"].append({"frame": "%dx%d" % (w, h), "levels": len(r["fil"]), "ms": ms,
+                               "same_as_oracle": bool(same), "cpu_oracle_ms_1_thread": cpu_ms,
+                               "reference_card_ms": card.get((w, h))})
+    ctx.close()
+    return out
+
+
 def run_profile(args) -> None:
     """Launches for an ncu capture, nothing timed: `batch` primes B 1080p streams (2 batched steps) and runs 2 more
     (capture lk_batch_kernel with -s 2); `ncc` runs one 1080p whole-picture search per precision (32 x 32 template)."""
@@ -665,6 +718,19 @@ def run_profile(args) -> None:
         _, m, _ = st.read()
         print("profile still: %d frames, %d moving" % (int(m["frames"]), int(m["moving"])))
         st.close()
+    elif args.profile == "framegen":
+        sys.path.insert(0, ORACLE)
+        import oracle as O
+
+        f0, f1, _, _ = S.warp_pair(W, H, (-17.0, 12.0), 3.0, seed=8)
+        a = torch.from_numpy(O.pyramid(f0, 1)[0]).cuda()
+        b = torch.from_numpy(O.pyramid(f1, 1)[0]).cuda()
+        torch.cuda.synchronize()
+        fg = vtg.Framegen(ctx, W, H)
+        for _ in range(2):
+            fg.run(a.data_ptr(), W, b.data_ptr(), W)
+        print("profile framegen: %d levels" % fg.levels)
+        fg.close()
     elif args.profile == "detect":
         sys.path.insert(0, ORACLE)
         import oracle as O
@@ -703,9 +769,11 @@ def main():
     ap.add_argument("--ncc", action="store_true",
                     help="the whole-picture appearance search on a 1080p frame (32, 64, 96 templates), per precision")
     ap.add_argument("--detect", action="store_true", help="corner detection on a 1080p plane: a 384 x 307 box, the frame")
+    ap.add_argument("--framegen", action="store_true",
+                    help="frame generation at 640 x 480, 1280 x 720 and 1920 x 1080 (motion field, middle vectors, blend)")
     ap.add_argument("--still", action="store_true",
                     help="the still picture a frame at 960 x 540 and 1920 x 1080 (vectors, decision, running mean)")
-    ap.add_argument("--profile", default=None, choices=["batch", "ncc", "detect", "still"],
+    ap.add_argument("--profile", default=None, choices=["batch", "ncc", "detect", "still", "framegen"],
                     help="a short run for an ncu capture: the batched step (prime, then 2 steps) or one NCC search")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -720,6 +788,9 @@ def main():
         return
     if args.still:
         print(json.dumps(run_still(args)))
+        return
+    if args.framegen:
+        print(json.dumps(run_framegen(args)))
         return
     line = run_reference(args) if args.impl == "reference" else run_ours(args)
     if line is not None:

@@ -304,6 +304,43 @@ int vtg_still_read(vtg_still *s, struct vtg_cell *cells, struct vtg_still_motion
 /* The mean plane in device memory (still_mean, still.h:45), valid until the next frame. */
 int vtg_still_mean(const vtg_still *s, const float **plane, int *pitch);
 
+/* ---- frame generation: a frame between two real ones (src/kern/framegen.h, src/kern/framegen.c; run as
+ *      tk_generate_make runs it, src/kern/track.c:847-888) ---- */
+
+typedef struct vtg_framegen vtg_framegen;
+
+/* struct fg_vec (src/kern/framegen.h:24-26): a block's vector, from the newer frame to the older, in pixels of its
+ * level. */
+struct vtg_fg_vec {
+    int16_t x, y;
+};
+
+/* For frames of w x h (64 to 8192 a side): the field's pyramid of both frames (their half size, then halves while
+ * both sides are >= 16, seven levels at most: track.c:547-556), its fields, the generated frame. */
+size_t vtg_framegen_bytes(int w, int h);
+int vtg_framegen_create(vtg_ctx *ctx, int w, int h, vtg_framegen **out);
+void vtg_framegen_destroy(vtg_framegen *g);
+void *vtg_framegen_stream(const vtg_framegen *g);
+int vtg_framegen_levels(const vtg_framegen *g);
+
+/* One generated frame between older and newer, w x h Q6 planes in device memory (e.g. two sets' level 0 of a tracker,
+ * vtg_level_device). The scene-change test (fg_hist_section, fg_scene_verdict), then coarsest first fg_search,
+ * fg_filter, fg_upscale, then fg_mid_vectors and fg_blend. out (device, rows out_pitch floats apart) receives the
+ * frame in Q6, or NULL keeps it inside (vtg_framegen_frame); pic (NULL, or host or device memory as `where` says)
+ * receives its bytes (img_q6_to_u8_vx, src/kern/img_vx.c:36-47), w a row. VTG_HOST waits for pic; otherwise
+ * asynchronous on `stream` (NULL: the generator's own). */
+int vtg_framegen_run(vtg_framegen *g, const float *older, int older_pitch, const float *newer, int newer_pitch,
+                     float *out, int out_pitch, uint8_t *pic, int where, void *stream);
+
+/* The last run's fields at `level` (raw = fg_search's, fil = fg_filter's, up = what the level started from; each
+ * ceil(level w / 8) x ceil(level h / 8)), the middle-instant field (level 0's blocks) and the scene verdict; any may
+ * be NULL. */
+int vtg_framegen_fields(vtg_framegen *g, int level, struct vtg_fg_vec *raw, struct vtg_fg_vec *fil,
+                        struct vtg_fg_vec *up, struct vtg_fg_vec *mid, int *scene, int where, void *stream);
+
+/* The generated frame inside the generator (device memory), valid until the next run. */
+int vtg_framegen_frame(const vtg_framegen *g, const float **plane, int *pitch);
+
 #ifdef __cplusplus
 }
 #endif

@@ -544,6 +544,81 @@ class Detector:
             pass
 
 
+FG_VEC = np.dtype([("x", "<i2"), ("y", "<i2")])  # struct vtg_fg_vec
+
+
+class Framegen:
+    """Frame generation (vtg_framegen): the motion field between two frames and the frame between them."""
+
+    def __init__(self, ctx: Context, w: int, h: int):
+        L = lib()
+        vp, i = C.c_void_p, C.c_int
+        L.vtg_framegen_bytes.argtypes = [i, i]
+        L.vtg_framegen_bytes.restype = C.c_size_t
+        L.vtg_framegen_create.argtypes = [vp, i, i, C.POINTER(vp)]
+        L.vtg_framegen_destroy.argtypes = [vp]
+        L.vtg_framegen_destroy.restype = None
+        L.vtg_framegen_stream.argtypes = [vp]
+        L.vtg_framegen_stream.restype = vp
+        L.vtg_framegen_levels.argtypes = [vp]
+        L.vtg_framegen_run.argtypes = [vp, vp, i, vp, i, vp, i, vp, i, vp]
+        L.vtg_framegen_fields.argtypes = [vp, i, vp, vp, vp, vp, vp, i, vp]
+        L.vtg_framegen_frame.argtypes = [vp, C.POINTER(vp), C.POINTER(i)]
+        self.ctx, self.w, self.h_ = ctx, w, h
+        self.h = C.c_void_p()
+        check(L.vtg_framegen_create(ctx.h, w, h, C.byref(self.h)), "vtg_framegen_create")
+        ctx._trackers.add(self)
+        self.levels = L.vtg_framegen_levels(self.h)
+        self.shapes = []
+        lw, lh = (w + 1) // 2, (h + 1) // 2
+        for _ in range(self.levels):
+            self.shapes.append((lw, lh, (lw + 7) // 8, (lh + 7) // 8))
+            lw, lh = (lw + 1) // 2, (lh + 1) // 2
+
+    def run(self, older_ptr: int, older_pitch: int, newer_ptr: int, newer_pitch: int, pic: bool = True):
+        """One generated frame between two device Q6 planes: its bytes (h x w) when pic, else None."""
+        out = np.zeros((self.h_, self.w), np.uint8) if pic else None
+        check(lib().vtg_framegen_run(self.h, older_ptr, older_pitch, newer_ptr, newer_pitch, None, 0,
+                                     None if out is None else _p(out), HOST, None), "vtg_framegen_run")
+        return out
+
+    def fields(self):
+        """{raw, fil, up: per level (bh x bw FG_VEC), mid, scene} of the last run."""
+        res = {"raw": [], "fil": [], "up": []}
+        _, _, bw0, bh0 = self.shapes[0]
+        mid = np.zeros((bh0, bw0), FG_VEC)
+        scene = C.c_int()
+        for L, (_, _, bw, bh) in enumerate(self.shapes):
+            a = [np.zeros((bh, bw), FG_VEC) for _ in range(3)]
+            check(lib().vtg_framegen_fields(self.h, L, _p(a[0]), _p(a[1]), _p(a[2]), _p(mid) if L == 0 else None,
+                                            C.byref(scene) if L == 0 else None, HOST, None), "vtg_framegen_fields")
+            for k, x in zip(("raw", "fil", "up"), a):
+                res[k].append(x)
+        res["mid"] = mid
+        res["scene"] = scene.value
+        return res
+
+    def frame_ptr(self):
+        """(device address, pitch in floats) of the last generated frame (Q6) inside the generator."""
+        p, pitch = C.c_void_p(), C.c_int()
+        check(lib().vtg_framegen_frame(self.h, C.byref(p), C.byref(pitch)), "vtg_framegen_frame")
+        return p.value, pitch.value
+
+    def stream(self):
+        return lib().vtg_framegen_stream(self.h)
+
+    def close(self):
+        if self.h:
+            lib().vtg_framegen_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class StillConfig(C.Structure):
     """struct vtg_still_config: still_cfg (src/kern/still.h:21-27) without its thread count."""
     _fields_ = [("w", C.c_int), ("h", C.c_int), ("avg", C.c_int), ("motion_px", C.c_float),

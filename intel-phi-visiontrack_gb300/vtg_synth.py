@@ -147,6 +147,16 @@ def still_sequence(w: int, h: int, frames: int, seed: int, jump_at: int | None =
     return out
 
 
+def framegen_pair(kind: str, w: int, h: int, shift, seed: int):
+    """A frame pair for frame generation: "pair", a warped pair (a global shift and a smooth field of 0.5 px); "scene",
+    a scene change (the same picture 110 grey brighter and inverted)."""
+    if kind == "scene":
+        f0 = noise_frame(w, h, seed)
+        return f0, (255 - np.minimum(f0.astype(np.int32) + 110, 255)).astype(np.uint8)
+    f0, f1, _, _ = warp_pair(w, h, shift, 0.5, seed=seed)
+    return f0, f1
+
+
 def seeded_shift(seed: int, stream: int, reach: float = 12.0):
     u = uniform(seed, 100 + stream, 2)
     return (float(-reach + 2 * reach * u[0]), float(-reach + 2 * reach * u[1]))

@@ -106,6 +106,9 @@ def lib() -> C.CDLL:
         _lib.or_still_update.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int]
         _lib.or_still_finish.argtypes = [C.c_void_p]
         _lib.or_still_motion.argtypes = [C.c_void_p, C.c_void_p]
+        _lib.or_fg_levels.argtypes = [C.c_int, C.c_int]
+        _lib.or_framegen.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                     C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
     return _lib
 
 
@@ -207,6 +210,9 @@ def ref() -> C.CDLL:
         _ref.ref_still_vectors.restype = C.c_int
         _ref.ref_still_vectors.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p]
         _ref.ref_still_run.restype = C.c_int
+        _ref.ref_framegen.restype = C.c_int
+        _ref.ref_framegen.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                      C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         _ref.ref_still_run.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float,
                                        C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
     return _ref
@@ -529,3 +535,61 @@ def ref_still_run(frames, avg=8, motion_px=1.0, motion_grey=4.0):
                               _p(cells), _p(motion), _p(hashes), _p(mean))
     assert got == n
     return cells, motion, hashes, mean
+
+
+# ---------------------------------------------------------------- frame generation (src/kern/framegen.c)
+
+FG_VEC = np.dtype([("x", "<i2"), ("y", "<i2")])  # struct fg_vec
+
+
+def fg_shapes(w: int, h: int):
+    """The field's levels for w x h frames: [(level w, level h, blocks across, blocks down)], level 0 first."""
+    out, lw, lh = [], (w + 1) // 2, (h + 1) // 2
+    while len(out) < 7 and lw >= 16 and lh >= 16:
+        out.append((lw, lh, (lw + 7) // 8, (lh + 7) // 8))
+        lw, lh = (lw + 1) // 2, (lh + 1) // 2
+    return out
+
+
+def _fg_outputs(w, h):
+    shapes = fg_shapes(w, h)
+    total = sum(bw * bh for _, _, bw, bh in shapes)
+    return (shapes, np.zeros(total, FG_VEC), np.zeros(total, FG_VEC), np.zeros(total, FG_VEC),
+            np.zeros(shapes[0][2] * shapes[0][3], FG_VEC), np.zeros((h, w), np.float32), np.zeros((h, w), np.uint8))
+
+
+def _fg_split(shapes, raw, fil, up, mid, out, pic, scene):
+    res = {"scene": int(scene), "raw": [], "fil": [], "up": [], "mid": mid.reshape(shapes[0][3], shapes[0][2]),
+           "out": out, "pic": pic}
+    o = 0
+    for _, _, bw, bh in shapes:
+        for k, a in (("raw", raw), ("fil", fil), ("up", up)):
+            res[k].append(a[o:o + bw * bh].reshape(bh, bw))
+        o += bw * bh
+    return res
+
+
+def framegen(a0, b0):
+    """The oracle's generated frame between Q6 planes a0 (older) and b0 (newer): a dict of the fields per level (raw,
+    fil, up), mid, the frame (Q6) and its bytes, and the scene verdict."""
+    a0 = np.ascontiguousarray(a0, np.float32)
+    b0 = np.ascontiguousarray(b0, np.float32)
+    h, w = a0.shape
+    shapes, raw, fil, up, mid, out, pic = _fg_outputs(w, h)
+    scene = lib().or_framegen(_p(a0), _p(b0), w, h, w, _p(raw), _p(fil), _p(up), _p(mid), _p(out), _p(pic))
+    assert scene >= 0
+    return _fg_split(shapes, raw, fil, up, mid, out, pic, scene)
+
+
+def ref_framegen(fa, fb):
+    """The reference's framegen.c on two 8-bit frames, the same dict."""
+    h, w = fa.shape
+    stride = (w + 15) & ~15
+    ba = np.zeros((h, stride), np.uint8)
+    bb = np.zeros((h, stride), np.uint8)
+    ba[:, :w] = fa
+    bb[:, :w] = fb
+    shapes, raw, fil, up, mid, out, pic = _fg_outputs(w, h)
+    scene = ref().ref_framegen(_p(ba), _p(bb), stride, w, h, _p(raw), _p(fil), _p(up), _p(mid), _p(out), _p(pic))
+    assert scene >= 0
+    return _fg_split(shapes, raw, fil, up, mid, out, pic, scene)

@@ -12,6 +12,7 @@
 #include <string.h>
 
 #include "detect.h"
+#include "framegen.h"
 #include "img.h"
 #include "lk.h"
 #include "plane.h"
@@ -255,4 +256,75 @@ int ref_still_run(const uint8_t *frames, int nframes, int stride, int w, int h, 
     for (int y = 0; y < h; y++)
         memcpy(mean_out + (size_t)y * (size_t)w, plane_row(mp, y), sizeof(float) * (size_t)w);
     return n;
+}
+
+
+/* The reference's frame generation between two 8-bit frames, in the order tk_generate_make runs it
+ * (src/kern/track.c:847-888, without the tracker): the field's pyramid from the frames' Q6 pyramids (levels 1 ..),
+ * fg_hist_section over the nine sections of each frame's field level 1, fg_scene_verdict, then coarsest first
+ * fg_search, fg_filter and fg_upscale, fg_mid_vectors, fg_blend, the padding and img_q6_to_u8_vx. Outputs as the
+ * oracle's or_framegen (fields level by level, up of the top level zero). Returns the verdict, or -1. */
+int ref_framegen(const uint8_t *fa, const uint8_t *fb, int stride, int w, int h, struct fg_vec *raw_out,
+                 struct fg_vec *fil_out, struct fg_vec *up_out, struct fg_vec *mid_out, float *out, uint8_t *pic)
+{
+    int lw = (w + 1) / 2, lh = (h + 1) / 2, levels = 0;
+    for (int i = 0; i < FG_MAX_LEVELS && lw >= 16 && lh >= 16; i++) {
+        levels++;
+        lw = (lw + 1) / 2;
+        lh = (lh + 1) / 2;
+    }
+    if (levels < 2)
+        return -1;
+    struct ref_pyr A, B;
+    build(&A, fa, stride, w, h, levels + 1, 0);
+    build(&B, fb, stride, w, h, levels + 1, 0);
+    struct fg_job j;
+    memset(&j, 0, sizeof j);
+    const size_t bytes = fg_bytes((w + 1) / 2, (h + 1) / 2, levels);
+    void *mem = aligned_alloc(64, (bytes + 63) & ~(size_t)63);
+    memset(mem, 0, bytes);
+    fg_init(&j, mem, (w + 1) / 2, (h + 1) / 2, levels);
+    for (int i = 0; i < levels; i++) {
+        j.a[i] = A.l[i + 1];
+        j.b[i] = B.l[i + 1];
+    }
+    j.a0 = A.l[0];
+    j.b0 = B.l[0];
+    j.out = new_plane(w, h);
+    for (int s = 0; s < FG_SECTIONS; s++) {
+        fg_hist_section(&j.a[1], j.hist_a, s);
+        fg_hist_section(&j.b[1], j.hist_b, s);
+    }
+    j.scene_changed = fg_scene_verdict(&j);
+    for (int L = levels - 1; L >= 0; L--) {
+        fg_search(&j, L, 0, j.raw[L].w * j.raw[L].h);
+        fg_filter(&j, L, 0, j.fil[L].w * j.fil[L].h);
+        if (L > 0)
+            fg_upscale(&j, L, 0, j.up[L - 1].w * j.up[L - 1].h);
+    }
+    fg_mid_vectors(&j, 0, j.mid.w * j.mid.h);
+    fg_blend(&j, 0, fg_tiles(&j));
+    img_pad_rows(&j.out, 0, h);
+    img_pad_tb(&j.out);
+    uint8_t *buf = malloc((size_t)w * (size_t)h + 64);
+    img_q6_to_u8_vx(&j.out, buf, 0, h);
+    size_t off = 0;
+    for (int L = 0; L < levels; L++) {
+        const size_t n = (size_t)j.raw[L].w * (size_t)j.raw[L].h;
+        memcpy(raw_out + off, j.raw[L].v, n * sizeof(struct fg_vec));
+        memcpy(fil_out + off, j.fil[L].v, n * sizeof(struct fg_vec));
+        memcpy(up_out + off, j.up[L].v, n * sizeof(struct fg_vec));
+        off += n;
+    }
+    memcpy(mid_out, j.mid.v, (size_t)j.mid.w * (size_t)j.mid.h * sizeof(struct fg_vec));
+    for (int y = 0; y < h; y++)
+        memcpy(out + (size_t)y * (size_t)w, plane_row(&j.out, y), sizeof(float) * (size_t)w);
+    memcpy(pic, buf, (size_t)w * (size_t)h);
+    const int scene = j.scene_changed;
+    free(buf);
+    free_plane(&j.out);
+    free(mem);
+    release(&A);
+    release(&B);
+    return scene;
 }

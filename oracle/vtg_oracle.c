@@ -16,6 +16,9 @@
  *     selection of detect_finish (detect.c:175-258), long double as the reference;
  *   - the still picture's decision and update (src/kern/still.c:143-246): the noise median, each cell's evidence, the
  *     3 x 3 vote, the counts and weights, the drift statistics, and the running mean; long double as the reference.
+ *   - frame generation (src/kern/framegen.c, as src/kern/track.c:847-888 runs it): the scene-change test, the block
+ *     SAD search, filter and upscale over the field's pyramid, the middle-instant vectors and the blended frame;
+ *     whole-number planes, so exact in any arithmetic.
  *
  * Two arithmetics for everything that is floating point:
  *   OR_LANE  the reference's replay arithmetic: F32 patch sums in 16 lanes, each lane a chain of fused multiply-adds in
@@ -1242,4 +1245,342 @@ void or_still_motion(const struct or_still *s, struct or_still_motion *m)
     m->diff_median = s->diff_median;
     m->diff_limit = s->diff_limit;
     m->frames = s->frames;
+}
+
+/* ---------------------------------------------------------------- frame generation (src/kern/framegen.c) */
+
+/* The field's pyramid, the 16 x 16 SAD search of each 8 x 8 block around the coarser level's estimate, the 3 x 3
+ * filter, the four-candidate upscale, the vectors at the middle instant and the blended frame, as the tracker runs
+ * them for one generated frame (src/kern/track.c:847-888). Planes are whole-number Q6 values, so every sum is exact in
+ * F32: the results are the reference's in any arithmetic. The reference reads its replicated padding; here that is a
+ * clamped index, except where the search window's origin is clamped (that moves the offsets searched). */
+
+#define OR_FG_LEVELS 7 /* FG_MAX_LEVELS */
+
+struct or_fg_vec {
+    int16_t x, y;
+};
+
+struct or_plane {
+    const float *p;
+    int w, h, stride;
+};
+
+static inline float fpx(const struct or_plane *q, int x, int y)
+{
+    return q->p[(size_t)clampi(y, 0, q->h - 1) * (size_t)q->stride + (size_t)clampi(x, 0, q->w - 1)];
+}
+
+/* The field's levels for w x h frames (track.c:547-556): level 0 is the frame's half size, each next half that, while
+ * both sides are at least 16, seven at most. */
+int or_fg_levels(int w, int h)
+{
+    int lw = (w + 1) / 2, lh = (h + 1) / 2, n = 0;
+    while (n < OR_FG_LEVELS && lw >= 16 && lh >= 16) {
+        n++;
+        lw = (lw + 1) / 2;
+        lh = (lh + 1) / 2;
+    }
+    return n;
+}
+
+/* fg_hist_section + fg_scene_verdict (framegen.c:85-113): 64 bins of 4 grey levels over every second row of nine
+ * sections (columns cut to multiples of 16); the scene changed when more than half the samples moved bins. */
+static void fg_hist(const struct or_plane *p, uint32_t *hist)
+{
+    memset(hist, 0, 9 * 64 * sizeof(uint32_t));
+    for (int s = 0; s < 9; s++) {
+        const int sx = s % 3, sy = s / 3;
+        const int x0 = (p->w * sx / 3) & ~15, x1 = (p->w * (sx + 1) / 3) & ~15;
+        const int y0 = p->h * sy / 3, y1 = p->h * (sy + 1) / 3;
+        for (int y = y0; y < y1; y += 2)
+            for (int x = x0; x < x1; x++)
+                hist[s * 64 + ((int)(p->p[(size_t)y * p->stride + x] * (1.0f / 256.0f)) & 63)]++;
+    }
+}
+
+/* The block search at one level (fg_search, framegen.c:117-214). */
+static void fg_search_level(const struct or_plane *cur, const struct or_plane *old, const struct or_fg_vec *pred,
+                            struct or_fg_vec *out, int bw, int bh, int level, int scene)
+{
+    const int lanes = (old->w + 15) & ~15;
+    for (int i = 0; i < bw * bh; i++) {
+        if (scene) {
+            out[i].x = out[i].y = 0;
+            continue;
+        }
+        const int px = (i % bw) * 8, py = (i / bw) * 8;
+        const int wx = pred ? pred[i].x : 0, wy = pred ? pred[i].y : 0;
+        const int x0 = clampi(px + wx - 8, -32, lanes), y0 = py + wy - 8;
+        const int pvx = x0 - px + 8, pvy = wy;
+        if (level == 0) {
+            /* a block the estimate already explains is not searched (at most 2 grey levels a pixel) */
+            float sum = 0.0f;
+            for (int r = 0; r < 8; r++)
+                for (int n = 0; n < 8; n++)
+                    sum += fabsf(fpx(cur, px + n, py + r) - fpx(old, px + pvx + n, py + r + pvy));
+            if (sum <= 8192.0f) {
+                out[i].x = (int16_t)pvx;
+                out[i].y = (int16_t)pvy;
+                continue;
+            }
+        }
+        /* 256 places, the cost of each with a tie-break toward less motion; the first lowest in row order */
+        float best = 0.0f;
+        int fx = 0, fy = 0;
+        for (int dy = 0; dy < 16; dy++)
+            for (int dx = 0; dx < 16; dx++) {
+                float cost = (float)(dx > 8 ? dx - 8 : 8 - dx) + (float)(dy > 8 ? dy - 8 : 8 - dy);
+                for (int r = 0; r < 8; r++)
+                    for (int n = 0; n < 8; n++)
+                        cost += fabsf(fpx(old, x0 + dx + n, y0 + dy + r) - fpx(cur, px + n, py + r));
+                if ((dx == 0 && dy == 0) || cost < best) {
+                    best = cost;
+                    fx = dx;
+                    fy = dy;
+                }
+            }
+        int vx = x0 - px + fx, vy = wy + fy - 8;
+        if (level == 0) {
+            /* no motion, when it matches as well as the best: the finest level's fallback */
+            float sum = 0.0f;
+            for (int r = 0; r < 8; r++)
+                for (int n = 0; n < 8; n++)
+                    sum += fabsf(fpx(cur, px + n, py + r) - fpx(old, px + n, py + r));
+            if (sum <= best)
+                vx = vy = 0;
+        }
+        out[i].x = (int16_t)vx;
+        out[i].y = (int16_t)vy;
+    }
+}
+
+/* fg_filter (framegen.c:218-247): of the 3 x 3 around a block (clamped), the vector with the least sum of squared
+ * differences from the other eight; ties to the first in column-major order. */
+static void fg_filter_level(const struct or_fg_vec *in, struct or_fg_vec *out, int bw, int bh)
+{
+    for (int i = 0; i < bw * bh; i++) {
+        const int bx = i % bw, by = i / bw;
+        int mx[9], my[9], k = 0;
+        for (int xx = -1; xx <= 1; xx++)
+            for (int yy = -1; yy <= 1; yy++) {
+                const struct or_fg_vec v = in[clampi(by + yy, 0, bh - 1) * bw + clampi(bx + xx, 0, bw - 1)];
+                mx[k] = v.x;
+                my[k] = v.y;
+                k++;
+            }
+        int pick = 0;
+        uint32_t least = 0;
+        for (int a = 0; a < 9; a++) {
+            uint32_t d = 0;
+            for (int b = 0; b < 9; b++) {
+                const int dx = mx[a] - mx[b], dy = my[a] - my[b];
+                d += (uint32_t)(dx * dx + dy * dy);
+            }
+            if (a == 0 || d < least) {
+                least = d;
+                pick = a;
+            }
+        }
+        out[i].x = (int16_t)mx[pick];
+        out[i].y = (int16_t)my[pick];
+    }
+}
+
+/* fg_upscale (framegen.c:251-288): each block of the finer level takes, of the four nearest blocks of this level, the
+ * vector whose 4 x 4 SAD at this level is least (the first on a tie), doubled. */
+static void fg_upscale_level(const struct or_plane *cur, const struct or_plane *old, const struct or_fg_vec *in,
+                             int bw, int bh, struct or_fg_vec *out, int ow, int oh, int scene)
+{
+    for (int i = 0; i < ow * oh; i++) {
+        if (scene) {
+            out[i].x = out[i].y = 0;
+            continue;
+        }
+        const int gx = i % ow, gy = i / ow;
+        float best = 0.0f;
+        int bx_ = 0, by_ = 0;
+        for (int n = 0; n < 4; n++) {
+            const int xo = n % 2 - 1 + gx % 2, yo = n / 2 - 1 + gy % 2;
+            const struct or_fg_vec v = in[clampi(gy / 2 + yo, 0, bh - 1) * bw + clampi(gx / 2 + xo, 0, bw - 1)];
+            float s = 0.0f;
+            for (int r = 0; r < 4; r++)
+                for (int c = 0; c < 4; c++)
+                    s += fabsf(fpx(cur, gx * 4 + c, gy * 4 + r) - fpx(old, gx * 4 + c + v.x, gy * 4 + r + v.y));
+            if (n == 0 || s < best) {
+                best = s;
+                bx_ = v.x;
+                by_ = v.y;
+            }
+        }
+        out[i].x = (int16_t)(bx_ * 2);
+        out[i].y = (int16_t)(by_ * 2);
+    }
+}
+
+/* How well the two frames agree over a block moved half way each (framegen.c:292-303). */
+static float fg_sad_mid(const struct or_plane *a, const struct or_plane *b, int x, int y, int vx, int vy)
+{
+    const int ax = vx >> 1, ay = vy >> 1, bx = vx - ax, by = vy - ay;
+    float s = 0.0f;
+    for (int r = 0; r < 8; r++)
+        for (int c = 0; c < 8; c++)
+            s += fabsf(fpx(a, x + c + ax, y + r + ay) - fpx(b, x + c - bx, y + r - by));
+    return s;
+}
+
+/* fg_mid_vectors (framegen.c:305-328): no motion first, favoured by one grey level over the block, then each vector
+ * of the 3 x 3 that agrees better. */
+static void fg_mid_level(const struct or_plane *a, const struct or_plane *b, const struct or_fg_vec *fil, int bw,
+                         int bh, struct or_fg_vec *out)
+{
+    for (int i = 0; i < bw * bh; i++) {
+        const int bx = i % bw, by = i / bw, px = bx * 8, py = by * 8;
+        float best = fg_sad_mid(a, b, px, py, 0, 0) - 64.0f;
+        int vx = 0, vy = 0;
+        for (int yy = -1; yy <= 1; yy++)
+            for (int xx = -1; xx <= 1; xx++) {
+                const struct or_fg_vec v = fil[clampi(by + yy, 0, bh - 1) * bw + clampi(bx + xx, 0, bw - 1)];
+                if ((v.x == vx && v.y == vy) || (v.x == 0 && v.y == 0))
+                    continue;
+                const float s = fg_sad_mid(a, b, px, py, v.x, v.y);
+                if (s < best) {
+                    best = s;
+                    vx = v.x;
+                    vy = v.y;
+                }
+            }
+        out[i].x = (int16_t)vx;
+        out[i].y = (int16_t)vy;
+    }
+}
+
+/* fg_blend (framegen.c:332-357): 16 x 16 tiles of the full-size frame; where the nine vectors around a tile agree,
+ * the two frames moved half way each, averaged; elsewhere a pixel takes from the tile's own row of vectors and the
+ * row above or below, by triangles in 32nds across and down, 2048ths in all, as six fused multiply-adds in order.
+ * Rounded to the nearest, ties to even. */
+static void fg_blend_frame(const struct or_plane *a0, const struct or_plane *b0, const struct or_fg_vec *mid, int bw,
+                           int bh, float *out, int out_stride)
+{
+    static const float WL[16] = {15, 13, 11, 9, 7, 5, 3, 1, 0, 0, 0, 0, 0, 0, 0, 0};
+    static const float WS[16] = {17, 19, 21, 23, 25, 27, 29, 31, 31, 29, 27, 25, 23, 21, 19, 17};
+    static const float WR[16] = {0, 0, 0, 0, 0, 0, 0, 0, 1, 3, 5, 7, 9, 11, 13, 15};
+    const float *wh[3] = {WL, WS, WR};
+    const int w = a0->w, h = a0->h, tw = (w + 15) / 16, th = (h + 15) / 16;
+    for (int t = 0; t < tw * th; t++) {
+        const int tx = t % tw, ty = t / tw, x0 = tx * 16, y0 = ty * 16;
+        struct or_fg_vec near[3][3];
+        int same = 1;
+        for (int yy = 0; yy < 3; yy++)
+            for (int xx = 0; xx < 3; xx++) {
+                near[yy][xx] = mid[clampi(ty + yy - 1, 0, bh - 1) * bw + clampi(tx + xx - 1, 0, bw - 1)];
+                same &= near[yy][xx].x == near[0][0].x && near[yy][xx].y == near[0][0].y;
+            }
+        for (int y = y0; y < y0 + 16 && y < h; y++)
+            for (int k = 0; k < 16 && x0 + k < w; k++) {
+                const int x = x0 + k;
+                float v;
+                if (same) {
+                    const int vx = near[0][0].x, vy = near[0][0].y;
+                    v = rintf((fpx(a0, x + vx, y + vy) + fpx(b0, x - vx, y - vy)) * 0.5f);
+                } else {
+                    const int s = y - y0, other = s < 8 ? 0 : 2, wo = s < 8 ? 15 - 2 * s : 2 * s - 15;
+                    const float vw[2] = {(float)(32 - wo), (float)wo};
+                    const int rows[2] = {1, other};
+                    float acc = 0.0f;
+                    for (int a = 0; a < 2; a++)
+                        for (int b = 0; b < 3; b++) {
+                            const struct or_fg_vec q = near[rows[a]][b];
+                            const float sum = fpx(a0, x + q.x, y + q.y) + fpx(b0, x - q.x, y - q.y);
+                            acc = fmaf(sum, wh[b][k] * vw[a], acc);
+                        }
+                    v = rintf(acc * (1.0f / 2048.0f));
+                }
+                out[(size_t)y * out_stride + x] = v;
+            }
+    }
+}
+
+/* One generated frame between a0 (older) and b0 (newer), w x h Q6 planes rows `stride` floats apart. Outputs, any
+ * may be NULL: the fields raw, fil and up of every level one after the other (level 0 first, each ceil(lw / 8) x
+ * ceil(lh / 8); up of the top level is zero), mid (level 0's blocks), the frame out (w x h, Q6) and pic (w x h bytes,
+ * img_q6_to_u8: clamp(rint(q / 64))). Returns the scene-change verdict, or -1 when the frames are smaller than
+ * 64 x 64. */
+int or_framegen(const float *a0, const float *b0, int w, int h, int stride, struct or_fg_vec *raw_out,
+                struct or_fg_vec *fil_out, struct or_fg_vec *up_out, struct or_fg_vec *mid_out, float *out,
+                uint8_t *pic)
+{
+    const int levels = or_fg_levels(w, h);
+    if (levels < 2)
+        return -1;
+    float *pa[OR_FG_LEVELS], *pb[OR_FG_LEVELS];
+    struct or_plane A[OR_FG_LEVELS], B[OR_FG_LEVELS];
+    int bw[OR_FG_LEVELS], bh[OR_FG_LEVELS];
+    size_t off[OR_FG_LEVELS + 1];
+    off[0] = 0;
+    int lw = w, lh = h;
+    const float *sa = a0, *sb = b0;
+    int ss = stride;
+    for (int L = 0; L < levels; L++) {
+        const int nw = (lw + 1) / 2, nh = (lh + 1) / 2;
+        pa[L] = malloc(sizeof(float) * (size_t)nw * (size_t)nh);
+        pb[L] = malloc(sizeof(float) * (size_t)nw * (size_t)nh);
+        or_reduce(sa, lw, lh, ss, pa[L], nw);
+        or_reduce(sb, lw, lh, ss, pb[L], nw);
+        A[L] = (struct or_plane){pa[L], nw, nh, nw};
+        B[L] = (struct or_plane){pb[L], nw, nh, nw};
+        bw[L] = (nw + 7) / 8;
+        bh[L] = (nh + 7) / 8;
+        off[L + 1] = off[L] + (size_t)bw[L] * (size_t)bh[L];
+        lw = nw;
+        lh = nh;
+        sa = pa[L];
+        sb = pb[L];
+        ss = nw;
+    }
+    struct or_fg_vec *raw = calloc(off[levels], sizeof *raw), *fil = calloc(off[levels], sizeof *fil);
+    struct or_fg_vec *up = calloc(off[levels], sizeof *up), *mid = calloc(off[0 + 1], sizeof *mid);
+    uint32_t ha[9 * 64], hb[9 * 64];
+    fg_hist(&A[1], ha);
+    fg_hist(&B[1], hb);
+    uint64_t diff = 0, total = 0;
+    for (int i = 0; i < 9 * 64; i++) {
+        diff += ha[i] > hb[i] ? ha[i] - hb[i] : hb[i] - ha[i];
+        total += hb[i];
+    }
+    const int scene = total && diff > total; /* diff / 2 / total > 0.5 */
+    for (int L = levels - 1; L >= 0; L--) {
+        fg_search_level(&B[L], &A[L], L == levels - 1 ? NULL : up + off[L], raw + off[L], bw[L], bh[L], L, scene);
+        fg_filter_level(raw + off[L], fil + off[L], bw[L], bh[L]);
+        if (L > 0)
+            fg_upscale_level(&B[L], &A[L], fil + off[L], bw[L], bh[L], up + off[L - 1], bw[L - 1], bh[L - 1], scene);
+    }
+    fg_mid_level(&A[0], &B[0], fil, bw[0], bh[0], mid);
+    float *frame = out ? out : malloc(sizeof(float) * (size_t)w * (size_t)h);
+    const struct or_plane F0 = {a0, w, h, stride}, G0 = {b0, w, h, stride};
+    fg_blend_frame(&F0, &G0, mid, bw[0], bh[0], frame, w);
+    if (pic)
+        for (size_t i = 0; i < (size_t)w * (size_t)h; i++) {
+            const float s = rintf(frame[i] * (1.0f / 64.0f));
+            pic[i] = s <= 0.0f ? 0u : s >= 255.0f ? 255u : (uint8_t)s;
+        }
+    if (raw_out)
+        memcpy(raw_out, raw, sizeof *raw * off[levels]);
+    if (fil_out)
+        memcpy(fil_out, fil, sizeof *fil * off[levels]);
+    if (up_out)
+        memcpy(up_out, up, sizeof *up * off[levels]);
+    if (mid_out)
+        memcpy(mid_out, mid, sizeof *mid * off[1]);
+    if (!out)
+        free(frame);
+    free(raw);
+    free(fil);
+    free(up);
+    free(mid);
+    for (int L = 0; L < levels; L++) {
+        free(pa[L]);
+        free(pb[L]);
+    }
+    return scene;
 }

@@ -19,6 +19,8 @@ Writes:
                     corners found.
   still.npz         the still picture (still_vectors, still_decide, still_update, still_finish) over a 12-frame
                     320 x 240 sequence: per frame the cells after the decision, still_motion and still_hash.
+  framegen.npz      frame generation (framegen.c as tk_generate_make runs it) on three pairs: the fields of every
+                    level, the middle-instant field, hashes of the generated frame and its bytes, the scene verdict.
 Frames are not stored: the generator reproduces them bit for bit, and their hashes are stored to prove it.
 """
 from __future__ import annotations
@@ -144,6 +146,7 @@ def main(ref_root: str = "/root/reference") -> None:
                         xs=np.concatenate(xs_all).astype(np.float32), ys=np.concatenate(ys_all).astype(np.float32),
                         counts=np.array(counts, np.int32))
     write_still()
+    write_framegen()
     print("golden fixtures written to", HERE)
 
 
@@ -162,6 +165,29 @@ def write_still() -> None:
                         seq=np.array([STILL_SEQ[k] for k in ("w", "h", "frames", "seed", "jump_at")], np.int64),
                         cfg=np.array([STILL_CFG["avg"], STILL_CFG["motion_px"], STILL_CFG["motion_grey"]], np.float64),
                         cells=cells, motion=motion, hashes=hashes, mean_fnv=np.uint64(O.fnv(mean)))
+
+
+FG_CASES = [("pair", 640, 480, (6.3, 1.1), 3), ("odd", 333, 199, (-9.0, 5.5), 2), ("scene", 320, 240, (0.0, 0.0), 4)]
+
+
+def write_framegen() -> None:
+    """framegen.npz: the reference's frame generation (framegen.c, in tk_generate_make's order) on three pairs: every
+    level's raw, filtered and upscaled fields, the middle-instant field, hashes of the frame and its bytes, the scene
+    verdict."""
+    out = {}
+    for kind, w, h, shift, seed in FG_CASES:
+        f0, f1 = S.framegen_pair("scene" if kind == "scene" else "pair", w, h, shift, seed)
+        r = O.ref_framegen(f0, f1)
+        out[kind + "_frames_fnv"] = np.array([O.fnv(f0), O.fnv(f1)], np.uint64)
+        out[kind + "_scene"] = np.int32(r["scene"])
+        for k in ("raw", "fil", "up"):
+            out[kind + "_" + k] = np.concatenate([a.ravel() for a in r[k]])
+        out[kind + "_mid"] = r["mid"].ravel()
+        out[kind + "_out_fnv"] = np.uint64(O.fnv(r["out"]))
+        out[kind + "_pic_fnv"] = np.uint64(O.fnv(r["pic"]))
+    out["cases"] = np.array([(k == "scene", w, h, sx, sy, seed) for k, w, h, (sx, sy), seed in FG_CASES], np.float64)
+    out["kinds"] = np.array([k for k, *_ in FG_CASES])
+    np.savez_compressed(os.path.join(HERE, "framegen.npz"), **out)
 
 
 if __name__ == "__main__":

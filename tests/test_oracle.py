@@ -334,3 +334,43 @@ def test_still_against_reference_code(w, h, frames, avg, px, grey):
         assert m.tobytes() == rm[k].tobytes(), k
     assert np.array_equal(st.mean, rmean)
     st.close()
+
+
+def fg_cases(g):
+    """The fixture's pairs: (kind, frames)."""
+    out = []
+    for kind, (scene, w, h, sx, sy, seed) in zip(g["kinds"], g["cases"]):
+        f0, f1 = S.framegen_pair("scene" if scene else "pair", int(w), int(h), (float(sx), float(sy)), int(seed))
+        assert [O.fnv(f0), O.fnv(f1)] == [int(v) for v in g[str(kind) + "_frames_fnv"]]
+        out.append((str(kind), f0, f1))
+    return out
+
+
+def test_framegen_fixture(golden):
+    """The oracle's frame generation reproduces the reference's framegen.c (tests/golden/framegen.npz) on every pair:
+    each level's raw, filtered and upscaled field, the middle-instant field, the frame, its bytes, the verdict."""
+    g = _golden(golden, "framegen.npz")
+    for kind, f0, f1 in fg_cases(g):
+        r = O.framegen(O.pyramid(f0, 1)[0], O.pyramid(f1, 1)[0])
+        assert r["scene"] == int(g[kind + "_scene"]), kind
+        for k in ("raw", "fil", "up"):
+            assert np.array_equal(np.concatenate([a.ravel() for a in r[k]]), g[kind + "_" + k]), (kind, k)
+        assert np.array_equal(r["mid"].ravel(), g[kind + "_mid"]), kind
+        assert O.fnv(r["out"]) == int(g[kind + "_out_fnv"]) and O.fnv(r["pic"]) == int(g[kind + "_pic_fnv"]), kind
+    assert int(g["scene_scene"]) == 1 and int(g["pair_scene"]) == 0
+
+
+@pytest.mark.skipif(not O.ref_available(), reason="the reference tree is not on this machine")
+@pytest.mark.parametrize("w,h,shift,amp,seed", [(256, 192, (30.0, -22.0), 2.0, 5), (401, 257, (-1.2, 0.4), 0.0, 6),
+                                                (130, 66, (4.5, 7.5), 1.0, 7), (800, 600, (-17.0, 12.0), 3.0, 8)])
+def test_framegen_against_reference_code(w, h, shift, amp, seed):
+    """Shifts past the finest level's reach (found through the coarse levels), no motion, small and odd sizes."""
+    f0, f1, _, _ = S.warp_pair(w, h, shift, amp, seed=seed)
+    r = O.ref_framegen(f0, f1)
+    o = O.framegen(O.pyramid(f0, 1)[0], O.pyramid(f1, 1)[0])
+    assert r["scene"] == o["scene"]
+    for k in ("raw", "fil", "up"):
+        for a, b in zip(r[k], o[k]):
+            assert np.array_equal(a, b), k
+    for k in ("mid", "out", "pic"):
+        assert np.array_equal(r[k], o[k]), k
