@@ -14,7 +14,8 @@
  *
  * One call, on one stream:
  *   fg_reduce_kernel      the field's pyramid of both frames: level 0 is the frames' half size (x(levels))
- *   fg_hist_kernel        64-bin histograms of nine sections of both frames' level 1; the last CTA's verdict
+ *   fg_hist_kernel        64-bin histograms of nine sections of both frames' level 1 (8 CTAs a section); the last
+ *                         CTA's verdict
  *   fg_search_kernel      a warp an 8 x 8 block: the 24 x 24 window in shared memory, a lane 8 of the 256 offsets
  *   fg_filter_kernel      a thread a block: the 3 x 3's vector nearest the others
  *   fg_upscale_kernel     a thread a finer block: of four coarse vectors, the least 4 x 4 SAD, doubled
@@ -90,13 +91,16 @@ __global__ void fg_reduce_kernel(const float *__restrict__ sa, const float *__re
     (blockIdx.z ? db : da)[(size_t)y * dp + x] = (float)((sum + 128) >> 8);
 }
 
-/* fg_hist_section (framegen.c:85-101): section blockIdx.x of frame blockIdx.y; the last CTA compares them
- * (fg_scene_verdict, framegen.c:103-113: more than half the samples in other bins, i.e. sum |a - b| > sum b). */
+/* fg_hist_section (framegen.c:85-101): section blockIdx.x % 9 of frame blockIdx.x / 9, its sampled rows split over
+ * FG_HIST_SPLIT CTAs (blockIdx.y), added into the global counts; the last CTA compares the frames (fg_scene_verdict,
+ * framegen.c:103-113: more than half the samples in other bins, i.e. sum |a - b| > sum b) and zeroes the counts for
+ * the next call. */
+#define FG_HIST_SPLIT 8
 __global__ void __launch_bounds__(256) fg_hist_kernel(FgLevel lv, unsigned *__restrict__ hist, int *scene)
 {
     __shared__ unsigned s_h[64];
     __shared__ bool s_last;
-    const int tid = threadIdx.x, s = blockIdx.x, f = blockIdx.y;
+    const int tid = threadIdx.x, s = blockIdx.x % 9, f = blockIdx.x / 9;
     if (tid < 64)
         s_h[tid] = 0;
     __syncthreads();
@@ -105,13 +109,13 @@ __global__ void __launch_bounds__(256) fg_hist_kernel(FgLevel lv, unsigned *__re
     const int x0 = (lv.w * sx / 3) & ~15, x1 = (lv.w * (sx + 1) / 3) & ~15;
     const int y0 = lv.h * sy / 3, y1 = lv.h * (sy + 1) / 3;
     const int cols = x1 - x0, rows = (y1 - y0 + 1) / 2;
-    for (int k = tid; k < cols * rows; k += blockDim.x) {
+    for (int k = (int)blockIdx.y * blockDim.x + tid; k < cols * rows; k += FG_HIST_SPLIT * blockDim.x) {
         const int y = y0 + 2 * (k / cols), x = x0 + k % cols;
         atomicAdd(&s_h[(int)(p[(size_t)y * lv.pitch + x] * (1.0f / 256.0f)) & 63], 1u);
     }
     __syncthreads();
-    if (tid < 64)
-        hist[(f * 9 + s) * 64 + tid] = s_h[tid];
+    if (tid < 64 && s_h[tid])
+        atomicAdd(&hist[(f * 9 + s) * 64 + tid], s_h[tid]);
     __threadfence();
     __syncthreads();
     if (tid == 0)
@@ -125,6 +129,8 @@ __global__ void __launch_bounds__(256) fg_hist_kernel(FgLevel lv, unsigned *__re
         const unsigned a = __ldcg(&hist[i]), b = __ldcg(&hist[9 * 64 + i]);
         diff += a > b ? a - b : b - a;
         total += b;
+        hist[i] = 0;
+        hist[9 * 64 + i] = 0;
     }
 #pragma unroll
     for (int d = 16; d >= 1; d >>= 1) {
@@ -160,10 +166,30 @@ __global__ void __launch_bounds__(32 * FG_WARPS) fg_search_kernel(FgLevel lv, co
     const int wx = want.x, wy = want.y;
     const int lanes = (lv.w + 15) & ~15;
     const int x0 = min(max(px + wx - 8, -32), lanes), y0 = py + wy - 8;
-    for (int k = lane; k < 24 * 24; k += 32)
-        s_win[warp][k / 24][k % 24] = fg_at(lv.a, lv.pitch, lv.w, lv.h, x0 + k % 24, y0 + k / 24);
-    for (int k = lane; k < 64; k += 32)
-        s_blk[warp][k >> 3][k & 7] = fg_at(lv.b, lv.pitch, lv.w, lv.h, px + (k & 7), py + (k >> 3));
+    {
+        /* every load of the window and the block in flight before the first store */
+        float wv[18], bv[2];
+#pragma unroll
+        for (int j = 0; j < 18; j++) {
+            const int k = lane + 32 * j;
+            wv[j] = fg_at(lv.a, lv.pitch, lv.w, lv.h, x0 + k % 24, y0 + k / 24);
+        }
+#pragma unroll
+        for (int j = 0; j < 2; j++) {
+            const int k = lane + 32 * j;
+            bv[j] = fg_at(lv.b, lv.pitch, lv.w, lv.h, px + (k & 7), py + (k >> 3));
+        }
+#pragma unroll
+        for (int j = 0; j < 18; j++) {
+            const int k = lane + 32 * j;
+            s_win[warp][k / 24][k % 24] = wv[j];
+        }
+#pragma unroll
+        for (int j = 0; j < 2; j++) {
+            const int k = lane + 32 * j;
+            s_blk[warp][k >> 3][k & 7] = bv[j];
+        }
+    }
     __syncwarp();
     if (level == 0) {
         /* the estimate's place is the window's centre: (x0 + 8, y0 + 8) */
@@ -275,25 +301,32 @@ __global__ void fg_upscale_kernel(FgLevel lv, short2 *__restrict__ up, int fbw, 
         return;
     }
     const int gx = i % fbw, gy = i / fbw;
-    float best = 0.0f;
-    int vx = 0, vy = 0;
+    /* the four candidates' SADs with all their loads in flight, then the first least */
+    short2 v[4];
+    float sad[4];
+#pragma unroll
     for (int n = 0; n < 4; n++) {
         const int xo = n % 2 - 1 + gx % 2, yo = n / 2 - 1 + gy % 2;
-        const short2 v = lv.fil[min(max(gy / 2 + yo, 0), lv.bh - 1) * lv.bw + min(max(gx / 2 + xo, 0), lv.bw - 1)];
+        v[n] = lv.fil[min(max(gy / 2 + yo, 0), lv.bh - 1) * lv.bw + min(max(gx / 2 + xo, 0), lv.bw - 1)];
+    }
+    float cur[16];
+#pragma unroll
+    for (int k = 0; k < 16; k++)
+        cur[k] = fg_at(lv.b, lv.pitch, lv.w, lv.h, gx * 4 + (k & 3), gy * 4 + (k >> 2));
+#pragma unroll
+    for (int n = 0; n < 4; n++) {
         float s = 0.0f;
 #pragma unroll
-        for (int r = 0; r < 4; r++)
-#pragma unroll
-            for (int c = 0; c < 4; c++)
-                s += fabsf(fg_at(lv.b, lv.pitch, lv.w, lv.h, gx * 4 + c, gy * 4 + r) -
-                           fg_at(lv.a, lv.pitch, lv.w, lv.h, gx * 4 + c + v.x, gy * 4 + r + v.y));
-        if (n == 0 || s < best) {
-            best = s;
-            vx = v.x;
-            vy = v.y;
-        }
+        for (int k = 0; k < 16; k++)
+            s += fabsf(cur[k] - fg_at(lv.a, lv.pitch, lv.w, lv.h, gx * 4 + (k & 3) + v[n].x, gy * 4 + (k >> 2) + v[n].y));
+        sad[n] = s;
     }
-    up[i] = make_short2((short)(2 * vx), (short)(2 * vy));
+    int pick = 0;
+#pragma unroll
+    for (int n = 1; n < 4; n++)
+        if (sad[n] < sad[pick])
+            pick = n;
+    up[i] = make_short2((short)(2 * v[pick].x), (short)(2 * v[pick].y));
 }
 
 /* fg_mid_vectors (framegen.c:292-328) on the finest level: no motion first, favoured by one grey level over the block
@@ -564,7 +597,7 @@ extern "C" int vtg_framegen_run(vtg_framegen *g, const float *older, int older_p
         sh = v.h;
         spa = spb = v.pitch;
     }
-    fg_hist_kernel<<<dim3(9, 2), 256, 0, st>>>(g->L[1], g->hist, g->scene);
+    fg_hist_kernel<<<dim3(18, FG_HIST_SPLIT), 256, 0, st>>>(g->L[1], g->hist, g->scene);
     for (int L = g->levels - 1; L >= 0; L--) {
         const FgLevel &v = g->L[L];
         const int nb = v.bw * v.bh;

@@ -120,7 +120,7 @@ __device__ __forceinline__ void reduce_tile(const void *__restrict__ src_, int s
             const int gy = min(max(sy0 + r, 0), sh - 1), gx = gx0 + 4 * k;
             const float *row = src + (size_t)gy * spitch;
             float4 v;
-            if (gx >= 0 && gx + 4 <= sw)
+            if (vec && gx >= 0 && gx + 4 <= sw) /* vec: the plane and its pitch are 16-byte aligned */
                 v = __ldg(reinterpret_cast<const float4 *>(row + gx));
             else
                 v = make_float4(__ldg(row + min(max(gx, 0), sw - 1)), __ldg(row + min(max(gx + 1, 0), sw - 1)),
@@ -195,7 +195,7 @@ __global__ void __launch_bounds__(256) pyr_reduce_kernel(const void *__restrict_
 {
     __shared__ TileSmem s_t;
     __shared__ __align__(16) int s_v[RT_Y][SF_P];
-    reduce_tile<FROM_U8>(src_, sw, sh, spitch, aligned16(src_, spitch), l0, l0pitch, dst, dw, dh, dpitch,
+    reduce_tile<FROM_U8>(src_, sw, sh, spitch, aligned16(src_, FROM_U8 ? spitch : spitch * 4), l0, l0pitch, dst, dw, dh, dpitch,
                          blockIdx.x * RT_X, blockIdx.y * RT_Y, s_t.b, s_t.f, s_v);
 }
 
@@ -275,5 +275,14 @@ cudaError_t vtg_launch_pyramid(const uint8_t *frame, int stride, int w, int h, f
         sw = dw;
         sh = dh;
     }
+    return cudaGetLastError();
+}
+
+/* One float level from another (the reduce alone): dst = reduce(src), dw x dh = ((sw + 1) / 2, (sh + 1) / 2). */
+cudaError_t vtg_launch_reduce(const float *src, int sw, int sh, int spitch, float *dst, int dpitch, cudaStream_t s)
+{
+    const int dw = (sw + 1) / 2, dh = (sh + 1) / 2;
+    const dim3 grid((dw + RT_X - 1) / RT_X, (dh + RT_Y - 1) / RT_Y);
+    pyr_reduce_kernel<false><<<grid, 256, 0, s>>>(src, sw, sh, spitch, nullptr, 0, dst, dw, dh, dpitch);
     return cudaGetLastError();
 }
