@@ -277,12 +277,3 @@ cudaError_t vtg_launch_pyramid(const uint8_t *frame, int stride, int w, int h, f
     }
     return cudaGetLastError();
 }
-
-/* One float level from another (the reduce alone): dst = reduce(src), dw x dh = ((sw + 1) / 2, (sh + 1) / 2). */
-cudaError_t vtg_launch_reduce(const float *src, int sw, int sh, int spitch, float *dst, int dpitch, cudaStream_t s)
-{
-    const int dw = (sw + 1) / 2, dh = (sh + 1) / 2;
-    const dim3 grid((dw + RT_X - 1) / RT_X, (dh + RT_Y - 1) / RT_Y);
-    pyr_reduce_kernel<false><<<grid, 256, 0, s>>>(src, sw, sh, spitch, nullptr, 0, dst, dw, dh, dpitch);
-    return cudaGetLastError();
-}

@@ -76,7 +76,6 @@ cudaError_t vtg_launch_pyramid(const uint8_t *frame, int stride, int w, int h, f
 cudaError_t vtg_launch_cells(const DevPyr *I, const DevPyr *J, int top, const LkPrm &p, const CellGrid &g, int base_w,
                              int base_h, vtg_lk_out *out, vtg_cell *cells, cudaStream_t s);
 int vtg_pyr_tiles(int w, int h, int level);
-cudaError_t vtg_launch_reduce(const float *src, int sw, int sh, int spitch, float *dst, int dpitch, cudaStream_t s);
 cudaError_t vtg_launch_pyramid_batch(const PyrJob *jobs, const int *starts, const int *tiles_total, int njobs,
                                      int max_levels, cudaStream_t s);
 /* Batched LK over jobs: items of `chunk` cells, job j's items from item_start[j]; `counter` must be 0 at launch. */
