@@ -368,8 +368,12 @@ int vtg_serve_run(vtg_ctx *ctx, const struct vtg_serve_cfg *c, struct vtg_serve_
             batched += m;
             idle = 0;
         }
-        if (idle && next_req < n) {
-            /* nothing to do until the next arrival: a short pause keeps the loop from burning a core */
+        int busy = 0;
+        for (int k = 0; k < c->inflight; k++)
+            busy |= sl[k].busy;
+        if (idle && !busy && next_req < n) {
+            /* nothing on the GPU and nothing to do until the next arrival: a short pause keeps the loop from burning a
+             * core. With a step in flight the loop keeps polling its event, so a completion is seen at once. */
             const double wait = rq[next_req].t_arrive - (now_s() - t0);
             if (wait > 200e-6) {
                 struct timespec ts = {0, 100000};

@@ -59,7 +59,9 @@ def test_framegen_against_reference_fixture(vtg_lib, ctx, golden):
 
 
 @pytest.mark.parametrize("w,h,shift,amp,seed", [(256, 192, (30.0, -22.0), 2.0, 5), (401, 257, (-1.2, 0.4), 0.0, 6),
-                                                (130, 66, (4.5, 7.5), 1.0, 7), (1920, 1080, (-17.0, 12.0), 3.0, 8)])
+                                                (130, 66, (4.5, 7.5), 1.0, 7), (1920, 1080, (-17.0, 12.0), 3.0, 8),
+                                                (64, 64, (10.0, -7.0), 1.0, 9), (128, 96, (40.0, 30.0), 4.0, 10),
+                                                (96, 200, (-45.0, 60.0), 0.0, 11)])
 def test_framegen_against_oracle(vtg_lib, ctx, w, h, shift, amp, seed):
     f0, f1, _, _ = S.warp_pair(w, h, shift, amp, seed=seed)
     r, frame, pic = _run(vtg_lib, ctx, f0, f1)

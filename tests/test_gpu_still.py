@@ -59,7 +59,8 @@ def test_still_decision_on_reference_cells(vtg_lib, ctx, golden):
 
 
 @pytest.mark.parametrize("w,h,frames,avg,px,grey", [(320, 240, 12, 8, 1.0, 4.0), (640, 480, 6, 4, 0.5, 3.0),
-                                                    (200, 121, 5, 16, 2.0, 6.0)])
+                                                    (200, 121, 5, 16, 2.0, 6.0), (32, 32, 4, 1, 1.0, 4.0),
+                                                    (47, 33, 6, 3, 0.0, 0.0)])
 def test_still_gpu_vectors(vtg_lib, ctx, w, h, frames, avg, px, grey):
     seq = S.still_sequence(w, h, frames, seed=21, jump_at=frames - 2, mover=20)
     st = vtg_lib.Still(ctx, w, h, avg, px, grey)
