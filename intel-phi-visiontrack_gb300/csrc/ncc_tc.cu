@@ -3,23 +3,24 @@
  * matrix descriptors, the accumulator read back with tcgen05.ld, scored with exact int64 window sums and reduced to the
  * per-cell map in the epilogue.
  *
- * The correlation as a GEMM. A CTA owns a tile of corners: 1024 consecutive x (X0 + 8 m + s, m < 128, s < 8) by 8
- * consecutive y (Y0 + q, q < 8). Then
+ * The correlation as a GEMM. A CTA owns a tile of corners: 1024 consecutive x (X0 + 8 m + s, m < 128, s < 8) by Q
+ * consecutive y (Y0 + q, q < Q; Q = 4 for templates up to 64 rows, else 8). Then
  *     st(X0 + 8 m + s, Y0 + q) = sum over image rows r, columns c of  A_r[m][c] * B_r[(q, s)][c]
  * with A_r[m][c] = J[r][X0 + 8 m + c] and B_r[(q, s)][c] = t[r - Y0 - q][c - s] (zero outside the template): D =
- * sum_r A_r B_r^T with M = 128, N = 8 x 8 = 64, and K = the tile's 8 + T_h - 1 image rows times K_row = T_w + 8
- * rounded up to 16.
+ * sum_r A_r B_r^T with M = 128, N = 8 Q, and K = the tile's Q + T_h - 1 image rows times K_row = T_w + 8 rounded up
+ * to 16.
  *   A needs no im2col. Consecutive rows of A_r start 8 elements (16 bytes) apart in the image row, so a K-major,
  *   no-swizzle descriptor with 16-byte core-matrix rows, a 16-byte leading (K) offset and a 128-byte stride (M) offset
  *   reads A_r straight from the row: address(m, k) = row + 2 (8 m + k). The picture is converted to 16 bits once per
  *   search (ncc_conv), shifted so that every tile's row segment starts on a 16-byte boundary.
  *   B_r depends only on r - Y0: the band (8 + T_h - 1 blocks of 64 x K_row) is built once per template in the canonical
  *   core-matrix layout.
- * Pipeline: one thread drives it. Six shared-memory stages, each an image-row segment and a band block, arrive by
- * cp.async.bulk on a "full" mbarrier (expected bytes); the MMAs of a stage commit to its "empty" mbarrier, which its
- * next filling waits for, so copies run several stages ahead of the tensor core. Every wait is bounded by the global
- * timer; past it the kernel records an error word.
- * Epilogue: each of the 128 threads owns one accumulator row (8 x-corners by 8 y-corners). Per corner: st = acc -
+ * Pipeline: two threads drive it. Six shared-memory stages, each an image-row segment and a band block, arrive by
+ * cp.async.bulk on a "full" mbarrier (expected bytes). A producer thread (warp 0) fills a stage again as soon as the
+ * MMAs of its last use commit to its "empty" mbarrier; an issuer thread (warp 1) issues each stage's MMAs as soon as
+ * its copies land, so copies run several stages ahead and the tensor core is fed back to back. Every wait is bounded by
+ * the global timer; past it the kernel records an error word.
+ * Epilogue: each of the 128 threads owns one accumulator row (8 x-corners by Q y-corners). Per corner: st = acc -
  * J(x, y) sum t' (the reference's st is relative to the corner's first pixel), times the corner's factor 1 / sqrt(norm
  * var) from ncc_box_prep (0 for a near-blank window: the exact integer rule), the best per 16 x 16 cell by value then scan
  * order, merged across tiles by a 64-bit atomicMax on (ordered score, inverted scan index). */
@@ -29,22 +30,25 @@
 #include "vtg_ncc.cuh"
 
 #define TC_M 128
-#define TC_Q 8
-#define TC_N (8 * TC_Q)
+#define TC_QMAX 8 /* y-corners of a tile, at most */
 #define TC_XS (8 * TC_M) /* x-corners of a tile */
 #define TC_STAGES 6
-#define TC_TMEM_COLS 64
 #define TC_WAIT_NS 2000000000ull /* a wait gives up after 2 s of the global timer */
 #define TC_MAX_KROW 144          /* T_w <= 128 */
 
 static inline int tc_krow(int tw) { return ((tw + 8 + 15) / 16) * 16; }
 
-size_t vtg_ncc_band_bytes(int tw, int th) { return (size_t)(TC_Q + th - 1) * TC_N * tc_krow(tw) * sizeof(uint16_t); }
+/* y-corners of a tile for a template th rows high: 4 (N = 32) gives twice the tiles of 8, so co-resident CTAs overlap
+ * one another's epilogues and MMAs; past 64 rows the band each tile copies grows too long for that to pay. */
+static inline int tc_q(int th) { return th <= 64 ? 4 : 8; }
 
-/* The 16-bit picture: rows up to h + TC_Q + T_h (zeros past the picture), TC_XS-aligned tiles plus the last K row. */
+/* the band at its largest tile height: enough for either */
+size_t vtg_ncc_band_bytes(int tw, int th) { return (size_t)(TC_QMAX + th - 1) * 8 * TC_QMAX * tc_krow(tw) * sizeof(uint16_t); }
+
+/* The 16-bit picture: rows up to h + TC_QMAX + T_h (zeros past the picture), TC_XS-aligned tiles plus the last K row. */
 static inline int conv_pitch(int w) { return ((w + TC_XS - 1) / TC_XS) * TC_XS + TC_MAX_KROW; }
 
-size_t vtg_ncc_conv_elems(int max_w, int max_h, int max_th) { return (size_t)conv_pitch(max_w) * (size_t)(max_h + TC_Q + max_th); }
+size_t vtg_ncc_conv_elems(int max_w, int max_h, int max_th) { return (size_t)conv_pitch(max_w) * (size_t)(max_h + TC_QMAX + max_th); }
 
 /* ---- the band ---- */
 
@@ -60,10 +64,11 @@ __device__ __forceinline__ float from16(uint16_t v, int kind)
 
 /* Band block k (image row Y0 + k of a tile), element (n = 8 q + s, c) at core matrix (c / 8, n / 8), row n % 8, column
  * c % 8: core matrices of 8 x 8 elements (128 bytes), K-chunks of 8 columns N / 8 matrices apart. */
-__global__ void ncc_band_kernel(const float *__restrict__ app, int tw, int th, int kind, int krow, int rows,
+__global__ void ncc_band_kernel(const float *__restrict__ app, int tw, int th, int kind, int krow, int rows, int nq,
                                 uint16_t *__restrict__ band)
 {
-    const size_t per = (size_t)TC_N * krow;
+    const int N = 8 * nq;
+    const size_t per = (size_t)N * krow;
     const size_t total = per * rows;
     for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total; idx += (size_t)gridDim.x * blockDim.x) {
         const int k = (int)(idx / per);
@@ -72,7 +77,7 @@ __global__ void ncc_band_kernel(const float *__restrict__ app, int tw, int th, i
         const int q = n >> 3, s = n & 7;
         const int i = k - q, j = c - s;
         const float v = (i >= 0 && i < th && j >= 0 && j < tw) ? app[i * tw + j] : 0.0f;
-        const size_t off = (size_t)k * per + ((size_t)(c >> 3) * (TC_N / 8) + (n >> 3)) * 64 + (n & 7) * 8 + (c & 7);
+        const size_t off = (size_t)k * per + ((size_t)(c >> 3) * (N / 8) + (n >> 3)) * 64 + (n & 7) * 8 + (c & 7);
         band[off] = to16(v, kind);
     }
 }
@@ -97,10 +102,10 @@ __global__ void ncc_band_sum(const float *__restrict__ app, int count, int kind,
 
 cudaError_t vtg_launch_ncc_band(const float *app, int tw, int th, int kind, uint16_t *band, float *sum_t, cudaStream_t st)
 {
-    const int krow = tc_krow(tw), rows = TC_Q + th - 1;
-    const size_t total = (size_t)TC_N * krow * rows;
+    const int q = tc_q(th), krow = tc_krow(tw), rows = q + th - 1;
+    const size_t total = (size_t)8 * q * krow * rows;
     const int blocks = (int)((total + 255) / 256 < 4096 ? (total + 255) / 256 : 4096);
-    ncc_band_kernel<<<blocks, 256, 0, st>>>(app, tw, th, kind, krow, rows, band);
+    ncc_band_kernel<<<blocks, 256, 0, st>>>(app, tw, th, kind, krow, rows, q, band);
     ncc_band_sum<<<1, 256, 0, st>>>(app, tw * th, kind, sum_t);
     return cudaGetLastError();
 }
@@ -317,17 +322,17 @@ struct TcSmem {
     uint32_t a_bytes, b_bytes, stage_bytes, total;
 };
 
-static TcSmem tc_smem(int krow)
+static TcSmem tc_smem(int krow, int q)
 {
     TcSmem s;
     s.a_bytes = (uint32_t)(((TC_XS + krow) * 2 + 127) & ~127);
-    s.b_bytes = (uint32_t)(TC_N * krow * 2);
+    s.b_bytes = (uint32_t)(8 * q * krow * 2);
     s.stage_bytes = s.a_bytes + s.b_bytes;
     s.total = TC_STAGES * s.stage_bytes + 256; /* + mbarriers and the tensor-memory address */
     return s;
 }
 
-template <int KIND>
+template <int KIND, int Q>
 __global__ void __launch_bounds__(128, 1) ncc_map_tc(const uint8_t *__restrict__ plane, int pitch, NccPrm p,
                                                      const uint16_t *__restrict__ band, int krow, int tiles_x,
                                                      uint32_t a_bytes, uint32_t stage_bytes,
@@ -338,13 +343,13 @@ __global__ void __launch_bounds__(128, 1) ncc_map_tc(const uint8_t *__restrict__
     extern __shared__ __align__(1024) uint8_t smem[];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
-    const int X0 = p.x0 + tx * TC_XS, Y0 = p.y0 + ty * TC_Q;
-    const int nk = TC_Q + p.th - 1;
+    const int X0 = p.x0 + tx * TC_XS, Y0 = p.y0 + ty * Q;
+    const int nk = Q + p.th - 1;
     const int kchunks = krow / 16;
     uint8_t *ctl = smem + TC_STAGES * stage_bytes;
     const uint32_t full0 = smem_u32(ctl), empty0 = full0 + 8 * TC_STAGES;
     uint32_t *tmem_slot = (uint32_t *)(ctl + 16 * TC_STAGES);
-    const uint32_t a_copy = (uint32_t)((TC_XS + krow) * 2), b_copy = (uint32_t)(TC_N * krow * 2);
+    const uint32_t a_copy = (uint32_t)((TC_XS + krow) * 2), b_copy = (uint32_t)((8 * Q) * krow * 2);
 
     if (tid == 0) {
         for (int s = 0; s < TC_STAGES; s++) {
@@ -355,7 +360,7 @@ __global__ void __launch_bounds__(128, 1) ncc_map_tc(const uint8_t *__restrict__
     }
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                     "r"(TC_TMEM_COLS)
+                     "r"((8 * Q))
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -365,19 +370,28 @@ __global__ void __launch_bounds__(128, 1) ncc_map_tc(const uint8_t *__restrict__
     const uint32_t tmem = *tmem_slot;
 
     const int fmt = KIND == VTG_NCC_BF16 ? 1 : 0;
-    const uint32_t idesc = (1u << 4) | ((uint32_t)fmt << 7) | ((uint32_t)fmt << 10) | ((uint32_t)(TC_N >> 3) << 17) |
+    const uint32_t idesc = (1u << 4) | ((uint32_t)fmt << 7) | ((uint32_t)fmt << 10) | ((uint32_t)((8 * Q) >> 3) << 17) |
                            ((uint32_t)(TC_M >> 4) << 24);
     int good = 1;
-    if (tid == 0) {
-        /* conv row r holds picture row r from column p.x0 on: this tile's segment starts at column tx * TC_XS */
-        const uint16_t *arow = conv + (size_t)Y0 * cpitch + (size_t)tx * TC_XS;
-        const int pre = nk < TC_STAGES ? nk : TC_STAGES;
-        for (int k = 0; k < pre; k++) {
-            uint8_t *sa = smem + k * stage_bytes;
-            tc_fill(full0 + 8 * k, smem_u32(sa), arow + (size_t)k * cpitch, a_copy, smem_u32(sa + a_bytes),
-                    band + (size_t)k * TC_N * krow, b_copy);
+    /* conv row r holds picture row r from column p.x0 on: this tile's segment starts at column tx * TC_XS */
+    const uint16_t *arow = conv + (size_t)Y0 * cpitch + (size_t)tx * TC_XS;
+    if (warp == 0 && lane == 0) {
+        /* the producer: stage k % TC_STAGES is filled with image row Y0 + k and band block k once the MMAs of its
+         * previous use have completed (the commit to its empty barrier) */
+        for (int k = 0; k < nk; k++) {
+            const int s = k % TC_STAGES;
+            if (k >= TC_STAGES && !mbar_wait(empty0 + 8 * s, (uint32_t)((k / TC_STAGES - 1) & 1))) {
+                good = 0;
+                break;
+            }
+            uint8_t *sa = smem + s * stage_bytes;
+            tc_fill(full0 + 8 * s, smem_u32(sa), arow + (size_t)k * cpitch, a_copy, smem_u32(sa + a_bytes),
+                    band + (size_t)k * (8 * Q) * krow, b_copy);
         }
-        for (int k = 0; k < nk && good; k++) {
+    } else if (warp == 1 && lane == 0) {
+        /* the MMA issuer: each stage's MMAs as soon as its copies have landed, back to back; a commit frees the stage
+         * for the producer */
+        for (int k = 0; k < nk; k++) {
             const int s = k % TC_STAGES;
             if (!mbar_wait(full0 + 8 * s, (uint32_t)((k / TC_STAGES) & 1))) {
                 good = 0;
@@ -387,22 +401,10 @@ __global__ void __launch_bounds__(128, 1) ncc_map_tc(const uint8_t *__restrict__
             const uint32_t a0 = smem_u32(smem + s * stage_bytes), b0 = a0 + a_bytes;
             for (int kc = 0; kc < kchunks; kc++) {
                 const uint64_t ad = mdesc(a0 + 32 * kc, 16, 128);
-                const uint64_t bd = mdesc(b0 + kc * 2 * (TC_N / 8) * 128, (TC_N / 8) * 128, 128);
+                const uint64_t bd = mdesc(b0 + kc * 2 * ((8 * Q) / 8) * 128, ((8 * Q) / 8) * 128, 128);
                 tc_mma(tmem, ad, bd, idesc, (k | kc) != 0);
             }
             tc_commit(empty0 + 8 * s);
-            /* refill the stage whose MMAs were issued last round with the stage TC_STAGES - 1 ahead of this one */
-            const int kr = k - 1 + TC_STAGES;
-            if (k >= 1 && kr < nk) {
-                const int sp = (k - 1) % TC_STAGES;
-                if (!mbar_wait(empty0 + 8 * sp, (uint32_t)(((k - 1) / TC_STAGES) & 1))) {
-                    good = 0;
-                    break;
-                }
-                uint8_t *sa = smem + sp * stage_bytes;
-                tc_fill(full0 + 8 * sp, smem_u32(sa), arow + (size_t)kr * cpitch, a_copy, smem_u32(sa + a_bytes),
-                        band + (size_t)kr * TC_N * krow, b_copy);
-            }
         }
         /* the last commit covers every MMA */
         if (good) {
@@ -419,11 +421,11 @@ __global__ void __launch_bounds__(128, 1) ncc_map_tc(const uint8_t *__restrict__
         /* epilogue: thread m owns accumulator row m: corners X0 + 8 m + s, Y0 + q */
         const int m = warp * 32 + lane;
         const int per = NCC_CELL / p.step;
-        const int ly0 = (ty & 1) * TC_Q; /* this tile's first row inside its cell row */
+        const int ly0 = (ty % (NCC_CELL / Q)) * Q; /* this tile's first row inside its cell row */
         float best = -2.0f;
         int bkey = 1 << 30;
 #pragma unroll 1
-        for (int c = 0; c < TC_N / 32; c++) {
+        for (int c = 0; c < (8 * Q) / 32; c++) {
             float v[32];
             tc_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(32 * c), v);
 #pragma unroll
@@ -456,7 +458,7 @@ __global__ void __launch_bounds__(128, 1) ncc_map_tc(const uint8_t *__restrict__
     __syncthreads();
     if (warp == 0) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS) : "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((8 * Q)) : "memory");
     }
 }
 
@@ -490,12 +492,12 @@ cudaError_t vtg_launch_ncc_map_tc(const void *plane, int pitch, int elem_bytes, 
     if (elem_bytes != 1 || !s.band || !s.conv || !s.fac || !s.cellw || (kind != VTG_NCC_BF16 && kind != VTG_NCC_FP16) ||
         p.tw > 128)
         return cudaErrorInvalidValue;
-    const int krow = tc_krow(p.tw);
-    const TcSmem sm = tc_smem(krow);
+    const int krow = tc_krow(p.tw), q = tc_q(p.th);
+    const TcSmem sm = tc_smem(krow, q);
     const int fw = p.x1 - p.x0 + 1, fh = p.y1 - p.y0 + 1;
-    const int tiles_x = (fw + TC_XS - 1) / TC_XS, tiles_y = (fh + TC_Q - 1) / TC_Q;
+    const int tiles_x = (fw + TC_XS - 1) / TC_XS, tiles_y = (fh + q - 1) / q;
     const int cpitch = tiles_x * TC_XS + TC_MAX_KROW;
-    const int rows = p.y0 + tiles_y * TC_Q + p.th; /* every row a tile's band reads */
+    const int rows = p.y0 + tiles_y * q + p.th; /* every row a tile's band reads */
     if ((size_t)cpitch * rows > s.conv_elems || (size_t)fw * fh > s.fac_elems)
         return cudaErrorInvalidValue;
     const int cells = p.ccols * p.crows;
@@ -510,21 +512,27 @@ cudaError_t vtg_launch_ncc_map_tc(const void *plane, int pitch, int elem_bytes, 
         ncc_conv<VTG_NCC_FP16><<<cblocks, 256, 0, st>>>((const uint8_t *)plane, pitch, p.w, p.h, p.x0, rows, cpitch, s.conv);
     ncc_box_prep<<<dim3((fw + BP_TX - 1) / BP_TX, (fh + BP_TY - 1) / BP_TY), 256, 0, st>>>((const uint8_t *)plane, pitch,
                                                                                           p, fw, s.fac);
+#define MAP_TC(K, QQ)                                                                                                  \
+    do {                                                                                                               \
+        e = cudaFuncSetAttribute(ncc_map_tc<K, QQ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm.total);       \
+        if (e != cudaSuccess)                                                                                          \
+            return e;                                                                                                  \
+        ncc_map_tc<K, QQ><<<tiles_x * tiles_y, 128, sm.total, st>>>((const uint8_t *)plane, pitch, p, s.band, krow,    \
+                                                                   tiles_x, sm.a_bytes, sm.stage_bytes, s.conv,        \
+                                                                   cpitch, s.fac, fw, s.cellw, s.err);                 \
+    } while (0)
     if (kind == VTG_NCC_BF16) {
-        e = cudaFuncSetAttribute(ncc_map_tc<VTG_NCC_BF16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm.total);
-        if (e != cudaSuccess)
-            return e;
-        ncc_map_tc<VTG_NCC_BF16><<<tiles_x * tiles_y, 128, sm.total, st>>>(
-            (const uint8_t *)plane, pitch, p, s.band, krow, tiles_x, sm.a_bytes, sm.stage_bytes, s.conv, cpitch, s.fac, fw,
-            s.cellw, s.err);
+        if (q == 4)
+            MAP_TC(VTG_NCC_BF16, 4);
+        else
+            MAP_TC(VTG_NCC_BF16, 8);
     } else {
-        e = cudaFuncSetAttribute(ncc_map_tc<VTG_NCC_FP16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm.total);
-        if (e != cudaSuccess)
-            return e;
-        ncc_map_tc<VTG_NCC_FP16><<<tiles_x * tiles_y, 128, sm.total, st>>>(
-            (const uint8_t *)plane, pitch, p, s.band, krow, tiles_x, sm.a_bytes, sm.stage_bytes, s.conv, cpitch, s.fac, fw,
-            s.cellw, s.err);
+        if (q == 4)
+            MAP_TC(VTG_NCC_FP16, 4);
+        else
+            MAP_TC(VTG_NCC_FP16, 8);
     }
+#undef MAP_TC
     ncc_cells_out<<<(cells + 255) / 256, 256, 0, st>>>(p, s.cellw, s.map_v, s.map_x, s.map_y);
     return cudaGetLastError();
 }
