@@ -117,13 +117,24 @@ template <int KIND>
 __global__ void ncc_conv(const uint8_t *__restrict__ plane, int pitch, int w, int h, int x0, int rows, int cpitch,
                          uint16_t *__restrict__ conv)
 {
-    const size_t total = (size_t)rows * cpitch;
-    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total; idx += (size_t)gridDim.x * blockDim.x) {
-        const int r = (int)(idx / cpitch), i = (int)(idx - (size_t)r * cpitch);
-        const int x = x0 + i;
-        const float v = (r < h && x < w) ? (float)__ldg(plane + (size_t)r * pitch + x) : 0.0f;
-        conv[idx] = to16(v, KIND);
+    /* row blockIdx.y, eight elements a thread and one 16-byte store (cpitch is a multiple of 8 and rows start 16-byte
+     * aligned: 2 cpitch = 2048 tiles_x + 288 bytes) */
+    const int r = (int)blockIdx.y, i0 = 8 * (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (r >= rows || i0 >= cpitch)
+        return;
+    uint32_t o[4];
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+        uint32_t pr = 0;
+#pragma unroll
+        for (int f = 0; f < 2; f++) {
+            const int x = x0 + i0 + 2 * e + f;
+            const float v = (r < h && x < w) ? (float)__ldg(plane + (size_t)r * pitch + x) : 0.0f;
+            pr |= (uint32_t)to16(v, KIND) << (16 * f);
+        }
+        o[e] = pr;
     }
+    *reinterpret_cast<uint4 *>(conv + (size_t)r * cpitch + i0) = make_uint4(o[0], o[1], o[2], o[3]);
 }
 
 /* fac[(y - y0) fw + (x - x0)] = 1 / sqrt(norm var) from the corner's exact window sums; 0 for a near-blank window
@@ -504,12 +515,11 @@ cudaError_t vtg_launch_ncc_map_tc(const void *plane, int pitch, int elem_bytes, 
     cudaError_t e = cudaMemsetAsync(s.cellw, 0, sizeof(unsigned long long) * (size_t)cells, st);
     if (e != cudaSuccess)
         return e;
-    const size_t conv_total = (size_t)cpitch * rows;
-    const int cblocks = (int)((conv_total + 255) / 256 < 8192 ? (conv_total + 255) / 256 : 8192);
+    const dim3 cgrid((cpitch / 8 + 255) / 256, rows);
     if (kind == VTG_NCC_BF16)
-        ncc_conv<VTG_NCC_BF16><<<cblocks, 256, 0, st>>>((const uint8_t *)plane, pitch, p.w, p.h, p.x0, rows, cpitch, s.conv);
+        ncc_conv<VTG_NCC_BF16><<<cgrid, 256, 0, st>>>((const uint8_t *)plane, pitch, p.w, p.h, p.x0, rows, cpitch, s.conv);
     else
-        ncc_conv<VTG_NCC_FP16><<<cblocks, 256, 0, st>>>((const uint8_t *)plane, pitch, p.w, p.h, p.x0, rows, cpitch, s.conv);
+        ncc_conv<VTG_NCC_FP16><<<cgrid, 256, 0, st>>>((const uint8_t *)plane, pitch, p.w, p.h, p.x0, rows, cpitch, s.conv);
     ncc_box_prep<<<dim3((fw + BP_TX - 1) / BP_TX, (fh + BP_TY - 1) / BP_TY), 256, 0, st>>>((const uint8_t *)plane, pitch,
                                                                                           p, fw, s.fac);
 #define MAP_TC(K, QQ)                                                                                                  \
