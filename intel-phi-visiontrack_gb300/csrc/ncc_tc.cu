@@ -139,25 +139,27 @@ __global__ void ncc_conv(const uint8_t *__restrict__ plane, int pitch, int w, in
 
 /* fac[(y - y0) fw + (x - x0)] = 1 / sqrt(norm var) from the corner's exact window sums; 0 for a near-blank window
  * (n var <= n norm / 16) or norm <= 0 -- the reference's rule (src/kern/track.c:203-205) on exact integers.
- * The sums come straight from the bytes, a tile of BP_TX x BP_TY corners a CTA, one thread a column of the tile:
+ * The sums come straight from the bytes, a tile of btx x BP_TY corners a CTA (btx = bp_tx(T_w)), one thread a column
+ * of the tile:
  *   - down its column, running sums over the template's T_h rows for the tile's BP_TY corner rows (registers);
  *   - across the columns, each row's prefix sums: a shuffle scan in the warp, the earlier warps' totals added from
  *     shared memory;
  *   - a corner's window sums are then P(x + T_w) - P(x), consecutive lanes on consecutive corners.
  * Bytes keep every window sum in 32 bits (sum J^2 <= 255^2 x 128^2 < 2^31). A row's prefix of J^2 may pass 2^32, so
  * the prefixes are unsigned and wrap: their differences are still exact. n var is formed in 64 bits. */
-#define BP_TX 128
 #define BP_TY 8
+/* corners a CTA across: the most, a multiple of 32, whose columns (+ T_w - 1) fit the CTA's 256 threads */
+static inline int bp_tx(int tw) { return ((257 - tw) / 32) * 32; }
 __global__ void __launch_bounds__(256) ncc_box_prep(const uint8_t *__restrict__ plane, int pitch, NccPrm p, int fw,
-                                                    float *__restrict__ fac)
+                                                    int btx, float *__restrict__ fac)
 {
     __shared__ unsigned P1[BP_TY][257], P2[BP_TY][257]; /* P[r][c]: columns 0 .. c - 1 of row r */
     __shared__ unsigned t1[8][BP_TY], t2[8][BP_TY];     /* each warp's column totals, then the earlier warps' */
     const int fh = p.y1 - p.y0 + 1;
-    const int tx0 = blockIdx.x * BP_TX, ty0 = blockIdx.y * BP_TY;
-    const int nx = min(BP_TX, fw - tx0), ny = min(BP_TY, fh - ty0);
+    const int tx0 = blockIdx.x * btx, ty0 = blockIdx.y * BP_TY;
+    const int nx = min(btx, fw - tx0), ny = min(BP_TY, fh - ty0);
     const int c = threadIdx.x, lane = c & 31, warp = c >> 5;
-    const int ncol = nx + p.tw - 1; /* <= 255 */
+    const int ncol = nx + p.tw - 1; /* <= 256 */
     unsigned a[BP_TY], b[BP_TY];
     if (c < ncol) {
         const uint8_t *col = plane + (size_t)(p.y0 + ty0) * pitch + (p.x0 + tx0 + c);
@@ -224,8 +226,8 @@ __global__ void __launch_bounds__(256) ncc_box_prep(const uint8_t *__restrict__ 
         }
     }
     __syncthreads();
-    for (int q = c; q < BP_TY * BP_TX; q += blockDim.x) {
-        const int r = q / BP_TX, x = q - r * BP_TX;
+    for (int q = c; q < BP_TY * btx; q += blockDim.x) {
+        const int r = q / btx, x = q - r * btx;
         if (r >= ny || x >= nx)
             continue;
         const long long s1 = (long long)(P1[r][x + p.tw] - P1[r][x]), s2 = (long long)(P2[r][x + p.tw] - P2[r][x]);
@@ -520,8 +522,9 @@ cudaError_t vtg_launch_ncc_map_tc(const void *plane, int pitch, int elem_bytes, 
         ncc_conv<VTG_NCC_BF16><<<cgrid, 256, 0, st>>>((const uint8_t *)plane, pitch, p.w, p.h, p.x0, rows, cpitch, s.conv);
     else
         ncc_conv<VTG_NCC_FP16><<<cgrid, 256, 0, st>>>((const uint8_t *)plane, pitch, p.w, p.h, p.x0, rows, cpitch, s.conv);
-    ncc_box_prep<<<dim3((fw + BP_TX - 1) / BP_TX, (fh + BP_TY - 1) / BP_TY), 256, 0, st>>>((const uint8_t *)plane, pitch,
-                                                                                          p, fw, s.fac);
+    const int btx = bp_tx(p.tw);
+    ncc_box_prep<<<dim3((fw + btx - 1) / btx, (fh + BP_TY - 1) / BP_TY), 256, 0, st>>>((const uint8_t *)plane, pitch, p,
+                                                                                      fw, btx, s.fac);
 #define MAP_TC(K, QQ)                                                                                                  \
     do {                                                                                                               \
         e = cudaFuncSetAttribute(ncc_map_tc<K, QQ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm.total);       \
