@@ -562,6 +562,70 @@ def run_detect(args) -> dict:
     return out
 
 
+def run_points(args) -> dict:
+    """The feature list path (OP_LK, track.c:275-292): LK with the forward-backward check for a list of points between
+    a tracker's two pyramid sets (vtg_points), at the tracker's sizes: 128 and 512 features at 640 x 480 (3 levels,
+    the reference's card: 245 us a frame for its feature list, docs/measurements.md:156) and 512 at 1920 x 1080 (4
+    levels).
+    CUDA-event time of one call with its arrays in device memory; flow against the FP64 oracle on the points both call
+    good; the oracle's time (all host cores) beside it."""
+    import torch
+
+    import vtg
+    import vtg_build
+
+    sys.path.insert(0, ORACLE)
+    import oracle as O
+
+    S = __import__("vtg_synth")
+    vtg_build.build()
+    ctx = vtg.Context(0)
+    L = vtg.lib()
+    cores = os.cpu_count() or 1
+    out = {"metric": "feature-list LK ms a call (21x21, <=10 iterations, flowback 0.5)", "unit": "ms",
+           "higher_is_better": False, "results": []}
+    for w, h, levels, n in ((640, 480, 3, 128), (640, 480, 3, 512), (1920, 1080, 4, 512)):
+        f0, f1, _, _ = S.warp_pair(w, h, (3.2, -1.7), 0.5, seed=5)
+        t = vtg.Tracker(ctx, vtg.config(w, h, levels=levels, fb_max=0.5))
+        t.build(0, f0)
+        t.build(1, f1)
+        t.sync()
+        u = S.uniform(5, 77, 2 * n)
+        xs = (20.0 + u[:n] * (w - 40)).astype(np.float32)
+        ys = (20.0 + u[n:] * (h - 40)).astype(np.float32)
+        dx = torch.from_numpy(xs).cuda()
+        dy = torch.from_numpy(ys).cuda()
+        dout = torch.zeros(n * 32, dtype=torch.uint8, device="cuda")
+        torch.cuda.synchronize()
+        stream = torch.cuda.ExternalStream(t.stream)
+        for _ in range(3):
+            vtg.check(L.vtg_points(t.h, 0, 1, -1, n, dx.data_ptr(), dy.data_ptr(), None, None, dout.data_ptr(),
+                                   vtg.DEVICE, None), "vtg_points")
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(20)]
+        for e0, e1 in ev:
+            e0.record(stream)
+            L.vtg_points(t.h, 0, 1, -1, n, dx.data_ptr(), dy.data_ptr(), None, None, dout.data_ptr(), vtg.DEVICE,
+                         None)
+            e1.record(stream)
+        torch.cuda.synchronize()
+        ms = float(np.median([e0.elapsed_time(e1) for e0, e1 in ev]))
+        got = dout.cpu().numpy().view(vtg.LK_OUT_DTYPE)
+        I, J = O.pyramid(f0, levels), O.pyramid(f1, levels)
+        t0 = time.perf_counter()
+        ref = O.lk_points(I, J, levels - 1, O.lk_cfg(21, 21, 10, 0.01, 0.1, 25.0), xs, ys, max_fb=0.5, mode=O.F64,
+                          threads=cores)
+        cpu_ms = 1e3 * (time.perf_counter() - t0)
+        both = (got["status"] == 0) & (ref["status"] == 0)
+        err = float(np.max(np.maximum(np.abs(got["x"] - ref["x"]), np.abs(got["y"] - ref["y"]))[both])) if both.any() else None
+        out["results"].append({"frame": "%dx%d" % (w, h), "levels": levels, "points": n, "ms": ms,
+                               "status_agreement": float(np.mean(got["status"] == ref["status"])),
+                               "max_err_px": err, "cpu_oracle_ms": cpu_ms, "cpu_cores": cores,
+                               "reference_card_us": 245 if w == 640 else None})
+        t.close()
+    ctx.close()
+    return out
+
+
 def run_still(args) -> dict:
     """The still picture (still_vectors, still_decide, still_update, still_finish) a frame, on a 12-frame sequence at
     level 1 of a 1080p camera (960 x 540, 4,080 cells) and at native 1080p (16,200 cells): CUDA-event time of a whole
@@ -771,6 +835,8 @@ def main():
     ap.add_argument("--detect", action="store_true", help="corner detection on a 1080p plane: a 384 x 307 box, the frame")
     ap.add_argument("--framegen", action="store_true",
                     help="frame generation at 640 x 480, 1280 x 720 and 1920 x 1080 (motion field, middle vectors, blend)")
+    ap.add_argument("--points", action="store_true",
+                    help="the feature-list LK path: 128 and 512 points at 640 x 480, 512 at 1920 x 1080")
     ap.add_argument("--still", action="store_true",
                     help="the still picture a frame at 960 x 540 and 1920 x 1080 (vectors, decision, running mean)")
     ap.add_argument("--profile", default=None, choices=["batch", "ncc", "detect", "still", "framegen"],
@@ -788,6 +854,9 @@ def main():
         return
     if args.still:
         print(json.dumps(run_still(args)))
+        return
+    if args.points:
+        print(json.dumps(run_points(args)))
         return
     if args.framegen:
         print(json.dumps(run_framegen(args)))
