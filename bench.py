@@ -626,6 +626,57 @@ def run_points(args) -> dict:
     return out
 
 
+def run_build(args) -> dict:
+    """tk_build with its optional input steps (track.c:584-629): the pyramid of one 8-bit frame from device memory
+    (vtg_build) with neither, the contrast stretch, the 5 x 5 binomial, or both, at 640 x 480 (3 levels), 1280 x 720
+    and 1920 x 1080 (4 levels). CUDA-event time of one call; every level checked against the oracle; the oracle's own
+    time (one host thread) beside it. Algorithmic bytes: the frame read once and every level written once (F32), plus
+    level 0 read once more by the reduce when an input step made it."""
+    import torch
+
+    import vtg
+    import vtg_build
+
+    sys.path.insert(0, ORACLE)
+    import oracle as O
+
+    S = __import__("vtg_synth")
+    vtg_build.build()
+    ctx = vtg.Context(0)
+    L = vtg.lib()
+    out = {"metric": "tk_build ms a frame (pyramid with the optional input steps)", "unit": "ms",
+           "higher_is_better": False, "results": []}
+    for w, h, levels in ((640, 480, 3), (1280, 720, 4), (1920, 1080, 4)):
+        f = S.build_frame("low", w, h, 11)
+        d = torch.from_numpy(f).cuda()
+        torch.cuda.synchronize()
+        t = vtg.Tracker(ctx, vtg.config(w, h, levels=levels))
+        stream = torch.cuda.ExternalStream(t.stream)
+        for opts, name in ((0, "plain"), (1, "contrast"), (2, "pre_gauss"), (3, "contrast+pre_gauss")):
+            t.set_build(opts)
+            for _ in range(3):
+                vtg.check(L.vtg_build(t.h, 0, d.data_ptr(), w, vtg.DEVICE, None), "vtg_build")
+            ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(20)]
+            for e0, e1 in ev:
+                e0.record(stream)
+                L.vtg_build(t.h, 0, d.data_ptr(), w, vtg.DEVICE, None)
+                e1.record(stream)
+            torch.cuda.synchronize()
+            ms = float(np.median([e0.elapsed_time(e1) for e0, e1 in ev]))
+            t0 = time.perf_counter()
+            want = O.pyramid(f, levels, opts)
+            cpu_ms = 1e3 * (time.perf_counter() - t0)
+            exact = all(np.array_equal(t.level(0, k), want[k]) for k in range(levels))
+            dims = O.level_dims(w, h, levels)
+            nbytes = w * h + 4 * sum(a * b for a, b in dims) + (4 * w * h if opts else 0)
+            out["results"].append({"frame": "%dx%d" % (w, h), "levels": levels, "steps": name, "ms": ms,
+                                   "gbs": nbytes / (ms * 1e-3) / 1e9, "bit_exact": exact, "cpu_oracle_ms": cpu_ms,
+                                   "cpu_cores": 1})
+        t.close()
+    ctx.close()
+    return out
+
+
 def run_still(args) -> dict:
     """The still picture (still_vectors, still_decide, still_update, still_finish) a frame, on a 12-frame sequence at
     level 1 of a 1080p camera (960 x 540, 4,080 cells) and at native 1080p (16,200 cells): CUDA-event time of a whole
@@ -837,6 +888,8 @@ def main():
                     help="frame generation at 640 x 480, 1280 x 720 and 1920 x 1080 (motion field, middle vectors, blend)")
     ap.add_argument("--points", action="store_true",
                     help="the feature-list LK path: 128 and 512 points at 640 x 480, 512 at 1920 x 1080")
+    ap.add_argument("--build", action="store_true",
+                    help="tk_build's pyramid with and without its optional input steps at 640 x 480, 720p and 1080p")
     ap.add_argument("--still", action="store_true",
                     help="the still picture a frame at 960 x 540 and 1920 x 1080 (vectors, decision, running mean)")
     ap.add_argument("--profile", default=None, choices=["batch", "ncc", "detect", "still", "framegen"],
@@ -857,6 +910,9 @@ def main():
         return
     if args.points:
         print(json.dumps(run_points(args)))
+        return
+    if args.build:
+        print(json.dumps(run_build(args)))
         return
     if args.framegen:
         print(json.dumps(run_framegen(args)))

@@ -107,8 +107,26 @@ void *vtg_tracker_stream(const vtg_tracker *t);
 /* The pyramid of one 8-bit frame into set `set` (tk_build, src/kern/track.c:584-629: img_u8_to_q6 + img_reduce per
  * level, src/kern/img_ref.c:32-40 / 98-114). Levels hold the reference's Q6 values (byte x 64, then the 5 x 5 binomial
  * with (h + 128) >> 8) bit for bit. frame: height rows of width bytes, `stride` bytes apart, in host (pinned or
- * pageable) or device memory as `where` says. Asynchronous on `stream` (NULL: the tracker's). */
+ * pageable) or device memory as `where` says. Asynchronous on `stream` (NULL: the tracker's). The build options below
+ * change level 0 first, as tk_build's do. */
 int vtg_build(vtg_tracker *t, int set, const uint8_t *frame, int stride, int where, void *stream);
+
+/* tk_build's optional steps on the input frame: struct vt_config's contrast and pre_gauss
+ * (src/common/vt_proto.h:89-90), switched per frame by the VT_SC_CONTRAST / VT_SC_PRE_GAUSS keys
+ * (src/kern/track.c:586-589). In the reference's order (track.c:600-622):
+ *   - VTG_BUILD_CONTRAST: the frame's Q6 min .. max stretched onto 0 .. 16320 (img_minmax + img_norm,
+ *     src/kern/img_ref.c:42-71), with vtg_contrast_gain's gain and offset;
+ *   - VTG_BUILD_PRE_GAUSS: then the 5 x 5 binomial with (h + 128) >> 8 (img_gauss5, img_ref.c:83-96).
+ * Level 0 is the result and the levels above reduce from it, bit for bit as the reference. The flags apply to the
+ * tracker's later vtg_build calls and batch steps. */
+#define VTG_BUILD_CONTRAST 1
+#define VTG_BUILD_PRE_GAUSS 2
+int vtg_tracker_set_build(vtg_tracker *t, int flags);
+int vtg_tracker_build_flags(const vtg_tracker *t);
+/* The stretch's gain_offset[0..1] for a frame whose Q6 minimum and maximum are lo and hi (whole numbers,
+ * 0 <= lo <= hi < 2^24), as tk_build forms them in x87 extended precision (track.c:603-614): gain = 16320 / (hi - lo)
+ * (1 when hi == lo), offset = -lo x gain, each rounded to F32 from the extended value. */
+int vtg_contrast_gain(int lo, int hi, float *gain_offset);
 
 /* Per-cell flow from set `prev` to set `cur` (still_vectors, src/kern/still.c:116-141, with the tracker's LK settings):
  * one LK vector per cell centre, the forward-backward check when fb_max > 0, and the cell record. `cells` (may be

@@ -1,8 +1,9 @@
 /* vtg_compat.h -- libvtg behind the reference's own kernel signatures.
  *
  * The reference reaches its hot path through kernel pairs of identical signatures, picked per frame by
- * enum vt_algorithm: img_u8_to_q6_{ref,vx}, img_reduce_{ref,vx}, lk_track_{ref,vx}, lk_flowback_{ref,vx},
- * lk_tile_bytes, still_vectors and tk_correlate (src/kern/img.h:17-33, src/kern/lk.h:42-53, src/kern/still.h:37,
+ * enum vt_algorithm: img_u8_to_q6_{ref,vx}, img_reduce_{ref,vx} (with img_norm, img_minmax and img_gauss5 for
+ * tk_build's optional steps, and img_sobel / img_absdiff beside them), lk_track_{ref,vx}, lk_flowback_{ref,vx},
+ * lk_tile_bytes, still_vectors and tk_correlate (src/kern/img.h:17-45, src/kern/lk.h:42-53, src/kern/still.h:37,
  * src/kern/track.h:59; the pick: src/kern/track.c:214, src/common/vt_proto.h:156). The functions here are the third
  * member of each pair, with a _cuda suffix: the same arguments with the same meaning, computed on the GPU. A
  * VT_ALG_CUDA branch calls them where the reference calls its _vx kernels today.
@@ -60,6 +61,25 @@ void img_u8_to_q6_cuda(const struct vtg_ref_plane *dst, const uint8_t *src, int 
 /* img_reduce_ref / _vx (src/kern/img.h:30-33, img_ref.c:98-114): rows y0 .. y1 - 1 of dst, which is
  * (src->w + 1) / 2 x (src->h + 1) / 2, from the 5 x 5 binomial of src at every second pixel, (h + 128) >> 8. */
 void img_reduce_cuda(const struct vtg_ref_plane *dst, const struct vtg_ref_plane *src, int y0, int y1);
+
+/* The rest of img.h's kernels, which tk_build's optional steps (src/kern/track.c:600-622) and the M1 gate
+ * (src/card/m1_gate.c:182-210) run. dst and src have the same size; rows y0 .. y1 - 1 are written. Planes hold whole
+ * numbers, as every plane of the reference does. */
+/* img_norm_ref / _vx (img.h:20-22, img_ref.c:42-55): dst = clamp(rint(src x gain_offset[0] + gain_offset[1]),
+ * 0, 16320), rounded once from the exact value as img_norm_vx does (img_norm_ref's x87 sum rounds the same value
+ * whenever that sum is exact, as it is for tk_build's gains). */
+void img_norm_cuda(const struct vtg_ref_plane *dst, const struct vtg_ref_plane *src, const float *gain_offset, int y0,
+                   int y1);
+/* img_minmax_ref / _vx (img.h:24-26, img_ref.c:57-71): out[0] = min, out[1] = max over rows y0 .. y1 - 1. */
+void img_minmax_cuda(const struct vtg_ref_plane *src, float *out, int y0, int y1);
+/* img_gauss5_ref / _vx (img.h:28-30, img_ref.c:83-96): the 5 x 5 binomial at every pixel, (h + 128) >> 8. */
+void img_gauss5_cuda(const struct vtg_ref_plane *dst, const struct vtg_ref_plane *src, int y0, int y1);
+/* img_sobel_ref / _vx (img.h:40-41, img_ref.c:116-127): the 3 x 3 Sobel x into ix, y into iy. */
+void img_sobel_cuda(const struct vtg_ref_plane *ix, const struct vtg_ref_plane *iy, const struct vtg_ref_plane *src,
+                    int y0, int y1);
+/* img_absdiff_ref / _vx (img.h:44-45, img_ref.c:129-137): dst = |a - b|. */
+void img_absdiff_cuda(const struct vtg_ref_plane *dst, const struct vtg_ref_plane *a, const struct vtg_ref_plane *b,
+                      int y0, int y1);
 
 /* lk_track_ref / _vx (src/kern/lk.h:45-47): tracks (x, y) from pyramid I to pyramid J (planes I[0 .. top],
  * J[0 .. top]), starting at level top with guess (gx, gy) in level-0 pixels. `tile` is not used. */

@@ -173,7 +173,7 @@ static int check_config(const vtg_config *c)
 
 struct Layout {
     int lw[VTG_MAX_LEVELS], lh[VTG_MAX_LEVELS], lpitch[VTG_MAX_LEVELS];
-    size_t loff[VTG_MAX_LEVELS], set_floats, staging_off, desc_off, lk_off, cells_off, bytes;
+    size_t loff[VTG_MAX_LEVELS], set_floats, staging_off, desc_off, lk_off, cells_off, mm_off, bytes;
     int cols, rows;
 };
 
@@ -207,6 +207,8 @@ static void layout(const vtg_config *c, Layout *L)
     b += up256(n * sizeof(vtg_lk_out));
     L->cells_off = b;
     b += up256(n * sizeof(vtg_cell));
+    L->mm_off = b;
+    b += up256(2 * VTG_MM_WORDS * sizeof(uint32_t)); /* one block a set, like the staging */
     L->bytes = b;
 }
 
@@ -296,10 +298,14 @@ extern "C" int vtg_tracker_create(vtg_ctx *ctx, const vtg_config *cfg, vtg_track
     t->desc = (DevPyr *)(t->mem + L.desc_off);
     t->d_lk = (vtg_lk_out *)(t->mem + L.lk_off);
     t->d_cells = (vtg_cell *)(t->mem + L.cells_off);
+    t->d_mm = (uint32_t *)(t->mem + L.mm_off);
+    t->build_opts = 0;
     DevPyr d[4] = {pyr_from(t, 0, 0), pyr_from(t, 0, (int)cfg->flow_level), pyr_from(t, 1, 0),
                    pyr_from(t, 1, (int)cfg->flow_level)};
     /* Pyramid planes start zeroed, as the reference's do (track.c:493-503). */
     e = cudaMemsetAsync(t->mem, 0, 2 * L.set_floats * sizeof(float), t->stream);
+    if (e == cudaSuccess) /* the build options' ticket starts at 0 */
+        e = cudaMemsetAsync(t->d_mm, 0, 2 * VTG_MM_WORDS * sizeof(uint32_t), t->stream);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(t->desc, d, sizeof d, cudaMemcpyHostToDevice, t->stream);
     if (e == cudaSuccess)
@@ -394,9 +400,20 @@ extern "C" int vtg_build(vtg_tracker *t, int set, const uint8_t *frame, int stri
     float *lv[VTG_MAX_LEVELS];
     for (int i = 0; i < t->levels; i++)
         lv[i] = t->sets[set] + t->loff[i];
-    CU(vtg_launch_pyramid(src, sstride, w, h, lv, t->lpitch, t->levels, s));
+    CU(vtg_launch_pyramid_opts(src, sstride, w, h, lv, t->lpitch, t->levels, t->build_opts,
+                               t->d_mm + (size_t)set * VTG_MM_WORDS, s));
     return VTG_OK;
 }
+
+extern "C" int vtg_tracker_set_build(vtg_tracker *t, int flags)
+{
+    if (!t || (flags & ~(VTG_BUILD_CONTRAST | VTG_BUILD_PRE_GAUSS)))
+        return VTG_EINVAL;
+    t->build_opts = flags;
+    return VTG_OK;
+}
+
+extern "C" int vtg_tracker_build_flags(const vtg_tracker *t) { return t ? t->build_opts : 0; }
 
 extern "C" int vtg_cells(vtg_tracker *t, int prev, int cur, vtg_cell *cells, vtg_lk_out *lk, int where, void *stream)
 {

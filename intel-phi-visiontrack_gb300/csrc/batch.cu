@@ -42,6 +42,15 @@ struct BatchSlot {
     std::vector<uint8_t *> h_dst;
     std::vector<int> h_stride, h_w, h_h;
     std::string key; /* the size mix, for the tuning cache */
+    /* frames under build options: their level 0 is made by launches of their own before the batched pyramid */
+    struct Input {
+        const uint8_t *src;
+        int stride, w, h, opts;
+        uint32_t *mm;
+        float *l0;
+        int pitch0;
+    };
+    std::vector<Input> inputs;
     cudaGraphExec_t graph;
     bool has_graph;
 };
@@ -176,6 +185,7 @@ extern "C" int vtg_batch_prepare(vtg_batch *b, int slot, int n, vtg_tracker *con
     sl.h_stride.clear();
     sl.h_w.clear();
     sl.h_h.clear();
+    sl.inputs.clear();
     int max_levels = 1;
     std::vector<std::string> keys;
     for (int j = 0; j < n; j++) {
@@ -209,6 +219,10 @@ extern "C" int vtg_batch_prepare(vtg_batch *b, int slot, int n, vtg_tracker *con
         p.w = w;
         p.h = h;
         p.levels = t->levels;
+        p.opts = t->build_opts;
+        if (p.opts)
+            sl.inputs.push_back({p.src, p.stride, w, h, p.opts, t->d_mm + (size_t)cur * VTG_MM_WORDS,
+                                 t->sets[cur] + t->loff[0], t->lpitch[0]});
         for (int L = 0; L < VTG_MAX_LEVELS; L++) {
             p.lv[L] = L < t->levels ? t->sets[cur] + t->loff[L] : nullptr;
             p.pitch[L] = t->lpitch[L];
@@ -290,6 +304,8 @@ static int launch_slot(vtg_batch *b, BatchSlot &sl, cudaStream_t s, int nwait = 
     /* the uploads went to each frame's own set's staging buffer; the kernels reuse pyramid sets and result buffers */
     for (int k = 0; k < nwait; k++)
         CU(cudaStreamWaitEvent(s, (cudaEvent_t)wait[k], 0));
+    for (const BatchSlot::Input &in : sl.inputs)
+        CU(vtg_launch_build_input(in.src, in.stride, in.w, in.h, in.opts, in.mm, in.l0, in.pitch0, s));
     CU(vtg_launch_pyramid_batch(sl.d_pyr, sl.d_tiles, sl.tiles, sl.njobs, sl.max_levels, s));
     CU(cudaMemsetAsync(sl.d_counter, 0, sizeof(int), s));
     LkTune t = b->tune;
@@ -514,6 +530,8 @@ extern "C" int vtg_batch_profile(vtg_batch *b, int slot, int reps, float *pyr_ms
         for (size_t k = 0; k < sl.h_src.size(); k++)
             CU(cudaMemcpy2DAsync(sl.h_dst[k], (size_t)sl.h_w[k], sl.h_src[k], (size_t)sl.h_stride[k], (size_t)sl.h_w[k],
                                  (size_t)sl.h_h[k], cudaMemcpyHostToDevice, b->stream));
+        for (const BatchSlot::Input &in : sl.inputs)
+            CU(vtg_launch_build_input(in.src, in.stride, in.w, in.h, in.opts, in.mm, in.l0, in.pitch0, b->stream));
         CU(vtg_launch_pyramid_batch(sl.d_pyr, sl.d_tiles, sl.tiles, sl.njobs, sl.max_levels, b->stream));
         CU(cudaMemsetAsync(sl.d_counter, 0, sizeof(int), b->stream));
         CU(cudaEventRecord(e[1], b->stream));

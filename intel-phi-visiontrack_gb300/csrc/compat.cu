@@ -310,6 +310,222 @@ extern "C" void img_reduce_cuda(const struct vtg_ref_plane *dst, const struct vt
     }();
 }
 
+namespace {
+
+/* The same-size image kernels of img.h, on rows [y0, y0 + rows) of a w x h plane. Sources a and b point at their row
+ * srow0, `spitch` floats a row; rows and columns past the plane are clamped (the reference's replicated border). */
+enum { IMG_NORM, IMG_GAUSS5, IMG_SOBEL, IMG_ABSDIFF };
+
+template <int OP>
+__global__ void img_rows_kernel(const float *__restrict__ a, int apitch, const float *__restrict__ b, int bpitch, int w,
+                                int h, int srow0, int y0, int rows, float gain, float offset, float *__restrict__ d1,
+                                float *__restrict__ d2, int dpitch)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, r = blockIdx.y, y = y0 + r;
+    if (x >= w || r >= rows)
+        return;
+    auto A = [&](int yy, int xx) {
+        return a[(size_t)(min(max(yy, 0), h - 1) - srow0) * apitch + min(max(xx, 0), w - 1)];
+    };
+    float *o1 = d1 + (size_t)r * dpitch + x;
+    if (OP == IMG_NORM) {
+        /* img_norm_vx (img_vx.c:49-59): one rounding of the exact value; img_norm_ref's x87 form rounds the same value
+         * whenever its extended sum is exact */
+        const float v = rintf(__fmaf_rn(A(y, x), gain, offset));
+        *o1 = fminf(fmaxf(v, 0.0f), 16320.0f);
+    } else if (OP == IMG_GAUSS5) {
+        /* img_gauss5_ref (img_ref.c:73-96) in its F32 order: vert5 per column, then the horizontal taps, shift8 */
+        float v[5];
+#pragma unroll
+        for (int k = 0; k < 5; k++) {
+            const int c = x + k - 2;
+            v[k] = A(y - 2, c) + A(y + 2, c) + 4.0f * (A(y - 1, c) + A(y + 1, c)) + 6.0f * A(y, c);
+        }
+        const float hs = v[0] + v[4] + 4.0f * (v[1] + v[3]) + 6.0f * v[2];
+        *o1 = (float)((__float2int_rn(hs) + 128) >> 8);
+    } else if (OP == IMG_SOBEL) {
+        /* img_sobel_ref (img_ref.c:116-127) */
+        const float pa = A(y - 1, x - 1), pb = A(y - 1, x), pc = A(y - 1, x + 1), pe = A(y, x - 1), pg = A(y, x + 1),
+                    pm = A(y + 1, x - 1), pn = A(y + 1, x), po = A(y + 1, x + 1);
+        *o1 = (pc + 2.0f * pg + po) - (pa + 2.0f * pe + pm);
+        d2[(size_t)r * dpitch + x] = (pm + 2.0f * pn + po) - (pa + 2.0f * pb + pc);
+    } else {
+        /* img_absdiff_ref (img_ref.c:129-137) */
+        *o1 = fabsf(A(y, x) - b[(size_t)(y - srow0) * bpitch + x]);
+    }
+}
+
+/* Min and max over rows [y0, y1) of a plane (img_minmax_ref, img_ref.c:57-71), one CTA: out[0..1]. */
+__global__ void __launch_bounds__(1024) img_minmax_kernel(const float *__restrict__ a, int pitch, int w, int rows,
+                                                          float *__restrict__ out)
+{
+    __shared__ float s_mn[32], s_mx[32];
+    float mn = a[0], mx = mn;
+    for (int r = 0; r < rows; r++)
+        for (int x = threadIdx.x; x < w; x += blockDim.x) {
+            const float v = a[(size_t)r * pitch + x];
+            mn = fminf(mn, v);
+            mx = fmaxf(mx, v);
+        }
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1) {
+        mn = fminf(mn, __shfl_xor_sync(VTG_FULL, mn, s));
+        mx = fmaxf(mx, __shfl_xor_sync(VTG_FULL, mx, s));
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) {
+        s_mn[warp] = mn;
+        s_mx[warp] = mx;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        mn = lane < (int)(blockDim.x >> 5) ? s_mn[lane] : s_mn[0];
+        mx = lane < (int)(blockDim.x >> 5) ? s_mx[lane] : s_mx[0];
+#pragma unroll
+        for (int s = 16; s > 0; s >>= 1) {
+            mn = fminf(mn, __shfl_xor_sync(VTG_FULL, mn, s));
+            mx = fmaxf(mx, __shfl_xor_sync(VTG_FULL, mx, s));
+        }
+        if (lane == 0) {
+            out[0] = mn;
+            out[1] = mx;
+        }
+    }
+}
+
+/* Stages rows [r0, r1] of a plane in device memory (or uses it in place): the rows' device address and pitch. */
+int stage_rows(const vtg_ref_plane *pl, int r0, int r1, char *base, size_t *off, const float **out, int *pitch)
+{
+    if (on_device(pl->p)) {
+        *out = pl->p + (size_t)r0 * pl->stride;
+        *pitch = pl->stride;
+        return VTG_OK;
+    }
+    float *d = (float *)(base + *off);
+    *off += up256((size_t)pl->w * (size_t)(r1 - r0 + 1) * sizeof(float));
+    TRY(cudaMemcpy2DAsync(d, (size_t)pl->w * sizeof(float), pl->p + (size_t)r0 * pl->stride,
+                          (size_t)pl->stride * sizeof(float), (size_t)pl->w * sizeof(float), (size_t)(r1 - r0 + 1),
+                          cudaMemcpyHostToDevice, g_c.stream));
+    *out = d;
+    *pitch = pl->w;
+    return VTG_OK;
+}
+
+/* Rows y0 .. y1 - 1 of d1 (and d2) from a (and b) by kernel OP, a's rows read `halo` rows each side. */
+template <int OP>
+int img_rows(const vtg_ref_plane *d1, const vtg_ref_plane *d2, const vtg_ref_plane *a, const vtg_ref_plane *b, int halo,
+             float gain, float offset, int y0, int y1)
+{
+    if (!plane_ok(d1) || !plane_ok(a) || a->w != d1->w || a->h != d1->h || y0 < 0 || y1 > d1->h)
+        return VTG_EINVAL;
+    if ((d2 && (!plane_ok(d2) || d2->w != d1->w || d2->h != d1->h)) || (OP == IMG_SOBEL && !d2))
+        return VTG_EINVAL;
+    if ((b && (!plane_ok(b) || b->w != d1->w || b->h != d1->h)) || (OP == IMG_ABSDIFF && !b))
+        return VTG_EINVAL;
+    if (y0 >= y1)
+        return VTG_OK;
+    int rc = ready();
+    if (rc != VTG_OK)
+        return rc;
+    const int w = d1->w, rows = y1 - y0;
+    const int s0 = max(y0 - halo, 0), s1 = min(y1 - 1 + halo, a->h - 1);
+    const size_t rows_bytes = up256((size_t)w * (size_t)(s1 - s0 + 1) * sizeof(float));
+    const size_t out_bytes = up256((size_t)w * (size_t)rows * sizeof(float));
+    char *base = nullptr;
+    if ((rc = scratch(2 * rows_bytes + 2 * out_bytes, &base)) != VTG_OK)
+        return rc;
+    size_t off = 0;
+    const float *pa = nullptr, *pb = nullptr;
+    int apitch = 0, bpitch = 0;
+    if ((rc = stage_rows(a, s0, s1, base, &off, &pa, &apitch)) != VTG_OK)
+        return rc;
+    if (b && (rc = stage_rows(b, s0, s1, base, &off, &pb, &bpitch)) != VTG_OK)
+        return rc;
+    const vtg_ref_plane *dst[2] = {d1, d2};
+    float *dd[2] = {nullptr, nullptr};
+    int dpitch = w;
+    const bool in_place = on_device(d1->p) && (!d2 || (on_device(d2->p) && d2->stride == d1->stride));
+    for (int k = 0; k < 2; k++) {
+        if (!dst[k])
+            continue;
+        if (in_place) {
+            dd[k] = dst[k]->p + (size_t)y0 * dst[k]->stride;
+            dpitch = dst[k]->stride;
+        } else {
+            dd[k] = (float *)(base + off);
+            off += out_bytes;
+        }
+    }
+    img_rows_kernel<OP><<<dim3((w + 127) / 128, rows), 128, 0, g_c.stream>>>(pa, apitch, pb, bpitch, w, a->h, s0, y0,
+                                                                             rows, gain, offset, dd[0], dd[1], dpitch);
+    TRY(cudaGetLastError());
+    if (!in_place)
+        for (int k = 0; k < 2; k++)
+            if (dst[k])
+                TRY(cudaMemcpy2DAsync(dst[k]->p + (size_t)y0 * dst[k]->stride, (size_t)dst[k]->stride * sizeof(float),
+                                      dd[k], (size_t)w * sizeof(float), (size_t)w * sizeof(float), (size_t)rows,
+                                      on_device(dst[k]->p) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                                      g_c.stream));
+    TRY(cudaStreamSynchronize(g_c.stream));
+    return VTG_OK;
+}
+
+} // namespace
+
+extern "C" void img_norm_cuda(const struct vtg_ref_plane *dst, const struct vtg_ref_plane *src,
+                              const float *gain_offset, int y0, int y1)
+{
+    std::lock_guard<std::mutex> g(g_c.mu);
+    t_status = gain_offset ? img_rows<IMG_NORM>(dst, nullptr, src, nullptr, 0, gain_offset[0], gain_offset[1], y0, y1)
+                           : VTG_EINVAL;
+}
+
+extern "C" void img_gauss5_cuda(const struct vtg_ref_plane *dst, const struct vtg_ref_plane *src, int y0, int y1)
+{
+    std::lock_guard<std::mutex> g(g_c.mu);
+    t_status = img_rows<IMG_GAUSS5>(dst, nullptr, src, nullptr, 2, 0.0f, 0.0f, y0, y1);
+}
+
+extern "C" void img_sobel_cuda(const struct vtg_ref_plane *ix, const struct vtg_ref_plane *iy,
+                               const struct vtg_ref_plane *src, int y0, int y1)
+{
+    std::lock_guard<std::mutex> g(g_c.mu);
+    t_status = img_rows<IMG_SOBEL>(ix, iy, src, nullptr, 1, 0.0f, 0.0f, y0, y1);
+}
+
+extern "C" void img_absdiff_cuda(const struct vtg_ref_plane *dst, const struct vtg_ref_plane *a,
+                                 const struct vtg_ref_plane *b, int y0, int y1)
+{
+    std::lock_guard<std::mutex> g(g_c.mu);
+    t_status = img_rows<IMG_ABSDIFF>(dst, nullptr, a, b, 0, 0.0f, 0.0f, y0, y1);
+}
+
+extern "C" void img_minmax_cuda(const struct vtg_ref_plane *src, float *out, int y0, int y1)
+{
+    std::lock_guard<std::mutex> g(g_c.mu);
+    t_status = [&]() -> int {
+        if (!plane_ok(src) || !out || y0 < 0 || y1 > src->h || y0 >= y1)
+            return VTG_EINVAL;
+        int rc = ready();
+        if (rc != VTG_OK)
+            return rc;
+        char *base = nullptr;
+        const size_t rows_bytes = up256((size_t)src->w * (size_t)(y1 - y0) * sizeof(float));
+        if ((rc = scratch(rows_bytes + 256, &base)) != VTG_OK)
+            return rc;
+        size_t off = 256; /* the result pair first */
+        const float *pa = nullptr;
+        int pitch = 0;
+        if ((rc = stage_rows(src, y0, y1 - 1, base, &off, &pa, &pitch)) != VTG_OK)
+            return rc;
+        img_minmax_kernel<<<1, 1024, 0, g_c.stream>>>(pa, pitch, src->w, y1 - y0, (float *)base);
+        TRY(cudaGetLastError());
+        TRY(cudaMemcpyAsync(out, base, 2 * sizeof(float), cudaMemcpyDeviceToHost, g_c.stream));
+        TRY(cudaStreamSynchronize(g_c.stream));
+        return VTG_OK;
+    }();
+}
+
 extern "C" void lk_track_cuda(const struct vtg_ref_plane *I, const struct vtg_ref_plane *J, int top,
                               const struct vtg_ref_lk_cfg *c, float x, float y, float gx, float gy,
                               struct vtg_lk_out *o, void *tile)

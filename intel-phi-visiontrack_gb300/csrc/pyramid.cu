@@ -10,6 +10,8 @@
  * same shared-memory tile; each further launch reduces the level below it (L2-resident at these sizes). A CTA of 256
  * threads makes a 64 x 16 tile of its output level from a 132 x 36 source tile staged in shared memory: the vertical
  * pass runs over the staged rows, the horizontal pass over the vertical sums, as the reference's vert5 / shift8 do. */
+#include <math.h>
+
 #include "vtg_internal.cuh"
 
 #define RT_X 64 /* output tile */
@@ -222,12 +224,323 @@ __global__ void __launch_bounds__(256) pyr_batch_kernel(const PyrJob *__restrict
     const int dw = (sw + 1) / 2, dh = (sh + 1) / 2;
     const int tiles_x = (dw + RT_X - 1) / RT_X;
     const int ox = (t % tiles_x) * RT_X, oy = (t / tiles_x) * RT_Y;
-    if (FROM_U8)
+    if (FROM_U8 && j.opts) {
+        /* level 0 came from the build options' launches: level 1 reduces it like any other level */
+        if (j.levels > 1)
+            reduce_tile<false>(j.lv[0], j.w, j.h, j.pitch[0], true, nullptr, 0, j.lv[1], dw, dh, j.pitch[1], ox, oy,
+                               s_t.b, s_t.f, s_v);
+    } else if (FROM_U8)
         reduce_tile<true>(j.src, j.w, j.h, j.stride, aligned16(j.src, j.stride), j.lv[0], j.pitch[0],
                           j.levels > 1 ? j.lv[1] : nullptr, dw, dh, j.pitch[1], ox, oy, s_t.b, s_t.f, s_v);
     else
         reduce_tile<false>(j.lv[level - 1], sw, sh, j.pitch[level - 1], true, nullptr, 0, j.lv[level], dw, dh,
                            j.pitch[level], ox, oy, s_t.b, s_t.f, s_v);
+}
+
+/* ---- tk_build's optional input steps (src/kern/track.c:600-622) ----
+ *
+ * CONTRAST: the min and max of the frame (img_minmax_ref, img_ref.c:57-71), the gain 16320 / (max - min) and the offset
+ * -min x gain in x87 extended precision (track.c:603-614), each rounded to F32, then per pixel
+ * clamp(rint(Q6 x gain + offset), 0, 16320) (img_norm, img_ref.c:42-55). PRE_GAUSS: the 5 x 5 binomial of that with
+ * (h + 128) >> 8 (img_gauss5, img_ref.c:83-96). The result is level 0. The stretch runs on the bytes through a table:
+ * a frame has 256 byte values, each mapped once per CTA. */
+
+/* An x87 extended value on whole-number arithmetic: m x 2^e, 2^63 <= m < 2^64 (m = 0 for zero). Round to nearest even
+ * at 64 bits, as the x87 unit does in its default precision. */
+struct X87 {
+    uint64_t m;
+    int e;
+};
+
+/* num / den rounded to a 64-bit significand; 0 < num, den < 2^31. Long division, one quotient bit a step. */
+__host__ __device__ static inline X87 x87_div(uint32_t num, uint32_t den)
+{
+    uint64_t R = num, D = den;
+    int s = 0;
+    while (D <= (R >> 1)) { /* D <= R < 2 D afterwards: the quotient is R / D x 2^s, R / D in [1, 2) */
+        D <<= 1;
+        s++;
+    }
+    while (R < D) {
+        R <<= 1;
+        s--;
+    }
+    uint64_t m = 0;
+    for (int i = 0; i < 64; i++) { /* R < 2 D throughout */
+        m <<= 1;
+        if (R >= D) {
+            m |= 1;
+            R -= D;
+        }
+        R <<= 1;
+    }
+    const bool guard = R >= D;
+    if (guard)
+        R -= D;
+    X87 r = {m, s - 63};
+    if (guard && (R != 0 || (m & 1))) {
+        r.m++;
+        if (r.m == 0) {
+            r.m = 1ull << 63;
+            r.e++;
+        }
+    }
+    return r;
+}
+
+/* a x k rounded to a 64-bit significand, k < 2^32: the 96-bit product in two words, then one rounding. */
+__host__ __device__ static inline X87 x87_mul(X87 a, uint32_t k)
+{
+    if (a.m == 0 || k == 0)
+        return X87{0, 0};
+    const uint64_t lo32 = (a.m & 0xffffffffull) * k, hi32 = (a.m >> 32) * k;
+    const uint64_t lo = lo32 + (hi32 << 32);
+    const uint64_t hi = (hi32 >> 32) + (lo < lo32 ? 1u : 0u); /* product = hi x 2^64 + lo, hi < 2^32 */
+    int sh = 0;
+    while ((hi >> sh) != 0)
+        sh++;
+    if (sh == 0)
+        return X87{lo, a.e};
+    const uint64_t m = (lo >> sh) | (hi << (64 - sh));
+    const uint64_t half = 1ull << (sh - 1), rest = lo & ((half << 1) - 1);
+    X87 r = {m, a.e + sh};
+    if (rest > half || (rest == half && (m & 1))) {
+        r.m++;
+        if (r.m == 0) {
+            r.m = 1ull << 63;
+            r.e++;
+        }
+    }
+    return r;
+}
+
+/* An extended value rounded to F32 (to nearest even). */
+__host__ __device__ static inline float x87_to_f32(X87 a)
+{
+    if (a.m == 0)
+        return 0.0f;
+    uint32_t t = (uint32_t)(a.m >> 40);
+    const uint64_t rest = a.m & ((1ull << 40) - 1), half = 1ull << 39;
+    int e = a.e + 40;
+    if (rest > half || (rest == half && (t & 1)))
+        t++;
+    if (t == (1u << 24)) {
+        t >>= 1;
+        e++;
+    }
+    return ldexpf((float)t, e);
+}
+
+/* tk_build's gain and offset (track.c:606-614) for Q6 minimum lo and maximum hi: gain = 16320 / (hi - lo) or 1, offset
+ * = -lo x gain, both formed in extended precision and rounded to F32. */
+__host__ __device__ static inline void contrast_gain(int lo, int hi, float *go)
+{
+    if (hi > lo) {
+        const X87 g = x87_div(16320u, (uint32_t)(hi - lo));
+        go[0] = x87_to_f32(g);
+        go[1] = -x87_to_f32(x87_mul(g, (uint32_t)lo));
+    } else {
+        go[0] = 1.0f;
+        go[1] = -(float)lo;
+    }
+}
+
+extern "C" int vtg_contrast_gain(int lo, int hi, float *gain_offset)
+{
+    if (!gain_offset || lo < 0 || hi < lo || hi >= (1 << 24))
+        return VTG_EINVAL;
+    contrast_gain(lo, hi, gain_offset);
+    return VTG_OK;
+}
+
+/* The minimum and maximum over a CTA of per-thread values (min in the low byte of the result, max in the next). */
+__device__ __forceinline__ uint32_t block_minmax(uint32_t mn, uint32_t mx, uint32_t *s_w)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    mn = __reduce_min_sync(VTG_FULL, mn);
+    mx = __reduce_max_sync(VTG_FULL, mx);
+    if (lane == 0)
+        s_w[warp] = mn | (mx << 8);
+    __syncthreads();
+    if (warp == 0) {
+        const uint32_t v = lane < (int)(blockDim.x >> 5) ? s_w[lane] : 255u;
+        mn = __reduce_min_sync(VTG_FULL, v & 255u);
+        mx = __reduce_max_sync(VTG_FULL, (v >> 8) & 255u);
+        if (lane == 0)
+            s_w[32] = mn | (mx << 8);
+    }
+    __syncthreads();
+    const uint32_t r = s_w[32];
+    __syncthreads();
+    return r;
+}
+
+/* The frame's byte min and max (x 64 = img_minmax of its Q6 plane): CTA b scans rows b, b + grid, ... four bytes at a
+ * time (16 with an aligned frame) and writes its partial to mm[b]; the last CTA to finish (a ticket in
+ * mm[VTG_MM_BLOCKS]) combines the partials, writes gain and offset to mm[VTG_MM_BLOCKS + 1 ..] and resets the ticket. */
+__global__ void __launch_bounds__(256) pyr_minmax_kernel(const uint8_t *__restrict__ src, int w, int h, int stride,
+                                                         uint32_t *__restrict__ mm)
+{
+    __shared__ uint32_t s_w[33];
+    __shared__ bool s_last;
+    uint32_t mn4 = 0xffffffffu, mx4 = 0u;
+    const bool vec = (((uintptr_t)src | (uintptr_t)stride) & 15) == 0;
+    for (int y = blockIdx.x; y < h; y += gridDim.x) {
+        const uint8_t *row = src + (size_t)y * stride;
+        for (int x = 16 * (int)threadIdx.x; x < w; x += 16 * (int)blockDim.x) {
+            uint32_t v[4];
+            if (vec && x + 16 <= w) {
+                const uint4 q = __ldg(reinterpret_cast<const uint4 *>(row + x));
+                v[0] = q.x;
+                v[1] = q.y;
+                v[2] = q.z;
+                v[3] = q.w;
+            } else {
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    uint32_t word = 0;
+#pragma unroll
+                    for (int e = 0; e < 4; e++) /* past the row's end: its last byte again, which changes nothing */
+                        word |= (uint32_t)__ldg(row + min(x + 4 * k + e, w - 1)) << (8 * e);
+                    v[k] = word;
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                mn4 = __vminu4(mn4, v[k]);
+                mx4 = __vmaxu4(mx4, v[k]);
+            }
+        }
+    }
+    uint32_t mn = min(min(mn4 & 255u, (mn4 >> 8) & 255u), min((mn4 >> 16) & 255u, mn4 >> 24));
+    uint32_t mx = max(max(mx4 & 255u, (mx4 >> 8) & 255u), max((mx4 >> 16) & 255u, mx4 >> 24));
+    const uint32_t part = block_minmax(mn, mx, s_w);
+    if (threadIdx.x == 0) {
+        mm[blockIdx.x] = part;
+        __threadfence();
+        s_last = atomicAdd(&mm[VTG_MM_BLOCKS], 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!s_last)
+        return;
+    __threadfence();
+    mn = 255u;
+    mx = 0u;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) {
+        const uint32_t p = __ldcg(&mm[i]);
+        mn = min(mn, p & 255u);
+        mx = max(mx, (p >> 8) & 255u);
+    }
+    const uint32_t all = block_minmax(mn, mx, s_w);
+    if (threadIdx.x == 0) {
+        float go[2];
+        contrast_gain(64 * (int)(all & 255u), 64 * (int)((all >> 8) & 255u), go);
+        reinterpret_cast<float *>(mm)[VTG_MM_BLOCKS + 1] = go[0];
+        reinterpret_cast<float *>(mm)[VTG_MM_BLOCKS + 2] = go[1];
+        mm[VTG_MM_BLOCKS] = 0u; /* the next frame's ticket; this kernel's CTAs have all taken theirs */
+    }
+}
+
+#define PT_X 64 /* level-0 tile of the input steps */
+#define PT_Y 16
+
+/* Level 0 under the build options, one 64 x 16 tile a CTA: the bytes mapped through the stretch's table (or x 64),
+ * staged with a two-pixel clamped border, then the binomial's vertical and horizontal passes on whole numbers
+ * (at most 16320 x 256, exact in int) when GAUSS. */
+template <bool CONTRAST, bool GAUSS>
+__global__ void __launch_bounds__(256) pyr_input_kernel(const uint8_t *__restrict__ src, int w, int h, int stride,
+                                                        const uint32_t *__restrict__ mm, float *__restrict__ l0,
+                                                        int pitch)
+{
+    __shared__ int s_lut[256];
+    __shared__ __align__(16) int s_n[PT_Y + 4][PT_X + 4];
+    __shared__ __align__(16) int s_v[PT_Y][PT_X + 4];
+    const int tid = threadIdx.x;
+    const int ox = blockIdx.x * PT_X, oy = blockIdx.y * PT_Y;
+    if (CONTRAST) {
+        const float g = __ldcg(reinterpret_cast<const float *>(mm) + VTG_MM_BLOCKS + 1);
+        const float o = __ldcg(reinterpret_cast<const float *>(mm) + VTG_MM_BLOCKS + 2);
+        /* the reference's x87 form rounds Q6 x gain + offset to F32 from an exact extended sum (the product has 38
+         * bits, the sum's lowest bit is at least 2^-23 and its size below 2^23); one fused multiply-add rounds the
+         * same exact value once */
+        const float v = rintf(__fmaf_rn((float)(64 * tid), g, o));
+        s_lut[tid] = (int)fminf(fmaxf(v, 0.0f), 16320.0f);
+    } else {
+        s_lut[tid] = 64 * tid;
+    }
+    __syncthreads();
+    if (GAUSS) {
+        for (int i = tid; i < (PT_Y + 4) * (PT_X + 4); i += blockDim.x) {
+            const int r = i / (PT_X + 4), c = i - r * (PT_X + 4);
+            const int gy = min(max(oy - 2 + r, 0), h - 1), gx = min(max(ox - 2 + c, 0), w - 1);
+            s_n[r][c] = s_lut[__ldg(src + (size_t)gy * stride + gx)];
+        }
+        __syncthreads();
+        for (int i = tid; i < PT_Y * (PT_X + 4); i += blockDim.x) {
+            const int r = i / (PT_X + 4), c = i - r * (PT_X + 4);
+            s_v[r][c] = s_n[r][c] + s_n[r + 4][c] + 4 * (s_n[r + 1][c] + s_n[r + 3][c]) + 6 * s_n[r + 2][c];
+        }
+        __syncthreads();
+    }
+    for (int i = tid; i < PT_Y * (PT_X / 4); i += blockDim.x) {
+        const int r = i / (PT_X / 4), g = i - r * (PT_X / 4);
+        const int gy = oy + r, gx = ox + 4 * g;
+        if (gy >= h || gx >= w)
+            continue;
+        float o[4];
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            if (GAUSS) {
+                const int c = 4 * g + e; /* vertical sums c .. c + 4 around output column c + 2 of the staged tile */
+                const int hs = s_v[r][c] + s_v[r][c + 4] + 4 * (s_v[r][c + 1] + s_v[r][c + 3]) + 6 * s_v[r][c + 2];
+                o[e] = small_int_to_float((hs + 128) >> 8);
+            } else {
+                o[e] = small_int_to_float(s_lut[__ldg(src + (size_t)gy * stride + min(gx + e, w - 1))]);
+            }
+        }
+        float *d = l0 + (size_t)gy * pitch + gx;
+        if (gx + 4 <= w) {
+            *reinterpret_cast<float4 *>(d) = make_float4(o[0], o[1], o[2], o[3]);
+        } else {
+            for (int e = 0; e < 4 && gx + e < w; e++)
+                d[e] = o[e];
+        }
+    }
+}
+
+cudaError_t vtg_launch_build_input(const uint8_t *frame, int stride, int w, int h, int opts, uint32_t *mm, float *l0,
+                                   int pitch0, cudaStream_t s)
+{
+    const bool contrast = (opts & VTG_BUILD_CONTRAST) != 0, gauss = (opts & VTG_BUILD_PRE_GAUSS) != 0;
+    if (contrast)
+        pyr_minmax_kernel<<<min(h, VTG_MM_BLOCKS), 256, 0, s>>>(frame, w, h, stride, mm);
+    const dim3 grid((w + PT_X - 1) / PT_X, (h + PT_Y - 1) / PT_Y);
+    if (contrast && gauss)
+        pyr_input_kernel<true, true><<<grid, 256, 0, s>>>(frame, w, h, stride, mm, l0, pitch0);
+    else if (contrast)
+        pyr_input_kernel<true, false><<<grid, 256, 0, s>>>(frame, w, h, stride, mm, l0, pitch0);
+    else if (gauss)
+        pyr_input_kernel<false, true><<<grid, 256, 0, s>>>(frame, w, h, stride, mm, l0, pitch0);
+    return cudaGetLastError();
+}
+
+cudaError_t vtg_launch_pyramid_opts(const uint8_t *frame, int stride, int w, int h, float *const *levels,
+                                    const int *pitches, int nlevels, int opts, uint32_t *mm, cudaStream_t s)
+{
+    if (!(opts & (VTG_BUILD_CONTRAST | VTG_BUILD_PRE_GAUSS)))
+        return vtg_launch_pyramid(frame, stride, w, h, levels, pitches, nlevels, s);
+    cudaError_t e = vtg_launch_build_input(frame, stride, w, h, opts, mm, levels[0], pitches[0], s);
+    int sw = w, sh = h;
+    for (int L = 1; L < nlevels && e == cudaSuccess; L++) {
+        const int dw = (sw + 1) / 2, dh = (sh + 1) / 2;
+        const dim3 grid((dw + RT_X - 1) / RT_X, (dh + RT_Y - 1) / RT_Y);
+        pyr_reduce_kernel<false><<<grid, 256, 0, s>>>(levels[L - 1], sw, sh, pitches[L - 1], nullptr, 0, levels[L], dw,
+                                                      dh, pitches[L]);
+        e = cudaGetLastError();
+        sw = dw;
+        sh = dh;
+    }
+    return e;
 }
 
 int vtg_pyr_tiles(int w, int h, int level)

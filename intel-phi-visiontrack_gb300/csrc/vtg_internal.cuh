@@ -43,10 +43,16 @@ struct CellGrid {
 
 static inline int vtg_pitch(int w) { return (w + 31) & ~31; }
 
-/* One frame's pyramid in a batched build: its bytes and its set's level planes. lw / lh: level sizes. */
+/* tk_build's optional input steps (VTG_BUILD_CONTRAST / VTG_BUILD_PRE_GAUSS) keep a frame's partial minima and maxima,
+ * a ticket and the gain / offset in VTG_MM_WORDS words of device memory. */
+#define VTG_MM_BLOCKS 304
+#define VTG_MM_WORDS (VTG_MM_BLOCKS + 4)
+
+/* One frame's pyramid in a batched build: its bytes and its set's level planes. lw / lh: level sizes. opts: build
+ * options; a job with options has its level 0 written by vtg_launch_build_input before the batched launches. */
 struct PyrJob {
     const uint8_t *src;
-    int stride, w, h, levels;
+    int stride, w, h, levels, opts;
     float *lv[VTG_MAX_LEVELS];
     int pitch[VTG_MAX_LEVELS], lw[VTG_MAX_LEVELS], lh[VTG_MAX_LEVELS];
 };
@@ -73,6 +79,13 @@ struct LkTune {
 /* Launchers (pyramid.cu, lk.cu). All asynchronous on `s`; each returns a cudaError_t. */
 cudaError_t vtg_launch_pyramid(const uint8_t *frame, int stride, int w, int h, float *const *levels, const int *pitches,
                                int nlevels, cudaStream_t s);
+/* Level 0 of a frame under build options (the contrast stretch and / or the 5 x 5 binomial); `mm`: VTG_MM_WORDS words
+ * of device memory whose ticket word (mm[VTG_MM_BLOCKS]) is 0. */
+cudaError_t vtg_launch_build_input(const uint8_t *frame, int stride, int w, int h, int opts, uint32_t *mm, float *l0,
+                                   int pitch0, cudaStream_t s);
+/* The whole pyramid under build options: level 0 as above, then the reduce per level. */
+cudaError_t vtg_launch_pyramid_opts(const uint8_t *frame, int stride, int w, int h, float *const *levels,
+                                    const int *pitches, int nlevels, int opts, uint32_t *mm, cudaStream_t s);
 cudaError_t vtg_launch_cells(const DevPyr *I, const DevPyr *J, int top, const LkPrm &p, const CellGrid &g, int base_w,
                              int base_h, vtg_lk_out *out, vtg_cell *cells, cudaStream_t s);
 int vtg_pyr_tiles(int w, int h, int level);

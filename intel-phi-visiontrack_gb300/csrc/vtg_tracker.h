@@ -25,6 +25,8 @@ struct vtg_tracker {
     DevPyr *desc;         /* [set][0: from level 0, 1: from flow_level] */
     vtg_lk_out *d_lk;     /* cells x lk_out */
     vtg_cell *d_cells;    /* cells x vt_cell */
+    uint32_t *d_mm;       /* the build options' VTG_MM_WORDS words a set (min / max partials, ticket, gain / offset) */
+    int build_opts;       /* VTG_BUILD_CONTRAST | VTG_BUILD_PRE_GAUSS */
     LkPrm prm;
 };
 

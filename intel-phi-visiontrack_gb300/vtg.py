@@ -17,6 +17,8 @@ LIB_PATH = os.path.join(HERE, "libvtg.so")
 
 OK, EINVAL, ENOMEM, ECUDA, ETIMEOUT, EBUSY, ENODEV, EBUDGET = 0, -1, -2, -3, -4, -5, -6, -7
 HOST, DEVICE = 0, 1
+# tk_build's optional input steps (vtg_tracker_set_build): the contrast stretch and the 5 x 5 binomial
+BUILD_CONTRAST, BUILD_PRE_GAUSS = 1, 2
 LK_OK, LK_OUT, LK_LOWEIG, LK_RESIDUAL, LK_FLOWBACK = 0, 1, 2, 4, 8
 MAX_LEVELS = 6
 
@@ -82,8 +84,18 @@ def lib() -> C.CDLL:
         L.vtg_points.argtypes = [vp, i, i, i, i, vp, vp, vp, vp, vp, i, vp]
         L.vtg_level.argtypes = [vp, i, i, vp, i, vp]
         L.vtg_level_size.argtypes = [vp, i, C.POINTER(i), C.POINTER(i)]
+        L.vtg_tracker_set_build.argtypes = [vp, i]
+        L.vtg_tracker_build_flags.argtypes = [vp]
+        L.vtg_contrast_gain.argtypes = [i, i, vp]
         _lib = L
     return _lib
+
+
+def contrast_gain(lo: int, hi: int):
+    """tk_build's stretch (gain, offset) as float32 for Q6 minimum lo and maximum hi (vtg_contrast_gain)."""
+    go = np.zeros(2, np.float32)
+    check(lib().vtg_contrast_gain(int(lo), int(hi), go.ctypes.data), "vtg_contrast_gain")
+    return go
 
 
 def check(code: int, what: str) -> int:
@@ -159,6 +171,14 @@ class Tracker:
             ptr = frame
             stride = self.cfg.width if stride is None else stride
         check(lib().vtg_build(self.h, set_, ptr, stride, where, stream), "vtg_build")
+
+    def set_build(self, flags: int):
+        """tk_build's optional steps for later builds: BUILD_CONTRAST | BUILD_PRE_GAUSS (0: neither)."""
+        check(lib().vtg_tracker_set_build(self.h, int(flags)), "vtg_tracker_set_build")
+
+    @property
+    def build_flags(self) -> int:
+        return lib().vtg_tracker_build_flags(self.h)
 
     def level(self, set_: int, level: int) -> np.ndarray:
         w, h = self.level_size(level)
@@ -476,6 +496,16 @@ def compat() -> C.CDLL:
         L.img_u8_to_q6_cuda.restype = None
         L.img_reduce_cuda.argtypes = [P, P, i, i]
         L.img_reduce_cuda.restype = None
+        L.img_norm_cuda.argtypes = [P, P, vp, i, i]
+        L.img_norm_cuda.restype = None
+        L.img_minmax_cuda.argtypes = [P, vp, i, i]
+        L.img_minmax_cuda.restype = None
+        L.img_gauss5_cuda.argtypes = [P, P, i, i]
+        L.img_gauss5_cuda.restype = None
+        L.img_sobel_cuda.argtypes = [P, P, P, i, i]
+        L.img_sobel_cuda.restype = None
+        L.img_absdiff_cuda.argtypes = [P, P, P, i, i]
+        L.img_absdiff_cuda.restype = None
         L.lk_track_cuda.argtypes = [PL, PL, i, C.POINTER(RefLkCfg), f, f, f, f, vp, vp]
         L.lk_track_cuda.restype = None
         L.lk_flowback_cuda.argtypes = [PL, PL, i, C.POINTER(RefLkCfg), f, f, f, vp, vp]

@@ -157,6 +157,22 @@ def framegen_pair(kind: str, w: int, h: int, shift, seed: int):
     return f0, f1
 
 
+def build_frame(kind: str, w: int, h: int, seed: int) -> np.ndarray:
+    """A frame for tk_build's input steps: "warp", a blurred-noise scene; "low", the same squeezed into grey 100 .. 140
+    (what the contrast stretch is for); "flat", one grey level (no range to stretch); "dark", the scene scaled into
+    0 .. 60 with a black corner (minimum 0)."""
+    if kind == "flat":
+        return np.full((h, w), 77, np.uint8)
+    f = noise_frame(w, h, seed)
+    if kind == "low":
+        return (100 + (f.astype(np.int32) * 40) // 255).astype(np.uint8)
+    if kind == "dark":
+        d = (f.astype(np.int32) * 60 // 255).astype(np.uint8)
+        d[: h // 8, : w // 8] = 0
+        return d
+    return f
+
+
 def seeded_shift(seed: int, stream: int, reach: float = 12.0):
     u = uniform(seed, 100 + stream, 2)
     return (float(-reach + 2 * reach * u[0]), float(-reach + 2 * reach * u[1]))

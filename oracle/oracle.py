@@ -89,6 +89,13 @@ def lib() -> C.CDLL:
         _lib.or_cut_template.argtypes = [C.POINTER(Img), C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
         _lib.or_u8_to_q6.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int]
         _lib.or_reduce.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int]
+        _lib.or_minmax.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p]
+        _lib.or_norm.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int]
+        _lib.or_gauss5.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int]
+        _lib.or_sobel.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int]
+        _lib.or_absdiff.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int]
+        _lib.or_contrast_gain.argtypes = [C.c_int, C.c_int, C.c_void_p]
+        _lib.or_build_input.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int]
         _lib.or_m1_image.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int]
         _lib.or_m2_render.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]
         _lib.or_cell_centre.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(LkCfg), C.c_int, C.c_int,
@@ -207,6 +214,8 @@ def ref() -> C.CDLL:
                                        C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int,
                                        C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]
         _ref.ref_pyramid.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p]
+        _ref.ref_tk_build.restype = C.c_int
+        _ref.ref_tk_build.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p]
         _ref.ref_still_vectors.restype = C.c_int
         _ref.ref_still_vectors.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p]
         _ref.ref_still_run.restype = C.c_int
@@ -235,14 +244,22 @@ def level_dims(w: int, h: int, levels: int):
     return dims
 
 
-def pyramid(frame: np.ndarray, levels: int):
-    """The Q6 pyramid of a uint8 frame: a list of float32 planes (exact whole numbers), level 0 first."""
+BUILD_CONTRAST = 1
+BUILD_PRE_GAUSS = 2
+
+
+def pyramid(frame: np.ndarray, levels: int, opts: int = 0):
+    """The Q6 pyramid of a uint8 frame: a list of float32 planes (exact whole numbers), level 0 first. opts: tk_build's
+    optional input steps, BUILD_CONTRAST and / or BUILD_PRE_GAUSS (src/kern/track.c:600-622)."""
     L = lib()
     frame = np.ascontiguousarray(frame, dtype=np.uint8)
     h, w = frame.shape
     out = []
     q = np.empty((h, w), np.float32)
-    L.or_u8_to_q6(_p(frame), C.c_int(w), C.c_int(w), C.c_int(h), _p(q), C.c_int(w))
+    if opts:
+        L.or_build_input(_p(frame), w, w, h, int(opts), _p(q), w)
+    else:
+        L.or_u8_to_q6(_p(frame), C.c_int(w), C.c_int(w), C.c_int(h), _p(q), C.c_int(w))
     out.append(q)
     for _ in range(1, levels):
         ph, pw = out[-1].shape
@@ -250,6 +267,77 @@ def pyramid(frame: np.ndarray, levels: int):
         L.or_reduce(_p(out[-1]), C.c_int(pw), C.c_int(ph), C.c_int(pw), _p(d), C.c_int(d.shape[1]))
         out.append(d)
     return out
+
+
+def _plane(a: np.ndarray) -> np.ndarray:
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    assert a.ndim == 2
+    return a
+
+
+def minmax(plane: np.ndarray):
+    """img_minmax: (min, max) of a plane."""
+    a = _plane(plane)
+    out = np.zeros(2, np.float32)
+    lib().or_minmax(_p(a), a.shape[1], a.shape[0], a.shape[1], _p(out))
+    return float(out[0]), float(out[1])
+
+
+def norm(plane: np.ndarray, gain: float, offset: float) -> np.ndarray:
+    """img_norm: clamp(rint(plane x gain + offset), 0, 16320)."""
+    a = _plane(plane)
+    go = np.array([gain, offset], np.float32)
+    d = np.empty_like(a)
+    lib().or_norm(_p(a), a.shape[1], a.shape[0], a.shape[1], _p(go), _p(d), a.shape[1])
+    return d
+
+
+def gauss5(plane: np.ndarray) -> np.ndarray:
+    """img_gauss5: the 5 x 5 binomial at every pixel."""
+    a = _plane(plane)
+    d = np.empty_like(a)
+    lib().or_gauss5(_p(a), a.shape[1], a.shape[0], a.shape[1], _p(d), a.shape[1])
+    return d
+
+
+def sobel(plane: np.ndarray):
+    """img_sobel: (ix, iy)."""
+    a = _plane(plane)
+    ix, iy = np.empty_like(a), np.empty_like(a)
+    lib().or_sobel(_p(a), a.shape[1], a.shape[0], a.shape[1], _p(ix), _p(iy), a.shape[1])
+    return ix, iy
+
+
+def absdiff(a: np.ndarray, b: np.ndarray) -> np.ndarray:
+    """img_absdiff: |a - b|."""
+    a, b = _plane(a), _plane(b)
+    assert a.shape == b.shape
+    d = np.empty_like(a)
+    lib().or_absdiff(_p(a), _p(b), a.shape[1], a.shape[0], a.shape[1], _p(d), a.shape[1])
+    return d
+
+
+def contrast_gain(lo: int, hi: int):
+    """tk_build's stretch gain and offset (float32) for Q6 minimum lo and maximum hi."""
+    go = np.zeros(2, np.float32)
+    lib().or_contrast_gain(int(lo), int(hi), _p(go))
+    return go
+
+
+def ref_tk_build(frame: np.ndarray, levels: int, opts: int = 0, x87: bool = False):
+    """The reference's own tk_build of one frame (width a multiple of 16): its pyramid's planes, level 0 first."""
+    frame = np.ascontiguousarray(frame, dtype=np.uint8)
+    h, w = frame.shape
+    dims = level_dims(w, h, levels)
+    out = np.zeros(sum(a * b for a, b in dims), np.float32)
+    rc = ref().ref_tk_build(_p(frame), w, h, levels, int(bool(opts & BUILD_CONTRAST)),
+                            int(bool(opts & BUILD_PRE_GAUSS)), int(x87), _p(out))
+    assert rc == 0, "tk_create refused the configuration"
+    planes, off = [], 0
+    for (lw, lh) in dims:
+        planes.append(out[off:off + lw * lh].reshape(lh, lw))
+        off += lw * lh
+    return planes
 
 
 def make_pyr(levels_list) -> Pyr:

@@ -78,3 +78,36 @@ void ref_search_half(const float *interior, int w, int h, const float *app, floa
 }
 
 double ref_peak_offset(double l, double c, double r) { return (double)peak_offset((long double)l, (long double)c, (long double)r); }
+
+/* tk_build (track.c:584-629) of one frame (w a multiple of 16, rows w bytes apart) with struct vt_config's contrast and
+ * pre_gauss as given, on the x87 kernels (alg 1) or the vector ones (alg 0): every level's w_L x h_L values, level 0
+ * first, into out. Returns 0, or -1 when the tracker cannot be made. */
+int ref_tk_build(const uint8_t *frame, int w, int h, int levels, int contrast, int pre_gauss, int alg, float *out)
+{
+    struct vt_config cfg;
+    memset(&cfg, 0, sizeof cfg);
+    cfg.width = (uint32_t)w;
+    cfg.height = (uint32_t)h;
+    cfg.levels = (uint32_t)levels;
+    cfg.patch_w = 21;
+    cfg.patch_h = 21;
+    cfg.max_iter = 10;
+    cfg.pipelines = 1;
+    cfg.contrast = (uint32_t)contrast;
+    cfg.pre_gauss = (uint32_t)pre_gauss;
+    struct tracker *t = tk_create(&cfg, 1, 1, tu_alloc, NULL, tu_run, NULL, tu_run, NULL);
+    if (!t)
+        return -1;
+    struct vt_msg m;
+    memset(&m, 0, sizeof m);
+    m.algorithm = alg ? VT_ALG_X87 : VT_ALG_MVEX;
+    tk_build(t, 0, frame, NULL, &m);
+    for (int L = 0; L < levels; L++) {
+        const struct vt_plane *pl = &t->pyr[0][0].l[L];
+        for (int y = 0; y < pl->h; y++) {
+            memcpy(out, plane_row(pl, y), sizeof(float) * (size_t)pl->w);
+            out += pl->w;
+        }
+    }
+    return 0;
+}

@@ -115,6 +115,179 @@ void or_reduce(const float *src, int w, int h, int src_stride, float *dst, int d
         }
 }
 
+/* ---------------------------------------------------------------- tk_build's optional input steps and the M1 gate's
+ * other image kernels (src/kern/img_ref.c), on w x h planes read with clamped indices (the reference's replicated
+ * border). */
+
+/* Min and max of the plane's values, the first value as the start (img_minmax_ref, img_ref.c:57-71). */
+void or_minmax(const float *src, int w, int h, int stride, float out[2])
+{
+    float mn = src[0], mx = mn;
+    for (int y = 0; y < h; y++)
+        for (int x = 0; x < w; x++) {
+            const float v = src[(size_t)y * stride + x];
+            if (v < mn)
+                mn = v;
+            if (v > mx)
+                mx = v;
+        }
+    out[0] = mn;
+    out[1] = mx;
+}
+
+/* dst = clamp(rint(src x gain + offset), 0, 16320) (img_norm_ref, img_ref.c:42-55). The reference rounds an x87
+ * extended src x gain + offset to F32; its vector form (img_vx.c:49-59) rounds the exact value once with a fused
+ * multiply-add, as here. The two agree whenever the extended sum is exact: always for tk_build's gains (whole-number
+ * src, gain >= 1), and for the M1 gate's (0.75, 512). */
+void or_norm(const float *src, int w, int h, int sstride, const float go[2], float *dst, int dstride)
+{
+    for (int y = 0; y < h; y++)
+        for (int x = 0; x < w; x++) {
+            float v = rintf(fmaf(src[(size_t)y * sstride + x], go[0], go[1]));
+            v = v < 0.0f ? 0.0f : v > 16320.0f ? 16320.0f : v;
+            dst[(size_t)y * dstride + x] = v;
+        }
+}
+
+/* The 5 x 5 binomial at every pixel, (sum + 128) >> 8 (img_gauss5_ref, img_ref.c:73-96): whole numbers, exact. */
+void or_gauss5(const float *src, int w, int h, int sstride, float *dst, int dstride)
+{
+    static const int k[5] = {1, 4, 6, 4, 1};
+    for (int y = 0; y < h; y++)
+        for (int x = 0; x < w; x++) {
+            int64_t s = 0;
+            for (int j = -2; j <= 2; j++) {
+                const float *row = src + (size_t)clampi(y + j, 0, h - 1) * sstride;
+                for (int i = -2; i <= 2; i++)
+                    s += (int64_t)k[j + 2] * k[i + 2] * (int64_t)row[clampi(x + i, 0, w - 1)];
+            }
+            dst[(size_t)y * dstride + x] = (float)((s + 128) >> 8);
+        }
+}
+
+/* Sobel x and y in the reference's F32 order (img_sobel_ref, img_ref.c:116-127). */
+void or_sobel(const float *src, int w, int h, int sstride, float *ix, float *iy, int dstride)
+{
+    for (int y = 0; y < h; y++) {
+        const float *r0 = src + (size_t)clampi(y - 1, 0, h - 1) * sstride, *r1 = src + (size_t)y * sstride,
+                    *r2 = src + (size_t)clampi(y + 1, 0, h - 1) * sstride;
+        for (int x = 0; x < w; x++) {
+            const int xl = clampi(x - 1, 0, w - 1), xr = clampi(x + 1, 0, w - 1);
+            const float a = r0[xl], b = r0[x], c = r0[xr], e = r1[xl], g = r1[xr], m = r2[xl], n = r2[x], o = r2[xr];
+            ix[(size_t)y * dstride + x] = (c + 2.0f * g + o) - (a + 2.0f * e + m);
+            iy[(size_t)y * dstride + x] = (m + 2.0f * n + o) - (a + 2.0f * b + c);
+        }
+    }
+}
+
+/* |a - b| (img_absdiff_ref, img_ref.c:129-137). */
+void or_absdiff(const float *a, const float *b, int w, int h, int stride, float *dst, int dstride)
+{
+    for (int y = 0; y < h; y++)
+        for (int x = 0; x < w; x++)
+            dst[(size_t)y * dstride + x] = fabsf(a[(size_t)y * stride + x] - b[(size_t)y * stride + x]);
+}
+
+/* q / d rounded to nearest even at 64 significant bits: (m, e) with q / d = m 2^e, 2^63 <= m < 2^64. q, d > 0. */
+static void x87_quot(unsigned __int128 q, unsigned __int128 d, uint64_t *m, int *e)
+{
+    int k = 0; /* q 2^k / d in [2^63, 2^64) */
+    while (q / d < ((unsigned __int128)1 << 63)) {
+        q <<= 1;
+        k++;
+    }
+    while (q / d >= ((unsigned __int128)1 << 64)) {
+        d <<= 1;
+        k--;
+    }
+    unsigned __int128 t = q / d;
+    const unsigned __int128 r = q % d;
+    if (2 * r > d || (2 * r == d && (t & 1)))
+        t++;
+    if (t == ((unsigned __int128)1 << 64)) {
+        t >>= 1;
+        k--;
+    }
+    *m = (uint64_t)t;
+    *e = -k;
+}
+
+/* m 2^e rounded to nearest even at `bits` significant bits, m below 2^127: the rounded significand and exponent. */
+static void round_bits(unsigned __int128 m, int e, int bits, uint64_t *mo, int *eo)
+{
+    int len = 0;
+    while (len < 128 && (m >> len) != 0)
+        len++;
+    if (len <= bits) {
+        *mo = (uint64_t)m;
+        *eo = e;
+        return;
+    }
+    const int s = len - bits;
+    unsigned __int128 t = m >> s;
+    const unsigned __int128 rest = m & (((unsigned __int128)1 << s) - 1), half = (unsigned __int128)1 << (s - 1);
+    if (rest > half || (rest == half && (t & 1)))
+        t++;
+    int ex = e + s;
+    if (t >> bits) {
+        t >>= 1;
+        ex++;
+    }
+    *mo = (uint64_t)t;
+    *eo = ex;
+}
+
+/* tk_build's stretch (src/kern/track.c:603-614): gain = 16320 / (hi - lo) (1 when hi == lo) and offset = -lo x gain,
+ * each an x87 extended value (64-bit significand, to nearest even) rounded to F32. Whole numbers 0 <= lo <= hi < 2^24.
+ * Exact integer arithmetic, so it is the same on every host. */
+void or_contrast_gain(int lo, int hi, float go[2])
+{
+    if (hi <= lo) {
+        go[0] = 1.0f;
+        go[1] = -(float)lo;
+        return;
+    }
+    uint64_t gm, om, fm;
+    int ge, oe, fe;
+    x87_quot(16320, (unsigned __int128)(hi - lo), &gm, &ge);
+    round_bits(gm, ge, 24, &fm, &fe);
+    go[0] = ldexpf((float)fm, fe);
+    if (lo == 0) {
+        go[1] = -0.0f;
+        return;
+    }
+    round_bits((unsigned __int128)gm * (unsigned __int128)lo, ge, 64, &om, &oe);
+    round_bits(om, oe, 24, &fm, &fe);
+    go[1] = -ldexpf((float)fm, fe);
+}
+
+/* Level 0 as tk_build makes it from a frame's bytes (track.c:596-622): Q6, then with opts & 1 the stretch of its min ..
+ * max, then with opts & 2 the binomial. dst: w x h, rows dstride floats apart. */
+void or_build_input(const uint8_t *src, int sstride, int w, int h, int opts, float *dst, int dstride)
+{
+    float *a = malloc(sizeof(float) * (size_t)w * h), *b = malloc(sizeof(float) * (size_t)w * h);
+    or_u8_to_q6(src, sstride, w, h, a, w);
+    if (opts & 1) {
+        float mm[2], go[2];
+        or_minmax(a, w, h, w, mm);
+        or_contrast_gain((int)mm[0], (int)mm[1], go);
+        or_norm(a, w, h, w, go, b, w);
+        float *t = a;
+        a = b;
+        b = t;
+    }
+    if (opts & 2) {
+        or_gauss5(a, w, h, w, b, w);
+        float *t = a;
+        a = b;
+        b = t;
+    }
+    for (int y = 0; y < h; y++)
+        memcpy(dst + (size_t)y * dstride, a + (size_t)y * w, sizeof(float) * (size_t)w);
+    free(a);
+    free(b);
+}
+
 /* ---------------------------------------------------------------- lane arithmetic */
 
 static float hsum16(const float *in)

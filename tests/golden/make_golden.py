@@ -19,6 +19,7 @@ Writes:
                     corners found.
   still.npz         the still picture (still_vectors, still_decide, still_update, still_finish) over a 12-frame
                     320 x 240 sequence: per frame the cells after the decision, still_motion and still_hash.
+  build_opts.npz    tk_build with the contrast stretch and / or the 5 x 5 binomial on six frames: per-level hashes.
   framegen.npz      frame generation (framegen.c as tk_generate_make runs it) on three pairs: the fields of every
                     level, the middle-instant field, hashes of the generated frame and its bytes, the scene verdict.
 Frames are not stored: the generator reproduces them bit for bit, and their hashes are stored to prove it.
@@ -49,6 +50,9 @@ def parse_logs(ref_root: str) -> dict:
                 m = re.match(r"kern (\S+)\s+(\d+)x(\d+) ([0-9a-f]{16})$", line.strip())
                 if m:
                     m1["%s %s" % (m.group(1), size)] = m.group(4)
+                m = re.match(r"kern minmax\s+(\d+)x(\d+) (\S+) (\S+)$", line.strip())
+                if m:
+                    m1["minmax " + size] = [float(m.group(3)), float(m.group(4))]
     m2 = []
     with open(os.path.join(ref_root, "logs", "m2", "host", "640x480.txt")) as f:
         for line in f:
@@ -147,6 +151,7 @@ def main(ref_root: str = "/root/reference") -> None:
                         counts=np.array(counts, np.int32))
     write_still()
     write_framegen()
+    write_build_opts()
     print("golden fixtures written to", HERE)
 
 
@@ -188,6 +193,31 @@ def write_framegen() -> None:
     out["cases"] = np.array([(k == "scene", w, h, sx, sy, seed) for k, w, h, (sx, sy), seed in FG_CASES], np.float64)
     out["kinds"] = np.array([k for k, *_ in FG_CASES])
     np.savez_compressed(os.path.join(HERE, "framegen.npz"), **out)
+
+
+BUILD_CASES = [("warp", 640, 480, 1), ("low", 640, 480, 2), ("flat", 160, 96, 0), ("dark", 208, 133, 4),
+               ("low", 1920, 1080, 5)]
+
+
+def write_build_opts() -> None:
+    """build_opts.npz: the reference's tk_build with struct vt_config's contrast and pre_gauss (all four settings, x87
+    and vector kernels alike) on the frames of vtg_synth.build_frame and the M1 gate's 640 x 480 frame: per case and
+    setting, the FNV hash of every level (3 levels)."""
+    out = {}
+    frames = [("m1", 640, 480, 0, O.m1_image(640, 480))]
+    frames += [(k, w, h, seed, S.build_frame(k, w, h, seed)) for k, w, h, seed in BUILD_CASES]
+    for i, (kind, w, h, seed, f) in enumerate(frames):
+        hashes = []
+        for opts in range(4):
+            planes = O.ref_tk_build(f, 3, opts, x87=True)
+            vx = O.ref_tk_build(f, 3, opts, x87=False)
+            assert all(a.tobytes() == b.tobytes() for a, b in zip(planes, vx)), (kind, opts)
+            hashes.append([O.fnv(p) for p in planes])
+        out["case%d_fnv" % i] = np.array(hashes, np.uint64)
+        out["case%d_frame_fnv" % i] = np.uint64(O.fnv(f))
+    out["kinds"] = np.array([k for k, *_ in frames])
+    out["dims"] = np.array([(w, h, seed) for _, w, h, seed, _ in frames], np.int64)
+    np.savez_compressed(os.path.join(HERE, "build_opts.npz"), **out)
 
 
 if __name__ == "__main__":

@@ -53,6 +53,26 @@ def test_host_only_entry_points(vtg_lib):
         assert lib.vtg_tracker_bytes(C.byref(vtg_lib.config(**kw))) == 0, bad
 
 
+def test_contrast_gain_matches_oracle(vtg_lib):
+    """vtg_contrast_gain (the host copy of the function the build options' kernel runs) against the oracle's integer
+    restatement of tk_build's x87 gain and offset, for every byte min / max pair (x 64) and some wider ranges."""
+    import numpy as np
+
+    import oracle as O
+
+    lib = vtg_lib.lib()
+    go = (C.c_float * 2)()
+    pairs = [(64 * a, 64 * b) for a in range(256) for b in range(a, 256)]
+    pairs += [(0, 16777215), (5, 16777215), (123456, 123457), (3, 7), (16000000, 16700001)]
+    for lo, hi in pairs:
+        assert lib.vtg_contrast_gain(lo, hi, go) == 0
+        want = O.contrast_gain(lo, hi)
+        assert np.array(go[:], np.float32).view(np.uint32).tolist() == want.view(np.uint32).tolist(), (lo, hi)
+    assert lib.vtg_contrast_gain(5, 4, go) == vtg_lib.EINVAL
+    assert lib.vtg_contrast_gain(-1, 4, go) == vtg_lib.EINVAL
+    assert lib.vtg_contrast_gain(0, 1 << 24, go) == vtg_lib.EINVAL
+
+
 def test_context_without_gpu_is_refused(vtg_lib):
     import torch
 

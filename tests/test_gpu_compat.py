@@ -91,6 +91,55 @@ def test_compat_pyramid(vtg_lib, torch_cuda, w, h, levels, where):
         assert np.array_equal(planes[lv].get(), ref[lv]), lv
 
 
+@pytest.mark.parametrize("where", ["host", "device"])
+def test_compat_image_kernels_m1(vtg_lib, torch_cuda, golden, where):
+    """img_norm / img_minmax / img_gauss5 / img_sobel / img_absdiff _cuda on the M1 gate's 640 x 480 frame, each over
+    three row ranges as a team would split them, reproduce the gate's hash lines (logs/m1/host/m1-host-640x480.txt);
+    then the stretch tk_build makes (vtg_contrast_gain's gain and offset) against the oracle."""
+    import ctypes as C
+    import json
+
+    L = vtg_lib.compat()
+    with open(os.path.join(golden, "m1_m2.json")) as f:
+        m1 = json.load(f)["m1"]
+    tc = torch_cuda if where == "device" else None
+    w, h = 640, 480
+    q = O.pyramid(O.m1_image(w, h), 1)[0]
+    src = Plane(vtg_lib, w, h, tc)
+    src.set(q)
+    ranges = ((0, 100), (100, 333), (333, h))
+    out = {k: Plane(vtg_lib, w, h, tc) for k in ("norm", "gauss5", "sobel_x", "sobel_y", "absdiff", "stretch")}
+    go = (C.c_float * 2)(0.75, 512.0)
+    for y0, y1 in ranges:
+        L.img_norm_cuda(out["norm"].ref, src.ref, go, y0, y1)
+        assert L.vtg_compat_error() == 0
+        L.img_gauss5_cuda(out["gauss5"].ref, src.ref, y0, y1)
+        assert L.vtg_compat_error() == 0
+        L.img_sobel_cuda(out["sobel_x"].ref, out["sobel_y"].ref, src.ref, y0, y1)
+        assert L.vtg_compat_error() == 0
+    for y0, y1 in ranges:  # the binomial is complete before it is read
+        L.img_absdiff_cuda(out["absdiff"].ref, src.ref, out["gauss5"].ref, y0, y1)
+        assert L.vtg_compat_error() == 0
+    for k in ("norm", "gauss5", "sobel_x", "sobel_y", "absdiff"):
+        assert "%016x" % O.fnv(out[k].get()) == m1[k + " 640x480"], k
+    mm = (C.c_float * 2)()
+    L.img_minmax_cuda(src.ref, mm, 0, h)
+    assert L.vtg_compat_error() == 0 and list(mm) == m1["minmax 640x480"]
+    L.img_minmax_cuda(src.ref, mm, 100, 101)
+    assert list(mm) == list(O.minmax(q[100:101]))
+    g = vtg_lib.contrast_gain(int(m1["minmax 640x480"][0]), int(m1["minmax 640x480"][1]))
+    L.img_norm_cuda(out["stretch"].ref, src.ref, g.ctypes.data, 0, h)
+    assert np.array_equal(out["stretch"].get(), O.norm(q, float(g[0]), float(g[1])))
+    # refusals: sizes that differ, a missing second output, rows outside the plane
+    small = Plane(vtg_lib, w // 2, h, tc)
+    L.img_gauss5_cuda(small.ref, src.ref, 0, 10)
+    assert L.vtg_compat_error() == vtg_lib.EINVAL
+    L.img_sobel_cuda(out["sobel_x"].ref, None, src.ref, 0, 10)
+    assert L.vtg_compat_error() == vtg_lib.EINVAL
+    L.img_minmax_cuda(src.ref, mm, 0, h + 1)
+    assert L.vtg_compat_error() == vtg_lib.EINVAL
+
+
 def test_compat_lk_track_and_flowback(vtg_lib, torch_cuda, golden):
     """lk_track_cuda + lk_flowback_cuda at every 6th of the first configuration's 1,200 cells, host pyramids and
     device pyramids, against the reference's lk_track_vx + lk_flowback_vx (tests/golden/lk_640x480.npz)."""

@@ -30,6 +30,71 @@ def test_pyramid_matches_m1_logs(golden, size):
     assert "%016x" % O.fnv(p[1]) == m1["reduce " + size]
 
 
+@pytest.mark.parametrize("size", ["640x480", "1280x720", "1920x1080"])
+def test_image_kernels_match_m1_logs(golden, size):
+    """The M1 gate's other kernels on its Q6 frame reproduce its hash lines: img_norm with gain / offset (0.75, 512),
+    img_minmax, img_gauss5, img_sobel (x and y) and img_absdiff of the frame and its binomial."""
+    with open(os.path.join(golden, "m1_m2.json")) as f:
+        m1 = json.load(f)["m1"]
+    w, h = map(int, size.split("x"))
+    q = O.pyramid(O.m1_image(w, h), 1)[0]
+    g = O.gauss5(q)
+    ix, iy = O.sobel(q)
+    got = {"norm": O.norm(q, 0.75, 512.0), "gauss5": g, "sobel_x": ix, "sobel_y": iy, "absdiff": O.absdiff(q, g)}
+    for k, plane in got.items():
+        assert "%016x" % O.fnv(plane) == m1[k + " " + size], k
+    assert list(O.minmax(q)) == m1["minmax " + size]
+
+
+@pytest.mark.skipif(not (X86 and np.finfo(np.longdouble).nmant == 63), reason="x87 long double on x86-64 only")
+def test_contrast_gain_is_x87():
+    """tk_build's stretch gain and offset (track.c:603-614), formed by the oracle in exact integer arithmetic, equal the
+    x87 extended computation rounded to F32 (numpy's long double on x86-64 is that format): every byte min / max pair
+    (x 64, the Q6 planes tk_build stretches) and 20,000 other whole-number ranges below 2^24."""
+    lo = np.repeat(np.arange(256), 256) * 64
+    hi = np.tile(np.arange(256), 256) * 64
+    keep = hi >= lo
+    lo, hi = lo[keep], hi[keep]
+    rng = np.random.default_rng(3)
+    rlo = rng.integers(0, 1 << 24, 20000)
+    rhi = np.minimum(rlo + rng.integers(0, 1 << 12, 20000) * rng.integers(1, 4096, 20000), (1 << 24) - 1)
+    lo, hi = np.concatenate([lo, rlo]), np.concatenate([hi, rhi])
+    span = (hi - lo).astype(np.longdouble)
+    gain = np.where(span > 0, np.longdouble(16320) / np.where(span > 0, span, 1), np.longdouble(1))
+    want = np.stack([gain.astype(np.float32), (-lo.astype(np.longdouble) * gain).astype(np.float32)], 1)
+    got = np.stack([O.contrast_gain(a, b) for a, b in zip(lo, hi)])
+    assert got.view(np.uint32).tobytes() == want.view(np.uint32).tobytes()
+
+
+def build_cases(g):
+    """(kind, frame, per-setting level hashes) of tests/golden/build_opts.npz, the frames regenerated."""
+    for i, (kind, (w, h, seed)) in enumerate(zip(g["kinds"], g["dims"])):
+        f = O.m1_image(int(w), int(h)) if kind == "m1" else S.build_frame(str(kind), int(w), int(h), int(seed))
+        assert O.fnv(f) == int(g["case%d_frame_fnv" % i])
+        yield str(kind), f, g["case%d_fnv" % i]
+
+
+def test_build_opts_fixture(golden):
+    """tk_build's optional input steps (contrast stretch, 5 x 5 binomial, both, neither) reproduce the reference's
+    pyramids on six frames (tests/golden/build_opts.npz), every level bit for bit."""
+    for kind, f, want in build_cases(_golden(golden, "build_opts.npz")):
+        for opts in range(4):
+            assert [O.fnv(p) for p in O.pyramid(f, 3, opts)] == [int(v) for v in want[opts]], (kind, opts)
+
+
+@pytest.mark.skipif(not O.ref_available(), reason="the reference tree is not on this machine")
+@pytest.mark.parametrize("w,h,lo,hi,seed", [(96, 64, 0, 255, 1), (112, 77, 30, 31, 2), (48, 41, 200, 255, 3),
+                                            (256, 150, 0, 3, 4), (64, 33, 128, 128, 5)])
+def test_build_opts_against_reference_code(w, h, lo, hi, seed):
+    """The oracle's build options against the reference's own tk_build (x87 and vector kernels) on uniform noise in
+    [lo, hi]: full range, two levels, the top edge, a tiny range, one level."""
+    f = (lo + np.floor(S.uniform(seed, 300, w * h) * (hi - lo + 1))).astype(np.uint8).reshape(h, w)
+    for opts in range(4):
+        want = O.ref_tk_build(f, 3, opts, x87=True)
+        assert [p.tobytes() for p in want] == [p.tobytes() for p in O.ref_tk_build(f, 3, opts, x87=False)]
+        assert [p.tobytes() for p in O.pyramid(f, 3, opts)] == [p.tobytes() for p in want], opts
+
+
 @x86_only
 def test_lk_lane_matches_m2_logs(golden):
     """The lane-model LK reproduces the reference's M2 gate lines (logs/m2/host/640x480.txt) bit for bit: 10 exact
