@@ -332,7 +332,7 @@ __global__ void img_rows_kernel(const float *__restrict__ a, int apitch, const f
         /* img_norm_vx (img_vx.c:49-59): one rounding of the exact value; img_norm_ref's x87 form rounds the same value
          * whenever its extended sum is exact */
         const float v = rintf(__fmaf_rn(A(y, x), gain, offset));
-        *o1 = fminf(fmaxf(v, 0.0f), 16320.0f);
+        *o1 = v < 0.0f ? 0.0f : v > 16320.0f ? 16320.0f : v; /* keeps a -0 from rint, as the reference does */
     } else if (OP == IMG_GAUSS5) {
         /* img_gauss5_ref (img_ref.c:73-96) in its F32 order: vert5 per column, then the horizontal taps, shift8 */
         float v[5];

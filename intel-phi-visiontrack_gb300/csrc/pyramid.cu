@@ -452,7 +452,7 @@ __global__ void __launch_bounds__(256) pyr_input_kernel(const uint8_t *__restric
                                                         const uint32_t *__restrict__ mm, float *__restrict__ l0,
                                                         int pitch)
 {
-    __shared__ int s_lut[256];
+    __shared__ float s_lut[256];
     __shared__ __align__(16) int s_n[PT_Y + 4][PT_X + 4];
     __shared__ __align__(16) int s_v[PT_Y][PT_X + 4];
     const int tid = threadIdx.x;
@@ -464,16 +464,17 @@ __global__ void __launch_bounds__(256) pyr_input_kernel(const uint8_t *__restric
          * bits, the sum's lowest bit is at least 2^-23 and its size below 2^23); one fused multiply-add rounds the
          * same exact value once */
         const float v = rintf(__fmaf_rn((float)(64 * tid), g, o));
-        s_lut[tid] = (int)fminf(fmaxf(v, 0.0f), 16320.0f);
+        /* the reference's select, which keeps the -0 that rint gives a small negative value (the level's bits) */
+        s_lut[tid] = v < 0.0f ? 0.0f : v > 16320.0f ? 16320.0f : v;
     } else {
-        s_lut[tid] = 64 * tid;
+        s_lut[tid] = (float)(64 * tid);
     }
     __syncthreads();
     if (GAUSS) {
         for (int i = tid; i < (PT_Y + 4) * (PT_X + 4); i += blockDim.x) {
             const int r = i / (PT_X + 4), c = i - r * (PT_X + 4);
             const int gy = min(max(oy - 2 + r, 0), h - 1), gx = min(max(ox - 2 + c, 0), w - 1);
-            s_n[r][c] = s_lut[__ldg(src + (size_t)gy * stride + gx)];
+            s_n[r][c] = (int)s_lut[__ldg(src + (size_t)gy * stride + gx)];
         }
         __syncthreads();
         for (int i = tid; i < PT_Y * (PT_X + 4); i += blockDim.x) {
@@ -495,7 +496,7 @@ __global__ void __launch_bounds__(256) pyr_input_kernel(const uint8_t *__restric
                 const int hs = s_v[r][c] + s_v[r][c + 4] + 4 * (s_v[r][c + 1] + s_v[r][c + 3]) + 6 * s_v[r][c + 2];
                 o[e] = small_int_to_float((hs + 128) >> 8);
             } else {
-                o[e] = small_int_to_float(s_lut[__ldg(src + (size_t)gy * stride + min(gx + e, w - 1))]);
+                o[e] = s_lut[__ldg(src + (size_t)gy * stride + min(gx + e, w - 1))];
             }
         }
         float *d = l0 + (size_t)gy * pitch + gx;

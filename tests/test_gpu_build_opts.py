@@ -45,7 +45,7 @@ def test_build_opts_against_oracle(vtg_lib, ctx, w, h, levels, lo, hi):
         t.build(1, f)
         want = O.pyramid(f, levels, opts)
         for L, (a, b) in enumerate(zip(_levels(t, 1, levels), want)):
-            assert np.array_equal(a, b), (opts, L)
+            assert a.tobytes() == b.tobytes(), (opts, L)  # bits: the stretch can leave -0 at the minimum
     t.close()
 
 
@@ -63,13 +63,13 @@ def test_build_opts_frames_in_turn_strided_and_device(vtg_lib, ctx):
         wide[:, :w] = f
         t.build(k & 1, wide, stride=w + 48)
         want = O.pyramid(f, 3, 3)
-        assert all(np.array_equal(a, b) for a, b in zip(_levels(t, k & 1, 3), want)), k
+        assert all(a.tobytes() == b.tobytes() for a, b in zip(_levels(t, k & 1, 3), want)), k
     f = S.build_frame("low", w, h, 9)
     d = torch.from_numpy(f).cuda()
     torch.cuda.synchronize()
     t.set_build(vtg_lib.BUILD_CONTRAST)
     t.build(0, d.data_ptr(), where=vtg_lib.DEVICE)
-    assert all(np.array_equal(a, b) for a, b in zip(_levels(t, 0, 3), O.pyramid(f, 3, 1)))
+    assert all(a.tobytes() == b.tobytes() for a, b in zip(_levels(t, 0, 3), O.pyramid(f, 3, 1)))
     with pytest.raises(vtg_lib.VtgError):
         t.set_build(4)
     t.close()
@@ -115,8 +115,8 @@ def test_build_opts_in_batch_steps(vtg_lib, ctx):
         ctx.sync()
         for k, t in enumerate(trackers):
             levels, (cells, lk) = singles[k]
-            assert all(np.array_equal(a, c) for a, c in zip(_levels(t, 1, 3), levels)), (k, replay)
-            assert all(np.array_equal(a, c) for a, c in zip(_levels(t, 1, 3), O.pyramid(pairs[k][1], 3, opts[k])))
+            assert all(a.tobytes() == c.tobytes() for a, c in zip(_levels(t, 1, 3), levels)), (k, replay)
+            assert all(a.tobytes() == c.tobytes() for a, c in zip(_levels(t, 1, 3), O.pyramid(pairs[k][1], 3, opts[k])))
             gc, gl = vtg_lib.tracker_results(t)
             assert gc.tobytes() == cells.tobytes() and gl.tobytes() == lk.tobytes(), (k, replay)
     b.close()
