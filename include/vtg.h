@@ -148,6 +148,23 @@ int vtg_level_size(const vtg_tracker *t, int level, int *w, int *h);
  * the tracker is destroyed; its contents change with every vtg_build of that set. */
 int vtg_level_device(const vtg_tracker *t, int set, int level, const float **plane, int *w, int *h, int *pitch);
 
+/* The appearance template of a region (store_appearance, src/kern/track.c:935-974), cut from a set's resident
+ * pyramid: the coarsest level where a 32 x 21 template still fits inside the region rw x rh, the 32 x 21 window there
+ * around the centre (cx, cy) (level-0 pixels, truncated to whole pixels of that level), made zero-mean, and its sum of
+ * squares, in the reference's F32 arithmetic bit for bit (its 16-lane sums and folds, the x87 mean). `a` (host memory)
+ * gets the level, the centre's fraction (fx, fy) and `valid`, at once; with valid = 0 (the window does not fit inside
+ * the level's border) nothing is written and nothing runs. Otherwise pix (VTG_APP_W x VTG_APP_H floats, row-major) and
+ * norm (one float) are written in host or device memory as `where` says, complete when the stream is; the pair is
+ * what vtg_search_template takes. */
+#define VTG_APP_W 32
+#define VTG_APP_H 21
+struct vtg_appearance {
+    float fx, fy;
+    int32_t level, valid;
+};
+int vtg_store_appearance(vtg_tracker *t, int set, float cx, float cy, float rw, float rh, float *pix, float *norm,
+                         struct vtg_appearance *a, int where, void *stream);
+
 /* The cell results of a tracker's last vtg_cells or batch step: cols x rows records each (either may be NULL). */
 int vtg_tracker_results(vtg_tracker *t, struct vtg_cell *cells, struct vtg_lk_out *lk, int where, void *stream);
 

@@ -13,6 +13,7 @@
 #include "vtg_ctx.h"
 #include "vtg_internal.cuh"
 #include "vtg_tracker.h"
+#include "x87.cuh"
 
 static thread_local int g_last_cuda = 0;
 
@@ -173,7 +174,7 @@ static int check_config(const vtg_config *c)
 
 struct Layout {
     int lw[VTG_MAX_LEVELS], lh[VTG_MAX_LEVELS], lpitch[VTG_MAX_LEVELS];
-    size_t loff[VTG_MAX_LEVELS], set_floats, staging_off, desc_off, lk_off, cells_off, mm_off, bytes;
+    size_t loff[VTG_MAX_LEVELS], set_floats, staging_off, desc_off, lk_off, cells_off, mm_off, app_off, bytes;
     int cols, rows;
 };
 
@@ -209,6 +210,8 @@ static void layout(const vtg_config *c, Layout *L)
     b += up256(n * sizeof(vtg_cell));
     L->mm_off = b;
     b += up256(2 * VTG_MM_WORDS * sizeof(uint32_t)); /* one block a set, like the staging */
+    L->app_off = b;
+    b += up256((VTG_APP_W * VTG_APP_H + 1) * sizeof(float));
     L->bytes = b;
 }
 
@@ -299,6 +302,7 @@ extern "C" int vtg_tracker_create(vtg_ctx *ctx, const vtg_config *cfg, vtg_track
     t->d_lk = (vtg_lk_out *)(t->mem + L.lk_off);
     t->d_cells = (vtg_cell *)(t->mem + L.cells_off);
     t->d_mm = (uint32_t *)(t->mem + L.mm_off);
+    t->d_app = (float *)(t->mem + L.app_off);
     t->build_opts = 0;
     DevPyr d[4] = {pyr_from(t, 0, 0), pyr_from(t, 0, (int)cfg->flow_level), pyr_from(t, 1, 0),
                    pyr_from(t, 1, (int)cfg->flow_level)};
@@ -484,6 +488,82 @@ extern "C" int vtg_level_device(const vtg_tracker *t, int set, int level, const 
         *h = t->lh[level];
     if (pitch)
         *pitch = t->lpitch[level];
+    return VTG_OK;
+}
+
+/* store_appearance's cut (track.c:947-965) in one warp. Lane l < 16 is the reference's vector lane l: it sums, then
+ * squares, columns l and 16 + l of each row in row order, and the lanes fold as vx_hsum does (i ^ 1, ^ 2, ^ 4, ^ 8).
+ * The sum is a whole number below 2^24 (672 Q6 values), so the mean is the x87 quotient rounded to F32 exactly. */
+__global__ void __launch_bounds__(32) app_kernel(const float *__restrict__ plane, int pitch, float *__restrict__ out)
+{
+    const int lane = threadIdx.x;
+    float s = 0.0f;
+    if (lane < 16)
+        for (int r = 0; r < VTG_APP_H; r++) {
+            const float v0 = plane[(size_t)r * pitch + lane], v1 = plane[(size_t)r * pitch + 16 + lane];
+            out[r * VTG_APP_W + lane] = v0;
+            out[r * VTG_APP_W + 16 + lane] = v1;
+            s = s + v0;
+            s = s + v1;
+        }
+#pragma unroll
+    for (int k = 1; k < 16; k <<= 1)
+        s = s + __shfl_xor_sync(VTG_FULL, s, k);
+    const uint32_t whole = (uint32_t)s; /* exact: a sum of whole numbers below 2^24 */
+    const float mean = whole ? x87_to_f32(x87_div(whole, VTG_APP_W * VTG_APP_H)) : 0.0f;
+    float ss = 0.0f;
+    if (lane < 16)
+        for (int r = 0; r < VTG_APP_H; r++) {
+            const float z0 = out[r * VTG_APP_W + lane] - mean, z1 = out[r * VTG_APP_W + 16 + lane] - mean;
+            out[r * VTG_APP_W + lane] = z0;
+            out[r * VTG_APP_W + 16 + lane] = z1;
+            ss = __fmaf_rn(z0, z0, ss);
+            ss = __fmaf_rn(z1, z1, ss);
+        }
+#pragma unroll
+    for (int k = 1; k < 16; k <<= 1)
+        ss = ss + __shfl_xor_sync(VTG_FULL, ss, k);
+    if (lane == 0)
+        out[VTG_APP_W * VTG_APP_H] = ss;
+}
+
+extern "C" int vtg_store_appearance(vtg_tracker *t, int set, float cx, float cy, float rw, float rh, float *pix,
+                                    float *norm, struct vtg_appearance *a, int where, void *stream)
+{
+    if (!t || !a || set < 0 || set > 1 || (where != VTG_HOST && where != VTG_DEVICE) || !(rw >= 0.0f) ||
+        !(rh >= 0.0f) || !isfinite(cx) || !isfinite(cy))
+        return VTG_EINVAL;
+    /* the coarsest level where the template fits inside the region (track.c:939-941); every quotient is exact */
+    int L = 0;
+    while (L < t->levels - 1 && (double)rw / (double)(1 << (L + 1)) >= VTG_APP_W &&
+           (double)rh / (double)(1 << (L + 1)) >= VTG_APP_H)
+        L++;
+    const double lx = ldexp((double)cx, -L), ly = ldexp((double)cy, -L);
+    if (!(fabs(lx) < 1e9 && fabs(ly) < 1e9))
+        return VTG_EINVAL;
+    const int ix = (int)lx, iy = (int)ly; /* truncation, as the reference's (int) */
+    const int x0 = ix - VTG_APP_W / 2, y0 = iy - VTG_APP_H / 2;
+    a->level = L;
+    a->fx = (float)(lx - ix);
+    a->fy = (float)(ly - iy);
+    a->valid = !(x0 < 1 || y0 < 1 || x0 + VTG_APP_W >= t->lw[L] - 1 || y0 + VTG_APP_H >= t->lh[L] - 1);
+    if (!a->valid)
+        return VTG_OK;
+    if (!pix || !norm)
+        return VTG_EINVAL;
+    const cudaStream_t s = pick(t, stream);
+    const float *plane = t->sets[set] + t->loff[L] + (size_t)y0 * t->lpitch[L] + x0;
+    const size_t n = VTG_APP_W * VTG_APP_H;
+    if (where == VTG_DEVICE && norm == pix + n) {
+        app_kernel<<<1, 32, 0, s>>>(plane, t->lpitch[L], pix);
+        CU(cudaGetLastError());
+        return VTG_OK;
+    }
+    app_kernel<<<1, 32, 0, s>>>(plane, t->lpitch[L], t->d_app);
+    CU(cudaGetLastError());
+    const cudaMemcpyKind k = where == VTG_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+    CU(cudaMemcpyAsync(pix, t->d_app, n * sizeof(float), k, s));
+    CU(cudaMemcpyAsync(norm, t->d_app + n, sizeof(float), k, s));
     return VTG_OK;
 }
 

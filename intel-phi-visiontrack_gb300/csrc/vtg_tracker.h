@@ -27,6 +27,7 @@ struct vtg_tracker {
     vtg_cell *d_cells;    /* cells x vt_cell */
     uint32_t *d_mm;       /* the build options' VTG_MM_WORDS words a set (min / max partials, ticket, gain / offset) */
     int build_opts;       /* VTG_BUILD_CONTRAST | VTG_BUILD_PRE_GAUSS */
+    float *d_app;         /* an appearance template and its norm (VTG_APP_W x VTG_APP_H + 1 floats), for host reads */
     LkPrm prm;
 };
 

@@ -87,8 +87,17 @@ def lib() -> C.CDLL:
         L.vtg_tracker_set_build.argtypes = [vp, i]
         L.vtg_tracker_build_flags.argtypes = [vp]
         L.vtg_contrast_gain.argtypes = [i, i, vp]
+        L.vtg_store_appearance.argtypes = [vp, i, f, f, f, f, vp, vp, C.POINTER(Appearance), i, vp]
         _lib = L
     return _lib
+
+
+APP_W, APP_H = 32, 21
+
+
+class Appearance(C.Structure):
+    """struct vtg_appearance: where store_appearance cut its template."""
+    _fields_ = [("fx", C.c_float), ("fy", C.c_float), ("level", C.c_int32), ("valid", C.c_int32)]
 
 
 def contrast_gain(lo: int, hi: int):
@@ -171,6 +180,17 @@ class Tracker:
             ptr = frame
             stride = self.cfg.width if stride is None else stride
         check(lib().vtg_build(self.h, set_, ptr, stride, where, stream), "vtg_build")
+
+    def store_appearance(self, set_: int, cx: float, cy: float, rw: float, rh: float) -> dict:
+        """store_appearance from a set's resident pyramid: pix (21 x 32), norm, fx, fy, level, valid (host copies)."""
+        a = Appearance()
+        pix = np.zeros((APP_H, APP_W), np.float32)
+        norm = np.zeros(1, np.float32)
+        check(lib().vtg_store_appearance(self.h, set_, cx, cy, rw, rh, pix.ctypes.data, norm.ctypes.data,
+                                         C.byref(a), HOST, None), "vtg_store_appearance")
+        self.sync()
+        return {"pix": pix, "norm": norm[0], "fx": np.float32(a.fx), "fy": np.float32(a.fy), "level": a.level,
+                "valid": bool(a.valid)}
 
     def set_build(self, flags: int):
         """tk_build's optional steps for later builds: BUILD_CONTRAST | BUILD_PRE_GAUSS (0: neither)."""

@@ -96,6 +96,8 @@ def lib() -> C.CDLL:
         _lib.or_absdiff.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int]
         _lib.or_contrast_gain.argtypes = [C.c_int, C.c_int, C.c_void_p]
         _lib.or_build_input.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int]
+        _lib.or_store_appearance.argtypes = [C.POINTER(Pyr), C.c_float, C.c_float, C.c_float, C.c_float, C.c_void_p,
+                                             C.c_void_p]
         _lib.or_m1_image.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int]
         _lib.or_m2_render.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]
         _lib.or_cell_centre.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(LkCfg), C.c_int, C.c_int,
@@ -215,6 +217,9 @@ def ref() -> C.CDLL:
                                        C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]
         _ref.ref_pyramid.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p]
         _ref.ref_tk_build.restype = C.c_int
+        _ref.ref_store_appearance.restype = C.c_int
+        _ref.ref_store_appearance.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float,
+                                              C.c_float, C.c_void_p, C.c_void_p]
         _ref.ref_tk_build.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p]
         _ref.ref_still_vectors.restype = C.c_int
         _ref.ref_still_vectors.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p]
@@ -338,6 +343,33 @@ def ref_tk_build(frame: np.ndarray, levels: int, opts: int = 0, x87: bool = Fals
         planes.append(out[off:off + lw * lh].reshape(lh, lw))
         off += lw * lh
     return planes
+
+
+APP_W, APP_H = 32, 21
+
+
+def _app_result(pix, info):
+    return {"pix": pix, "norm": np.float32(info[0]), "fx": np.float32(info[1]), "fy": np.float32(info[2]),
+            "level": int(info[3]), "valid": bool(info[4])}
+
+
+def store_appearance(levels_list, cx: float, cy: float, rw: float, rh: float) -> dict:
+    """store_appearance on a pyramid (list of planes): pix (21 x 32 float32), norm, fx, fy, level, valid."""
+    p = make_pyr(levels_list)
+    pix = np.zeros((APP_H, APP_W), np.float32)
+    info = np.zeros(5, np.float32)
+    lib().or_store_appearance(C.byref(p), cx, cy, rw, rh, _p(pix), _p(info))
+    return _app_result(pix, info)
+
+
+def ref_store_appearance(frame: np.ndarray, levels: int, cx: float, cy: float, rw: float, rh: float) -> dict:
+    """The reference's own store_appearance on the pyramid its tk_build makes of `frame` (width a multiple of 16)."""
+    frame = np.ascontiguousarray(frame, dtype=np.uint8)
+    h, w = frame.shape
+    pix = np.zeros((APP_H, APP_W), np.float32)
+    info = np.zeros(5, np.float32)
+    assert ref().ref_store_appearance(_p(frame), w, h, levels, cx, cy, rw, rh, _p(pix), _p(info)) == 0
+    return _app_result(pix, info)
 
 
 def make_pyr(levels_list) -> Pyr:

@@ -111,3 +111,42 @@ int ref_tk_build(const uint8_t *frame, int w, int h, int levels, int contrast, i
     }
     return 0;
 }
+
+/* store_appearance (track.c:935-974) on the pyramid tk_build makes of a frame (w a multiple of 16, rows w bytes apart),
+ * for the region centred at (cx, cy) of size rw x rh: the template into pix (32 x 21) and info = norm, fx, fy, level,
+ * valid. Returns 0, or -1 when the tracker cannot be made. */
+int ref_store_appearance(const uint8_t *frame, int w, int h, int levels, float cx, float cy, float rw, float rh,
+                         float *pix, float *info)
+{
+    struct vt_config cfg;
+    memset(&cfg, 0, sizeof cfg);
+    cfg.width = (uint32_t)w;
+    cfg.height = (uint32_t)h;
+    cfg.levels = (uint32_t)levels;
+    cfg.patch_w = 21;
+    cfg.patch_h = 21;
+    cfg.max_iter = 10;
+    cfg.pipelines = 1;
+    struct tracker *t = tk_create(&cfg, 1, 1, tu_alloc, NULL, tu_run, NULL, tu_run, NULL);
+    if (!t)
+        return -1;
+    struct vt_msg m;
+    memset(&m, 0, sizeof m);
+    m.algorithm = VT_ALG_MVEX;
+    tk_build(t, 0, frame, NULL, &m);
+    t->cur = 0;
+    t->cx = cx;
+    t->cy = cy;
+    t->rw = rw;
+    t->rh = rh;
+    store_appearance(t, 0);
+    const struct app_slot *a = &t->app[0];
+    if (a->valid)
+        memcpy(pix, a->pix, sizeof(float) * APP_W * APP_H);
+    info[0] = a->norm;
+    info[1] = a->fx;
+    info[2] = a->fy;
+    info[3] = (float)a->level;
+    info[4] = (float)a->valid;
+    return 0;
+}

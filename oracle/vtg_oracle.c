@@ -877,6 +877,21 @@ double or_peak_offset(double l, double c, double r)
 
 /* The zero-mean template store_appearance cuts (src/kern/track.c:935-974): T_w x T_h pixels at corner (x0, y0), their
  * mean (lane sums, long double division) taken off, norm = the lane-folded sum of squares. */
+/* (float)((long double)sum / n), the x87 quotient rounded to F32, for a whole-number sum: exact integer arithmetic, so
+ * the same on every host. Other sums go through the host's long double. */
+static float x87_mean(float sum, int n)
+{
+    if (sum == 0.0f)
+        return 0.0f;
+    if (!(sum > 0.0f && sum == floorf(sum)))
+        return (float)((long double)sum / (long double)n);
+    uint64_t m, fm;
+    int e, fe;
+    x87_quot((unsigned __int128)sum, (unsigned __int128)n, &m, &e);
+    round_bits(m, e, 24, &fm, &fe);
+    return ldexpf((float)fm, fe);
+}
+
 void or_cut_template(const struct or_img *m, int x0, int y0, int tw, int th, float *app, float *norm)
 {
     float sum[16] = {0};
@@ -886,7 +901,7 @@ void or_cut_template(const struct or_img *m, int x0, int y0, int tw, int th, flo
             app[r * tw + k] = v;
             sum[k & 15] = sum[k & 15] + v;
         }
-    const float mean = (float)((long double)hsum16(sum) / (long double)(tw * th));
+    const float mean = x87_mean(hsum16(sum), tw * th);
     float ss[16] = {0};
     for (int r = 0; r < th; r++)
         for (int k = 0; k < tw; k++) {
@@ -895,6 +910,29 @@ void or_cut_template(const struct or_img *m, int x0, int y0, int tw, int th, flo
             ss[k & 15] = fmaf(z, z, ss[k & 15]);
         }
     *norm = hsum16(ss);
+}
+
+/* store_appearance (src/kern/track.c:935-974) on a pyramid: the coarsest level where a 32 x 21 template fits inside
+ * the region rw x rh, the window around the centre (cx, cy) there (truncated to whole pixels), zero-mean, and its sum
+ * of squares. info: norm, fx, fy, level, valid (valid 0: the window leaves the level's border; app untouched). */
+void or_store_appearance(const struct or_pyr *p, float cx, float cy, float rw, float rh, float *app, float info[5])
+{
+    enum { AW = 32, AH = 21 };
+    int L = 0;
+    while (L < p->levels - 1 && (double)rw / (double)(1 << (L + 1)) >= AW && (double)rh / (double)(1 << (L + 1)) >= AH)
+        L++;
+    const double lx = ldexp((double)cx, -L), ly = ldexp((double)cy, -L);
+    const int ix = (int)lx, iy = (int)ly;
+    const int x0 = ix - AW / 2, y0 = iy - AH / 2;
+    info[1] = (float)(lx - ix);
+    info[2] = (float)(ly - iy);
+    info[3] = (float)L;
+    info[4] = 0.0f;
+    if (x0 < 1 || y0 < 1 || x0 + AW >= p->w[L] - 1 || y0 + AH >= p->h[L] - 1)
+        return;
+    const struct or_img m = {p->lv[L], p->w[L], p->h[L], p->stride[L]};
+    or_cut_template(&m, x0, y0, AW, AH, app, &info[0]);
+    info[4] = 1.0f;
 }
 
 /* What one search found (struct found, src/kern/track.c:1608-1612): the best corner in half pixels, its score, the best

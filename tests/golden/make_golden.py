@@ -19,6 +19,7 @@ Writes:
                     corners found.
   still.npz         the still picture (still_vectors, still_decide, still_update, still_finish) over a 12-frame
                     320 x 240 sequence: per frame the cells after the decision, still_motion and still_hash.
+  appearance.npz    store_appearance on two frames' pyramids, 60 regions each: validity, level, fraction, norm, hash.
   build_opts.npz    tk_build with the contrast stretch and / or the 5 x 5 binomial on six frames: per-level hashes.
   framegen.npz      frame generation (framegen.c as tk_generate_make runs it) on three pairs: the fields of every
                     level, the middle-instant field, hashes of the generated frame and its bytes, the scene verdict.
@@ -152,6 +153,7 @@ def main(ref_root: str = "/root/reference") -> None:
     write_still()
     write_framegen()
     write_build_opts()
+    write_appearance()
     print("golden fixtures written to", HERE)
 
 
@@ -218,6 +220,34 @@ def write_build_opts() -> None:
     out["kinds"] = np.array([k for k, *_ in frames])
     out["dims"] = np.array([(w, h, seed) for _, w, h, seed, _ in frames], np.int64)
     np.savez_compressed(os.path.join(HERE, "build_opts.npz"), **out)
+
+
+APP_CASES = [(640, 480, 3, 1), (1920, 1080, 4, 2)]
+
+
+def write_appearance() -> None:
+    """appearance.npz: the reference's store_appearance on the pyramids its tk_build makes of two frames, for 60 seeded
+    regions each (centres past the borders included): valid, level, fx, fy, norm and a hash of the template."""
+    out = {}
+    for i, (w, h, levels, seed) in enumerate(APP_CASES):
+        f = S.build_frame("warp", w, h, seed)
+        u = S.uniform(seed, 400, 4 * 60).reshape(60, 4)
+        reg = np.stack([-20 + u[:, 0] * (w + 40), -20 + u[:, 1] * (h + 40), 10 + u[:, 2] * (w / 2 - 10),
+                        10 + u[:, 3] * (h / 2 - 10)], 1).astype(np.float32)
+        rows = []
+        for cx, cy, rw, rh in reg:
+            r = O.ref_store_appearance(f, levels, float(cx), float(cy), float(rw), float(rh))
+            rows.append((r["valid"], r["level"] if r["valid"] else -1, r["fx"] if r["valid"] else 0.0,
+                         r["fy"] if r["valid"] else 0.0, r["norm"] if r["valid"] else 0.0,
+                         O.fnv(r["pix"]) if r["valid"] else 0))
+        out["case%d_frame_fnv" % i] = np.uint64(O.fnv(f))
+        out["case%d_regions" % i] = reg
+        out["case%d_valid" % i] = np.array([r[0] for r in rows], np.int32)
+        out["case%d_level" % i] = np.array([r[1] for r in rows], np.int32)
+        out["case%d_f" % i] = np.array([(r[2], r[3], r[4]) for r in rows], np.float32)
+        out["case%d_pix_fnv" % i] = np.array([r[5] for r in rows], np.uint64)
+    out["cases"] = np.array(APP_CASES, np.int64)
+    np.savez_compressed(os.path.join(HERE, "appearance.npz"), **out)
 
 
 if __name__ == "__main__":

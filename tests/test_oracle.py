@@ -95,6 +95,47 @@ def test_build_opts_against_reference_code(w, h, lo, hi, seed):
         assert [p.tobytes() for p in O.pyramid(f, 3, opts)] == [p.tobytes() for p in want], opts
 
 
+def appearance_cases(g):
+    """(levels, pyramid planes, regions, fixture rows) of tests/golden/appearance.npz, the frames regenerated."""
+    for i, (w, h, levels, seed) in enumerate(g["cases"]):
+        f = S.build_frame("warp", int(w), int(h), int(seed))
+        assert O.fnv(f) == int(g["case%d_frame_fnv" % i])
+        yield int(levels), f, O.pyramid(f, int(levels)), g["case%d_regions" % i], i
+
+
+def test_appearance_fixture(golden):
+    """store_appearance (track.c:935-974) restated: validity, level, fraction, norm and template equal the reference's
+    on 120 regions of two frames (tests/golden/appearance.npz)."""
+    g = _golden(golden, "appearance.npz")
+    for levels, f, P, regions, i in appearance_cases(g):
+        for k, (cx, cy, rw, rh) in enumerate(regions):
+            a = O.store_appearance(P, float(cx), float(cy), float(rw), float(rh))
+            assert int(a["valid"]) == int(g["case%d_valid" % i][k]), (i, k)
+            if a["valid"]:
+                assert a["level"] == int(g["case%d_level" % i][k])
+                fx, fy, norm = g["case%d_f" % i][k]
+                assert (a["fx"], a["fy"]) == (fx, fy) and a["norm"].tobytes() == norm.tobytes()
+                assert O.fnv(a["pix"]) == int(g["case%d_pix_fnv" % i][k])
+
+
+@pytest.mark.skipif(not O.ref_available(), reason="the reference tree is not on this machine")
+def test_appearance_against_reference_code():
+    """The restatement against the reference's own store_appearance on 300 random regions of a 208 x 133 frame's
+    two-level pyramid and of a low-contrast 640 x 480 frame stretched by tk_build's contrast step."""
+    for (w, h, levels, kind) in ((208, 133, 2, "warp"), (640, 480, 3, "low")):
+        f = S.build_frame(kind, w, h, 7)
+        P = O.pyramid(f, levels)
+        u = S.uniform(7, 500, 4 * 300).reshape(300, 4)
+        for cx, cy, rw, rh in np.stack([-20 + u[:, 0] * (w + 40), -20 + u[:, 1] * (h + 40), 10 + u[:, 2] * w / 2,
+                                        10 + u[:, 3] * h / 2], 1).astype(np.float32):
+            a = O.store_appearance(P, float(cx), float(cy), float(rw), float(rh))
+            r = O.ref_store_appearance(f, levels, float(cx), float(cy), float(rw), float(rh))
+            assert a["valid"] == r["valid"]
+            if a["valid"]:
+                assert (a["level"], a["fx"], a["fy"]) == (r["level"], r["fx"], r["fy"])
+                assert a["pix"].tobytes() == r["pix"].tobytes() and a["norm"].tobytes() == r["norm"].tobytes()
+
+
 @x86_only
 def test_lk_lane_matches_m2_logs(golden):
     """The lane-model LK reproduces the reference's M2 gate lines (logs/m2/host/640x480.txt) bit for bit: 10 exact
