@@ -88,6 +88,11 @@ void vtg_ctx_destroy(vtg_ctx *ctx);
 size_t vtg_ctx_used(const vtg_ctx *ctx);
 /* Waits for all of the context's work, at most timeout_ms (VTG_ETIMEOUT after that). */
 int vtg_ctx_sync(vtg_ctx *ctx, int timeout_ms);
+/* The bounds record of the checked build (libvtg_checked.so, built with VTG_CHECKED): after the device is idle,
+ * out[0] = the LK patch operations whose pixel rectangle would have left its level (bit 1 template build, 2 window
+ * pass, 4 sample pass), out[1] = how many times; then clears it. Returns 1 in the checked build, 0 (out zeroed) in the
+ * production build, which has no checks. */
+int vtg_check_read(uint32_t *out);
 
 /* ---- a tracker: one camera stream's device-resident state (tk_create, src/kern/track.h:22 / track.c:447-572) ---- */
 

@@ -25,6 +25,57 @@
 #define LK_GRAD_SCALE (1.0f / 512.0f)
 #define LK_Q6_INV (1.0f / 64.0f)
 
+/* The checked build (-DVTG_CHECKED: vtg_build.py's libvtg_checked.so). Each patch operation first tests the rectangle
+ * of pixels its loads touch against the level; one that would leave the level records its site in g_vtg_check (bit 1
+ * the template build, 2 the window pass, 4 the sample pass) and returns zero sums without reading. The production build
+ * has no test: the driver's bounds tests keep every rectangle inside the level by construction, and the checked build
+ * is how the tests confirm it. */
+#ifdef VTG_CHECKED
+__device__ unsigned int g_vtg_check[2]; /* failed sites (bits), failures */
+
+__device__ __forceinline__ bool lk_window_ok(const DevLevel &L, int x0, int x1, int y0, int y1, unsigned site)
+{
+    if (x0 >= 0 && y0 >= 0 && x1 < L.w && y1 < L.h)
+        return true;
+    if ((threadIdx.x & 31) == 0) {
+        atomicOr(&g_vtg_check[0], site);
+        atomicAdd(&g_vtg_check[1], 1u);
+    }
+    return false;
+}
+#define LK_CHECK_WINDOW(L, x0, x1, y0, y1, site, ...)                                                                   \
+    do {                                                                                                               \
+        if (!lk_window_ok(L, x0, x1, y0, y1, site)) {                                                                  \
+            __VA_ARGS__;                                                                                               \
+            return;                                                                                                    \
+        }                                                                                                              \
+    } while (0)
+#else
+#define LK_CHECK_WINDOW(L, x0, x1, y0, y1, site, ...)                                                                   \
+    do {                                                                                                               \
+    } while (0)
+#endif
+
+extern "C" int vtg_check_read(uint32_t *out)
+{
+    if (!out)
+        return VTG_EINVAL;
+    out[0] = out[1] = 0;
+#ifdef VTG_CHECKED
+    unsigned h[2] = {0u, 0u};
+    if (cudaDeviceSynchronize() != cudaSuccess || cudaMemcpyFromSymbol(h, g_vtg_check, sizeof h) != cudaSuccess)
+        return VTG_ECUDA;
+    const unsigned z[2] = {0u, 0u};
+    if (cudaMemcpyToSymbol(g_vtg_check, z, sizeof z) != cudaSuccess)
+        return VTG_ECUDA;
+    out[0] = h[0];
+    out[1] = h[1];
+    return 1;
+#else
+    return 0;
+#endif
+}
+
 /* Two floats in one 64-bit register (lo, hi), for the packed FP32 pair instructions (add/sub/mul/fma .f32x2): one
  * instruction moves two independent row chains of a patch. Each half rounds like its scalar instruction. */
 typedef unsigned long long f2_t;
@@ -192,6 +243,7 @@ __device__ __forceinline__ void lk_build(const DevLevel &L, int ix, float fx, in
     constexpr int HH = MAXH / 2;
     const int H = EXACT ? MAXH : Hr;
     const int x0 = ix - W / 2, y0 = iy - H / 2;
+    LK_CHECK_WINDOW(L, x0 - 1, x0 + W + 1, y0 - 1, y0 + H + 1, 1u, gxx = gxy = gyy = tco = cxo = cyo = 0.0f);
     /* Lane c samples window column c - 1 (c = 0 .. W + 1; lane W + 2 feeds lane W + 1's right neighbour; the lanes past
      * it read a clamped column and feed nothing). Patch columns are lanes 1 .. W; the others' sums are dropped before
      * the fold. */
@@ -322,6 +374,7 @@ __device__ __forceinline__ void lk_correlate(const DevLevel &L, int jx, int jy, 
     constexpr int HH = MAXH / 2;
     const int H = EXACT ? MAXH : Hr;
     const int x0 = jx - W / 2, y0 = jy - H / 2;
+    LK_CHECK_WINDOW(L, x0 - 1, x0 + W, y0, y0 + H, 2u, for (int k = 0; k < 8; k++) X[k] = 0.0f);
     const bool act = lane >= 1 && lane <= W;
     const float *col = L.p + (size_t)y0 * L.pitch + (x0 - 1 + min(lane, W + 1));
     const float *ra = col;
@@ -408,6 +461,7 @@ __device__ __forceinline__ void lk_sample(const DevLevel &L, int jx, float fx, i
     constexpr int HH = MAXH / 2;
     const int H = EXACT ? MAXH : Hr;
     const int x0 = jx - W / 2, y0 = jy - H / 2;
+    LK_CHECK_WINDOW(L, x0 - 1, x0 + W, y0, y0 + H, 4u, b0 = b1 = 0.0f);
     const bool act = lane >= 1 && lane <= W;
     const float q6 = act ? LK_Q6_INV : 0.0f;
     const float *col = L.p + (size_t)y0 * L.pitch + (x0 - 1 + min(lane, W + 1));

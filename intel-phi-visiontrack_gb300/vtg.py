@@ -13,7 +13,8 @@ import weakref
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libvtg.so")
+# VTG_LIB names another build of the library (the bounds-checked libvtg_checked.so) for this process
+LIB_PATH = os.environ.get("VTG_LIB") or os.path.join(HERE, "libvtg.so")
 
 OK, EINVAL, ENOMEM, ECUDA, ETIMEOUT, EBUSY, ENODEV, EBUDGET = 0, -1, -2, -3, -4, -5, -6, -7
 HOST, DEVICE = 0, 1
@@ -88,6 +89,7 @@ def lib() -> C.CDLL:
         L.vtg_tracker_build_flags.argtypes = [vp]
         L.vtg_contrast_gain.argtypes = [i, i, vp]
         L.vtg_store_appearance.argtypes = [vp, i, f, f, f, f, vp, vp, C.POINTER(Appearance), i, vp]
+        L.vtg_check_read.argtypes = [vp]
         _lib = L
     return _lib
 

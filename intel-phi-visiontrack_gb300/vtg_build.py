@@ -17,6 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 HOST = os.path.join(HERE, "host")
 OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libvtg.so")
+CHECKED_LIB = os.path.join(HERE, "libvtg_checked.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -53,17 +54,22 @@ def _compile(cmd):
     return r.stderr
 
 
-def build(verbose: bool = False, extra=()) -> str:
-    os.makedirs(OBJ, exist_ok=True)
+def build(verbose: bool = False, extra=(), checked: bool = False) -> str:
+    """libvtg.so; with checked=True the separate libvtg_checked.so, whose LK patch operations test every window they
+    read against the level's bounds and record a failure instead of reading (-DVTG_CHECKED)."""
+    obj_dir = OBJ + "_checked" if checked else OBJ
+    lib = CHECKED_LIB if checked else LIB
+    extra = tuple(extra) + (("-DVTG_CHECKED",) if checked else ())
+    os.makedirs(obj_dir, exist_ok=True)
     nvcc = _nvcc()
     jobs, objs = [], []
     for src in sorted(glob.glob(os.path.join(CSRC, "*.cu"))):
-        obj = os.path.join(OBJ, os.path.basename(src)[:-3] + ".o")
+        obj = os.path.join(obj_dir, os.path.basename(src)[:-3] + ".o")
         objs.append(obj)
         if _stale(obj, src):
             jobs.append([nvcc, *ARCH, *NVFLAGS, *extra, "-c", src, "-o", obj])
     for src in sorted(glob.glob(os.path.join(HOST, "*.c"))):
-        obj = os.path.join(OBJ, os.path.basename(src)[:-2] + ".o")
+        obj = os.path.join(obj_dir, os.path.basename(src)[:-2] + ".o")
         objs.append(obj)
         if _stale(obj, src):
             jobs.append(["cc", *CFLAGS, "-I" + "/usr/local/cuda/include", "-c", src, "-o", obj])
@@ -71,10 +77,10 @@ def build(verbose: bool = False, extra=()) -> str:
         for log in ex.map(_compile, jobs):
             if verbose and log:
                 print(log, file=sys.stderr)
-    if jobs or not os.path.exists(LIB):
-        cmd = [nvcc, *ARCH, "-shared", "-o", LIB, *objs, "-lcudart", "-lpthread"]
+    if jobs or not os.path.exists(lib):
+        cmd = [nvcc, *ARCH, "-shared", "-o", lib, *objs, "-lcudart", "-lpthread"]
         _compile(cmd)
-    return LIB
+    return lib
 
 
 if __name__ == "__main__":
