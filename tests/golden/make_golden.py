@@ -58,7 +58,20 @@ def parse_logs(ref_root: str) -> dict:
     with open(os.path.join(ref_root, "logs", "m2", "host", "640x480.txt")) as f:
         for line in f:
             m2.append(line.rstrip("\n"))
-    return {"m1": m1, "m2": m2}
+    # the M2 pattern's accuracy against exact truth (docs/measurements.md, the table under "Displacement, px"):
+    # displacement, points with status OK of 330, EPE median / p95 / max
+    acc = []
+    with open(os.path.join(ref_root, "docs", "measurements.md")) as f:
+        lines = f.read().splitlines()
+    start = next(i for i, line in enumerate(lines) if line.startswith("| Displacement, px"))
+    for line in lines[start + 2:]:
+        if not line.startswith("|"):
+            break
+        cols = [c.strip().strip("*") for c in line.strip("|").split("|")]
+        d = [float(v) for v in cols[0].strip("()").split(",")]
+        ok = int(cols[1].split("/")[0])
+        acc.append({"d": d, "ok": ok, "median": float(cols[2]), "p95": float(cols[3]), "max": float(cols[4])})
+    return {"m1": m1, "m2": m2, "m2_accuracy": acc}
 
 
 def frames_1080():

@@ -156,6 +156,42 @@ def test_still_vectors_config(vtg_lib, ctx, golden):
     t.close()
 
 
+def test_m2_accuracy_against_exact_truth(vtg_lib, ctx, golden):
+    """The reference's accuracy table against exact truth (docs/measurements.md:93-104; the M2 gate's ten quarter-pixel
+    displacements of its pattern, 330 points, 21 x 21, eps 0.005, 4 levels) through vtg_points: as many points with
+    status OK (within 3, where a point sits on a threshold), and EPE median / p95 / max within 0.002 / 0.003 / 0.005 px
+    of the table's on every displacement the reference tracks in full. On the last one, where the reference loses 27
+    tracks to the pattern's repeats, the points both call good agree with the FP64 oracle within 0.01 px."""
+    import json
+
+    from test_oracle import m2_case_stats, m2_points
+
+    with open(os.path.join(golden, "m1_m2.json")) as f:
+        table = json.load(f)["m2_accuracy"]
+    xs, ys = m2_points()
+    cfg = O.lk_cfg(21, 21, 10, 0.005, 0.1, 40.0)
+    t = _tracker(vtg_lib, ctx, 640, 480, levels=4, eps=0.005, max_residual=40.0, fb_max=0.0)
+    f0 = O.m2_render(640, 480, 2048, 2048)
+    t.build(0, f0)
+    P0 = O.pyramid(f0, 4)
+    for row in table:
+        dx, dy = int(round(4 * row["d"][0])), int(round(4 * row["d"][1]))
+        f1 = O.m2_render(640, 480, 2048 - dx, 2048 - dy)
+        t.build(1, f1)
+        out = t.points(0, 1, xs, ys)
+        n, med, p95, mx = m2_case_stats(out, xs, ys, dx, dy)
+        assert abs(n - row["ok"]) <= 3, (row, n)
+        if row["ok"] == len(xs):
+            assert n == row["ok"]
+            assert abs(med - row["median"]) <= 0.002 and abs(p95 - row["p95"]) <= 0.003, (row, med, p95)
+            assert abs(mx - row["max"]) <= 0.005, (row, mx)
+        else:
+            ref = O.lk_points(P0, O.pyramid(f1, 4), 3, cfg, xs, ys, mode=O.F64)
+            ok, err = _flow_err(out, ref)
+            assert err <= TOL_PX and np.mean(out["status"] == ref["status"]) >= 0.99
+    t.close()
+
+
 def test_repeatable_and_set_order(vtg_lib, ctx):
     """Same inputs, same bits, run after run; and the sets are symmetric (build order does not matter)."""
     f0, f1, _, _ = S.warp_pair(320, 240, (1.0, 0.5), 0.5, seed=3)

@@ -163,6 +163,42 @@ def test_lk_lane_matches_m2_logs(golden):
     assert lines == m2
 
 
+def m2_case_stats(out, xs, ys, dx, dy):
+    """The M2 gate's accuracy line (src/card/m2_gate.c:145-164): points with status OK, and the EPE median, p95 and max
+    against the exact displacement (dx, dy) / 4, as epe[ok / 2], epe[ok * 95 / 100] of the sorted F32 errors."""
+    ok = out["status"] == 0
+    ex = out["x"].astype(np.float64) - (xs.astype(np.float64) + 0.25 * dx)
+    ey = out["y"].astype(np.float64) - (ys.astype(np.float64) + 0.25 * dy)
+    e64 = np.sqrt(ex * ex + ey * ey)[ok]
+    e = np.sort(e64.astype(np.float32))
+    n = len(e)
+    return n, float(e[n // 2]), float(e[n * 95 // 100]), float(e64.max())
+
+
+def m2_points():
+    w, h, margin = 640, 480, 40 + 21
+    pts = [(x, y) for y in range(margin, h - margin, 24) for x in range(margin, w - margin, 24)]
+    return np.array([p[0] for p in pts], np.float32), np.array([p[1] for p in pts], np.float32)
+
+
+@x86_only
+def test_lk_lane_matches_m2_accuracy_table(golden):
+    """The lane model reproduces the reference's accuracy table against exact truth (docs/measurements.md:93-104: ten
+    quarter-pixel displacements of the M2 pattern, 330 points): status-OK counts, EPE median, p95 and max to the
+    printed 4 decimals."""
+    with open(os.path.join(golden, "m1_m2.json")) as f:
+        table = json.load(f)["m2_accuracy"]
+    cfg = O.lk_cfg(21, 21, 10, 0.005, 0.1, 40.0)
+    xs, ys = m2_points()
+    p0 = O.pyramid(O.m2_render(640, 480, 2048, 2048), 4)
+    for row in table:
+        dx, dy = int(round(4 * row["d"][0])), int(round(4 * row["d"][1]))
+        p1 = O.pyramid(O.m2_render(640, 480, 2048 - dx, 2048 - dy), 4)
+        n, med, p95, mx = m2_case_stats(O.lk_points(p0, p1, 3, cfg, xs, ys, mode=O.LANE), xs, ys, dx, dy)
+        assert n == row["ok"], row
+        assert ["%.4f" % v for v in (med, p95, mx)] == ["%.4f" % row[k] for k in ("median", "p95", "max")], row
+
+
 def test_m2_f64_accuracy_against_exact_truth():
     """The FP64 oracle recovers the M2 pattern's exact quarter-pixel displacements to within 0.05 px (the reference's
     own accuracy table, docs/measurements.md:93-104, reads EPE medians of 0.007-0.012 px)."""
