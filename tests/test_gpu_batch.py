@@ -140,3 +140,54 @@ def test_batch_refuses_mixed_settings_and_repeats(vtg_lib, ctx, batch_setup):
     with pytest.raises(vtg_lib.VtgError):
         b.prepare(0, [trackers[0], trackers[0]], [dev[0][0].data_ptr()] * 2, [0, 0])
     other.close()
+
+
+def test_batch_at_its_maximum_of_512_streams(vtg_lib, ctx):
+    """The largest batch (512 streams, the LK launch's job table at its limit) of small uneven frames, host frames,
+    launched and replayed: every stream's cells equal its single-stream vtg_cells; a batch of 513 is refused."""
+    import ctypes as C
+
+    h = C.c_void_p()
+    assert vtg_lib.lib().vtg_batch_create(ctx.h, 513, C.byref(h)) == vtg_lib.EINVAL
+    sizes = [(32 + 8 * (k % 5), 32 + 4 * (k % 7)) for k in range(512)]
+    frames = []
+    for k, (w, h_) in enumerate(sizes):
+        f0, f1, _, _ = S.warp_pair(w, h_, (0.7 + 0.01 * (k % 9), -0.4), 0.3, seed=1000 + k)
+        frames.append((f0, f1))
+    cfg = dict(levels=2, patch_w=7, patch_h=7, cell_w=8, cell_h=8)
+    singles = []
+    for (w, h_), (f0, f1) in zip(sizes[:64], frames[:64]):  # the single-stream results of a sample
+        t = vtg_lib.Tracker(ctx, vtg_lib.config(w, h_, **cfg))
+        t.build(0, f0)
+        t.build(1, f1)
+        singles.append(t.cells(0, 1))
+        t.close()
+    trackers = [vtg_lib.Tracker(ctx, vtg_lib.config(w, h_, **cfg)) for (w, h_) in sizes]
+    b = vtg_lib.Batch(ctx, 512)
+    b.prepare(0, trackers, [f0 for f0, _ in frames], [0] * 512, where=vtg_lib.HOST)
+    b.prepare(1, trackers, [f1 for _, f1 in frames], [1] * 512, where=vtg_lib.HOST)
+    assert b.cells(1) == sum(t.cols * t.rows for t in trackers)
+    for replay in (False, True):
+        if replay:
+            b.capture(0)
+            b.capture(1)
+            b.replay(0)
+            b.replay(1)
+        else:
+            b.launch(0)
+            b.launch(1)
+        ctx.sync()
+        _check(vtg_lib, trackers[:64], singles)
+    # the rest against the oracle's pyramid and the single-stream code path once more, spread over the batch
+    for k in range(64, 512, 37):
+        t = vtg_lib.Tracker(ctx, vtg_lib.config(*sizes[k], **cfg))
+        t.build(0, frames[k][0])
+        t.build(1, frames[k][1])
+        c_ref, l_ref = t.cells(0, 1)
+        t.close()
+        c, l = vtg_lib.tracker_results(trackers[k])
+        assert c.tobytes() == c_ref.tobytes() and l.tobytes() == l_ref.tobytes(), k
+        assert np.array_equal(trackers[k].level(1, 1), O.pyramid(frames[k][1], 2)[1])
+    b.close()
+    for t in trackers:
+        t.close()
