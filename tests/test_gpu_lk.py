@@ -208,6 +208,35 @@ def test_repeatable_and_set_order(vtg_lib, ctx):
     t.close()
 
 
+def test_concurrent_streams_same_bits(vtg_lib, ctx):
+    """Four trackers working at once, each on its own CUDA stream with nothing between them, give the same bits as the
+    same work one tracker after another (the GPU form of the reference's team-size invariance)."""
+    sizes = [(640, 480), (333, 199), (1280, 720), (97, 61)]
+    pairs = [S.warp_pair(w, h, S.seeded_shift(60 + k, 0), 0.5, seed=60 + k)[:2] for k, (w, h) in enumerate(sizes)]
+    alone = []
+    for (w, h), (f0, f1) in zip(sizes, pairs):
+        t = _tracker(vtg_lib, ctx, w, h, levels=3, cell_w=8, cell_h=8)
+        t.build(0, f0)
+        t.build(1, f1)
+        alone.append(t.cells(0, 1))
+        t.close()
+    ts = [_tracker(vtg_lib, ctx, w, h, levels=3, cell_w=8, cell_h=8) for (w, h) in sizes]
+    outs = []
+    for t, (f0, f1) in zip(ts, pairs):  # enqueue everything first, read afterwards
+        t.build(0, f0)
+        t.build(1, f1)
+        n = t.cols * t.rows
+        c = np.zeros(n, vtg_lib.CELL_DTYPE)
+        lk = np.zeros(n, vtg_lib.LK_OUT_DTYPE)
+        vtg_lib.check(vtg_lib.lib().vtg_cells(t.h, 0, 1, c.ctypes.data, lk.ctypes.data, vtg_lib.HOST, None), "cells")
+        outs.append((c, lk))
+    ctx.sync()
+    for (c, lk), (c0, lk0) in zip(outs, alone):
+        assert c.tobytes() == c0.tobytes() and lk.tobytes() == lk0.tobytes()
+    for t in ts:
+        t.close()
+
+
 def test_empty_point_list(vtg_lib, ctx):
     f0, f1, _, _ = S.warp_pair(64, 64, (1.0, 0.5), 0.5, seed=4)
     t = _tracker(vtg_lib, ctx, 64, 64, levels=2)

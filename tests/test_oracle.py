@@ -199,6 +199,24 @@ def test_lk_lane_matches_m2_accuracy_table(golden):
         assert ["%.4f" % v for v in (med, p95, mx)] == ["%.4f" % row[k] for k in ("median", "p95", "max")], row
 
 
+def test_oracle_team_size_invariance():
+    """The reference's race check is hash invariance across thread counts; the oracle's threaded cells and points
+    (an atomic work counter, as the reference's team) give the same bits on 1, 2, 3 and 8 threads, in both
+    arithmetics."""
+    f0, f1, _, _ = S.warp_pair(320, 240, (2.3, -1.1), 0.5, seed=21)
+    P0, P1 = O.pyramid(f0, 3), O.pyramid(f1, 3)
+    cfg = O.lk_cfg()
+    xs, ys = O.cell_centres(320, 240, 16, 16)
+    for mode in (O.LANE, O.F64):
+        base_pts = O.lk_points(P0, P1, 2, cfg, xs, ys, max_fb=0.5, mode=mode, threads=1)
+        base_cells = O.cells(P0, P1, 2, cfg, 16, 8, max_fb=0.5, mode=mode, threads=1)
+        for threads in (2, 3, 8):
+            assert O.lk_points(P0, P1, 2, cfg, xs, ys, max_fb=0.5, mode=mode, threads=threads).tobytes() == \
+                base_pts.tobytes()
+            got = O.cells(P0, P1, 2, cfg, 16, 8, max_fb=0.5, mode=mode, threads=threads)
+            assert all(a.tobytes() == b.tobytes() for a, b in zip(got, base_cells))
+
+
 def test_m2_f64_accuracy_against_exact_truth():
     """The FP64 oracle recovers the M2 pattern's exact quarter-pixel displacements to within 0.05 px (the reference's
     own accuracy table, docs/measurements.md:93-104, reads EPE medians of 0.007-0.012 px)."""
