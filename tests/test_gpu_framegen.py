@@ -74,6 +74,20 @@ def test_framegen_against_oracle(vtg_lib, ctx, w, h, shift, amp, seed):
     assert np.array_equal(frame, o["out"]) and np.array_equal(pic, o["pic"])
 
 
+@pytest.mark.parametrize("w,h", [(8192, 96), (96, 8192)])
+def test_framegen_largest_sides(vtg_lib, ctx, w, h):
+    """The widest and the tallest frames frame generation takes (8192 a side) against the oracle, bit for bit."""
+    f0, f1, _, _ = S.warp_pair(w, h, (6.0, -3.5), 1.0, seed=w + h)
+    r, frame, pic = _run(vtg_lib, ctx, f0, f1)
+    o = O.framegen(O.pyramid(f0, 1)[0], O.pyramid(f1, 1)[0])
+    assert r["scene"] == o["scene"]
+    for k in ("raw", "fil", "up"):
+        for L, (a, b) in enumerate(zip(r[k], o[k])):
+            assert a.tobytes() == b.tobytes(), (k, L)
+    assert r["mid"].tobytes() == o["mid"].tobytes()
+    assert np.array_equal(frame, o["out"]) and np.array_equal(pic, o["pic"])
+
+
 def test_framegen_api(vtg_lib, ctx):
     L = vtg_lib.lib()
     h = C.c_void_p()

@@ -237,6 +237,41 @@ def test_concurrent_streams_same_bits(vtg_lib, ctx):
         t.close()
 
 
+def test_largest_frame(vtg_lib, ctx):
+    """The largest frame a tracker takes, 16384 x 16384 (6 levels, 2.1 M cells): every level bit-exact, the cell grid
+    computed, and its cells at 512 sampled places, plus 512 points with guesses, within 0.01 px of the FP64 oracle.
+    Offsets here pass 2^28 elements a plane, so any 32-bit index arithmetic would show."""
+    w = h = 16384
+    base = S.noise_frame(1024, 1024, seed=77)
+    frame = np.tile(base, (16, 16))
+    frame[::7, ::5] ^= 0x5A  # break the tiling's periodicity
+    f1 = np.roll(frame, (3, -2), axis=(0, 1))
+    t = _tracker(vtg_lib, ctx, w, h, levels=6)
+    t.build(0, frame)
+    t.build(1, f1)
+    P0, P1 = O.pyramid(frame, 6), O.pyramid(f1, 6)
+    for L in range(6):
+        assert np.array_equal(t.level(1, L), P1[L]), "level %d" % L
+    cells, lk = t.cells(0, 1)
+    assert len(cells) == (w // 16) * (h // 8)
+    cfg = O.lk_cfg()
+    sel = np.sort(S.hash_u64(77, 1, 512) % len(cells)).astype(np.int64)
+    xs, ys = O.cell_centres(w, h, 16, 8)
+    ref = O.lk_points(P0, P1, 5, cfg, xs[sel], ys[sel], max_fb=0.5, mode=O.F64, threads=os.cpu_count() or 1)
+    ok, err = _flow_err(lk[sel], ref)
+    assert err <= TOL_PX and np.mean(lk[sel]["status"] == ref["status"]) >= 0.99
+    u = S.uniform(77, 2, 4 * 512).reshape(4, 512)
+    px = (20 + u[0] * (w - 40)).astype(np.float32)
+    py = (20 + u[1] * (h - 40)).astype(np.float32)
+    gx = (-3 + 6 * u[2]).astype(np.float32)
+    gy = (-3 + 6 * u[3]).astype(np.float32)
+    got = t.points(0, 1, px, py, gx, gy)
+    ref = O.lk_points(P0, P1, 5, cfg, px, py, gx, gy, max_fb=0.5, mode=O.F64, threads=os.cpu_count() or 1)
+    ok, err = _flow_err(got, ref)
+    assert err <= TOL_PX and np.mean(got["status"] == ref["status"]) >= 0.99 and ok.mean() > 0.5
+    t.close()
+
+
 def test_empty_point_list(vtg_lib, ctx):
     f0, f1, _, _ = S.warp_pair(64, 64, (1.0, 0.5), 0.5, seed=4)
     t = _tracker(vtg_lib, ctx, 64, 64, levels=2)
