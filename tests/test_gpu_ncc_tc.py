@@ -41,6 +41,26 @@ def test_tc_map_matches_f32_map(vtg_lib, ctx, precision, tw, th, w, h):
     s.close()
 
 
+@pytest.mark.parametrize("tw,th,w,h", [(64, 64, 3840, 2160), (32, 32, 16384, 256), (96, 96, 256, 16384)])
+def test_tc_map_on_large_pictures(vtg_lib, ctx, tw, th, w, h):
+    """A 4K picture and the widest and tallest pictures a search takes (16384 a side): the BF16 map within its bound of
+    the F32 map, the same cells, and the template found where it was cut, with the F32 re-score's value."""
+    frame = S.noise_frame(w, h, seed=w + 7 * h)
+    tpl, xs, ys, blank = S.ncc_templates(frame, max(tw, th), 2, seed=5, blank_share=0.0)
+    patch = tpl[0][:th, :tw].astype(np.float32)
+    app = (patch - np.float32(patch.mean(dtype=np.float64))).astype(np.float32)
+    norm = float(np.sum(app.astype(np.float64) ** 2))
+    dp = _dev(frame)
+    s = vtg_lib.Search(ctx, w, h, max_tw=128, max_th=128)
+    s.template(app, norm)
+    f32, v32, _, _ = s.run(dp.data_ptr(), w, h, w, vtg_lib.PLANE_U8, 1, w, 1, h, 1, vtg_lib.NCC_F32, want_map=True)
+    ftc, vtc, _, _ = s.run(dp.data_ptr(), w, h, w, vtg_lib.PLANE_U8, 1, w, 1, h, 1, vtg_lib.NCC_BF16, want_map=True)
+    assert ftc["cells"] == f32["cells"] and np.abs(vtc - v32).max() < TOL_MAP[1]
+    assert (ftc["hx"], ftc["hy"]) == (f32["hx"], f32["hy"]) == (2 * xs[0], 2 * ys[0])
+    assert abs(ftc["ncc"] - f32["ncc"]) < 1e-6
+    s.close()
+
+
 @pytest.mark.parametrize("precision", [1, 2])
 def test_tc_step2_and_window(vtg_lib, ctx, precision):
     """A window that starts off the cell grid, at step 2, as the whole-picture band search runs at levels 0 and 1."""
