@@ -24,6 +24,7 @@
 #define SB_X 160
 #define SF_X 136
 #define SF_P 140 /* int row pitch of staged F32 values and of the vertical sums: 16-byte aligned rows */
+#define PK_G (SF_X / 4) /* four-column groups of vertical sums in a row (the byte path's packed words) */
 
 /* A whole number 0 <= v < 2^23 as a float without a conversion instruction: the bits of 2^23 + v, less 2^23. */
 __device__ __forceinline__ float small_int_to_float(int v)
@@ -98,23 +99,53 @@ __device__ __forceinline__ void reduce_tile(const void *__restrict__ src_, int s
         }
         if (!dst)
             return;
-        /* vertical sums of staged byte columns 12 .. 147 (source 2 ox - 4 ..), four columns a thread */
-        for (int i = tid; i < RT_Y * (SF_X / 4); i += blockDim.x) {
-            const int r = i / (SF_X / 4), g = i - r * (SF_X / 4);
-            uint32_t w[5];
+        /* vertical sums of staged byte columns 12 .. 147 (source 2 ox - 4 ..), four columns a thread, two to a word:
+         * group g's even columns in the 16-bit halves of E_g, its odd columns in O_g. A sum is at most 16 x 255 =
+         * 4080, so whole-word adds never carry from one half into the other. */
+        uint32_t *s_e = reinterpret_cast<uint32_t *>(&s_v[0][0]), *s_o = s_e + RT_Y * PK_G;
+        for (int i = tid; i < RT_Y * PK_G; i += blockDim.x) {
+            const int r = i / PK_G, g = i - r * PK_G;
+            uint32_t e[5], o[5];
 #pragma unroll
-            for (int t = 0; t < 5; t++)
-                w[t] = *reinterpret_cast<const uint32_t *>(&s_b[2 * r + t][12 + 4 * g]);
-            int4 o;
-            int *op = &o.x;
-#pragma unroll
-            for (int e = 0; e < 4; e++) {
-                const int a = (w[0] >> (8 * e)) & 255, b = (w[1] >> (8 * e)) & 255, c = (w[2] >> (8 * e)) & 255,
-                          d = (w[3] >> (8 * e)) & 255, f = (w[4] >> (8 * e)) & 255;
-                op[e] = a + f + 4 * (b + d) + 6 * c;
+            for (int t = 0; t < 5; t++) {
+                const uint32_t w = *reinterpret_cast<const uint32_t *>(&s_b[2 * r + t][12 + 4 * g]);
+                e[t] = w & 0x00FF00FFu;
+                o[t] = (w >> 8) & 0x00FF00FFu;
             }
-            *reinterpret_cast<int4 *>(&s_v[r][4 * g]) = o;
+            s_e[i] = e[0] + e[4] + 4u * (e[1] + e[3]) + 6u * e[2];
+            s_o[i] = o[0] + o[4] + 4u * (o[1] + o[3]) + 6u * o[2];
         }
+        __syncthreads();
+        /* horizontal, two outputs a word: outputs 2m and 2m + 1 take vertical sums 4m + 2 .. 4m + 6 and 4m + 4 ..
+         * 4m + 8, i.e. the pairs (E_m hi, E_m+1 lo), (O_m hi, O_m+1 lo), E_m+1, O_m+1, (E_m+1 hi, E_m+2 lo) with
+         * weights 1, 4, 6, 4, 1. A sum is at most 16 x 4080 = 65280 in each half; (h + 2) >> 2 is at most 16320, so
+         * the mask drops exactly the bits the high half shifts into the low one. Four outputs a thread. */
+        for (int i = tid; i < RT_Y * (RT_X / 4); i += blockDim.x) {
+            const int r = i / (RT_X / 4), q = i - r * (RT_X / 4);
+            const int gy = oy + r, gx = ox + 4 * q;
+            if (gy >= dh || gx >= dw)
+                continue;
+            const uint32_t *E = s_e + r * PK_G + 2 * q, *O = s_o + r * PK_G + 2 * q;
+            uint32_t res[2];
+#pragma unroll
+            for (int p = 0; p < 2; p++) {
+                const uint32_t e1 = E[p + 1], o1 = O[p + 1];
+                const uint32_t A = __byte_perm(E[p], e1, 0x5432), B = __byte_perm(O[p], o1, 0x5432);
+                const uint32_t F = __byte_perm(e1, E[p + 2], 0x5432);
+                const uint32_t h = A + F + 4u * (B + o1) + 6u * e1;
+                res[p] = ((h + 0x00020002u) >> 2) & 0x3FFF3FFFu;
+            }
+            const float o[4] = {small_int_to_float((int)(res[0] & 0xFFFFu)), small_int_to_float((int)(res[0] >> 16)),
+                                small_int_to_float((int)(res[1] & 0xFFFFu)), small_int_to_float((int)(res[1] >> 16))};
+            float *d = dst + (size_t)gy * dpitch + gx;
+            if (gx + 4 <= dw) {
+                *reinterpret_cast<float4 *>(d) = make_float4(o[0], o[1], o[2], o[3]);
+            } else {
+                for (int e = 0; e < 4 && gx + e < dw; e++)
+                    d[e] = o[e];
+            }
+        }
+        return;
     } else {
         const float *src = (const float *)src_;
         const int gx0 = 2 * ox - 4;
@@ -161,14 +192,9 @@ __device__ __forceinline__ void reduce_tile(const void *__restrict__ src_, int s
 #pragma unroll
         for (int e = 0; e < 4; e++) {
             const int c = 2 * e + 4;
-            if (FROM_U8) {
-                const int h = v[c - 2] + v[c + 2] + 4 * (v[c - 1] + v[c + 1]) + 6 * v[c];
-                o[e] = small_int_to_float((h + 2) >> 2);
-            } else {
-                const float *f = reinterpret_cast<const float *>(v);
-                const float h = f[c - 2] + f[c + 2] + 4.0f * (f[c - 1] + f[c + 1]) + 6.0f * f[c];
-                o[e] = floorf((h + 128.0f) * (1.0f / 256.0f)); /* (h + 128) >> 8, exact */
-            }
+            const float *f = reinterpret_cast<const float *>(v);
+            const float h = f[c - 2] + f[c + 2] + 4.0f * (f[c - 1] + f[c + 1]) + 6.0f * f[c];
+            o[e] = floorf((h + 128.0f) * (1.0f / 256.0f)); /* (h + 128) >> 8, exact */
         }
         float *d = dst + (size_t)gy * dpitch + gx;
         if (gx + 4 <= dw) {
