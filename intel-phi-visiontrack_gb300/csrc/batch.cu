@@ -306,11 +306,12 @@ static int launch_slot(vtg_batch *b, BatchSlot &sl, cudaStream_t s, int nwait = 
         CU(cudaStreamWaitEvent(s, (cudaEvent_t)wait[k], 0));
     for (const BatchSlot::Input &in : sl.inputs)
         CU(vtg_launch_build_input(in.src, in.stride, in.w, in.h, in.opts, in.mm, in.l0, in.pitch0, s));
-    CU(vtg_launch_pyramid_batch(sl.d_pyr, sl.d_tiles, sl.tiles, sl.njobs, sl.max_levels, s));
-    CU(cudaMemsetAsync(sl.d_counter, 0, sizeof(int), s));
+    /* the pyramid's levels and the LK launch as a chain of programmatic dependents: each starts as the one before
+     * drains; the last pyramid launch zeroes the LK launch's work counter */
+    CU(vtg_launch_pyramid_batch(sl.d_pyr, sl.d_tiles, sl.tiles, sl.njobs, sl.max_levels, s, sl.d_counter, true));
     LkTune t = b->tune;
     t.chunk = sl.chunk;
-    CU(vtg_launch_lk_batch(sl.d_lk, sl.d_items, sl.njobs, sl.items, sl.prm, t, b->sms, sl.d_counter, s));
+    CU(vtg_launch_lk_batch(sl.d_lk, sl.d_items, sl.njobs, sl.items, sl.prm, t, b->sms, sl.d_counter, s, true));
     return VTG_OK;
 }
 

@@ -778,8 +778,9 @@ __global__ void __launch_bounds__(WARPS * 32, MINB) lk_batch_kernel(const LkJob 
     extern __shared__ f2_t s_t[]; /* TS: WARPS x (MAXH / 2) x 32 pairs */
     f2_t *ts = TS ? s_t + (size_t)(threadIdx.x >> 5) * (MAXH / 2) * 32 : nullptr;
     for (int k = threadIdx.x; k <= njobs; k += blockDim.x)
-        s_start[k] = item_start[k];
+        s_start[k] = item_start[k]; /* the step's own table, written when it was prepared */
     __syncthreads();
+    vtg_grid_dependency_wait(); /* the pyramids and the counter, when launched as a dependent of the pyramid */
     const int lane = threadIdx.x & 31;
     int item = PERSISTENT ? 0 : (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     for (;;) {
@@ -810,13 +811,15 @@ __global__ void __launch_bounds__(WARPS * 32, MINB) lk_batch_kernel(const LkJob 
 
 template <int MAXH, bool EXACT>
 static cudaError_t lk_batch_launch(const LkJob *jobs, const int *item_start, int njobs, int items, const LkPrm &p,
-                                   const LkTune &t, int sms, int *counter, cudaStream_t s)
+                                   const LkTune &t, int sms, int *counter, cudaStream_t s, bool pdl)
 {
 #define LKB(P, WARPS, MINB)                                                                                            \
     do {                                                                                                               \
         const int blocks = P ? sms * t.ctas_per_sm : (items + WARPS - 1) / WARPS;                                      \
-        lk_batch_kernel<MAXH, EXACT, P, WARPS, MINB, false><<<blocks, WARPS * 32, 0, s>>>(jobs, item_start, njobs,    \
-                                                                                          items, t.chunk, p, counter); \
+        const cudaError_t e = vtg_launch_k(lk_batch_kernel<MAXH, EXACT, P, WARPS, MINB, false>, blocks, WARPS * 32, 0, \
+                                           s, pdl, jobs, item_start, njobs, items, t.chunk, p, counter);               \
+        if (e != cudaSuccess)                                                                                          \
+            return e;                                                                                                  \
     } while (0)
 #define LKT(WARPS, MINB)                                                                                               \
     do {                                                                                                               \
@@ -828,8 +831,11 @@ static cudaError_t lk_batch_launch(const LkJob *jobs, const int *item_start, int
             if (e != cudaSuccess)                                                                                      \
                 return e;                                                                                              \
         }                                                                                                              \
-        lk_batch_kernel<MAXH, EXACT, true, WARPS, MINB, true><<<sms * t.ctas_per_sm, WARPS * 32, smem, s>>>(          \
-            jobs, item_start, njobs, items, t.chunk, p, counter);                                                      \
+        const cudaError_t e2 = vtg_launch_k(lk_batch_kernel<MAXH, EXACT, true, WARPS, MINB, true>,                    \
+                                            sms * t.ctas_per_sm, WARPS * 32, smem, s, pdl, jobs, item_start, njobs,    \
+                                            items, t.chunk, p, counter);                                               \
+        if (e2 != cudaSuccess)                                                                                         \
+            return e2;                                                                                                 \
     } while (0)
     if (t.tsmem) {
         /* the template's T in shared memory: fewer registers, or more warps an SM */
@@ -860,15 +866,15 @@ static cudaError_t lk_batch_launch(const LkJob *jobs, const int *item_start, int
 }
 
 cudaError_t vtg_launch_lk_batch(const LkJob *jobs, const int *item_start, int njobs, int items, const LkPrm &p,
-                                const LkTune &tune, int sms, int *counter, cudaStream_t s)
+                                const LkTune &tune, int sms, int *counter, cudaStream_t s, bool pdl)
 {
     if (njobs < 1 || njobs > LK_BATCH_MAX_JOBS || items <= 0)
         return items <= 0 ? cudaSuccess : cudaErrorInvalidValue;
     if (p.H == 21)
-        return lk_batch_launch<21, true>(jobs, item_start, njobs, items, p, tune, sms, counter, s);
+        return lk_batch_launch<21, true>(jobs, item_start, njobs, items, p, tune, sms, counter, s, pdl);
     if (p.H == 15)
-        return lk_batch_launch<15, true>(jobs, item_start, njobs, items, p, tune, sms, counter, s);
-    return lk_batch_launch<31, false>(jobs, item_start, njobs, items, p, tune, sms, counter, s);
+        return lk_batch_launch<15, true>(jobs, item_start, njobs, items, p, tune, sms, counter, s, pdl);
+    return lk_batch_launch<31, false>(jobs, item_start, njobs, items, p, tune, sms, counter, s, pdl);
 }
 
 template <int MAXH, bool EXACT>

@@ -232,10 +232,13 @@ __global__ void __launch_bounds__(256) pyr_reduce_kernel(const void *__restrict_
  * binary search over the tile offsets. Level 1 (with level 0) from each job's bytes, or level L from level L - 1. */
 template <bool FROM_U8>
 __global__ void __launch_bounds__(256) pyr_batch_kernel(const PyrJob *__restrict__ jobs, const int *__restrict__ start,
-                                                        int njobs, int level)
+                                                        int njobs, int level, int *__restrict__ reset)
 {
     __shared__ TileSmem s_t;
     __shared__ __align__(16) int s_v[RT_Y][SF_P];
+    vtg_grid_dependency_wait(); /* the level below, when launched as a dependent of its launch */
+    if (reset && blockIdx.x == 0 && threadIdx.x == 0)
+        *reset = 0;
     const int b = blockIdx.x;
     int lo = 0, hi = njobs; /* start[lo] <= b < start[hi] */
     while (hi - lo > 1) {
@@ -498,16 +501,23 @@ int vtg_pyr_tiles(int w, int h, int level)
 }
 
 cudaError_t vtg_launch_pyramid_batch(const PyrJob *jobs, const int *starts, const int *tiles_total, int njobs,
-                                     int max_levels, cudaStream_t s)
+                                     int max_levels, cudaStream_t s, int *reset, bool pdl)
 {
-    for (int L = 1; L < (max_levels > 1 ? max_levels : 2); L++) {
+    const int top = max_levels > 1 ? max_levels : 2;
+    int last = 1; /* the last level launched (level 1's launch always has tiles) */
+    for (int L = 1; L < top; L++)
+        if (tiles_total[L - 1] > 0)
+            last = L;
+    for (int L = 1; L < top; L++) {
         const int tiles = tiles_total[L - 1];
         if (tiles <= 0)
             continue;
-        if (L == 1)
-            pyr_batch_kernel<true><<<tiles, 256, 0, s>>>(jobs, starts + (size_t)(L - 1) * (njobs + 1), njobs, L);
-        else
-            pyr_batch_kernel<false><<<tiles, 256, 0, s>>>(jobs, starts + (size_t)(L - 1) * (njobs + 1), njobs, L);
+        const int *st = starts + (size_t)(L - 1) * (njobs + 1);
+        int *r = L == last ? reset : nullptr;
+        const cudaError_t e = L == 1 ? vtg_launch_k(pyr_batch_kernel<true>, tiles, 256, 0, s, false, jobs, st, njobs, L, r)
+                                     : vtg_launch_k(pyr_batch_kernel<false>, tiles, 256, 0, s, pdl, jobs, st, njobs, L, r);
+        if (e != cudaSuccess)
+            return e;
     }
     return cudaGetLastError();
 }

@@ -89,11 +89,38 @@ cudaError_t vtg_launch_pyramid_opts(const uint8_t *frame, int stride, int w, int
 cudaError_t vtg_launch_cells(const DevPyr *I, const DevPyr *J, int top, const LkPrm &p, const CellGrid &g, int base_w,
                              int base_h, vtg_lk_out *out, vtg_cell *cells, cudaStream_t s);
 int vtg_pyr_tiles(int w, int h, int level);
+/* The batched pyramid: one launch per level for all jobs. With pdl, each level after the first is launched as a
+ * programmatic dependent of the one before (it starts as the previous level drains and waits in griddepcontrol.wait
+ * until that level's writes are visible). reset (may be NULL): a device int the last launch sets to 0, for a
+ * programmatic dependent launched after it (the LK launch's work counter). */
 cudaError_t vtg_launch_pyramid_batch(const PyrJob *jobs, const int *starts, const int *tiles_total, int njobs,
-                                     int max_levels, cudaStream_t s);
+                                     int max_levels, cudaStream_t s, int *reset = nullptr, bool pdl = false);
 /* Batched LK over jobs: items of `chunk` cells, job j's items from item_start[j]; `counter` must be 0 at launch. */
 cudaError_t vtg_launch_lk_batch(const LkJob *jobs, const int *item_start, int njobs, int items, const LkPrm &p,
-                                const LkTune &tune, int sms, int *counter, cudaStream_t s);
+                                const LkTune &tune, int sms, int *counter, cudaStream_t s, bool pdl = false);
+
+/* A kernel launch, as a programmatic dependent of the stream's previous kernel when pdl (the kernel itself runs
+ * griddepcontrol.wait before it reads what that kernel wrote). */
+template <typename... KArgs, typename... Args>
+static inline cudaError_t vtg_launch_k(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                                       bool pdl, Args... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = pdl ? at : nullptr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, k, args...);
+}
+
+/* Waits until the kernels this launch programmatically depends on have finished and their writes are visible (at
+ * once when there are none). */
+__device__ __forceinline__ void vtg_grid_dependency_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 cudaError_t vtg_launch_points(const DevPyr *I, const DevPyr *J, int top, const LkPrm &p, int n, const float *xs,
                               const float *ys, const float *gx, const float *gy, vtg_lk_out *out, cudaStream_t s);
 
