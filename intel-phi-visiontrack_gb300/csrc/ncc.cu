@@ -266,10 +266,12 @@ __device__ __forceinline__ void top_insert(unsigned long long (&t)[NCC_TOP], uns
 
 /* The eight best cells: each thread its strided share, then the lists merge across the warp by xor partners (both
  * partners end with the best eight of the pair) and across the eight warps in the first warp. */
-__global__ void __launch_bounds__(256) ncc_top(const float *__restrict__ map_v, int cells, int *__restrict__ top,
-                                               int *__restrict__ ntop)
+#define NCC_TOP_THREADS 1024
+
+__global__ void __launch_bounds__(NCC_TOP_THREADS) ncc_top(const float *__restrict__ map_v, int cells,
+                                                           int *__restrict__ top, int *__restrict__ ntop)
 {
-    __shared__ unsigned long long s[8][NCC_TOP];
+    __shared__ unsigned long long s[NCC_TOP_THREADS / 32][NCC_TOP];
     unsigned long long t[NCC_TOP];
 #pragma unroll
     for (int k = 0; k < NCC_TOP; k++)
@@ -321,8 +323,8 @@ __global__ void __launch_bounds__(256) ncc_top(const float *__restrict__ map_v, 
     if (warp == 0) {
 #pragma unroll
         for (int k = 0; k < NCC_TOP; k++)
-            t[k] = lane < 8 ? s[lane][k] : 0ull;
-        merge(8);
+            t[k] = lane < NCC_TOP_THREADS / 32 ? s[lane][k] : 0ull;
+        merge(32);
         if (lane == 0) {
             int n = 0;
             for (int k = 0; k < NCC_TOP; k++) {
@@ -567,7 +569,7 @@ static cudaError_t launch_all(const T *plane, int pitch, const float *app, const
         if (e != cudaSuccess)
             return e;
     }
-    ncc_top<<<1, 256, 0, st>>>(s.map_v, cells, s.top, s.ntop);
+    ncc_top<<<1, NCC_TOP_THREADS, 0, st>>>(s.map_v, cells, s.top, s.ntop);
     const int around = p.step > 1 ? 2 * p.step - 1 : 1, ring = 2 * around + 3;
     ncc_half_all<T><<<NCC_TOP * ring * ring, 256, 0, st>>>(plane, pitch, app, p, s.map_x, s.map_y, s.top, s.ntop,
                                                             s.half);
