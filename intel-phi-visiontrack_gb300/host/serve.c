@@ -213,8 +213,7 @@ int vtg_serve_run(vtg_ctx *ctx, const struct vtg_serve_cfg *c, struct vtg_serve_
     long served = 0, cells = 0, ncc = 0, batches = 0, batched = 0;
     const double t0 = now_s();
     double t_last = t0;
-    int next_req = 0, next_stream_check = 0;
-    (void)next_stream_check;
+    int next_req = 0;
     while (rc == VTG_OK && served < n) {
         const double now = now_s() - t0;
         if (now > c->duration_s + SERVE_DRAIN_S)
@@ -281,41 +280,39 @@ int vtg_serve_run(vtg_ctx *ctx, const struct vtg_serve_cfg *c, struct vtg_serve_
             /* the oldest arrived frame of each stream with a slot to spare, oldest first. A stream's next frame may
              * go to one slot while its previous one is on the GPU in another: the new step then waits on the GPU
              * for that slot's work (its pyramid set and result buffers are reused), with no host round trip. */
-            for (int pass = 0; pass < 1; pass++) {
-                for (;;) {
-                    int best = -1;
-                    double bt = 1e300;
-                    for (int s = 0; s < ns; s++) {
-                        struct sstate *ss = &st[s];
-                        if (!ss->admitted || ss->finished || ss->in_flight >= c->inflight || ss->next >= ss->count)
-                            continue;
-                        const struct req *r = &rq[order[ss->first + ss->next]];
-                        if (r->t_arrive > now || r->t_arrive >= bt)
-                            continue;
-                        int taken = 0;
-                        for (int i = 0; i < m; i++)
-                            taken |= stream_of[i] == s;
-                        if (taken)
-                            continue;
-                        best = s;
-                        bt = r->t_arrive;
-                    }
-                    if (best < 0 || m >= c->max_batch)
-                        break;
-                    struct sstate *ss = &st[best];
-                    const int ri = order[ss->first + ss->next];
-                    const int kk = rq[ri].k;
-                    if (ss->in_flight)
-                        wait_slots |= 1u << ss->last_slot;
-                    stream_of[m] = best;
-                    sl[k].reqs[m] = ri;
-                    tr[m] = ss->t;
-                    cur[m] = (kk + 1) & 1;
-                    fr[m] = c->frames[2 * best + ((kk + 1) & 1)];
-                    m++;
-                    if (c->plain)
-                        break; /* the plain form: one frame pair at a time */
+            for (;;) {
+                int best = -1;
+                double bt = 1e300;
+                for (int s = 0; s < ns; s++) {
+                    struct sstate *ss = &st[s];
+                    if (!ss->admitted || ss->finished || ss->in_flight >= c->inflight || ss->next >= ss->count)
+                        continue;
+                    const struct req *r = &rq[order[ss->first + ss->next]];
+                    if (r->t_arrive > now || r->t_arrive >= bt)
+                        continue;
+                    int taken = 0;
+                    for (int i = 0; i < m; i++)
+                        taken |= stream_of[i] == s;
+                    if (taken)
+                        continue;
+                    best = s;
+                    bt = r->t_arrive;
                 }
+                if (best < 0 || m >= c->max_batch)
+                    break;
+                struct sstate *ss = &st[best];
+                const int ri = order[ss->first + ss->next];
+                const int kk = rq[ri].k;
+                if (ss->in_flight)
+                    wait_slots |= 1u << ss->last_slot;
+                stream_of[m] = best;
+                sl[k].reqs[m] = ri;
+                tr[m] = ss->t;
+                cur[m] = (kk + 1) & 1;
+                fr[m] = c->frames[2 * best + ((kk + 1) & 1)];
+                m++;
+                if (c->plain)
+                    break; /* the plain form: one frame pair at a time */
             }
             if (m == 0)
                 break;
@@ -347,14 +344,12 @@ int vtg_serve_run(vtg_ctx *ctx, const struct vtg_serve_cfg *c, struct vtg_serve_
                 if (sl[k].s && urand(&seed) < (double)c->ncc_share) {
                     const float *plane;
                     int lw, lh, lp;
-                    const int s = stream_of[i];
                     const int lev = c->lk.levels > 1 ? 1 : 0;
                     rc = vtg_level_device(tr[i], cur[i], lev, &plane, &lw, &lh, &lp);
                     if (rc == VTG_OK)
                         rc = vtg_search_run(sl[k].s, plane, lw, lh, lp, VTG_PLANE_F32, 1, lw, 1, lh, 2, VTG_NCC_F32,
                                             sl[k].d_found, NULL, NULL, NULL, VTG_DEVICE, bs);
                     ncc++;
-                    (void)s;
                 }
                 st[stream_of[i]].in_flight++;
                 st[stream_of[i]].last_slot = k;
