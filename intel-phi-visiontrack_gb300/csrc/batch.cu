@@ -428,9 +428,9 @@ extern "C" int vtg_batch_autotune(vtg_batch *b, int slot, int reps, struct vtg_t
                 if (pers) {
                     const int max_ctas = 16 / warps; /* 128 registers a thread: 16 warps an SM */
                     for (int c = 1; c <= max_ctas; c *= 2)
-                        cands.push_back({warps, chunk, 1, c});
+                        cands.push_back({warps, chunk, 1, c, 0});
                 } else if (chunk <= 2) {
-                    cands.push_back({warps, chunk, 0, 1});
+                    cands.push_back({warps, chunk, 0, 1, 0});
                 }
             }
     /* the template's intensities in shared memory: 20 or 24 warps an SM */
