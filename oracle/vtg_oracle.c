@@ -265,7 +265,12 @@ void or_contrast_gain(int lo, int hi, float go[2])
  * max, then with opts & 2 the binomial. dst: w x h, rows dstride floats apart. */
 void or_build_input(const uint8_t *src, int sstride, int w, int h, int opts, float *dst, int dstride)
 {
-    float *a = malloc(sizeof(float) * (size_t)w * h), *b = malloc(sizeof(float) * (size_t)w * h);
+    float *a = calloc((size_t)w * h, sizeof(float)), *b = calloc((size_t)w * h, sizeof(float));
+    if (!a || !b) {
+        free(a);
+        free(b);
+        return;
+    }
     or_u8_to_q6(src, sstride, w, h, a, w);
     if (opts & 1) {
         float mm[2], go[2];
