@@ -34,7 +34,7 @@ sys.path.insert(0, PKG)
 METRIC = "LK cells/s + p99 ms/frame-pair, served-batched vs plain GPU; ≤0.01px vs FP64"
 W, H, LEVELS, CELL_W, CELL_H, PATCH = 1920, 1080, 4, 16, 8, 21
 # DRAM bytes (read + write) of one batched LK launch of 8 streams, from ncu (profiles/lk_batch_kernel_1080p_x8.md)
-LK_TRAFFIC_BYTES = 176_632_576 + 8_843_520 + 8_708_352
+LK_TRAFFIC_BYTES = 176_632_576 + 8_843_520
 CELLS = 16200
 
 
