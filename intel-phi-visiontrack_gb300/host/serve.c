@@ -322,8 +322,10 @@ int vtg_serve_run(vtg_ctx *ctx, const struct vtg_serve_cfg *c, struct vtg_serve_
             for (int j = 0; j < c->inflight; j++)
                 if (wait_slots >> j & 1u)
                     waits[nw++] = (void *)sl[j].ev;
-            if (c->plain) {
-                /* one launch set per frame pair, no batching: vtg_build + vtg_cells on the batch's stream */
+            if (c->plain || m == 1) {
+                /* one frame pair: vtg_build + vtg_cells on the slot's stream (the plain form always; the served form
+                 * when only one request is ready, where the batched step's tables and persistent grid only add
+                 * latency; the cells are the same bits either way) */
                 const int s = stream_of[0];
                 for (int j = 0; j < nw && rc == VTG_OK; j++)
                     if (cudaStreamWaitEvent(bs, (cudaEvent_t)waits[j], 0) != cudaSuccess)
