@@ -73,6 +73,22 @@ def test_contrast_gain_matches_oracle(vtg_lib):
     assert lib.vtg_contrast_gain(0, 1 << 24, go) == vtg_lib.EINVAL
 
 
+def _build_c_caller(vtg_lib, out_dir):
+    """tests/c/track_pair.c compiled as C11 and linked against libvtg.so, as the reference's host code would be."""
+    exe = os.path.join(str(out_dir), "track_pair")
+    lib_dir = os.path.dirname(vtg_lib.LIB_PATH)
+    subprocess.run(["cc", "-std=c11", "-O2", "-Wall", "-Wextra", "-Werror", "-I" + os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "c", "track_pair.c"), "-o", exe, "-L" + lib_dir, "-lvtg",
+                    "-Wl,-rpath," + lib_dir, "-lm"], check=True, capture_output=True, text=True)
+    return exe
+
+
+def test_c_caller_builds_and_links(vtg_lib, tmp_path):
+    """The public headers are C11 (the reference's language), and a C program links against libvtg.so."""
+    exe = _build_c_caller(vtg_lib, tmp_path)
+    assert os.path.exists(exe)
+
+
 def test_context_without_gpu_is_refused(vtg_lib):
     import torch
 
