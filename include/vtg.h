@@ -102,7 +102,8 @@ int vtg_tracker_create(vtg_ctx *ctx, const struct vtg_config *cfg, vtg_tracker *
 void vtg_tracker_destroy(vtg_tracker *t);
 /* Pyramid sets (tk_sets, src/kern/track.h:26): frame k goes to set k mod this. */
 int vtg_tracker_sets(const vtg_tracker *t);
-/* Cells of the grid: ceil(w_f / cell_w) x ceil(h_f / cell_h) at the flow level's size w_f x h_f. */
+/* Cells of the grid: ceil(w_f / cell_w) x ceil(h_f / cell_h) at the flow level's size w_f x h_f. Returns their
+ * number (cols x rows), or a negative status. */
 int vtg_tracker_cells(const vtg_tracker *t, int *cols, int *rows);
 /* The tracker's stream (a cudaStream_t) -- work of one tracker is ordered on it. */
 void *vtg_tracker_stream(const vtg_tracker *t);

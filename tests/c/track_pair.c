@@ -30,8 +30,8 @@ static int cmp_float(const void *a, const void *b)
 
 #define CHECK(call)                                                                                                    \
     do {                                                                                                               \
-        const int rc_ = (call);                                                                                        \
-        if (rc_ != VTG_OK) {                                                                                           \
+        const int rc_ = (call); /* a status, or a count for the calls that return one */                            \
+        if (rc_ < 0) {                                                                                                 \
             fprintf(stderr, "%s: %s\n", #call, vtg_strerror(rc_));                                                     \
             return 1;                                                                                                  \
         }                                                                                                              \
