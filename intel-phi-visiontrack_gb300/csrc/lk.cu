@@ -547,7 +547,8 @@ __device__ __forceinline__ void lk_track(const DevPyr &I, const DevPyr &J, int t
     for (int L = top; L >= 0; L--) {
         const DevLevel IL = I.l[L], JL = J.l[L];
         const float px = ldexpf(x, -L), py = ldexpf(y, -L); /* exact */
-        if (px < (float)mx || py < (float)my || px >= (float)(IL.w - mx - 1) || py >= (float)(IL.h - my - 1)) {
+        /* written so that NaN fails it: a caller's NaN point is out, never a window at a garbage place */
+        if (!(px >= (float)mx && py >= (float)my && px < (float)(IL.w - mx - 1) && py < (float)(IL.h - my - 1))) {
             if (L == 0)
                 status |= VTG_LK_OUT;
             else {
@@ -598,7 +599,7 @@ __device__ __forceinline__ void lk_track(const DevPyr &I, const DevPyr &J, int t
         int cjx = INT_MIN, cjy = INT_MIN;
         for (int it = 0; it < p.max_iter; it++) {
             const float qx = (rx + gx) + vx, qy = (ry + gy) + vy; /* offsets from (bx, by) */
-            if (qx < lo_x || qy < lo_y || qx >= hi_x || qy >= hi_y) {
+            if (!(qx >= lo_x && qy >= lo_y && qx < hi_x && qy < hi_y)) { /* NaN fails it too (a NaN guess) */
                 if (L == 0) {
                     status |= VTG_LK_OUT;
                     valid0 = false;
@@ -640,7 +641,8 @@ __device__ __forceinline__ void lk_track(const DevPyr &I, const DevPyr &J, int t
         const float fx0 = floorf(x), fy0 = floorf(y);
         const int bx = (int)fx0, by = (int)fy0;
         const float qx = (x - fx0) + gx, qy = (y - fy0) + gy;
-        if (qx < (float)(mx - bx) || qy < (float)(my - by) || qx >= (float)(J0.w - mx - 1 - bx) || qy >= (float)(J0.h - my - 1 - by)) {
+        if (!(qx >= (float)(mx - bx) && qy >= (float)(my - by) && qx < (float)(J0.w - mx - 1 - bx) &&
+              qy < (float)(J0.h - my - 1 - by))) {
             status |= VTG_LK_OUT;
         } else {
             int jx, jy;
@@ -683,7 +685,7 @@ __device__ __forceinline__ void lk_point(const DevPyr &I, const DevPyr &J, int t
             gy = y - o.y;
         } else {
             const float ex = r.x - x, ey = r.y - y;
-            if (r.status || __fmaf_rn(ex, ex, ey * ey) > p.fb_max2)
+            if (r.status || !(__fmaf_rn(ex, ex, ey * ey) <= p.fb_max2))
                 o.status |= VTG_LK_FLOWBACK;
         }
     }

@@ -272,6 +272,61 @@ def test_largest_frame(vtg_lib, ctx):
     t.close()
 
 
+NONFINITE = r"""
+import ctypes as C, json, sys
+sys.path[:0] = [%(pkg)r, %(oracle)r]
+import numpy as np
+import vtg, vtg_synth as S
+ctx = vtg.Context(0)
+f0, f1, _, _ = S.warp_pair(320, 240, (1.2, -0.7), 0.4, seed=31)
+t = vtg.Tracker(ctx, vtg.config(320, 240, levels=3))
+t.build(0, f0)
+t.build(1, f1)
+nan, inf = float("nan"), float("inf")
+xs = np.array([160, nan, 100, inf, -inf, 200, 120, 150, 1e30, 80], np.float32)
+ys = np.array([120, 100, nan, 100, 100, inf, 90, 130, 100, 60], np.float32)
+gx = np.array([0, 0, 0, 0, 0, 0, nan, inf, 0, -1e30], np.float32)
+gy = np.array([0, 0, 0, 0, 0, 0, 0, 0, 0, 0], np.float32)
+out = t.points(0, 1, xs, ys, gx, gy)
+clean = t.points(0, 1, xs[:1], ys[:1], gx[:1], gy[:1])
+word = (C.c_uint32 * 2)()
+checked = vtg.lib().vtg_check_read(word)
+print(json.dumps({"status": out["status"].tolist(), "first": out[:1].tobytes().hex(),
+                  "clean": clean.tobytes().hex(), "checked": checked, "word": [word[0], word[1]]}))
+"""
+
+
+def test_points_with_nonfinite_inputs(vtg_lib):
+    """Points and guesses that are NaN, infinite or absurd are VTG_LK_OUT, never a window read at a garbage place, and
+    the good point beside them gets the same bits as alone. Run first through the bounds-checked build, whose window
+    tests would record (and skip) any read outside a level, then through the production build."""
+    import json
+    import subprocess
+    import sys
+
+    import vtg_build
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    code = NONFINITE % {"pkg": os.path.join(root, "intel-phi-visiontrack_gb300"), "oracle": os.path.join(root, "oracle")}
+    results = []
+    for lib in (vtg_build.build(checked=True), None):
+        env = dict(os.environ)
+        env.pop("VTG_LIB", None)
+        if lib:
+            env["VTG_LIB"] = lib
+        r = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=600)
+        assert r.returncode == 0, r.stderr[-3000:]
+        res = json.loads(r.stdout.strip().splitlines()[-1])
+        if lib:
+            assert res["checked"] == 1 and res["word"] == [0, 0], res["word"]
+        results.append(res)
+    for res in results:
+        st = res["status"]
+        assert st[0] == 0 and res["first"] == res["clean"]
+        assert all(s & 1 for s in st[1:]), st  # VTG_LK_OUT
+    assert results[0]["status"] == results[1]["status"]
+
+
 def test_empty_point_list(vtg_lib, ctx):
     f0, f1, _, _ = S.warp_pair(64, 64, (1.0, 0.5), 0.5, seed=4)
     t = _tracker(vtg_lib, ctx, 64, 64, levels=2)
