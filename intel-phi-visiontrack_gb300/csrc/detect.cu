@@ -557,6 +557,10 @@ __global__ void __launch_bounds__(DET_SELECT_THREADS, 1) det_select(DetPrm q, co
 /* detect_begin's layout (src/kern/detect.c:28-66); false when nothing of the rectangle lies inside the margin. */
 static bool det_geometry(int w, int h, float rx, float ry, float rw, float rh, int margin, DetGeo &g)
 {
+    /* a region past any plane (or not a number) holds nothing; so does a negative margin's outside */
+    const float lim = 1.0e8f;
+    if (margin < 0 || !(fabsf(rx) < lim && fabsf(ry) < lim && fabsf(rw) < lim && fabsf(rh) < lim))
+        return false;
     int x0 = (int)rx, y0 = (int)ry, x1 = (int)(rx + rw), y1 = (int)(ry + rh);
     x0 = x0 < margin ? margin : x0;
     y0 = y0 < margin ? margin : y0;
@@ -769,7 +773,8 @@ extern "C" int vtg_detect_maps(vtg_detector *d, float rx, float ry, float rw, fl
     if (!d || !geo)
         return VTG_EINVAL;
     DetGeo g;
-    if (!det_geometry(w, h, rx, ry, rw, rh, margin, g))
+    if (!det_geometry(w, h, rx, ry, rw, rh, margin, g) || g.rows > d->max_h || g.cols > d->max_cols ||
+        g.nv * g.cell_rows > d->max_cells)
         return VTG_EINVAL;
     const int v[9] = {g.x0, g.y0, g.x1, g.y1, g.ax, g.cols, g.rows, g.nv, g.cell_rows};
     for (int k = 0; k < 9; k++)

@@ -119,4 +119,11 @@ def test_detect_empty_and_refusals(vtg_lib, ctx):
     big = _dev(np.zeros((300, 400), np.float32))
     with pytest.raises(vtg_lib.VtgError):
         det.detect(big.data_ptr(), 400, 300, 400, 0, 0, 400, 300, 12, 64, 4.0, 0.05)
+    # regions that are not numbers are refused; infinite or astronomically far ones, and a negative margin, hold nothing
+    with pytest.raises(vtg_lib.VtgError):
+        det.detect(dp.data_ptr(), 200, 100, 200, float("nan"), 0, 50, 50, 12, 64, 4.0, 0.05)
+    for reg in ((float("inf"), 0, 50, 50), (0, 0, float("inf"), 50), (-float("inf"), 0, 50, 50), (3e9, 0, 50, 50),
+                (-3e9, -3e9, 6e9, 6e9)):
+        assert len(det.detect(dp.data_ptr(), 200, 100, 200, *reg, 12, 64, 4.0, 0.05)[0]) == 0, reg
+    assert len(det.detect(dp.data_ptr(), 200, 100, 200, 0, 0, 200, 100, -1, 64, 4.0, 0.05)[0]) == 0
     det.close()
