@@ -203,6 +203,11 @@ int vtg_batch_launch(vtg_batch *b, int slot, void *stream);
  * streams: host frames are uploaded at once (each set has its own staging buffer), then the kernels wait for the
  * `nwait` CUDA events (cudaEvent_t) recorded after those steps. */
 int vtg_batch_launch_after(vtg_batch *b, int slot, void *stream, int nwait, void *const *events);
+/* As vtg_batch_launch_after, with `nwait_lk` more events that only the step's LK launch waits for, after its pyramid:
+ * e.g. the copies of earlier results out of the result buffers this LK launch writes, which may then overlap this
+ * step's pyramid. */
+int vtg_batch_launch_split(vtg_batch *b, int slot, void *stream, int nwait, void *const *events, int nwait_lk,
+                           void *const *events_lk);
 /* Captures a prepared step into a CUDA graph, and replays it. */
 int vtg_batch_capture(vtg_batch *b, int slot);
 int vtg_batch_replay(vtg_batch *b, int slot, void *stream);

@@ -296,7 +296,8 @@ extern "C" int vtg_batch_prepare(vtg_batch *b, int slot, int n, vtg_tracker *con
 }
 
 /* The tiles table is laid out with the prepared n; the batched pyramid launcher wants one row per level. */
-static int launch_slot(vtg_batch *b, BatchSlot &sl, cudaStream_t s, int nwait = 0, void *const *wait = nullptr)
+static int launch_slot(vtg_batch *b, BatchSlot &sl, cudaStream_t s, int nwait = 0, void *const *wait = nullptr,
+                       int nwait_lk = 0, void *const *wait_lk = nullptr)
 {
     for (size_t k = 0; k < sl.h_src.size(); k++)
         CU(cudaMemcpy2DAsync(sl.h_dst[k], (size_t)sl.h_w[k], sl.h_src[k], (size_t)sl.h_stride[k], (size_t)sl.h_w[k],
@@ -309,9 +310,13 @@ static int launch_slot(vtg_batch *b, BatchSlot &sl, cudaStream_t s, int nwait = 
     /* the pyramid's levels and the LK launch as a chain of programmatic dependents: each starts as the one before
      * drains; the last pyramid launch zeroes the LK launch's work counter */
     CU(vtg_launch_pyramid_batch(sl.d_pyr, sl.d_tiles, sl.tiles, sl.njobs, sl.max_levels, s, sl.d_counter, true));
+    /* what only the LK launch must wait for (earlier reads of the result buffers it writes) */
+    for (int k = 0; k < nwait_lk; k++)
+        CU(cudaStreamWaitEvent(s, (cudaEvent_t)wait_lk[k], 0));
     LkTune t = b->tune;
     t.chunk = sl.chunk;
-    CU(vtg_launch_lk_batch(sl.d_lk, sl.d_items, sl.njobs, sl.items, sl.prm, t, b->sms, sl.d_counter, s, true));
+    CU(vtg_launch_lk_batch(sl.d_lk, sl.d_items, sl.njobs, sl.items, sl.prm, t, b->sms, sl.d_counter, s,
+                           nwait_lk == 0));
     return VTG_OK;
 }
 
@@ -328,6 +333,17 @@ extern "C" int vtg_batch_launch_after(vtg_batch *b, int slot, void *stream, int 
         return VTG_EINVAL;
     CU(cudaSetDevice(vtg_ctx_device(b->ctx)));
     return launch_slot(b, b->slot[slot], stream ? (cudaStream_t)stream : b->stream, nwait, events);
+}
+
+extern "C" int vtg_batch_launch_split(vtg_batch *b, int slot, void *stream, int nwait, void *const *events,
+                                      int nwait_lk, void *const *events_lk)
+{
+    if (!b || slot < 0 || slot >= BATCH_SLOTS || !b->slot[slot].ready || nwait < 0 || (nwait > 0 && !events) ||
+        nwait_lk < 0 || (nwait_lk > 0 && !events_lk))
+        return VTG_EINVAL;
+    CU(cudaSetDevice(vtg_ctx_device(b->ctx)));
+    return launch_slot(b, b->slot[slot], stream ? (cudaStream_t)stream : b->stream, nwait, events, nwait_lk,
+                       events_lk);
 }
 
 extern "C" int vtg_batch_capture(vtg_batch *b, int slot)

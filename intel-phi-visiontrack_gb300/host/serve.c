@@ -64,7 +64,8 @@ struct slot {
     vtg_batch *b;
     vtg_search *s;
     struct vtg_found *d_found;
-    cudaEvent_t ev;
+    cudaEvent_t ev;    /* the step done: its results on the host */
+    cudaEvent_t ev_lk; /* its LK done (batched steps): the pyramid sets it read are free again */
     int busy, n;
     int *reqs;                  /* indices into the request list */
 };
@@ -196,6 +197,8 @@ int vtg_serve_run(vtg_ctx *ctx, const struct vtg_serve_cfg *c, struct vtg_serve_
         if (rc == VTG_OK && cudaMalloc((void **)&sl[k].d_found, sizeof(struct vtg_found)) != cudaSuccess)
             rc = VTG_ENOMEM;
         if (rc == VTG_OK && cudaEventCreateWithFlags(&sl[k].ev, cudaEventDisableTiming) != cudaSuccess)
+            rc = VTG_ECUDA;
+        if (rc == VTG_OK && cudaEventCreateWithFlags(&sl[k].ev_lk, cudaEventDisableTiming) != cudaSuccess)
             rc = VTG_ECUDA;
     }
     /* a template for the searches: 32 x 21 zero-mean values in 8-bit grey (its contents do not change the cost) */
@@ -336,9 +339,18 @@ int vtg_serve_run(vtg_ctx *ctx, const struct vtg_serve_cfg *c, struct vtg_serve_
                     rc = vtg_cells(tr[0], cur[0] ^ 1, cur[0], st[s].host_cells[k], NULL, VTG_HOST, bs);
             } else {
                 rc = vtg_batch_prepare(sl[k].b, 0, m, tr, fr, NULL, VTG_HOST, cur);
-                /* the uploads overlap the other slot's step; the kernels wait for it on the GPU */
+                /* the uploads overlap the other slot's step. On the GPU the pyramid waits for that step's LK (it
+                 * rewrites the sets that LK read), and the LK launch for that step's result copies (it rewrites the
+                 * buffers they read), so those copies overlap this step's pyramid */
+                void *waits_lk[SERVE_SLOTS];
+                int nl = 0;
+                for (int j = 0; j < c->inflight; j++)
+                    if (wait_slots >> j & 1u)
+                        waits_lk[nl++] = (void *)sl[j].ev_lk;
                 if (rc == VTG_OK)
-                    rc = vtg_batch_launch_after(sl[k].b, 0, NULL, nw, waits);
+                    rc = vtg_batch_launch_split(sl[k].b, 0, NULL, nl, waits_lk, nw, waits);
+                if (rc == VTG_OK && cudaEventRecord(sl[k].ev_lk, bs) != cudaSuccess)
+                    rc = VTG_ECUDA;
                 for (int i = 0; i < m && rc == VTG_OK; i++)
                     rc = vtg_tracker_results(tr[i], st[stream_of[i]].host_cells[k], NULL, VTG_HOST, bs);
             }
@@ -358,6 +370,9 @@ int vtg_serve_run(vtg_ctx *ctx, const struct vtg_serve_cfg *c, struct vtg_serve_
                 st[stream_of[i]].next++;
             }
             if (rc == VTG_OK && cudaEventRecord(sl[k].ev, bs) != cudaSuccess)
+                rc = VTG_ECUDA;
+            /* a one-pair step's LK copies its results on its way out: later steps wait for all of it */
+            if (rc == VTG_OK && (c->plain || m == 1) && cudaEventRecord(sl[k].ev_lk, bs) != cudaSuccess)
                 rc = VTG_ECUDA;
             sl[k].n = m;
             sl[k].busy = 1;
@@ -412,6 +427,8 @@ int vtg_serve_run(vtg_ctx *ctx, const struct vtg_serve_cfg *c, struct vtg_serve_
             cudaFree(sl[k].d_found);
         if (sl[k].ev)
             cudaEventDestroy(sl[k].ev);
+        if (sl[k].ev_lk)
+            cudaEventDestroy(sl[k].ev_lk);
         free(sl[k].reqs);
     }
     free(tr);
