@@ -38,6 +38,24 @@ LK_TRAFFIC_BYTES = 176_632_576 + 8_843_520
 CELLS = 16200
 
 
+def max_over_ranks(ms: float, device) -> float:
+    """The job's time: the slowest rank's (every rank times its own replica between the same barriers). One process:
+    its own."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return ms
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_cells_per_s(world: int, streams: int, cells: int, steps: int, total_ms: float) -> float:
+    """Cells every rank tracked over the job's time: world replicas of `streams` streams of `cells` cells a step."""
+    return world * streams * cells * steps / (total_ms / 1e3)
+
+
 def workload(form: str, streams: int) -> dict:
     return {"workload": "per-cell LK flow, 1920x1080 frame pairs, 4 levels, 16,200 cells (16x8), 21x21 patch, "
                         "<=10 iters, eps 0.01, fb 0.5",
@@ -284,11 +302,8 @@ def run_ours(args) -> dict | None:
     torch.cuda.synchronize()
     step_ms = np.array([a.elapsed_time(b) for a, b in ev])
     total_ms = float(step_ms.sum())
-    if world > 1:
-        tt = torch.tensor([total_ms], device=device)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(tt.item())
-    value = world * B * CELLS * args.steps / (total_ms / 1e3)
+    total_ms = max_over_ranks(total_ms, device)
+    value = whole_job_cells_per_s(world, B, CELLS, args.steps, total_ms)
 
     # ---- rooflines: the LK launch and the pyramid launches of a batched step, timed apart
     pyr_ms, lk_ms = batch.profile(1, reps=7)
