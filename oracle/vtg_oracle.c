@@ -5,12 +5,16 @@
  * project's own code, for checking the CUDA kernels:
  *   - the pyramid: u8 -> Q6 (src/kern/img_ref.c:32-40) and the 5 x 5 binomial reduce with clamp-to-edge borders
  *     (src/kern/img_ref.c:9-30, 74-114); exact integers;
+ *   - tk_build's optional input steps (src/kern/track.c:600-622): the contrast stretch (img_minmax, img_norm,
+ *     img_ref.c:42-71, with the gain and offset formed as the x87 unit forms them, in exact integer arithmetic) and
+ *     the 5 x 5 binomial at every pixel (img_gauss5, img_ref.c:83-96); and the M1 gate's img_sobel / img_absdiff
+ *     (img_ref.c:116-137);
  *   - one point of pyramidal LK: the driver of src/kern/lk_driver.inc:7-109 and the three patch operations of
  *     src/kern/lk_vx.c:36-175, and the forward-backward check (src/kern/lk_driver.inc:111-121);
  *   - the per-cell grid of src/kern/still.c:116-141, generalised to any cell size and patch;
  *   - the appearance correlation of src/kern/track.c:184-206, its half-pixel form (track.c:1615-1647), the parabola
  *     (track.c:1650-1657), the per-cell map (track.c:301-329) and the top-8 search (track.c:1661-1726), generalised to
- *     a T_w x T_h template (T_w a multiple of 16);
+ *     a T_w x T_h template (T_w a multiple of 16); and the template cut of store_appearance (track.c:935-974);
  *   - corner detection: the Harris response over Sobel gradients on a 5 x 5 box and the cells' strongest responses
  *     in the reference's F32 operation order (src/kern/detect.c:68-141), exact in any IEEE arithmetic, and the
  *     selection of detect_finish (detect.c:175-258), long double as the reference;
