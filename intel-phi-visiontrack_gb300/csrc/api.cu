@@ -3,7 +3,9 @@
  * A tracker is one camera stream's device-resident state, the GPU form of the reference's struct tracker
  * (src/kern/track.c:75-160) as far as this path goes: two pyramid sets (the ring tk_sets describes), the frame staging
  * buffer, the pyramids' descriptors, and the cell results, all in one device allocation charged to the context's
- * budget. Each tracker owns a CUDA stream; its work is ordered there. */
+ * budget, with the build options' scratch and the appearance template's. Each tracker owns a CUDA stream; its work is
+ * ordered there. The appearance template cut (store_appearance, track.c:935-974) is here too, as one warp's kernel on
+ * the resident pyramid. */
 #include <chrono>
 #include <mutex>
 #include <new>
