@@ -33,7 +33,8 @@ sys.path.insert(0, PKG)
 
 METRIC = "LK cells/s + p99 ms/frame-pair, served-batched vs plain GPU; ≤0.01px vs FP64"
 W, H, LEVELS, CELL_W, CELL_H, PATCH = 1920, 1080, 4, 16, 8, 21
-# DRAM bytes (read + write) of one batched LK launch of 8 streams, from ncu (profiles/lk_batch_kernel_1080p_x8.md)
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one batched LK launch of 8 such streams, from an ncu
+# capture of `bench.py --profile batch` (the same kernel and launch shape); a constant, not measured by this run
 LK_TRAFFIC_BYTES = 176_632_576 + 8_843_520
 CELLS = 16200
 
@@ -107,14 +108,12 @@ class Clocks:
                 "reasons": reasons, "samples": len(sm)}
 
 
-def lk_flops(lk: np.ndarray, levels: int = LEVELS, w: int = PATCH, h: int = PATCH) -> float:
-    """Algorithmic FLOPs of computed cells, counting the reference's patch operations (src/kern/lk_ref.c) with FMA = 2:
-    build 9 (W+2)(H+2) + 20 W H per level, iterate 14 W H per iteration, residual 12 W H; the forward-backward track
-    costs the same again for the cells that ran it (its iteration count taken equal to the forward track's)."""
+def lk_flops(work: dict, w: int = PATCH, h: int = PATCH) -> float:
+    """Algorithmic FLOPs of one LK launch from its counted work (vtg_batch_count: every template build, iteration and
+    residual pass of both walks of every cell), with the reference's operation counts per patch operation
+    (src/kern/lk_ref.c, FMA = 2): build 9 (W+2)(H+2) + 20 W H, iterate 14 W H, residual 12 W H."""
     build = 9 * (w + 2) * (h + 2) + 20 * w * h
-    fwd = levels * build + 14 * w * h * lk["iters"].astype(np.float64) + 12 * w * h
-    back = np.where((lk["status"] == 0) | (lk["status"] == 8), fwd, 0.0)
-    return float(np.sum(fwd + back))
+    return float(work["builds"] * build + work["iterations"] * 14 * w * h + work["residuals"] * 12 * w * h)
 
 
 def peaks() -> dict:
@@ -307,19 +306,23 @@ def run_ours(args) -> dict | None:
 
     # ---- rooflines: the LK launch and the pyramid launches of a batched step, timed apart
     pyr_ms, lk_ms = batch.profile(1, reps=7)
-    flops = sum(lk_flops(vtg.tracker_results(t)[1]) for t in trackers)
+    work = batch.count(1)
+    flops = lk_flops(work)
     pk = peaks()
     sm_max = pk.get("sm_max_mhz", 2070.0)
-    fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    fp32_peak = sms * 128 * 2 * sm_max * 1e6 / 1e12
     achieved = flops / (lk_ms / 1e3) / 1e12
     roofline = {"kernel": "lk_batch_kernel", "bound": "fp32", "achieved": achieved, "peak": fp32_peak,
                 "unit": "TFLOP/s", "frac": achieved / fp32_peak,
-                "peak_source": "nominal FP32 CUDA-core rate (152 SMs x 128 lanes x 2) at the measured max SM clock "
-                               "(MEASURED_PEAKS.json sm_max_mhz); MEASURED_PEAKS.json holds no FP32 rate",
-                "algorithmic_flop_per_launch": flops, "launch_ms": lk_ms, "traffic": LK_TRAFFIC_BYTES * B / 8,
-                "traffic_note": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch of this step "
-                                "(profiles/lk_batch_kernel_1080p_x8.md); the algorithmic bytes are the 8 streams' "
-                                "two pyramid sets read once plus the cell records written"}
+                "peak_source": "nominal FP32 CUDA-core rate (%d SMs x 128 lanes x 2) at the measured max SM clock "
+                               "(MEASURED_PEAKS.json sm_max_mhz); MEASURED_PEAKS.json holds no FP32 rate" % sms,
+                "algorithmic_flop_per_launch": flops, "work_per_launch": work, "launch_ms": lk_ms,
+                "traffic": LK_TRAFFIC_BYTES * B / 8,
+                "traffic_source": "constant: ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch of this "
+                                  "step (8 streams, scaled by streams / 8), captured apart from this run",
+                "traffic_note": "the algorithmic bytes are the streams' two pyramid sets read once plus the cell "
+                                "records written"}
     pyr_bytes = B * (W * H + 4 * sum(a * b for a, b in [(1920, 1080), (960, 540), (480, 270), (240, 135)]))
     roof_pyr = {"kernel": "pyr_batch_kernel (3 launches a step)", "bound": "hbm",
                 "achieved": pyr_bytes / (pyr_ms / 1e3) / 1e9, "peak": pk.get("hbm_gbs", 6800.0), "unit": "GB/s",
@@ -330,6 +333,7 @@ def run_ours(args) -> dict | None:
     for t in trackers:
         t.close()
     mix64 = time_batched_mix(vtg, torch, ctx, device)
+    ncc = ncc_config3(vtg, torch, ctx)
 
     # ---- end to end: the served loop through the C ABI, pinned host frames in, cell records out
     pinned = []
@@ -393,7 +397,8 @@ def run_ours(args) -> dict | None:
                            "plain": {k: mixed_plain[k] for k in ("cells_per_s", "p50_ms", "p99_ms", "served")},
                            "streams": "2x1080p@60 (4,080 cells), 1x720p@15, 13 more 640x480..1080p@30"},
             # a batched step: one pyramid launch for each level above 0, then one LK launch
-            "roofline": roofline, "roofline_pyramid": roof_pyr, "gpu_launches": args.steps * ((LEVELS - 1) + 1),
+            "roofline": roofline, "roofline_pyramid": roof_pyr, "ncc": ncc,
+            "gpu_launches": args.steps * ((LEVELS - 1) + 1),
             "clocks": clk.summary()}
     line["cpu_baseline"] = cpu_baseline(pairs[0])
     return line
@@ -466,62 +471,86 @@ def run_reference(args) -> dict | None:
             "e2e": {"value": value, "unit": "cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def ncc_config3(vtg, torch, ctx, templates: int = 10, reps: int = 5) -> dict:
+    """The whole-picture appearance search at the NCC configuration: a seeded 1920 x 1080 8-bit frame, templates of 32,
+    64 and 96 cut at seeded corners and perturbed (gain 0.8-1.2, offset +-20, noise sigma 3), one in ten near-blank
+    (standard deviation below 2), step 1, per map precision (F32 on CUDA cores, BF16 and FP16 on the tensor cores).
+    Per size and precision: the CUDA-event time of the map kernel alone and of the whole search (window sums, map,
+    eight candidates, half-pixel re-score; median over the templates of the median of `reps` runs), the map's useful
+    FLOP rate (2 T^2 per corner) and its fraction of the measured BF16 burst rate, the found corner against the true one
+    and the F32 map's, the score against the FP64 oracle at the found half-pixel corner, and the near-blank templates'
+    best scores (a match would be 0.5 or more)."""
+    sys.path.insert(0, ORACLE)
+    import oracle as O
+    import vtg_synth as S
+
+    frame = S.noise_frame(W, H, seed=3)
+    fplane = frame.astype(np.float32)
+    d = torch.from_numpy(frame).cuda()
+    torch.cuda.synchronize()
+    s = vtg.Search(ctx, W, H)
+    pk = peaks()
+    peak = pk.get("bf16_tflops", 1900.0)
+    names = ((vtg.NCC_F32, "f32"), (vtg.NCC_BF16, "bf16"), (vtg.NCC_FP16, "fp16"))
+    out = {"frame": "%dx%d u8, seeded blurred noise" % (W, H), "templates_per_size": templates, "step": 1,
+           "peak_bf16_tflops": peak,
+           "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst; of measured)" if "bf16_tflops" in pk else
+           "fallback 1.9 PFLOP/s", "sizes": {}}
+    for size in (32, 64, 96):
+        tpl, xs, ys, blank = S.ncc_templates(frame, size, templates, seed=size, blank_share=0.1)
+        corners = (W - size - 2) * (H - size - 2)
+        rows = {name: {"map_ms": [], "search_ms": [], "found_true": 0, "agree_f32": 0, "err_fp64": 0.0,
+                       "blank_best": []} for _, name in names}
+        for k in range(templates):
+            app = (tpl[k].astype(np.float32) - np.float32(tpl[k].mean(dtype=np.float64))).astype(np.float32)
+            norm = float(np.sum(app.astype(np.float64) ** 2))
+            s.template(app, norm)
+            f32 = None
+            for prec, name in names:
+                f = s.run(d.data_ptr(), W, H, W, vtg.PLANE_U8, 1, W, 1, H, 1, prec)
+                f32 = f if prec == vtg.NCC_F32 else f32
+                mms, tms = s.profile(d.data_ptr(), W, H, W, vtg.PLANE_U8, 1, W, 1, H, 1, prec,
+                                     reps=3 if prec == vtg.NCC_F32 else reps)
+                r = rows[name]
+                r["map_ms"].append(mms)
+                r["search_ms"].append(tms)
+                if blank[k]:
+                    r["blank_best"].append(f["ncc"])
+                    continue
+                r["found_true"] += int((f["hx"], f["hy"]) == (2 * int(xs[k]), 2 * int(ys[k])))
+                r["agree_f32"] += int((f["hx"], f["hy"]) == (f32["hx"], f32["hy"]))
+                o = O.ncc_half(fplane, app, norm, f["hx"], f["hy"], O.F64)
+                r["err_fp64"] = max(r["err_fp64"], abs(f["ncc"] - o))
+        res = {}
+        nb = int(blank.sum())
+        for _, name in names:
+            r = rows[name]
+            map_ms = float(np.median(r["map_ms"]))
+            tflops = 2.0 * size * size * corners / (map_ms / 1e3) / 1e12
+            res[name] = {"map_ms": map_ms, "search_ms": float(np.median(r["search_ms"])),
+                         "map_tflops_useful": tflops, "frac_of_bf16_burst": tflops / peak,
+                         "found_true": "%d/%d" % (r["found_true"], templates - nb),
+                         "agree_with_f32": "%d/%d" % (r["agree_f32"], templates - nb),
+                         "max_score_err_vs_fp64": r["err_fp64"],
+                         "near_blank": {"templates": nb, "best_scores": r["blank_best"],
+                                        "matched": int(sum(v >= 0.5 for v in r["blank_best"]))}}
+        out["sizes"][str(size)] = res
+    s.close()
+    return out
+
+
 def run_ncc(args) -> dict:
-    """The whole-picture appearance search over a 1920 x 1080 8-bit frame, templates of 32, 64 and 96 (5 each, one in
-    ten near-blank at 10 %, here one of each size), per map precision: CUDA-event time of the whole search (integral
-    images, map, eight candidates, half-pixel re-score), the map's tensor FLOP rate, and agreement: the found corner
-    against the true one and against the F32 map's, the score against the FP64 oracle at the found corner."""
+    """`--ncc`: the appearance search at the NCC configuration alone (see ncc_config3)."""
     import torch
 
     import vtg
     import vtg_build
-    import vtg_synth as S
-
-    sys.path.insert(0, ORACLE)
-    import oracle as O
 
     vtg_build.build()
-    frame = S.noise_frame(W, H, seed=3)
-    d = torch.from_numpy(frame).cuda()
-    torch.cuda.synchronize()
     ctx = vtg.Context(0)
-    s = vtg.Search(ctx, W, H)
-    stream = torch.cuda.ExternalStream(vtg.lib().vtg_search_stream(s.h))
     out = {"metric": "appearance search ms per template (whole 1920x1080 picture, step 1)", "unit": "ms",
-           "higher_is_better": False, "results": []}
-    pk = peaks()
-    for size in (32, 64, 96):
-        tpl, xs, ys, blank = S.ncc_templates(frame, size, 5, seed=size, blank_share=0.2)
-        for k in range(5):
-            app = (tpl[k].astype(np.float32) - np.float32(tpl[k].mean(dtype=np.float64))).astype(np.float32)
-            norm = float(np.sum(app.astype(np.float64) ** 2))
-            s.template(app, norm)
-            row = {"size": size, "blank": bool(blank[k]), "true": [int(xs[k]), int(ys[k])]}
-            for prec, name in ((vtg.NCC_F32, "f32"), (vtg.NCC_BF16, "bf16"), (vtg.NCC_FP16, "fp16")):
-                reps = 3 if prec == vtg.NCC_F32 else 10
-                s.run(d.data_ptr(), W, H, W, vtg.PLANE_U8, 1, W, 1, H, 1, prec)
-                ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
-                for a, b in ev:
-                    a.record(stream)
-                    f = s.run(d.data_ptr(), W, H, W, vtg.PLANE_U8, 1, W, 1, H, 1, prec)
-                    b.record(stream)
-                torch.cuda.synchronize()
-                ms = float(np.median([a.elapsed_time(b) for a, b in ev]))
-                corners = (W - size - 2) * (H - size - 2)
-                row[name] = {"ms": ms, "found": [f["hx"] / 2, f["hy"] / 2], "ncc": f["ncc"], "second": f["second"]}
-                if prec != vtg.NCC_F32:
-                    row[name]["map_tflops_useful"] = 2.0 * size * size * corners / (ms / 1e3) / 1e12
-            o = O.ncc_half(frame.astype(np.float32), app, norm, int(row["f32"]["found"][0] * 2),
-                           int(row["f32"]["found"][1] * 2), O.F64)
-            row["fp64_score_at_found"] = o
-            row["score_err_f32"] = abs(row["f32"]["ncc"] - o)
-            row["agree_bf16_f32"] = row["bf16"]["found"] == row["f32"]["found"]
-            row["agree_fp16_f32"] = row["fp16"]["found"] == row["f32"]["found"]
-            row["found_true"] = row["f32"]["found"] == row["true"]
-            out["results"].append(row)
-    s.close()
+           "higher_is_better": False, **ncc_config3(vtg, torch, ctx)}
     ctx.close()
-    out["peak_bf16_tflops"] = pk.get("bf16_tflops")
     return out
 
 

@@ -221,6 +221,11 @@ int vtg_batch_autotune(vtg_batch *b, int slot, int reps, struct vtg_tune *best, 
 /* Runs a prepared step reps times with events between its phases: the median time of the pyramids (with any host
  * frames' upload) and of the LK launch. For rooflines. */
 int vtg_batch_profile(vtg_batch *b, int slot, int reps, float *pyr_ms, float *lk_ms);
+/* Runs a prepared step's LK launch once more (its pyramids as they stand) and counts the work of every cell's walks,
+ * forward and backward: counts[0] template builds, [1] residual passes, [2] window passes, [3] iterations. With the
+ * reference's operation counts per patch operation (src/kern/lk_ref.c) they give the launch's algorithmic FLOPs.
+ * Waits for the result. */
+int vtg_batch_count(vtg_batch *b, int slot, uint64_t *counts);
 
 /* ---- the appearance search (reacquisition) ---- */
 
@@ -261,6 +266,11 @@ int vtg_search_template(vtg_search *s, const float *app, int tw, int th, float n
 int vtg_search_run(vtg_search *s, const void *plane, int w, int h, int pitch, int plane_type, int x0, int x1, int y0,
                    int y1, int step, int precision, struct vtg_found *found, float *map_v, int *map_x, int *map_y,
                    int where, void *stream);
+/* Runs vtg_search_run's work reps times (after one warm-up) on the search's stream and reports the median CUDA-event
+ * time of the correlation map's kernel alone and of the whole search (window sums, map, candidates, half-pixel
+ * re-score). For rooflines. */
+int vtg_search_profile(vtg_search *s, const void *plane, int w, int h, int pitch, int plane_type, int x0, int x1,
+                       int y0, int y1, int step, int precision, int reps, float *map_ms, float *total_ms);
 /* tk_correlate (src/kern/track.c:208, track.h:59) at n corners: the score of each, -1 where the template does not fit. */
 int vtg_correlate(vtg_search *s, const void *plane, int w, int h, int pitch, int plane_type, int n, const int *xs,
                   const int *ys, float *out, int where, void *stream);
@@ -276,9 +286,11 @@ int vtg_correlate(vtg_search *s, const void *plane, int w, int h, int pitch, int
  * search as vtg_search_run with an F32 map, but nothing is allocated: no context, no search context; the caller
  * passes the plane, the template (th rows of tw zero-mean floats, tw a multiple of 8) and its norm, and *found (and the
  * optional per-cell map) in device memory; the scratch lives in one fixed device array of VTG_NOALLOC_SCRATCH_BYTES.
- * Larger planes or templates than the limits above, or a step above 4, return VTG_EINVAL. All calls share that array: calls whose work
- * overlaps on the GPU race, so order them on one stream. The first call on a device looks the array's address up;
- * make it before any stream capture. Asynchronous on `stream` (a cudaStream_t, NULL for the legacy default). */
+ * Larger planes or templates than the limits above, or a step other than 1, 2 or 4, return VTG_EINVAL. All calls
+ * share that array: calls whose work overlaps on the GPU race, so order them on one stream. The first call on a device
+ * looks the array's address up and keeps it for the life of the process; make it before any stream capture, and do
+ * not call this entry point on a device after cudaDeviceReset of that device. Asynchronous on `stream` (a
+ * cudaStream_t, NULL for the legacy default). */
 int vtg_search_run_noalloc(const void *plane, int w, int h, int pitch, int plane_type, const float *app, int tw, int th,
                            float norm, int x0, int x1, int y0, int y1, int step, struct vtg_found *found, float *map_v,
                            int *map_x, int *map_y, void *stream);

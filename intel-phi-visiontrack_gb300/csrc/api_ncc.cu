@@ -1,7 +1,9 @@
 /* api_ncc.cu -- the C ABI of the appearance search (include/vtg.h): search contexts, their template, the search and
  * tk_correlate. */
+#include <algorithm>
 #include <mutex>
 #include <new>
+#include <vector>
 
 #include "vtg_ncc.cuh"
 #include "vtg_ctx.h"
@@ -155,6 +157,7 @@ extern "C" int vtg_search_create(vtg_ctx *ctx, int max_w, int max_h, int max_tw,
     s->sc.fac = (float *)(s->mem + L.fac);
     s->sc.fac_elems = L.fac_elems;
     s->sc.cellw = (unsigned long long *)(s->mem + L.cellw);
+    s->sc.map_ev0 = s->sc.map_ev1 = nullptr;
     s->found = (vtg_found *)(s->mem + L.found);
     s->xy = nullptr;
     s->vals = nullptr;
@@ -309,5 +312,63 @@ extern "C" int vtg_correlate(vtg_search *s, const void *plane, int w, int h, int
     CU(cudaMemcpyAsync(out, dv, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, st));
     CU(cudaFreeAsync(d, st));
     CU(cudaStreamSynchronize(st));
+    return VTG_OK;
+}
+
+extern "C" int vtg_search_profile(vtg_search *s, const void *plane, int w, int h, int pitch, int plane_type, int x0,
+                                  int x1, int y0, int y1, int step, int precision, int reps, float *map_ms,
+                                  float *total_ms)
+{
+    if (!s || !plane || reps < 1 || pitch < w || (plane_type != VTG_PLANE_U8 && plane_type != VTG_PLANE_F32) ||
+        (precision != VTG_NCC_F32 && plane_type != VTG_PLANE_U8))
+        return VTG_EINVAL;
+    NccPrm p;
+    bool empty = false;
+    const int chk = make_prm(s, w, h, x0, x1, y0, y1, step, precision, &p, &empty);
+    if (chk != VTG_OK)
+        return chk;
+    if (empty)
+        return VTG_EINVAL;
+    CU(cudaSetDevice(vtg_ctx_device(s->ctx)));
+    cudaEvent_t ev[4];
+    for (int k = 0; k < 4; k++)
+        CU(cudaEventCreate(&ev[k]));
+    NccScratch sc = s->sc;
+    sc.band = precision == VTG_NCC_BF16 ? s->band[0] : precision == VTG_NCC_FP16 ? s->band[1] : nullptr;
+    sc.map_ev0 = ev[1];
+    sc.map_ev1 = ev[2];
+    std::vector<float> tm, tt;
+    int rc = VTG_OK;
+    for (int r = 0; r < reps + 1 && rc == VTG_OK; r++) {
+        cudaError_t e = cudaEventRecord(ev[0], s->stream);
+        if (e == cudaSuccess)
+            e = vtg_launch_ncc(plane, pitch, plane_type, s->app, p, sc, precision, s->found, s->stream);
+        if (e == cudaSuccess)
+            e = cudaEventRecord(ev[3], s->stream);
+        if (e == cudaSuccess)
+            e = cudaEventSynchronize(ev[3]);
+        float a = 0.0f, b = 0.0f;
+        if (e == cudaSuccess)
+            e = cudaEventElapsedTime(&a, ev[1], ev[2]);
+        if (e == cudaSuccess)
+            e = cudaEventElapsedTime(&b, ev[0], ev[3]);
+        if (e != cudaSuccess) {
+            vtg_set_cuda_error(e);
+            rc = VTG_ECUDA;
+        } else if (r > 0) { /* the first run warms up */
+            tm.push_back(a);
+            tt.push_back(b);
+        }
+    }
+    for (int k = 0; k < 4; k++)
+        cudaEventDestroy(ev[k]);
+    if (rc != VTG_OK)
+        return rc;
+    std::sort(tm.begin(), tm.end());
+    std::sort(tt.begin(), tt.end());
+    if (map_ms)
+        *map_ms = tm[tm.size() / 2];
+    if (total_ms)
+        *total_ms = tt[tt.size() / 2];
     return VTG_OK;
 }

@@ -32,6 +32,7 @@ struct BatchSlot {
     LkJob *d_lk;
     int *d_items;   /* [max_jobs + 1] */
     int *d_counter;
+    unsigned long long *d_count; /* vtg_batch_count's four totals, in the counter's 256-byte block */
     int njobs, max_levels, items, cells;
     int chunk; /* cells per work item the item table was laid out for */
     int tiles[VTG_MAX_LEVELS];
@@ -129,6 +130,7 @@ extern "C" int vtg_batch_create(vtg_ctx *ctx, int max_jobs, vtg_batch **out)
         sl.d_items = (int *)m;
         m += up256(sizeof(int) * (size_t)(max_jobs + 1));
         sl.d_counter = (int *)m;
+        sl.d_count = (unsigned long long *)(m + 64);
         sl.ready = false;
         sl.has_graph = false;
         sl.njobs = sl.items = sl.cells = 0;
@@ -569,5 +571,25 @@ extern "C" int vtg_batch_profile(vtg_batch *b, int slot, int reps, float *pyr_ms
         *pyr_ms = tp[tp.size() / 2];
     if (lk_ms)
         *lk_ms = tl[tl.size() / 2];
+    return VTG_OK;
+}
+
+extern "C" int vtg_batch_count(vtg_batch *b, int slot, uint64_t *counts)
+{
+    if (!b || slot < 0 || slot >= BATCH_SLOTS || !b->slot[slot].ready || !counts)
+        return VTG_EINVAL;
+    BatchSlot &sl = b->slot[slot];
+    LkTune t = b->tune;
+    t.chunk = sl.chunk;
+    CU(cudaSetDevice(vtg_ctx_device(b->ctx)));
+    CU(cudaMemsetAsync(sl.d_count, 0, 4 * sizeof(unsigned long long), b->stream));
+    CU(cudaMemsetAsync(sl.d_counter, 0, sizeof(int), b->stream));
+    CU(vtg_launch_lk_batch(sl.d_lk, sl.d_items, sl.njobs, sl.items, sl.prm, t, b->sms, sl.d_counter, b->stream, false,
+                           sl.d_count));
+    unsigned long long h[4];
+    CU(cudaMemcpyAsync(h, sl.d_count, sizeof h, cudaMemcpyDeviceToHost, b->stream));
+    CU(cudaStreamSynchronize(b->stream));
+    for (int k = 0; k < 4; k++)
+        counts[k] = h[k];
     return VTG_OK;
 }

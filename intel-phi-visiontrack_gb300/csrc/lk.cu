@@ -534,9 +534,17 @@ __device__ __forceinline__ void split(int base, float t, int &i, float &f)
 }
 
 /* The pyramid walk (src/kern/lk_driver.inc:7-109), warp-uniform, F32. */
+/* The work one point's walks did, for counting runs (vtg_batch_count): template builds, window passes, residual passes
+ * and iterations, packed into one warp-uniform word (LK_WORK_* shifts). */
+#define LK_WORK_BUILD 1u
+#define LK_WORK_RESID (1u << 5)
+#define LK_WORK_PASS (1u << 8)
+#define LK_WORK_ITER (1u << 16)
+
 template <int MAXH, bool EXACT, bool TS>
 __device__ __forceinline__ void lk_track(const DevPyr &I, const DevPyr &J, int top, const LkPrm &p, float x, float y,
-                                         float gx0, float gy0, int lane, Patch<MAXH, TS> &P, vtg_lk_out &o)
+                                         float gx0, float gy0, int lane, Patch<MAXH, TS> &P, vtg_lk_out &o,
+                                         unsigned &work)
 {
     const int W = p.W, H = EXACT ? MAXH : p.H;
     const int mx = W / 2 + 1, my = H / 2 + 1;
@@ -562,6 +570,7 @@ __device__ __forceinline__ void lk_track(const DevPyr &I, const DevPyr &J, int t
         const float rx = px - fpx, ry = py - fpy; /* exact */
         float gxx, gxy, gyy, tc, cx, cy;
         lk_build<MAXH, EXACT, TS>(IL, bx, rx, by, ry, W, H, lane, P, gxx, gxy, gyy, tc, cx, cy);
+        work += LK_WORK_BUILD;
         /* det = gxx gyy - gxy^2 by Kahan's product difference; the smaller eigenvalue as det / lambda_max. */
         const float w2 = gxy * gxy;
         const float e2 = __fmaf_rn(gxy, gxy, -w2);
@@ -612,6 +621,7 @@ __device__ __forceinline__ void lk_track(const DevPyr &I, const DevPyr &J, int t
             split(by, qy, jy, fy);
             if (jx != cjx || jy != cjy) {
                 lk_correlate<MAXH, EXACT, TS>(JL, jx, jy, W, H, lane, P, tc, X);
+                work += LK_WORK_PASS;
                 cjx = jx;
                 cjy = jy;
             }
@@ -620,6 +630,7 @@ __device__ __forceinline__ void lk_track(const DevPyr &I, const DevPyr &J, int t
             vx += ex;
             vy += ey;
             iters++;
+            work += LK_WORK_ITER;
             if (__fmaf_rn(ex, ex, ey * ey) < p.eps2)
                 break;
         }
@@ -651,6 +662,7 @@ __device__ __forceinline__ void lk_track(const DevPyr &I, const DevPyr &J, int t
             split(by, qy, jy, fy);
             float sa, ss;
             lk_sample<MAXH, EXACT, true, TS>(J0, jx, fx, jy, fy, W, H, lane, P, sa, ss);
+            work += LK_WORK_RESID;
             const float r0 = sa / p.area, r1 = ss / p.area;
             o.residual = r0;
             if (r0 > p.max_residual)
@@ -668,13 +680,14 @@ __device__ __forceinline__ void lk_track(const DevPyr &I, const DevPyr &J, int t
  * found point tracked back from J to I from minus the found flow. One copy of the walk serves both passes. */
 template <int MAXH, bool EXACT, bool TS>
 __device__ __forceinline__ void lk_point(const DevPyr &I, const DevPyr &J, int top, const LkPrm &p, float x, float y,
-                                         float gx, float gy, int lane, Patch<MAXH, TS> &P, vtg_lk_out &o)
+                                         float gx, float gy, int lane, Patch<MAXH, TS> &P, vtg_lk_out &o,
+                                         unsigned &work)
 {
     const int passes = p.fb_max2 > 0.0f ? 2 : 1;
     float sx = x, sy = y;
     for (int pass = 0; pass < passes; pass++) {
         vtg_lk_out r;
-        lk_track<MAXH, EXACT, TS>(pass ? J : I, pass ? I : J, top, p, sx, sy, gx, gy, lane, P, r);
+        lk_track<MAXH, EXACT, TS>(pass ? J : I, pass ? I : J, top, p, sx, sy, gx, gy, lane, P, r, work);
         if (pass == 0) {
             o = r;
             if (o.status)
@@ -720,10 +733,21 @@ __device__ __forceinline__ float cell_diff(const DevLevel &A, const DevLevel &B,
 
 /* One cell of a grid: its centre (cw c + cw / 2, ch r + ch / 2), clamped to where the patch fits (still.c:127-130),
  * LK with the forward-backward check, and the cell record (still.c:132-140). The whole warp calls it. */
+/* Adds one point's work word to the four counters (template builds, residual passes, window passes, iterations). */
+__device__ __forceinline__ void lk_count(unsigned long long *count, unsigned work, int lane)
+{
+    if (count && lane == 0) {
+        atomicAdd(count + 0, (unsigned long long)(work & 31u));
+        atomicAdd(count + 1, (unsigned long long)((work >> 5) & 7u));
+        atomicAdd(count + 2, (unsigned long long)((work >> 8) & 255u));
+        atomicAdd(count + 3, (unsigned long long)(work >> 16));
+    }
+}
+
 template <int MAXH, bool EXACT, bool TS>
 __device__ __forceinline__ void lk_cell(const DevPyr &I, const DevPyr &J, int top, const LkPrm &p, const CellGrid &g,
                                         int base_w, int base_h, int i, int lane, vtg_lk_out *__restrict__ out,
-                                        vtg_cell *__restrict__ cells, f2_t *ts)
+                                        vtg_cell *__restrict__ cells, f2_t *ts, unsigned long long *count = nullptr)
 {
     const int col = i % g.cols, row = i / g.cols;
     const float mx = (float)(p.W / 2 + 2), my = (float)(p.H / 2 + 2);
@@ -733,7 +757,9 @@ __device__ __forceinline__ void lk_cell(const DevPyr &I, const DevPyr &J, int to
     Patch<MAXH, TS> P;
     P.ts = ts;
     vtg_lk_out o;
-    lk_point<MAXH, EXACT, TS>(I, J, top, p, x, y, 0.0f, 0.0f, lane, P, o);
+    unsigned work = 0;
+    lk_point<MAXH, EXACT, TS>(I, J, top, p, x, y, 0.0f, 0.0f, lane, P, o, work);
+    lk_count(count, work, lane);
     if (out)
         store_out(out + i, o, lane);
     if (cells) {
@@ -774,7 +800,8 @@ template <int MAXH, bool EXACT, bool PERSISTENT, int WARPS, int MINB, bool TS>
 __global__ void __launch_bounds__(WARPS * 32, MINB) lk_batch_kernel(const LkJob *__restrict__ jobs,
                                                                     const int *__restrict__ item_start, int njobs,
                                                                     int items, int chunk, LkPrm p,
-                                                                    int *__restrict__ counter)
+                                                                    int *__restrict__ counter,
+                                                                    unsigned long long *__restrict__ count)
 {
     __shared__ int s_start[LK_BATCH_MAX_JOBS + 1];
     extern __shared__ f2_t s_t[]; /* TS: WARPS x (MAXH / 2) x 32 pairs */
@@ -805,7 +832,8 @@ __global__ void __launch_bounds__(WARPS * 32, MINB) lk_batch_kernel(const LkJob 
         const LkJob &jb = jobs[lo];
         const int c0 = (item - s_start[lo]) * chunk, c1 = min(c0 + chunk, jb.g.n);
         for (int c = c0; c < c1; c++)
-            lk_cell<MAXH, EXACT, TS>(*jb.I, *jb.J, jb.top, p, jb.g, jb.base_w, jb.base_h, c, lane, jb.out, jb.cells, ts);
+            lk_cell<MAXH, EXACT, TS>(*jb.I, *jb.J, jb.top, p, jb.g, jb.base_w, jb.base_h, c, lane, jb.out, jb.cells, ts,
+                                     count);
         if (!PERSISTENT)
             break;
     }
@@ -813,13 +841,14 @@ __global__ void __launch_bounds__(WARPS * 32, MINB) lk_batch_kernel(const LkJob 
 
 template <int MAXH, bool EXACT>
 static cudaError_t lk_batch_launch(const LkJob *jobs, const int *item_start, int njobs, int items, const LkPrm &p,
-                                   const LkTune &t, int sms, int *counter, cudaStream_t s, bool pdl)
+                                   const LkTune &t, int sms, int *counter, cudaStream_t s, bool pdl,
+                                   unsigned long long *count)
 {
 #define LKB(P, WARPS, MINB)                                                                                            \
     do {                                                                                                               \
         const int blocks = P ? sms * t.ctas_per_sm : (items + WARPS - 1) / WARPS;                                      \
         const cudaError_t e = vtg_launch_k(lk_batch_kernel<MAXH, EXACT, P, WARPS, MINB, false>, blocks, WARPS * 32, 0, \
-                                           s, pdl, jobs, item_start, njobs, items, t.chunk, p, counter);               \
+                                           s, pdl, jobs, item_start, njobs, items, t.chunk, p, counter, count);        \
         if (e != cudaSuccess)                                                                                          \
             return e;                                                                                                  \
     } while (0)
@@ -835,7 +864,7 @@ static cudaError_t lk_batch_launch(const LkJob *jobs, const int *item_start, int
         }                                                                                                              \
         const cudaError_t e2 = vtg_launch_k(lk_batch_kernel<MAXH, EXACT, true, WARPS, MINB, true>,                    \
                                             sms * t.ctas_per_sm, WARPS * 32, smem, s, pdl, jobs, item_start, njobs,    \
-                                            items, t.chunk, p, counter);                                               \
+                                            items, t.chunk, p, counter, count);                                        \
         if (e2 != cudaSuccess)                                                                                         \
             return e2;                                                                                                 \
     } while (0)
@@ -868,15 +897,16 @@ static cudaError_t lk_batch_launch(const LkJob *jobs, const int *item_start, int
 }
 
 cudaError_t vtg_launch_lk_batch(const LkJob *jobs, const int *item_start, int njobs, int items, const LkPrm &p,
-                                const LkTune &tune, int sms, int *counter, cudaStream_t s, bool pdl)
+                                const LkTune &tune, int sms, int *counter, cudaStream_t s, bool pdl,
+                                unsigned long long *count)
 {
     if (njobs < 1 || njobs > LK_BATCH_MAX_JOBS || items <= 0)
         return items <= 0 ? cudaSuccess : cudaErrorInvalidValue;
     if (p.H == 21)
-        return lk_batch_launch<21, true>(jobs, item_start, njobs, items, p, tune, sms, counter, s, pdl);
+        return lk_batch_launch<21, true>(jobs, item_start, njobs, items, p, tune, sms, counter, s, pdl, count);
     if (p.H == 15)
-        return lk_batch_launch<15, true>(jobs, item_start, njobs, items, p, tune, sms, counter, s, pdl);
-    return lk_batch_launch<31, false>(jobs, item_start, njobs, items, p, tune, sms, counter, s, pdl);
+        return lk_batch_launch<15, true>(jobs, item_start, njobs, items, p, tune, sms, counter, s, pdl, count);
+    return lk_batch_launch<31, false>(jobs, item_start, njobs, items, p, tune, sms, counter, s, pdl, count);
 }
 
 template <int MAXH, bool EXACT>
@@ -892,7 +922,9 @@ __global__ void __launch_bounds__(256, 2) lk_points_kernel(const DevPyr *__restr
     Patch<MAXH, true> P;
     P.ts = s_tp + (size_t)(threadIdx.x >> 5) * (MAXH / 2) * 32;
     vtg_lk_out o;
-    lk_point<MAXH, EXACT, true>(*Ip, *Jp, top, p, xs[i], ys[i], gxs ? gxs[i] : 0.0f, gys ? gys[i] : 0.0f, lane, P, o);
+    unsigned work = 0;
+    lk_point<MAXH, EXACT, true>(*Ip, *Jp, top, p, xs[i], ys[i], gxs ? gxs[i] : 0.0f, gys ? gys[i] : 0.0f, lane, P, o,
+                                work);
     store_out(out + i, o, lane);
 }
 

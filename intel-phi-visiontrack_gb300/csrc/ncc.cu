@@ -563,7 +563,11 @@ static cudaError_t launch_all(const T *plane, int pitch, const float *app, const
         e = cudaFuncSetAttribute(ncc_map_f32<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess)
             return e;
+        if (s.map_ev0 && (e = cudaEventRecord(s.map_ev0, st)) != cudaSuccess)
+            return e;
         ncc_map_f32<T><<<cells, 256, smem, st>>>(plane, pitch, app, p, s.S1, s.S2, s.tp, s.map_v, s.map_x, s.map_y);
+        if (s.map_ev1 && (e = cudaEventRecord(s.map_ev1, st)) != cudaSuccess)
+            return e;
     } else {
         e = vtg_launch_ncc_map_tc(plane, pitch, sizeof(T), p, s, map_kind, st);
         if (e != cudaSuccess)

@@ -530,9 +530,13 @@ cudaError_t vtg_launch_ncc_map_tc(const void *plane, int pitch, int elem_bytes, 
         e = cudaFuncSetAttribute(ncc_map_tc<K, QQ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm.total);       \
         if (e != cudaSuccess)                                                                                          \
             return e;                                                                                                  \
+        if (s.map_ev0 && (e = cudaEventRecord(s.map_ev0, st)) != cudaSuccess)                                          \
+            return e;                                                                                                  \
         ncc_map_tc<K, QQ><<<tiles_x * tiles_y, 128, sm.total, st>>>((const uint8_t *)plane, pitch, p, s.band, krow,    \
                                                                    tiles_x, sm.a_bytes, sm.stage_bytes, s.conv,        \
                                                                    cpitch, s.fac, fw, s.cellw, s.err);                 \
+        if (s.map_ev1 && (e = cudaEventRecord(s.map_ev1, st)) != cudaSuccess)                                          \
+            return e;                                                                                                  \
     } while (0)
     if (kind == VTG_NCC_BF16) {
         if (q == 4)

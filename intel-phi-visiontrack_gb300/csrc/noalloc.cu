@@ -11,13 +11,16 @@
  * What that costs and what it limits:
  *   - VTG_NOALLOC_SCRATCH_BYTES (5 MiB) of device memory on every GPU that loads this library, held until the process
  *     exits, whether or not the entry point is ever called;
- *   - planes with (w + 1) (h + 1) <= VTG_NOALLOC_MAX_PIXELS (320,000: 640 x 480 fits), templates up to 64 x 64, steps up
- *     to 4 (the reference searches at 1 and 2), F32 map only; larger requests are refused with VTG_EINVAL, before
- *     anything runs;
+ *   - planes with (w + 1) (h + 1) <= VTG_NOALLOC_MAX_PIXELS (320,000: 640 x 480 fits), templates up to 64 x 64, steps 1,
+ *     2 or 4 (the reference searches at 1 and 2; a step must divide the map's 16-corner cells), F32 map only; other
+ *     requests are refused with VTG_EINVAL, before anything runs;
  *   - every call shares the one array, so calls whose work overlaps on the GPU (different streams, or different host
  *     threads) race and corrupt each other's results: order them on one stream, or serialize them;
  *   - the first call on a device looks the array's device address up (cudaGetSymbolAddress, once per device, with that
- *     device current); make that first call before any stream capture begins.
+ *     device current); make that first call before any stream capture begins;
+ *   - that address is kept for the life of the process. cudaDeviceReset destroys the context the array lives in, and
+ *     the array may sit elsewhere in the next one, so a process that resets a device must not call this entry point on
+ *     that device afterwards.
  * Nothing in the array needs to start at zero: every call writes all the scratch it reads (both integral images in
  * full, every cell of its map, the candidate list and its count) before reading it. */
 #include <mutex>
@@ -73,7 +76,8 @@ extern "C" int vtg_search_run_noalloc(const void *plane, int w, int h, int pitch
         return VTG_EINVAL;
     if (tw < 8 || th < 1 || (tw % 8) || tw > VTG_NOALLOC_MAX_T || th > VTG_NOALLOC_MAX_T || !(norm >= 0.0f))
         return VTG_EINVAL;
-    if ((long long)(w + 1) * (long long)(h + 1) > VTG_NOALLOC_MAX_PIXELS || step < 1 || step > VTG_NOALLOC_MAX_STEP ||
+    if (w > VTG_NOALLOC_MAX_PIXELS || h > VTG_NOALLOC_MAX_PIXELS ||
+        ((long long)w + 1) * ((long long)h + 1) > VTG_NOALLOC_MAX_PIXELS || step < 1 || step > VTG_NOALLOC_MAX_STEP ||
         (NCC_CELL % step))
         return VTG_EINVAL;
     NccPrm p;
@@ -132,6 +136,7 @@ extern "C" int vtg_search_run_noalloc(const void *plane, int w, int h, int pitch
     s.fac = nullptr;
     s.fac_elems = 0;
     s.cellw = nullptr;
+    s.map_ev0 = s.map_ev1 = nullptr;
     e = vtg_launch_ncc(plane, pitch, plane_type, app, p, s, VTG_NCC_F32, found, st);
     const size_t cells = (size_t)p.ccols * p.crows;
     if (e == cudaSuccess && map_v)

@@ -95,9 +95,12 @@ int vtg_pyr_tiles(int w, int h, int level);
  * programmatic dependent launched after it (the LK launch's work counter). */
 cudaError_t vtg_launch_pyramid_batch(const PyrJob *jobs, const int *starts, const int *tiles_total, int njobs,
                                      int max_levels, cudaStream_t s, int *reset = nullptr, bool pdl = false);
-/* Batched LK over jobs: items of `chunk` cells, job j's items from item_start[j]; `counter` must be 0 at launch. */
+/* Batched LK over jobs: items of `chunk` cells, job j's items from item_start[j]; `counter` must be 0 at launch.
+ * count (NULL, or four device words): adds the launch's template builds, residual passes, window passes and
+ * iterations, both walks of every cell, for the algorithmic operation count. */
 cudaError_t vtg_launch_lk_batch(const LkJob *jobs, const int *item_start, int njobs, int items, const LkPrm &p,
-                                const LkTune &tune, int sms, int *counter, cudaStream_t s, bool pdl = false);
+                                const LkTune &tune, int sms, int *counter, cudaStream_t s, bool pdl = false,
+                                unsigned long long *count = nullptr);
 
 /* A kernel launch, as a programmatic dependent of the stream's previous kernel when pdl (the kernel itself runs
  * griddepcontrol.wait before it reads what that kernel wrote). */

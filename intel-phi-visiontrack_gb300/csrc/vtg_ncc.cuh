@@ -52,6 +52,8 @@ struct NccScratch {
     float *fac;
     size_t fac_elems;
     unsigned long long *cellw;
+    /* vtg_search_profile: events recorded just before and just after the map kernel (NULL: none) */
+    cudaEvent_t map_ev0, map_ev1;
 };
 
 /* Elements of the tensor-core map's scratch for planes up to max_w x max_h and templates up to max_tw x max_th. */

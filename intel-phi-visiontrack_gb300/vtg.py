@@ -270,6 +270,7 @@ def _search_sigs(L):
     L.vtg_search_template.argtypes = [vp, vp, i, i, f, i, vp]
     L.vtg_search_run.argtypes = [vp, vp, i, i, i, i, i, i, i, i, i, i, C.POINTER(Found), vp, vp, vp, i, vp]
     L.vtg_correlate.argtypes = [vp, vp, i, i, i, i, i, vp, vp, vp, i, vp]
+    L.vtg_search_profile.argtypes = [vp, vp, i, i, i, i, i, i, i, i, i, i, i, C.POINTER(f), C.POINTER(f)]
     L.vtg_level_device.argtypes = [vp, i, i, C.POINTER(vp), C.POINTER(i), C.POINTER(i), C.POINTER(i)]
 
 
@@ -302,6 +303,14 @@ class Search:
             n = d["cells"]
             return d, mv[:n], mx[:n], my[:n]
         return d
+
+    def profile(self, plane_ptr: int, w: int, h: int, pitch: int, plane_type: int, x0: int, x1: int, y0: int, y1: int,
+                step: int = 1, precision: int = NCC_F32, reps: int = 10):
+        """(map kernel ms, whole search ms): medians of reps CUDA-event timed runs (vtg_search_profile)."""
+        a, b = C.c_float(), C.c_float()
+        check(lib().vtg_search_profile(self.h, plane_ptr, w, h, pitch, plane_type, x0, x1, y0, y1, step, precision,
+                                       reps, C.byref(a), C.byref(b)), "vtg_search_profile")
+        return a.value, b.value
 
     def correlate(self, plane_ptr: int, w: int, h: int, pitch: int, plane_type: int, xs, ys) -> np.ndarray:
         xs = np.ascontiguousarray(xs, np.int32)
@@ -360,6 +369,7 @@ def _batch_sigs(L):
     L.vtg_batch_autotune.argtypes = [vp, i, i, C.POINTER(Tune), C.POINTER(C.c_float), C.POINTER(C.c_float)]
     L.vtg_tracker_results.argtypes = [vp, vp, vp, i, vp]
     L.vtg_batch_profile.argtypes = [vp, i, i, C.POINTER(C.c_float), C.POINTER(C.c_float)]
+    L.vtg_batch_count.argtypes = [vp, i, C.POINTER(C.c_uint64)]
 
 
 class Batch:
@@ -428,6 +438,13 @@ class Batch:
         a, b = C.c_float(), C.c_float()
         check(lib().vtg_batch_profile(self.h, slot, reps, C.byref(a), C.byref(b)), "vtg_batch_profile")
         return a.value, b.value
+
+    def count(self, slot: int) -> dict:
+        """The work of one LK launch of the prepared step, both walks of every cell: template builds, residual passes,
+        window passes, iterations (vtg_batch_count)."""
+        c = (C.c_uint64 * 4)()
+        check(lib().vtg_batch_count(self.h, slot, c), "vtg_batch_count")
+        return {"builds": int(c[0]), "residuals": int(c[1]), "passes": int(c[2]), "iterations": int(c[3])}
 
     def close(self):
         if self.h:

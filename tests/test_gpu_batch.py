@@ -191,3 +191,27 @@ def test_batch_at_its_maximum_of_512_streams(vtg_lib, ctx):
     b.close()
     for t in trackers:
         t.close()
+
+
+def test_batch_count(vtg_lib, ctx, batch_setup):
+    """vtg_batch_count runs the step's LK launch once more with counters on: the work it reports bounds what the
+    records say (forward iterations are lk_out.iters; every good track runs its backward walk), and the cells are
+    the same bits after it."""
+    pairs, trackers, dev, singles, b = batch_setup
+    for t, (d0, _) in zip(trackers, dev):
+        t.build(0, d0.data_ptr(), where=vtg_lib.DEVICE)
+    ctx.sync()
+    b.prepare(0, trackers, [d1.data_ptr() for _, d1 in dev], [1] * len(trackers))
+    b.launch(0)
+    ctx.sync()
+    w = b.count(0)
+    _check(vtg_lib, trackers, singles)
+    lks = [vtg_lib.tracker_results(t)[1] for t in trackers]
+    cells = sum(len(l) for l in lks)
+    fwd_iters = sum(int(l["iters"].astype(np.int64).sum()) for l in lks)
+    good = sum(int(((l["status"] == 0) | (l["status"] == vtg_lib.LK_FLOWBACK)).sum()) for l in lks)
+    assert w["iterations"] > fwd_iters  # the backward walks' iterations come on top
+    assert w["iterations"] <= 2 * 10 * 4 * cells
+    assert good <= w["residuals"] <= 2 * cells
+    assert cells <= w["builds"] <= 2 * 4 * cells
+    assert w["passes"] <= w["iterations"]
