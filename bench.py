@@ -12,7 +12,8 @@ plain form beside it runs one stream, one vtg_build + vtg_cells per frame pair, 
 `e2e` is the served request loop (vtg_serve_run) through the C ABI: pinned host frames in, cell records out, Poisson
 arrivals from B 1080p streams at a saturating rate, continuous batching, 2 % of pairs followed by an appearance
 search; beside it the same loop in its plain form, and a mixed-size served run at nominal frame rates for latency.
-`--impl reference` times the CPU restatement of the reference's path (oracle/, FP64 form) on all host cores.
+`--impl reference` times the reference's own CPU kernels (its C sources, built on this host by oracle/Makefile) on all
+host cores.
 """
 from __future__ import annotations
 
@@ -248,6 +249,59 @@ def time_batched_mix(vtg, torch, ctx, device: str, nstreams: int = 64, steps: in
             "autotune": {"chosen": tuned, "chosen_ms": tuned_ms, "default": default_tune, "default_ms": default_ms}}
 
 
+def served_256(vtg, torch, ctx, pairs_1080) -> dict:
+    """The served configuration at its upper end: 256 streams on Poisson schedules, two 1920x1080 at 60 fps with their
+    cells on level 1 (4,080 cells), one 1280x720 at 15 fps, and 253 of 640x480 at 30 fps (2,400 cells), all with 2 %
+    of frames followed by an appearance search. At nominal rates and at saturation (every stream at 200 fps), the
+    served loop (continuous batching, two steps in flight) against the plain one (one frame pair at a time); at
+    saturation also with LIVE priority, where frames queued behind a newer one are skipped and counted."""
+    import vtg_synth as S
+
+    small = [S.warp_pair(640, 480, S.seeded_shift(300 + k, 0), 0.5, seed=300 + k)[:2] for k in range(8)]
+    p720 = S.warp_pair(1280, 720, S.seeded_shift(310, 0), 0.5, seed=310)[:2]
+    pin = lambda f: torch.from_numpy(np.ascontiguousarray(f)).pin_memory()
+    small_p = [(pin(a), pin(b)) for a, b in small]
+    big_p = [(pin(a), pin(b)) for a, b in pairs_1080[:2]]
+    p720_p = (pin(p720[0]), pin(p720[1]))
+    lkcfg = vtg.config(64, 64, levels=LEVELS, cell_w=CELL_W, cell_h=CELL_H)
+
+    def streams(rate, frames_at):
+        # the cameras connect over the first half second (stream k at k / 512 s), as a server sees them come
+        out, ptrs = [], []
+        for k in range(2):
+            out.append(dict(width=1920, height=1080, flow_level=1, fps=rate or 60.0, start_s=k / 512.0,
+                            frames=frames_at(rate or 60.0)))
+            ptrs += [big_p[k][0].data_ptr(), big_p[k][1].data_ptr()]
+        out.append(dict(width=1280, height=720, fps=rate or 15.0, start_s=2 / 512.0, frames=frames_at(rate or 15.0)))
+        ptrs += [p720_p[0].data_ptr(), p720_p[1].data_ptr()]
+        for k in range(253):
+            out.append(dict(width=640, height=480, fps=rate or 30.0, start_s=(3 + k) / 512.0,
+                            frames=frames_at(rate or 30.0)))
+            a, b = small_p[k % len(small_p)]
+            ptrs += [a.data_ptr(), b.data_ptr()]
+        return out, ptrs
+
+    keys = ("cells_per_s", "p50_ms", "p99_ms", "max_ms", "mean_batch", "served", "requests", "skipped", "dropped", "ncc")
+    res = {"streams": "2x1920x1080@60 (level 1, 4,080 cells), 1x1280x720@15, 253x640x480@30 (2,400 cells); "
+                      "2 % of frames searched; streams start over the first 0.5 s"}
+    nominal, ptrs = streams(None, lambda fps: max(2, int(round(2.0 * fps))))
+    for name, plain in (("served", False), ("plain", True)):
+        st = vtg.serve(ctx, nominal, ptrs, lkcfg, duration_s=2.5, max_batch=256, inflight=2, ncc_share=0.02,
+                       plain=plain, seed=21)
+        res.setdefault("nominal", {})[name] = {k: st[k] for k in keys}
+    sat, ptrs = streams(200.0, lambda fps: 200)
+    for name, plain, live in (("served", False, False), ("plain", True, False), ("served_live", False, True)):
+        st = vtg.serve(ctx, sat, ptrs, lkcfg, duration_s=1.0, max_batch=256, inflight=2, ncc_share=0.02,
+                       plain=plain, live=live, seed=22, allow_timeout=True)
+        res.setdefault("saturation", {})[name] = {k: st[k] for k in keys}
+        res["saturation"][name]["rc"] = st["rc"]
+    n, s_ = res["nominal"], res["saturation"]
+    res["nominal"]["served_vs_plain_cells_per_s"] = n["served"]["cells_per_s"] / max(n["plain"]["cells_per_s"], 1e-9)
+    res["saturation"]["served_vs_plain_cells_per_s"] = s_["served"]["cells_per_s"] / max(s_["plain"]["cells_per_s"],
+                                                                                         1e-9)
+    return res
+
+
 def run_ours(args) -> dict | None:
     import torch
 
@@ -334,6 +388,7 @@ def run_ours(args) -> dict | None:
         t.close()
     mix64 = time_batched_mix(vtg, torch, ctx, device)
     ncc = ncc_config3(vtg, torch, ctx)
+    s256 = served_256(vtg, torch, ctx, pairs)
 
     # ---- end to end: the served loop through the C ABI, pinned host frames in, cell records out
     pinned = []
@@ -397,6 +452,7 @@ def run_ours(args) -> dict | None:
                            "plain": {k: mixed_plain[k] for k in ("cells_per_s", "p50_ms", "p99_ms", "served")},
                            "streams": "2x1080p@60 (4,080 cells), 1x720p@15, 13 more 640x480..1080p@30"},
             # a batched step: one pyramid launch for each level above 0, then one LK launch
+            "served_256": s256,
             "roofline": roofline, "roofline_pyramid": roof_pyr, "ncc": ncc,
             "gpu_launches": args.steps * ((LEVELS - 1) + 1),
             "clocks": clk.summary()}
@@ -404,15 +460,83 @@ def run_ours(args) -> dict | None:
     return line
 
 
-def cpu_baseline(frames, seconds: float = 10.0) -> dict:
-    """The oracle's FP64 restatement of the reference's path on all host cores: the new frame's pyramid and LK with
-    the forward-backward check at every 4th cell of the 16,200, repeated for `seconds`."""
-    sys.path.insert(0, ORACLE)
+def cpu_model() -> str:
+    """The host CPU as /proc/cpuinfo names it (model name on x86; implementer / part on Arm), with its core count."""
     import platform
 
+    model = ""
+    try:
+        with open("/proc/cpuinfo") as f:
+            info = f.read()
+        for line in info.splitlines():
+            if line.lower().startswith("model name"):
+                model = line.split(":", 1)[1].strip()
+                break
+        if not model:
+            impl = [l.split(":", 1)[1].strip() for l in info.splitlines() if l.startswith("CPU implementer")]
+            part = [l.split(":", 1)[1].strip() for l in info.splitlines() if l.startswith("CPU part")]
+            if impl and part:
+                model = "Arm implementer %s part %s" % (impl[0], part[0])
+    except OSError:
+        pass
+    return "%s, %s, %d cores" % (model or "unknown", platform.machine(), os.cpu_count() or 1)
+
+
+REF_BENCH = os.path.join(ORACLE, "_ref", "vtref_bench")
+
+
+def reference_bench(frames, steps: int, warmup: int, threads: int, lk: str = "ref", pyr: str = "ref",
+                    every: int = 1, interleave: int = 0) -> dict | None:
+    """Runs oracle/_ref/vtref_bench, the reference's own pyramid and LK kernels (its C sources, built on this host by
+    oracle/Makefile) on the workload's frame pair and its 16,200 cell centres; None where it is not built."""
+    import tempfile
+
+    sys.path.insert(0, ORACLE)
     import oracle as O
 
+    if not os.path.exists(REF_BENCH):
+        subprocess.run(["make", "-s", "-C", ORACLE, "refbin"], capture_output=True)
+    if not os.path.exists(REF_BENCH):
+        return None
+    f0, f1 = frames
+    xs, ys = O.cell_centres(W, H, CELL_W, CELL_H)
+    with tempfile.NamedTemporaryFile(suffix=".bin", delete=False) as f:
+        f.write(np.array([W, H, LEVELS, len(xs)], np.int32).tobytes())
+        f.write(np.ascontiguousarray(f0, np.uint8).tobytes())
+        f.write(np.ascontiguousarray(f1, np.uint8).tobytes())
+        f.write(np.asarray(xs, np.float32).tobytes())
+        f.write(np.asarray(ys, np.float32).tobytes())
+        path = f.name
+    try:
+        cmd = [REF_BENCH, path, "--lk", lk, "--pyr", pyr, "--threads", str(threads), "--steps", str(steps),
+               "--warmup", str(warmup), "--every", str(every)]
+        if interleave:
+            cmd += ["--interleave", str(interleave)]
+        r = subprocess.run(cmd, capture_output=True, text=True, timeout=900)
+        if r.returncode != 0:
+            return None
+        return json.loads(r.stdout.strip().splitlines()[-1])
+    finally:
+        os.unlink(path)
+
+
+def cpu_baseline(frames, seconds: float = 10.0) -> dict:
+    """The reference's own CPU code on all host cores: its plain-C pyramid (img_u8_to_q6_ref, img_reduce_ref) and LK
+    with the forward-backward check (lk_track_ref, lk_flowback_ref) over the workload's 16,200 cells, frame pairs
+    repeated for about `seconds`. Where that build is missing, the oracle's FP64 restatement instead (kind "port")."""
     threads = os.cpu_count() or 1
+    probe = reference_bench(frames, 1, 1, threads)
+    if probe is not None:
+        steps = max(2, int(seconds / max(probe["median_s"], 1e-3)))
+        r = reference_bench(frames, steps, 1, threads)
+        if r is not None:
+            return {"value": r["cells_per_s"], "unit": "cells/s", "cores": threads, "kind": "reference",
+                    "sample": "%d whole frame pairs (pyramid + 16,200 cells with flowback) in %.1f s: the reference's "
+                              "img_*_ref + lk_track_ref / lk_flowback_ref built from its sources, on %s"
+                              % (steps, r["total_s"], cpu_model())}
+    sys.path.insert(0, ORACLE)
+    import oracle as O
+
     f0, f1 = frames
     xs, ys = O.cell_centres(W, H, CELL_W, CELL_H)
     xs, ys = xs[::4], ys[::4]
@@ -425,21 +549,52 @@ def cpu_baseline(frames, seconds: float = 10.0) -> dict:
         done += len(xs)
     dt = time.perf_counter() - t0
     return {"value": done / dt, "unit": "cells/s", "cores": threads, "kind": "port",
-            "sample": "the new frame's pyramid + every 4th of the 16,200 cells (4,050) per repetition, FP64 oracle form, "
-                      "%d repetitions in %.1f s on %s" % (done // len(xs), dt, platform.machine())}
+            "sample": "the reference's own build is missing here: the new frame's pyramid + every 4th of the 16,200 "
+                      "cells per repetition, FP64 oracle form, %d repetitions in %.1f s on %s"
+                      % (done // len(xs), dt, cpu_model())}
 
 
 def run_reference(args) -> dict | None:
+    """The reference arm: the reference's own CPU implementation of the path (its C kernels, built from its sources on
+    this host) on all host cores, K timed steps after W warm-up steps, a step being one frame pair of this bench's
+    workload (the new frame's pyramid and LK with flowback at all 16,200 cells). Beside it, the reference's vector
+    kernels (their 16-lane host model) against the plain C ones, median of 7 interleaved rounds on every 8th cell."""
     if int(os.environ.get("RANK", "0")) != 0:
         return None
-    sys.path.insert(0, ORACLE)
-    import platform
-
-    import oracle as O
     import vtg_synth as S
 
     threads = os.cpu_count() or 1
-    f0, f1, _, _ = S.warp_pair(W, H, S.seeded_shift(2, 0), 0.5, seed=2)
+    frames = S.warp_pair(W, H, S.seeded_shift(2, 0), 0.5, seed=2)[:2]
+    r = reference_bench(frames, args.steps, args.warmup, threads)
+    if r is None:
+        return run_reference_port(args, frames)
+    inter = reference_bench(frames, 1, 0, threads, every=8, interleave=7)
+    value = r["cells_per_s"]
+    cb = {"value": value, "unit": "cells/s", "cores": threads, "kind": "reference",
+          "sample": "per step one whole frame pair: the reference's img_u8_to_q6_ref + img_reduce_ref pyramid and "
+                    "lk_track_ref + lk_flowback_ref at all 16,200 cells, its C sources built on this host, "
+                    "threads over an atomic cell counter, on %s" % cpu_model()}
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * r["total_s"] / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 patch sums, long double driver",
+            "data": "synthetic (seeded noise, blur 1.5, warp)", "config": workload("batched, graph-replayed",
+                                                                                args.streams),
+            "cpu_baseline": cb, "median_ms_per_step": 1e3 * r["median_s"],
+            "e2e": {"value": value, "unit": "cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if inter is not None:
+        line["vector_kernels"] = {"what": "the reference's _vx kernels (its 16-lane host model) against its plain C "
+                                          "ones, median of 7 interleaved rounds on every 8th cell",
+                                  "ref_cells_per_s": inter["ref_cells_per_s"], "vx_cells_per_s": inter["vx_cells_per_s"]}
+    return line
+
+
+def run_reference_port(args, frames) -> dict:
+    """The reference arm where the reference's own build is missing: the oracle's FP64 restatement of its path."""
+    sys.path.insert(0, ORACLE)
+    import oracle as O
+
+    threads = os.cpu_count() or 1
+    f0, f1 = frames
     xs, ys = O.cell_centres(W, H, CELL_W, CELL_H)
     xs, ys = xs[::8], ys[::8]
     cfg = O.lk_cfg()
@@ -459,14 +614,13 @@ def run_reference(args) -> dict | None:
     total = sum(times)
     value = len(xs) * args.steps / total
     cb = {"value": value, "unit": "cells/s", "cores": threads, "kind": "port",
-          "sample": "per step: one stream's new frame's pyramid and every 8th cell (2,025 of 16,200), FP64 oracle "
-                    "form, all host threads, %s" % platform.machine()}
-    # the same config as this bench's own line (the workload's cells/s); where it ran is in cpu_baseline
+          "sample": "the reference's own build is missing here: per step one stream's new frame's pyramid and every "
+                    "8th cell (2,025 of 16,200), FP64 oracle form, all host threads, %s" % cpu_model()}
     return {"impl": "reference", "metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded noise, blur 1.5, warp)", "config": workload("batched, graph-replayed",
-                                                                                 args.streams),
+                                                                                args.streams),
             "cpu_baseline": cb,
             "e2e": {"value": value, "unit": "cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 

@@ -479,24 +479,29 @@ class ServeCfg(C.Structure):
     _fields_ = [("nstreams", C.c_int), ("streams", C.POINTER(ServeStream)), ("frames", C.POINTER(C.c_void_p)),
                 ("lk", Config), ("duration_s", C.c_double), ("max_batch", C.c_int), ("inflight", C.c_int),
                 ("hbm_budget", C.c_size_t), ("ncc_share", C.c_float), ("plain", C.c_int), ("seed", C.c_uint64),
-                ("last_cells", C.POINTER(C.c_void_p))]
+                ("last_cells", C.POINTER(C.c_void_p)), ("live", C.c_int), ("max_queue", C.c_int),
+                ("stall_at_s", C.c_double), ("stall_timeout_s", C.c_double)]
 
 
 class ServeStats(C.Structure):
     _fields_ = [("streams_admitted", C.c_int), ("streams_waited", C.c_int), ("streams_rejected", C.c_int),
                 ("requests", C.c_long), ("served", C.c_long), ("cells", C.c_long), ("ncc", C.c_long),
                 ("wall_s", C.c_double), ("cells_per_s", C.c_double), ("p50_ms", C.c_double), ("p99_ms", C.c_double),
-                ("max_ms", C.c_double), ("mean_batch", C.c_double)]
+                ("max_ms", C.c_double), ("mean_batch", C.c_double), ("skipped", C.c_long), ("dropped", C.c_long),
+                ("submitted", C.c_long)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 def serve(ctx: Context, streams, frames, lk: Config, duration_s: float, max_batch: int = 64, inflight: int = 2,
-          hbm_budget: int = 0, ncc_share: float = 0.0, plain: bool = False, seed: int = 1, last_cells=None) -> dict:
+          hbm_budget: int = 0, ncc_share: float = 0.0, plain: bool = False, seed: int = 1, last_cells=None,
+          live: bool = False, max_queue: int = 0, stall_at_s: float = 0.0, stall_timeout_s: float = 0.0,
+          allow_timeout: bool = False) -> dict:
     """Runs vtg_serve_run. streams: dicts (width, height, flow_level, fps, start_s, frames); frames: two host
     addresses per stream (pinned uint8 buffers, width bytes a row); last_cells: optional list of CELL_DTYPE arrays
-    (cols x rows each, or None) that end with each stream's last frame pair's cells."""
+    (cols x rows each, or None) that end with each stream's last frame pair's cells. With allow_timeout, a
+    VTG_ETIMEOUT run returns its stats with "rc" set instead of raising."""
     L = lib()
     L.vtg_serve_run.argtypes = [C.c_void_p, C.POINTER(ServeCfg), C.POINTER(ServeStats)]
     ss = (ServeStream * len(streams))(*[ServeStream(s["width"], s["height"], s.get("flow_level", 0), s["fps"],
@@ -506,10 +511,119 @@ def serve(ctx: Context, streams, frames, lk: Config, duration_s: float, max_batc
     if last_cells is not None:
         lc = (C.c_void_p * len(streams))(*[None if a is None else a.ctypes.data for a in last_cells])
     cfg = ServeCfg(len(streams), ss, fp, lk, duration_s, max_batch, inflight, hbm_budget, ncc_share, int(plain), seed,
-                   lc)
+                   lc, int(live), max_queue, stall_at_s, stall_timeout_s)
     st = ServeStats()
-    check(L.vtg_serve_run(ctx.h, C.byref(cfg), C.byref(st)), "vtg_serve_run")
-    return st.as_dict()
+    rc = L.vtg_serve_run(ctx.h, C.byref(cfg), C.byref(st))
+    if not (allow_timeout and rc == ETIMEOUT):
+        check(rc, "vtg_serve_run")
+    d = st.as_dict()
+    d["rc"] = rc
+    return d
+
+
+# ---------------------------------------------------------------- the request API (vtg_server_*)
+
+PRIO_ORDERED, PRIO_LIVE = 0, 1
+REQ_SEARCH = 1
+RES_DONE, RES_SKIPPED, RES_RETIRED = 0, 1, 2
+
+
+class ServerCfg(C.Structure):
+    _fields_ = [("lk", Config), ("max_batch", C.c_int), ("inflight", C.c_int), ("plain", C.c_int),
+                ("max_queue", C.c_int), ("idle_timeout_s", C.c_double)]
+
+
+class ServerResult(C.Structure):
+    _fields_ = [("stream", C.c_int), ("status", C.c_int), ("ticket", C.c_int64), ("tag", C.c_uint64),
+                ("frames_skipped", C.c_uint32), ("searched", C.c_int), ("latency_ms", C.c_double), ("found", Found)]
+
+    def as_dict(self) -> dict:
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k != "found"}
+        d["found"] = self.found.as_dict()
+        return d
+
+
+def _server_sigs(L):
+    vp, i, i64 = C.c_void_p, C.c_int, C.c_int64
+    L.vtg_server_create.argtypes = [vp, C.POINTER(ServerCfg), C.POINTER(vp)]
+    L.vtg_server_destroy.argtypes = [vp]
+    L.vtg_server_destroy.restype = None
+    L.vtg_server_template.argtypes = [vp, vp, i, i, C.c_float]
+    L.vtg_server_open.argtypes = [vp, C.c_uint32, C.c_uint32, C.c_uint32, i, vp, i]
+    L.vtg_server_close.argtypes = [vp, i]
+    L.vtg_server_submit.argtypes = [vp, i, vp, i, vp, C.c_uint64, i]
+    L.vtg_server_submit.restype = i64
+    L.vtg_server_poll.argtypes = [vp, C.POINTER(ServerResult), i, i]
+    L.vtg_server_pending.argtypes = [vp]
+    L.vtg_server_counts.argtypes = [vp, C.POINTER(C.c_long), C.POINTER(C.c_long)]
+
+
+class Server:
+    """The request API (vtg_server): open streams, submit frames as they arrive, poll for their cells."""
+
+    def __init__(self, ctx: Context, lk: Config, max_batch: int = 64, inflight: int = 2, plain: bool = False,
+                 max_queue: int = 16, idle_timeout_s: float = 0.0):
+        _server_sigs(lib())
+        self.ctx = ctx
+        self.h = C.c_void_p()
+        cfg = ServerCfg(lk, max_batch, inflight, int(plain), max_queue, idle_timeout_s)
+        check(lib().vtg_server_create(ctx.h, C.byref(cfg), C.byref(self.h)), "vtg_server_create")
+        ctx._trackers.add(self)
+        self._keep = {}
+        self._widths = {}
+
+    def template(self, app, norm: float):
+        app = np.ascontiguousarray(app, np.float32)
+        check(lib().vtg_server_template(self.h, _p(app), app.shape[1], app.shape[0], C.c_float(norm)),
+              "vtg_server_template")
+
+    def open(self, width: int, height: int, first, flow_level: int = 0, priority: int = PRIO_ORDERED,
+             stride: int = 0) -> int:
+        """A stream id (>= 0) or a negative status (not raised: EINVAL and EBUDGET are answers here)."""
+        sid = lib().vtg_server_open(self.h, width, height, flow_level, priority, first, stride or width)
+        if sid >= 0:
+            self._widths[sid] = width
+        return sid
+
+    def close_stream(self, stream: int) -> int:
+        return lib().vtg_server_close(self.h, stream)
+
+    def submit(self, stream: int, frame, cells=None, tag: int = 0, flags: int = 0, stride: int = 0) -> int:
+        """frame: a host address (pinned); cells: a CELL_DTYPE array (kept alive until polled) or None."""
+        t = lib().vtg_server_submit(self.h, stream, frame, stride or self._width(stream), _p(cells), tag, flags)
+        if t >= 0 and cells is not None:
+            self._keep[t] = cells
+        return t
+
+    def _width(self, stream: int) -> int:
+        return self._widths.get(stream, 0)
+
+    def poll(self, max_results: int = 256, timeout_us: int = 0):
+        out = (ServerResult * max_results)()
+        n = check(lib().vtg_server_poll(self.h, out, max_results, timeout_us), "vtg_server_poll")
+        res = [out[i].as_dict() for i in range(n)]
+        for r in res:
+            self._keep.pop(r["ticket"], None)
+        return res
+
+    def pending(self) -> int:
+        return check(lib().vtg_server_pending(self.h), "vtg_server_pending")
+
+    def counts(self):
+        a, b = C.c_long(), C.c_long()
+        check(lib().vtg_server_counts(self.h, C.byref(a), C.byref(b)), "vtg_server_counts")
+        return a.value, b.value
+
+    def close(self):
+        if self.h:
+            lib().vtg_server_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 # ---------------------------------------------------------------- the reference's kernel signatures (vtg_compat.h)

@@ -115,6 +115,7 @@ def test_config3_near_blank_windows_score_zero(vtg_lib, ctx, size):
     checked = 0
     for k in range(3):
         app, norm = _app(tpl[k])
+        s.template(app, norm)
         maps = {}
         for prec in (vtg_lib.NCC_F32, vtg_lib.NCC_BF16, vtg_lib.NCC_FP16):
             f, v, mx, my = s.run(dp.data_ptr(), W, H, W, vtg_lib.PLANE_U8, 1, W, 1, H, 1, prec, want_map=True)
