@@ -362,6 +362,7 @@ __global__ void __launch_bounds__(128, 1) ncc_map_tc(const uint8_t *__restrict__
     uint8_t *ctl = smem + TC_STAGES * stage_bytes;
     const uint32_t full0 = smem_u32(ctl), empty0 = full0 + 8 * TC_STAGES;
     uint32_t *tmem_slot = (uint32_t *)(ctl + 16 * TC_STAGES);
+    int *issued = (int *)(ctl + 16 * TC_STAGES + 8); /* [0]: stages filled, [1]: stages whose MMAs were committed */
     const uint32_t a_copy = (uint32_t)((TC_XS + krow) * 2), b_copy = (uint32_t)((8 * Q) * krow * 2);
 
     if (tid == 0) {
@@ -391,7 +392,8 @@ __global__ void __launch_bounds__(128, 1) ncc_map_tc(const uint8_t *__restrict__
     if (warp == 0 && lane == 0) {
         /* the producer: stage k % TC_STAGES is filled with image row Y0 + k and band block k once the MMAs of its
          * previous use have completed (the commit to its empty barrier) */
-        for (int k = 0; k < nk; k++) {
+        int k = 0;
+        for (; k < nk; k++) {
             const int s = k % TC_STAGES;
             if (k >= TC_STAGES && !mbar_wait(empty0 + 8 * s, (uint32_t)((k / TC_STAGES - 1) & 1))) {
                 good = 0;
@@ -401,10 +403,12 @@ __global__ void __launch_bounds__(128, 1) ncc_map_tc(const uint8_t *__restrict__
             tc_fill(full0 + 8 * s, smem_u32(sa), arow + (size_t)k * cpitch, a_copy, smem_u32(sa + a_bytes),
                     band + (size_t)k * (8 * Q) * krow, b_copy);
         }
+        issued[0] = k;
     } else if (warp == 1 && lane == 0) {
         /* the MMA issuer: each stage's MMAs as soon as its copies have landed, back to back; a commit frees the stage
          * for the producer */
-        for (int k = 0; k < nk; k++) {
+        int k = 0;
+        for (; k < nk; k++) {
             const int s = k % TC_STAGES;
             if (!mbar_wait(full0 + 8 * s, (uint32_t)((k / TC_STAGES) & 1))) {
                 good = 0;
@@ -419,6 +423,7 @@ __global__ void __launch_bounds__(128, 1) ncc_map_tc(const uint8_t *__restrict__
             }
             tc_commit(empty0 + 8 * s);
         }
+        issued[1] = k;
         /* the last commit covers every MMA */
         if (good) {
             const int last = nk - 1;
@@ -428,8 +433,19 @@ __global__ void __launch_bounds__(128, 1) ncc_map_tc(const uint8_t *__restrict__
     const int ok_all = __syncthreads_and(good);
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if (!ok_all) {
-        if (tid == 0)
+        /* A wait gave up. Before the CTA frees its tensor memory and exits, what it started must be done: the MMAs of
+         * every committed stage (the last commit tracks them all) and the bulk copies of every stage filled but not
+         * consumed (each completes its full barrier's phase), else they would still write into tensor and shared
+         * memory that the next CTA on this SM may own. These waits are bounded too; past them the engines themselves
+         * have stopped and the context cannot be saved from here. */
+        if (tid == 0) {
             atomicExch(err, 1);
+            const int kp = issued[0], ki = issued[1];
+            if (ki > 0)
+                mbar_wait(empty0 + 8 * ((ki - 1) % TC_STAGES), (uint32_t)(((ki - 1) / TC_STAGES) & 1));
+            for (int k = ki; k < kp; k++)
+                mbar_wait(full0 + 8 * (k % TC_STAGES), (uint32_t)((k / TC_STAGES) & 1));
+        }
     } else {
         /* epilogue: thread m owns accumulator row m: corners X0 + 8 m + s, Y0 + q */
         const int m = warp * 32 + lane;

@@ -11,7 +11,6 @@ in baseline/_ref that build() makes).
     and tk_track's feature LK with flowback on the GPU, everything else the reference's own C) held to the scene's own
     gate, tests/scenes.md:13 of the reference (continuity >= 0.99, EPE median <= 0.02 px, centre median <= 0.05 px),
     and its EPE within 0.005 px of the CPU replay's."""
-import json
 import os
 import re
 import struct
@@ -68,11 +67,23 @@ def test_m2_ref_on_the_gpu(programs):
             assert abs(g[k][0] - c[k][0]) <= 0.01 and abs(g[k][1] - c[k][1]) <= 0.01, (k, g[k], c[k])
 
 
+def _score(path):
+    """The figures the test reads from the replay's score file (src/host/score.c writes it as JSON-like fragments,
+    not one JSON document, so they are read by name)."""
+    text = open(path).read()
+    num = r"(-?[0-9.]+)"
+    epe = re.search(r'"epe_px":\{"n":(\d+),"median":' + num, text)
+    return {"continuity": float(re.search(r'"continuity":' + num, text).group(1)),
+            "epe_n": int(epe.group(1)), "epe_median": float(epe.group(2)),
+            "id_changes": int(re.search(r'"id_changes":(\d+)', text).group(1)),
+            "hidden_said_observed": int(re.search(r'"hidden_said_observed":(\d+)', text).group(1))}
+
+
 def _replay(prog, tmp, name):
     out = os.path.join(tmp, name + ".json")
     r = subprocess.run([prog, "translate", "640x480", "--mono", "--gate", "--frames", "60", "--json", out], cwd=tmp,
                        capture_output=True, text=True, timeout=900)
-    return r, json.load(open(out)) if os.path.exists(out) else None
+    return r, _score(out) if os.path.exists(out) else None
 
 
 def test_vt_replay_tracker_on_the_gpu_passes_the_scene_gate(programs, tmp_path):
@@ -82,7 +93,7 @@ def test_vt_replay_tracker_on_the_gpu_passes_the_scene_gate(programs, tmp_path):
     assert "GATE MISS" not in gpu.stderr
     cpu, cs = _replay(os.path.join(programs, "vt_replay"), tmp, "cpu")
     assert cpu.returncode == 0, cpu.stderr[-2000:]
-    assert gs["continuity"] >= 0.99 and gs["epe_px"]["median"] <= 0.02
-    assert gs["epe_px"]["n"] > 0.9 * cs["epe_px"]["n"]
-    assert abs(gs["epe_px"]["median"] - cs["epe_px"]["median"]) <= 0.005
-    assert gs["states"]["id_changes"] == 0 and gs["hidden_said_observed"] == 0
+    assert gs["continuity"] >= 0.99 and gs["epe_median"] <= 0.02
+    assert gs["epe_n"] > 0.9 * cs["epe_n"]
+    assert abs(gs["epe_median"] - cs["epe_median"]) <= 0.005
+    assert gs["id_changes"] == 0 and gs["hidden_said_observed"] == 0
