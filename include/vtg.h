@@ -179,9 +179,11 @@ int vtg_tracker_results(vtg_tracker *t, struct vtg_cell *cells, struct vtg_lk_ou
 /* How the batched LK launch runs (its autotuner's choices): warps per CTA (4, 8 or 16), cells per work item, a
  * persistent grid of ctas_per_sm CTAs per SM pulling items from a device counter (persistent = 1) or one warp per item
  * (persistent = 0); tsmem = 1 keeps the template's intensities in shared memory instead of registers, for more warps
- * an SM (persistent only; 4 warps with ctas_per_sm <= 5, 8 with <= 3, 16 with 1). */
+ * an SM (persistent only; 4 warps with ctas_per_sm <= 5, 8 with <= 3, 16 with 1); tiled = 1 walks each stream's cells
+ * in tiles of 8 x 4 and gives a CTA whole tiles, so the cells an SM runs at once are neighbours that share their
+ * windows in its L1 (persistent only; chunk must divide 32). */
 struct vtg_tune {
-    int block_warps, chunk, persistent, ctas_per_sm, tsmem;
+    int block_warps, chunk, persistent, ctas_per_sm, tsmem, tiled;
 };
 
 typedef struct vtg_batch vtg_batch;

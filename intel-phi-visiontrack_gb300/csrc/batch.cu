@@ -35,6 +35,7 @@ struct BatchSlot {
     unsigned long long *d_count; /* vtg_batch_count's four totals, in the counter's 256-byte block */
     int njobs, max_levels, items, cells;
     int chunk; /* cells per work item the item table was laid out for */
+    int tiled; /* and its order: row-major or 8 x 4 tiles */
     int tiles[VTG_MAX_LEVELS];
     LkPrm prm;
     bool ready;
@@ -76,7 +77,7 @@ static size_t slot_bytes(int max_jobs)
            up256(sizeof(LkJob) * (size_t)max_jobs) + up256(sizeof(int) * (size_t)(max_jobs + 1)) + 256;
 }
 
-static const LkTune k_default_tune = {16, 2, 1, 1, 1};
+static const LkTune k_default_tune = {16, 2, 1, 1, 1, 1};
 
 #define CU(call)                                                                                                       \
     do {                                                                                                               \
@@ -273,15 +274,16 @@ extern "C" int vtg_batch_prepare(vtg_batch *b, int slot, int n, vtg_tracker *con
         sl.tiles[L - 1] = acc;
     }
     int acc = 0, cells = 0;
-    const int chunk = std::max(1, b->tune.chunk);
+    const int chunk = std::max(1, b->tune.chunk), tiled = b->tune.tiled;
     for (int j = 0; j < n; j++) {
         items[(size_t)j] = acc;
-        acc += (lj[(size_t)j].g.n + chunk - 1) / chunk;
+        acc += vtg_lk_items(lj[(size_t)j].g.cols, lj[(size_t)j].g.rows, chunk, tiled);
         cells += lj[(size_t)j].g.n;
     }
     items[(size_t)n] = acc;
     sl.items = acc;
     sl.chunk = chunk;
+    sl.tiled = tiled;
     sl.cells = cells;
     sl.njobs = n;
     sl.max_levels = max_levels;
@@ -317,6 +319,7 @@ static int launch_slot(vtg_batch *b, BatchSlot &sl, cudaStream_t s, int nwait = 
         CU(cudaStreamWaitEvent(s, (cudaEvent_t)wait_lk[k], 0));
     LkTune t = b->tune;
     t.chunk = sl.chunk;
+    t.tiled = sl.tiled;
     CU(vtg_launch_lk_batch(sl.d_lk, sl.d_items, sl.njobs, sl.items, sl.prm, t, b->sms, sl.d_counter, s,
                            nwait_lk == 0));
     return VTG_OK;
@@ -388,6 +391,8 @@ extern "C" int vtg_batch_set_tune(vtg_batch *b, const struct vtg_tune *t)
     if (!b || !t || (t->block_warps != 4 && t->block_warps != 8 && t->block_warps != 16) || t->chunk < 1 ||
         t->chunk > 64 || t->ctas_per_sm < 1 || t->ctas_per_sm > 8)
         return VTG_EINVAL;
+    if (t->tiled && (!t->persistent || 32 % t->chunk))
+        return VTG_EINVAL;
     if (t->tsmem && (!t->persistent || t->ctas_per_sm > (t->block_warps == 4 ? 5 : t->block_warps == 8 ? 3 : 1)))
         return VTG_EINVAL;
     std::lock_guard<std::mutex> g(b->mu);
@@ -396,6 +401,7 @@ extern "C" int vtg_batch_set_tune(vtg_batch *b, const struct vtg_tune *t)
     b->tune.persistent = t->persistent ? 1 : 0;
     b->tune.ctas_per_sm = t->ctas_per_sm;
     b->tune.tsmem = t->tsmem ? 1 : 0;
+    b->tune.tiled = t->tiled ? 1 : 0;
     return VTG_OK;
 }
 
@@ -408,11 +414,12 @@ extern "C" int vtg_batch_get_tune(const vtg_batch *b, struct vtg_tune *t)
     t->persistent = b->tune.persistent;
     t->ctas_per_sm = b->tune.ctas_per_sm;
     t->tsmem = b->tune.tsmem;
+    t->tiled = b->tune.tiled;
     return VTG_OK;
 }
 
-/* Re-lays the prepared slot's item table for a new chunk (items depend on it). */
-static int relay_items(vtg_batch *b, BatchSlot &sl, int chunk)
+/* Re-lays the prepared slot's item table for a new chunk and order (items depend on them). */
+static int relay_items(vtg_batch *b, BatchSlot &sl, int chunk, int tiled)
 {
     std::vector<LkJob> lj((size_t)sl.njobs);
     CU(cudaMemcpyAsync(lj.data(), sl.d_lk, sizeof(LkJob) * (size_t)sl.njobs, cudaMemcpyDeviceToHost, b->stream));
@@ -421,11 +428,12 @@ static int relay_items(vtg_batch *b, BatchSlot &sl, int chunk)
     int acc = 0;
     for (int j = 0; j < sl.njobs; j++) {
         items[(size_t)j] = acc;
-        acc += (lj[(size_t)j].g.n + chunk - 1) / chunk;
+        acc += vtg_lk_items(lj[(size_t)j].g.cols, lj[(size_t)j].g.rows, chunk, tiled);
     }
     items[(size_t)sl.njobs] = acc;
     sl.items = acc;
     sl.chunk = chunk;
+    sl.tiled = tiled;
     CU(cudaMemcpyAsync(sl.d_items, items.data(), sizeof(int) * items.size(), cudaMemcpyHostToDevice, b->stream));
     CU(cudaStreamSynchronize(b->stream));
     drop_graph(sl);
@@ -446,30 +454,33 @@ extern "C" int vtg_batch_autotune(vtg_batch *b, int slot, int reps, struct vtg_t
                 if (pers) {
                     const int max_ctas = 16 / warps; /* 128 registers a thread: 16 warps an SM */
                     for (int c = 1; c <= max_ctas; c *= 2)
-                        cands.push_back({warps, chunk, 1, c, 0});
+                        for (int tl = 0; tl <= 1; tl++)
+                            cands.push_back({warps, chunk, 1, c, 0, tl});
                 } else if (chunk <= 2) {
-                    cands.push_back({warps, chunk, 0, 1, 0});
+                    cands.push_back({warps, chunk, 0, 1, 0, 0});
                 }
             }
     /* the template's intensities in shared memory: 20 or 24 warps an SM */
-    for (int chunk : {1, 2, 4}) {
-        cands.push_back({4, chunk, 1, 5, 1});
-        cands.push_back({8, chunk, 1, 3, 1});
-        cands.push_back({16, chunk, 1, 1, 1});
-    }
+    for (int chunk : {1, 2, 4})
+        for (int tl = 0; tl <= 1; tl++) {
+            cands.push_back({4, chunk, 1, 5, 1, tl});
+            cands.push_back({8, chunk, 1, 3, 1, tl});
+            cands.push_back({16, chunk, 1, 1, 1, tl});
+        }
     cudaEvent_t e0, e1;
     CU(cudaEventCreate(&e0));
     CU(cudaEventCreate(&e1));
     float best_t = 1e30f, def_t = 0.0f;
     LkTune best_c = k_default_tune;
-    int cur_chunk = -1;
+    int cur_chunk = -1, cur_tiled = -1;
     for (size_t ci = 0; ci < cands.size(); ci++) {
         const LkTune &c = cands[ci];
-        if (c.chunk != cur_chunk) {
-            const int rc = relay_items(b, sl, c.chunk);
+        if (c.chunk != cur_chunk || c.tiled != cur_tiled) {
+            const int rc = relay_items(b, sl, c.chunk, c.tiled);
             if (rc != VTG_OK)
                 return rc;
             cur_chunk = c.chunk;
+            cur_tiled = c.tiled;
         }
         b->tune = c;
         std::vector<float> t;
@@ -501,7 +512,7 @@ extern "C" int vtg_batch_autotune(vtg_batch *b, int slot, int reps, struct vtg_t
         b->tune = best_c;
         b->tuned[sl.key] = best_c;
     }
-    const int rc = relay_items(b, sl, best_c.chunk);
+    const int rc = relay_items(b, sl, best_c.chunk, best_c.tiled);
     if (rc != VTG_OK)
         return rc;
     if (best) {
@@ -510,6 +521,7 @@ extern "C" int vtg_batch_autotune(vtg_batch *b, int slot, int reps, struct vtg_t
         best->persistent = best_c.persistent;
         best->ctas_per_sm = best_c.ctas_per_sm;
         best->tsmem = best_c.tsmem;
+        best->tiled = best_c.tiled;
     }
     if (best_ms)
         *best_ms = best_t;
@@ -544,6 +556,7 @@ extern "C" int vtg_batch_profile(vtg_batch *b, int slot, int reps, float *pyr_ms
     std::vector<float> tp, tl;
     LkTune t = b->tune;
     t.chunk = sl.chunk;
+    t.tiled = sl.tiled;
     for (int r = 0; r < reps; r++) {
         CU(cudaEventRecord(e[0], b->stream));
         for (size_t k = 0; k < sl.h_src.size(); k++)
@@ -581,6 +594,7 @@ extern "C" int vtg_batch_count(vtg_batch *b, int slot, uint64_t *counts)
     BatchSlot &sl = b->slot[slot];
     LkTune t = b->tune;
     t.chunk = sl.chunk;
+    t.tiled = sl.tiled;
     CU(cudaSetDevice(vtg_ctx_device(b->ctx)));
     CU(cudaMemsetAsync(sl.d_count, 0, 4 * sizeof(unsigned long long), b->stream));
     CU(cudaMemsetAsync(sl.d_counter, 0, sizeof(int), b->stream));

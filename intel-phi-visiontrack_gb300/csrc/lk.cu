@@ -256,7 +256,7 @@ __device__ __forceinline__ void lk_build(const DevLevel &L, int ix, float fx, in
     f2_t prev = hlerp2(pa, pb, FX);
     /* S rows k - 1, k, k + 1 of each half: values, and their x + 1 minus x - 1 differences */
     f2_t u = 0ull, ul = 0ull, ur = 0ull, m = 0ull, ml = 0ull, mr = 0ull, mdx = 0ull, udx = 0ull;
-    f2_t sxx = 0ull, sxy = 0ull, syy = 0ull, scx = 0ull, scy = 0ull, TC = 0ull;
+    f2_t sxx = 0ull, sxy = 0ull, syy = 0ull, scx = 0ull, scy = 0ull, TC = 0ull, hu2 = 0ull, hm2 = 0ull;
     float tc = 0.0f;
 #pragma unroll
     for (int t = 0; t < HH + 2; t++) {
@@ -279,7 +279,9 @@ __device__ __forceinline__ void lk_build(const DevLevel &L, int ix, float fx, in
             if (t >= 2) {
                 const int k = t - 2; /* rows k and HH + k */
                 f2_t tx = f2_fma(mdx, TWO, f2_add(udx, ddx));
-                f2_t ty = f2_fma(f2_sub(d, u), TWO, f2_add(f2_sub(dl, ul), f2_sub(dr, ur)));
+                /* Sobel y as the horizontal smoothing (l + 2 c + r) of S row k + 1 less that of S row k - 1, the
+                 * latter kept from two steps back */
+                f2_t ty = f2_sub(f2_fma(d, TWO, f2_add(dl, dr)), hu2);
                 if (!EXACT) {
                     const f2_t keep = f2_pack(k < H ? 1.0f : 0.0f, HH + k < H ? 1.0f : 0.0f);
                     tx = f2_mul(tx, keep);
@@ -301,6 +303,7 @@ __device__ __forceinline__ void lk_build(const DevLevel &L, int ix, float fx, in
                 scx = f2_fma(tt, tx, scx);
                 scy = f2_fma(tt, ty, scy);
             }
+            hu2 = hm2; hm2 = f2_fma(d, TWO, f2_add(dl, dr));
             u = m; ul = ml; ur = mr; udx = mdx;
             m = d; ml = dl; mr = dr; mdx = ddx;
         }
@@ -578,7 +581,8 @@ __device__ __forceinline__ void lk_track(const DevPyr &I, const DevPyr &J, int t
         const float tr = gxx + gyy, df = gxx - gyy;
         const float root = sqrtf(__fmaf_rn(df, df, 4.0f * w2));
         const float lmax = 0.5f * (tr + root);
-        const float eig = lmax > 0.0f ? (det / lmax) / p.area : 0.0f;
+        /* the threshold test and min_eig's report need no correctly rounded quotient: the fast division's 2 ulp */
+        const float eig = lmax > 0.0f ? __fdividef(det, lmax * p.area) : 0.0f;
         if (L == 0)
             eig0 = eig;
         if (eig < p.min_eig || det <= 0.0f) {
@@ -590,7 +594,7 @@ __device__ __forceinline__ void lk_track(const DevPyr &I, const DevPyr &J, int t
             }
             continue;
         }
-        const float idet = 1.0f / det;
+        const float idet = __frcp_rn(det);
         if (L == 0) {
             idet0 = idet;
             gxx0 = gxx;
@@ -793,30 +797,60 @@ __global__ void __launch_bounds__(256, 2) lk_cells_kernel(const DevPyr *__restri
 /* Many streams' cells in one launch. Work items are runs of `chunk` cells of one job; job j's items start at
  * item_start[j]. PERSISTENT: a fixed grid whose warps take items from `counter` until none is left, so uneven streams
  * balance themselves; otherwise one warp per item. The cell code is the single-stream kernel's: a cell's result does
- * not depend on what else is in the batch. */
+ * not depend on what else is in the batch.
+ *
+ * TILED (persistent only): a job's cells are walked in tiles of LK_TILE_W x LK_TILE_H cells (row-major inside a tile,
+ * the tiles row-major over the grid; cells past the grid's edge are skipped), and each CTA takes whole tiles, tile
+ * g x gridDim.x + blockIdx.x for g = 0, 1, ..., its warps taking the tile's items from a counter in shared memory. So
+ * the cells a CTA runs at once are neighbours, whose windows overlap (at level L cells are 16 / 2^L by 8 / 2^L pixels
+ * apart, under a 23 x 23 window), and the SM's L1 serves one cell's rows to the next. The tiles are dealt to the CTAs
+ * in a fixed order, with no global counter. */
 #define LK_BATCH_MAX_JOBS 512
+#define LK_TILE_W 8
+#define LK_TILE_H 4
+#define LK_TILE_CELLS (LK_TILE_W * LK_TILE_H)
+
+/* Cell of work index w of a grid walked in tiles, or -1 past the grid's edge. */
+__device__ __forceinline__ int lk_tile_cell(const CellGrid &g, int w)
+{
+    const int tiles_x = (g.cols + LK_TILE_W - 1) / LK_TILE_W;
+    const int t = w / LK_TILE_CELLS, u = w - t * LK_TILE_CELLS;
+    const int col = (t % tiles_x) * LK_TILE_W + u % LK_TILE_W, row = (t / tiles_x) * LK_TILE_H + u / LK_TILE_W;
+    return (col < g.cols && row < g.rows) ? row * g.cols + col : -1;
+}
 
 template <int MAXH, bool EXACT, bool PERSISTENT, int WARPS, int MINB, bool TS>
 __global__ void __launch_bounds__(WARPS * 32, MINB) lk_batch_kernel(const LkJob *__restrict__ jobs,
                                                                     const int *__restrict__ item_start, int njobs,
                                                                     int items, int chunk, LkPrm p,
                                                                     int *__restrict__ counter,
-                                                                    unsigned long long *__restrict__ count)
+                                                                    unsigned long long *__restrict__ count,
+                                                                    int tiled)
 {
     __shared__ int s_start[LK_BATCH_MAX_JOBS + 1];
+    __shared__ int s_taken; /* tiled: the CTA's items taken so far */
     extern __shared__ f2_t s_t[]; /* TS: WARPS x (MAXH / 2) x 32 pairs */
     f2_t *ts = TS ? s_t + (size_t)(threadIdx.x >> 5) * (MAXH / 2) * 32 : nullptr;
     for (int k = threadIdx.x; k <= njobs; k += blockDim.x)
         s_start[k] = item_start[k]; /* the step's own table, written when it was prepared */
+    if (threadIdx.x == 0)
+        s_taken = 0;
     __syncthreads();
     vtg_grid_dependency_wait(); /* the pyramids and the counter, when launched as a dependent of the pyramid */
     const int lane = threadIdx.x & 31;
+    const int per_tile = LK_TILE_CELLS / chunk; /* items of a tile (tiled: chunk divides LK_TILE_CELLS) */
     int item = PERSISTENT ? 0 : (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     for (;;) {
         if (PERSISTENT) {
             int t = 0;
-            if (lane == 0)
-                t = atomicAdd(counter, 1);
+            if (lane == 0) {
+                if (tiled) {
+                    const int i = atomicAdd(&s_taken, 1), g = i / per_tile;
+                    t = (g * (int)gridDim.x + (int)blockIdx.x) * per_tile + (i - g * per_tile);
+                } else {
+                    t = atomicAdd(counter, 1);
+                }
+            }
             item = __shfl_sync(VTG_FULL, t, 0);
         }
         if (item >= items)
@@ -830,10 +864,13 @@ __global__ void __launch_bounds__(WARPS * 32, MINB) lk_batch_kernel(const LkJob 
                 hi = mid;
         }
         const LkJob &jb = jobs[lo];
-        const int c0 = (item - s_start[lo]) * chunk, c1 = min(c0 + chunk, jb.g.n);
-        for (int c = c0; c < c1; c++)
-            lk_cell<MAXH, EXACT, TS>(*jb.I, *jb.J, jb.top, p, jb.g, jb.base_w, jb.base_h, c, lane, jb.out, jb.cells, ts,
-                                     count);
+        const int c0 = (item - s_start[lo]) * chunk;
+        for (int c = c0; c < c0 + chunk; c++) {
+            const int cell = tiled ? lk_tile_cell(jb.g, c) : (c < jb.g.n ? c : -1);
+            if (cell >= 0)
+                lk_cell<MAXH, EXACT, TS>(*jb.I, *jb.J, jb.top, p, jb.g, jb.base_w, jb.base_h, cell, lane, jb.out,
+                                         jb.cells, ts, count);
+        }
         if (!PERSISTENT)
             break;
     }
@@ -848,7 +885,8 @@ static cudaError_t lk_batch_launch(const LkJob *jobs, const int *item_start, int
     do {                                                                                                               \
         const int blocks = P ? sms * t.ctas_per_sm : (items + WARPS - 1) / WARPS;                                      \
         const cudaError_t e = vtg_launch_k(lk_batch_kernel<MAXH, EXACT, P, WARPS, MINB, false>, blocks, WARPS * 32, 0, \
-                                           s, pdl, jobs, item_start, njobs, items, t.chunk, p, counter, count);        \
+                                           s, pdl, jobs, item_start, njobs, items, t.chunk, p, counter, count,         \
+                                           P ? t.tiled : 0);                                                           \
         if (e != cudaSuccess)                                                                                          \
             return e;                                                                                                  \
     } while (0)
@@ -864,7 +902,7 @@ static cudaError_t lk_batch_launch(const LkJob *jobs, const int *item_start, int
         }                                                                                                              \
         const cudaError_t e2 = vtg_launch_k(lk_batch_kernel<MAXH, EXACT, true, WARPS, MINB, true>,                    \
                                             sms * t.ctas_per_sm, WARPS * 32, smem, s, pdl, jobs, item_start, njobs,    \
-                                            items, t.chunk, p, counter, count);                                        \
+                                            items, t.chunk, p, counter, count, t.tiled);                               \
         if (e2 != cudaSuccess)                                                                                         \
             return e2;                                                                                                 \
     } while (0)

@@ -74,7 +74,16 @@ struct LkTune {
     int persistent;    /* 1: a grid of ctas_per_sm x SMs pulling items from a counter; 0: one warp per item */
     int ctas_per_sm;   /* for the persistent form */
     int tsmem;         /* 1: the template's T in shared memory (persistent; 4 warps x <= 5, 8 x <= 3 or 16 x 1 CTAs an SM) */
+    int tiled;         /* 1: cells in tiles of 8 x 4, whole tiles a CTA (persistent; chunk divides 32) */
 };
+
+/* Work items of one job's grid of cols x rows cells in runs of `chunk`: row-major, or (tiled) whole 8 x 4 tiles. */
+static inline int vtg_lk_items(int cols, int rows, int chunk, int tiled)
+{
+    if (tiled)
+        return ((cols + 7) / 8) * ((rows + 3) / 4) * (32 / chunk);
+    return (cols * rows + chunk - 1) / chunk;
+}
 
 /* Launchers (pyramid.cu, lk.cu). All asynchronous on `s`; each returns a cudaError_t. */
 cudaError_t vtg_launch_pyramid(const uint8_t *frame, int stride, int w, int h, float *const *levels, const int *pitches,

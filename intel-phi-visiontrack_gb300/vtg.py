@@ -346,7 +346,7 @@ def level_device(tracker: Tracker, set_: int, level: int):
 class Tune(C.Structure):
     """struct vtg_tune."""
     _fields_ = [("block_warps", C.c_int), ("chunk", C.c_int), ("persistent", C.c_int), ("ctas_per_sm", C.c_int),
-                ("tsmem", C.c_int)]
+                ("tsmem", C.c_int), ("tiled", C.c_int)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}

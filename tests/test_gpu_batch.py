@@ -70,15 +70,19 @@ def test_batch_equals_single_streams(vtg_lib, ctx, batch_setup):
             assert np.array_equal(trackers[k].level(1, L), ref[L])
 
 
-@pytest.mark.parametrize("tune", [dict(persistent=1, block_warps=8, chunk=1, ctas_per_sm=2, tsmem=0),
-                                  dict(persistent=1, block_warps=4, chunk=4, ctas_per_sm=4, tsmem=0),
-                                  dict(persistent=0, block_warps=16, chunk=2, ctas_per_sm=1, tsmem=0),
-                                  dict(persistent=1, block_warps=16, chunk=8, ctas_per_sm=1, tsmem=0),
-                                  dict(persistent=1, block_warps=4, chunk=2, ctas_per_sm=5, tsmem=1),
-                                  dict(persistent=1, block_warps=8, chunk=1, ctas_per_sm=3, tsmem=1),
-                                  dict(persistent=1, block_warps=16, chunk=2, ctas_per_sm=1, tsmem=1)])
+@pytest.mark.parametrize("tune", [dict(persistent=1, block_warps=8, chunk=1, ctas_per_sm=2, tsmem=0, tiled=0),
+                                  dict(persistent=1, block_warps=4, chunk=4, ctas_per_sm=4, tsmem=0, tiled=0),
+                                  dict(persistent=0, block_warps=16, chunk=2, ctas_per_sm=1, tsmem=0, tiled=0),
+                                  dict(persistent=1, block_warps=16, chunk=8, ctas_per_sm=1, tsmem=0, tiled=0),
+                                  dict(persistent=1, block_warps=4, chunk=2, ctas_per_sm=5, tsmem=1, tiled=0),
+                                  dict(persistent=1, block_warps=8, chunk=1, ctas_per_sm=3, tsmem=1, tiled=0),
+                                  dict(persistent=1, block_warps=16, chunk=2, ctas_per_sm=1, tsmem=1, tiled=0),
+                                  dict(persistent=1, block_warps=16, chunk=2, ctas_per_sm=1, tsmem=1, tiled=1),
+                                  dict(persistent=1, block_warps=8, chunk=4, ctas_per_sm=2, tsmem=0, tiled=1),
+                                  dict(persistent=1, block_warps=4, chunk=1, ctas_per_sm=5, tsmem=1, tiled=1)])
 def test_batch_launch_shapes_do_not_change_results(vtg_lib, ctx, batch_setup, tune):
-    """Every launch shape, the template in registers or in shared memory, gives the single-stream bits."""
+    """Every launch shape, the template in registers or in shared memory, cells in row order or in 8 x 4 tiles dealt
+    to the CTAs, gives the single-stream bits."""
     pairs, trackers, dev, singles, b = batch_setup
     for t, (d0, _) in zip(trackers, dev):
         t.build(0, d0.data_ptr(), where=vtg_lib.DEVICE)
@@ -92,11 +96,13 @@ def test_batch_launch_shapes_do_not_change_results(vtg_lib, ctx, batch_setup, tu
 def test_batch_refuses_bad_tunes(vtg_lib, ctx, batch_setup):
     b = batch_setup[4]
     before = b.get_tune()
-    for bad in (dict(persistent=1, block_warps=16, chunk=1, ctas_per_sm=2, tsmem=1),
-                dict(persistent=0, block_warps=4, chunk=1, ctas_per_sm=1, tsmem=1),
-                dict(persistent=1, block_warps=8, chunk=1, ctas_per_sm=4, tsmem=1),
-                dict(persistent=1, block_warps=6, chunk=1, ctas_per_sm=1, tsmem=0),
-                dict(persistent=1, block_warps=8, chunk=0, ctas_per_sm=1, tsmem=0)):
+    for bad in (dict(persistent=1, block_warps=16, chunk=1, ctas_per_sm=2, tsmem=1, tiled=0),
+                dict(persistent=0, block_warps=4, chunk=1, ctas_per_sm=1, tsmem=1, tiled=0),
+                dict(persistent=1, block_warps=8, chunk=1, ctas_per_sm=4, tsmem=1, tiled=0),
+                dict(persistent=1, block_warps=6, chunk=1, ctas_per_sm=1, tsmem=0, tiled=0),
+                dict(persistent=1, block_warps=8, chunk=0, ctas_per_sm=1, tsmem=0, tiled=0),
+                dict(persistent=0, block_warps=8, chunk=1, ctas_per_sm=1, tsmem=0, tiled=1),
+                dict(persistent=1, block_warps=8, chunk=3, ctas_per_sm=1, tsmem=0, tiled=1)):
         with pytest.raises(vtg_lib.VtgError):
             b.set_tune(**bad)
     assert b.get_tune() == before
