@@ -177,17 +177,14 @@ def ref_detect(plane, rx, ry, rw, rh, margin, max_n, min_dist, quality):
 
 
 def ref_available() -> bool:
-    """True where the reference's own sources are here to build oracle/_ref (this container, not the GPU machine)."""
+    """True where oracle/_ref/libvtref.so, the reference's own kernels, is built or can be: where the reference tree the
+    Makefile reads is on this host. Elsewhere the Makefile's `ref` target fails and the checks that need it are
+    skipped."""
     path = os.path.join(HERE, "_ref", "libvtref.so")
     if os.path.exists(path):
         return True
-    if os.path.isdir("/root/reference/src/kern"):
-        try:
-            _build("ref")
-        except subprocess.CalledProcessError:
-            return False
-        return os.path.exists(path)
-    return False
+    r = subprocess.run(["make", "-s", "-C", HERE, "ref"], capture_output=True)
+    return r.returncode == 0 and os.path.exists(path)
 
 
 def ref() -> C.CDLL:
