@@ -999,7 +999,8 @@ def run_framegen(args) -> dict:
 
 def run_profile(args) -> None:
     """Launches for an ncu capture, nothing timed: `batch` primes B 1080p streams (2 batched steps) and runs 2 more
-    (capture lk_batch_kernel with -s 2); `ncc` runs one 1080p whole-picture search per precision (32 x 32 template)."""
+    (capture lk_batch_kernel with -s 2); `ncc` runs one 1080p whole-picture search per precision (a --ncc-size
+    template)."""
     import torch
 
     import vtg
@@ -1061,7 +1062,7 @@ def run_profile(args) -> None:
         det.close()
     else:
         frame = S.noise_frame(W, H, seed=3)
-        tpl, xs, ys, _ = S.ncc_templates(frame, 32, 1, seed=1, blank_share=0.0)
+        tpl, xs, ys, _ = S.ncc_templates(frame, args.ncc_size, 1, seed=1, blank_share=0.0)
         app = (tpl[0].astype(np.float32) - np.float32(tpl[0].mean(dtype=np.float64))).astype(np.float32)
         norm = float(np.sum(app.astype(np.float64) ** 2))
         d = torch.from_numpy(frame).cuda()
@@ -1095,6 +1096,7 @@ def main():
                     help="the still picture a frame at 960 x 540 and 1920 x 1080 (vectors, decision, running mean)")
     ap.add_argument("--profile", default=None, choices=["batch", "ncc", "detect", "still", "framegen"],
                     help="a short run for an ncu capture: the batched step (prime, then 2 steps) or one NCC search")
+    ap.add_argument("--ncc-size", type=int, default=32, help="--profile ncc: the template's side (32, 64 or 96)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.profile:

@@ -190,3 +190,35 @@ def test_serve_live_under_overload_counts_skips(vtg_lib, ctx):
     assert st["served"] + st["skipped"] + st["dropped"] == st["requests"]
     ordered = vtg_lib.serve(ctx, streams, [b.data_ptr() for b in bufs], lk, duration_s=2.0, live=False)
     assert ordered["skipped"] == 0 and st["p99_ms"] < ordered["p99_ms"]
+
+
+def test_server_search_request_matches_a_direct_search(vtg_lib, ctx):
+    """A frame submitted with VTG_REQ_SEARCH comes back with the appearance search of its level 1 (step 2, the whole
+    plane, the server's template): the same corner and score as vtg_search_run on that plane with that template."""
+    import oracle as O
+
+    seq = _seq(640, 480, 1, seed=140)
+    frame = seq[1].numpy()
+    level1 = O.pyramid(frame, 4)[1]
+    app, norm = O.cut_template(level1.astype(np.float32), 150, 90, 32, 21)
+    srv = vtg_lib.Server(ctx, vtg_lib.config(64, 64, levels=4))
+    srv.template(app, norm)
+    sid = srv.open(640, 480, seq[0].data_ptr())
+    assert sid >= 0
+    assert srv.submit(sid, seq[1].data_ptr(), flags=vtg_lib.REQ_SEARCH, tag=7) >= 0
+    res = _drain(srv, 1)
+    srv.close()
+    assert len(res) == 1 and res[0]["status"] == vtg_lib.RES_DONE and res[0]["searched"] == 1
+    got = res[0]["found"]
+    t = vtg_lib.Tracker(ctx, vtg_lib.config(640, 480, levels=4))
+    t.build(0, frame)
+    t.sync()
+    ptr, lw, lh, lp = vtg_lib.level_device(t, 0, 1)
+    s = vtg_lib.Search(ctx, lw, lh, 32, 21)
+    s.template(app, norm)
+    want = s.run(ptr, lw, lh, lp, vtg_lib.PLANE_F32, 1, lw, 1, lh, 2, vtg_lib.NCC_F32)
+    s.close()
+    t.close()
+    assert (got["hx"], got["hy"], got["ntop"], got["cells"]) == (want["hx"], want["hy"], want["ntop"], want["cells"])
+    assert got["ncc"] == want["ncc"] and got["second"] == want["second"]
+    assert (got["hx"], got["hy"]) == (300, 180)  # the template's own corner, in half pixels
