@@ -78,7 +78,7 @@ static SearchLayout search_layout(int max_w, int max_h, int max_tw, int max_th)
     L.conv_elems = vtg_ncc_conv_elems(max_w, max_h, max_th);
     L.conv = b;
     b += up256(sizeof(uint16_t) * L.conv_elems);
-    L.fac_elems = (size_t)max_w * max_h;
+    L.fac_elems = vtg_ncc_fac_elems(max_w, max_h);
     L.fac = b;
     b += up256(sizeof(float) * L.fac_elems);
     L.cellw = b;

@@ -4,7 +4,7 @@
  * per-cell map in the epilogue.
  *
  * The correlation as a GEMM. A CTA owns a tile of corners: 1024 consecutive x (X0 + 8 m + s, m < 128, s < 8) by Q
- * consecutive y (Y0 + q, q < Q; Q = 4 for templates up to 64 rows, else 8). Then
+ * consecutive y (Y0 + q, q < Q; Q = 16, or 8 for templates wider than 120). Then
  *     st(X0 + 8 m + s, Y0 + q) = sum over image rows r, columns c of  A_r[m][c] * B_r[(q, s)][c]
  * with A_r[m][c] = J[r][X0 + 8 m + c] and B_r[(q, s)][c] = t[r - Y0 - q][c - s] (zero outside the template): D =
  * sum_r A_r B_r^T with M = 128, N = 8 Q, and K = the tile's Q + T_h - 1 image rows times K_row = T_w + 8 rounded up
@@ -13,34 +13,48 @@
  *   no-swizzle descriptor with 16-byte core-matrix rows, a 16-byte leading (K) offset and a 128-byte stride (M) offset
  *   reads A_r straight from the row: address(m, k) = row + 2 (8 m + k). The picture is converted to 16 bits once per
  *   search (ncc_conv), shifted so that every tile's row segment starts on a 16-byte boundary.
- *   B_r depends only on r - Y0: the band (8 + T_h - 1 blocks of 64 x K_row) is built once per template in the canonical
+ *   B_r depends only on r - Y0: the band (Q + T_h - 1 blocks of 8 Q x K_row) is built once per template in the canonical
  *   core-matrix layout.
- * Pipeline: two threads drive it. Six shared-memory stages, each an image-row segment and a band block, arrive by
+ * Pipeline: three threads drive it. Six shared-memory stages, each an image-row segment and a band block, arrive by
  * cp.async.bulk on a "full" mbarrier (expected bytes). A producer thread (warp 0) fills a stage again as soon as the
- * MMAs of its last use commit to its "empty" mbarrier; an issuer thread (warp 1) issues each stage's MMAs as soon as
- * its copies land, so copies run several stages ahead and the tensor core is fed back to back. Every wait is bounded by
- * the global timer; past it the kernel records an error word.
- * Epilogue: each of the 128 threads owns one accumulator row (8 x-corners by Q y-corners). Per corner: st = acc -
- * J(x, y) sum t' (the reference's st is relative to the corner's first pixel), times the corner's factor 1 / sqrt(norm
- * var) from ncc_box_prep (0 for a near-blank window: the exact integer rule), the best per 16 x 16 cell by value then scan
- * order, merged across tiles by a 64-bit atomicMax on (ordered score, inverted scan index). */
+ * MMAs of its last use commit to its "empty" mbarrier. Two issuer threads (warps 1 and 2) take alternate stages, each
+ * into its own accumulator: issuing a stage's MMAs takes a lone thread longer than the tensor core takes to run them,
+ * so one issuer would leave it idle. Every wait is bounded by the global timer; past it the kernel records an error
+ * word.
+ * Epilogue: each of the 128 threads owns one accumulator row (8 x-corners by Q y-corners) of each issuer and sums
+ * them. Per corner: st = acc - J(x, y) sum t' (the reference's st is relative to the corner's first pixel), times the
+ * corner's factor 1 / sqrt(norm var) from ncc_box_prep (0 for a near-blank window: the exact integer rule), the best
+ * per 16 x 16 cell by value then scan order, merged across tiles by a 64-bit atomicMax on (ordered score, inverted scan
+ * index). */
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
 #include "vtg_ncc.cuh"
 
 #define TC_M 128
-#define TC_QMAX 8 /* y-corners of a tile, at most */
+#define TC_QMAX 16 /* y-corners of a tile, at most */
 #define TC_XS (8 * TC_M) /* x-corners of a tile */
 #define TC_STAGES 6
+#ifndef TC_ISSUERS
+#define TC_ISSUERS 2 /* MMA-issuing threads, each with its own accumulator, taking every TC_ISSUERS-th stage */
+#endif
 #define TC_WAIT_NS 2000000000ull /* a wait gives up after 2 s of the global timer */
 #define TC_MAX_KROW 144          /* T_w <= 128 */
 
 static inline int tc_krow(int tw) { return ((tw + 8 + 15) / 16) * 16; }
 
-/* y-corners of a tile for a template th rows high: 4 (N = 32) gives twice the tiles of 8, so co-resident CTAs overlap
- * one another's epilogues and MMAs; past 64 rows the band each tile copies grows too long for that to pay. */
-static inline int tc_q(int th) { return th <= 64 ? 4 : 8; }
+/* y-corners of a tile (N = 8 Q). An MMA reads its A (4 KB) and B (16 N bytes) from shared memory at 128 bytes a cycle
+ * and multiplies for N / 2 cycles, so below N = 128 the shared-memory reads bound it. Q = 16 while six stages of it fit
+ * the shared memory (K_row <= 128), else 8. The band's zero rows (Q - 1 of every Q + th - 1 image rows) cost less than
+ * the reads they save. */
+#ifndef TC_Q_BIG
+#define TC_Q_BIG 16
+#endif
+static inline int tc_q(int tw, int th)
+{
+    (void)th;
+    return TC_Q_BIG == 16 && tc_krow(tw) > 128 ? 8 : TC_Q_BIG;
+}
 
 /* the band at its largest tile height: enough for either */
 size_t vtg_ncc_band_bytes(int tw, int th) { return (size_t)(TC_QMAX + th - 1) * 8 * TC_QMAX * tc_krow(tw) * sizeof(uint16_t); }
@@ -49,6 +63,9 @@ size_t vtg_ncc_band_bytes(int tw, int th) { return (size_t)(TC_QMAX + th - 1) * 
 static inline int conv_pitch(int w) { return ((w + TC_XS - 1) / TC_XS) * TC_XS + TC_MAX_KROW; }
 
 size_t vtg_ncc_conv_elems(int max_w, int max_h, int max_th) { return (size_t)conv_pitch(max_w) * (size_t)(max_h + TC_QMAX + max_th); }
+
+/* The corners' factors: rows of whole tiles (TC_XS corners), so a tile's factor loads stay inside its row. */
+size_t vtg_ncc_fac_elems(int max_w, int max_h) { return (size_t)((max_w + TC_XS - 1) / TC_XS) * TC_XS * (size_t)max_h; }
 
 /* ---- the band ---- */
 
@@ -102,7 +119,7 @@ __global__ void ncc_band_sum(const float *__restrict__ app, int count, int kind,
 
 cudaError_t vtg_launch_ncc_band(const float *app, int tw, int th, int kind, uint16_t *band, float *sum_t, cudaStream_t st)
 {
-    const int q = tc_q(th), krow = tc_krow(tw), rows = q + th - 1;
+    const int q = tc_q(tw, th), krow = tc_krow(tw), rows = q + th - 1;
     const size_t total = (size_t)8 * q * krow * rows;
     const int blocks = (int)((total + 255) / 256 < 4096 ? (total + 255) / 256 : 4096);
     ncc_band_kernel<<<blocks, 256, 0, st>>>(app, tw, th, kind, krow, rows, q, band);
@@ -137,7 +154,7 @@ __global__ void ncc_conv(const uint8_t *__restrict__ plane, int pitch, int w, in
     *reinterpret_cast<uint4 *>(conv + (size_t)r * cpitch + i0) = make_uint4(o[0], o[1], o[2], o[3]);
 }
 
-/* fac[(y - y0) fw + (x - x0)] = 1 / sqrt(norm var) from the corner's exact window sums; 0 for a near-blank window
+/* fac[(y - y0) fpitch + (x - x0)] = 1 / sqrt(norm var) from the corner's exact window sums; 0 for a near-blank window
  * (n var <= n norm / 16) or norm <= 0 -- the reference's rule (src/kern/track.c:203-205) on exact integers.
  * The sums come straight from the bytes, a tile of btx x BP_TY corners a CTA (btx = bp_tx(T_w)), one thread a column
  * of the tile:
@@ -151,7 +168,7 @@ __global__ void ncc_conv(const uint8_t *__restrict__ plane, int pitch, int w, in
 /* corners a CTA across: the most, a multiple of 32, whose columns (+ T_w - 1) fit the CTA's 256 threads */
 static inline int bp_tx(int tw) { return ((257 - tw) / 32) * 32; }
 __global__ void __launch_bounds__(256) ncc_box_prep(const uint8_t *__restrict__ plane, int pitch, NccPrm p, int fw,
-                                                    int btx, float *__restrict__ fac)
+                                                    int fpitch, int btx, float *__restrict__ fac)
 {
     __shared__ unsigned P1[BP_TY][257], P2[BP_TY][257]; /* P[r][c]: columns 0 .. c - 1 of row r */
     __shared__ unsigned t1[8][BP_TY], t2[8][BP_TY];     /* each warp's column totals, then the earlier warps' */
@@ -233,7 +250,7 @@ __global__ void __launch_bounds__(256) ncc_box_prep(const uint8_t *__restrict__ 
         const long long s1 = (long long)(P1[r][x + p.tw] - P1[r][x]), s2 = (long long)(P2[r][x + p.tw] - P2[r][x]);
         const long long nvar = (long long)p.n * s2 - s1 * s1;
         /* 1 / sqrt(norm var) = sqrt(n / norm) / sqrt(n var) */
-        fac[(size_t)(ty0 + r) * fw + (tx0 + x)] = (nvar <= p.nthr || p.norm <= 0.0f) ? 0.0f : p.rnorm * rsqrtf((float)nvar);
+        fac[(size_t)(ty0 + r) * fpitch + (tx0 + x)] = (nvar <= p.nthr || p.norm <= 0.0f) ? 0.0f : p.rnorm * rsqrtf((float)nvar);
     }
 }
 
@@ -304,21 +321,14 @@ __device__ __forceinline__ void tc_commit(uint32_t mbar)
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar) : "memory");
 }
 
-__device__ __forceinline__ void tc_ld32(uint32_t taddr, float (&v)[32])
+/* 16 consecutive accumulator columns of the thread's row (lane = row within the warp's 32), not yet waited for */
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, uint32_t (&r)[16])
 {
-    uint32_t r[32];
-    asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
-                 "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+                 "%15}, [%16];"
                  : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-                   "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]),
-                   "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]),
-                   "=r"(r[30]), "=r"(r[31])
+                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
                  : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int i = 0; i < 32; i++)
-        v[i] = __uint_as_float(r[i]);
 }
 
 /* A cell's candidate as one orderable word: higher score first, then the earlier corner in scan order. 0: none. */
@@ -330,6 +340,16 @@ __device__ __forceinline__ unsigned long long cell_word(float v, int key)
 }
 
 /* ---- the map ---- */
+
+/* Tensor-memory columns a CTA allocates: the issuers' accumulators (8 Q columns each), rounded up to a power of two
+ * of at least 32 as tcgen05.alloc requires. */
+__host__ __device__ constexpr uint32_t tc_cols(int q)
+{
+    return 8u * q * TC_ISSUERS <= 32u ? 32u : 8u * q * TC_ISSUERS <= 64u ? 64u : 8u * q * TC_ISSUERS <= 128u ? 128u
+           : 8u * q * TC_ISSUERS <= 256u ? 256u : 512u;
+}
+static_assert(8 * TC_QMAX * TC_ISSUERS <= 512, "the accumulators fit the tensor memory");
+static_assert(TC_ISSUERS >= 1 && TC_ISSUERS <= 3, "issuers are warps 1 .. 3 of the CTA's four");
 
 struct TcSmem {
     uint32_t a_bytes, b_bytes, stage_bytes, total;
@@ -345,12 +365,19 @@ static TcSmem tc_smem(int krow, int q)
     return s;
 }
 
+/* Threads of a CTA: four warps cover the accumulator's 128 lanes; at Q = 16 eight, two to a lane quarter, each warp
+ * of a pair reading half the columns. chunks: 16-column blocks a thread reads. */
+template <int Q> struct TcShape {
+    static constexpr int threads = Q == 16 ? 256 : 128;
+    static constexpr int halves = threads / 128;
+    static constexpr int chunks = Q / 2 / halves;
+};
+
 template <int KIND, int Q>
-__global__ void __launch_bounds__(128, 1) ncc_map_tc(const uint8_t *__restrict__ plane, int pitch, NccPrm p,
-                                                     const uint16_t *__restrict__ band, int krow, int tiles_x,
+__global__ void __launch_bounds__(TcShape<Q>::threads, 1) ncc_map_tc(NccPrm p, const uint16_t *__restrict__ band, int krow, int tiles_x,
                                                      uint32_t a_bytes, uint32_t stage_bytes,
                                                      const uint16_t *__restrict__ conv, int cpitch,
-                                                     const float *__restrict__ fac, int fw,
+                                                     const float *__restrict__ fac, int fpitch,
                                                      unsigned long long *__restrict__ cellw, int *__restrict__ err)
 {
     extern __shared__ __align__(1024) uint8_t smem[];
@@ -362,8 +389,32 @@ __global__ void __launch_bounds__(128, 1) ncc_map_tc(const uint8_t *__restrict__
     uint8_t *ctl = smem + TC_STAGES * stage_bytes;
     const uint32_t full0 = smem_u32(ctl), empty0 = full0 + 8 * TC_STAGES;
     uint32_t *tmem_slot = (uint32_t *)(ctl + 16 * TC_STAGES);
-    int *issued = (int *)(ctl + 16 * TC_STAGES + 8); /* [0]: stages filled, [1]: stages whose MMAs were committed */
+    /* [0]: stages filled; [1 + i]: 1 + the last stage issuer i committed (0: none) */
+    int *issued = (int *)(ctl + 16 * TC_STAGES + 8);
     const uint32_t a_copy = (uint32_t)((TC_XS + krow) * 2), b_copy = (uint32_t)((8 * Q) * krow * 2);
+
+    /* The epilogue's inputs, loaded first: they are in memory before the MMAs start, and arrive while those run. Thread
+     * (quad, lane) owns accumulator row m = 32 quad + lane, corners X0 + 8 m + s, and of its y-corners the pair half of
+     * the CTA's reads: 2 chunks each. A y-corner's eight picture values (the converted row holds the bytes exactly) and
+     * eight factors are one 16-byte and two 16-byte loads. */
+    constexpr int CH = TcShape<Q>::chunks;
+    const int m = (warp & 3) * 32 + lane, c0 = (warp >> 2) * CH;
+    const int xr = tx * TC_XS + 8 * m; /* x - x0 of the thread's first corner */
+    const int fh = p.y1 - p.y0 + 1;
+    uint4 jr[2 * CH];
+    float4 fr[4 * CH];
+#pragma unroll
+    for (int i = 0; i < 2 * CH; i++) {
+        const int yr = ty * Q + 2 * c0 + i;
+        if (yr < fh) {
+            jr[i] = __ldg(reinterpret_cast<const uint4 *>(conv + (size_t)(p.y0 + yr) * cpitch + xr));
+            fr[2 * i] = __ldg(reinterpret_cast<const float4 *>(fac + (size_t)yr * fpitch + xr));
+            fr[2 * i + 1] = __ldg(reinterpret_cast<const float4 *>(fac + (size_t)yr * fpitch + xr + 4));
+        } else {
+            jr[i] = make_uint4(0u, 0u, 0u, 0u);
+            fr[2 * i] = fr[2 * i + 1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        }
+    }
 
     if (tid == 0) {
         for (int s = 0; s < TC_STAGES; s++) {
@@ -374,7 +425,7 @@ __global__ void __launch_bounds__(128, 1) ncc_map_tc(const uint8_t *__restrict__
     }
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                     "r"((8 * Q))
+                     "r"(tc_cols(Q))
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -404,31 +455,33 @@ __global__ void __launch_bounds__(128, 1) ncc_map_tc(const uint8_t *__restrict__
                     band + (size_t)k * (8 * Q) * krow, b_copy);
         }
         issued[0] = k;
-    } else if (warp == 1 && lane == 0) {
-        /* the MMA issuer: each stage's MMAs as soon as its copies have landed, back to back; a commit frees the stage
-         * for the producer */
-        int k = 0;
-        for (; k < nk; k++) {
+    } else if (warp >= 1 && warp <= TC_ISSUERS && lane == 0) {
+        /* the MMA issuers: issuer i takes stages i, i + TC_ISSUERS, ... into its own accumulator (8 Q columns at
+         * 8 Q i), each stage's MMAs as soon as its copies have landed; a commit frees the stage for the producer. A
+         * lone thread spends most of a stage issuing its MMAs, so several threads shorten the tile's chain. */
+        const int ia = warp - 1;
+        const uint32_t acc = tmem + (uint32_t)(8 * Q * ia);
+        int last = -1;
+        for (int k = ia; k < nk; k += TC_ISSUERS) {
             const int s = k % TC_STAGES;
             if (!mbar_wait(full0 + 8 * s, (uint32_t)((k / TC_STAGES) & 1))) {
                 good = 0;
                 break;
             }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            /* K chunk kc starts 32 bytes further into the row and 2 Q core matrices further into the band block: the
+             * descriptors' start fields (16-byte units, no carry below 256 KB) step by 2 and by 16 Q */
             const uint32_t a0 = smem_u32(smem + s * stage_bytes), b0 = a0 + a_bytes;
-            for (int kc = 0; kc < kchunks; kc++) {
-                const uint64_t ad = mdesc(a0 + 32 * kc, 16, 128);
-                const uint64_t bd = mdesc(b0 + kc * 2 * ((8 * Q) / 8) * 128, ((8 * Q) / 8) * 128, 128);
-                tc_mma(tmem, ad, bd, idesc, (k | kc) != 0);
-            }
+            const uint64_t ad = mdesc(a0, 16, 128), bd = mdesc(b0, Q * 128, 128);
+            for (int kc = 0; kc < kchunks; kc++)
+                tc_mma(acc, ad + 2u * kc, bd + (uint64_t)(16 * Q) * kc, idesc, (k != ia || kc != 0) ? 1u : 0u);
             tc_commit(empty0 + 8 * s);
+            last = k;
         }
-        issued[1] = k;
-        /* the last commit covers every MMA */
-        if (good) {
-            const int last = nk - 1;
+        issued[1 + ia] = last + 1;
+        /* an issuer's last commit covers every MMA it issued */
+        if (good && last >= 0)
             good = mbar_wait(empty0 + 8 * (last % TC_STAGES), (uint32_t)((last / TC_STAGES) & 1)) ? 1 : 0;
-        }
     }
     const int ok_all = __syncthreads_and(good);
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -440,36 +493,71 @@ __global__ void __launch_bounds__(128, 1) ncc_map_tc(const uint8_t *__restrict__
          * have stopped and the context cannot be saved from here. */
         if (tid == 0) {
             atomicExch(err, 1);
-            const int kp = issued[0], ki = issued[1];
-            if (ki > 0)
-                mbar_wait(empty0 + 8 * ((ki - 1) % TC_STAGES), (uint32_t)(((ki - 1) / TC_STAGES) & 1));
-            for (int k = ki; k < kp; k++)
-                mbar_wait(full0 + 8 * (k % TC_STAGES), (uint32_t)((k / TC_STAGES) & 1));
+            const int kp = issued[0];
+            for (int i = 0; i < TC_ISSUERS; i++) {
+                const int lk = issued[1 + i] - 1;
+                if (lk >= 0)
+                    mbar_wait(empty0 + 8 * (lk % TC_STAGES), (uint32_t)((lk / TC_STAGES) & 1));
+            }
+            /* a stage not committed by its issuer was not refilled: its barrier is still in that stage's phase */
+            for (int k = 0; k < kp; k++)
+                if (k >= issued[1 + k % TC_ISSUERS])
+                    mbar_wait(full0 + 8 * (k % TC_STAGES), (uint32_t)((k / TC_STAGES) & 1));
         }
     } else {
-        /* epilogue: thread m owns accumulator row m: corners X0 + 8 m + s, Y0 + q */
-        const int m = warp * 32 + lane;
-        const int per = NCC_CELL / p.step;
+        /* epilogue. The step is a power of two dividing the cell, and X0 - x0 is a multiple of 16, so the corner (x, y)
+         * is on the step grid when (8 m + s) and y - y0 are multiples of it. */
+        const int sh = __ffs(p.step) - 1;
+        const int per = NCC_CELL >> sh;
         const int ly0 = (ty % (NCC_CELL / Q)) * Q; /* this tile's first row inside its cell row */
+        uint32_t xmask = 0;
+#pragma unroll
+        for (int s = 0; s < 8; s++)
+            if (xr + s <= p.x1 - p.x0 && ((8 * m + s) & (p.step - 1)) == 0)
+                xmask |= 1u << s;
         float best = -2.0f;
         int bkey = 1 << 30;
-#pragma unroll 1
-        for (int c = 0; c < (8 * Q) / 32; c++) {
-            float v[32];
-            tc_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(32 * c), v);
 #pragma unroll
-            for (int j = 0; j < 32; j++) {
-                const int q = 4 * c + (j >> 3), s = j & 7;
-                const int x = X0 + 8 * m + s, y = Y0 + q;
-                if (x > p.x1 || y > p.y1 || ((x - p.x0) % p.step) || ((y - p.y0) % p.step))
+        for (int cc = 0; cc < CH; cc++) {
+            const int c = c0 + cc;
+            /* columns 16 c .. 16 c + 15 (y-corners 2 c, 2 c + 1) of every issuer's accumulator, summed in issuer order */
+            float v[16];
+            {
+                const uint32_t row = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(16 * c);
+                uint32_t r[TC_ISSUERS][16];
+#pragma unroll
+                for (int i = 0; i < TC_ISSUERS; i++)
+                    tc_ld16(row + (uint32_t)(8 * Q * i), r[i]);
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+                for (int e = 0; e < 16; e++) {
+                    v[e] = __uint_as_float(r[0][e]);
+#pragma unroll
+                    for (int i = 1; i < TC_ISSUERS; i++)
+                        if (i < nk) /* an issuer with no stage left its accumulator unwritten */
+                            v[e] += __uint_as_float(r[i][e]);
+                }
+            }
+#pragma unroll
+            for (int qq = 0; qq < 2; qq++) {
+                const int q = 2 * c + qq, yr = ty * Q + q;
+                if (yr >= fh || (yr & (p.step - 1)))
                     continue;
-                const float j0 = (float)__ldg(plane + (size_t)y * pitch + x);
-                const float f = __ldg(fac + (size_t)(y - p.y0) * fw + (x - p.x0));
-                const float score = (v[j] - j0 * p.sum_t) * f;
-                const int key = ((ly0 + q) / p.step) * per + ((8 * (m & 1) + s) / p.step);
-                if (score > best || (score == best && key < bkey)) {
-                    best = score;
-                    bkey = key;
+                const int i = 2 * cc + qq;
+                const uint32_t jw[4] = {jr[i].x, jr[i].y, jr[i].z, jr[i].w};
+                const float fq[8] = {fr[2 * i].x, fr[2 * i].y, fr[2 * i].z, fr[2 * i].w,
+                                     fr[2 * i + 1].x, fr[2 * i + 1].y, fr[2 * i + 1].z, fr[2 * i + 1].w};
+#pragma unroll
+                for (int s = 0; s < 8; s++) {
+                    if (!((xmask >> s) & 1u))
+                        continue;
+                    const float j0 = from16((uint16_t)(jw[s >> 1] >> (16 * (s & 1))), KIND);
+                    const float score = (v[8 * qq + s] - j0 * p.sum_t) * fq[s];
+                    const int key = ((ly0 + q) >> sh) * per + ((8 * (m & 1) + s) >> sh);
+                    if (score > best || (score == best && key < bkey)) {
+                        best = score;
+                        bkey = key;
+                    }
                 }
             }
         }
@@ -487,7 +575,7 @@ __global__ void __launch_bounds__(128, 1) ncc_map_tc(const uint8_t *__restrict__
     __syncthreads();
     if (warp == 0) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((8 * Q)) : "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(tc_cols(Q)) : "memory");
     }
 }
 
@@ -521,13 +609,15 @@ cudaError_t vtg_launch_ncc_map_tc(const void *plane, int pitch, int elem_bytes, 
     if (elem_bytes != 1 || !s.band || !s.conv || !s.fac || !s.cellw || (kind != VTG_NCC_BF16 && kind != VTG_NCC_FP16) ||
         p.tw > 128)
         return cudaErrorInvalidValue;
-    const int krow = tc_krow(p.tw), q = tc_q(p.th);
+    const int krow = tc_krow(p.tw), q = tc_q(p.tw, p.th);
     const TcSmem sm = tc_smem(krow, q);
     const int fw = p.x1 - p.x0 + 1, fh = p.y1 - p.y0 + 1;
     const int tiles_x = (fw + TC_XS - 1) / TC_XS, tiles_y = (fh + q - 1) / q;
     const int cpitch = tiles_x * TC_XS + TC_MAX_KROW;
+    const int fpitch = tiles_x * TC_XS; /* every tile's 1,024 corners inside a factor row */
     const int rows = p.y0 + tiles_y * q + p.th; /* every row a tile's band reads */
-    if ((size_t)cpitch * rows > s.conv_elems || (size_t)fw * fh > s.fac_elems)
+    if ((size_t)cpitch * rows > s.conv_elems || (size_t)fpitch * fh > s.fac_elems || (p.step & (p.step - 1)) ||
+        NCC_CELL % p.step)
         return cudaErrorInvalidValue;
     const int cells = p.ccols * p.crows;
     cudaError_t e = cudaMemsetAsync(s.cellw, 0, sizeof(unsigned long long) * (size_t)cells, st);
@@ -540,7 +630,7 @@ cudaError_t vtg_launch_ncc_map_tc(const void *plane, int pitch, int elem_bytes, 
         ncc_conv<VTG_NCC_FP16><<<cgrid, 256, 0, st>>>((const uint8_t *)plane, pitch, p.w, p.h, p.x0, rows, cpitch, s.conv);
     const int btx = bp_tx(p.tw);
     ncc_box_prep<<<dim3((fw + btx - 1) / btx, (fh + BP_TY - 1) / BP_TY), 256, 0, st>>>((const uint8_t *)plane, pitch, p,
-                                                                                      fw, btx, s.fac);
+                                                                                      fw, fpitch, btx, s.fac);
 #define MAP_TC(K, QQ)                                                                                                  \
     do {                                                                                                               \
         e = cudaFuncSetAttribute(ncc_map_tc<K, QQ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm.total);       \
@@ -548,22 +638,22 @@ cudaError_t vtg_launch_ncc_map_tc(const void *plane, int pitch, int elem_bytes, 
             return e;                                                                                                  \
         if (s.map_ev0 && (e = cudaEventRecord(s.map_ev0, st)) != cudaSuccess)                                          \
             return e;                                                                                                  \
-        ncc_map_tc<K, QQ><<<tiles_x * tiles_y, 128, sm.total, st>>>((const uint8_t *)plane, pitch, p, s.band, krow,    \
-                                                                   tiles_x, sm.a_bytes, sm.stage_bytes, s.conv,        \
-                                                                   cpitch, s.fac, fw, s.cellw, s.err);                 \
+        ncc_map_tc<K, QQ><<<tiles_x * tiles_y, TcShape<QQ>::threads, sm.total, st>>>(p, s.band, krow, tiles_x, sm.a_bytes,              \
+                                                                   sm.stage_bytes, s.conv, cpitch, s.fac, fpitch,      \
+                                                                   s.cellw, s.err);                                    \
         if (s.map_ev1 && (e = cudaEventRecord(s.map_ev1, st)) != cudaSuccess)                                          \
             return e;                                                                                                  \
     } while (0)
     if (kind == VTG_NCC_BF16) {
-        if (q == 4)
-            MAP_TC(VTG_NCC_BF16, 4);
-        else
+        if (q == 8)
             MAP_TC(VTG_NCC_BF16, 8);
-    } else {
-        if (q == 4)
-            MAP_TC(VTG_NCC_FP16, 4);
         else
+            MAP_TC(VTG_NCC_BF16, 16);
+    } else {
+        if (q == 8)
             MAP_TC(VTG_NCC_FP16, 8);
+        else
+            MAP_TC(VTG_NCC_FP16, 16);
     }
 #undef MAP_TC
     ncc_cells_out<<<(cells + 255) / 256, 256, 0, st>>>(p, s.cellw, s.map_v, s.map_x, s.map_y);

@@ -58,6 +58,7 @@ struct NccScratch {
 
 /* Elements of the tensor-core map's scratch for planes up to max_w x max_h and templates up to max_tw x max_th. */
 size_t vtg_ncc_conv_elems(int max_w, int max_h, int max_th);
+size_t vtg_ncc_fac_elems(int max_w, int max_h);
 
 cudaError_t vtg_launch_ncc(const void *plane, int pitch, int plane_type, const float *app, const NccPrm &p,
                            const NccScratch &s, int map_kind, vtg_found *out, cudaStream_t st);
