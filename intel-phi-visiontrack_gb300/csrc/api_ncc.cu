@@ -30,7 +30,8 @@ struct vtg_search {
 static size_t up256(size_t n) { return (n + 255) & ~(size_t)255; }
 
 struct SearchLayout {
-    size_t app, sum, S1, S2, map_v, map_x, map_y, top, ntop, err, half, band0, band1, found, conv, fac, cellw, bytes;
+    size_t app, sum, S1, S2, map_v, map_x, map_y, top, ntop, err, half, band0, band1, found, conv, fac, cellw, topblk,
+        arrive, bytes;
     size_t conv_elems, fac_elems;
     int tp, cells;
 };
@@ -83,6 +84,10 @@ static SearchLayout search_layout(int max_w, int max_h, int max_tw, int max_th)
     b += up256(sizeof(float) * L.fac_elems);
     L.cellw = b;
     b += up256(sizeof(unsigned long long) * (size_t)L.cells);
+    L.topblk = b;
+    b += up256(sizeof(unsigned long long) * NCC_TOP * (size_t)ncc_top_ctas(L.cells));
+    L.arrive = b; /* zeroed with the rest at creation */
+    b += 256;
     L.bytes = b;
     return L;
 }
@@ -157,6 +162,8 @@ extern "C" int vtg_search_create(vtg_ctx *ctx, int max_w, int max_h, int max_tw,
     s->sc.fac = (float *)(s->mem + L.fac);
     s->sc.fac_elems = L.fac_elems;
     s->sc.cellw = (unsigned long long *)(s->mem + L.cellw);
+    s->sc.topblk = (unsigned long long *)(s->mem + L.topblk);
+    s->sc.arrive = (unsigned *)(s->mem + L.arrive);
     s->sc.map_ev0 = s->sc.map_ev1 = nullptr;
     s->found = (vtg_found *)(s->mem + L.found);
     s->xy = nullptr;

@@ -264,57 +264,77 @@ __device__ __forceinline__ void top_insert(unsigned long long (&t)[NCC_TOP], uns
     }
 }
 
-/* The eight best cells: each thread its strided share, then the lists merge across the warp by xor partners (both
- * partners end with the best eight of the pair) and across the eight warps in the first warp. */
-#define NCC_TOP_THREADS 1024
-
-__global__ void __launch_bounds__(NCC_TOP_THREADS) ncc_top(const float *__restrict__ map_v, int cells,
-                                                           int *__restrict__ top, int *__restrict__ ntop)
+/* Two descending lists' best eight: max(a_k, b_(7 - k)) is their top eight as a bitonic sequence, which three
+ * compare-exchange layers sort. Across the warp by xor partners, so every lane ends with the warp's best eight. */
+__device__ __forceinline__ void top_warp_merge(unsigned long long (&t)[NCC_TOP])
 {
-    __shared__ unsigned long long s[NCC_TOP_THREADS / 32][NCC_TOP];
+#pragma unroll 1
+    for (int sh = 1; sh < 32; sh <<= 1) {
+        unsigned long long c[NCC_TOP];
+#pragma unroll
+        for (int k = 0; k < NCC_TOP; k++) {
+            const unsigned long long o = __shfl_xor_sync(VTG_FULL, t[NCC_TOP - 1 - k], sh);
+            c[k] = t[k] > o ? t[k] : o;
+        }
+#pragma unroll
+        for (int d = NCC_TOP / 2; d >= 1; d >>= 1)
+#pragma unroll
+            for (int k = 0; k < NCC_TOP; k++)
+                if ((k & d) == 0) {
+                    const unsigned long long hi = c[k] > c[k + d] ? c[k] : c[k + d];
+                    const unsigned long long lo = c[k] > c[k + d] ? c[k + d] : c[k];
+                    c[k] = hi;
+                    c[k + d] = lo;
+                }
+#pragma unroll
+        for (int k = 0; k < NCC_TOP; k++)
+            t[k] = c[k];
+    }
+}
+
+/* The eight best cells. Each CTA takes NCC_TOPB_PER x NCC_TOPB_THREADS cells (a thread keeps its best eight in
+ * registers; the lists merge across each warp, then across the CTA's warps) and writes its eight to blk. The CTA that
+ * arrives last merges every CTA's list into top / ntop and resets the counter, so the pass is one launch. WORDS: the
+ * cells come as the tensor-core map's 64-bit words, which this pass also decodes into map_v / map_x / map_y. */
+template <bool WORDS>
+__global__ void __launch_bounds__(NCC_TOPB_THREADS) ncc_top_ctas(NccPrm p, const unsigned long long *__restrict__ cellw,
+                                                                 float *__restrict__ map_v, int *__restrict__ map_x,
+                                                                 int *__restrict__ map_y, int cells,
+                                                                 unsigned long long *__restrict__ blk,
+                                                                 unsigned *__restrict__ arrive, int *__restrict__ top,
+                                                                 int *__restrict__ ntop)
+{
+    __shared__ unsigned long long s[NCC_TOPB_THREADS / 32][NCC_TOP];
+    __shared__ bool s_last;
     unsigned long long t[NCC_TOP];
 #pragma unroll
     for (int k = 0; k < NCC_TOP; k++)
         t[k] = 0ull;
-    /* eight loads in flight a thread, then their inserts */
-    for (int i0 = threadIdx.x; i0 < cells; i0 += 8 * blockDim.x) {
-        float v[8];
+    float v[NCC_TOPB_PER];
+    const int i0 = blockIdx.x * NCC_TOPB_THREADS * NCC_TOPB_PER + threadIdx.x;
 #pragma unroll
-        for (int u = 0; u < 8; u++) {
-            const int i = i0 + u * blockDim.x;
+    for (int u = 0; u < NCC_TOPB_PER; u++) {
+        const int i = i0 + u * NCC_TOPB_THREADS;
+        if (WORDS) {
+            const unsigned long long w = i < cells ? __ldg(cellw + i) : 0ull;
+            if (i < cells) {
+                int x, y;
+                ncc_cell_decode(p, i, w, v[u], x, y);
+                map_v[i] = v[u];
+                map_x[i] = x;
+                map_y[i] = y;
+            } else {
+                v[u] = -3.0f;
+            }
+        } else {
             v[u] = i < cells ? __ldg(map_v + i) : -3.0f;
         }
-#pragma unroll
-        for (int u = 0; u < 8; u++)
-            top_insert(t, top_key(v[u], i0 + u * blockDim.x));
     }
+#pragma unroll
+    for (int u = 0; u < NCC_TOPB_PER; u++)
+        top_insert(t, top_key(v[u], i0 + u * NCC_TOPB_THREADS));
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    /* two descending lists' best eight: max(a_k, b_(7 - k)) is their top eight as a bitonic sequence, which three
-     * compare-exchange layers sort; both xor partners compute the same list */
-    auto merge = [&](int width) {
-        for (int sh = 1; sh < width; sh <<= 1) {
-            unsigned long long c[NCC_TOP];
-#pragma unroll
-            for (int k = 0; k < NCC_TOP; k++) {
-                const unsigned long long o = __shfl_xor_sync(VTG_FULL, t[NCC_TOP - 1 - k], sh);
-                c[k] = t[k] > o ? t[k] : o;
-            }
-#pragma unroll
-            for (int d = NCC_TOP / 2; d >= 1; d >>= 1)
-#pragma unroll
-                for (int k = 0; k < NCC_TOP; k++)
-                    if ((k & d) == 0) {
-                        const unsigned long long hi = c[k] > c[k + d] ? c[k] : c[k + d];
-                        const unsigned long long lo = c[k] > c[k + d] ? c[k + d] : c[k];
-                        c[k] = hi;
-                        c[k + d] = lo;
-                    }
-#pragma unroll
-            for (int k = 0; k < NCC_TOP; k++)
-                t[k] = c[k];
-        }
-    };
-    merge(32);
+    top_warp_merge(t);
     if (lane == 0)
 #pragma unroll
         for (int k = 0; k < NCC_TOP; k++)
@@ -323,17 +343,36 @@ __global__ void __launch_bounds__(NCC_TOP_THREADS) ncc_top(const float *__restri
     if (warp == 0) {
 #pragma unroll
         for (int k = 0; k < NCC_TOP; k++)
-            t[k] = lane < NCC_TOP_THREADS / 32 ? s[lane][k] : 0ull;
-        merge(32);
-        if (lane == 0) {
-            int n = 0;
-            for (int k = 0; k < NCC_TOP; k++) {
-                if (t[k] == 0ull)
-                    break;
-                top[n++] = (int)(0xFFFFFFFFu - (unsigned)(t[k] & 0xFFFFFFFFull));
-            }
-            *ntop = n;
+            t[k] = lane < NCC_TOPB_THREADS / 32 ? s[lane][k] : 0ull;
+        top_warp_merge(t);
+        if (lane < NCC_TOP)
+            blk[(size_t)blockIdx.x * NCC_TOP + lane] = t[lane];
+        /* publish this CTA's list before counting it */
+        __threadfence();
+        if (lane == 0)
+            s_last = atomicAdd(arrive, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!s_last || warp != 0)
+        return;
+    __threadfence();
+#pragma unroll
+    for (int k = 0; k < NCC_TOP; k++)
+        t[k] = 0ull;
+    for (int b = lane; b < (int)gridDim.x; b += 32)
+#pragma unroll
+        for (int k = 0; k < NCC_TOP; k++)
+            top_insert(t, __ldcg(blk + (size_t)b * NCC_TOP + k));
+    top_warp_merge(t);
+    if (lane == 0) {
+        int n = 0;
+        for (int k = 0; k < NCC_TOP; k++) {
+            if (t[k] == 0ull)
+                break;
+            top[n++] = (int)(0xFFFFFFFFu - (unsigned)(t[k] & 0xFFFFFFFFull));
         }
+        *ntop = n;
+        *arrive = 0u;
     }
 }
 
@@ -411,38 +450,15 @@ __device__ __forceinline__ float parabola(float l, float c, float r)
     return fminf(fmaxf(o, -0.5f), 0.5f);
 }
 
-/* The half-pixel corners around every candidate, one CTA each: the window of +-around half pixels that
- * search_slot compares, and one ring past it, so the parabola's neighbours of any best are already scored. Scores go
- * to hs[candidate][(around + 1 + dy) ring + around + 1 + dx], ring = 2 around + 3. */
-template <typename T>
-__global__ void __launch_bounds__(256) ncc_half_all(const T *__restrict__ plane, int pitch, const float *__restrict__ app,
-                                                    NccPrm p, const int *__restrict__ map_x, const int *__restrict__ map_y,
-                                                    const int *__restrict__ top, const int *__restrict__ ntop,
-                                                    float *__restrict__ hs)
-{
-    const int around = p.step > 1 ? 2 * p.step - 1 : 1, ring = 2 * around + 3, r = around + 1;
-    const int c = blockIdx.x / (ring * ring), o = blockIdx.x - c * ring * ring;
-    if (c >= *ntop)
-        return;
-    const int cell = top[c];
-    const int hx = 2 * map_x[cell] + (o % ring) - r, hy = 2 * map_y[cell] + (o / ring) - r;
-    const float v = half_score_cta(plane, pitch, app, p, hx, hy);
-    if (threadIdx.x == 0)
-        hs[c * ring * ring + o] = v;
-}
-
 /* The best of each candidate's window (row-major first maximum, as search_slot's strict > over hy then hx: the
  * smallest index among equal scores), one warp a candidate; then, on one thread, the best over candidates in rank
  * order, the second peak half a template away, and the parabola through the four neighbours of the best (take_back's
- * peak_offset), all from hs. */
-__global__ void __launch_bounds__(NCC_TOP * 32) ncc_pick(NccPrm p, const int *__restrict__ map_x,
-                                                         const int *__restrict__ map_y, const int *__restrict__ top,
-                                                         const int *__restrict__ ntop, const float *__restrict__ hs,
-                                                         vtg_found *__restrict__ out)
+ * peak_offset), all from hs (read through L2: other CTAs wrote it). Run by a CTA of NCC_TOP warps. */
+__device__ void ncc_pick(const NccPrm &p, const int *__restrict__ map_x, const int *__restrict__ map_y,
+                         const int *__restrict__ top, int n, const float *__restrict__ hs, vtg_found *__restrict__ out)
 {
     __shared__ float s_score[NCC_TOP];
     __shared__ int s_hx[NCC_TOP], s_hy[NCC_TOP], s_at[NCC_TOP];
-    const int n = *ntop;
     const int around = p.step > 1 ? 2 * p.step - 1 : 1, side = 2 * around + 1, ring = side + 2;
     const int c = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (c < n) {
@@ -450,7 +466,7 @@ __global__ void __launch_bounds__(NCC_TOP * 32) ncc_pick(NccPrm p, const int *__
         float best = -2.0f;
         int bo = side * side; /* scan index of the best; side^2: none */
         for (int o = lane; o < side * side; o += 32) {
-            const float v = h[(o / side + 1) * ring + o % side + 1];
+            const float v = __ldcg(h + (o / side + 1) * ring + o % side + 1);
             if (v > best) {
                 best = v;
                 bo = o;
@@ -502,12 +518,49 @@ __global__ void __launch_bounds__(NCC_TOP * 32) ncc_pick(NccPrm p, const int *__
     if (win >= 0) {
         const float *h = hs + (size_t)win * ring * ring;
         const int k = s_at[win];
-        f.ox = parabola(h[k - 1], ncc, h[k + 1]);
-        f.oy = parabola(h[k - ring], ncc, h[k + ring]);
+        f.ox = parabola(__ldcg(h + k - 1), ncc, __ldcg(h + k + 1));
+        f.oy = parabola(__ldcg(h + k - ring), ncc, __ldcg(h + k + ring));
     }
     f.ntop = n;
     f.cells = p.ccols * p.crows;
     *out = f;
+}
+
+/* The half-pixel corners around every candidate, one CTA each: the window of +-around half pixels that
+ * search_slot compares, and one ring past it, so the parabola's neighbours of any best are already scored. Scores go
+ * to hs[candidate][(around + 1 + dy) ring + around + 1 + dx], ring = 2 around + 3. The CTA that arrives last (every
+ * CTA counts, those past the candidates too) makes the pick and resets the counter. */
+template <typename T>
+__global__ void __launch_bounds__(NCC_TOP * 32) ncc_half_all(const T *__restrict__ plane, int pitch,
+                                                             const float *__restrict__ app, NccPrm p,
+                                                             const int *__restrict__ map_x, const int *__restrict__ map_y,
+                                                             const int *__restrict__ top, const int *__restrict__ ntop,
+                                                             float *__restrict__ hs, unsigned *__restrict__ arrive,
+                                                             vtg_found *__restrict__ out)
+{
+    __shared__ bool s_last;
+    const int around = p.step > 1 ? 2 * p.step - 1 : 1, ring = 2 * around + 3, r = around + 1;
+    const int c = blockIdx.x / (ring * ring), o = blockIdx.x - c * ring * ring;
+    const int n = *ntop;
+    if (c < n) {
+        const int cell = top[c];
+        const int hx = 2 * map_x[cell] + (o % ring) - r, hy = 2 * map_y[cell] + (o / ring) - r;
+        const float v = half_score_cta(plane, pitch, app, p, hx, hy);
+        if (threadIdx.x == 0)
+            hs[c * ring * ring + o] = v;
+    }
+    if (threadIdx.x == 0) {
+        /* publish the score before counting it */
+        __threadfence();
+        s_last = atomicAdd(arrive, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!s_last)
+        return;
+    __threadfence();
+    ncc_pick(p, map_x, map_y, top, n, hs, out);
+    if (threadIdx.x == 0)
+        *arrive = 0u;
 }
 
 /* ---- corners one by one (tk_correlate): one warp per corner ---- */
@@ -573,11 +626,15 @@ static cudaError_t launch_all(const T *plane, int pitch, const float *app, const
         if (e != cudaSuccess)
             return e;
     }
-    ncc_top<<<1, NCC_TOP_THREADS, 0, st>>>(s.map_v, cells, s.top, s.ntop);
+    if (map_kind == VTG_NCC_F32)
+        ncc_top_ctas<false><<<ncc_top_ctas(cells), NCC_TOPB_THREADS, 0, st>>>(p, nullptr, s.map_v, s.map_x, s.map_y, cells,
+                                                                              s.topblk, s.arrive, s.top, s.ntop);
+    else
+        ncc_top_ctas<true><<<ncc_top_ctas(cells), NCC_TOPB_THREADS, 0, st>>>(p, s.cellw, s.map_v, s.map_x, s.map_y, cells,
+                                                                             s.topblk, s.arrive, s.top, s.ntop);
     const int around = p.step > 1 ? 2 * p.step - 1 : 1, ring = 2 * around + 3;
-    ncc_half_all<T><<<NCC_TOP * ring * ring, 256, 0, st>>>(plane, pitch, app, p, s.map_x, s.map_y, s.top, s.ntop,
-                                                            s.half);
-    ncc_pick<<<1, NCC_TOP * 32, 0, st>>>(p, s.map_x, s.map_y, s.top, s.ntop, s.half, out);
+    ncc_half_all<T><<<NCC_TOP * ring * ring, NCC_TOP * 32, 0, st>>>(plane, pitch, app, p, s.map_x, s.map_y, s.top,
+                                                                      s.ntop, s.half, s.arrive + 1, out);
     return cudaGetLastError();
 }
 

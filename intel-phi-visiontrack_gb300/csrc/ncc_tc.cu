@@ -579,30 +579,6 @@ __global__ void __launch_bounds__(TcShape<Q>::threads, 1) ncc_map_tc(NccPrm p, c
     }
 }
 
-/* The map from the cells' words: value and corner, or -2 and the cell's origin where no corner was scored. */
-__global__ void ncc_cells_out(NccPrm p, const unsigned long long *__restrict__ cellw, float *__restrict__ map_v,
-                              int *__restrict__ map_x, int *__restrict__ map_y)
-{
-    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
-    if (cell >= p.ccols * p.crows)
-        return;
-    const int cx0 = p.x0 + (cell % p.ccols) * NCC_CELL, cy0 = p.y0 + (cell / p.ccols) * NCC_CELL;
-    const unsigned long long w = cellw[cell];
-    const int per = NCC_CELL / p.step;
-    if (w == 0ull) {
-        map_v[cell] = -2.0f;
-        map_x[cell] = cx0;
-        map_y[cell] = cy0;
-        return;
-    }
-    unsigned u = (unsigned)(w >> 32);
-    u = (u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u;
-    const int key = (int)(0xFFFFFFFFu - (unsigned)(w & 0xFFFFFFFFull));
-    map_v[cell] = __uint_as_float(u);
-    map_x[cell] = cx0 + (key % per) * p.step;
-    map_y[cell] = cy0 + (key / per) * p.step;
-}
-
 cudaError_t vtg_launch_ncc_map_tc(const void *plane, int pitch, int elem_bytes, const NccPrm &p, const NccScratch &s,
                                   int kind, cudaStream_t st)
 {
@@ -656,6 +632,5 @@ cudaError_t vtg_launch_ncc_map_tc(const void *plane, int pitch, int elem_bytes, 
             MAP_TC(VTG_NCC_FP16, 16);
     }
 #undef MAP_TC
-    ncc_cells_out<<<(cells + 255) / 256, 256, 0, st>>>(p, s.cellw, s.map_v, s.map_x, s.map_y);
     return cudaGetLastError();
 }

@@ -21,8 +21,9 @@
  *   - that address is kept for the life of the process. cudaDeviceReset destroys the context the array lives in, and
  *     the array may sit elsewhere in the next one, so a process that resets a device must not call this entry point on
  *     that device afterwards.
- * Nothing in the array needs to start at zero: every call writes all the scratch it reads (both integral images in
- * full, every cell of its map, the candidate list and its count) before reading it. */
+ * Of the array only the two arrival counters (the last CTA of a pass does its final step) need to start at zero: the
+ * first call on a device zeroes them, and every search leaves them at zero. Every call writes all the other scratch it
+ * reads (both integral images in full, every cell of its map, the candidate list and its count) before reading it. */
 #include <mutex>
 
 #include "vtg_ctx.h"
@@ -30,16 +31,19 @@
 
 #define VTG_NOALLOC_MAX_CELLS 2048
 
-/* The scratch: two integral images of VTG_NOALLOC_MAX_PIXELS int64 each, then the map and the candidates. */
+/* The scratch: two integral images of VTG_NOALLOC_MAX_PIXELS int64 each, then the map and the candidates, the top-8
+ * pass's per-CTA lists and the two arrival counters. */
 static __device__ __align__(256) unsigned char g_noalloc_scratch[VTG_NOALLOC_SCRATCH_BYTES];
 
 #define VTG_NOALLOC_MAX_STEP 4
 #define VTG_NOALLOC_HALF (NCC_TOP * (4 * VTG_NOALLOC_MAX_STEP + 1) * (4 * VTG_NOALLOC_MAX_STEP + 1))
 
-static_assert(2 * sizeof(long long) * (size_t)VTG_NOALLOC_MAX_PIXELS +
-                      (size_t)VTG_NOALLOC_MAX_CELLS * (sizeof(float) + 2 * sizeof(int)) + 256 +
-                      sizeof(float) * VTG_NOALLOC_HALF <=
-                  VTG_NOALLOC_SCRATCH_BYTES,
+#define VTG_NOALLOC_TOPB ((VTG_NOALLOC_MAX_CELLS + NCC_TOPB_THREADS * NCC_TOPB_PER - 1) / (NCC_TOPB_THREADS * NCC_TOPB_PER))
+#define VTG_NOALLOC_REST (2 * sizeof(long long) * (size_t)VTG_NOALLOC_MAX_PIXELS)
+#define VTG_NOALLOC_HALF_AT (VTG_NOALLOC_REST + sizeof(float) * VTG_NOALLOC_MAX_CELLS + 2 * sizeof(int) * VTG_NOALLOC_MAX_CELLS + 256)
+#define VTG_NOALLOC_TOPB_AT (((VTG_NOALLOC_HALF_AT + sizeof(float) * VTG_NOALLOC_HALF) + 255) & ~(size_t)255)
+#define VTG_NOALLOC_ARRIVE_AT (VTG_NOALLOC_TOPB_AT + sizeof(unsigned long long) * NCC_TOP * VTG_NOALLOC_TOPB)
+static_assert(VTG_NOALLOC_ARRIVE_AT + 2 * sizeof(unsigned) <= VTG_NOALLOC_SCRATCH_BYTES,
               "the scratch array holds the largest search it accepts");
 
 #define VTG_NOALLOC_DEVICES 64
@@ -47,8 +51,9 @@ static_assert(2 * sizeof(long long) * (size_t)VTG_NOALLOC_MAX_PIXELS +
 static std::mutex g_noalloc_mu;
 static unsigned char *g_noalloc_ptr[VTG_NOALLOC_DEVICES];
 
-/* The array's device address on the current device, looked up once per device. */
-static cudaError_t noalloc_scratch(unsigned char **out)
+/* The array's device address on the current device, looked up once per device; that first lookup also zeroes the
+ * arrival counters, on the call's stream, ahead of the search it launches there. */
+static cudaError_t noalloc_scratch(unsigned char **out, cudaStream_t st)
 {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -60,6 +65,9 @@ static cudaError_t noalloc_scratch(unsigned char **out)
     if (!g_noalloc_ptr[dev]) {
         void *p = nullptr;
         e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        /* the arrival counters start at zero; every search leaves them there */
+        if (e == cudaSuccess)
+            e = cudaMemsetAsync((unsigned char *)p + VTG_NOALLOC_ARRIVE_AT, 0, 2 * sizeof(unsigned), st);
         if (e != cudaSuccess)
             return e;
         g_noalloc_ptr[dev] = (unsigned char *)p;
@@ -111,7 +119,7 @@ extern "C" int vtg_search_run_noalloc(const void *plane, int w, int h, int pitch
     if (p.ccols * p.crows > VTG_NOALLOC_MAX_CELLS)
         return VTG_EINVAL;
     unsigned char *base = nullptr;
-    cudaError_t e = noalloc_scratch(&base);
+    cudaError_t e = noalloc_scratch(&base, st);
     if (e != cudaSuccess) {
         vtg_set_cuda_error(e);
         return VTG_ECUDA;
@@ -121,7 +129,7 @@ extern "C" int vtg_search_run_noalloc(const void *plane, int w, int h, int pitch
     s.tp = w + 1;
     s.S1 = (long long *)base;
     s.S2 = (long long *)(base + table);
-    unsigned char *rest = base + 2 * sizeof(long long) * (size_t)VTG_NOALLOC_MAX_PIXELS;
+    unsigned char *rest = base + VTG_NOALLOC_REST;
     s.map_v = (float *)rest;
     s.map_x = (int *)(rest + sizeof(float) * VTG_NOALLOC_MAX_CELLS);
     s.map_y = s.map_x + VTG_NOALLOC_MAX_CELLS;
@@ -130,7 +138,9 @@ extern "C" int vtg_search_run_noalloc(const void *plane, int w, int h, int pitch
     s.band = nullptr;
     s.band_rows = s.krow = 0;
     s.err = s.ntop + 1;
-    s.half = (float *)(rest + sizeof(float) * VTG_NOALLOC_MAX_CELLS + 2 * sizeof(int) * VTG_NOALLOC_MAX_CELLS + 256);
+    s.half = (float *)(base + VTG_NOALLOC_HALF_AT);
+    s.topblk = (unsigned long long *)(base + VTG_NOALLOC_TOPB_AT);
+    s.arrive = (unsigned *)(base + VTG_NOALLOC_ARRIVE_AT);
     s.conv = nullptr; /* the F32 map needs none of the tensor-core map's scratch */
     s.conv_elems = 0;
     s.fac = nullptr;

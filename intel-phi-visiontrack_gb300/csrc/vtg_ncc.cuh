@@ -52,9 +52,38 @@ struct NccScratch {
     float *fac;
     size_t fac_elems;
     unsigned long long *cellw;
+    /* the top-8 pass's per-CTA lists (NCC_TOP keys a CTA, ncc_top_ctas(cells) CTAs) and two arrival counters, one for
+     * it and one for the half-pixel pass: zero between searches, each reset by the CTA that arrives last */
+    unsigned long long *topblk;
+    unsigned *arrive;
     /* vtg_search_profile: events recorded just before and just after the map kernel (NULL: none) */
     cudaEvent_t map_ev0, map_ev1;
 };
+
+/* The top-8 pass: NCC_TOPB_THREADS threads a CTA, NCC_TOPB_PER cells a thread. */
+#define NCC_TOPB_THREADS 256
+#define NCC_TOPB_PER 4
+static inline int ncc_top_ctas(int cells) { return (cells + NCC_TOPB_THREADS * NCC_TOPB_PER - 1) / (NCC_TOPB_THREADS * NCC_TOPB_PER); }
+
+/* A cell of the tensor-core map from its 64-bit word (ordered score, inverted scan index): value and corner, or -2 and
+ * the cell's origin where no corner was scored (the F32 map's convention). */
+__device__ __forceinline__ void ncc_cell_decode(const NccPrm &p, int cell, unsigned long long w, float &v, int &x, int &y)
+{
+    const int cx0 = p.x0 + (cell % p.ccols) * NCC_CELL, cy0 = p.y0 + (cell / p.ccols) * NCC_CELL;
+    const int per = NCC_CELL / p.step;
+    if (w == 0ull) {
+        v = -2.0f;
+        x = cx0;
+        y = cy0;
+        return;
+    }
+    unsigned u = (unsigned)(w >> 32);
+    u = (u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u;
+    const int key = (int)(0xFFFFFFFFu - (unsigned)(w & 0xFFFFFFFFull));
+    v = __uint_as_float(u);
+    x = cx0 + (key % per) * p.step;
+    y = cy0 + (key / per) * p.step;
+}
 
 /* Elements of the tensor-core map's scratch for planes up to max_w x max_h and templates up to max_tw x max_th. */
 size_t vtg_ncc_conv_elems(int max_w, int max_h, int max_th);
