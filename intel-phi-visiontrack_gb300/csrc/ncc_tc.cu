@@ -164,7 +164,9 @@ __global__ void ncc_conv(const uint8_t *__restrict__ plane, int pitch, int w, in
  *   - a corner's window sums are then P(x + T_w) - P(x), consecutive lanes on consecutive corners.
  * Bytes keep every window sum in 32 bits (sum J^2 <= 255^2 x 128^2 < 2^31). A row's prefix of J^2 may pass 2^32, so
  * the prefixes are unsigned and wrap: their differences are still exact. n var is formed in 64 bits. */
-#define BP_TY 8
+#ifndef BP_TY
+#define BP_TY 16 /* corner rows a CTA: a multiple of the 8 warps, each warp writing rows warp, warp + 8, .. */
+#endif
 /* corners a CTA across: the most, a multiple of 32, whose columns (+ T_w - 1) fit the CTA's 256 threads */
 static inline int bp_tx(int tw) { return ((257 - tw) / 32) * 32; }
 __global__ void __launch_bounds__(256) ncc_box_prep(const uint8_t *__restrict__ plane, int pitch, NccPrm p, int fw,
@@ -243,14 +245,16 @@ __global__ void __launch_bounds__(256) ncc_box_prep(const uint8_t *__restrict__ 
         }
     }
     __syncthreads();
-    for (int q = c; q < BP_TY * btx; q += blockDim.x) {
-        const int r = q / btx, x = q - r * btx;
-        if (r >= ny || x >= nx)
-            continue;
-        const long long s1 = (long long)(P1[r][x + p.tw] - P1[r][x]), s2 = (long long)(P2[r][x + p.tw] - P2[r][x]);
-        const long long nvar = (long long)p.n * s2 - s1 * s1;
-        /* 1 / sqrt(norm var) = sqrt(n / norm) / sqrt(n var) */
-        fac[(size_t)(ty0 + r) * fpitch + (tx0 + x)] = (nvar <= p.nthr || p.norm <= 0.0f) ? 0.0f : p.rnorm * rsqrtf((float)nvar);
+    /* warp w writes corner rows w, w + 8, ..; its lanes consecutive corners (btx is a multiple of 32) */
+    for (int r = warp; r < ny; r += 8) {
+        float *frow = fac + (size_t)(ty0 + r) * fpitch + tx0;
+#pragma unroll 1
+        for (int x = lane; x < nx; x += 32) {
+            const long long s1 = (long long)(P1[r][x + p.tw] - P1[r][x]), s2 = (long long)(P2[r][x + p.tw] - P2[r][x]);
+            const long long nvar = (long long)p.n * s2 - s1 * s1;
+            /* 1 / sqrt(norm var) = sqrt(n / norm) / sqrt(n var) */
+            frow[x] = (nvar <= p.nthr || p.norm <= 0.0f) ? 0.0f : p.rnorm * rsqrtf((float)nvar);
+        }
     }
 }
 
@@ -383,7 +387,7 @@ __global__ void __launch_bounds__(TcShape<Q>::threads, 1) ncc_map_tc(NccPrm p, c
     extern __shared__ __align__(1024) uint8_t smem[];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
-    const int X0 = p.x0 + tx * TC_XS, Y0 = p.y0 + ty * Q;
+    const int Y0 = p.y0 + ty * Q;
     const int nk = Q + p.th - 1;
     const int kchunks = krow / 16;
     uint8_t *ctl = smem + TC_STAGES * stage_bytes;
