@@ -13,14 +13,14 @@
  *
  * Pipeline (all on one stream, no host round trip):
  *   integral_rows / integral_cols  int64 tables of J and J^2 ((h + 1) x (w + 1)), exact (for the F32 map; the
- *                                 tensor-core map's ncc_box_prep sums the window bytes directly)
+ *                                 tensor-core map's preparation (ncc_prep) sums the window bytes directly)
  *   ncc_map_f32 (or the tensor-core map in ncc_tc.cu)  per cell: best score and its corner
- *   ncc_top                       the eight best cells, value descending then cell index ascending (the reference's
- *                                 insertion order)
- *   ncc_half_all / ncc_pick       each candidate in half pixels within +-(2 step - 1) (or +-1) and one ring past it,
- *                                 one CTA per corner; then the best, the second peak clear of it by half a template,
- *                                 and the parabola offsets from the ring; F32 products with exact integer
- *                                 (quarter-pixel) window sums. */
+ *   ncc_top_ctas                  the eight best cells, value descending then cell index ascending (the reference's
+ *                                 insertion order): a list a CTA, merged by the CTA that finishes last
+ *   ncc_half_all (+ ncc_pick)     each candidate in half pixels within +-(2 step - 1) (or +-1) and one ring past it,
+ *                                 one CTA per corner; then, in the CTA that finishes last, the best, the second peak
+ *                                 clear of it by half a template, and the parabola offsets from the ring; F32 products
+ *                                 with exact integer (quarter-pixel) window sums. */
 #include <float.h>
 
 #include <type_traits>

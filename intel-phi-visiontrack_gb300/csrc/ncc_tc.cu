@@ -12,7 +12,7 @@
  *   A needs no im2col. Consecutive rows of A_r start 8 elements (16 bytes) apart in the image row, so a K-major,
  *   no-swizzle descriptor with 16-byte core-matrix rows, a 16-byte leading (K) offset and a 128-byte stride (M) offset
  *   reads A_r straight from the row: address(m, k) = row + 2 (8 m + k). The picture is converted to 16 bits once per
- *   search (ncc_conv), shifted so that every tile's row segment starts on a 16-byte boundary.
+ *   search (ncc_prep), shifted so that every tile's row segment starts on a 16-byte boundary.
  *   B_r depends only on r - Y0: the band (Q + T_h - 1 blocks of 8 Q x K_row) is built once per template in the canonical
  *   core-matrix layout.
  * Pipeline: three threads drive it. Six shared-memory stages, each an image-row segment and a band block, arrive by
@@ -23,7 +23,7 @@
  * word.
  * Epilogue: each of the 128 threads owns one accumulator row (8 x-corners by Q y-corners) of each issuer and sums
  * them. Per corner: st = acc - J(x, y) sum t' (the reference's st is relative to the corner's first pixel), times the
- * corner's factor 1 / sqrt(norm var) from ncc_box_prep (0 for a near-blank window: the exact integer rule), the best
+ * corner's factor 1 / sqrt(norm var) from ncc_prep (0 for a near-blank window: the exact integer rule), the best
  * per 16 x 16 cell by value then scan order, merged across tiles by a 64-bit atomicMax on (ordered score, inverted scan
  * index). */
 #include <cuda_bf16.h>
@@ -129,14 +129,14 @@ cudaError_t vtg_launch_ncc_band(const float *app, int tw, int th, int kind, uint
 
 /* ---- per-search preparation ---- */
 
-/* conv[r][i] = 16-bit J[r][x0 + i] (zero past the picture), for rows 0 .. rows - 1 and columns 0 .. cpitch - 1. */
+/* conv[r][i] = 16-bit J[r][x0 + i] (zero past the picture), for rows 0 .. rows - 1 and columns 0 .. cpitch - 1: the
+ * CTA (bx, by) of 256 threads converts row by, eight elements a thread and one 16-byte store (cpitch is a multiple of 8
+ * and rows start 16-byte aligned: 2 cpitch = 2048 tiles_x + 288 bytes). */
 template <int KIND>
-__global__ void ncc_conv(const uint8_t *__restrict__ plane, int pitch, int w, int h, int x0, int rows, int cpitch,
-                         uint16_t *__restrict__ conv)
+__device__ __forceinline__ void conv_cta(const uint8_t *__restrict__ plane, int pitch, int w, int h, int x0, int rows,
+                                         int cpitch, uint16_t *__restrict__ conv, int bx, int by)
 {
-    /* row blockIdx.y, eight elements a thread and one 16-byte store (cpitch is a multiple of 8 and rows start 16-byte
-     * aligned: 2 cpitch = 2048 tiles_x + 288 bytes) */
-    const int r = (int)blockIdx.y, i0 = 8 * (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int r = by, i0 = 8 * (bx * 256 + (int)threadIdx.x);
     if (r >= rows || i0 >= cpitch)
         return;
     uint32_t o[4];
@@ -169,13 +169,13 @@ __global__ void ncc_conv(const uint8_t *__restrict__ plane, int pitch, int w, in
 #endif
 /* corners a CTA across: the most, a multiple of 32, whose columns (+ T_w - 1) fit the CTA's 256 threads */
 static inline int bp_tx(int tw) { return ((257 - tw) / 32) * 32; }
-__global__ void __launch_bounds__(256) ncc_box_prep(const uint8_t *__restrict__ plane, int pitch, NccPrm p, int fw,
-                                                    int fpitch, int btx, float *__restrict__ fac)
+__device__ void box_cta(const uint8_t *__restrict__ plane, int pitch, const NccPrm &p, int fw, int fpitch, int btx,
+                        float *__restrict__ fac, int bx, int by)
 {
     __shared__ unsigned P1[BP_TY][257], P2[BP_TY][257]; /* P[r][c]: columns 0 .. c - 1 of row r */
     __shared__ unsigned t1[8][BP_TY], t2[8][BP_TY];     /* each warp's column totals, then the earlier warps' */
     const int fh = p.y1 - p.y0 + 1;
-    const int tx0 = blockIdx.x * btx, ty0 = blockIdx.y * BP_TY;
+    const int tx0 = bx * btx, ty0 = by * BP_TY;
     const int nx = min(btx, fw - tx0), ny = min(BP_TY, fh - ty0);
     const int c = threadIdx.x, lane = c & 31, warp = c >> 5;
     const int ncol = nx + p.tw - 1; /* <= 256 */
@@ -256,6 +256,26 @@ __global__ void __launch_bounds__(256) ncc_box_prep(const uint8_t *__restrict__ 
             frow[x] = (nvar <= p.nthr || p.norm <= 0.0f) ? 0.0f : p.rnorm * rsqrtf((float)nvar);
         }
     }
+}
+
+/* The map's preparation in one launch of 256-thread CTAs: the first nbox sum the windows (the longer work, so they
+ * start first), the rest convert the picture, and those also zero the cells' words the map merges into. The two jobs
+ * are independent and run side by side. */
+template <int KIND>
+__global__ void __launch_bounds__(256) ncc_prep(const uint8_t *__restrict__ plane, int pitch, NccPrm p, int fw, int fpitch,
+                                                int btx, int bgx, int nbox, float *__restrict__ fac, int rows, int cpitch,
+                                                int cgx, uint16_t *__restrict__ conv, unsigned long long *__restrict__ cellw,
+                                                int cells)
+{
+    const int b = (int)blockIdx.x;
+    if (b < nbox) {
+        box_cta(plane, pitch, p, fw, fpitch, btx, fac, b % bgx, b / bgx);
+        return;
+    }
+    const int k = b - nbox, g = k * 256 + (int)threadIdx.x;
+    if (g < cells)
+        cellw[g] = 0ull;
+    conv_cta<KIND>(plane, pitch, p.w, p.h, p.x0, rows, cpitch, conv, k % cgx, k / cgx);
 }
 
 /* ---- PTX helpers ---- */
@@ -600,17 +620,17 @@ cudaError_t vtg_launch_ncc_map_tc(const void *plane, int pitch, int elem_bytes, 
         NCC_CELL % p.step)
         return cudaErrorInvalidValue;
     const int cells = p.ccols * p.crows;
-    cudaError_t e = cudaMemsetAsync(s.cellw, 0, sizeof(unsigned long long) * (size_t)cells, st);
-    if (e != cudaSuccess)
-        return e;
-    const dim3 cgrid((cpitch / 8 + 255) / 256, rows);
+    cudaError_t e = cudaSuccess;
+    const int btx = bp_tx(p.tw), bgx = (fw + btx - 1) / btx, nbox = bgx * ((fh + BP_TY - 1) / BP_TY);
+    const int cgx = (cpitch / 8 + 255) / 256, nconv = cgx * rows;
+    if ((long long)nconv * 256 < cells) /* the converting CTAs zero the cells' words */
+        return cudaErrorInvalidValue;
     if (kind == VTG_NCC_BF16)
-        ncc_conv<VTG_NCC_BF16><<<cgrid, 256, 0, st>>>((const uint8_t *)plane, pitch, p.w, p.h, p.x0, rows, cpitch, s.conv);
+        ncc_prep<VTG_NCC_BF16><<<nbox + nconv, 256, 0, st>>>((const uint8_t *)plane, pitch, p, fw, fpitch, btx, bgx, nbox,
+                                                             s.fac, rows, cpitch, cgx, s.conv, s.cellw, cells);
     else
-        ncc_conv<VTG_NCC_FP16><<<cgrid, 256, 0, st>>>((const uint8_t *)plane, pitch, p.w, p.h, p.x0, rows, cpitch, s.conv);
-    const int btx = bp_tx(p.tw);
-    ncc_box_prep<<<dim3((fw + btx - 1) / btx, (fh + BP_TY - 1) / BP_TY), 256, 0, st>>>((const uint8_t *)plane, pitch, p,
-                                                                                      fw, fpitch, btx, s.fac);
+        ncc_prep<VTG_NCC_FP16><<<nbox + nconv, 256, 0, st>>>((const uint8_t *)plane, pitch, p, fw, fpitch, btx, bgx, nbox,
+                                                             s.fac, rows, cpitch, cgx, s.conv, s.cellw, cells);
 #define MAP_TC(K, QQ)                                                                                                  \
     do {                                                                                                               \
         e = cudaFuncSetAttribute(ncc_map_tc<K, QQ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm.total);       \
