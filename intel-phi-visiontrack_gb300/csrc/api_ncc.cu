@@ -33,7 +33,7 @@ struct SearchLayout {
     size_t app, sum, S1, S2, map_v, map_x, map_y, top, ntop, err, half, band0, band1, found, conv, fac, cellw, topblk,
         arrive, bytes;
     size_t conv_elems, fac_elems;
-    int tp, cells;
+    int tp, cells, lists;
 };
 
 static bool search_dims_ok(int max_w, int max_h, int max_tw, int max_th)
@@ -85,7 +85,8 @@ static SearchLayout search_layout(int max_w, int max_h, int max_tw, int max_th)
     L.cellw = b;
     b += up256(sizeof(unsigned long long) * (size_t)L.cells);
     L.topblk = b;
-    b += up256(sizeof(unsigned long long) * NCC_TOP * (size_t)ncc_top_ctas(L.cells));
+    L.lists = ncc_top_ctas(L.cells);
+    b += up256(sizeof(unsigned long long) * NCC_TOP * (size_t)L.lists);
     L.arrive = b; /* zeroed with the rest at creation */
     b += 256;
     L.bytes = b;
@@ -163,6 +164,7 @@ extern "C" int vtg_search_create(vtg_ctx *ctx, int max_w, int max_h, int max_tw,
     s->sc.fac_elems = L.fac_elems;
     s->sc.cellw = (unsigned long long *)(s->mem + L.cellw);
     s->sc.topblk = (unsigned long long *)(s->mem + L.topblk);
+    s->sc.topblk_lists = L.lists;
     s->sc.arrive = (unsigned *)(s->mem + L.arrive);
     s->sc.map_ev0 = s->sc.map_ev1 = nullptr;
     s->found = (vtg_found *)(s->mem + L.found);

@@ -241,57 +241,6 @@ __global__ void __launch_bounds__(256) ncc_map_f32(const T *__restrict__ plane, 
 
 /* ---- the eight best cells ---- */
 
-__device__ __forceinline__ unsigned long long top_key(float v, int i)
-{
-    if (!(v > -2.0f))
-        return 0ull;
-    unsigned u = __float_as_uint(v);
-    u = (u & 0x80000000u) ? ~u : (u | 0x80000000u); /* ascending float order as unsigned */
-    return ((unsigned long long)u << 32) | (unsigned long long)(0xFFFFFFFFu - (unsigned)i);
-}
-
-/* k into the descending list t, keeping its NCC_TOP largest: one compare-exchange a place, unrolled, so t stays in
- * registers. Keys are distinct (the cell index is in their low bits). */
-__device__ __forceinline__ void top_insert(unsigned long long (&t)[NCC_TOP], unsigned long long k)
-{
-    if (k <= t[NCC_TOP - 1])
-        return;
-#pragma unroll
-    for (int j = 0; j < NCC_TOP; j++) {
-        const unsigned long long hi = t[j] > k ? t[j] : k;
-        k = t[j] > k ? k : t[j];
-        t[j] = hi;
-    }
-}
-
-/* Two descending lists' best eight: max(a_k, b_(7 - k)) is their top eight as a bitonic sequence, which three
- * compare-exchange layers sort. Across the warp by xor partners, so every lane ends with the warp's best eight. */
-__device__ __forceinline__ void top_warp_merge(unsigned long long (&t)[NCC_TOP])
-{
-#pragma unroll 1
-    for (int sh = 1; sh < 32; sh <<= 1) {
-        unsigned long long c[NCC_TOP];
-#pragma unroll
-        for (int k = 0; k < NCC_TOP; k++) {
-            const unsigned long long o = __shfl_xor_sync(VTG_FULL, t[NCC_TOP - 1 - k], sh);
-            c[k] = t[k] > o ? t[k] : o;
-        }
-#pragma unroll
-        for (int d = NCC_TOP / 2; d >= 1; d >>= 1)
-#pragma unroll
-            for (int k = 0; k < NCC_TOP; k++)
-                if ((k & d) == 0) {
-                    const unsigned long long hi = c[k] > c[k + d] ? c[k] : c[k + d];
-                    const unsigned long long lo = c[k] > c[k + d] ? c[k + d] : c[k];
-                    c[k] = hi;
-                    c[k + d] = lo;
-                }
-#pragma unroll
-        for (int k = 0; k < NCC_TOP; k++)
-            t[k] = c[k];
-    }
-}
-
 /* The eight best cells. Each CTA takes NCC_TOPB_PER x NCC_TOPB_THREADS cells (a thread keeps its best eight in
  * registers; the lists merge across each warp, then across the CTA's warps) and writes its eight to blk. The CTA that
  * arrives last merges every CTA's list into top / ntop and resets the counter, so the pass is one launch. WORDS: the
@@ -345,35 +294,34 @@ __global__ void __launch_bounds__(NCC_TOPB_THREADS) ncc_top_ctas(NccPrm p, const
         for (int k = 0; k < NCC_TOP; k++)
             t[k] = lane < NCC_TOPB_THREADS / 32 ? s[lane][k] : 0ull;
         top_warp_merge(t);
-        if (lane < NCC_TOP)
-            blk[(size_t)blockIdx.x * NCC_TOP + lane] = t[lane];
-        /* publish this CTA's list before counting it */
-        __threadfence();
-        if (lane == 0)
+        /* every lane holds the list: lane 0 publishes it, then counts it */
+        if (lane == 0) {
+#pragma unroll
+            for (int k = 0; k < NCC_TOP; k++)
+                blk[(size_t)blockIdx.x * NCC_TOP + k] = t[k];
+            __threadfence();
             s_last = atomicAdd(arrive, 1u) == gridDim.x - 1;
+        }
     }
     __syncthreads();
     if (!s_last || warp != 0)
         return;
     __threadfence();
-#pragma unroll
-    for (int k = 0; k < NCC_TOP; k++)
-        t[k] = 0ull;
-    for (int b = lane; b < (int)gridDim.x; b += 32)
-#pragma unroll
-        for (int k = 0; k < NCC_TOP; k++)
-            top_insert(t, __ldcg(blk + (size_t)b * NCC_TOP + k));
-    top_warp_merge(t);
-    if (lane == 0) {
-        int n = 0;
-        for (int k = 0; k < NCC_TOP; k++) {
-            if (t[k] == 0ull)
-                break;
-            top[n++] = (int)(0xFFFFFFFFu - (unsigned)(t[k] & 0xFFFFFFFFull));
-        }
-        *ntop = n;
-        *arrive = 0u;
-    }
+    ncc_top_final(blk, gridDim.x, arrive, top, ntop);
+}
+
+cudaError_t vtg_launch_ncc_top(const NccPrm &p, const NccScratch &s, bool words, cudaStream_t st)
+{
+    const int cells = p.ccols * p.crows;
+    if (ncc_top_ctas(cells) > s.topblk_lists) /* each CTA leaves its best eight */
+        return cudaErrorInvalidValue;
+    if (words)
+        ncc_top_ctas<true><<<ncc_top_ctas(cells), NCC_TOPB_THREADS, 0, st>>>(p, s.cellw, s.map_v, s.map_x, s.map_y, cells,
+                                                                             s.topblk, s.arrive, s.top, s.ntop);
+    else
+        ncc_top_ctas<false><<<ncc_top_ctas(cells), NCC_TOPB_THREADS, 0, st>>>(p, nullptr, s.map_v, s.map_x, s.map_y,
+                                                                              cells, s.topblk, s.arrive, s.top, s.ntop);
+    return cudaGetLastError();
 }
 
 /* ---- half-pixel refinement (search_half, search_slot's second half, take_back's parabola) ---- */
@@ -397,10 +345,17 @@ __device__ float half_score_cta(const T *__restrict__ plane, int pitch, const fl
     const float first = (float)__ldg(plane + (size_t)y * pitch + x);
     float st = 0.0f;
     Q a1 = 0, a2 = 0; /* in quarters */
+    /* the columns of a row as four unrolled, predicated steps (T_w <= 128) and two rows at a time, so a thread's loads
+     * are in flight together; the order of its sums is still rows, then columns, ascending */
+#pragma unroll 2
     for (int i = warp; i < p.th; i += 8) {
         const T *r0 = plane + (size_t)(y + i) * pitch + x, *r1 = r0 + pitch;
         const float *ar = app + (size_t)i * p.tw;
-        for (int j = lane; j < p.tw; j += 32) {
+#pragma unroll
+        for (int u = 0; u < VTG_NCC_MAX_T / 32; u++) {
+            const int j = lane + 32 * u;
+            if (j >= p.tw)
+                break;
             const Q a = (Q)__ldg(r0 + j), b = ox ? (Q)__ldg(r0 + j + 1) : a;
             Q q = 2 * (a + b);
             if (oy) {
@@ -626,12 +581,9 @@ static cudaError_t launch_all(const T *plane, int pitch, const float *app, const
         if (e != cudaSuccess)
             return e;
     }
-    if (map_kind == VTG_NCC_F32)
-        ncc_top_ctas<false><<<ncc_top_ctas(cells), NCC_TOPB_THREADS, 0, st>>>(p, nullptr, s.map_v, s.map_x, s.map_y, cells,
-                                                                              s.topblk, s.arrive, s.top, s.ntop);
-    else
-        ncc_top_ctas<true><<<ncc_top_ctas(cells), NCC_TOPB_THREADS, 0, st>>>(p, s.cellw, s.map_v, s.map_x, s.map_y, cells,
-                                                                             s.topblk, s.arrive, s.top, s.ntop);
+    /* the tensor-core map's launcher ends with the top-8 pass over its cell words (ncc_tc.cu) */
+    if (map_kind == VTG_NCC_F32 && (e = vtg_launch_ncc_top(p, s, false, st)) != cudaSuccess)
+        return e;
     const int around = p.step > 1 ? 2 * p.step - 1 : 1, ring = 2 * around + 3;
     ncc_half_all<T><<<NCC_TOP * ring * ring, NCC_TOP * 32, 0, st>>>(plane, pitch, app, p, s.map_x, s.map_y, s.top,
                                                                       s.ntop, s.half, s.arrive + 1, out);

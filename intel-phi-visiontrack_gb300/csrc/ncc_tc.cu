@@ -656,5 +656,8 @@ cudaError_t vtg_launch_ncc_map_tc(const void *plane, int pitch, int elem_bytes, 
             MAP_TC(VTG_NCC_FP16, 16);
     }
 #undef MAP_TC
-    return cudaGetLastError();
+    if ((e = cudaGetLastError()) != cudaSuccess)
+        return e;
+    /* the cells from their words, and their best eight */
+    return vtg_launch_ncc_top(p, s, true, st);
 }

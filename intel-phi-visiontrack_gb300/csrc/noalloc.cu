@@ -140,6 +140,7 @@ extern "C" int vtg_search_run_noalloc(const void *plane, int w, int h, int pitch
     s.err = s.ntop + 1;
     s.half = (float *)(base + VTG_NOALLOC_HALF_AT);
     s.topblk = (unsigned long long *)(base + VTG_NOALLOC_TOPB_AT);
+    s.topblk_lists = VTG_NOALLOC_TOPB;
     s.arrive = (unsigned *)(base + VTG_NOALLOC_ARRIVE_AT);
     s.conv = nullptr; /* the F32 map needs none of the tensor-core map's scratch */
     s.conv_elems = 0;

@@ -55,12 +55,13 @@ struct NccScratch {
     /* the top-8 pass's per-CTA lists (NCC_TOP keys a CTA, ncc_top_ctas(cells) CTAs) and two arrival counters, one for
      * it and one for the half-pixel pass: zero between searches, each reset by the CTA that arrives last */
     unsigned long long *topblk;
+    int topblk_lists; /* lists topblk holds */
     unsigned *arrive;
     /* vtg_search_profile: events recorded just before and just after the map kernel (NULL: none) */
     cudaEvent_t map_ev0, map_ev1;
 };
 
-/* The top-8 pass: NCC_TOPB_THREADS threads a CTA, NCC_TOPB_PER cells a thread. */
+/* The top-8 pass: NCC_TOPB_THREADS threads a CTA, NCC_TOPB_PER cells a thread; it needs ncc_top_ctas(cells) lists. */
 #define NCC_TOPB_THREADS 256
 #define NCC_TOPB_PER 4
 static inline int ncc_top_ctas(int cells) { return (cells + NCC_TOPB_THREADS * NCC_TOPB_PER - 1) / (NCC_TOPB_THREADS * NCC_TOPB_PER); }
@@ -85,10 +86,93 @@ __device__ __forceinline__ void ncc_cell_decode(const NccPrm &p, int cell, unsig
     y = cy0 + (key / per) * p.step;
 }
 
+/* ---- the eight best cells: keys, a register list, a warp's merge ---- */
+
+/* A cell's key: its value in ascending float order as unsigned, then the inverted cell index (the earlier cell first
+ * among equal values); 0 for no value (-2). */
+__device__ __forceinline__ unsigned long long top_key(float v, int i)
+{
+    if (!(v > -2.0f))
+        return 0ull;
+    unsigned u = __float_as_uint(v);
+    u = (u & 0x80000000u) ? ~u : (u | 0x80000000u); /* ascending float order as unsigned */
+    return ((unsigned long long)u << 32) | (unsigned long long)(0xFFFFFFFFu - (unsigned)i);
+}
+
+/* k into the descending list t, keeping its NCC_TOP largest: one compare-exchange a place, unrolled, so t stays in
+ * registers. Keys are distinct (the cell index is in their low bits). */
+__device__ __forceinline__ void top_insert(unsigned long long (&t)[NCC_TOP], unsigned long long k)
+{
+    if (k <= t[NCC_TOP - 1])
+        return;
+#pragma unroll
+    for (int j = 0; j < NCC_TOP; j++) {
+        const unsigned long long hi = t[j] > k ? t[j] : k;
+        k = t[j] > k ? k : t[j];
+        t[j] = hi;
+    }
+}
+
+/* Two descending lists' best eight: max(a_k, b_(7 - k)) is their top eight as a bitonic sequence, which three
+ * compare-exchange layers sort. Across the warp by xor partners, so every lane ends with the warp's best eight. */
+__device__ __forceinline__ void top_warp_merge(unsigned long long (&t)[NCC_TOP])
+{
+#pragma unroll 1
+    for (int sh = 1; sh < 32; sh <<= 1) {
+        unsigned long long c[NCC_TOP];
+#pragma unroll
+        for (int k = 0; k < NCC_TOP; k++) {
+            const unsigned long long o = __shfl_xor_sync(VTG_FULL, t[NCC_TOP - 1 - k], sh);
+            c[k] = t[k] > o ? t[k] : o;
+        }
+#pragma unroll
+        for (int d = NCC_TOP / 2; d >= 1; d >>= 1)
+#pragma unroll
+            for (int k = 0; k < NCC_TOP; k++)
+                if ((k & d) == 0) {
+                    const unsigned long long hi = c[k] > c[k + d] ? c[k] : c[k + d];
+                    const unsigned long long lo = c[k] > c[k + d] ? c[k + d] : c[k];
+                    c[k] = hi;
+                    c[k + d] = lo;
+                }
+#pragma unroll
+        for (int k = 0; k < NCC_TOP; k++)
+            t[k] = c[k];
+    }
+}
+
+/* The last CTA of a top-8 pass, its warp 0: the best eight of the n CTAs' lists in blk (read through L2) into top /
+ * ntop, and the arrival counter back to zero. */
+__device__ __forceinline__ void ncc_top_final(const unsigned long long *blk, int n, unsigned *arrive, int *top, int *ntop)
+{
+    const int lane = threadIdx.x & 31;
+    unsigned long long t[NCC_TOP];
+#pragma unroll
+    for (int k = 0; k < NCC_TOP; k++)
+        t[k] = 0ull;
+    for (int b = lane; b < n; b += 32)
+#pragma unroll
+        for (int k = 0; k < NCC_TOP; k++)
+            top_insert(t, __ldcg(blk + (size_t)b * NCC_TOP + k));
+    top_warp_merge(t);
+    if (lane == 0) {
+        int c = 0;
+        for (int k = 0; k < NCC_TOP; k++) {
+            if (t[k] == 0ull)
+                break;
+            top[c++] = (int)(0xFFFFFFFFu - (unsigned)(t[k] & 0xFFFFFFFFull));
+        }
+        *ntop = c;
+        *arrive = 0u;
+    }
+}
+
 /* Elements of the tensor-core map's scratch for planes up to max_w x max_h and templates up to max_tw x max_th. */
 size_t vtg_ncc_conv_elems(int max_w, int max_h, int max_th);
 size_t vtg_ncc_fac_elems(int max_w, int max_h);
 
+/* The top-8 pass on its own launch: over map_v, or (words) over the tensor-core map's cell words, which it decodes. */
+cudaError_t vtg_launch_ncc_top(const NccPrm &p, const NccScratch &s, bool words, cudaStream_t st);
 cudaError_t vtg_launch_ncc(const void *plane, int pitch, int plane_type, const float *app, const NccPrm &p,
                            const NccScratch &s, int map_kind, vtg_found *out, cudaStream_t st);
 cudaError_t vtg_launch_ncc_corners(const void *plane, int pitch, int plane_type, const float *app, const NccPrm &p,
