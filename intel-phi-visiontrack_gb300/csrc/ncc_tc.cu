@@ -576,7 +576,9 @@ __global__ void __launch_bounds__(TcShape<Q>::threads, 1) ncc_map_tc(NccPrm p, c
                     if (!((xmask >> s) & 1u))
                         continue;
                     const float j0 = from16((uint16_t)(jw[s >> 1] >> (16 * (s & 1))), KIND);
-                    const float score = (v[8 * qq + s] - j0 * p.sum_t) * fq[s];
+                    /* a near-blank window's factor is 0: + 0 makes its score +0 whatever the sign of the sum, the
+                     * reference's 0 (a -0 would order below the other cells' +0 in the top-8 keys) */
+                    const float score = (v[8 * qq + s] - j0 * p.sum_t) * fq[s] + 0.0f;
                     const int key = ((ly0 + q) >> sh) * per + ((8 * (m & 1) + s) >> sh);
                     if (score > best || (score == best && key < bkey)) {
                         best = score;

@@ -127,6 +127,7 @@ def test_config3_near_blank_windows_score_zero(vtg_lib, ctx, size):
         assert len(inside) > 0
         for prec, v in maps.items():
             assert np.all(v[inside] == 0.0), (size, k, prec, v[inside][v[inside] != 0.0][:5])
+            assert not np.any(np.signbit(v[inside])), (size, k, prec)  # +0, the reference's 0, never -0
         checked += len(inside)
         # the oracle agrees that those windows are near-blank: the FP64 map over one such cell is 0 everywhere
         c = int(inside[0])

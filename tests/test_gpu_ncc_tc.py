@@ -119,3 +119,27 @@ def test_window_without_corners(vtg_lib, ctx):
         f = s.run(dp.data_ptr(), w, h, w, vtg_lib.PLANE_U8, w - 20, w, 1, h, 1, prec)
         assert f["ntop"] == 0 and f["ncc"] == -2.0
     s.close()
+
+
+def test_flat_picture_ties_across_ctas(vtg_lib, ctx):
+    """A flat 1920 x 1080 picture: every window is near-blank, so every cell of every map scores exactly 0, and the
+    eight candidates are the eight lowest cell indices (the reference's insertion order keeps the first of equal
+    values), although each of the top-8 pass's CTAs offers a list of equal values. The F32 and the tensor-core paths
+    then find the same corner with score 0."""
+    w, h = 1920, 1080
+    frame = np.full((h, w), 100, np.uint8)
+    tpl, _, _, _ = S.ncc_templates(S.noise_frame(w, h, seed=6), 32, 1, seed=6, blank_share=0.0)
+    app = (tpl[0].astype(np.float32) - np.float32(tpl[0].mean(dtype=np.float64))).astype(np.float32)
+    norm = float(np.sum(app.astype(np.float64) ** 2))
+    dp = _dev(frame)
+    s = vtg_lib.Search(ctx, w, h)
+    s.template(app, norm)
+    found = []
+    for prec in (vtg_lib.NCC_F32, vtg_lib.NCC_BF16, vtg_lib.NCC_FP16):
+        f, v, mx, my = s.run(dp.data_ptr(), w, h, w, vtg_lib.PLANE_U8, 1, w, 1, h, 1, prec, True)
+        assert f["cells"] > 4 * 1024  # the top-8 pass runs several CTAs
+        assert np.all(v == 0.0) and not np.any(np.signbit(v)), prec
+        assert f["ntop"] == 8 and f["ncc"] == 0.0, (prec, f)
+        found.append((f["hx"], f["hy"], f["second"]))
+    assert found[0] == found[1] == found[2]
+    s.close()
