@@ -270,7 +270,8 @@ int vtg_search_run(vtg_search *s, const void *plane, int w, int h, int pitch, in
                    int where, void *stream);
 /* Runs vtg_search_run's work reps times (after one warm-up) on the search's stream and reports the median CUDA-event
  * time of the correlation map's kernel alone and of the whole search (window sums, map, candidates, half-pixel
- * re-score). For rooflines. */
+ * re-score). Each rep runs it twice: once with events around the map kernel, once with events around the whole
+ * search only, launched as vtg_search_run launches it. For rooflines. */
 int vtg_search_profile(vtg_search *s, const void *plane, int w, int h, int pitch, int plane_type, int x0, int x1,
                        int y0, int y1, int step, int precision, int reps, float *map_ms, float *total_ms);
 /* tk_correlate (src/kern/track.c:208, track.h:59) at n corners: the score of each, -1 where the template does not fit. */

@@ -255,6 +255,8 @@ __global__ void __launch_bounds__(NCC_TOPB_THREADS) ncc_top_ctas(NccPrm p, const
 {
     __shared__ unsigned long long s[NCC_TOPB_THREADS / 32][NCC_TOP];
     __shared__ bool s_last;
+    vtg_grid_launch_dependents(); /* the half-pixel pass may start its CTAs and wait */
+    vtg_grid_dependency_wait();   /* the map's cells, when launched as its programmatic dependent */
     unsigned long long t[NCC_TOP];
 #pragma unroll
     for (int k = 0; k < NCC_TOP; k++)
@@ -265,7 +267,7 @@ __global__ void __launch_bounds__(NCC_TOPB_THREADS) ncc_top_ctas(NccPrm p, const
     for (int u = 0; u < NCC_TOPB_PER; u++) {
         const int i = i0 + u * NCC_TOPB_THREADS;
         if (WORDS) {
-            const unsigned long long w = i < cells ? __ldg(cellw + i) : 0ull;
+            const unsigned long long w = i < cells ? __ldca(cellw + i) : 0ull;
             if (i < cells) {
                 int x, y;
                 ncc_cell_decode(p, i, w, v[u], x, y);
@@ -276,7 +278,7 @@ __global__ void __launch_bounds__(NCC_TOPB_THREADS) ncc_top_ctas(NccPrm p, const
                 v[u] = -3.0f;
             }
         } else {
-            v[u] = i < cells ? __ldg(map_v + i) : -3.0f;
+            v[u] = i < cells ? __ldca(map_v + i) : -3.0f;
         }
     }
 #pragma unroll
@@ -310,18 +312,16 @@ __global__ void __launch_bounds__(NCC_TOPB_THREADS) ncc_top_ctas(NccPrm p, const
     ncc_top_final(blk, gridDim.x, arrive, top, ntop);
 }
 
-cudaError_t vtg_launch_ncc_top(const NccPrm &p, const NccScratch &s, bool words, cudaStream_t st)
+cudaError_t vtg_launch_ncc_top(const NccPrm &p, const NccScratch &s, bool words, cudaStream_t st, bool pdl)
 {
     const int cells = p.ccols * p.crows;
     if (ncc_top_ctas(cells) > s.topblk_lists) /* each CTA leaves its best eight */
         return cudaErrorInvalidValue;
-    if (words)
-        ncc_top_ctas<true><<<ncc_top_ctas(cells), NCC_TOPB_THREADS, 0, st>>>(p, s.cellw, s.map_v, s.map_x, s.map_y, cells,
-                                                                             s.topblk, s.arrive, s.top, s.ntop);
-    else
-        ncc_top_ctas<false><<<ncc_top_ctas(cells), NCC_TOPB_THREADS, 0, st>>>(p, nullptr, s.map_v, s.map_x, s.map_y,
-                                                                              cells, s.topblk, s.arrive, s.top, s.ntop);
-    return cudaGetLastError();
+    const unsigned long long *w = words ? s.cellw : nullptr;
+    return words ? vtg_launch_k(ncc_top_ctas<true>, dim3(ncc_top_ctas(cells)), dim3(NCC_TOPB_THREADS), 0, st, pdl, p, w,
+                                s.map_v, s.map_x, s.map_y, cells, s.topblk, s.arrive, s.top, s.ntop)
+                 : vtg_launch_k(ncc_top_ctas<false>, dim3(ncc_top_ctas(cells)), dim3(NCC_TOPB_THREADS), 0, st, pdl, p, w,
+                                s.map_v, s.map_x, s.map_y, cells, s.topblk, s.arrive, s.top, s.ntop);
 }
 
 /* ---- half-pixel refinement (search_half, search_slot's second half, take_back's parabola) ---- */
@@ -437,12 +437,12 @@ __device__ void ncc_pick(const NccPrm &p, const int *__restrict__ map_x, const i
             }
         }
         if (lane == 0) {
-            const int cell = top[c];
+            const int cell = __ldca(top + c);
             if (bo == side * side)
                 bo = (side * side) / 2; /* no score above -2: the centre */
             s_score[c] = best;
-            s_hx[c] = 2 * map_x[cell] + bo % side - around;
-            s_hy[c] = 2 * map_y[cell] + bo / side - around;
+            s_hx[c] = 2 * __ldca(map_x + cell) + bo % side - around;
+            s_hy[c] = 2 * __ldca(map_y + cell) + bo / side - around;
             s_at[c] = (bo / side + 1) * ring + bo % side + 1;
         }
     }
@@ -494,12 +494,14 @@ __global__ void __launch_bounds__(NCC_TOP * 32) ncc_half_all(const T *__restrict
                                                              vtg_found *__restrict__ out)
 {
     __shared__ bool s_last;
+    vtg_grid_dependency_wait(); /* the candidates, when launched as the top-8 pass's programmatic dependent */
     const int around = p.step > 1 ? 2 * p.step - 1 : 1, ring = 2 * around + 3, r = around + 1;
     const int c = blockIdx.x / (ring * ring), o = blockIdx.x - c * ring * ring;
-    const int n = *ntop;
+    /* what the top-8 pass wrote, by coherent loads: it was not read-only while this kernel ran */
+    const int n = __ldca(ntop);
     if (c < n) {
-        const int cell = top[c];
-        const int hx = 2 * map_x[cell] + (o % ring) - r, hy = 2 * map_y[cell] + (o / ring) - r;
+        const int cell = __ldca(top + c);
+        const int hx = 2 * __ldca(map_x + cell) + (o % ring) - r, hy = 2 * __ldca(map_y + cell) + (o / ring) - r;
         const float v = half_score_cta(plane, pitch, app, p, hx, hy);
         if (threadIdx.x == 0)
             hs[c * ring * ring + o] = v;
@@ -581,13 +583,15 @@ static cudaError_t launch_all(const T *plane, int pitch, const float *app, const
         if (e != cudaSuccess)
             return e;
     }
-    /* the tensor-core map's launcher ends with the top-8 pass over its cell words (ncc_tc.cu) */
-    if (map_kind == VTG_NCC_F32 && (e = vtg_launch_ncc_top(p, s, false, st)) != cudaSuccess)
+    /* the tensor-core map's launcher ends with the top-8 pass over its cell words (ncc_tc.cu); the passes after the
+     * map start as programmatic dependents, except when events around the map time it alone */
+    const bool pdl = !s.map_ev1;
+    if (map_kind == VTG_NCC_F32 && (e = vtg_launch_ncc_top(p, s, false, st, pdl)) != cudaSuccess)
         return e;
     const int around = p.step > 1 ? 2 * p.step - 1 : 1, ring = 2 * around + 3;
-    ncc_half_all<T><<<NCC_TOP * ring * ring, NCC_TOP * 32, 0, st>>>(plane, pitch, app, p, s.map_x, s.map_y, s.top,
-                                                                      s.ntop, s.half, s.arrive + 1, out);
-    return cudaGetLastError();
+    return vtg_launch_k(ncc_half_all<T>, dim3(NCC_TOP * ring * ring), dim3(NCC_TOP * 32), 0, st, pdl, plane, pitch, app, p,
+                        (const int *)s.map_x, (const int *)s.map_y, (const int *)s.top, (const int *)s.ntop, s.half,
+                        s.arrive + 1, out);
 }
 
 cudaError_t vtg_launch_ncc(const void *plane, int pitch, int plane_type, const float *app, const NccPrm &p,

@@ -267,6 +267,7 @@ __global__ void __launch_bounds__(256) ncc_prep(const uint8_t *__restrict__ plan
                                                 int cgx, uint16_t *__restrict__ conv, unsigned long long *__restrict__ cellw,
                                                 int cells)
 {
+    vtg_grid_launch_dependents(); /* the map may start its setup as this launch's last CTAs run */
     const int b = (int)blockIdx.x;
     if (b < nbox) {
         box_cta(plane, pitch, p, fw, fpitch, btx, fac, b % bgx, b / bgx);
@@ -405,6 +406,7 @@ __global__ void __launch_bounds__(TcShape<Q>::threads, 1) ncc_map_tc(NccPrm p, c
                                                      unsigned long long *__restrict__ cellw, int *__restrict__ err)
 {
     extern __shared__ __align__(1024) uint8_t smem[];
+    vtg_grid_launch_dependents(); /* the top-8 pass may take the SMs this launch leaves free and wait there */
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
     const int Y0 = p.y0 + ty * Q;
@@ -416,29 +418,6 @@ __global__ void __launch_bounds__(TcShape<Q>::threads, 1) ncc_map_tc(NccPrm p, c
     /* [0]: stages filled; [1 + i]: 1 + the last stage issuer i committed (0: none) */
     int *issued = (int *)(ctl + 16 * TC_STAGES + 8);
     const uint32_t a_copy = (uint32_t)((TC_XS + krow) * 2), b_copy = (uint32_t)((8 * Q) * krow * 2);
-
-    /* The epilogue's inputs, loaded first: they are in memory before the MMAs start, and arrive while those run. Thread
-     * (quad, lane) owns accumulator row m = 32 quad + lane, corners X0 + 8 m + s, and of its y-corners the pair half of
-     * the CTA's reads: 2 chunks each. A y-corner's eight picture values (the converted row holds the bytes exactly) and
-     * eight factors are one 16-byte and two 16-byte loads. */
-    constexpr int CH = TcShape<Q>::chunks;
-    const int m = (warp & 3) * 32 + lane, c0 = (warp >> 2) * CH;
-    const int xr = tx * TC_XS + 8 * m; /* x - x0 of the thread's first corner */
-    const int fh = p.y1 - p.y0 + 1;
-    uint4 jr[2 * CH];
-    float4 fr[4 * CH];
-#pragma unroll
-    for (int i = 0; i < 2 * CH; i++) {
-        const int yr = ty * Q + 2 * c0 + i;
-        if (yr < fh) {
-            jr[i] = __ldg(reinterpret_cast<const uint4 *>(conv + (size_t)(p.y0 + yr) * cpitch + xr));
-            fr[2 * i] = __ldg(reinterpret_cast<const float4 *>(fac + (size_t)yr * fpitch + xr));
-            fr[2 * i + 1] = __ldg(reinterpret_cast<const float4 *>(fac + (size_t)yr * fpitch + xr + 4));
-        } else {
-            jr[i] = make_uint4(0u, 0u, 0u, 0u);
-            fr[2 * i] = fr[2 * i + 1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        }
-    }
 
     if (tid == 0) {
         for (int s = 0; s < TC_STAGES; s++) {
@@ -457,6 +436,33 @@ __global__ void __launch_bounds__(TcShape<Q>::threads, 1) ncc_map_tc(NccPrm p, c
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tmem_slot;
+    /* Launched as a programmatic dependent of the preparation, the CTA got here (barriers, tensor memory) while that
+     * drained; everything below reads what it wrote (the 16-bit rows, the factors, the cells' reset), with ordinary
+     * coherent loads: that data was not read-only while this kernel ran. */
+    vtg_grid_dependency_wait();
+
+    /* The epilogue's inputs, loaded before the MMAs start: they arrive while those run. Thread
+     * (quad, lane) owns accumulator row m = 32 quad + lane, corners X0 + 8 m + s, and of its y-corners the pair half of
+     * the CTA's reads: 2 chunks each. A y-corner's eight picture values (the converted row holds the bytes exactly) and
+     * eight factors are one 16-byte and two 16-byte loads. */
+    constexpr int CH = TcShape<Q>::chunks;
+    const int m = (warp & 3) * 32 + lane, c0 = (warp >> 2) * CH;
+    const int xr = tx * TC_XS + 8 * m; /* x - x0 of the thread's first corner */
+    const int fh = p.y1 - p.y0 + 1;
+    uint4 jr[2 * CH];
+    float4 fr[4 * CH];
+#pragma unroll
+    for (int i = 0; i < 2 * CH; i++) {
+        const int yr = ty * Q + 2 * c0 + i;
+        if (yr < fh) {
+            jr[i] = __ldca(reinterpret_cast<const uint4 *>(conv + (size_t)(p.y0 + yr) * cpitch + xr));
+            fr[2 * i] = __ldca(reinterpret_cast<const float4 *>(fac + (size_t)yr * fpitch + xr));
+            fr[2 * i + 1] = __ldca(reinterpret_cast<const float4 *>(fac + (size_t)yr * fpitch + xr + 4));
+        } else {
+            jr[i] = make_uint4(0u, 0u, 0u, 0u);
+            fr[2 * i] = fr[2 * i + 1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        }
+    }
 
     const int fmt = KIND == VTG_NCC_BF16 ? 1 : 0;
     const uint32_t idesc = (1u << 4) | ((uint32_t)fmt << 7) | ((uint32_t)fmt << 10) | ((uint32_t)((8 * Q) >> 3) << 17) |
@@ -633,6 +639,9 @@ cudaError_t vtg_launch_ncc_map_tc(const void *plane, int pitch, int elem_bytes, 
     else
         ncc_prep<VTG_NCC_FP16><<<nbox + nconv, 256, 0, st>>>((const uint8_t *)plane, pitch, p, fw, fpitch, btx, bgx, nbox,
                                                              s.fac, rows, cpitch, cgx, s.conv, s.cellw, cells);
+    /* the map and the passes after it start as programmatic dependents (their launch and setup overlap the kernel
+     * before), except when events around the map time it alone */
+    const bool pdl = !s.map_ev0;
 #define MAP_TC(K, QQ)                                                                                                  \
     do {                                                                                                               \
         e = cudaFuncSetAttribute(ncc_map_tc<K, QQ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm.total);       \
@@ -640,9 +649,11 @@ cudaError_t vtg_launch_ncc_map_tc(const void *plane, int pitch, int elem_bytes, 
             return e;                                                                                                  \
         if (s.map_ev0 && (e = cudaEventRecord(s.map_ev0, st)) != cudaSuccess)                                          \
             return e;                                                                                                  \
-        ncc_map_tc<K, QQ><<<tiles_x * tiles_y, TcShape<QQ>::threads, sm.total, st>>>(p, s.band, krow, tiles_x, sm.a_bytes,              \
-                                                                   sm.stage_bytes, s.conv, cpitch, s.fac, fpitch,      \
-                                                                   s.cellw, s.err);                                    \
+        e = vtg_launch_k(ncc_map_tc<K, QQ>, dim3(tiles_x * tiles_y), dim3(TcShape<QQ>::threads), sm.total, st, pdl,    \
+                         p, (const uint16_t *)s.band, krow, tiles_x, sm.a_bytes, sm.stage_bytes,                        \
+                         (const uint16_t *)s.conv, cpitch, (const float *)s.fac, fpitch, s.cellw, s.err);              \
+        if (e != cudaSuccess)                                                                                          \
+            return e;                                                                                                  \
         if (s.map_ev1 && (e = cudaEventRecord(s.map_ev1, st)) != cudaSuccess)                                          \
             return e;                                                                                                  \
     } while (0)
@@ -661,5 +672,5 @@ cudaError_t vtg_launch_ncc_map_tc(const void *plane, int pitch, int elem_bytes, 
     if ((e = cudaGetLastError()) != cudaSuccess)
         return e;
     /* the cells from their words, and their best eight */
-    return vtg_launch_ncc_top(p, s, true, st);
+    return vtg_launch_ncc_top(p, s, true, st, pdl);
 }

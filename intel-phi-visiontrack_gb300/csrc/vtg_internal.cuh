@@ -133,6 +133,10 @@ static inline cudaError_t vtg_launch_k(void (*k)(KArgs...), dim3 grid, dim3 bloc
 /* Waits until the kernels this launch programmatically depends on have finished and their writes are visible (at
  * once when there are none). */
 __device__ __forceinline__ void vtg_grid_dependency_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+/* Lets the stream's next kernel, when launched as a programmatic dependent, start once every CTA of this launch has
+ * called it (or exited): a CTA that calls it at its start is resident, so the dependent's waiting CTAs can take only
+ * the room this launch no longer needs. */
+__device__ __forceinline__ void vtg_grid_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 cudaError_t vtg_launch_points(const DevPyr *I, const DevPyr *J, int top, const LkPrm &p, int n, const float *xs,
                               const float *ys, const float *gx, const float *gy, vtg_lk_out *out, cudaStream_t s);
 

@@ -171,8 +171,9 @@ __device__ __forceinline__ void ncc_top_final(const unsigned long long *blk, int
 size_t vtg_ncc_conv_elems(int max_w, int max_h, int max_th);
 size_t vtg_ncc_fac_elems(int max_w, int max_h);
 
-/* The top-8 pass on its own launch: over map_v, or (words) over the tensor-core map's cell words, which it decodes. */
-cudaError_t vtg_launch_ncc_top(const NccPrm &p, const NccScratch &s, bool words, cudaStream_t st);
+/* The top-8 pass on its own launch: over map_v, or (words) over the tensor-core map's cell words, which it decodes;
+ * with pdl as a programmatic dependent of the kernel before it. */
+cudaError_t vtg_launch_ncc_top(const NccPrm &p, const NccScratch &s, bool words, cudaStream_t st, bool pdl);
 cudaError_t vtg_launch_ncc(const void *plane, int pitch, int plane_type, const float *app, const NccPrm &p,
                            const NccScratch &s, int map_kind, vtg_found *out, cudaStream_t st);
 cudaError_t vtg_launch_ncc_corners(const void *plane, int pitch, int plane_type, const float *app, const NccPrm &p,
