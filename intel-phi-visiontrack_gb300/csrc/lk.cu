@@ -551,13 +551,17 @@ __device__ __forceinline__ void lk_track(const DevPyr &I, const DevPyr &J, int t
 {
     const int W = p.W, H = EXACT ? MAXH : p.H;
     const int mx = W / 2 + 1, my = H / 2 + 1;
-    float gx = ldexpf(gx0, -top), gy = ldexpf(gy0, -top);
+    /* scalings by 2^-L are products with an exact power of two (levels stay far from the exponent's limits): the
+     * same bits as ldexpf, in one instruction */
+    const float stop = __int_as_float((127 - top) << 23);
+    float gx = gx0 * stop, gy = gy0 * stop;
     int status = 0, iters = 0;
     bool valid0 = false;
     float eig0 = 0.0f, idet0 = 0.0f, gxx0 = 0.0f, gxy0 = 0.0f, gyy0 = 0.0f;
     for (int L = top; L >= 0; L--) {
         const DevLevel IL = I.l[L], JL = J.l[L];
-        const float px = ldexpf(x, -L), py = ldexpf(y, -L); /* exact */
+        const float sl = __int_as_float((127 - L) << 23);
+        const float px = x * sl, py = y * sl; /* exact */
         /* written so that NaN fails it: a caller's NaN point is out, never a window at a garbage place */
         if (!(px >= (float)mx && py >= (float)my && px < (float)(IL.w - mx - 1) && py < (float)(IL.h - my - 1))) {
             if (L == 0)
@@ -727,8 +731,12 @@ __device__ __forceinline__ float cell_diff(const DevLevel &A, const DevLevel &B,
 {
     const int x = col * g.cell_w, y0 = row * g.cell_h, y1 = min(y0 + g.cell_h, A.h);
     float s = 0.0f;
+    /* a cell's row and column of element k: a shift and a mask for power-of-two widths (the 16 x 8 grid) */
+    const bool p2 = (g.cell_w & (g.cell_w - 1)) == 0;
+    const int sh = __ffs(g.cell_w) - 1;
     for (int k = lane; k < g.cell_w * (y1 - y0); k += 32) {
-        const int yy = y0 + k / g.cell_w, xx = min(x + k % g.cell_w, A.w - 1);
+        const int kr = p2 ? k >> sh : k / g.cell_w, kc = p2 ? k & (g.cell_w - 1) : k % g.cell_w;
+        const int yy = y0 + kr, xx = min(x + kc, A.w - 1);
         s += fabsf(__ldg(B.p + (size_t)yy * B.pitch + xx) - __ldg(A.p + (size_t)yy * A.pitch + xx));
     }
     s = warp_fold(s);
