@@ -777,10 +777,11 @@ def run_detect(args) -> dict:
 def run_points(args) -> dict:
     """The feature list path (OP_LK, track.c:275-292): LK with the forward-backward check for a list of points between
     a tracker's two pyramid sets (vtg_points), at the tracker's sizes: 128 and 512 features at 640 x 480 (3 levels,
-    the reference's card: 245 us a frame for its feature list, docs/measurements.md:156) and 512 at 1920 x 1080 (4
-    levels).
-    CUDA-event time of one call with its arrays in device memory; flow against the FP64 oracle on the points both call
-    good; the oracle's time (all host cores) beside it."""
+    the reference's card: 245 us a frame for its feature list, docs/measurements.md:156), 512 and 2,048 at 1920 x 1080
+    (4 levels).
+    CUDA-event time of one call with its arrays in device memory, with one and with two warps a point (the warps-a-point
+    choice) and with the default (one); flow (the default's) against the FP64 oracle on the points both call good; the
+    oracle's time (all host cores) beside it."""
     import torch
 
     import vtg
@@ -796,7 +797,7 @@ def run_points(args) -> dict:
     cores = os.cpu_count() or 1
     out = {"metric": "feature-list LK ms a call (21x21, <=10 iterations, flowback 0.5)", "unit": "ms",
            "higher_is_better": False, "results": []}
-    for w, h, levels, n in ((640, 480, 3, 128), (640, 480, 3, 512), (1920, 1080, 4, 512)):
+    for w, h, levels, n in ((640, 480, 3, 128), (640, 480, 3, 512), (1920, 1080, 4, 512), (1920, 1080, 4, 2048)):
         f0, f1, _, _ = S.warp_pair(w, h, (3.2, -1.7), 0.5, seed=5)
         t = vtg.Tracker(ctx, vtg.config(w, h, levels=levels, fb_max=0.5))
         t.build(0, f0)
@@ -810,17 +811,23 @@ def run_points(args) -> dict:
         dout = torch.zeros(n * 32, dtype=torch.uint8, device="cuda")
         torch.cuda.synchronize()
         stream = torch.cuda.ExternalStream(t.stream)
-        for _ in range(3):
-            vtg.check(L.vtg_points(t.h, 0, 1, -1, n, dx.data_ptr(), dy.data_ptr(), None, None, dout.data_ptr(),
-                                   vtg.DEVICE, None), "vtg_points")
-        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(20)]
-        for e0, e1 in ev:
-            e0.record(stream)
-            L.vtg_points(t.h, 0, 1, -1, n, dx.data_ptr(), dy.data_ptr(), None, None, dout.data_ptr(), vtg.DEVICE,
-                         None)
-            e1.record(stream)
-        torch.cuda.synchronize()
-        ms = float(np.median([e0.elapsed_time(e1) for e0, e1 in ev]))
+
+        def timed(warps):
+            t.set_point_warps(warps)
+            for _ in range(3):
+                vtg.check(L.vtg_points(t.h, 0, 1, -1, n, dx.data_ptr(), dy.data_ptr(), None, None, dout.data_ptr(),
+                                       vtg.DEVICE, None), "vtg_points")
+            ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(20)]
+            for e0, e1 in ev:
+                e0.record(stream)
+                L.vtg_points(t.h, 0, 1, -1, n, dx.data_ptr(), dy.data_ptr(), None, None, dout.data_ptr(), vtg.DEVICE,
+                             None)
+                e1.record(stream)
+            torch.cuda.synchronize()
+            return float(np.median([e0.elapsed_time(e1) for e0, e1 in ev]))
+
+        ms_by_warps = {w_: timed(w_) for w_ in (1, 2)}
+        ms = timed(0)  # the default: one warp a point
         got = dout.cpu().numpy().view(vtg.LK_OUT_DTYPE)
         I, J = O.pyramid(f0, levels), O.pyramid(f1, levels)
         t0 = time.perf_counter()
@@ -830,6 +837,7 @@ def run_points(args) -> dict:
         both = (got["status"] == 0) & (ref["status"] == 0)
         err = float(np.max(np.maximum(np.abs(got["x"] - ref["x"]), np.abs(got["y"] - ref["y"]))[both])) if both.any() else None
         out["results"].append({"frame": "%dx%d" % (w, h), "levels": levels, "points": n, "ms": ms,
+                               "ms_one_warp_a_point": ms_by_warps[1], "ms_two_warps_a_point": ms_by_warps[2],
                                "status_agreement": float(np.mean(got["status"] == ref["status"])),
                                "max_err_px": err, "cpu_oracle_ms": cpu_ms, "cpu_cores": cores,
                                "reference_card_us": 245 if w == 640 else None})

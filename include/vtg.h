@@ -145,6 +145,10 @@ int vtg_cells(vtg_tracker *t, int prev, int cur, struct vtg_cell *cells, struct 
  * `top` the first level (-1: the tracker's top). Arrays in host or device memory as `where` says. */
 int vtg_points(vtg_tracker *t, int prev, int cur, int top, int n, const float *xs, const float *ys, const float *gx,
                const float *gy, struct vtg_lk_out *out, int where, void *stream);
+/* Warps a point for the tracker's later vtg_points calls: 1 (a warp walks the whole patch), 2 (two warps each walk half
+ * the patch's rows and add their sums after every pass), or 0, the default, which is 1: on the GB300 two warps were
+ * slower at every list length measured (128 to 2,048 points). The two differ only in the F32 rounding of the sums. */
+int vtg_tracker_set_point_warps(vtg_tracker *t, int warps);
 
 /* Copies one level of a set out (tk_level, src/kern/track.h:61): h_L rows of w_L floats, Q6. */
 int vtg_level(vtg_tracker *t, int set, int level, float *out, int where, void *stream);

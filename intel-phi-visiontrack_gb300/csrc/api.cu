@@ -306,6 +306,7 @@ extern "C" int vtg_tracker_create(vtg_ctx *ctx, const vtg_config *cfg, vtg_track
     t->d_mm = (uint32_t *)(t->mem + L.mm_off);
     t->d_app = (float *)(t->mem + L.app_off);
     t->build_opts = 0;
+    t->point_warps = 0;
     DevPyr d[4] = {pyr_from(t, 0, 0), pyr_from(t, 0, (int)cfg->flow_level), pyr_from(t, 1, 0),
                    pyr_from(t, 1, (int)cfg->flow_level)};
     /* Pyramid planes start zeroed, as the reference's do (track.c:493-503). */
@@ -421,6 +422,14 @@ extern "C" int vtg_tracker_set_build(vtg_tracker *t, int flags)
 
 extern "C" int vtg_tracker_build_flags(const vtg_tracker *t) { return t ? t->build_opts : 0; }
 
+extern "C" int vtg_tracker_set_point_warps(vtg_tracker *t, int warps)
+{
+    if (!t || warps < 0 || warps > 2)
+        return VTG_EINVAL;
+    t->point_warps = warps;
+    return VTG_OK;
+}
+
 extern "C" int vtg_cells(vtg_tracker *t, int prev, int cur, vtg_cell *cells, vtg_lk_out *lk, int where, void *stream)
 {
     if (!t || prev < 0 || prev > 1 || cur < 0 || cur > 1 || (where != VTG_HOST && where != VTG_DEVICE))
@@ -458,7 +467,8 @@ extern "C" int vtg_points(vtg_tracker *t, int prev, int cur, int top, int n, con
     if (top < 0)
         top = t->levels - 1;
     if (where == VTG_DEVICE) {
-        CU(vtg_launch_points(t->desc + 2 * prev, t->desc + 2 * cur, top, t->prm, n, xs, ys, gx, gy, out, s));
+        CU(vtg_launch_points(t->desc + 2 * prev, t->desc + 2 * cur, top, t->prm, n, xs, ys, gx, gy, out, s,
+                             t->point_warps));
         return VTG_OK;
     }
     /* Host arrays: one stream-ordered scratch allocation for the call. */
@@ -473,7 +483,8 @@ extern "C" int vtg_points(vtg_tracker *t, int prev, int cur, int top, int n, con
         CU(cudaMemcpyAsync(dgx, gx, fbytes, cudaMemcpyHostToDevice, s));
     if (gy)
         CU(cudaMemcpyAsync(dgy, gy, fbytes, cudaMemcpyHostToDevice, s));
-    CU(vtg_launch_points(t->desc + 2 * prev, t->desc + 2 * cur, top, t->prm, n, dx, dy, dgx, dgy, dout, s));
+    CU(vtg_launch_points(t->desc + 2 * prev, t->desc + 2 * cur, top, t->prm, n, dx, dy, dgx, dgy, dout, s,
+                         t->point_warps));
     CU(cudaMemcpyAsync(out, dout, (size_t)n * sizeof(vtg_lk_out), cudaMemcpyDeviceToHost, s));
     CU(cudaFreeAsync(d, s));
     return VTG_OK;

@@ -205,7 +205,7 @@ int track_one(const vtg_ref_plane *I, const vtg_ref_plane *J, int top, const vtg
     const float hp[4] = {x, y, gx, gy};
     TRY(cudaMemcpyAsync(dp, h, sizeof(h), cudaMemcpyHostToDevice, g_c.stream));
     TRY(cudaMemcpyAsync(pt, hp, sizeof(hp), cudaMemcpyHostToDevice, g_c.stream));
-    TRY(vtg_launch_points(dp, dp + 1, top, lk_prm(c, 0.0f), 1, pt, pt + 1, pt + 2, pt + 3, dout, g_c.stream));
+    TRY(vtg_launch_points(dp, dp + 1, top, lk_prm(c, 0.0f), 1, pt, pt + 1, pt + 2, pt + 3, dout, g_c.stream, 1));
     TRY(cudaMemcpyAsync(o, dout, sizeof(vtg_lk_out), cudaMemcpyDeviceToHost, g_c.stream));
     TRY(cudaStreamSynchronize(g_c.stream));
     return VTG_OK;

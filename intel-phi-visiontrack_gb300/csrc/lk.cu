@@ -528,6 +528,30 @@ __device__ __forceinline__ void lk_sample(const DevLevel &L, int jx, float fx, i
     b1 = RESID ? t1 : t1 * LK_GRAD_SCALE;
 }
 
+/* Two warps on one point (NW = 2): each takes half the patch's rows, and after every pass over them the pair adds its
+ * partial sums. Lane 0 of each posts its warp's N folded sums to the pair's slot, both wait at the pair's named barrier
+ * (64 threads), every lane adds the two in one order (the top half's first), and a second wait frees the slot. Both
+ * warps then hold the same totals, so they take the same decisions in the walk. */
+struct LkPair {
+    float *slot; /* [2][8] floats in shared memory */
+    int bar;     /* the pair's named barrier */
+    int half;    /* 0: the top rows, 1: the bottom rows */
+};
+
+template <int N>
+__device__ __forceinline__ void pair_add(float (&v)[N], const LkPair &q, int lane)
+{
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < N; k++)
+            q.slot[q.half * 8 + k] = v[k];
+    asm volatile("bar.sync %0, 64;" ::"r"(q.bar) : "memory");
+#pragma unroll
+    for (int k = 0; k < N; k++)
+        v[k] = q.slot[k] + q.slot[8 + k];
+    asm volatile("bar.sync %0, 64;" ::"r"(q.bar) : "memory");
+}
+
 /* A position as whole pixel + offset: floor and phase of base + t, base a whole number. */
 __device__ __forceinline__ void split(int base, float t, int &i, float &f)
 {
@@ -544,13 +568,18 @@ __device__ __forceinline__ void split(int base, float t, int &i, float &f)
 #define LK_WORK_PASS (1u << 8)
 #define LK_WORK_ITER (1u << 16)
 
-template <int MAXH, bool EXACT, bool TS>
+template <int MAXH, bool EXACT, bool TS, int NW = 1>
 __device__ __forceinline__ void lk_track(const DevPyr &I, const DevPyr &J, int top, const LkPrm &p, float x, float y,
                                          float gx0, float gy0, int lane, Patch<MAXH, TS> &P, vtg_lk_out &o,
-                                         unsigned &work)
+                                         unsigned &work, const LkPair &q = LkPair{nullptr, 0, 0})
 {
-    const int W = p.W, H = EXACT ? MAXH : p.H;
-    const int mx = W / 2 + 1, my = H / 2 + 1;
+    /* NW = 2: the patch's rows split as Ht = ceil(H / 2) on top and the rest below; this warp's Hs rows start `off`
+     * rows down, so its passes see a patch of Hs rows whose centre row sits dy rows below the point's */
+    const int Hf = NW == 2 ? p.H : (EXACT ? MAXH : p.H);
+    const int Ht = (Hf + 1) / 2, off = NW == 2 && q.half ? Ht : 0;
+    const int W = p.W, H = NW == 2 ? (q.half ? Hf - Ht : Ht) : Hf;
+    const int dy = NW == 2 ? off + H / 2 - Hf / 2 : 0;
+    const int mx = W / 2 + 1, my = Hf / 2 + 1;
     /* scalings by 2^-L are products with an exact power of two (levels stay far from the exponent's limits): the
      * same bits as ldexpf, in one instruction */
     const float stop = __int_as_float((127 - top) << 23);
@@ -576,7 +605,16 @@ __device__ __forceinline__ void lk_track(const DevPyr &I, const DevPyr &J, int t
         const int bx = (int)fpx, by = (int)fpy;
         const float rx = px - fpx, ry = py - fpy; /* exact */
         float gxx, gxy, gyy, tc, cx, cy;
-        lk_build<MAXH, EXACT, TS>(IL, bx, rx, by, ry, W, H, lane, P, gxx, gxy, gyy, tc, cx, cy);
+        lk_build<MAXH, EXACT, TS>(IL, bx, rx, by + dy, ry, W, H, lane, P, gxx, gxy, gyy, tc, cx, cy);
+        if constexpr (NW == 2) { /* tc stays each half's own: its terms cancel within the half */
+            float v[5] = {gxx, gxy, gyy, cx, cy};
+            pair_add(v, q, lane);
+            gxx = v[0];
+            gxy = v[1];
+            gyy = v[2];
+            cx = v[3];
+            cy = v[4];
+        }
         work += LK_WORK_BUILD;
         /* det = gxx gyy - gxy^2 by Kahan's product difference; the smaller eigenvalue as det / lambda_max. */
         const float w2 = gxy * gxy;
@@ -628,7 +666,9 @@ __device__ __forceinline__ void lk_track(const DevPyr &I, const DevPyr &J, int t
             split(bx, qx, jx, fx);
             split(by, qy, jy, fy);
             if (jx != cjx || jy != cjy) {
-                lk_correlate<MAXH, EXACT, TS>(JL, jx, jy, W, H, lane, P, tc, X);
+                lk_correlate<MAXH, EXACT, TS>(JL, jx, jy + dy, W, H, lane, P, tc, X);
+                if constexpr (NW == 2)
+                    pair_add(X, q, lane);
                 work += LK_WORK_PASS;
                 cjx = jx;
                 cjy = jy;
@@ -669,7 +709,13 @@ __device__ __forceinline__ void lk_track(const DevPyr &I, const DevPyr &J, int t
             split(bx, qx, jx, fx);
             split(by, qy, jy, fy);
             float sa, ss;
-            lk_sample<MAXH, EXACT, true, TS>(J0, jx, fx, jy, fy, W, H, lane, P, sa, ss);
+            lk_sample<MAXH, EXACT, true, TS>(J0, jx, fx, jy + dy, fy, W, H, lane, P, sa, ss);
+            if constexpr (NW == 2) {
+                float v[2] = {sa, ss};
+                pair_add(v, q, lane);
+                sa = v[0];
+                ss = v[1];
+            }
             work += LK_WORK_RESID;
             const float r0 = sa / p.area, r1 = ss / p.area;
             o.residual = r0;
@@ -686,16 +732,16 @@ __device__ __forceinline__ void lk_track(const DevPyr &I, const DevPyr &J, int t
 
 /* lk_track then, when asked and the track is good, the forward-backward check (src/kern/lk_driver.inc:111-121): the
  * found point tracked back from J to I from minus the found flow. One copy of the walk serves both passes. */
-template <int MAXH, bool EXACT, bool TS>
+template <int MAXH, bool EXACT, bool TS, int NW = 1>
 __device__ __forceinline__ void lk_point(const DevPyr &I, const DevPyr &J, int top, const LkPrm &p, float x, float y,
                                          float gx, float gy, int lane, Patch<MAXH, TS> &P, vtg_lk_out &o,
-                                         unsigned &work)
+                                         unsigned &work, const LkPair &q = LkPair{nullptr, 0, 0})
 {
     const int passes = p.fb_max2 > 0.0f ? 2 : 1;
     float sx = x, sy = y;
     for (int pass = 0; pass < passes; pass++) {
         vtg_lk_out r;
-        lk_track<MAXH, EXACT, TS>(pass ? J : I, pass ? I : J, top, p, sx, sy, gx, gy, lane, P, r, work);
+        lk_track<MAXH, EXACT, TS, NW>(pass ? J : I, pass ? I : J, top, p, sx, sy, gx, gy, lane, P, r, work, q);
         if (pass == 0) {
             o = r;
             if (o.status)
@@ -974,6 +1020,35 @@ __global__ void __launch_bounds__(256, 2) lk_points_kernel(const DevPyr *__restr
     store_out(out + i, o, lane);
 }
 
+/* The point list with two warps a point (consecutive warps of a CTA): each walks the same pyramid with half the patch's
+ * rows, and the pair adds its sums after every pass. The warps-a-point choice of vtg_tracker_set_point_warps; not the
+ * default, as a pass's latency is one round of row loads however many rows a warp takes. MAXH bounds a half's rows
+ * (11 for a 21-row patch, 16 for any up to 31). */
+template <int MAXH>
+__global__ void __launch_bounds__(256, 2) lk_points_pair_kernel(const DevPyr *__restrict__ Ip,
+                                                             const DevPyr *__restrict__ Jp, int top, LkPrm p, int n,
+                                                             const float *__restrict__ xs, const float *__restrict__ ys,
+                                                             const float *__restrict__ gxs,
+                                                             const float *__restrict__ gys,
+                                                             vtg_lk_out *__restrict__ out)
+{
+    extern __shared__ f2_t s_tp[]; /* the template's T: 8 warps x (MAXH / 2) x 32 pairs */
+    __shared__ float s_pair[4][16];
+    const int wg = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    const int i = wg >> 1, pr = (threadIdx.x >> 6) & 3;
+    if (i >= n) /* both warps of a pair leave together */
+        return;
+    const LkPair q{s_pair[pr], 1 + pr, wg & 1};
+    Patch<MAXH, true> P;
+    P.ts = s_tp + (size_t)(threadIdx.x >> 5) * (MAXH / 2) * 32;
+    vtg_lk_out o;
+    unsigned work = 0;
+    lk_point<MAXH, false, true, 2>(*Ip, *Jp, top, p, xs[i], ys[i], gxs ? gxs[i] : 0.0f, gys ? gys[i] : 0.0f, lane, P,
+                                   o, work, q);
+    if (q.half == 0)
+        store_out(out + i, o, lane);
+}
+
 /* shared memory of a 256-thread single-stream CTA: its 8 warps' template intensities (at most 30 KB) */
 static constexpr size_t lk_t_bytes(int maxh) { return sizeof(f2_t) * 8 * (size_t)(maxh / 2) * 32; }
 
@@ -991,11 +1066,22 @@ cudaError_t vtg_launch_cells(const DevPyr *I, const DevPyr *J, int top, const Lk
 }
 
 cudaError_t vtg_launch_points(const DevPyr *I, const DevPyr *J, int top, const LkPrm &p, int n, const float *xs,
-                              const float *ys, const float *gx, const float *gy, vtg_lk_out *out, cudaStream_t s)
+                              const float *ys, const float *gx, const float *gy, vtg_lk_out *out, cudaStream_t s,
+                              int warps)
 {
-    const int blocks = (n + 7) / 8;
     if (n <= 0)
         return cudaSuccess;
+    if (warps < 0 || warps > 2)
+        return cudaErrorInvalidValue;
+    if (vtg_points_pair(n, warps)) {
+        const int pblocks = (n + 3) / 4;
+        if (p.H <= 22)
+            lk_points_pair_kernel<11><<<pblocks, 256, lk_t_bytes(11), s>>>(I, J, top, p, n, xs, ys, gx, gy, out);
+        else
+            lk_points_pair_kernel<16><<<pblocks, 256, lk_t_bytes(16), s>>>(I, J, top, p, n, xs, ys, gx, gy, out);
+        return cudaGetLastError();
+    }
+    const int blocks = (n + 7) / 8;
     if (p.H == 21)
         lk_points_kernel<21, true><<<blocks, 256, lk_t_bytes(21), s>>>(I, J, top, p, n, xs, ys, gx, gy, out);
     else if (p.H == 15)

@@ -137,7 +137,13 @@ __device__ __forceinline__ void vtg_grid_dependency_wait() { asm volatile("gridd
  * called it (or exited): a CTA that calls it at its start is resident, so the dependent's waiting CTAs can take only
  * the room this launch no longer needs. */
 __device__ __forceinline__ void vtg_grid_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+/* The point list. warps: warps a point (1 or 2), or 0 for the default (vtg_points_pair). */
 cudaError_t vtg_launch_points(const DevPyr *I, const DevPyr *J, int top, const LkPrm &p, int n, const float *xs,
-                              const float *ys, const float *gx, const float *gy, vtg_lk_out *out, cudaStream_t s);
+                              const float *ys, const float *gx, const float *gy, vtg_lk_out *out, cudaStream_t s,
+                              int warps = 0);
+/* Two warps a point only when asked: measured on the GB300 it was slower at every list length (128 points at 640 x
+ * 480: 0.037 against 0.029 ms; 2,048 at 1080p: 0.104 against 0.047 ms), because a pass's latency is one round of row
+ * loads however many rows a warp takes, and the pair's exchanges add to it. */
+static inline bool vtg_points_pair(int n, int warps) { return warps == 2 && n > 0; }
 
 #endif

@@ -29,6 +29,7 @@ struct vtg_tracker {
     int build_opts;       /* VTG_BUILD_CONTRAST | VTG_BUILD_PRE_GAUSS */
     float *d_app;         /* an appearance template and its norm (VTG_APP_W x VTG_APP_H + 1 floats), for host reads */
     LkPrm prm;
+    int point_warps; /* warps a point of the point list: 0 by the list's length, 1 or 2 */
 };
 
 #endif

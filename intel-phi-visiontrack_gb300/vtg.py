@@ -86,6 +86,7 @@ def lib() -> C.CDLL:
         L.vtg_level.argtypes = [vp, i, i, vp, i, vp]
         L.vtg_level_size.argtypes = [vp, i, C.POINTER(i), C.POINTER(i)]
         L.vtg_tracker_set_build.argtypes = [vp, i]
+        L.vtg_tracker_set_point_warps.argtypes = [vp, i]
         L.vtg_tracker_build_flags.argtypes = [vp]
         L.vtg_contrast_gain.argtypes = [i, i, vp]
         L.vtg_store_appearance.argtypes = [vp, i, f, f, f, f, vp, vp, C.POINTER(Appearance), i, vp]
@@ -201,6 +202,10 @@ class Tracker:
     @property
     def build_flags(self) -> int:
         return lib().vtg_tracker_build_flags(self.h)
+
+    def set_point_warps(self, warps: int):
+        """Warps a point for later points() calls: 1, 2 (half the patch's rows each), or 0 (the default: 1)."""
+        check(lib().vtg_tracker_set_point_warps(self.h, int(warps)), "vtg_tracker_set_point_warps")
 
     def level(self, set_: int, level: int) -> np.ndarray:
         w, h = self.level_size(level)

@@ -349,3 +349,37 @@ def test_errors_are_status_codes(vtg_lib, ctx):
         vtg_lib.Tracker(small, vtg_lib.config(1920, 1080))
     assert e.value.code == vtg_lib.EBUDGET
     small.close()
+
+
+def test_points_two_warps_a_point(vtg_lib, ctx):
+    """The point list walked by two warps a point, each over half the patch's rows (vtg_tracker_set_point_warps):
+    the same points as one warp a point up to the F32 rounding of the sums, and within 0.01 px of the FP64 oracle, for
+    patches whose halves are even, odd and unequal."""
+    w, h = 320, 240
+    f0, f1, _, _ = S.warp_pair(w, h, (1.5, -2.25), 0.5, seed=21)
+    rng = np.random.default_rng(21)
+    xs = rng.uniform(20, w - 20, 200).astype(np.float32)
+    ys = rng.uniform(20, h - 20, 200).astype(np.float32)
+    for (pw, ph, levels, fb) in ((21, 21, 3, 0.5), (15, 15, 2, 0.25), (9, 13, 2, 0.0), (29, 31, 2, 0.5)):
+        t = _tracker(vtg_lib, ctx, w, h, levels=levels, patch_w=pw, patch_h=ph, fb_max=fb)
+        t.build(0, f0)
+        t.build(1, f1)
+        t.set_point_warps(1)
+        one = t.points(0, 1, xs, ys)
+        t.set_point_warps(2)
+        two = t.points(0, 1, xs, ys)
+        t.set_point_warps(0)
+        auto = t.points(0, 1, xs, ys)
+        assert auto.tobytes() == one.tobytes()  # the default is one warp a point
+        assert (one["status"] == two["status"]).mean() >= 0.99, (pw, ph)
+        both = (one["status"] == 0) & (two["status"] == 0)
+        assert both.sum() > 0.5 * len(xs)
+        assert np.abs(one["x"] - two["x"])[both].max() <= 1e-3 and np.abs(one["y"] - two["y"])[both].max() <= 1e-3
+        P0, P1 = O.pyramid(f0, levels), O.pyramid(f1, levels)
+        ref = O.lk_points(P0, P1, levels - 1, O.lk_cfg(pw, ph), xs, ys, max_fb=fb, mode=O.F64)
+        assert (two["status"] == ref["status"]).mean() >= 0.99
+        ok, err = _flow_err(two, ref)
+        assert err <= TOL_PX, (pw, ph, err)
+        with pytest.raises(vtg_lib.VtgError):
+            t.set_point_warps(3)
+        t.close()
