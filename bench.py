@@ -36,7 +36,7 @@ METRIC = "LK cells/s + p99 ms/frame-pair, served-batched vs plain GPU; ≤0.01px
 W, H, LEVELS, CELL_W, CELL_H, PATCH = 1920, 1080, 4, 16, 8, 21
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one batched LK launch of 8 such streams, from an ncu
 # capture of `bench.py --profile batch` (the same kernel and launch shape); a constant, not measured by this run
-LK_TRAFFIC_BYTES = 176_632_320 + 7_767_296
+LK_TRAFFIC_BYTES = 177_114_880 + 8_196_864
 CELLS = 16200
 
 
