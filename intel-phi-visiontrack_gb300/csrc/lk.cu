@@ -899,8 +899,15 @@ __global__ void __launch_bounds__(WARPS * 32, MINB) lk_batch_kernel(const LkJob 
             int t = 0;
             if (lane == 0) {
                 if (tiled) {
+                    /* Whole tiles to each CTA in turn (tile g x CTAs + its index), its warps taking the tile's items
+                     * from s_taken: neighbouring cells on one SM. All but the last round of tiles; those items any
+                     * warp of any CTA takes one by one from the global counter, so SMs whose tiles cost less pick up
+                     * the rest instead of idling at the launch's end. */
                     const int i = atomicAdd(&s_taken, 1), g = i / per_tile;
-                    t = (g * (int)gridDim.x + (int)blockIdx.x) * per_tile + (i - g * per_tile);
+                    const int tiles = (items + per_tile - 1) / per_tile, rounds = tiles / (int)gridDim.x;
+                    const int fixed = (rounds > 1 ? rounds - 1 : 0) * (int)gridDim.x;
+                    const int tile = g * (int)gridDim.x + (int)blockIdx.x;
+                    t = tile < fixed ? tile * per_tile + (i - g * per_tile) : fixed * per_tile + atomicAdd(counter, 1);
                 } else {
                     t = atomicAdd(counter, 1);
                 }
