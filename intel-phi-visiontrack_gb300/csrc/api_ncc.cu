@@ -157,7 +157,6 @@ extern "C" int vtg_search_create(vtg_ctx *ctx, int max_w, int max_h, int max_tw,
     s->band[0] = (uint16_t *)(s->mem + L.band0);
     s->band[1] = (uint16_t *)(s->mem + L.band1);
     s->sc.band = nullptr;
-    s->sc.band_rows = s->sc.krow = 0;
     s->sc.conv = (uint16_t *)(s->mem + L.conv);
     s->sc.conv_elems = L.conv_elems;
     s->sc.fac = (float *)(s->mem + L.fac);

@@ -136,7 +136,6 @@ extern "C" int vtg_search_run_noalloc(const void *plane, int w, int h, int pitch
     s.top = s.map_y + VTG_NOALLOC_MAX_CELLS;
     s.ntop = s.top + NCC_TOP;
     s.band = nullptr;
-    s.band_rows = s.krow = 0;
     s.err = s.ntop + 1;
     s.half = (float *)(base + VTG_NOALLOC_HALF_AT);
     s.topblk = (unsigned long long *)(base + VTG_NOALLOC_TOPB_AT);

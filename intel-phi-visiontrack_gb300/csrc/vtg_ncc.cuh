@@ -43,7 +43,6 @@ struct NccScratch {
     int *top, *ntop;
     float *half;          /* the candidates' half-pixel scores: NCC_TOP x (2 around + 3)^2, around <= 2 x 16 - 1 */
     const uint16_t *band; /* the template band for the tensor-core map (ncc_tc.cu), NULL if unset */
-    int band_rows, krow;  /* image rows of a tile's band (NCC_TC_Q + th - 1), K per image row */
     int *err;             /* device status word: nonzero when a bounded wait gave up */
     /* the tensor-core map's own scratch: the 16-bit picture (shifted so a tile's row starts 16-byte aligned), each
      * corner's normalisation factor, and one 64-bit (score, corner) word per cell */
