@@ -21,8 +21,9 @@
  * into its own accumulator: issuing a stage's MMAs takes a lone thread longer than the tensor core takes to run them,
  * so one issuer would leave it idle. Every wait is bounded by the global timer; past it the kernel records an error
  * word.
- * Epilogue: each of the 128 threads owns one accumulator row (8 x-corners by Q y-corners) of each issuer and sums
- * them. Per corner: st = acc - J(x, y) sum t' (the reference's st is relative to the corner's first pixel), times the
+ * Epilogue: four warps cover the accumulator's 128 lanes, one row (8 x-corners by Q y-corners) a thread; at Q = 16
+ * eight, two to a lane quarter, each reading half the row's columns. A thread sums the issuers' accumulators for its
+ * row. Per corner: st = acc - J(x, y) sum t' (the reference's st is relative to the corner's first pixel), times the
  * corner's factor 1 / sqrt(norm var) from ncc_prep (0 for a near-blank window: the exact integer rule), the best
  * per 16 x 16 cell by value then scan order, merged across tiles by a 64-bit atomicMax on (ordered score, inverted scan
  * index). */
