@@ -153,7 +153,7 @@ __device__ __forceinline__ float ncc_score(float st, long long s1, long long s2,
     return st / sqrtf(p.norm * var);
 }
 
-/* ---- the map, F32 products: one CTA per cell ---- */
+/* ---- the map, F32 products: one CTA a cell (steps 4 to 16), or 32 x 32 corners a CTA (steps 1 and 2) ---- */
 
 /* A cell's best: value descending, then row-major scan order (the first maximum wins, as OP_SEARCH's strict > does). */
 __device__ __forceinline__ bool better(float v, int k, float bv, int bk) { return v > bv || (v == bv && k < bk); }
@@ -164,7 +164,7 @@ __global__ void __launch_bounds__(256) ncc_map_f32(const T *__restrict__ plane, 
                                                    const long long *__restrict__ S2, int tp, float *__restrict__ map_v,
                                                    int *__restrict__ map_x, int *__restrict__ map_y)
 {
-    extern __shared__ float sm[];
+    extern __shared__ __align__(16) float sm[];
     const int cell = blockIdx.x;
     const int cx0 = p.x0 + (cell % p.ccols) * NCC_CELL, cy0 = p.y0 + (cell / p.ccols) * NCC_CELL;
     const int cx1 = min(cx0 + NCC_CELL, p.x1 + 1), cy1 = min(cy0 + NCC_CELL, p.y1 + 1);
@@ -237,6 +237,137 @@ __global__ void __launch_bounds__(256) ncc_map_f32(const T *__restrict__ plane, 
             map_y[cell] = fired ? cy0 + (bk / per) * p.step : cy0;
         }
     }
+}
+
+/* The F32 map at steps 1 and 2 (the steps the reference's searches take), four corners a thread. A CTA of 256 threads
+ * takes 32 x 32 corners: 2 x 2 cells at step 1, 4 x 4 at step 2. It stages their window and the template in shared
+ * memory, the window's rows at an odd pitch so that the four or eight picture rows a warp reads fall in different
+ * banks. A thread scores four corners of one row, ST apart. As the column pair j advances by 2, the picture values
+ * the four corners read are a window of M = 3 ST + 2 registers sliding along the row: two loads and one template load
+ * feed eight products. Each corner's sums run in ncc_map_f32's order (rows, then columns in even and odd chains), so
+ * the map is the same bits. A cell's best is a shared-memory atomicMax of (ordered score, inverted scan index): value
+ * descending, then scan order, as `better`. A score that underflowed to -0 is taken as +0 first (adding +0), so the two
+ * zeros tie as they compare in `better`. */
+#define NMQ_K 4       /* corners a thread */
+#define NMQ_CORNERS 32 /* corners a CTA's side */
+
+/* The window a CTA of ncc_map_f32q<ST> stages: columns (with the two values the sliding window reads past the last
+ * corner's row on its last column pair), its odd pitch, and rows. */
+__host__ __device__ inline int nmq_cols(int st, int tw) { return (NMQ_CORNERS - 1) * st + tw + 2; }
+__host__ __device__ inline int nmq_pitch(int st, int tw) { return nmq_cols(st, tw) | 1; }
+__host__ __device__ inline int nmq_rows(int st, int th) { return (NMQ_CORNERS - 1) * st + th; }
+
+template <typename T, int ST>
+__global__ void __launch_bounds__(256) ncc_map_f32q(const T *__restrict__ plane, int pitch, const float *__restrict__ app,
+                                                    NccPrm p, const long long *__restrict__ S1,
+                                                    const long long *__restrict__ S2, int tp, int bcols,
+                                                    float *__restrict__ map_v, int *__restrict__ map_x,
+                                                    int *__restrict__ map_y)
+{
+    constexpr int BC = NMQ_CORNERS * ST / NCC_CELL; /* cells a CTA's side */
+    constexpr int PER = NCC_CELL / ST;             /* corners a cell's side */
+    constexpr int M = (NMQ_K - 1) * ST + 2;        /* the sliding window */
+    extern __shared__ __align__(16) float sm[];
+    __shared__ unsigned long long s_best[BC * BC];
+    const int bx = blockIdx.x % bcols, by = blockIdx.x / bcols;
+    const int ccx0 = BC * bx, ccy0 = BC * by; /* the CTA's first cell column and row */
+    const int X0 = p.x0 + ccx0 * NCC_CELL, Y0 = p.y0 + ccy0 * NCC_CELL;
+    const int iw = nmq_cols(ST, p.tw), ip = nmq_pitch(ST, p.tw), ih = nmq_rows(ST, p.th);
+    float *s_app = sm, *s_img = sm + p.tw * p.th; /* tw th is a multiple of 8: s_img stays 16-byte aligned */
+    for (int i = threadIdx.x; i < p.tw * p.th; i += blockDim.x)
+        s_app[i] = app[i];
+    for (int i = threadIdx.x; i < iw * ih; i += blockDim.x) {
+        const int r = i / iw, c = i - r * iw;
+        const int yy = min(Y0 + r, p.h - 1), xx = min(X0 + c, p.w - 1);
+        s_img[r * ip + c] = (float)__ldg(plane + (size_t)yy * pitch + xx);
+    }
+    if (threadIdx.x < BC * BC)
+        s_best[threadIdx.x] = 0ull;
+    __syncthreads();
+    constexpr int GROUPS = NMQ_CORNERS / NMQ_K;
+    const int t = threadIdx.x;
+    const int b = t / GROUPS, a0 = (t - b * GROUPS) * NMQ_K; /* corner row, first corner column in the CTA */
+    const float *rowb = s_img + (b * ST) * ip + a0 * ST;
+    float first[NMQ_K], s0[NMQ_K], s1[NMQ_K];
+#pragma unroll
+    for (int c = 0; c < NMQ_K; c++) {
+        first[c] = rowb[c * ST];
+        s0[c] = s1[c] = 0.0f;
+    }
+    for (int i = 0; i < p.th; i++) {
+        const float *row = rowb + i * ip, *tt = s_app + i * p.tw;
+        float w[M];
+#pragma unroll
+        for (int m = 0; m < M; m++)
+            w[m] = row[m];
+#pragma unroll 4
+        for (int j = 0; j < p.tw; j += 2) {
+            const float2 tv = *reinterpret_cast<const float2 *>(tt + j);
+#pragma unroll
+            for (int c = 0; c < NMQ_K; c++) {
+                s0[c] = __fmaf_rn(w[c * ST] - first[c], tv.x, s0[c]);
+                s1[c] = __fmaf_rn(w[c * ST + 1] - first[c], tv.y, s1[c]);
+            }
+#pragma unroll
+            for (int m = 0; m < M - 2; m++)
+                w[m] = w[m + 2];
+            w[M - 2] = row[j + M];
+            w[M - 1] = row[j + M + 1];
+        }
+    }
+    const int y = Y0 + b * ST;
+#pragma unroll
+    for (int c = 0; c < NMQ_K; c++) {
+        const int a = a0 + c, x = X0 + a * ST;
+        const int ccx = ccx0 + a / PER, ccy = ccy0 + b / PER;
+        if (x > p.x1 || y > p.y1 || ccx >= p.ccols || ccy >= p.crows)
+            continue;
+        const float v = ncc_score(s0[c] + s1[c], box(S1, tp, x, y, p.tw, p.th), box(S2, tp, x, y, p.tw, p.th), p) + 0.0f;
+        const int key = (b % PER) * PER + a % PER;
+        unsigned u = __float_as_uint(v);
+        u = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+        atomicMax(&s_best[(b / PER) * BC + a / PER], ((unsigned long long)u << 32) | (unsigned long long)(0xFFFFFFFFu - (unsigned)key));
+    }
+    __syncthreads();
+    if (t < BC * BC) {
+        const int ccx = ccx0 + t % BC, ccy = ccy0 + t / BC;
+        if (ccx < p.ccols && ccy < p.crows) {
+            const int cell = ccy * p.ccols + ccx;
+            const int cx0 = p.x0 + ccx * NCC_CELL, cy0 = p.y0 + ccy * NCC_CELL;
+            const unsigned long long wd = s_best[t];
+            if (wd == 0ull) { /* no corner: the reference leaves top at -2 and the cell origin */
+                map_v[cell] = -2.0f;
+                map_x[cell] = cx0;
+                map_y[cell] = cy0;
+            } else {
+                unsigned u = (unsigned)(wd >> 32);
+                u = (u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u;
+                const float bv = __uint_as_float(u);
+                const int bk = (int)(0xFFFFFFFFu - (unsigned)(wd & 0xFFFFFFFFull));
+                /* a cell whose every corner reads -1 (out of bounds) keeps -2 and its origin, as `v > top` never fires */
+                const bool fired = bv > -2.0f;
+                map_v[cell] = fired ? bv : -2.0f;
+                map_x[cell] = fired ? cx0 + (bk % PER) * ST : cx0;
+                map_y[cell] = fired ? cy0 + (bk / PER) * ST : cy0;
+            }
+        }
+    }
+}
+
+template <typename T, int ST>
+static cudaError_t launch_map_f32q(const T *plane, int pitch, const float *app, const NccPrm &p, const NccScratch &s,
+                                   cudaStream_t st)
+{
+    constexpr int BC = NMQ_CORNERS * ST / NCC_CELL;
+    const size_t smem = sizeof(float) * ((size_t)p.tw * p.th + (size_t)nmq_pitch(ST, p.tw) * nmq_rows(ST, p.th));
+    cudaError_t e = cudaFuncSetAttribute(ncc_map_f32q<T, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess)
+        return e;
+    const int bcols = (p.ccols + BC - 1) / BC, brows = (p.crows + BC - 1) / BC;
+    ncc_map_f32q<T, ST><<<bcols * brows, NMQ_CORNERS * NMQ_CORNERS / NMQ_K, smem, st>>>(plane, pitch, app, p, s.S1, s.S2,
+                                                                                       s.tp, bcols, s.map_v, s.map_x,
+                                                                                       s.map_y);
+    return cudaGetLastError();
 }
 
 /* ---- the eight best cells ---- */
@@ -569,13 +700,20 @@ static cudaError_t launch_all(const T *plane, int pitch, const float *app, const
         /* the F32 map takes its window sums from the integral images; the tensor-core map's prep sums the bytes */
         integral_rows<T><<<(p.h + 1 + 7) / 8, 256, 0, st>>>(plane, pitch, p.w, p.h, s.S1, s.S2, s.tp);
         integral_cols<<<(p.w + 1 + IC_COLS - 1) / IC_COLS, IC_COLS * IC_SEGS, 0, st>>>(p.w, p.h, s.S1, s.S2, s.tp);
+        /* steps 1 and 2: four corners a thread; the other steps one corner a thread, a CTA a cell */
+        const bool quad = p.step == 1 || p.step == 2;
         const size_t smem = sizeof(float) * ((size_t)p.tw * p.th + (size_t)(NCC_CELL + p.tw) * (NCC_CELL + p.th));
-        e = cudaFuncSetAttribute(ncc_map_f32<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess)
+        if (!quad && (e = cudaFuncSetAttribute(ncc_map_f32<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
+                         cudaSuccess)
             return e;
         if (s.map_ev0 && (e = cudaEventRecord(s.map_ev0, st)) != cudaSuccess)
             return e;
-        ncc_map_f32<T><<<cells, 256, smem, st>>>(plane, pitch, app, p, s.S1, s.S2, s.tp, s.map_v, s.map_x, s.map_y);
+        if (quad)
+            e = p.step == 1 ? launch_map_f32q<T, 1>(plane, pitch, app, p, s, st) : launch_map_f32q<T, 2>(plane, pitch, app, p, s, st);
+        else
+            ncc_map_f32<T><<<cells, 256, smem, st>>>(plane, pitch, app, p, s.S1, s.S2, s.tp, s.map_v, s.map_x, s.map_y);
+        if (e != cudaSuccess)
+            return e;
         if (s.map_ev1 && (e = cudaEventRecord(s.map_ev1, st)) != cudaSuccess)
             return e;
     } else {

@@ -95,6 +95,43 @@ def test_txt_templates_against_fp64_oracle(vtg_lib, ctx, torch_cuda, size):
     s.close()
 
 
+@pytest.mark.parametrize("tw,th,step,window,plane_type", [
+    (32, 21, 1, (7, 250, 3, 131), "u8"),     # 16 x 9 cells: a half-filled last row of 2 x 2 blocks
+    (32, 21, 2, (5, 283, 9, 190), "f32"),    # 18 x 12 cells: 4 x 4 blocks, two columns of the last one filled
+    (24, 7, 2, (1, 320, 1, 240), "u8"),      # 19 x 15 cells
+    (128, 128, 1, (1, 320, 1, 240), "u8"),   # the largest template: the most shared memory a block takes
+    (128, 128, 2, (3, 320, 2, 240), "f32"),
+    (8, 1, 1, (2, 301, 1, 200), "u8"),       # the smallest template
+])
+def test_map_blocks_against_fp64_oracle(vtg_lib, ctx, torch_cuda, tw, th, step, window, plane_type):
+    """The F32 map at the reference's steps (1 and 2) scores 32 x 32 corners a CTA; windows whose cells fill its last
+    blocks only in part, at both plane types, against the FP64 oracle's map and search."""
+    frame = S.noise_frame(320, 240, seed=31 + tw + step)
+    plane = frame.astype(np.float32)
+    rng = np.random.default_rng(tw * 7 + th + step)
+    tx, ty = int(rng.integers(window[0], min(window[1], 320 - tw - 2) + 1)), int(rng.integers(window[2], min(window[3], 240 - th - 2) + 1))
+    patch = plane[ty:ty + th, tx:tx + tw]
+    app = (patch - np.float32(patch.mean(dtype=np.float64))).astype(np.float32)
+    norm = float(np.sum(app.astype(np.float64) ** 2))
+    dp = _dev(torch_cuda, frame if plane_type == "u8" else plane)
+    pt = vtg_lib.PLANE_U8 if plane_type == "u8" else vtg_lib.PLANE_F32
+    s = vtg_lib.Search(ctx, 320, 240)
+    s.template(app, norm)
+    f, mv, mx, my = s.run(dp.data_ptr(), 320, 240, 320, pt, *window, step, want_map=True)
+    ref, rv, rx, ry = O.search_slot(plane, app, norm, *window, step, mode=O.F64)
+    n = f["cells"]
+    assert n > 0
+    assert np.abs(mv - rv[:n]).max() < 1e-4
+    same = np.abs(mv - rv[:n]) < 1e-6  # where two corners of a cell are within rounding, either may win
+    assert np.array_equal(mx[same], rx[:n][same]) and np.array_equal(my[same], ry[:n][same])
+    assert (f["hx"], f["hy"]) == (ref["hx"], ref["hy"])
+    assert abs(f["ncc"] - ref["ncc"]) < 1e-4 and abs(f["second"] - ref["second"]) < 1e-4
+    on_grid = tx % step == max(window[0], 1) % step and ty % step == max(window[2], 1) % step
+    if on_grid and tw * th >= 256:  # a short row of smooth noise has near twins elsewhere
+        assert (f["hx"], f["hy"]) == (2 * tx, 2 * ty) and f["ncc"] > 0.999
+    s.close()
+
+
 def test_near_blank_windows_score_zero(vtg_lib, ctx, torch_cuda):
     """vt_ncc_check's property on the GPU: nearly blank windows never read 0.5 or more, none reads over 1, and the
     template itself reads 1."""
