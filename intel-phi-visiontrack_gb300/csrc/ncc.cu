@@ -12,9 +12,11 @@
  * near-blank rule compares an exact integer n var with n norm / 16 and never lets a flat window through.
  *
  * Pipeline (all on one stream, no host round trip):
- *   integral_rows / integral_cols  int64 tables of J and J^2 ((h + 1) x (w + 1)), exact (for the F32 map; the
+ *   integral_rows / integral_cols  int64 tables of J and J^2 ((h + 1) x (w + 1)), exact: for the F32 map at steps 4 to
+ *                                 16, and at steps 1 and 2 where ncc_sums_in_map leaves the window sums to them (the
  *                                 tensor-core map's preparation (ncc_prep) sums the window bytes directly)
- *   ncc_map_f32 (or the tensor-core map in ncc_tc.cu)  per cell: best score and its corner
+ *   ncc_map_f32q (steps 1 and 2), ncc_map_f32 (steps 4 to 16), or the tensor-core map in ncc_tc.cu
+ *                                 per cell: best score and its corner
  *   ncc_top_ctas                  the eight best cells, value descending then cell index ascending (the reference's
  *                                 insertion order): a list a CTA, merged by the CTA that finishes last
  *   ncc_half_all (+ ncc_pick)     each candidate in half pixels within +-(2 step - 1) (or +-1) and one ring past it,
@@ -247,7 +249,13 @@ __global__ void __launch_bounds__(256) ncc_map_f32(const T *__restrict__ plane, 
  * feed eight products. Each corner's sums run in ncc_map_f32's order (rows, then columns in even and odd chains), so
  * the map is the same bits. A cell's best is a shared-memory atomicMax of (ordered score, inverted scan index): value
  * descending, then scan order, as `better`. A score that underflowed to -0 is taken as +0 first (adding +0), so the two
- * zeros tie as they compare in `better`. */
+ * zeros tie as they compare in `better`.
+ * With SUMS the window sums (sum J, sum J^2) come from the staged window too, in 64-bit integers, once the products are
+ * done and the template's shared memory is free: a thread a column keeps the column's sum over the template's rows,
+ * sliding down the corner rows, and writes eight corner rows of column sums at a time; each corner's thread adds its
+ * row's T_w column sums, and slides ST columns to the next corner. The integers are the integral images' box sums, so
+ * the scores are those of ncc_map_f32 bit for bit, and the search needs no integral images. Without SUMS they come from
+ * the integral images (ncc_sums_in_map decides). */
 #define NMQ_K 4       /* corners a thread */
 #define NMQ_CORNERS 32 /* corners a CTA's side */
 
@@ -256,9 +264,59 @@ __global__ void __launch_bounds__(256) ncc_map_f32(const T *__restrict__ plane, 
 __host__ __device__ inline int nmq_cols(int st, int tw) { return (NMQ_CORNERS - 1) * st + tw + 2; }
 __host__ __device__ inline int nmq_pitch(int st, int tw) { return nmq_cols(st, tw) | 1; }
 __host__ __device__ inline int nmq_rows(int st, int th) { return (NMQ_CORNERS - 1) * st + th; }
+/* the columns a CTA's corners' windows cover, and the floats of shared memory before the window: the template, later
+ * eight corner rows of column sums (two int64 tables) in the same place */
+__host__ __device__ inline int nmq_sum_cols(int st, int tw) { return (NMQ_CORNERS - 1) * st + tw; }
+__host__ __device__ inline int nmq_head(int st, int tw, int th)
+{
+    const int t = tw * th, c = 32 * nmq_sum_cols(st, tw);
+    return t > c ? t : c;
+}
 
-template <typename T, int ST>
-__global__ void __launch_bounds__(256) ncc_map_f32q(const T *__restrict__ plane, int pitch, const float *__restrict__ app,
+/* A staged value as the integral images take it, (long long) of the plane's value: in 32 bits where it is known to fit
+ * (bytes always; F32 planes when every value the CTA staged does), since the 64-bit conversion runs on the FP64 pipe. */
+template <bool W32>
+__device__ __forceinline__ long long nmq_int(float v)
+{
+    return W32 ? (long long)__float2int_rz(v) : __float2ll_rz(v);
+}
+
+/* Column t's sums (J, J^2) over rows 0 .. th - 1 of the staged window, as two chains. */
+template <bool W32>
+__device__ __forceinline__ void nmq_col_first(const float *s_img, int ip, int th, int t, long long &r1, long long &r2)
+{
+    long long a1 = 0, a2 = 0, b1 = 0, b2 = 0;
+    int i = 0;
+    for (; i + 1 < th; i += 2) {
+        const long long u = nmq_int<W32>(s_img[i * ip + t]), v = nmq_int<W32>(s_img[(i + 1) * ip + t]);
+        a1 += u;
+        a2 += u * u;
+        b1 += v;
+        b2 += v * v;
+    }
+    if (i < th) {
+        const long long u = nmq_int<W32>(s_img[i * ip + t]);
+        a1 += u;
+        a2 += u * u;
+    }
+    r1 = a1 + b1;
+    r2 = a2 + b2;
+}
+
+/* Column t's sums one window row down: row ro leaves, row ro + th enters. */
+template <bool W32>
+__device__ __forceinline__ void nmq_col_slide(const float *s_img, int ip, int th, int t, int ro, long long &r1, long long &r2)
+{
+    const long long vo = nmq_int<W32>(s_img[ro * ip + t]), vn = nmq_int<W32>(s_img[(ro + th) * ip + t]);
+    r1 += vn - vo;
+    r2 += vn * vn - vo * vo;
+}
+
+/* With SUMS, six CTAs an SM: the sums' phase would otherwise take the registers to 48 and small templates to five CTAs
+ * an SM. Without it no bound: the integral images' variant runs large templates, which shared memory already holds to
+ * one or two CTAs an SM, and the bound slowed it (96 x 96 by 4 %). */
+template <typename T, int ST, bool SUMS>
+__global__ void __launch_bounds__(256, SUMS ? 6 : 1) ncc_map_f32q(const T *__restrict__ plane, int pitch, const float *__restrict__ app,
                                                     NccPrm p, const long long *__restrict__ S1,
                                                     const long long *__restrict__ S2, int tp, int bcols,
                                                     float *__restrict__ map_v, int *__restrict__ map_x,
@@ -273,17 +331,20 @@ __global__ void __launch_bounds__(256) ncc_map_f32q(const T *__restrict__ plane,
     const int ccx0 = BC * bx, ccy0 = BC * by; /* the CTA's first cell column and row */
     const int X0 = p.x0 + ccx0 * NCC_CELL, Y0 = p.y0 + ccy0 * NCC_CELL;
     const int iw = nmq_cols(ST, p.tw), ip = nmq_pitch(ST, p.tw), ih = nmq_rows(ST, p.th);
-    float *s_app = sm, *s_img = sm + p.tw * p.th; /* tw th is a multiple of 8: s_img stays 16-byte aligned */
+    float *s_app = sm, *s_img = sm + nmq_head(ST, p.tw, p.th); /* a multiple of 8 floats: s_img stays 16-byte aligned */
     for (int i = threadIdx.x; i < p.tw * p.th; i += blockDim.x)
         s_app[i] = app[i];
+    bool small = true; /* every value this thread staged converts to the same integer in 32 bits */
     for (int i = threadIdx.x; i < iw * ih; i += blockDim.x) {
         const int r = i / iw, c = i - r * iw;
         const int yy = min(Y0 + r, p.h - 1), xx = min(X0 + c, p.w - 1);
-        s_img[r * ip + c] = (float)__ldg(plane + (size_t)yy * pitch + xx);
+        const float v = (float)__ldg(plane + (size_t)yy * pitch + xx);
+        s_img[r * ip + c] = v;
+        small = small && fabsf(v) < 2147483648.0f;
     }
     if (threadIdx.x < BC * BC)
         s_best[threadIdx.x] = 0ull;
-    __syncthreads();
+    const bool w32 = __syncthreads_and(small ? 1 : 0) != 0 || sizeof(T) == 1;
     constexpr int GROUPS = NMQ_CORNERS / NMQ_K;
     const int t = threadIdx.x;
     const int b = t / GROUPS, a0 = (t - b * GROUPS) * NMQ_K; /* corner row, first corner column in the CTA */
@@ -315,14 +376,80 @@ __global__ void __launch_bounds__(256) ncc_map_f32q(const T *__restrict__ plane,
             w[M - 1] = row[j + M + 1];
         }
     }
+    float sc[NMQ_K]; /* the corners' st, then their scores */
+#pragma unroll
+    for (int c = 0; c < NMQ_K; c++)
+        sc[c] = s0[c] + s1[c];
     const int y = Y0 + b * ST;
+    if constexpr (!SUMS) {
+        /* the window sums from the integral images */
+#pragma unroll
+        for (int c = 0; c < NMQ_K; c++) {
+            const int x = X0 + (a0 + c) * ST;
+            if (x <= p.x1 && y <= p.y1)
+                sc[c] = ncc_score(sc[c], box(S1, tp, x, y, p.tw, p.th), box(S2, tp, x, y, p.tw, p.th), p) + 0.0f;
+        }
+    } else {
+        /* the window sums, eight corner rows at a time, in the template's place */
+        __syncthreads();
+        const int ncols = nmq_sum_cols(ST, p.tw);
+        long long *cs1 = reinterpret_cast<long long *>(sm), *cs2 = cs1 + 8 * ncols;
+        long long r1 = 0, r2 = 0; /* thread t < ncols: column t's sums over the current corner row's window rows */
+        if (t < ncols) {
+            if (w32)
+                nmq_col_first<true>(s_img, ip, p.th, t, r1, r2);
+            else
+                nmq_col_first<false>(s_img, ip, p.th, t, r1, r2);
+        }
+#pragma unroll 1
+        for (int q = 0; q < NMQ_CORNERS / 8; q++) {
+            if (t < ncols)
+                for (int k = 0; k < 8; k++) {
+                    const int rb = 8 * q + k;
+                    if (rb > 0)
+#pragma unroll
+                        for (int u = 0; u < ST; u++) {
+                            if (w32)
+                                nmq_col_slide<true>(s_img, ip, p.th, t, (rb - 1) * ST + u, r1, r2);
+                            else
+                                nmq_col_slide<false>(s_img, ip, p.th, t, (rb - 1) * ST + u, r1, r2);
+                        }
+                    cs1[k * ncols + t] = r1;
+                    cs2[k * ncols + t] = r2;
+                }
+            __syncthreads();
+            if (b / 8 == q) {
+                const long long *c1 = cs1 + (b % 8) * ncols + a0 * ST, *c2 = cs2 + (b % 8) * ncols + a0 * ST;
+                long long x1 = 0, x2 = 0, y1 = 0, y2 = 0; /* two chains; tw is even */
+                for (int j = 0; j < p.tw; j += 2) {
+                    x1 += c1[j];
+                    x2 += c2[j];
+                    y1 += c1[j + 1];
+                    y2 += c2[j + 1];
+                }
+                x1 += y1;
+                x2 += y2;
+                sc[0] = ncc_score(sc[0], x1, x2, p) + 0.0f;
+#pragma unroll
+                for (int c = 1; c < NMQ_K; c++) {
+#pragma unroll
+                    for (int u = 0; u < ST; u++) {
+                        x1 += c1[(c - 1) * ST + p.tw + u] - c1[(c - 1) * ST + u];
+                        x2 += c2[(c - 1) * ST + p.tw + u] - c2[(c - 1) * ST + u];
+                    }
+                    sc[c] = ncc_score(sc[c], x1, x2, p) + 0.0f;
+                }
+            }
+            __syncthreads();
+        }
+    }
 #pragma unroll
     for (int c = 0; c < NMQ_K; c++) {
         const int a = a0 + c, x = X0 + a * ST;
         const int ccx = ccx0 + a / PER, ccy = ccy0 + b / PER;
         if (x > p.x1 || y > p.y1 || ccx >= p.ccols || ccy >= p.crows)
             continue;
-        const float v = ncc_score(s0[c] + s1[c], box(S1, tp, x, y, p.tw, p.th), box(S2, tp, x, y, p.tw, p.th), p) + 0.0f;
+        const float v = sc[c];
         const int key = (b % PER) * PER + a % PER;
         unsigned u = __float_as_uint(v);
         u = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
@@ -354,20 +481,31 @@ __global__ void __launch_bounds__(256) ncc_map_f32q(const T *__restrict__ plane,
     }
 }
 
-template <typename T, int ST>
+template <typename T, int ST, bool SUMS>
 static cudaError_t launch_map_f32q(const T *plane, int pitch, const float *app, const NccPrm &p, const NccScratch &s,
                                    cudaStream_t st)
 {
     constexpr int BC = NMQ_CORNERS * ST / NCC_CELL;
-    const size_t smem = sizeof(float) * ((size_t)p.tw * p.th + (size_t)nmq_pitch(ST, p.tw) * nmq_rows(ST, p.th));
-    cudaError_t e = cudaFuncSetAttribute(ncc_map_f32q<T, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const int head = SUMS ? nmq_head(ST, p.tw, p.th) : p.tw * p.th;
+    const size_t smem = sizeof(float) * ((size_t)head + (size_t)nmq_pitch(ST, p.tw) * nmq_rows(ST, p.th));
+    cudaError_t e = cudaFuncSetAttribute(ncc_map_f32q<T, ST, SUMS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess)
         return e;
     const int bcols = (p.ccols + BC - 1) / BC, brows = (p.crows + BC - 1) / BC;
-    ncc_map_f32q<T, ST><<<bcols * brows, NMQ_CORNERS * NMQ_CORNERS / NMQ_K, smem, st>>>(plane, pitch, app, p, s.S1, s.S2,
-                                                                                       s.tp, bcols, s.map_v, s.map_x,
-                                                                                       s.map_y);
+    ncc_map_f32q<T, ST, SUMS><<<bcols * brows, NMQ_CORNERS * NMQ_CORNERS / NMQ_K, smem, st>>>(
+        plane, pitch, app, p, s.S1, s.S2, s.tp, bcols, s.map_v, s.map_x, s.map_y);
     return cudaGetLastError();
+}
+
+/* Where the F32 map at steps 1 and 2 takes its window sums. In the map kernel they cost a serial phase after the
+ * products, which other CTAs' products hide while enough CTAs share an SM: up to 64 x 64 templates (measured at 1080p:
+ * as fast or faster at every size up to there, 2-6 % slower at 96 x 96 and 128 x 128, where shared memory leaves one
+ * or two CTAs an SM). The integral images cost two passes over the whole plane, whatever the window, so a window under
+ * half the plane takes the in-kernel sums at any template size. */
+static bool ncc_sums_in_map(const NccPrm &p)
+{
+    const long long win = (long long)(p.x1 - p.x0 + 1) * (long long)(p.y1 - p.y0 + 1);
+    return p.tw * p.th <= 64 * 64 || 2 * win < (long long)p.w * (long long)p.h;
 }
 
 /* ---- the eight best cells ---- */
@@ -697,11 +835,14 @@ static cudaError_t launch_all(const T *plane, int pitch, const float *app, const
     const int cells = p.ccols * p.crows;
     cudaError_t e = cudaSuccess;
     if (map_kind == VTG_NCC_F32) {
-        /* the F32 map takes its window sums from the integral images; the tensor-core map's prep sums the bytes */
-        integral_rows<T><<<(p.h + 1 + 7) / 8, 256, 0, st>>>(plane, pitch, p.w, p.h, s.S1, s.S2, s.tp);
-        integral_cols<<<(p.w + 1 + IC_COLS - 1) / IC_COLS, IC_COLS * IC_SEGS, 0, st>>>(p.w, p.h, s.S1, s.S2, s.tp);
-        /* steps 1 and 2: four corners a thread; the other steps one corner a thread, a CTA a cell */
+        /* steps 1 and 2: four corners a thread, the window sums from the staged window; the other steps one corner a
+         * thread, a CTA a cell, the window sums from the integral images (the tensor-core map's prep sums the bytes) */
         const bool quad = p.step == 1 || p.step == 2;
+        const bool sums = quad && ncc_sums_in_map(p);
+        if (!sums) {
+            integral_rows<T><<<(p.h + 1 + 7) / 8, 256, 0, st>>>(plane, pitch, p.w, p.h, s.S1, s.S2, s.tp);
+            integral_cols<<<(p.w + 1 + IC_COLS - 1) / IC_COLS, IC_COLS * IC_SEGS, 0, st>>>(p.w, p.h, s.S1, s.S2, s.tp);
+        }
         const size_t smem = sizeof(float) * ((size_t)p.tw * p.th + (size_t)(NCC_CELL + p.tw) * (NCC_CELL + p.th));
         if (!quad && (e = cudaFuncSetAttribute(ncc_map_f32<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
                          cudaSuccess)
@@ -709,7 +850,10 @@ static cudaError_t launch_all(const T *plane, int pitch, const float *app, const
         if (s.map_ev0 && (e = cudaEventRecord(s.map_ev0, st)) != cudaSuccess)
             return e;
         if (quad)
-            e = p.step == 1 ? launch_map_f32q<T, 1>(plane, pitch, app, p, s, st) : launch_map_f32q<T, 2>(plane, pitch, app, p, s, st);
+            e = p.step == 1 ? (sums ? launch_map_f32q<T, 1, true>(plane, pitch, app, p, s, st)
+                                    : launch_map_f32q<T, 1, false>(plane, pitch, app, p, s, st))
+                            : (sums ? launch_map_f32q<T, 2, true>(plane, pitch, app, p, s, st)
+                                    : launch_map_f32q<T, 2, false>(plane, pitch, app, p, s, st));
         else
             ncc_map_f32<T><<<cells, 256, smem, st>>>(plane, pitch, app, p, s.S1, s.S2, s.tp, s.map_v, s.map_x, s.map_y);
         if (e != cudaSuccess)

@@ -95,29 +95,33 @@ def test_txt_templates_against_fp64_oracle(vtg_lib, ctx, torch_cuda, size):
     s.close()
 
 
-@pytest.mark.parametrize("tw,th,step,window,plane_type", [
-    (32, 21, 1, (7, 250, 3, 131), "u8"),     # 16 x 9 cells: a half-filled last row of 2 x 2 blocks
-    (32, 21, 2, (5, 283, 9, 190), "f32"),    # 18 x 12 cells: 4 x 4 blocks, two columns of the last one filled
-    (24, 7, 2, (1, 320, 1, 240), "u8"),      # 19 x 15 cells
-    (128, 128, 1, (1, 320, 1, 240), "u8"),   # the largest template: the most shared memory a block takes
-    (128, 128, 2, (3, 320, 2, 240), "f32"),
-    (8, 1, 1, (2, 301, 1, 200), "u8"),       # the smallest template
+@pytest.mark.parametrize("tw,th,step,window,plane_type,size", [
+    (32, 21, 1, (7, 250, 3, 131), "u8", (320, 240)),     # 16 x 9 cells: a half-filled last row of 2 x 2 blocks
+    (32, 21, 2, (5, 283, 9, 190), "f32", (320, 240)),    # 18 x 12 cells: 4 x 4 blocks, two columns of the last one
+    (24, 7, 2, (1, 320, 1, 240), "u8", (320, 240)),      # 19 x 15 cells
+    (128, 128, 1, (1, 320, 1, 240), "u8", (320, 240)),   # the largest template: the most shared memory a block takes
+    (128, 128, 2, (3, 320, 2, 240), "f32", (320, 240)),
+    (8, 1, 1, (2, 301, 1, 200), "u8", (320, 240)),       # the smallest template
+    (72, 72, 1, (1, 640, 1, 480), "u8", (640, 480)),     # over 64 x 64 and most of the plane: integral images
+    (80, 64, 2, (3, 640, 5, 480), "f32", (640, 480)),
 ])
-def test_map_blocks_against_fp64_oracle(vtg_lib, ctx, torch_cuda, tw, th, step, window, plane_type):
+def test_map_blocks_against_fp64_oracle(vtg_lib, ctx, torch_cuda, tw, th, step, window, plane_type, size):
     """The F32 map at the reference's steps (1 and 2) scores 32 x 32 corners a CTA; windows whose cells fill its last
-    blocks only in part, at both plane types, against the FP64 oracle's map and search."""
-    frame = S.noise_frame(320, 240, seed=31 + tw + step)
+    blocks only in part, at both plane types, with the window sums from the staged window and (a template over 64 x 64
+    searching most of the plane) from the integral images, against the FP64 oracle's map and search."""
+    W, H = size
+    frame = S.noise_frame(W, H, seed=31 + tw + step)
     plane = frame.astype(np.float32)
     rng = np.random.default_rng(tw * 7 + th + step)
-    tx, ty = int(rng.integers(window[0], min(window[1], 320 - tw - 2) + 1)), int(rng.integers(window[2], min(window[3], 240 - th - 2) + 1))
+    tx, ty = int(rng.integers(window[0], min(window[1], W - tw - 2) + 1)), int(rng.integers(window[2], min(window[3], H - th - 2) + 1))
     patch = plane[ty:ty + th, tx:tx + tw]
     app = (patch - np.float32(patch.mean(dtype=np.float64))).astype(np.float32)
     norm = float(np.sum(app.astype(np.float64) ** 2))
     dp = _dev(torch_cuda, frame if plane_type == "u8" else plane)
     pt = vtg_lib.PLANE_U8 if plane_type == "u8" else vtg_lib.PLANE_F32
-    s = vtg_lib.Search(ctx, 320, 240)
+    s = vtg_lib.Search(ctx, W, H)
     s.template(app, norm)
-    f, mv, mx, my = s.run(dp.data_ptr(), 320, 240, 320, pt, *window, step, want_map=True)
+    f, mv, mx, my = s.run(dp.data_ptr(), W, H, W, pt, *window, step, want_map=True)
     ref, rv, rx, ry = O.search_slot(plane, app, norm, *window, step, mode=O.F64)
     n = f["cells"]
     assert n > 0
