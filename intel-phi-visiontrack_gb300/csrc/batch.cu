@@ -28,7 +28,7 @@
 
 struct BatchSlot {
     PyrJob *d_pyr;
-    int *d_tiles;   /* [VTG_MAX_LEVELS - 1][max_jobs + 1] tile offsets per level */
+    int *d_tiles;   /* [VTG_MAX_LEVELS][max_jobs + 1] tile offsets per level launch, the fused launch's last */
     LkJob *d_lk;
     int *d_items;   /* [max_jobs + 1] */
     int *d_counter;
@@ -73,7 +73,7 @@ static size_t up256(size_t n) { return (n + 255) & ~(size_t)255; }
 
 static size_t slot_bytes(int max_jobs)
 {
-    return up256(sizeof(PyrJob) * (size_t)max_jobs) + up256(sizeof(int) * (size_t)(VTG_MAX_LEVELS - 1) * (max_jobs + 1)) +
+    return up256(sizeof(PyrJob) * (size_t)max_jobs) + up256(sizeof(int) * (size_t)VTG_MAX_LEVELS * (max_jobs + 1)) +
            up256(sizeof(LkJob) * (size_t)max_jobs) + up256(sizeof(int) * (size_t)(max_jobs + 1)) + 256;
 }
 
@@ -125,7 +125,7 @@ extern "C" int vtg_batch_create(vtg_ctx *ctx, int max_jobs, vtg_batch **out)
         sl.d_pyr = (PyrJob *)m;
         m += up256(sizeof(PyrJob) * (size_t)max_jobs);
         sl.d_tiles = (int *)m;
-        m += up256(sizeof(int) * (size_t)(VTG_MAX_LEVELS - 1) * (max_jobs + 1));
+        m += up256(sizeof(int) * (size_t)VTG_MAX_LEVELS * (max_jobs + 1));
         sl.d_lk = (LkJob *)m;
         m += up256(sizeof(LkJob) * (size_t)max_jobs);
         sl.d_items = (int *)m;
@@ -181,7 +181,7 @@ extern "C" int vtg_batch_prepare(vtg_batch *b, int slot, int n, vtg_tracker *con
     BatchSlot &sl = b->slot[slot];
     std::vector<PyrJob> pj((size_t)n);
     std::vector<LkJob> lj((size_t)n);
-    std::vector<int> tiles((size_t)(VTG_MAX_LEVELS - 1) * (n + 1), 0);
+    std::vector<int> tiles((size_t)VTG_MAX_LEVELS * (n + 1), 0);
     std::vector<int> items((size_t)n + 1, 0);
     sl.h_src.clear();
     sl.h_dst.clear();
@@ -273,6 +273,17 @@ extern "C" int vtg_batch_prepare(vtg_batch *b, int slot, int n, vtg_tracker *con
         row[n] = acc;
         sl.tiles[L - 1] = acc;
     }
+    {
+        /* the fused launch's blocks (levels 0 .. 3 at once), the last row */
+        int acc = 0;
+        int *row = tiles.data() + (size_t)(VTG_MAX_LEVELS - 1) * (n + 1);
+        for (int j = 0; j < n; j++) {
+            row[j] = acc;
+            acc += vtg_pyr_fused_tiles(pj[(size_t)j].w, pj[(size_t)j].h);
+        }
+        row[n] = acc;
+        sl.tiles[VTG_MAX_LEVELS - 1] = acc;
+    }
     int acc = 0, cells = 0;
     const int chunk = std::max(1, b->tune.chunk), tiled = b->tune.tiled;
     for (int j = 0; j < n; j++) {
@@ -313,7 +324,8 @@ static int launch_slot(vtg_batch *b, BatchSlot &sl, cudaStream_t s, int nwait = 
         CU(vtg_launch_build_input(in.src, in.stride, in.w, in.h, in.opts, in.mm, in.l0, in.pitch0, s));
     /* the pyramid's levels and the LK launch as a chain of programmatic dependents: each starts as the one before
      * drains; the last pyramid launch zeroes the LK launch's work counter */
-    CU(vtg_launch_pyramid_batch(sl.d_pyr, sl.d_tiles, sl.tiles, sl.njobs, sl.max_levels, s, sl.d_counter, true));
+    CU(vtg_launch_pyramid_batch(sl.d_pyr, sl.d_tiles, sl.tiles, sl.njobs, sl.max_levels, s, sl.d_counter, true,
+                                sl.inputs.empty()));
     /* what only the LK launch must wait for (earlier reads of the result buffers it writes) */
     for (int k = 0; k < nwait_lk; k++)
         CU(cudaStreamWaitEvent(s, (cudaEvent_t)wait_lk[k], 0));
@@ -564,7 +576,8 @@ extern "C" int vtg_batch_profile(vtg_batch *b, int slot, int reps, float *pyr_ms
                                  (size_t)sl.h_h[k], cudaMemcpyHostToDevice, b->stream));
         for (const BatchSlot::Input &in : sl.inputs)
             CU(vtg_launch_build_input(in.src, in.stride, in.w, in.h, in.opts, in.mm, in.l0, in.pitch0, b->stream));
-        CU(vtg_launch_pyramid_batch(sl.d_pyr, sl.d_tiles, sl.tiles, sl.njobs, sl.max_levels, b->stream));
+        CU(vtg_launch_pyramid_batch(sl.d_pyr, sl.d_tiles, sl.tiles, sl.njobs, sl.max_levels, b->stream, nullptr, false,
+                                    sl.inputs.empty()));
         CU(cudaMemsetAsync(sl.d_counter, 0, sizeof(int), b->stream));
         CU(cudaEventRecord(e[1], b->stream));
         CU(vtg_launch_lk_batch(sl.d_lk, sl.d_items, sl.njobs, sl.items, sl.prm, t, b->sms, sl.d_counter, b->stream));

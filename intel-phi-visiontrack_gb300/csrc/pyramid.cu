@@ -6,10 +6,11 @@
  * reading a replicated border. Every value is a whole number below 2^24, so the reference's F32 sums are exact; here
  * they are int32 sums, the border is a clamped index, and the results are the same bits.
  *
- * One launch per level: the first reads the bytes once from HBM and writes level 0 (byte x 64) and level 1 from the
- * same shared-memory tile; each further launch reduces the level below it (L2-resident at these sizes). A CTA of 256
- * threads makes a 64 x 16 tile of its output level from a 132 x 36 source tile staged in shared memory: the vertical
- * pass runs over the staged rows, the horizontal pass over the vertical sums, as the reference's vert5 / shift8 do. */
+ * Levels 0 to 3 in one launch (pyr_fused_kernel, pyr_fused_batch_kernel): a CTA reads its block's bytes once and
+ * reduces level by level in shared memory, halos included (below). Levels from 4 on, and level 1 when level 0 came
+ * from tk_build's input steps, take one launch per level (pyr_reduce_kernel, pyr_batch_kernel): a CTA of 256 threads
+ * makes a 64 x 16 tile of its output level from a 132 x 36 source tile staged in shared memory, the vertical pass over
+ * the staged rows, the horizontal pass over the vertical sums, as the reference's vert5 / shift8 do. */
 #include <math.h>
 
 #include "vtg_internal.cuh"
@@ -267,6 +268,261 @@ __global__ void __launch_bounds__(256) pyr_batch_kernel(const PyrJob *__restrict
                            j.pitch[level], ox, oy, s_t.b, s_t.f, s_v);
 }
 
+/* ---- levels 0 to 3 from the bytes in one launch ----
+ *
+ * A CTA owns a 128 x 64 block of level 0 and the blocks of levels 1, 2 and 3 under it (64 x 32, 32 x 16, 16 x 8). It
+ * stages the bytes the block's level 3 depends on (rows Y0 - 14 .. Y0 + 70, columns X0 - 16 .. X0 + 143, each clamped
+ * into the frame: the reference's replicated border), writes level 0 from them, and reduces in shared memory: level 1
+ * over 73 x 41 values (the block and the halo level 2 needs), level 2 over 35 x 19, level 3 over its 16 x 8. A level's
+ * reduce reads the level below at the reference's clamped indices, which always fall inside the computed halo, so the
+ * values outside a level's plane that the halo holds are never read. Every sum is an exact integer: (sum of the bytes'
+ * taps + 2) >> 2 for level 1 ((64 h + 128) >> 8 of the Q6 values), (h + 128) >> 8 above. Level 1 is then never read
+ * back from memory, and three launches become one. */
+#define FP_X 128 /* a CTA's level-0 block */
+#define FP_Y 64
+#define FB_R 85  /* staged byte rows: Y0 - 14 .. Y0 + 70 */
+#define FB_C 160 /* staged byte columns: X0 - 16 .. X0 + 143 (16-byte chunks) */
+#define F1_R 41  /* level 1 computed: rows Y0 / 2 - 6 .. Y0 / 2 + 34 */
+#define F1_C 73  /*                   columns X0 / 2 - 6 .. X0 / 2 + 66 */
+#define F1_P 76
+#define F2_R 19  /* level 2: rows Y0 / 4 - 2 .. Y0 / 4 + 16 */
+#define F2_C 35  /*          columns X0 / 4 - 2 .. X0 / 4 + 32 */
+#define F2_P 36
+#define F3_R 8   /* level 3: the block, rows Y0 / 8 .. + 7 */
+#define F3_C 16  /*          columns X0 / 8 .. + 15 */
+
+struct FusedSmem {
+    __align__(16) uint8_t b[FB_R][FB_C];   /* the bytes */
+    __align__(16) uint16_t v1[F1_R][FB_C]; /* level 1's vertical sums of the bytes (at most 16 x 255) */
+    __align__(16) uint16_t l1[F1_R][F1_P]; /* level 1 (at most 16320) */
+    __align__(16) int v2[F2_R][F1_P];      /* level 2's vertical sums of level 1 */
+    __align__(16) uint16_t l2[F2_R][F2_P]; /* level 2 */
+    __align__(16) int v3[F3_R][F2_P];      /* level 3's vertical sums of level 2 */
+};
+
+/* One frame of a fused launch: the bytes (rows `stride` apart), and levels 0 .. min(levels, 4) - 1. */
+struct FusedFrame {
+    const uint8_t *src;
+    int stride, w, h, levels;
+    float *lv[4];
+    int pitch[4];
+};
+
+__device__ __forceinline__ int tap5(int a, int b, int c, int d, int e) { return a + e + 4 * (b + d) + 6 * c; }
+
+/* A block is interior when every byte it stages lies inside the frame. Then no index of any level needs a clamp, and
+ * every write of its blocks lies inside their planes. */
+__device__ __forceinline__ bool fused_interior(const FusedFrame &f, int X0, int Y0)
+{
+    return X0 >= 16 && X0 + 144 <= f.w && Y0 >= 14 && Y0 + 71 <= f.h;
+}
+
+template <bool EDGE>
+__device__ void fused_block(const FusedFrame &f, int X0, int Y0, FusedSmem &S)
+{
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const int w = f.w, h = f.h;
+    const int w1 = (w + 1) / 2, h1 = (h + 1) / 2, w2 = (w1 + 1) / 2, h2 = (h1 + 1) / 2, w3 = (w2 + 1) / 2,
+              h3 = (h2 + 1) / 2;
+    const bool vec = (((uintptr_t)f.src | (uintptr_t)f.stride) & 15) == 0;
+    /* the bytes: staged row r is frame row Y0 - 14 + r, staged column c frame column X0 - 16 + c, both clamped */
+    for (int i = tid; i < FB_R * (FB_C / 16); i += nt) {
+        const int r = i / (FB_C / 16), k = i - r * (FB_C / 16);
+        const int gy = EDGE ? min(max(Y0 - 14 + r, 0), h - 1) : Y0 - 14 + r, gx = X0 - 16 + 16 * k;
+        const uint8_t *row = f.src + (size_t)gy * f.stride;
+        uint4 v;
+        if (vec && (!EDGE || (gx >= 0 && gx + 16 <= w))) {
+            v = __ldg(reinterpret_cast<const uint4 *>(row + gx));
+        } else {
+            uint32_t q[4];
+#pragma unroll
+            for (int a = 0; a < 4; a++) {
+                uint32_t x = 0;
+#pragma unroll
+                for (int e = 0; e < 4; e++)
+                    x |= (uint32_t)__ldg(row + min(max(gx + 4 * a + e, 0), w - 1)) << (8 * e);
+                q[a] = x;
+            }
+            v = make_uint4(q[0], q[1], q[2], q[3]);
+        }
+        *reinterpret_cast<uint4 *>(&S.b[r][16 * k]) = v;
+    }
+    __syncthreads();
+    /* level 0: the block's rows (staged 14 ..) and columns (staged 16 ..), four a thread */
+    for (int i = tid; i < FP_Y * (FP_X / 4); i += nt) {
+        const int r = i / (FP_X / 4), g = i - r * (FP_X / 4);
+        const int gy = Y0 + r, gx = X0 + 4 * g;
+        if (EDGE && (gy >= h || gx >= w))
+            continue;
+        const uint32_t q = *reinterpret_cast<const uint32_t *>(&S.b[r + 14][16 + 4 * g]);
+        const float4 o = make_float4(q6_of(q, 0), q6_of(q, 1), q6_of(q, 2), q6_of(q, 3));
+        float *d = f.lv[0] + (size_t)gy * f.pitch[0] + gx;
+        if (!EDGE || gx + 4 <= w) {
+            *reinterpret_cast<float4 *>(d) = o;
+        } else {
+            d[0] = o.x;
+            if (gx + 1 < w)
+                d[1] = o.y;
+            if (gx + 2 < w)
+                d[2] = o.z;
+        }
+    }
+    if (f.levels < 2)
+        return;
+    /* level 1's vertical sums: local row y (frame row of level 1 Y0 / 2 - 6 + y) takes staged rows 2 y .. 2 y + 4;
+     * four columns a thread, even and odd bytes in the 16-bit halves of two words (no half carries: at most 4080) */
+    for (int i = tid; i < F1_R * (FB_C / 4); i += nt) {
+        const int y = i / (FB_C / 4), g = i - y * (FB_C / 4);
+        uint32_t e[5], o[5];
+#pragma unroll
+        for (int t = 0; t < 5; t++) {
+            const uint32_t q = *reinterpret_cast<const uint32_t *>(&S.b[2 * y + t][4 * g]);
+            e[t] = q & 0x00FF00FFu;
+            o[t] = (q >> 8) & 0x00FF00FFu;
+        }
+        const uint32_t E = e[0] + e[4] + 4u * (e[1] + e[3]) + 6u * e[2];
+        const uint32_t O = o[0] + o[4] + 4u * (o[1] + o[3]) + 6u * o[2];
+        *reinterpret_cast<uint2 *>(&S.v1[y][4 * g]) = make_uint2((E & 0xFFFFu) | (O << 16), (E >> 16) | (O & 0xFFFF0000u));
+    }
+    __syncthreads();
+    /* level 1: local column x (frame column X0 / 2 - 6 + x) centres on staged column 2 x + 4. Two columns a thread in
+     * the halves of one word: with w_k = v1 columns 2 x + 2 + 2 k and 2 x + 3 + 2 k, column x takes (w_0 lo, w_0 hi,
+     * w_1 lo, w_1 hi, w_2 lo) and column x + 1 the same one word on. A sum is at most 16 x 4080 = 65280 a half, and
+     * (h + 2) >> 2 at most 16320, so the mask drops exactly what the high half shifts into the low one. */
+    for (int i = tid; i < F1_R * ((F1_C + 1) / 2); i += nt) {
+        const int y = i / ((F1_C + 1) / 2), x = 2 * (i - y * ((F1_C + 1) / 2));
+        const uint32_t *v = reinterpret_cast<const uint32_t *>(&S.v1[y][2 * x + 2]);
+        const uint32_t w0 = v[0], w1 = v[1], w2 = v[2], w3 = v[3];
+        const uint32_t L0 = __byte_perm(w0, w1, 0x5410), H0 = __byte_perm(w0, w1, 0x7632);
+        const uint32_t L1 = __byte_perm(w1, w2, 0x5410), H1 = __byte_perm(w1, w2, 0x7632);
+        const uint32_t L2 = __byte_perm(w2, w3, 0x5410);
+        const uint32_t hs = L0 + L2 + 4u * (H0 + H1) + 6u * L1;
+        *reinterpret_cast<uint32_t *>(&S.l1[y][x]) = ((hs + 0x00020002u) >> 2) & 0x3FFF3FFFu;
+    }
+    __syncthreads();
+    /* level 1's block (local rows and columns 6 ..), four columns a thread */
+    const int o1x = X0 / 2 - 6, o1y = Y0 / 2 - 6; /* level 1's local origin */
+    for (int i = tid; i < (FP_Y / 2) * (FP_X / 8); i += nt) {
+        const int r = i / (FP_X / 8), c = 4 * (i - r * (FP_X / 8));
+        const int gy = Y0 / 2 + r, gx = X0 / 2 + c;
+        if (EDGE && (gy >= h1 || gx >= w1))
+            continue;
+        const uint32_t a = *reinterpret_cast<const uint32_t *>(&S.l1[r + 6][c + 6]);
+        const uint32_t b = *reinterpret_cast<const uint32_t *>(&S.l1[r + 6][c + 8]);
+        const float4 o = make_float4(small_int_to_float((int)(a & 0xFFFFu)), small_int_to_float((int)(a >> 16)),
+                                     small_int_to_float((int)(b & 0xFFFFu)), small_int_to_float((int)(b >> 16)));
+        float *d = f.lv[1] + (size_t)gy * f.pitch[1] + gx;
+        if (!EDGE || gx + 4 <= w1) {
+            *reinterpret_cast<float4 *>(d) = o;
+        } else {
+            d[0] = o.x;
+            if (gx + 1 < w1)
+                d[1] = o.y;
+            if (gx + 2 < w1)
+                d[2] = o.z;
+        }
+    }
+    if (f.levels < 3)
+        return;
+    /* level 2's vertical sums over level 1's (clamped) rows */
+    const int o2x = X0 / 4 - 2, o2y = Y0 / 4 - 2; /* level 2's local origin */
+    for (int i = tid; i < F2_R * F1_C; i += nt) {
+        const int y = i / F1_C, x = i - y * F1_C;
+        int a[5];
+#pragma unroll
+        for (int t = 0; t < 5; t++)
+            a[t] = S.l1[EDGE ? min(max(2 * (o2y + y) - 2 + t, 0), h1 - 1) - o1y : 2 * y + t][x];
+        S.v2[y][x] = tap5(a[0], a[1], a[2], a[3], a[4]);
+    }
+    __syncthreads();
+    for (int i = tid; i < F2_R * F2_C; i += nt) {
+        const int y = i / F2_C, x = i - y * F2_C;
+        int a[5];
+#pragma unroll
+        for (int t = 0; t < 5; t++)
+            a[t] = S.v2[y][EDGE ? min(max(2 * (o2x + x) - 2 + t, 0), w1 - 1) - o1x : 2 * x + t];
+        S.l2[y][x] = (uint16_t)((tap5(a[0], a[1], a[2], a[3], a[4]) + 128) >> 8);
+    }
+    __syncthreads();
+    for (int i = tid; i < (FP_Y / 4) * (FP_X / 4); i += nt) {
+        const int r = i / (FP_X / 4), c = i - r * (FP_X / 4);
+        const int gy = Y0 / 4 + r, gx = X0 / 4 + c;
+        if (!EDGE || (gy < h2 && gx < w2))
+            f.lv[2][(size_t)gy * f.pitch[2] + gx] = small_int_to_float(S.l2[r + 2][c + 2]);
+    }
+    if (f.levels < 4)
+        return;
+    for (int i = tid; i < F3_R * F2_C; i += nt) {
+        const int y = i / F2_C, x = i - y * F2_C;
+        int a[5];
+#pragma unroll
+        for (int t = 0; t < 5; t++)
+            a[t] = S.l2[EDGE ? min(max(2 * (Y0 / 8 + y) - 2 + t, 0), h2 - 1) - o2y : 2 * y + t][x];
+        S.v3[y][x] = tap5(a[0], a[1], a[2], a[3], a[4]);
+    }
+    __syncthreads();
+    for (int i = tid; i < F3_R * F3_C; i += nt) {
+        const int y = i / F3_C, x = i - y * F3_C;
+        const int gy = Y0 / 8 + y, gx = X0 / 8 + x;
+        if (EDGE && (gy >= h3 || gx >= w3))
+            continue;
+        int a[5];
+#pragma unroll
+        for (int t = 0; t < 5; t++)
+            a[t] = S.v3[y][EDGE ? min(max(2 * gx - 2 + t, 0), w2 - 1) - o2x : 2 * x + t];
+        f.lv[3][(size_t)gy * f.pitch[3] + gx] = small_int_to_float((tap5(a[0], a[1], a[2], a[3], a[4]) + 128) >> 8);
+    }
+}
+
+__device__ __forceinline__ void fused_any(const FusedFrame &f, int bx, int by, FusedSmem &S)
+{
+    const int X0 = bx * FP_X, Y0 = by * FP_Y;
+    if (fused_interior(f, X0, Y0))
+        fused_block<false>(f, X0, Y0, S);
+    else
+        fused_block<true>(f, X0, Y0, S);
+}
+
+__global__ void __launch_bounds__(256) pyr_fused_kernel(FusedFrame f)
+{
+    __shared__ FusedSmem S;
+    fused_any(f, blockIdx.x, blockIdx.y, S);
+}
+
+/* Many frames: the launch's blocks are every job's blocks back to back; a CTA finds its job by binary search. */
+__global__ void __launch_bounds__(256) pyr_fused_batch_kernel(const PyrJob *__restrict__ jobs, const int *__restrict__ start,
+                                                              int njobs, int *__restrict__ reset)
+{
+    __shared__ FusedSmem S;
+    if (reset && blockIdx.x == 0 && threadIdx.x == 0)
+        *reset = 0;
+    const int b = blockIdx.x;
+    int lo = 0, hi = njobs; /* start[lo] <= b < start[hi] */
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(start + mid) <= b)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    const PyrJob &j = jobs[lo];
+    FusedFrame f;
+    f.src = j.src;
+    f.stride = j.stride;
+    f.w = j.w;
+    f.h = j.h;
+    f.levels = j.levels;
+#pragma unroll
+    for (int L = 0; L < 4; L++) {
+        f.lv[L] = L < j.levels ? j.lv[L] : nullptr;
+        f.pitch[L] = L < j.levels ? j.pitch[L] : 0;
+    }
+    const int t = b - __ldg(start + lo), bcols = (j.w + FP_X - 1) / FP_X;
+    fused_any(f, t % bcols, t / bcols, S);
+}
+
+int vtg_pyr_fused_tiles(int w, int h) { return ((w + FP_X - 1) / FP_X) * ((h + FP_Y - 1) / FP_Y); }
+
 /* ---- tk_build's optional input steps (src/kern/track.c:600-622) ----
  *
  * CONTRAST: the min and max of the frame (img_minmax_ref, img_ref.c:57-71), the gain 16320 / (max - min) and the offset
@@ -501,14 +757,22 @@ int vtg_pyr_tiles(int w, int h, int level)
 }
 
 cudaError_t vtg_launch_pyramid_batch(const PyrJob *jobs, const int *starts, const int *tiles_total, int njobs,
-                                     int max_levels, cudaStream_t s, int *reset, bool pdl)
+                                     int max_levels, cudaStream_t s, int *reset, bool pdl, bool fused)
 {
     const int top = max_levels > 1 ? max_levels : 2;
     int last = 1; /* the last level launched (level 1's launch always has tiles) */
-    for (int L = 1; L < top; L++)
+    for (int L = fused ? 4 : 1; L < top; L++)
         if (tiles_total[L - 1] > 0)
             last = L;
-    for (int L = 1; L < top; L++) {
+    if (fused) {
+        /* levels 0 .. 3 of every job in one launch (row VTG_MAX_LEVELS - 1 of the tables), then levels 4 .. */
+        const cudaError_t e = vtg_launch_k(pyr_fused_batch_kernel, tiles_total[VTG_MAX_LEVELS - 1], 256, 0, s, false,
+                                           jobs, (const int *)(starts + (size_t)(VTG_MAX_LEVELS - 1) * (njobs + 1)),
+                                           njobs, last < 4 ? reset : (int *)nullptr);
+        if (e != cudaSuccess)
+            return e;
+    }
+    for (int L = fused ? 4 : 1; L < top; L++) {
         const int tiles = tiles_total[L - 1];
         if (tiles <= 0)
             continue;
@@ -525,14 +789,24 @@ cudaError_t vtg_launch_pyramid_batch(const PyrJob *jobs, const int *starts, cons
 cudaError_t vtg_launch_pyramid(const uint8_t *frame, int stride, int w, int h, float *const *levels, const int *pitches,
                                int nlevels, cudaStream_t s)
 {
-    /* Level 0 and level 1 from the bytes. */
-    int sw = (w + 1) / 2, sh = (h + 1) / 2;
-    {
-        const dim3 grid((sw + RT_X - 1) / RT_X, (sh + RT_Y - 1) / RT_Y);
-        pyr_reduce_kernel<true><<<grid, 256, 0, s>>>(frame, w, h, stride, levels[0], pitches[0],
-                                                     nlevels > 1 ? levels[1] : nullptr, sw, sh, nlevels > 1 ? pitches[1] : 0);
+    /* Levels 0 .. 3 from the bytes in one launch, then one launch per further level. */
+    FusedFrame f;
+    f.src = frame;
+    f.stride = stride;
+    f.w = w;
+    f.h = h;
+    f.levels = nlevels;
+    for (int L = 0; L < 4; L++) {
+        f.lv[L] = L < nlevels ? levels[L] : nullptr;
+        f.pitch[L] = L < nlevels ? pitches[L] : 0;
     }
-    for (int L = 2; L < nlevels; L++) {
+    pyr_fused_kernel<<<dim3((w + FP_X - 1) / FP_X, (h + FP_Y - 1) / FP_Y), 256, 0, s>>>(f);
+    int sw = w, sh = h;
+    for (int L = 1; L < 4 && L < nlevels; L++) {
+        sw = (sw + 1) / 2;
+        sh = (sh + 1) / 2;
+    }
+    for (int L = 4; L < nlevels; L++) {
         const int dw = (sw + 1) / 2, dh = (sh + 1) / 2;
         const dim3 grid((dw + RT_X - 1) / RT_X, (dh + RT_Y - 1) / RT_Y);
         pyr_reduce_kernel<false><<<grid, 256, 0, s>>>(levels[L - 1], sw, sh, pitches[L - 1], nullptr, 0, levels[L], dw, dh,

@@ -98,12 +98,17 @@ cudaError_t vtg_launch_pyramid_opts(const uint8_t *frame, int stride, int w, int
 cudaError_t vtg_launch_cells(const DevPyr *I, const DevPyr *J, int top, const LkPrm &p, const CellGrid &g, int base_w,
                              int base_h, vtg_lk_out *out, vtg_cell *cells, cudaStream_t s);
 int vtg_pyr_tiles(int w, int h, int level);
+/* Blocks of the fused launch that makes levels 0 .. 3 of a w x h frame at once. */
+int vtg_pyr_fused_tiles(int w, int h);
 /* The batched pyramid: one launch per level for all jobs. With pdl, each level after the first is launched as a
  * programmatic dependent of the one before (it starts as the previous level drains and waits in griddepcontrol.wait
  * until that level's writes are visible). reset (may be NULL): a device int the last launch sets to 0, for a
- * programmatic dependent launched after it (the LK launch's work counter). */
+ * programmatic dependent launched after it (the LK launch's work counter). fused (no job with build options): levels 0
+ * .. 3 of every job in one launch, whose tiles are row VTG_MAX_LEVELS - 1 of starts / tiles_total, then a launch per
+ * further level. */
 cudaError_t vtg_launch_pyramid_batch(const PyrJob *jobs, const int *starts, const int *tiles_total, int njobs,
-                                     int max_levels, cudaStream_t s, int *reset = nullptr, bool pdl = false);
+                                     int max_levels, cudaStream_t s, int *reset = nullptr, bool pdl = false,
+                                     bool fused = false);
 /* Batched LK over jobs: items of `chunk` cells, job j's items from item_start[j]; `counter` must be 0 at launch.
  * count (NULL, or four device words): adds the launch's template builds, residual passes, window passes and
  * iterations, both walks of every cell, for the algorithmic operation count. */
