@@ -63,13 +63,16 @@ typedef struct vtg_server vtg_server;
 int vtg_server_create(vtg_ctx *ctx, const struct vtg_server_cfg *cfg, vtg_server **out);
 /* Waits (at most 10 s) for the steps on the GPU, then frees everything, streams included. */
 void vtg_server_destroy(vtg_server *s);
-/* The template of the appearance searches (vtg_search_template's arguments, host memory; at most 32 x 21). */
+/* The template of the appearance searches (vtg_search_template's arguments, host memory; at most 32 x 21). The searches'
+ * device scratch is allocated here for the streams already open, and by vtg_server_open for each later one, never in
+ * a step; it is charged to the context's budget. */
 int vtg_server_template(vtg_server *s, const float *app, int tw, int th, float norm);
 /* Admits a stream of width x height frames whose cells live on flow_level, with priority VTG_PRIO_*; `first` (host
  * memory, `stride` bytes a row; it must stay valid until the stream's first result is polled) is its first frame,
  * whose pyramid is queued at once and which the stream's first step waits for on the GPU. Returns the stream's id
  * (>= 0), VTG_EINVAL for a size or level the tracker does not take (the server goes on), VTG_EBUDGET when its memory
- * does not fit the budget now (retry when streams close). */
+ * (with a template set, the searches' scratch for its size too) does not fit the budget now (retry when streams
+ * close). */
 int vtg_server_open(vtg_server *s, uint32_t width, uint32_t height, uint32_t flow_level, int priority,
                     const uint8_t *first, int stride);
 /* Closes a stream: at once if nothing of it is queued or on the GPU, else as soon as that is done (queued frames are

@@ -231,6 +231,8 @@ void vtg_server_destroy(vtg_server *s)
     free(s);
 }
 
+static int ensure_search(vtg_server *s, int w, int h);
+
 int vtg_server_template(vtg_server *s, const float *app, int tw, int th, float norm)
 {
     if (!s || !app || tw < 8 || th < 1 || (tw % 8) || tw * th > SRV_APP_MAX || !(norm >= 0.0f))
@@ -245,6 +247,12 @@ int vtg_server_template(vtg_server *s, const float *app, int tw, int th, float n
             if (s->sl[k].busy && wait_event(s->sl[k].ev) != VTG_OK)
                 return VTG_ETIMEOUT;
             const int rc = vtg_search_template(s->sl[k].srch, s->app, tw, th, norm, VTG_HOST, NULL);
+            if (rc != VTG_OK)
+                return rc;
+        }
+    for (int i = 0; i < s->nst; i++)
+        if (s->st[i].used) {
+            const int rc = ensure_search(s, (int)s->st[i].w, (int)s->st[i].h);
             if (rc != VTG_OK)
                 return rc;
         }
@@ -304,6 +312,8 @@ int vtg_server_open(vtg_server *s, uint32_t width, uint32_t height, uint32_t flo
         rc = vtg_build(ss->t, 0, first, stride, VTG_HOST, NULL);
     if (rc == VTG_OK && cudaEventRecord(ss->first_built, (cudaStream_t)vtg_tracker_stream(ss->t)) != cudaSuccess)
         rc = VTG_ECUDA;
+    if (rc == VTG_OK)
+        rc = ensure_search(s, (int)width, (int)height); /* searches of this stream allocate nothing in a step */
     if (rc != VTG_OK) {
         free_stream(ss);
         return rc;
@@ -461,6 +471,27 @@ static int slot_search(vtg_server *s, struct srv_slot *sl, int w, int h)
     sl->srch_w = nw;
     sl->srch_h = nh;
     return vtg_search_template(sl->srch, s->app, s->tw, s->th, s->norm, VTG_HOST, NULL);
+}
+
+/* Every slot's search context sized for a w x h stream's search plane (its level 1, or level 0 with one level), so
+ * that no step allocates: called when a stream is admitted and when the template is set, never inside a step. A busy
+ * slot is waited for first, as its context may be replaced. */
+static int ensure_search(vtg_server *s, int w, int h)
+{
+    if (!s->has_template)
+        return VTG_OK;
+    const int lw = s->cfg.lk.levels > 1 ? (w + 1) / 2 : w, lh = s->cfg.lk.levels > 1 ? (h + 1) / 2 : h;
+    for (int k = 0; k < SRV_SLOTS; k++) {
+        struct srv_slot *sl = &s->sl[k];
+        if (sl->srch && sl->srch_w >= lw && sl->srch_h >= lh)
+            continue;
+        if (sl->busy && wait_event(sl->ev) != VTG_OK)
+            return VTG_ETIMEOUT;
+        const int rc = slot_search(s, sl, lw, lh);
+        if (rc != VTG_OK)
+            return rc;
+    }
+    return VTG_OK;
 }
 
 /* The server whose streams cmp_head orders (qsort takes no context; calls on one server come from one thread). */
