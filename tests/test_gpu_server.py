@@ -222,3 +222,32 @@ def test_server_search_request_matches_a_direct_search(vtg_lib, ctx):
     assert (got["hx"], got["hy"], got["ntop"], got["cells"]) == (want["hx"], want["hy"], want["ntop"], want["cells"])
     assert got["ncc"] == want["ncc"] and got["second"] == want["second"]
     assert (got["hx"], got["hy"]) == (300, 180)  # the template's own corner, in half pixels
+
+
+def test_server_search_scratch_at_admission(vtg_lib, ctx):
+    """With a template set, both slots' search scratch is charged to the budget when a stream is admitted, sized for the
+    stream's level 1; a step that searches then allocates nothing (the loop never allocates inside a step)."""
+    import ctypes
+
+    seq = _seq(640, 480, 1, seed=141)
+    app = np.zeros((21, 32), np.float32)
+    app[::2] = 1.0
+    app -= np.float32(app.mean(dtype=np.float64))
+    norm = float((app.astype(np.float64) ** 2).sum())
+    L = vtg_lib.lib()
+    L.vtg_search_bytes.argtypes = [ctypes.c_int] * 4
+    L.vtg_search_bytes.restype = ctypes.c_size_t
+    srv = vtg_lib.Server(ctx, vtg_lib.config(64, 64, levels=4))
+    srv.template(app, norm)
+    used0 = ctx.used()
+    sid = srv.open(640, 480, seq[0].data_ptr())
+    assert sid >= 0
+    tracker = L.vtg_tracker_bytes(ctypes.byref(vtg_lib.config(640, 480, levels=4)))
+    scratch = L.vtg_search_bytes(320, 240, 32, 21)
+    assert ctx.used() - used0 == tracker + 2 * scratch
+    used1 = ctx.used()
+    assert srv.submit(sid, seq[1].data_ptr(), flags=vtg_lib.REQ_SEARCH) >= 0
+    res = _drain(srv, 1)
+    assert len(res) == 1 and res[0]["status"] == vtg_lib.RES_DONE and res[0]["searched"] == 1
+    assert ctx.used() == used1
+    srv.close()
