@@ -27,7 +27,11 @@ def _tracker(vtg_lib, ctx, w, h, **kw):
 
 
 @pytest.mark.parametrize("w,h,levels", [(32, 32, 1), (33, 47, 3), (97, 61, 4), (640, 480, 3), (1281, 719, 5),
-                                        (1920, 1080, 4)])
+                                        (1920, 1080, 4),
+                                        # levels 0-3 are made in 128 x 64 blocks of level 0: block (1, 1) just inside
+                                        # the frame (its staged bytes end on the last column and row), just not, and a
+                                        # one-pixel sliver of a block
+                                        (272, 135, 4), (271, 134, 4), (129, 65, 4)])
 def test_pyramid_bit_exact(vtg_lib, ctx, w, h, levels):
     frame = S.noise_frame(w, h, seed=w + 3 * h)
     t = _tracker(vtg_lib, ctx, w, h, levels=levels)
