@@ -445,11 +445,19 @@ __device__ __forceinline__ void lk_correlate(const DevLevel &L, int jx, int jy, 
     warp_fold8<8>(X);
 }
 
-/* sum (T - J) T_grad at phase (fx, fy) from the correlation's four shifts and C, times the Sobel scale */
+/* sum (T - J) T_grad at phase (fx, fy) from the correlation's four shifts and C, times the Sobel scale. X holds the
+ * shifts (0, 0) and (0, 1) and the x differences (1, 0) - (0, 0), (1, 1) - (0, 1), formed once a window pass
+ * (lk_phase_diffs): the same values each iteration would form. */
 __device__ __forceinline__ float lk_at_phase(const float *X, float C, float fx, float fy)
 {
-    const float r0 = __fmaf_rn(X[1] - X[0], fx, X[0]), r1 = __fmaf_rn(X[3] - X[2], fx, X[2]);
+    const float r0 = __fmaf_rn(X[1], fx, X[0]), r1 = __fmaf_rn(X[3], fx, X[2]);
     return (C - __fmaf_rn(r1 - r0, fy, r0)) * LK_GRAD_SCALE;
+}
+__device__ __forceinline__ void lk_phase_diffs(float (&X)[8])
+{
+#pragma unroll
+    for (int k = 0; k < 8; k += 2)
+        X[k + 1] -= X[k];
 }
 
 /* iterate (RESID = false): J at pixel (jx + fx, jy + fy); the sums of It Tx and It Ty.
@@ -669,6 +677,7 @@ __device__ __forceinline__ void lk_track(const DevPyr &I, const DevPyr &J, int t
                 lk_correlate<MAXH, EXACT, TS>(JL, jx, jy + dy, W, H, lane, P, tc, X);
                 if constexpr (NW == 2)
                     pair_add(X, q, lane);
+                lk_phase_diffs(X);
                 work += LK_WORK_PASS;
                 cjx = jx;
                 cjy = jy;
