@@ -445,13 +445,14 @@ __device__ __forceinline__ void lk_correlate(const DevLevel &L, int jx, int jy, 
     warp_fold8<8>(X);
 }
 
-/* sum (T - J) T_grad at phase (fx, fy) from the correlation's four shifts and C, times the Sobel scale. X holds the
- * shifts (0, 0) and (0, 1) and the x differences (1, 0) - (0, 0), (1, 1) - (0, 1), formed once a window pass
- * (lk_phase_diffs): the same values each iteration would form. */
+/* sum (T - J) T_grad at phase (fx, fy) from the correlation's four shifts and C, before the Sobel scale (which the
+ * walk folds into G^-1: a power of two, so the products round the same). X holds the shifts (0, 0) and (0, 1) and the
+ * x differences (1, 0) - (0, 0), (1, 1) - (0, 1), formed once a window pass (lk_phase_diffs): the same values each
+ * iteration would form. */
 __device__ __forceinline__ float lk_at_phase(const float *X, float C, float fx, float fy)
 {
     const float r0 = __fmaf_rn(X[1], fx, X[0]), r1 = __fmaf_rn(X[3], fx, X[2]);
-    return (C - __fmaf_rn(r1 - r0, fy, r0)) * LK_GRAD_SCALE;
+    return C - __fmaf_rn(r1 - r0, fy, r0);
 }
 __device__ __forceinline__ void lk_phase_diffs(float (&X)[8])
 {
@@ -652,8 +653,11 @@ __device__ __forceinline__ void lk_track(const DevPyr &I, const DevPyr &J, int t
             gyy0 = gyy;
             valid0 = true;
         }
-        /* G^-1 / 64: b arrives in Q6 grey x 8-bit grey per pixel */
-        const float ia = gyy * idet * LK_Q6_INV, ib = -gxy * idet * LK_Q6_INV, ic = gxx * idet * LK_Q6_INV;
+        /* G^-1 / 64: b arrives in Q6 grey x 8-bit grey per pixel; times the Sobel scale of b's sums, exact (a power of
+         * two far from the exponent's limits at these magnitudes), so each product below rounds as it would with b
+         * scaled first */
+        const float ia = gyy * idet * LK_Q6_INV * LK_GRAD_SCALE, ib = -gxy * idet * LK_Q6_INV * LK_GRAD_SCALE,
+                    ic = gxx * idet * LK_Q6_INV * LK_GRAD_SCALE;
         const float lo_x = (float)(mx - bx), lo_y = (float)(my - by);
         const float hi_x = (float)(JL.w - mx - 1 - bx), hi_y = (float)(JL.h - my - 1 - by);
         float vx = 0.0f, vy = 0.0f;
